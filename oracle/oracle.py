@@ -1,0 +1,278 @@
+"""ctypes bindings for the CPU oracle (oracle/sde_oracle.c).
+
+TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs
+import this module.  The product package (sde_gb300) never imports it.
+
+Every wrapper takes/returns numpy arrays in the reference's layouts: images [ny][nx]
+float32 (Fortran IMAGE(NX,NY) column-major == C row-major [NY][NX]), grids [nv][nu]
+complex64, visibilities complex64, coordinates float32 wavelengths.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+c64p = np.ctypeslib.ndpointer(np.complex64, flags="C_CONTIGUOUS")
+c128p = np.ctypeslib.ndpointer(np.complex128, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+RMODES = {"NONE": 0, "NORM": 1, "ABS": 2, "AZ-NORM": 3}
+
+
+class UvmapParams(C.Structure):
+    _fields_ = [("imsize", C.c_int), ("cellsize", C.c_float), ("fov", C.c_float),
+                ("rmode", C.c_int), ("robust", C.c_float * 3), ("ds", C.c_float),
+                ("vra", C.c_double), ("vdec", C.c_double),
+                ("shift_ra", C.c_float), ("shift_dec", C.c_float)]
+
+
+class Geom(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("fnu", C.c_int), ("nu", C.c_int),
+                ("nv", C.c_int), ("uscale", C.c_float), ("vscale", C.c_float),
+                ("uorigin", C.c_int), ("vorigin", C.c_int), ("cenx", C.c_float),
+                ("ceny", C.c_float), ("shift", C.c_double * 9)]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(
+                os.path.join(_HERE, "sde_oracle.c")):
+            build()
+        L = C.CDLL(_LIB)
+        L.orc_grdsf.restype = C.c_double
+        L.orc_grdsf.argtypes = [C.c_double]
+        L.orc_fftpwr2.restype = C.c_int
+        L.orc_grdcf.argtypes = [C.c_int, f32p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.orc_grdccf.argtypes = [C.c_int, f32p, C.c_int]
+        L.orc_crdshift.argtypes = [C.c_double] * 4 + [C.c_float, f64p]
+        common = [f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                  C.c_int, C.c_int]
+        L.orc_grduwt2d.argtypes = common + [f32p, f32p, C.c_int, C.c_int, f64p,
+                                            C.POINTER(C.c_int)]
+        L.orc_grdruw2d.argtypes = common + [f32p, f32p, C.c_int, C.c_int, f64p, C.c_char_p,
+                                            f32p, C.c_float, C.POINTER(C.c_int),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_float)]
+        L.orc_grdh2d.argtypes = [c64p, f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float,
+                                 C.c_float, C.c_float, C.c_int, C.c_int, c64p, C.c_int, C.c_int,
+                                 C.c_int, f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, f64p,
+                                 C.POINTER(C.c_float), C.POINTER(C.c_double)]
+        L.orc_grddeh2d.argtypes = [c64p, f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float,
+                                   C.c_float, C.c_float, C.c_int, C.c_int, c64p, C.c_int,
+                                   C.c_int, f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int,
+                                   f64p, C.POINTER(C.c_int)]
+        L.orc_fftr2d.argtypes = [f32p, c64p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_fftx.argtypes = [c64p, c64p, C.c_int, C.c_int]
+        L.orc_pixcor2d.argtypes = [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, f32p,
+                                   C.c_float, C.c_float]
+        L.orc_pixisama.restype = C.c_int
+        L.orc_pixisama.argtypes = [C.c_int, f32p, C.c_int]
+        L.orc_pix2drcl.argtypes = [f32p, f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_float, C.c_int, C.c_int, C.c_float, f32p, f32p,
+                                   C.POINTER(C.c_int), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_float), f32p, i32p, i32p]
+        L.orc_make_geom.argtypes = [C.POINTER(UvmapParams), C.POINTER(Geom)]
+        L.orc_uvmap.argtypes = [C.POINTER(UvmapParams), C.c_int, f32p, f32p, f32p, c64p, f32p,
+                                f32p, f32p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_vismodel.argtypes = [C.POINTER(UvmapParams), C.c_int, f32p, f32p, f32p, c64p,
+                                   f32p, f32p]
+        L.orc64_uvmap_image.argtypes = [C.POINTER(Geom), C.c_int, f32p, f32p, f32p, c64p, f32p,
+                                        C.c_int, f64p]
+        L.orc64_fftr2d_inv.argtypes = [c128p, f64p, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc64_dft_image.argtypes = [C.POINTER(Geom), C.c_int, f32p, f32p, c64p, f32p,
+                                      C.c_int, f64p]
+        _lib = L
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _c64(a):
+    return np.ascontiguousarray(a, dtype=np.complex64)
+
+
+def params(imsize, cellsize, fov=1.0, rmode="NONE", robust=(0.0, 0.0, 0.0), ds=0.0,
+           vra=0.0, vdec=40.0, shift=(0.0, 0.0)):
+    p = UvmapParams()
+    p.imsize, p.cellsize, p.fov, p.rmode = imsize, cellsize, fov, RMODES[rmode]
+    p.robust = (C.c_float * 3)(*robust)
+    p.ds, p.vra, p.vdec = ds, vra, vdec
+    p.shift_ra, p.shift_dec = shift
+    return p
+
+
+def geom(p):
+    g = Geom()
+    lib().orc_make_geom(C.byref(p), C.byref(g))
+    return g
+
+
+def grdcf():
+    cf = np.zeros(1 + 8 * 129, np.float32)
+    s, o = C.c_int(), C.c_int()
+    lib().orc_grdcf(1, cf, C.byref(s), C.byref(o))
+    return cf, s.value, o.value
+
+
+def grdccf(ccflen):
+    ccf = np.zeros(ccflen, np.float32)
+    lib().orc_grdccf(1, ccf, ccflen)
+    return ccf
+
+
+def crdshift(vra, vdec, ira, idec, rota=0.0):
+    s = np.zeros(9, np.float64)
+    lib().orc_crdshift(vra, vdec, ira, idec, rota, s)
+    return s
+
+
+def grduwt2d(wt, u, v, w, uscale, vscale, uorigin, vorigin, nu, nv, shift,
+             uoffset=0.0, voffset=0.0):
+    wt = _f32(wt)
+    newwt = np.empty_like(wt)
+    gwt = np.zeros((nv, nu), np.float32)
+    nd = C.c_int()
+    lib().orc_grduwt2d(wt, _f32(u), _f32(v), _f32(w), len(wt), uscale, uoffset, vscale,
+                       voffset, uorigin, vorigin, newwt, gwt, nu, nv,
+                       np.ascontiguousarray(shift, np.float64), C.byref(nd))
+    return newwt, gwt, nd.value
+
+
+def grdruw2d(wt, u, v, w, uscale, vscale, uorigin, vorigin, nu, nv, shift, rmode,
+             robust, ds=0.0, uoffset=0.0, voffset=0.0):
+    wt = _f32(wt)
+    newwt = np.empty_like(wt)
+    gwt = np.zeros((nv, nu), np.float32)
+    nd, sw, slw, f2 = C.c_int(), C.c_double(), C.c_double(), C.c_float()
+    rc = lib().orc_grdruw2d(wt, _f32(u), _f32(v), _f32(w), len(wt), uscale, uoffset, vscale,
+                            voffset, uorigin, vorigin, newwt, gwt, nu, nv,
+                            np.ascontiguousarray(shift, np.float64), rmode.encode(),
+                            _f32(list(robust) + [0.0] * (3 - len(robust))), ds, C.byref(nd),
+                            C.byref(sw), C.byref(slw), C.byref(f2))
+    return rc, newwt, gwt, nd.value, sw.value, slw.value, f2.value
+
+
+def grdh2d(vis, wt, u, v, w, uscale, vscale, uorigin, vorigin, nu, nv, shift, psf=False,
+           cf=None, supp=3, osamp=128, uoffset=0.0, voffset=0.0):
+    if cf is None:
+        cf, supp, osamp = grdcf()
+    gvis = np.zeros((nv, nu), np.complex64)
+    sw, lsw = C.c_float(), C.c_double()
+    rc = lib().orc_grdh2d(_c64(vis), _f32(wt), _f32(u), _f32(v), _f32(w), len(wt), uscale,
+                          uoffset, vscale, voffset, uorigin, vorigin, gvis, int(psf), nu, nv,
+                          cf, supp, osamp, cf, supp, osamp,
+                          np.ascontiguousarray(shift, np.float64), C.byref(sw), C.byref(lsw))
+    return rc, gvis, sw.value, lsw.value
+
+
+def grddeh2d(vis, wt, u, v, w, uscale, vscale, uorigin, vorigin, gvis, shift, cf=None,
+             supp=3, osamp=128, uoffset=0.0, voffset=0.0):
+    """Returns (vis_out, wt_out, nbad); inputs are not modified."""
+    if cf is None:
+        cf, supp, osamp = grdcf()
+    vis = _c64(vis).copy()
+    wt = _f32(wt).copy()
+    nv, nu = gvis.shape
+    nb = C.c_int()
+    lib().orc_grddeh2d(vis, wt, _f32(u), _f32(v), _f32(w), len(wt), uscale, uoffset, vscale,
+                       voffset, uorigin, vorigin, _c64(gvis), nu, nv, cf, supp, osamp, cf,
+                       supp, osamp, np.ascontiguousarray(shift, np.float64), C.byref(nb))
+    return vis, wt, nb.value
+
+
+def fftr2d(nx, ny, fnu, nv, direction, rarray=None, xarray=None):
+    """DIR=-1: xarray [nv][fnu/2+1] -> image [ny][nx]; DIR=+1: image -> grid."""
+    nu = fnu // 2 + 1
+    r = np.zeros((ny, nx), np.float32) if rarray is None else _f32(rarray).copy()
+    x = np.zeros((nv, nu), np.complex64) if xarray is None else _c64(xarray).copy()
+    lib().orc_fftr2d(r, x, nx, ny, fnu, nv, direction)
+    return r, x
+
+
+def fftx(x, isig):
+    x = _c64(x).copy()
+    wk = np.zeros_like(x)
+    lib().orc_fftx(x, wk, len(x), isig)
+    return x
+
+
+def pixcor2d(img, ccf, cenx, ceny, correct=True):
+    img = _f32(img)
+    out = np.empty_like(img)
+    ny, nx = img.shape
+    lib().orc_pixcor2d(img, nx, ny, _f32(ccf), len(ccf), int(correct), out, cenx, ceny)
+    return out
+
+
+def pixisama(a):
+    a = _f32(a).ravel()
+    return lib().orc_pixisama(len(a), a, 1)
+
+
+def pix2drcl(drt, psf, box, gain, nsub, bsub=1, flux=0.0, tflux=0.0):
+    drt, psf, box = _f32(drt), _f32(psf), _f32(box)
+    ny, nx = drt.shape
+    pny, pnx = psf.shape
+    cln = np.zeros_like(drt)
+    res = np.zeros_like(drt)
+    n = abs(nsub)
+    cflux = np.zeros(max(n, 1), np.float32)
+    cx = np.zeros(max(n, 1), np.int32)
+    cy = np.zeros(max(n, 1), np.int32)
+    ansub, maxres, tf = C.c_int(), C.c_float(), C.c_float(tflux)
+    lib().orc_pix2drcl(drt, psf, box, nx, ny, pnx, pny, gain, nsub, bsub, flux, cln, res,
+                       C.byref(ansub), C.byref(maxres), C.byref(tf), cflux, cx, cy)
+    return dict(cln=cln, res=res, ansub=ansub.value, maxres=maxres.value, tflux=tf.value,
+                cflux=cflux, cx=cx, cy=cy)
+
+
+def uvmap(p, u, v, w, vis, wt):
+    """Returns (dirty, psf, wt_after_weighting, maxpsf, sumwt, rc)."""
+    wt = _f32(wt).copy()
+    dirty = np.zeros((p.imsize, p.imsize), np.float32)
+    psf = np.zeros_like(dirty)
+    mx, sw = C.c_float(), C.c_float()
+    rc = lib().orc_uvmap(C.byref(p), len(wt), _f32(u), _f32(v), _f32(w), _c64(vis), wt, dirty,
+                         psf, C.byref(mx), C.byref(sw))
+    return dirty, psf, wt, mx.value, sw.value, rc
+
+
+def vismodel(p, u, v, w, vis, wt, image):
+    vis = _c64(vis).copy()
+    wt = _f32(wt).copy()
+    lib().orc_vismodel(C.byref(p), len(wt), _f32(u), _f32(v), _f32(w), vis, wt, _f32(image))
+    return vis, wt
+
+
+def uvmap_image64(g, u, v, w, vis, wt, psf):
+    img = np.zeros((g.ny, g.nx), np.float64)
+    lib().orc64_uvmap_image(C.byref(g), len(wt), _f32(u), _f32(v), _f32(w), _c64(vis),
+                            _f32(wt), int(psf), img)
+    return img
+
+
+def fftr2d_inv64(xarray, nx, ny, fnu, nv):
+    img = np.zeros((ny, nx), np.float64)
+    lib().orc64_fftr2d_inv(np.ascontiguousarray(xarray, np.complex128), img, nx, ny, fnu, nv)
+    return img
+
+
+def dft_image64(g, u, v, vis, wt, psf):
+    img = np.zeros((g.ny, g.nx), np.float64)
+    lib().orc64_dft_image(C.byref(g), len(wt), _f32(u), _f32(v), _c64(vis), _f32(wt),
+                          int(psf), img)
+    return img

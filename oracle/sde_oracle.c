@@ -1,0 +1,1227 @@
+/*
+ * sde_oracle.c -- CPU restatement of SDE's imaging hot path.  TEST INFRASTRUCTURE ONLY:
+ * the product library never links, loads or calls this code.  See sde_oracle.h for the
+ * conventions.  Every routine cites the Fortran file and lines (timcornwell/sde,
+ * source/ tree) whose arithmetic it follows, statement by statement.
+ *
+ * Build: gcc -O2 -ffp-contract=off -fno-fast-math -fPIC -shared (oracle/Makefile).
+ */
+#include "sde_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define F2(a, i, j, ld) ((a)[((i)-1) + (size_t)((j)-1) * (size_t)(ld)]) /* 1-based col-major */
+
+int orc_nint_f(float x) { return (int)lroundf(x); }  /* Fortran NINT: half away from zero */
+int orc_nint_d(double x) { return (int)lround(x); }
+
+/* fft/fftpwr2.f:28-39 */
+int orc_fftpwr2(int i) {
+    if (i < 1) return 1;
+    int lg = orc_nint_f(logf((float)i) / logf(2.0f));
+    int p = 1;
+    for (int k = 0; k < lg; k++) p *= 2;
+    while (p < i) p *= 2;
+    return p;
+}
+
+/* grd/grdsf.f:338-372: prolate spheroidal m=6, alpha=1 rational approximation */
+double orc_grdsf(double nu) {
+    static const double P[2][5] = {
+        {8.203343e-2, -3.644705e-1, 6.278660e-1, -5.335581e-1, 2.312756e-1},
+        {4.028559e-3, -3.697768e-2, 1.021332e-1, -1.201436e-1, 6.412774e-2}};
+    static const double Q[2][3] = {{1.0000000e0, 8.212018e-1, 2.078043e-1},
+                                   {1.0000000e0, 9.599102e-1, 2.918724e-1}};
+    int part;
+    double nuend;
+    if (nu >= 0.0 && nu < 0.75) {
+        part = 0;
+        nuend = 0.75;
+    } else if (nu >= 0.75 && nu <= 1.00) {
+        part = 1;
+        nuend = 1.00;
+    } else {
+        return 0.0;
+    }
+    double top = P[part][0];
+    double delnusq = nu * nu - nuend * nuend;
+    for (int k = 1; k <= 4; k++) top = top + P[part][k] * pow(delnusq, (double)k);
+    double bot = Q[part][0];
+    for (int k = 1; k <= 2; k++) bot = bot + Q[part][k] * pow(delnusq, (double)k);
+    return (bot != 0.0) ? top / bot : 0.0;
+}
+
+/* grd/grdcf.f:245-294.  code_sf: 1 = 'SF', 0 = 'BOX'.  cf must hold 1+8*129 floats
+ * (vis/visgrid.f CFLEN); CF(CFOFFSET+I) == cf[CFOFFSET-1+I]. */
+void orc_grdcf(int code_sf, float *cf, int *cfsupp, int *cfosamp) {
+    int osamp = 128, supp, off;
+    if (!code_sf) {
+        supp = 1;
+        off = (supp + 1) * osamp + 1;
+        for (int i = 0; i <= osamp / 2; i++) {
+            cf[off - 1 + i] = 1.0f;
+            cf[off - 1 - i] = 1.0f;
+        }
+        for (int i = osamp / 2 + 1; i <= 2 * osamp; i++) {
+            cf[off - 1 + i] = 0.0f;
+            cf[off - 1 - i] = 0.0f;
+        }
+    } else {
+        supp = 3;
+        off = (supp + 1) * osamp + 1;
+        for (int i = 0; i <= supp * osamp; i++) {
+            double nu = (double)i / (double)(supp * osamp);
+            cf[off - 1 + i] = (float)((1 - pow(nu, 2.0)) * orc_grdsf(nu));
+            cf[off - 1 - i] = cf[off - 1 + i];
+        }
+        for (int i = supp * osamp + 1; i <= (supp + 1) * osamp; i++) {
+            cf[off - 1 + i] = 0.0f;
+            cf[off - 1 - i] = 0.0f;
+        }
+    }
+    float sum = 0.0f;
+    for (int i = -(supp + 1) * osamp; i <= (supp + 1) * osamp; i++) sum = sum + cf[off - 1 + i];
+    for (int i = -(supp + 1) * osamp; i <= (supp + 1) * osamp; i++)
+        cf[off - 1 + i] = cf[off - 1 + i] / sum;
+    *cfsupp = supp;
+    *cfosamp = osamp;
+}
+
+/* grd/grdccf.f:423-427 ('SF' branch); 'BOX' (grdccf.f:417-422) uses SINC(0.5*PI*NU). */
+void orc_grdccf(int code_sf, float *ccf, int ccflen) {
+    if (code_sf) {
+        for (int i = 1; i <= ccflen; i++) {
+            double nu = (double)(i - 1) / (double)(ccflen - 1);
+            ccf[i - 1] = (float)orc_grdsf(nu);
+        }
+    } else {
+        const float PI = 3.141592554f;
+        ccf[0] = 1.0f;
+        for (int i = 2; i <= ccflen; i++) {
+            double nu = (double)(i - 1) / (double)(ccflen - 1);
+            float x = 0.5f * PI * (float)nu;
+            ccf[i - 1] = sinf(x) / x;
+        }
+    }
+}
+
+/* crd/crdshift.f:95-160.  shift is SHIFT(3,3) column-major: SHIFT(I,J) = shift[(I-1)+3(J-1)] */
+void orc_crdshift(double vra_deg, double vdec_deg, double ira_deg, double idec_deg,
+                  float vrota3_deg, double *shift) {
+    double dtor = 4.0 * atan(1.0) / 180.0;
+    double rao = dtor * vra_deg, deco = dtor * vdec_deg;
+    double ra = dtor * ira_deg, dec = dtor * idec_deg;
+    double T[3][3]; /* T[i][j] == TMAT(i+1, j+1) */
+    T[0][0] = cos(ra - rao);
+    T[1][0] = sin(ra - rao) * sin(deco);
+    T[2][0] = -sin(ra - rao) * cos(deco);
+    T[0][1] = -sin(ra - rao) * sin(dec);
+    T[1][1] = cos(ra - rao) * sin(dec) * sin(deco) + cos(dec) * cos(deco);
+    T[2][1] = -cos(ra - rao) * cos(deco) * sin(dec) + cos(dec) * sin(deco);
+    T[0][2] = sin(ra - rao) * cos(dec);
+    T[1][2] = -cos(ra - rao) * sin(deco) * cos(dec) + sin(dec) * cos(deco);
+    T[2][2] = cos(ra - rao) * cos(dec) * cos(deco) + sin(dec) * sin(deco);
+    float rota = (float)(dtor * vrota3_deg); /* REAL ROTA */
+    if (rota != 0.0f) {
+        double R[3][3], S[3][3];
+        R[0][0] = cos(rota); R[0][1] = sin(rota); R[0][2] = 0.0;
+        R[1][0] = -sin(rota); R[1][1] = cos(rota); R[1][2] = 0.0;
+        R[2][0] = 0.0; R[2][1] = 0.0; R[2][2] = 1.0;
+        for (int j = 0; j < 3; j++)
+            for (int i = 0; i < 3; i++) {
+                S[i][j] = 0.0;
+                for (int k = 0; k < 3; k++) S[i][j] = S[i][j] + T[k][j] * R[i][k];
+            }
+        for (int j = 0; j < 3; j++)
+            for (int i = 0; i < 3; i++) {
+                double s = 0.0;
+                for (int k = 0; k < 3; k++) s = s + R[j][k] * S[i][k];
+                shift[i + 3 * j] = s;
+            }
+    } else {
+        for (int j = 0; j < 3; j++)
+            for (int i = 0; i < 3; i++) shift[i + 3 * j] = T[i][j];
+    }
+}
+
+#define SH(i, j) shift[((i)-1) + 3 * ((j)-1)]
+
+static int doshift_of(const double *shift) {
+    return (SH(1, 1) != 1.0) || (SH(2, 2) != 1.0) || (SH(3, 3) != 1.0);
+}
+
+/* FP32 uv -> cell for the weighting routines: grd/grduwt2d.f:92-111 (and grdruw2d.f:304-323).
+ * Returns 0 and the 1-based cell if on the grid, else -1. */
+static int wcell(const float *u, const float *v, const float *w, int i, float uscale,
+                 float uoffset, float vscale, float voffset, int uorigin, int vorigin,
+                 const double *shift, int doshift, int nu, int nv, int *ucen, int *vcen,
+                 float *ulocal_out, float *vlocal_out) {
+    float ucell, vcell, ulocal, vlocal;
+    if (doshift) {
+        ulocal = (float)(SH(1, 1) * (double)u[i] + SH(2, 1) * (double)v[i] + SH(3, 1) * (double)w[i]);
+        vlocal = (float)(SH(1, 2) * (double)u[i] + SH(2, 2) * (double)v[i] + SH(3, 2) * (double)w[i]);
+        ucell = uscale * ulocal + uoffset;
+        vcell = vscale * vlocal + voffset;
+    } else {
+        ulocal = u[i];
+        vlocal = v[i];
+        ucell = uscale * u[i] + uoffset;
+        vcell = vscale * v[i] + voffset;
+    }
+    if (ucell > 0.0f) {
+        ucell = ucell + (float)uorigin;
+        vcell = vcell + (float)vorigin;
+    } else {
+        ucell = -ucell + (float)uorigin;
+        vcell = -vcell + (float)vorigin;
+    }
+    *ucen = orc_nint_f(ucell);
+    *vcen = orc_nint_f(vcell);
+    if (ulocal_out) *ulocal_out = ulocal;
+    if (vlocal_out) *vlocal_out = vlocal;
+    if (*ucen < 1 || *ucen > nu || *vcen < 1 || *vcen > nv) return -1;
+    return 0;
+}
+
+/* grd/grduwt2d.f:75-167 (uniform weighting, pass 1 density count then pass 2 NEWWT).
+ * newwt may alias wt, as in GRDUWT (grd/grduwt.f:122). */
+void orc_grduwt2d(const float *wt, const float *u, const float *v, const float *w, int nvis,
+                  float uscale, float uoffset, float vscale, float voffset, int uorigin,
+                  int vorigin, float *newwt, float *gwt, int nu, int nv, const double *shift,
+                  int *ndrop) {
+    for (size_t k = 0; k < (size_t)nu * nv; k++) gwt[k] = 0.0f;
+    int doshift = doshift_of(shift);
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        int uc, vc;
+        if (wcell(u, v, w, i, uscale, uoffset, vscale, voffset, uorigin, vorigin, shift, doshift,
+                  nu, nv, &uc, &vc, NULL, NULL))
+            continue;
+        F2(gwt, uc, vc, nu) = F2(gwt, uc, vc, nu) + wt[i];
+    }
+    int nd = 0;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        int uc, vc;
+        if (wcell(u, v, w, i, uscale, uoffset, vscale, voffset, uorigin, vorigin, shift, doshift,
+                  nu, nv, &uc, &vc, NULL, NULL)) {
+            newwt[i] = -1.0f;
+            nd++;
+            continue;
+        }
+        float g = F2(gwt, uc, vc, nu);
+        if (g > 0.0f) {
+            if (uc == uorigin) {
+                if (vc == vorigin)
+                    newwt[i] = wt[i] / g;
+                else
+                    newwt[i] = 0.5f * wt[i] / g;
+            } else {
+                newwt[i] = wt[i] / g;
+            }
+        } else {
+            newwt[i] = -1.0f;
+        }
+    }
+    if (ndrop) *ndrop = nd;
+}
+
+/* grd/grdruw2d.f:257-419 (robust weighting).  rmode: "NORM", "ABS", "NONE", "AZ-NORM". */
+int orc_grdruw2d(const float *wt, const float *u, const float *v, const float *w, int nvis,
+                 float uscale, float uoffset, float vscale, float voffset, int uorigin,
+                 int vorigin, float *newwt, float *gwt, int nu, int nv, const double *shift,
+                 const char *rmode, const float *robust, float ds, int *ndrop,
+                 double *sumwt_out, double *sumlocwt_out, float *f2_out) {
+    for (size_t k = 0; k < (size_t)nu * nv; k++) gwt[k] = 0.0f;
+    int doshift = doshift_of(shift);
+    int doaz = (strncmp(rmode, "AZ", 2) == 0);
+    float rob, rpa = 0.0f, rbscale = 0.0f, pi = 0.0f;
+    if (doaz) {
+        rob = (robust[0] + robust[1]) / 2.0f;
+        rpa = -robust[2] + 90.0f - 90.0f;
+        while (rpa < -90.0f) rpa = rpa + 180.0f;
+        while (rpa > 90.0f) rpa = rpa - 180.0f;
+        pi = 4.0f * atanf(1.0f);
+        rpa = rpa * pi / 180.0f;
+        rbscale = (robust[0] - robust[1]) / (pi / 2.0f);
+    } else {
+        rob = robust[0];
+    }
+    double sumwt = 0.0;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        int uc, vc;
+        if (wcell(u, v, w, i, uscale, uoffset, vscale, voffset, uorigin, vorigin, shift, doshift,
+                  nu, nv, &uc, &vc, NULL, NULL))
+            continue;
+        F2(gwt, uc, vc, nu) = F2(gwt, uc, vc, nu) + wt[i];
+        sumwt = sumwt + (double)wt[i];
+    }
+    float f2, d2;
+    double sumlocwt = 0.0;
+    if (!strcmp(rmode, "NORM") || !strcmp(rmode, "AZ-NORM")) {
+        for (int vg = 1; vg <= nv; vg++)
+            for (int ug = 1; ug <= nu; ug++) {
+                float g = F2(gwt, ug, vg, nu);
+                if (g > 0.0f) sumlocwt = sumlocwt + (double)(g * g);
+            }
+        float t = 5.0f * powf(10.0f, -rob);
+        f2 = (float)((double)(t * t) / (sumlocwt / sumwt));
+        d2 = 1.0f;
+    } else if (!strcmp(rmode, "ABS")) {
+        f2 = rob * rob;
+        d2 = 2.0f * (ds * ds);
+    } else if (!strcmp(rmode, "NONE")) {
+        f2 = 1.0f;
+        d2 = 0.0f;
+    } else {
+        return ORC_EBADMODE;
+    }
+    if (sumwt_out) *sumwt_out = sumwt;
+    if (sumlocwt_out) *sumlocwt_out = sumlocwt;
+    if (f2_out) *f2_out = f2;
+    int nd = 0;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        int uc, vc;
+        float ul, vl;
+        if (wcell(u, v, w, i, uscale, uoffset, vscale, voffset, uorigin, vorigin, shift, doshift,
+                  nu, nv, &uc, &vc, &ul, &vl)) {
+            newwt[i] = -1.0f;
+            nd++;
+            continue;
+        }
+        if (doaz) {
+            float t = atan2f(vl, ul);
+            t = fmodf(t - rpa + 2.5f * pi, pi) - pi / 2.0f;
+            float r = robust[0] - fabsf(t) * rbscale;
+            float tt = 5.0f * powf(10.0f, -r);
+            f2 = (float)((double)(tt * tt) / (sumlocwt / sumwt));
+        }
+        float g = F2(gwt, uc, vc, nu);
+        if (g > 0.0f) {
+            if (uc == uorigin && vc != vorigin)
+                newwt[i] = 0.5f * wt[i] / (g * f2 + d2);
+            else
+                newwt[i] = wt[i] / (g * f2 + d2);
+        } else {
+            newwt[i] = -1.0f;
+        }
+    }
+    if (ndrop) *ndrop = nd;
+    return ORC_OK;
+}
+
+/* grd/grdh2d.f:89-226 -- the 2-D gridder (shifted by SUPPU, symmetrised, normalised). */
+int orc_grdh2d(const float *vis, const float *wt, const float *u, const float *v, const float *w,
+               int nvis, float uscale, float uoffset, float vscale, float voffset, int uorigin,
+               int vorigin, float *gvis, int psf, int nu, int nv, const float *gridfnu, int suppu,
+               int osampu, const float *gridfnv, int suppv, int osampv, const double *shift,
+               float *sumwt, double *lsumwt_out) {
+    const double twopi = (double)(8.0f * atanf(1.0f));
+    const int cfoffset = (suppu + 1) * osampu + 1;
+    const int doshift = doshift_of(shift);
+    for (size_t k = 0; k < 2 * (size_t)nu * nv; k++) gvis[k] = 0.0f;
+    double lsumwt = 0.0;
+    float swt = 0.0f;
+#define GRE(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu)]
+#define GIM(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu) + 1]
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        double ug = (double)u[i], vg = (double)v[i], wg = (double)w[i];
+        double ucell, vcell;
+        float fr, fi;
+        if (doshift) {
+            double ul = SH(1, 1) * ug + SH(2, 1) * vg + SH(3, 1) * wg;
+            double vl = SH(1, 2) * ug + SH(2, 2) * vg + SH(3, 2) * wg;
+            double wl = SH(1, 3) * ug + SH(2, 3) * vg + SH(3, 3) * wg;
+            double phase = twopi * (wl - wg);
+            float c = (float)cos(phase), s = (float)(-sin(phase));
+            float a = vis[2 * i], b = vis[2 * i + 1];
+            fr = a * c - b * s;
+            fi = a * s + b * c;
+            ucell = (double)uscale * ul + (double)uoffset;
+            vcell = (double)vscale * vl + (double)voffset;
+        } else {
+            fr = vis[2 * i];
+            fi = vis[2 * i + 1];
+            ucell = (double)uscale * ug + (double)uoffset;
+            vcell = (double)vscale * vg + (double)voffset;
+        }
+        if (ucell > 0.0) {
+            fi = -fi;
+            ucell = ucell + (double)(float)uorigin;
+            vcell = vcell + (double)(float)vorigin;
+        } else {
+            ucell = -ucell + (double)(float)uorigin;
+            vcell = -vcell + (double)(float)vorigin;
+        }
+        if (psf) {
+            fr = 1.0f;
+            fi = 0.0f;
+        }
+        int nuc = orc_nint_d(ucell), nvc = orc_nint_d(vcell);
+        if (nuc + 2 * suppu > nu) continue;
+        if (nvc + suppv > nv) continue;
+        if (nvc - suppv < 1) continue;
+        swt = swt + wt[i];
+        int delui = orc_nint_d((double)osampu * ((double)(float)nuc - ucell)) + cfoffset;
+        int delvi = orc_nint_d((double)osampv * ((double)(float)nvc - vcell)) + cfoffset;
+        int ucen = nuc + suppu, vcen = nvc;
+        for (int offv = -suppv; offv <= suppv; offv++) {
+            int delv = delvi + osampv * offv;
+            int vgrid = vcen + offv;
+            for (int offu = -suppu; offu <= suppu; offu++) {
+                int delu = delui + osampu * offu;
+                int ugrid = ucen + offu;
+                double uvwt = (double)(wt[i] * gridfnu[delu - 1] * gridfnv[delv - 1]);
+                GRE(ugrid, vgrid) = (float)((double)GRE(ugrid, vgrid) + uvwt * (double)fr);
+                GIM(ugrid, vgrid) = (float)((double)GIM(ugrid, vgrid) + uvwt * (double)fi);
+                lsumwt = lsumwt + uvwt;
+            }
+        }
+    }
+    if (sumwt) *sumwt = swt;
+    if (lsumwt_out) *lsumwt_out = lsumwt;
+    if (lsumwt == 0.0) return ORC_ENOWEIGHT;
+    /* Symmetrize: grd/grdh2d.f:202-214 */
+    int ucen = uorigin + suppu, vcen = vorigin;
+    for (int offv = -nv / 2 + 1; offv <= nv / 2 - 1; offv++)
+        for (int offu = 1; offu <= suppu; offu++) {
+            GRE(ucen + offu, vcen + offv) = GRE(ucen + offu, vcen + offv) + GRE(ucen - offu, vcen - offv);
+            GIM(ucen + offu, vcen + offv) = GIM(ucen + offu, vcen + offv) - GIM(ucen - offu, vcen - offv);
+        }
+    for (int offv = 0; offv <= nv / 2 - 1; offv++) {
+        GRE(ucen, vcen + offv) = GRE(ucen, vcen + offv) + GRE(ucen, vcen - offv);
+        GIM(ucen, vcen + offv) = GIM(ucen, vcen + offv) - GIM(ucen, vcen - offv);
+        GRE(ucen, vcen - offv) = GRE(ucen, vcen + offv);
+        GIM(ucen, vcen - offv) = -GIM(ucen, vcen + offv);
+    }
+    /* Shift left and normalize: grd/grdh2d.f:218-226 */
+    double scale = (double)((float)(nu - 1) * (float)nv) / lsumwt;
+    for (int vg = 1; vg <= nv; vg++) {
+        for (int ug = 1; ug <= nu - suppu; ug++) {
+            GRE(ug, vg) = (float)(scale * (double)GRE(ug + suppu, vg));
+            GIM(ug, vg) = (float)(scale * (double)GIM(ug + suppu, vg));
+        }
+        for (int ug = nu - suppu + 1; ug <= nu; ug++) {
+            GRE(ug, vg) = 0.0f;
+            GIM(ug, vg) = 0.0f;
+        }
+    }
+#undef GRE
+#undef GIM
+    return ORC_OK;
+}
+
+/* grd/grddeh2d.f:77-200 -- the 2-D degridder. */
+void orc_grddeh2d(float *vis, float *wt, const float *u, const float *v, const float *w, int nvis,
+                  float uscale, float uoffset, float vscale, float voffset, int uorigin,
+                  int vorigin, const float *gvis, int nu, int nv, const float *intfnu, int suppu,
+                  int osampu, const float *intfnv, int suppv, int osampv, const double *shift,
+                  int *nbad_out) {
+    const double twopi = (double)(8.0f * atanf(1.0f));
+    const int cfoffset = (suppu + 1) * osampu + 1;
+    int nbad = 0;
+#define GR(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu)]
+#define GI(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu) + 1]
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        float vr = 0.0f, vi = 0.0f, sumwt = 0.0f;
+        vis[2 * i] = 0.0f;
+        vis[2 * i + 1] = 0.0f;
+        wt[i] = -wt[i];
+        double ug = (double)u[i], vg = (double)v[i], wg = (double)w[i];
+        double ul = SH(1, 1) * ug + SH(2, 1) * vg + SH(3, 1) * wg;
+        double vl = SH(1, 2) * ug + SH(2, 2) * vg + SH(3, 2) * wg;
+        double wl = SH(1, 3) * ug + SH(2, 3) * vg + SH(3, 3) * wg;
+        double phase = twopi * (wl - wg);
+        float rc = (float)cos(phase), rs = (float)sin(phase);
+        float ucell = (float)((double)uscale * ul + (double)uoffset);
+        float vcell = (float)((double)vscale * vl + (double)voffset);
+        if (ucell > 0.0f) {
+            ucell = ucell + (float)uorigin;
+            vcell = vcell + (float)vorigin;
+        } else {
+            ucell = -ucell + (float)uorigin;
+            vcell = -vcell + (float)vorigin;
+        }
+        int nuc = orc_nint_f(ucell), nvc = orc_nint_f(vcell);
+        if (nuc + suppu > nu) continue;
+        if (nvc + suppv > nv) continue;
+        if (nvc - suppv < 1) continue;
+        int delui = orc_nint_f((float)osampu * ((float)nuc - ucell));
+        int delvi = orc_nint_f((float)osampv * ((float)nvc - vcell));
+        int ucen = nuc - uorigin, vcen = nvc - vorigin;
+        if (nuc <= suppu) {
+            for (int offu = -suppu; offu <= suppu; offu++) {
+                if (ucen != -offu) {
+                    int usign = (ucen + offu) >= 0 ? 1 : -1;
+                    int delu = delui + osampu * offu + cfoffset;
+                    int uint_ = uorigin + usign * (ucen + offu);
+                    for (int offv = -suppv; offv <= suppv; offv++) {
+                        int delv = delvi + osampv * offv + cfoffset;
+                        int vint = vorigin + usign * (vcen + offv);
+                        float uvwt = intfnu[delu - 1] * intfnv[delv - 1];
+                        float fr = GR(uint_, vint), fi = GI(uint_, vint);
+                        if (usign <= 0) fi = -fi;
+                        vr = vr + fr * uvwt;
+                        vi = vi + fi * uvwt;
+                        sumwt = sumwt + uvwt;
+                    }
+                } else {
+                    int delu = delui + osampu * offu + cfoffset;
+                    int uint_ = uorigin;
+                    for (int offv = -suppv; offv <= suppv; offv++) {
+                        int delv = delvi + osampv * offv + cfoffset;
+                        int vint = vorigin + (vcen + offv);
+                        float uvwt = intfnu[delu - 1] * intfnv[delv - 1];
+                        vr = vr + GR(uint_, vint) * uvwt;
+                        vi = vi + GI(uint_, vint) * uvwt;
+                        sumwt = sumwt + uvwt;
+                    }
+                }
+            }
+        } else {
+            for (int offv = -suppv; offv <= suppv; offv++) {
+                int delv = delvi + osampv * offv + cfoffset;
+                int vint = vorigin + vcen + offv;
+                for (int offu = -suppu; offu <= suppu; offu++) {
+                    int delu = delui + osampu * offu + cfoffset;
+                    int uint_ = uorigin + ucen + offu;
+                    float uvwt = intfnu[delu - 1] * intfnv[delv - 1];
+                    vr = vr + GR(uint_, vint) * uvwt;
+                    vi = vi + GI(uint_, vint) * uvwt;
+                    sumwt = sumwt + uvwt;
+                }
+            }
+        }
+        if (sumwt > 0.0f) {
+            vr = vr / sumwt;
+            vi = vi / sumwt;
+            wt[i] = fabsf(wt[i]);
+        } else {
+            nbad++;
+            vr = 0.0f;
+            vi = 0.0f;
+        }
+        if ((double)uscale * ul > 0.0) vi = -vi;
+        vis[2 * i] = vr * rc - vi * rs;
+        vis[2 * i + 1] = vr * rs + vi * rc;
+    }
+#undef GR
+#undef GI
+    if (nbad_out) *nbad_out = nbad;
+}
+
+/* fft/fftx.f:261-452 -- radix-2 complex FFT with quarter-length tables (Newman/AIPS). */
+void orc_fftx(float *x, float *wk, int m, int isig) {
+#define X1(i) x[2 * ((i)-1)]
+#define X2(i) x[2 * ((i)-1) + 1]
+#define W1(i) wk[2 * ((i)-1)]
+#define W2(i) wk[2 * ((i)-1) + 1]
+    float arg = (float)m;
+    int n = (int)(logf(arg) / logf(2.0f) + 0.1f);
+    int m4 = m / 4, nm2 = n - 2;
+    float tpi = 8.0f * atanf(1.0f);
+    tpi = tpi / (float)m;
+    float *C = (float *)malloc(sizeof(float) * (size_t)(m4 > 0 ? m4 : 1));
+    float *S = (float *)malloc(sizeof(float) * (size_t)(m4 > 0 ? m4 : 1));
+    int *ibitrv = (int *)malloc(sizeof(int) * (size_t)m);
+    for (int i = 1; i <= m4; i++) {
+        arg = tpi * (float)(i - 1);
+        C[i - 1] = cosf(arg);
+        S[i - 1] = sinf(arg);
+    }
+    for (int i = 1; i <= m4; i++) {
+        int i1 = i - 1, j = 0;
+        for (int k = 1; k <= nm2; k++) {
+            int l = i1 / 2;
+            j = i1 + 2 * (j - l);
+            i1 = l;
+        }
+        j = j + 1;
+        if (i >= j) continue;
+        float xt = C[i - 1]; C[i - 1] = C[j - 1]; C[j - 1] = xt;
+        xt = S[i - 1]; S[i - 1] = S[j - 1]; S[j - 1] = xt;
+    }
+    for (int i = 1; i <= m; i++) {
+        int i1 = i - 1, j = 0;
+        for (int k = 1; k <= n; k++) {
+            int l = i1 / 2;
+            j = i1 + 2 * (j - l);
+            i1 = l;
+        }
+        ibitrv[i - 1] = j + 1;
+    }
+    if (isig == -1) {
+        for (int i = 1; i <= m; i++) { W1(i) = X1(i); W2(i) = X2(i); }
+    } else {
+        for (int i = 1; i <= m; i++) { W1(i) = X1(i); W2(i) = -X2(i); }
+    }
+    for (int mstep = 1; mstep <= n; mstep++) {
+        int isep = 1 << (n - mstep);
+        int isep4 = isep * 4;
+        int itimes = 1 << (mstep - 1);
+        if (itimes <= isep) {
+            for (int i = 1; i <= itimes; i++) {
+                int isepi1 = 2 * (i - 1) * isep;
+                int ii = (i + 1) / 2;
+                int ji1 = isepi1 + 1;
+                int ji = ji1 + isep;
+                float c = C[ii - 1], s = S[ii - 1];
+                if (i != 2 * (i / 2)) {
+                    for (int j = 1; j <= isep; j++) {
+                        float ar = W1(ji) * c - W2(ji) * s;
+                        float ai = W1(ji) * s + W2(ji) * c;
+                        W1(ji) = W1(ji1) - ar;
+                        W2(ji) = W2(ji1) - ai;
+                        W1(ji1) = W1(ji1) + ar;
+                        W2(ji1) = W2(ji1) + ai;
+                        ji1++;
+                        ji++;
+                    }
+                } else {
+                    for (int j = 1; j <= isep; j++) {
+                        float ar = W1(ji) * s + W2(ji) * c;
+                        float ai = W1(ji) * c - W2(ji) * s;
+                        W1(ji) = W1(ji1) + ar;
+                        W2(ji) = W2(ji1) - ai;
+                        W1(ji1) = W1(ji1) - ar;
+                        W2(ji1) = W2(ji1) + ai;
+                        ji1++;
+                        ji++;
+                    }
+                }
+            }
+        } else {
+            for (int j = 1; j <= isep; j++) {
+                int ii = 1, ji1 = j, ji = ji1 + isep;
+                for (int i = 1; i <= itimes; i += 2) {
+                    float c = C[ii - 1], s = S[ii - 1];
+                    float ar = W1(ji) * c - W2(ji) * s;
+                    float ai = W1(ji) * s + W2(ji) * c;
+                    W1(ji) = W1(ji1) - ar;
+                    W2(ji) = W2(ji1) - ai;
+                    W1(ji1) = W1(ji1) + ar;
+                    W2(ji1) = W2(ji1) + ai;
+                    ii++;
+                    ji1 += isep4;
+                    ji += isep4;
+                }
+                ii = 1;
+                ji1 = j + 2 * isep;
+                ji = ji1 + isep;
+                for (int i = 2; i <= itimes; i += 2) {
+                    float c = C[ii - 1], s = S[ii - 1];
+                    float ar = W1(ji) * s + W2(ji) * c;
+                    float ai = W1(ji) * c - W2(ji) * s;
+                    W1(ji) = W1(ji1) + ar;
+                    W2(ji) = W2(ji1) - ai;
+                    W1(ji1) = W1(ji1) - ar;
+                    W2(ji1) = W2(ji1) + ai;
+                    ii++;
+                    ji1 += isep4;
+                    ji += isep4;
+                }
+            }
+        }
+    }
+    if (isig == -1) {
+        for (int i = 1; i <= m; i++) { int ii = ibitrv[i - 1]; X1(i) = W1(ii); X2(i) = W2(ii); }
+    } else {
+        for (int i = 1; i <= m; i++) { int ii = ibitrv[i - 1]; X1(i) = W1(ii); X2(i) = -W2(ii); }
+    }
+    if (isig == -1) {
+        for (int i = 1; i <= m; i++) {
+            X1(i) = X1(i) / (float)m;
+            X2(i) = X2(i) / (float)m;
+        }
+    }
+    free(C);
+    free(S);
+    free(ibitrv);
+#undef X1
+#undef X2
+#undef W1
+#undef W2
+}
+
+/* fft/fftx1d.f:508-547 (power-of-two branch) */
+void orc_fftx1d(float *xarray, float *xwork, float *xwork2, int nx, int dir) {
+    int icen = (nx + 1) / 2, ioff = nx - icen + 1;
+    for (int ix = 1; ix <= icen - 1; ix++) {
+        xwork2[2 * (ix + ioff - 1)] = xarray[2 * (ix - 1)];
+        xwork2[2 * (ix + ioff - 1) + 1] = xarray[2 * (ix - 1) + 1];
+    }
+    ioff = -icen + 1;
+    for (int ix = icen; ix <= nx; ix++) {
+        xwork2[2 * (ix + ioff - 1)] = xarray[2 * (ix - 1)];
+        xwork2[2 * (ix + ioff - 1) + 1] = xarray[2 * (ix - 1) + 1];
+    }
+    orc_fftx(xwork2, xwork, nx, dir);
+    ioff = nx - icen + 1;
+    for (int ix = 1; ix <= icen - 1; ix++) {
+        xarray[2 * (ix - 1)] = xwork2[2 * (ix + ioff - 1)];
+        xarray[2 * (ix - 1) + 1] = xwork2[2 * (ix + ioff - 1) + 1];
+    }
+    ioff = -icen + 1;
+    for (int ix = icen; ix <= nx; ix++) {
+        xarray[2 * (ix - 1)] = xwork2[2 * (ix + ioff - 1)];
+        xarray[2 * (ix - 1) + 1] = xwork2[2 * (ix + ioff - 1) + 1];
+    }
+}
+
+/* fft/fftr.f:80-176 (non-Cray branch): real FFT via a half-length complex FFT. */
+void orc_fftr(float *R, float *C, float *work, int n, int f) {
+#define RR(i) R[(i)-1]
+#define CC(i) C[(i)-1]
+    if (n <= 0) return;
+    const float twopi = 6.2831852f;
+    int h = n / 2, q = h / 2;
+    float *tablr = (float *)malloc(sizeof(float) * (size_t)(q + 1));
+    float *tabli = (float *)malloc(sizeof(float) * (size_t)(q + 1));
+    float phas0 = -twopi / 4.0f, dphas = -twopi / (float)n;
+    for (int loop = 1; loop <= q; loop++) {
+        float phase = phas0 + (float)loop * dphas;
+        tablr[loop] = cosf(phase);
+        tabli[loop] = sinf(phase);
+    }
+    if (f >= 0) {
+        for (int loop = 1; loop <= n; loop++) CC(loop) = RR(loop);
+        orc_fftx(C, work, h, f);
+        for (int loop = 1; loop <= q; loop++) {
+            float sumr = CC(1 + 2 * loop) + CC(1 + 2 * (h - loop));
+            float sumi = CC(2 + 2 * loop) - CC(2 + 2 * (h - loop));
+            float diffr = CC(1 + 2 * loop) - CC(1 + 2 * (h - loop));
+            float diffi = CC(2 + 2 * loop) + CC(2 + 2 * (h - loop));
+            CC(1 + 2 * loop) = sumr + (tablr[loop] * diffr - tabli[loop] * diffi);
+            CC(2 + 2 * loop) = sumi + (tabli[loop] * diffr + tablr[loop] * diffi);
+            CC(1 + 2 * (h - loop)) = sumr - (tablr[loop] * diffr - tabli[loop] * diffi);
+            CC(2 + 2 * (h - loop)) = -sumi + (tabli[loop] * diffr + tablr[loop] * diffi);
+        }
+        float tempr = 2.0f * (CC(1) + CC(2));
+        CC(2) = 2.0f * (CC(1) - CC(2));
+        CC(1) = tempr;
+        for (int loop = 1; loop <= n; loop++) CC(loop) = 0.5f * CC(loop);
+        CC(n + 1) = CC(2);
+        CC(n + 2) = 0.0f;
+        CC(2) = 0.0f;
+    } else {
+        for (int loop = 1; loop <= n; loop++) RR(loop) = CC(loop);
+        RR(2) = CC(n + 1);
+        RR(n + 1) = 0.0f;
+        RR(n + 2) = 0.0f;
+        for (int loop = 1; loop <= q; loop++) {
+            float sumr = RR(1 + 2 * loop) + RR(1 + 2 * (h - loop));
+            float sumi = RR(2 + 2 * loop) - RR(2 + 2 * (h - loop));
+            float diffr = RR(1 + 2 * loop) - RR(1 + 2 * (h - loop));
+            float diffi = RR(2 + 2 * loop) + RR(2 + 2 * (h - loop));
+            RR(1 + 2 * loop) = sumr + (tablr[loop] * diffr + tabli[loop] * diffi);
+            RR(2 + 2 * loop) = sumi - (tabli[loop] * diffr - tablr[loop] * diffi);
+            RR(1 + 2 * (h - loop)) = sumr - (tablr[loop] * diffr + tabli[loop] * diffi);
+            RR(2 + 2 * (h - loop)) = -sumi - (tabli[loop] * diffr - tablr[loop] * diffi);
+        }
+        float tempr = RR(1) + RR(2);
+        RR(2) = RR(1) - RR(2);
+        RR(1) = tempr;
+        orc_fftx(R, work, h, f);
+        for (int loop = 1; loop <= n; loop++) RR(loop) = 0.5f * RR(loop);
+    }
+    free(tablr);
+    free(tabli);
+#undef RR
+#undef CC
+}
+
+/* fft/fftr1d.f:253-299 (power-of-two branch).  rwork needs nx+2 floats, xwork nx/2 complex. */
+void orc_fftr1d(float *rarray, float *xarray, float *rwork, float *xwork, int nx, int dir) {
+    int icen = (nx + 1) / 2;
+    if (dir > 0) {
+        int ioff = nx - icen + 1;
+        for (int ix = 1; ix <= icen - 1; ix++) rwork[ix + ioff - 1] = rarray[ix - 1];
+        ioff = -icen + 1;
+        for (int ix = icen; ix <= nx; ix++) rwork[ix + ioff - 1] = rarray[ix - 1];
+        orc_fftr(rwork, xarray, xwork, nx, dir);
+    } else {
+        orc_fftr(rwork, xarray, xwork, nx, dir);
+        int ioff = nx - icen + 1;
+        for (int ix = 1; ix <= icen - 1; ix++) rarray[ix - 1] = rwork[ix + ioff - 1];
+        ioff = -icen + 1;
+        for (int ix = icen; ix <= nx; ix++) rarray[ix - 1] = rwork[ix + ioff - 1];
+    }
+}
+
+/* fft/fftr1d2.f:137-184 */
+void orc_fftr1d2(float *rarray, float *xarray, float *xwork, float *xwork2, float *rwork,
+                 int nx, int fnu, int dir) {
+    if (dir > 0) {
+        if (fnu > nx) {
+            int ioff = (fnu - nx) / 2;
+            for (int ix = 1; ix <= fnu; ix++) rwork[ix - 1] = 0.0f;
+            for (int ix = 1; ix <= nx; ix++) rwork[ioff + ix - 1] = rarray[ix - 1];
+        } else {
+            for (int ix = 1; ix <= nx; ix++) rwork[ix - 1] = rarray[ix - 1];
+        }
+        orc_fftr1d(rwork, xarray, xwork, xwork2, fnu, dir);
+    } else {
+        orc_fftr1d(rwork, xarray, xwork, xwork2, fnu, dir);
+        if (fnu == nx) {
+            for (int ix = 1; ix <= nx; ix++) rarray[ix - 1] = rwork[ix - 1];
+        } else {
+            int ioff = (fnu - nx) / 2;
+            for (int ix = 1; ix <= nx; ix++) rarray[ix - 1] = rwork[ioff + ix - 1];
+        }
+    }
+}
+
+/* fft/fftr2d.f:46-97.  rarray [ny][nx] real, xarray [nv][fnu/2+1] complex. */
+void orc_fftr2d(float *rarray, float *xarray, int nx, int ny, int fnu, int nv, int dir) {
+    int nu = fnu / 2 + 1, fny = nv;
+    int ibegy = (fny + 1) / 2 - (ny + 1) / 2 + 1;
+    int iendy = (fny + 1) / 2 + ny / 2;
+    int maxn = (fnu > nv ? fnu : nv) + 8;
+    float *work = (float *)calloc(2 * (size_t)maxn, sizeof(float));
+    float *work2 = (float *)calloc(2 * (size_t)maxn, sizeof(float));
+    float *rwork = (float *)calloc(2 * (size_t)maxn, sizeof(float));
+#define XA(ix, iy) (xarray + 2 * (((size_t)(ix)-1) + (size_t)((iy)-1) * (size_t)nu))
+    if (dir > 0) {
+        for (int iy = 1; iy <= ibegy - 1; iy++)
+            for (int ix = 1; ix <= nu; ix++) { XA(ix, iy)[0] = 0.0f; XA(ix, iy)[1] = 0.0f; }
+        for (int iy = 1; iy <= ny; iy++)
+            orc_fftr1d2(rarray + (size_t)(iy - 1) * nx, XA(1, iy + ibegy - 1), work, work2, rwork,
+                        nx, fnu, dir);
+        for (int iy = iendy + 1; iy <= fny; iy++)
+            for (int ix = 1; ix <= nu; ix++) { XA(ix, iy)[0] = 0.0f; XA(ix, iy)[1] = 0.0f; }
+        for (int ix = 1; ix <= nu; ix++) {
+            for (int iy = 1; iy <= fny; iy++) { work2[2 * (iy - 1)] = XA(ix, iy)[0]; work2[2 * (iy - 1) + 1] = XA(ix, iy)[1]; }
+            orc_fftx1d(work2, work, rwork, fny, dir);
+            for (int iy = 1; iy <= fny; iy++) { XA(ix, iy)[0] = work2[2 * (iy - 1)]; XA(ix, iy)[1] = work2[2 * (iy - 1) + 1]; }
+        }
+    } else {
+        for (int ix = 1; ix <= nu; ix++) {
+            for (int iy = 1; iy <= fny; iy++) { work2[2 * (iy - 1)] = XA(ix, iy)[0]; work2[2 * (iy - 1) + 1] = XA(ix, iy)[1]; }
+            orc_fftx1d(work2, work, rwork, fny, dir);
+            for (int iy = 1; iy <= fny; iy++) { XA(ix, iy)[0] = work2[2 * (iy - 1)]; XA(ix, iy)[1] = work2[2 * (iy - 1) + 1]; }
+        }
+        for (int iy = 1; iy <= ny; iy++)
+            orc_fftr1d2(rarray + (size_t)(iy - 1) * nx, XA(1, iy + ibegy - 1), work, work2, rwork,
+                        nx, fnu, dir);
+    }
+#undef XA
+    free(work);
+    free(work2);
+    free(rwork);
+}
+
+/* pix/pixcor2d.f:44-68 */
+void orc_pixcor2d(const float *in, int nx, int ny, const float *cf, int cflen, int correct,
+                  float *out, float cenx, float ceny) {
+    int fnx = orc_fftpwr2(nx), fny = orc_fftpwr2(ny);
+    float scalex = (float)(cflen - 1) * 2.0f / (float)fnx;
+    float scaley = (float)(cflen - 1) * 2.0f / (float)fny;
+    for (int iy = 1; iy <= ny; iy++) {
+        int icfy = 1 + abs(orc_nint_f(scaley * ((float)iy - ceny)));
+        for (int ix = 1; ix <= nx; ix++) {
+            int icfx = 1 + abs(orc_nint_f(scalex * ((float)ix - cenx)));
+            size_t k = (size_t)(ix - 1) + (size_t)(iy - 1) * nx;
+            if (correct)
+                out[k] = in[k] / (cf[icfx - 1] * cf[icfy - 1]);
+            else
+                out[k] = cf[icfx - 1] * cf[icfy - 1] * in[k];
+        }
+    }
+}
+
+/* pix/pixisama.f:269-277 -- first index of strictly greatest |A|, 1-based; I if none */
+int orc_pixisama(int n, const float *a, int i) {
+    int r = i;
+    float maxval = 0.0f;
+    for (int j = 1; j <= n; j++) {
+        if (fabsf(a[j - 1]) > maxval) {
+            maxval = fabsf(a[j - 1]);
+            r = j;
+        }
+    }
+    return r;
+}
+
+/* pix/pix2drcl.f:134-215 -- Hogbom CLEAN minor cycle.  A PSF read whose flat
+ * column-major offset falls outside the PSF array reads 0 (the reference reads
+ * whatever memory follows; no caller in the reference does that). */
+void orc_pix2drcl(const float *drt, const float *psf, const float *box, int nx, int ny, int pnx,
+                  int pny, float gain, int nsub, int bsub, float flux, float *cln, float *res,
+                  int *ansub, float *maxres, float *tflux, float *cflux, int *cx, int *cy) {
+    const size_t npix = (size_t)nx * ny, pnpix = (size_t)pnx * pny;
+    for (size_t k = 0; k < npix; k++) res[k] = drt[k] * box[k];
+    int ipeak = orc_pixisama(pnx * pny, psf, 1) - 1;
+    int pmpx = 1 + ipeak % pnx;
+    int pmpy = 1 + (ipeak - pmpx + 1) / pnx;
+    if (pmpx >= pnx) pmpx = pnx / 2;
+    if (pmpy >= pny) pmpy = pny / 2;
+    int isub, pmx, pmy;
+    float mres = 0.0f;
+    int nabs = nsub < 0 ? -nsub : nsub;
+    for (isub = bsub; isub <= nabs; isub++) {
+        ipeak = orc_pixisama(nx * ny, res, 1) - 1;
+        pmx = 1 + ipeak % nx;
+        pmy = 1 + (ipeak - pmx + 1) / nx;
+        mres = res[(size_t)(pmx - 1) + (size_t)(pmy - 1) * nx];
+        if (nsub < 0 && mres < 0.0f) goto stopped;
+        if (fabsf(mres) <= flux) goto stopped;
+        float pntsub = gain * mres;
+        *tflux = *tflux + pntsub;
+        cln[(size_t)(pmx - 1) + (size_t)(pmy - 1) * nx] += pntsub;
+        cflux[isub - 1] = pntsub;
+        cx[isub - 1] = pmx;
+        cy[isub - 1] = pmy;
+        int offx = pmpx + pmx, offy = pmpy + pmy;
+        for (int iy = 1; iy <= ny; iy++)
+            for (int ix = 1; ix <= nx; ix++) {
+                long long flat = (long long)(offx - ix - 1) + (long long)(offy - iy - 1) * pnx;
+                float p = (flat >= 0 && (size_t)flat < pnpix) ? psf[flat] : 0.0f;
+                size_t k = (size_t)(ix - 1) + (size_t)(iy - 1) * nx;
+                res[k] = res[k] - (pntsub * p * box[k]);
+            }
+    }
+    *ansub = nsub;
+    ipeak = orc_pixisama(nx * ny, res, 1) - 1;
+    pmx = 1 + ipeak % nx;
+    pmy = 1 + (ipeak - pmx + 1) / nx;
+    *maxres = res[(size_t)(pmx - 1) + (size_t)(pmy - 1) * nx];
+    return;
+stopped:
+    *ansub = isub - 1;
+    *maxres = mres;
+}
+
+/* pix/pixrscal.f: OUT(I) = SCALE * IN(I) + OFFSET */
+void orc_pixrscal(const float *in, float scale, float offset, float *out, int64_t n) {
+    for (int64_t i = 0; i < n; i++) out[i] = scale * in[i] + offset;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Task-level drivers.
+ * img/imgmake.f (CDELT = -/+ CELLSIZE/3600, CRPIX = (N+1)/2), fft/fftconja.f:159-163 and
+ * fft/fftconj.f (FNU = pow2(N), NU = FNU/2+1, CDELT = 1/(D2R*WIDTH), RPIX = 1, (NV+1)/2),
+ * vis/visgrid.f:317-322 (USCALE = 1/CDELT, UORIGIN = NINT(RPIX)). */
+void orc_make_geom(const orc_uvmap_params *p, orc_geom *g) {
+    const float PI = 3.141592654f;
+    const float D2R = PI / 180.0f;
+    int n = p->imsize;
+    float delt_ra = -p->cellsize / 3600.0f, delt_dec = p->cellsize / 3600.0f;
+    g->nx = n;
+    g->ny = n;
+    g->fnu = orc_fftpwr2(n);
+    g->nu = g->fnu / 2 + 1;
+    g->nv = orc_fftpwr2(n);
+    float width_u = (float)orc_fftpwr2(n) * delt_ra;
+    float width_v = (float)orc_fftpwr2(n) * delt_dec;
+    float cdelt_u = 1.0f / (D2R * width_u);
+    float cdelt_v = 1.0f / (D2R * width_v);
+    g->uscale = 1.0f / cdelt_u;
+    g->vscale = 1.0f / cdelt_v;
+    g->uorigin = 1;
+    g->vorigin = orc_nint_f((float)((g->nv + 1) / 2));
+    g->cenx = (float)((n + 1) / 2);
+    g->ceny = (float)((n + 1) / 2);
+    double ira = p->vra + (double)(p->shift_ra / 3600.0f);
+    double idec = p->vdec + (double)(p->shift_dec / 3600.0f);
+    orc_crdshift(p->vra, p->vdec, ira, idec, 0.0f, g->shift);
+}
+
+static void image_from_grid(const orc_geom *g, float *grid, float *image, const float *ccf,
+                            int ccflen) {
+    orc_fftr2d(image, grid, g->nx, g->ny, g->fnu, g->nv, -1);
+    orc_pixcor2d(image, g->nx, g->ny, ccf, ccflen, 1, image, g->cenx, g->ceny);
+}
+
+/* task/uvmap.f:212-314 (weighting), 414-491 (PSF + dirty, PSF-peak normalisation). */
+int orc_uvmap(const orc_uvmap_params *p, int nvis, const float *u, const float *v,
+              const float *w, const float *vis, float *wt, float *dirty, float *psf,
+              float *maxpsf_out, float *sumwt_psf) {
+    orc_geom g;
+    orc_make_geom(p, &g);
+    size_t ncell = (size_t)g.nu * g.nv;
+    float *grid = (float *)malloc(2 * ncell * sizeof(float));
+    int rc = ORC_OK;
+    if (p->fov != 0.0f) {
+        /* CDELT of the XFR axes is 1/uscale; GRDUWT/GRDRUWT use WTFOV/CDELT (grd/grduwt.f:115). */
+        float cdelt_u = 1.0f / g.uscale, cdelt_v = 1.0f / g.vscale;
+        float us = p->fov / cdelt_u, vs = p->fov / cdelt_v;
+        if (p->rmode == 0) {
+            orc_grduwt2d(wt, u, v, w, nvis, us, 0.0f, vs, 0.0f, g.uorigin, g.vorigin, wt, grid,
+                         g.nu, g.nv, g.shift, NULL);
+        } else {
+            static const char *modes[] = {"NONE", "NORM", "ABS", "AZ-NORM"};
+            rc = orc_grdruw2d(wt, u, v, w, nvis, us, 0.0f, vs, 0.0f, g.uorigin, g.vorigin, wt,
+                              grid, g.nu, g.nv, g.shift, modes[p->rmode], p->robust, p->ds, NULL,
+                              NULL, NULL, NULL);
+            if (rc) goto done;
+        }
+    }
+    float cf[1 + 8 * 129];
+    int supp, osamp;
+    orc_grdcf(1, cf, &supp, &osamp);
+    int ccflen = 1 + orc_fftpwr2(g.nx > g.ny ? g.nx : g.ny) / 2;
+    float *ccf = (float *)malloc(sizeof(float) * (size_t)ccflen);
+    orc_grdccf(1, ccf, ccflen);
+    float sumwt;
+    rc = orc_grdh2d(vis, wt, u, v, w, nvis, g.uscale, 0.0f, g.vscale, 0.0f, g.uorigin, g.vorigin,
+                    grid, 1, g.nu, g.nv, cf, supp, osamp, cf, supp, osamp, g.shift, &sumwt, NULL);
+    if (rc) { free(ccf); goto done; }
+    if (sumwt_psf) *sumwt_psf = sumwt;
+    image_from_grid(&g, grid, psf, ccf, ccflen);
+    size_t npix = (size_t)g.nx * g.ny;
+    float maxpsf = psf[0];
+    for (size_t k = 1; k < npix; k++)
+        if (psf[k] > maxpsf) maxpsf = psf[k];
+    if (maxpsf_out) *maxpsf_out = maxpsf;
+    if (maxpsf == 0.0f) { rc = ORC_EBADARG; free(ccf); goto done; }
+    orc_pixrscal(psf, 1.0f / maxpsf, 0.0f, psf, (int64_t)npix);
+    rc = orc_grdh2d(vis, wt, u, v, w, nvis, g.uscale, 0.0f, g.vscale, 0.0f, g.uorigin, g.vorigin,
+                    grid, 0, g.nu, g.nv, cf, supp, osamp, cf, supp, osamp, g.shift, &sumwt, NULL);
+    if (rc) { free(ccf); goto done; }
+    image_from_grid(&g, grid, dirty, ccf, ccflen);
+    orc_pixrscal(dirty, 1.0f / maxpsf, 0.0f, dirty, (int64_t)npix);
+    free(ccf);
+done:
+    free(grid);
+    return rc;
+}
+
+/* task/vismodel.f:70-73: IMGGRIDC(CORRECT) -> IMGFFT (r2c, DIR +1) -> VISDEGRI. */
+int orc_vismodel(const orc_uvmap_params *p, int nvis, const float *u, const float *v,
+                 const float *w, float *vis, float *wt, const float *image) {
+    orc_geom g;
+    orc_make_geom(p, &g);
+    size_t npix = (size_t)g.nx * g.ny;
+    float *img = (float *)malloc(npix * sizeof(float));
+    float *grid = (float *)malloc(2 * (size_t)g.nu * g.nv * sizeof(float));
+    int ccflen = 1 + orc_fftpwr2(g.nx > g.ny ? g.nx : g.ny) / 2;
+    float *ccf = (float *)malloc(sizeof(float) * (size_t)ccflen);
+    orc_grdccf(1, ccf, ccflen);
+    orc_pixcor2d(image, g.nx, g.ny, ccf, ccflen, 1, img, g.cenx, g.ceny);
+    orc_fftr2d(img, grid, g.nx, g.ny, g.fnu, g.nv, +1);
+    float cf[1 + 8 * 129];
+    int supp, osamp;
+    orc_grdcf(1, cf, &supp, &osamp);
+    orc_grddeh2d(vis, wt, u, v, w, nvis, g.uscale, 0.0f, g.vscale, 0.0f, g.uorigin, g.vorigin,
+                 grid, g.nu, g.nv, cf, supp, osamp, cf, supp, osamp, g.shift, NULL);
+    free(img);
+    free(grid);
+    free(ccf);
+    return ORC_OK;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * FP64 oracle: the gridder, inverse FFT and grid correction of the same algorithm carried
+ * in double precision (convolution-function table kept at its REAL values, since it is
+ * part of the algorithm's definition).  Used to state every result's error vs FP64. */
+int orc64_grdh2d(const float *vis, const float *wt, const float *u, const float *v,
+                 const float *w, int nvis, const orc_geom *g, int psf, double *gvis) {
+    float cf[1 + 8 * 129];
+    int supp, osamp;
+    orc_grdcf(1, cf, &supp, &osamp);
+    const double *shift = g->shift;
+    const int nu = g->nu, nv = g->nv;
+    const double twopi = 2.0 * M_PI;
+    const int cfoffset = (supp + 1) * osamp + 1;
+    const int doshift = doshift_of(shift);
+    memset(gvis, 0, 2 * (size_t)nu * nv * sizeof(double));
+    double lsumwt = 0.0;
+#define GRE(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu)]
+#define GIM(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu) + 1]
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        double ug = u[i], vg = v[i], wg = w[i], ucell, vcell, fr, fi;
+        if (doshift) {
+            double ul = SH(1, 1) * ug + SH(2, 1) * vg + SH(3, 1) * wg;
+            double vl = SH(1, 2) * ug + SH(2, 2) * vg + SH(3, 2) * wg;
+            double wl = SH(1, 3) * ug + SH(2, 3) * vg + SH(3, 3) * wg;
+            double ph = twopi * (wl - wg), c = cos(ph), s = -sin(ph);
+            double a = vis[2 * i], b = vis[2 * i + 1];
+            fr = a * c - b * s;
+            fi = a * s + b * c;
+            ucell = (double)g->uscale * ul;
+            vcell = (double)g->vscale * vl;
+        } else {
+            fr = vis[2 * i];
+            fi = vis[2 * i + 1];
+            ucell = (double)g->uscale * ug;
+            vcell = (double)g->vscale * vg;
+        }
+        if (ucell > 0.0) {
+            fi = -fi;
+            ucell += g->uorigin;
+            vcell += g->vorigin;
+        } else {
+            ucell = -ucell + g->uorigin;
+            vcell = -vcell + g->vorigin;
+        }
+        if (psf) { fr = 1.0; fi = 0.0; }
+        int nuc = orc_nint_d(ucell), nvc = orc_nint_d(vcell);
+        if (nuc + 2 * supp > nu || nvc + supp > nv || nvc - supp < 1) continue;
+        int delui = orc_nint_d((double)osamp * ((double)nuc - ucell)) + cfoffset;
+        int delvi = orc_nint_d((double)osamp * ((double)nvc - vcell)) + cfoffset;
+        for (int offv = -supp; offv <= supp; offv++)
+            for (int offu = -supp; offu <= supp; offu++) {
+                double uvwt = (double)wt[i] * (double)cf[delui + osamp * offu - 1] *
+                              (double)cf[delvi + osamp * offv - 1];
+                GRE(nuc + supp + offu, nvc + offv) += uvwt * fr;
+                GIM(nuc + supp + offu, nvc + offv) += uvwt * fi;
+                lsumwt += uvwt;
+            }
+    }
+    if (lsumwt == 0.0) return ORC_ENOWEIGHT;
+    int ucen = g->uorigin + supp, vcen = g->vorigin;
+    for (int offv = -nv / 2 + 1; offv <= nv / 2 - 1; offv++)
+        for (int offu = 1; offu <= supp; offu++) {
+            GRE(ucen + offu, vcen + offv) += GRE(ucen - offu, vcen - offv);
+            GIM(ucen + offu, vcen + offv) -= GIM(ucen - offu, vcen - offv);
+        }
+    for (int offv = 0; offv <= nv / 2 - 1; offv++) {
+        GRE(ucen, vcen + offv) += GRE(ucen, vcen - offv);
+        GIM(ucen, vcen + offv) -= GIM(ucen, vcen - offv);
+        GRE(ucen, vcen - offv) = GRE(ucen, vcen + offv);
+        GIM(ucen, vcen - offv) = -GIM(ucen, vcen + offv);
+    }
+    double scale = (double)(nu - 1) * (double)nv / lsumwt;
+    for (int vg = 1; vg <= nv; vg++) {
+        for (int ug = 1; ug <= nu - supp; ug++) {
+            GRE(ug, vg) = scale * GRE(ug + supp, vg);
+            GIM(ug, vg) = scale * GIM(ug + supp, vg);
+        }
+        for (int ug = nu - supp + 1; ug <= nu; ug++) { GRE(ug, vg) = 0.0; GIM(ug, vg) = 0.0; }
+    }
+#undef GRE
+#undef GIM
+    return ORC_OK;
+}
+
+/* in-place radix-2 complex FFT in double, x[k] <- sum_j x[j] exp(sgn*2*pi*i*j*k/n) */
+static void fft64(double *x, int n, int sgn) {
+    for (int i = 1, j = 0; i < n; i++) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) {
+            double t0 = x[2 * i], t1 = x[2 * i + 1];
+            x[2 * i] = x[2 * j]; x[2 * i + 1] = x[2 * j + 1];
+            x[2 * j] = t0; x[2 * j + 1] = t1;
+        }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        double ang = sgn * 2.0 * M_PI / len;
+        for (int i = 0; i < n; i += len)
+            for (int k = 0; k < len / 2; k++) {
+                double wr = cos(ang * k), wi = sin(ang * k);
+                double *a = x + 2 * (i + k), *b = x + 2 * (i + k + len / 2);
+                double tr = b[0] * wr - b[1] * wi, ti = b[0] * wi + b[1] * wr;
+                b[0] = a[0] - tr; b[1] = a[1] - ti;
+                a[0] += tr; a[1] += ti;
+            }
+    }
+}
+
+/* Inverse (DIR = -1) transform of fft/fftr2d.f in double.  The reference's FFTX with
+ * ISIG = -1 computes sum_j x_j exp(+2 pi i jk/M)/M, FFTX1D/FFTR1D shift the centre by
+ * (N+1)/2-1 on both sides, and FFTR's c2r (FFTX of length N/2 then x0.5) gives
+ * r_n = (1/N) sum over the Hermitian extension of C_k exp(+2 pi i kn/N), reading only the
+ * real parts of C_1 and C_{N/2+1}. */
+void orc64_fftr2d_inv(const double *xarray, double *image, int nx, int ny, int fnu, int nv) {
+    int nu = fnu / 2 + 1;
+    double *col = (double *)malloc(2 * (size_t)nv * sizeof(double));
+    double *xt = (double *)malloc(2 * (size_t)nu * nv * sizeof(double));
+    int icv = (nv + 1) / 2, cv = icv - 1;
+    for (int ix = 0; ix < nu; ix++) {
+        for (int j = 0; j < nv; j++) { /* packed: xw[j] = x[(j + cv) mod nv] */
+            int src = (j + cv) % nv;
+            col[2 * j] = xarray[2 * ((size_t)src * nu + ix)];
+            col[2 * j + 1] = xarray[2 * ((size_t)src * nu + ix) + 1];
+        }
+        fft64(col, nv, +1);
+        for (int j = 0; j < nv; j++) {
+            int dst = (j + cv) % nv;
+            xt[2 * ((size_t)dst * nu + ix)] = col[2 * j] / nv;
+            xt[2 * ((size_t)dst * nu + ix) + 1] = col[2 * j + 1] / nv;
+        }
+    }
+    free(col);
+    double *row = (double *)malloc(2 * (size_t)fnu * sizeof(double));
+    int icu = (fnu + 1) / 2, cu = icu - 1;
+    int ibegy = (nv + 1) / 2 - (ny + 1) / 2 + 1;
+    for (int iy = 0; iy < ny; iy++) {
+        const double *xr = xt + 2 * (size_t)(iy + ibegy - 1) * nu;
+        for (int k = 0; k < fnu; k++) {
+            double re, im;
+            if (k == 0) { re = xr[0]; im = 0.0; }
+            else if (k == fnu / 2) { re = xr[2 * k]; im = 0.0; }
+            else if (k < fnu / 2) { re = xr[2 * k]; im = xr[2 * k + 1]; }
+            else { re = xr[2 * (fnu - k)]; im = -xr[2 * (fnu - k) + 1]; }
+            row[2 * k] = re;
+            row[2 * k + 1] = im;
+        }
+        fft64(row, fnu, +1);
+        int ioff = (fnu - nx) / 2;
+        for (int ix = 0; ix < nx; ix++) {
+            int n = ((ix + ioff) - cu + fnu) % fnu; /* rarray(ix) = r[(ix - cu) mod fnu] */
+            image[(size_t)iy * nx + ix] = row[2 * n] / fnu;
+        }
+    }
+    free(row);
+    free(xt);
+}
+
+void orc64_uvmap_image(const orc_geom *g, int nvis, const float *u, const float *v,
+                       const float *w, const float *vis, const float *wt, int psf,
+                       double *image) {
+    double *grid = (double *)malloc(2 * (size_t)g->nu * g->nv * sizeof(double));
+    if (orc64_grdh2d(vis, wt, u, v, w, nvis, g, psf, grid) != ORC_OK) {
+        memset(image, 0, sizeof(double) * (size_t)g->nx * g->ny);
+        free(grid);
+        return;
+    }
+    orc64_fftr2d_inv(grid, image, g->nx, g->ny, g->fnu, g->nv);
+    free(grid);
+    int ccflen = 1 + orc_fftpwr2(g->nx > g->ny ? g->nx : g->ny) / 2;
+    int fnx = orc_fftpwr2(g->nx), fny = orc_fftpwr2(g->ny);
+    double sx = (double)(ccflen - 1) * 2.0 / fnx, sy = (double)(ccflen - 1) * 2.0 / fny;
+    for (int iy = 1; iy <= g->ny; iy++) {
+        int icy = 1 + abs(orc_nint_d(sy * (iy - g->ceny)));
+        double cy = orc_grdsf((double)(icy - 1) / (double)(ccflen - 1));
+        for (int ix = 1; ix <= g->nx; ix++) {
+            int icx = 1 + abs(orc_nint_d(sx * (ix - g->cenx)));
+            double cx = orc_grdsf((double)(icx - 1) / (double)(ccflen - 1));
+            image[(size_t)(iy - 1) * g->nx + (ix - 1)] /= (cx * cy);
+        }
+    }
+}
+
+/* Direct Fourier sum of the weighted visibilities onto the image pixels (the idea of the
+ * reference's VISDFT, vis/visdft.f), with the same sign and centre conventions as the
+ * gridded path: I(ix,iy) = sum_k wt_k Re{V_k exp(2 pi i (u_k l + v_k m))}, l = (ix-cenx)*dl.
+ * Sign of l follows CDELT(RA) < 0.  Normalised so that the PSF peak is 1 (psf=1). */
+void orc64_dft_image(const orc_geom *g, int nvis, const float *u, const float *v,
+                     const float *vis, const float *wt, int psf, double *image) {
+    double dl = -1.0 / ((double)g->uscale * g->fnu);
+    double dm = -1.0 / ((double)g->vscale * g->nv);
+    double wsum = 0.0;
+    for (int k = 0; k < nvis; k++)
+        if (wt[k] > 0.0f) wsum += wt[k];
+    for (int iy = 1; iy <= g->ny; iy++) {
+        double m = (iy - g->ceny) * dm;
+        for (int ix = 1; ix <= g->nx; ix++) {
+            double l = (ix - g->cenx) * dl, s = 0.0;
+            for (int k = 0; k < nvis; k++) {
+                if (wt[k] <= 0.0f) continue;
+                double ph = 2.0 * M_PI * ((double)u[k] * l + (double)v[k] * m);
+                double vr = psf ? 1.0 : vis[2 * k], vi = psf ? 0.0 : vis[2 * k + 1];
+                s += wt[k] * (vr * cos(ph) - vi * sin(ph));
+            }
+            image[(size_t)(iy - 1) * g->nx + (ix - 1)] = s / wsum;
+        }
+    }
+}

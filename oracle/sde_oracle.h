@@ -1,0 +1,122 @@
+/*
+ * sde_oracle.h -- CPU restatement of the SDE imaging hot path (test infrastructure).
+ *
+ * This library is the ORACLE used by the tests, by __graft_entry__.smoke() and by
+ * bench.py's cpu_baseline / --impl reference legs.  It is never linked into, loaded by
+ * or called from the product library (libsdegpu).  Each routine restates one Fortran-77
+ * routine of timcornwell/sde with the same arithmetic types and evaluation order
+ * (REAL -> float, DOUBLE PRECISION -> double, NINT -> round-half-away, no FMA
+ * contraction: build with -ffp-contract=off).  Arrays are passed 0-based but index
+ * arithmetic follows the Fortran 1-based formulas; 2-D arrays are column-major
+ * (Fortran GVIS(NU,NV) == C row-major [NV][NU]).  Complex arrays are interleaved
+ * float pairs (re, im).
+ *
+ * Documented deviations from the reference source:
+ *   - FFTX's bit-reverse table is sized to M (reference IBITRV(4096) overflows at
+ *     M = 8192, fft/fftx.f:289), and FFTX/FFTR tables are recomputed on every call
+ *     (the reference keeps them in non-SAVEd locals, fft/fftx.f:289-292, fft/fftr.f:87).
+ */
+#ifndef SDE_ORACLE_H
+#define SDE_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* error codes returned where the reference calls ERRREPOR */
+#define ORC_OK 0
+#define ORC_ENOWEIGHT 1   /* grd/grdh2d.f:195-197 'No weight!'          */
+#define ORC_EBADMODE 2    /* grd/grdruw2d.f:361 'Unrecognized RMODE'      */
+#define ORC_EBADARG 3
+
+double orc_grdsf(double nu);                                   /* grd/grdsf.f:306-375   */
+int    orc_fftpwr2(int i);                                     /* fft/fftpwr2.f:7-42    */
+int    orc_nint_f(float x);                                    /* Fortran NINT(REAL)    */
+int    orc_nint_d(double x);                                   /* Fortran NINT(DOUBLE)  */
+void   orc_grdcf(int code_sf, float *cf, int *cfsupp, int *cfosamp); /* grd/grdcf.f:211-299 */
+void   orc_grdccf(int code_sf, float *ccf, int ccflen);        /* grd/grdccf.f:382-443  */
+void   orc_crdshift(double vra_deg, double vdec_deg, double ira_deg, double idec_deg,
+                    float vrota3_deg, double *shift);          /* crd/crdshift.f:7-169  */
+
+void orc_grduwt2d(const float *wt, const float *u, const float *v, const float *w, int nvis,
+                  float uscale, float uoffset, float vscale, float voffset, int uorigin,
+                  int vorigin, float *newwt, float *gwt, int nu, int nv, const double *shift,
+                  int *ndrop);                                 /* grd/grduwt2d.f:7-170  */
+int orc_grdruw2d(const float *wt, const float *u, const float *v, const float *w, int nvis,
+                 float uscale, float uoffset, float vscale, float voffset, int uorigin,
+                 int vorigin, float *newwt, float *gwt, int nu, int nv, const double *shift,
+                 const char *rmode, const float *robust, float ds, int *ndrop,
+                 double *sumwt_out, double *sumlocwt_out, float *f2_out); /* grd/grdruw2d.f:177-422 */
+
+int orc_grdh2d(const float *vis, const float *wt, const float *u, const float *v, const float *w,
+               int nvis, float uscale, float uoffset, float vscale, float voffset, int uorigin,
+               int vorigin, float *gvis, int psf, int nu, int nv, const float *gridfnu, int suppu,
+               int osampu, const float *gridfnv, int suppv, int osampv, const double *shift,
+               float *sumwt, double *lsumwt_out);              /* grd/grdh2d.f:7-229    */
+void orc_grddeh2d(float *vis, float *wt, const float *u, const float *v, const float *w, int nvis,
+                  float uscale, float uoffset, float vscale, float voffset, int uorigin,
+                  int vorigin, const float *gvis, int nu, int nv, const float *intfnu, int suppu,
+                  int osampu, const float *intfnv, int suppv, int osampv, const double *shift,
+                  int *nbad);                                  /* grd/grddeh2d.f:7-204  */
+
+void orc_fftx(float *x, float *w, int m, int isig);            /* fft/fftx.f:261-452    */
+void orc_fftx1d(float *xarray, float *xwork, float *xwork2, int nx, int dir); /* fft/fftx1d.f */
+void orc_fftr(float *r, float *c, float *work, int n, int f);  /* fft/fftr.f:60-176     */
+void orc_fftr1d(float *rarray, float *xarray, float *rwork, float *xwork, int nx, int dir);
+void orc_fftr1d2(float *rarray, float *xarray, float *xwork, float *xwork2, float *rwork,
+                 int nx, int fnu, int dir);
+void orc_fftr2d(float *rarray, float *xarray, int nx, int ny, int fnu, int nv, int dir); /* fft/fftr2d.f */
+
+void orc_pixcor2d(const float *in, int nx, int ny, const float *cf, int cflen, int correct,
+                  float *out, float cenx, float ceny);         /* pix/pixcor2d.f:7-71   */
+int  orc_pixisama(int n, const float *a, int i);               /* pix/pixisama.f:231-288 */
+void orc_pix2drcl(const float *drt, const float *psf, const float *box, int nx, int ny, int pnx,
+                  int pny, float gain, int nsub, int bsub, float flux, float *cln, float *res,
+                  int *ansub, float *maxres, float *tflux, float *cflux, int *cx, int *cy);
+void orc_pixrscal(const float *in, float scale, float offset, float *out, int64_t n); /* pix/pixrscal.f */
+
+/* ---- task-level drivers (task/uvmap.f, task/vismodel.f) ---------------------------- */
+typedef struct {
+    int imsize;          /* Imsize (square)                         */
+    float cellsize;      /* arcsec                                  */
+    float fov;           /* FOV for weighting (0 = natural)          */
+    int rmode;           /* 0 NONE(uniform) 1 NORM 2 ABS 3 AZ-NORM  */
+    float robust[3];
+    float ds;
+    double vra, vdec;    /* visibility phase centre (deg)           */
+    float shift_ra, shift_dec; /* image shift (arcsec), task/uvmap.f Shift */
+} orc_uvmap_params;
+
+/* Image/grid geometry of IMGMAKE + FFTCONJA (img/imgmake.f, fft/fftconja.f, fft/fftconj.f). */
+typedef struct {
+    int nx, ny, fnu, nu, nv;
+    float uscale, vscale;       /* 1/CDELT of the XFR axes                 */
+    int uorigin, vorigin;
+    float cenx, ceny;           /* image reference pixel (N+1)/2            */
+    double shift[9];
+} orc_geom;
+void orc_make_geom(const orc_uvmap_params *p, orc_geom *g);
+
+/* uvmap: weighting -> PSF -> dirty, both normalised by the PSF peak.  wt is updated
+ * in place to the reweighted values (as the reference does).  Returns an error code. */
+int orc_uvmap(const orc_uvmap_params *p, int nvis, const float *u, const float *v,
+              const float *w, const float *vis, float *wt, float *dirty, float *psf,
+              float *maxpsf, float *sumwt_psf);
+/* vismodel: grid-correct -> r2c FFT -> degrid (task/vismodel.f:70-74). */
+int orc_vismodel(const orc_uvmap_params *p, int nvis, const float *u, const float *v,
+                 const float *w, float *vis, float *wt, const float *image);
+
+/* ---- FP64 oracle: same algorithms in double, plus a direct DFT --------------------- */
+int  orc64_grdh2d(const float *vis, const float *wt, const float *u, const float *v,
+                  const float *w, int nvis, const orc_geom *g, int psf, double *gvis);
+void orc64_fftr2d_inv(const double *xarray, double *image, int nx, int ny, int fnu, int nv);
+void orc64_uvmap_image(const orc_geom *g, int nvis, const float *u, const float *v,
+                       const float *w, const float *vis, const float *wt, int psf,
+                       double *image);
+void orc64_dft_image(const orc_geom *g, int nvis, const float *u, const float *v,
+                     const float *vis, const float *wt, int psf, double *image);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
