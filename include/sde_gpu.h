@@ -1,0 +1,213 @@
+/*
+ * sde_gpu.h -- C ABI of libsdegpu, the GB300 (sm_103a) implementation of SDE's imaging
+ * hot path: uniform/robust weight-density counts, convolutional gridding with the
+ * 128x-oversampled prolate-spheroidal kernel, the half-plane 2-D FFT with grid
+ * correction, degridding, and the Hogbom CLEAN minor cycle.
+ *
+ * Two layers:
+ *
+ *  1. Drop-in entry points with the reference's Fortran-77 calling convention (every
+ *     argument by reference, column-major arrays, hidden trailing CHARACTER lengths).
+ *     Each replaces one pixel-level routine of timcornwell/sde, cited beside it; they
+ *     take HOST arrays, run on the GPU and write the results back in place, honouring
+ *     the reference's global ERROR flag (COMMON /SYSI/, include/stdinc.h:66): they return
+ *     at once when ERROR is set and set it (through errrepor_) on failure.
+ *
+ *  2. A handle API (sde_*) that keeps visibilities, grids and images resident in HBM
+ *     and runs asynchronously on the context's stream; this is what the batched and
+ *     served paths, the Python host layer and the benchmark use.
+ *
+ * All functions return SDE_OK (0) or an SDE_E* code; sde_last_error() gives the text.
+ * Nothing here falls back to the CPU: without a usable GPU every call fails with
+ * SDE_ENODEV.
+ */
+#ifndef SDE_GPU_H
+#define SDE_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define SDE_OK 0
+#define SDE_EINVAL 1      /* bad argument (size, mode, pointer)                        */
+#define SDE_ENOMEM 2      /* device allocation failed / admission refused                */
+#define SDE_ECUDA 3       /* CUDA runtime error                                          */
+#define SDE_ENOWEIGHT 4   /* gridder found no weight (grd/grdh2d.f:195-197 'No weight!') */
+#define SDE_ETIMEDOUT 5   /* a bounded device wait gave up                                */
+#define SDE_EBADMODE 6    /* unrecognised RMODE (grd/grdruw2d.f:361)                      */
+#define SDE_ENODEV 7      /* no CUDA device                                               */
+#define SDE_ECANCELLED 8  /* stopped by the interrupt flag (SYSINTRP analogue)            */
+
+const char *sde_last_error(void);
+int sde_version(void);
+
+/* ======================================================================================
+ * Layer 1: Fortran-77 drop-in entry points (gfortran symbol names).
+ * ====================================================================================== */
+
+/* Replaces GRDH2D (source/grd/grdh2d.f:7-9), called by VISGRID (vis/visgrid.f:329). */
+void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+             float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
+             float *gvis, int *psf, int *nu, int *nv, float *gridfnu, int *suppu, int *osampu,
+             float *gridfnv, int *suppv, int *osampv, double *shift, float *sumwt);
+
+/* Replaces GRDDEH2D (source/grd/grddeh2d.f:7-9), called by VISDEGRI (vis/visdegri.f:81). */
+void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+               float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
+               float *gvis, int *nu, int *nv, float *intfnu, int *suppu, int *osampu,
+               float *intfnv, int *suppv, int *osampv, double *shift);
+
+/* Replaces GRDUWT2D (source/grd/grduwt2d.f:7-8), called by GRDUWT (grd/grduwt.f:122). */
+void grduwt2d_(float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+               float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
+               float *newwt, float *gwt, int *nu, int *nv, double *shift);
+
+/* Replaces GRDRUW2D (source/grd/grdruw2d.f:177-179), called by GRDRUWT (grd/grdruwt.f:346). */
+void grdruw2d_(float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+               float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
+               float *newwt, float *gwt, int *nu, int *nv, double *shift, char *rmode,
+               float *robust, float *ds, size_t rmode_len);
+
+/* Replaces FFTR2D (source/fft/fftr2d.f:7-8), called by ARRFFTR (arr/arrfftr.f:139).
+ * WORK, WORK2 and RWORK are accepted for signature compatibility and not touched. */
+void fftr2d_(float *rarray, float *xarray, float *work, float *work2, float *rwork, int *nx,
+             int *ny, int *fnu, int *nv, int *dir);
+
+/* Replaces PIXCOR2D (source/pix/pixcor2d.f:7-8), called by IMGGRIDC (img/imggridc.f:384). */
+void pixcor2d_(float *in, int *nx, int *ny, float *cf, int *cflen, char *mode, float *out,
+               float *cenx, float *ceny, size_t mode_len);
+
+/* Replaces PIX2DRCL (source/pix/pix2drcl.f:78-80), called by IMGCLEAN (img/imgclean.f:186). */
+void pix2drcl_(float *drt, float *psf, float *box, int *nx, int *ny, int *pnx, int *pny,
+               float *gain, int *nsub, int *bsub, float *flux, float *cln, float *res,
+               int *ansub, float *maxres, float *tflux, float *cflux, int *cx, int *cy);
+
+/* Replaces PIXISAMA (source/pix/pixisama.f:231), called by PIX2DRCL (pix/pix2drcl.f:146). */
+int pixisama_(int *n, float *a, int *i);
+
+/* The reference's error channel: COMMON /SYSI/ (include/stdinc.h:64-66).  libsdegpu
+ * defines it; a Fortran program's own definition interposes at link time.  errrepor_ and
+ * msgput_ are weak defaults (main/err.f:532, main/msg.f:7) that a host program overrides. */
+typedef struct {
+    int error, msgwidth, sysdebug, sysmon, sysintrp, sysmsg, syspar;
+} sde_sysi_common;
+extern sde_sysi_common sysi_;
+void errrepor_(const char *reason, const char *routine, const char *text, size_t lreason,
+               size_t lroutine, size_t ltext);
+void msgput_(const char *msg, const char *type, size_t lmsg, size_t ltype);
+
+/* ======================================================================================
+ * Layer 2: resident handle API.
+ * ====================================================================================== */
+typedef struct sde_ctx sde_ctx;     /* one device + one stream + scratch pools          */
+typedef struct sde_plan sde_plan;   /* a tile-sorted, device-resident visibility set     */
+
+int sde_ctx_create(sde_ctx **out, int device);
+int sde_ctx_destroy(sde_ctx *ctx);
+int sde_ctx_sync(sde_ctx *ctx);
+void *sde_ctx_stream(sde_ctx *ctx);            /* the cudaStream_t all calls run on       */
+int sde_ctx_set_stream(sde_ctx *ctx, void *stream); /* run on a caller's stream instead   */
+/* Device memory owned by the context's pools (bytes), for admission control. */
+int64_t sde_ctx_bytes_in_use(sde_ctx *ctx);
+
+/* Geometry of one gridding/degridding job (the scalar arguments of GRDH2D/GRDDEH2D). */
+typedef struct {
+    int nu, nv;                 /* half-plane grid: NU = FNU/2+1 columns, NV rows        */
+    float uscale, uoffset, vscale, voffset;
+    int uorigin, vorigin;
+    int supp, osamp;            /* 3, 128 for the 'SF' kernel                           */
+    double shift[9];            /* SHIFT(3,3) column-major (crd/crdshift.f)              */
+} sde_gridspec;
+
+/* Weighting (GRDUWT2D / GRDRUW2D).  rmode: 0 uniform (GRDUWT2D), 1 NORM, 2 ABS,
+ * 3 AZ-NORM, 4 NONE (GRDRUW2D).  Pointers are device pointers (async on the stream).
+ * newwt may alias wt.  gwt (nu*nv floats, [nv][nu]) may be NULL.  stats may be NULL;
+ * when given, the call synchronises and fills it. */
+typedef struct {
+    int64_t ndrop;              /* points dropped off the reweighting grid                */
+    double sumwt, sumlocwt;     /* GRDRUW2D's SUMWT and SUMLOCWT                          */
+    float f2, d2;               /* robust parameters actually used                        */
+} sde_wstats;
+int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const float *wt,
+                const float *u, const float *v, const float *w, int64_t nvis, float uscale,
+                float uoffset, float vscale, float voffset, int uorigin, int vorigin,
+                int nu, int nv, const double shift[9], float *newwt, float *gwt,
+                sde_wstats *stats);
+
+/* Plans.  where: SDE_HOST or SDE_DEVICE for the input arrays (vis is complex64 pairs).
+ * The plan copies what it needs; inputs may be freed afterwards.  Visibilities with
+ * WT <= 0 or outside the gridding bounds are excluded from gridding exactly as GRDH2D
+ * excludes them. */
+#define SDE_HOST 0
+#define SDE_DEVICE 1
+int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const float *u,
+                    const float *v, const float *w, const float *vis, const float *wt,
+                    int where, sde_plan **out);
+int sde_plan_destroy(sde_plan *plan);
+int64_t sde_plan_nvis(const sde_plan *plan);       /* visibilities that grid              */
+int64_t sde_plan_bytes(const sde_plan *plan);
+/* Replace the plan's visibilities (same order/length as at creation). */
+int sde_plan_set_vis(sde_plan *plan, const float *vis, int where);
+
+/* Grid the plan's residual visibilities (or the PSF) onto a device grid in the final
+ * GRDH2D layout: [nv][pitch] complex64, pitch >= nu (use sde_grid_pitch), already
+ * symmetrised, shifted by SUPPU and normalised by (NU-1)*NV/sum(UVWT).  sumwt (host,
+ * may be NULL) receives GRDH2D's SUMWT; passing it synchronises the stream. */
+#define SDE_GRID_VIS 0
+#define SDE_GRID_PSF 1
+int sde_grid_pitch(int nu);
+int sde_plan_grid(sde_plan *plan, int what, float *grid, int pitch, float *sumwt);
+
+/* Degrid a device grid ([nv][pitch] complex64, GRDDEH2D layout) at the plan's
+ * visibilities and update the residual: residual = observed - model.  Asynchronous. */
+int sde_plan_degrid_residual(sde_plan *plan, const float *grid, int pitch);
+/* Reset the residual to the observed visibilities. */
+int sde_plan_reset_residual(sde_plan *plan);
+/* Degrid a device grid into user-ordered visibilities exactly as GRDDEH2D does
+ * (normalised interpolation, reflection, conjugation, phase rotation, WT sign flags).
+ * vis_out/wt_out are device or host pointers per `where` (length = nvis at creation);
+ * entries GRDDEH2D would not touch are left unchanged. */
+int sde_plan_degrid(sde_plan *plan, const float *grid, int pitch, float *vis_out,
+                    float *wt_out, int where, int64_t *nbad);
+/* Copy the residual visibilities back in the caller's original order (complex64). */
+int sde_plan_get_residual(sde_plan *plan, float *vis_out, int where);
+
+/* 2-D transforms (FFTR2D conventions) on device arrays, with the grid correction
+ * (PIXCOR2D 'CORRECT' by the GRDCCF 'SF' table) fused.
+ *   grid -> image: column c2c along v (FFTX1D, DIR -1), row c2r along u (FFTR1D2), then
+ *     image /= CCF(|x-cx|) CCF(|y-cy|), then image *= *scale_dev when scale_dev != NULL.
+ *   image -> grid: image / CCF, row r2c, column c2c (DIR +1).
+ * grid is [nv][pitch] complex64 (NU = fnu/2+1 columns used); image is [ny][nx] float32.
+ * correct: 1 applies the correction, 0 skips it (plain FFTR2D). */
+int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, int fnu, int nv,
+                        int correct, const float *scale_dev, float *image);
+int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fnu, int nv,
+                        int correct, float *grid, int pitch);
+
+/* max over an image (ARRSTAT ARRMAX) into a device float, and OUT = scale*IN + offset
+ * with scale = 1/(*max_dev) (task/uvmap.f:434-440, 480-482 with pix/pixrscal.f). */
+int sde_image_max(sde_ctx *ctx, const float *image, int64_t n, float *max_dev);
+int sde_image_scale_by_inverse(sde_ctx *ctx, float *image, int64_t n, const float *max_dev);
+
+/* Hogbom CLEAN (PIX2DRCL) on device arrays: drt, box, cln, res [ny][nx]; psf [pny][pnx];
+ * cflux/cx/cy device arrays of |nsub| entries.  One persistent launch runs every
+ * iteration; scalars come back in *out (host) after an internal synchronisation.
+ * cancel_flag (host pinned or NULL) is polled like SYSINTRP (pix/pix2drcl.f:165). */
+typedef struct {
+    int ansub;
+    float maxres, tflux;
+} sde_clean_result;
+int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *box, int nx,
+               int ny, int pnx, int pny, float gain, int nsub, int bsub, float flux,
+               float tflux_in, float *cln, float *res, float *cflux, int *cx, int *cy,
+               volatile int *cancel_flag, sde_clean_result *out);
+
+/* Index (1-based) of the first strictly largest |a| (PIXISAMA) of a device array. */
+int sde_isamax(sde_ctx *ctx, const float *a, int64_t n, int64_t *index_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

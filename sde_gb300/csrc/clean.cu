@@ -1,0 +1,372 @@
+// clean.cu -- Hogbom CLEAN minor cycle (PIX2DRCL), PIXISAMA, and the uvmap PSF-peak
+// normalisation (ARRSTAT max + ARRSCALE by 1/max).
+//
+// PIX2DRCL (pix/pix2drcl.f:138-203): RES = DRT*BOX; per iteration the first index of the
+// strictly largest |RES| (PIXISAMA, pix/pixisama.f:269-277), stop tests, component record,
+// then RES -= (PNTSUB*PSF(OFFX-IX,OFFY-IY))*BOX over the whole window in FP32.  Here one
+// cooperative persistent launch runs every iteration: each CTA owns a contiguous slice of
+// the window, applies the previous component's subtraction to it with the same FP32
+// operations (no FMA), finds its slice's first maximum, and a grid barrier (bounded spin)
+// publishes the partial maxima; every CTA then reduces the same partials to the same
+// global (max, first index), so component positions are identical to the reference's.
+#include <cooperative_groups.h>
+#include <math.h>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int CL_THREADS = 512;
+constexpr unsigned SPIN_LIMIT = 1u << 26;
+
+struct Cand {
+    float a;      // |value|
+    int32_t idx;  // flat 0-based index, INT32_MAX if none
+    float v;      // signed value
+};
+
+__device__ __forceinline__ Cand better(Cand x, Cand y) {
+    // larger |a| wins; ties go to the smaller index (first occurrence)
+    if (y.a > x.a || (y.a == x.a && y.idx < x.idx)) return y;
+    return x;
+}
+
+__device__ Cand block_best(Cand c) {
+    __shared__ Cand sh[32];
+    for (int d = 16; d > 0; d >>= 1) {
+        Cand o;
+        o.a = __shfl_down_sync(0xffffffffu, c.a, d);
+        o.idx = __shfl_down_sync(0xffffffffu, c.idx, d);
+        o.v = __shfl_down_sync(0xffffffffu, c.v, d);
+        c = better(c, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = c;
+    __syncthreads();
+    if (warp == 0) {
+        c = lane < (int)(blockDim.x >> 5) ? sh[lane] : Cand{-1.0f, INT32_MAX, 0.0f};
+        for (int d = 16; d > 0; d >>= 1) {
+            Cand o;
+            o.a = __shfl_down_sync(0xffffffffu, c.a, d);
+            o.idx = __shfl_down_sync(0xffffffffu, c.idx, d);
+            o.v = __shfl_down_sync(0xffffffffu, c.v, d);
+            c = better(c, o);
+        }
+        if (lane == 0) sh[0] = c;
+    }
+    __syncthreads();
+    Cand r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+struct Barrier {
+    unsigned count;
+    unsigned gen;
+    int stopreq[2];  // cancel requests published by CTA 0 before each barrier
+};
+
+// Grid-wide barrier; gives up after SPIN_LIMIT polls and reports through *timeout.
+__device__ bool grid_sync(Barrier *b, unsigned nblocks, int *timeout) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned *vgen = &b->gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&b->count, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (*vgen == g) {
+                if (++spins > SPIN_LIMIT) {
+                    atomicExch(timeout, 1);
+                    ok = 0;
+                    break;
+                }
+                if (*(volatile int *)timeout) {
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+struct CleanArgs {
+    const float *drt, *psf, *box;
+    float *cln, *res, *cflux;
+    int *cx, *cy;
+    int nx, ny, pnx, pny, pmpx, pmpy;
+    float gain, flux, tflux_in;
+    int nsub, bsub;
+    volatile int *cancel;
+    Cand *partial;   // [2][gridDim]
+    Barrier *bar;
+    int *status;     // [STATUS_TIMEOUT]
+    float *out;      // [0] maxres [1] tflux [2] ansub (as int bits)
+};
+
+__global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
+    const int64_t npix = (int64_t)A.nx * A.ny;
+    const int64_t per = (npix + gridDim.x - 1) / gridDim.x;
+    const int64_t lo = per * blockIdx.x;
+    const int64_t hi = lo + per < npix ? lo + per : npix;
+    const int64_t pnpix = (int64_t)A.pnx * A.pny;
+    __shared__ int stop_sh;
+    // RES = DRT * BOX, and the first maximum of the slice
+    Cand c{-1.0f, INT32_MAX, 0.0f};
+    for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+        float r = A.box ? __fmul_rn(A.drt[k], A.box[k]) : __fmul_rn(A.drt[k], 1.0f);
+        A.res[k] = r;
+        c = better(c, Cand{fabsf(r), (int32_t)k, r});
+    }
+    c = block_best(c);
+    if (threadIdx.x == 0) A.partial[blockIdx.x] = c;
+    if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->stopreq[0] = (A.cancel && *A.cancel) ? 1 : 0;
+    if (!grid_sync(A.bar, gridDim.x, &A.status[STATUS_TIMEOUT])) return;
+    int cur = 0;
+    float tflux = A.tflux_in;
+    const int nabs = A.nsub < 0 ? -A.nsub : A.nsub;
+    int isub;
+    int stopped = 0;
+    float maxres = 0.0f;
+    for (isub = A.bsub; isub <= nabs; isub++) {
+        // global first maximum from the partials of every CTA
+        Cand g{-1.0f, INT32_MAX, 0.0f};
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            g = better(g, A.partial[cur * gridDim.x + b]);
+        g = block_best(g);
+        // PIXISAMA returns 1 (index 0) when no |value| exceeds 0
+        // every |value| >= 0 beats the -1 sentinel, so when nothing exceeds 0 the winner
+        // is index 0 -- PIXISAMA's default of 1 (pix/pixisama.f:269)
+        const int32_t ip = g.idx;
+        const int pmx = 1 + ip % A.nx, pmy = 1 + ip / A.nx;
+        maxres = g.v;
+        if (threadIdx.x == 0) {
+            int s = 0;
+            if (A.nsub < 0 && maxres < 0.0f) s = 1;
+            if (fabsf(maxres) <= A.flux) s = 1;
+            if (((volatile int *)A.bar->stopreq)[cur]) s = 2;
+            stop_sh = s;
+        }
+        __syncthreads();
+        if (stop_sh) {
+            stopped = stop_sh;
+            break;
+        }
+        const float pntsub = __fmul_rn(A.gain, maxres);
+        tflux = __fadd_rn(tflux, pntsub);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            const int64_t ci = (int64_t)(pmy - 1) * A.nx + (pmx - 1);
+            A.cln[ci] = __fadd_rn(A.cln[ci], pntsub);
+            A.cflux[isub - 1] = pntsub;
+            A.cx[isub - 1] = pmx;
+            A.cy[isub - 1] = pmy;
+        }
+        const int offx = A.pmpx + pmx, offy = A.pmpy + pmy;
+        Cand lc{-1.0f, INT32_MAX, 0.0f};
+        for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+            const int iy = (int)(k / A.nx) + 1, ix = (int)(k - (int64_t)(iy - 1) * A.nx) + 1;
+            const int64_t flat = (int64_t)(offx - ix - 1) + (int64_t)(offy - iy - 1) * A.pnx;
+            const float p = (flat >= 0 && flat < pnpix) ? A.psf[flat] : 0.0f;
+            const float bx = A.box ? A.box[k] : 1.0f;
+            const float r = __fsub_rn(A.res[k], __fmul_rn(__fmul_rn(pntsub, p), bx));
+            A.res[k] = r;
+            lc = better(lc, Cand{fabsf(r), (int32_t)k, r});
+        }
+        lc = block_best(lc);
+        cur ^= 1;
+        if (threadIdx.x == 0) A.partial[cur * gridDim.x + blockIdx.x] = lc;
+        if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->stopreq[cur] = (A.cancel && *A.cancel) ? 1 : 0;
+        if (!grid_sync(A.bar, gridDim.x, &A.status[STATUS_TIMEOUT])) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int ansub;
+        if (!stopped) {
+            ansub = A.nsub;
+        } else {
+            ansub = isub - 1;
+        }
+        A.out[1] = tflux;
+        A.out[2] = __int_as_float(ansub);
+        A.out[3] = __int_as_float(stopped);
+        if (stopped) A.out[0] = maxres;
+    }
+    if (!stopped) {
+        // final PIXISAMA over the residual (pix/pix2drcl.f:206-209)
+        Cand g{-1.0f, INT32_MAX, 0.0f};
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            g = better(g, A.partial[cur * gridDim.x + b]);
+        g = block_best(g);
+        if (blockIdx.x == 0 && threadIdx.x == 0) A.out[0] = g.v;
+    }
+}
+
+// first strictly-largest |a| (PIXISAMA), two-level
+__global__ void __launch_bounds__(CL_THREADS) k_isamax_part(const float *a, int64_t n, Cand *part) {
+    Cand c{-1.0f, INT32_MAX, 0.0f};
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        c = better(c, Cand{fabsf(a[k]), (int32_t)k, a[k]});
+    c = block_best(c);
+    if (threadIdx.x == 0) part[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(CL_THREADS) k_isamax_final(const Cand *part, int nb, int64_t *out) {
+    Cand c{-1.0f, INT32_MAX, 0.0f};
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) c = better(c, part[b]);
+    c = block_best(c);
+    // 1-based index of the first largest |a|, or 0 when no |a| exceeds 0
+    if (threadIdx.x == 0) *out = c.a > 0.0f ? (int64_t)c.idx + 1 : 0;
+}
+
+// max value (ARRSTAT's ARRMAX) over an image
+__global__ void __launch_bounds__(CL_THREADS) k_max_part(const float *a, int64_t n, float *part) {
+    __shared__ float sh[32];
+    float m = -INFINITY;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, a[k]);
+    for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, d));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : -INFINITY;
+        for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, d));
+        if (threadIdx.x == 0) part[blockIdx.x] = m;
+    }
+}
+
+__global__ void k_max_final(const float *part, int nb, float *out) {
+    float m = -INFINITY;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) m = fmaxf(m, part[b]);
+    for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, d));
+    if (threadIdx.x == 0) *out = m;
+}
+
+// OUT = (1/max) * IN + 0.0 (task/uvmap.f:440 with pix/pixrscal.f)
+__global__ void k_scale_inv(float *a, int64_t n, const float *maxp) {
+    const float s = 1.0f / *maxp;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        a[k] = __fadd_rn(__fmul_rn(s, a[k]), 0.0f);
+}
+
+}  // namespace
+
+int sde_isamax(sde_ctx *ctx, const float *a, int64_t n, int64_t *index_out) {
+    SDE_TRY(sde_isamax0(ctx, a, n, index_out));
+    if (*index_out == 0) *index_out = 1;  // PIXISAMA's default I = 1
+    return SDE_OK;
+}
+
+int sde_isamax0(sde_ctx *ctx, const float *a, int64_t n, int64_t *index_out) {
+    if (!ctx || !a || n <= 0 || !index_out || n > INT32_MAX) return SDE_EINVAL;
+    SDE_CUDA_TRY(cudaSetDevice(ctx->device));
+    int nb = ctx->num_sms * 2;
+    Cand *part;
+    int64_t *d;
+    SDE_TRY(ctx_scratch(ctx, "isa_part", sizeof(Cand) * (size_t)nb, (void **)&part));
+    SDE_TRY(ctx_scratch(ctx, "isa_out", sizeof(int64_t), (void **)&d));
+    k_isamax_part<<<nb, CL_THREADS, 0, ctx->stream>>>(a, n, part);
+    SDE_CHECK_LAUNCH();
+    k_isamax_final<<<1, CL_THREADS, 0, ctx->stream>>>(part, nb, d);
+    SDE_CHECK_LAUNCH();
+    SDE_CUDA_TRY(cudaMemcpyAsync(index_out, d, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    SDE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SDE_OK;
+}
+
+int sde_image_max(sde_ctx *ctx, const float *image, int64_t n, float *max_dev) {
+    if (!ctx || !image || n <= 0 || !max_dev) return SDE_EINVAL;
+    int nb = ctx->num_sms * 2;
+    float *part;
+    SDE_TRY(ctx_scratch(ctx, "max_part", sizeof(float) * (size_t)nb, (void **)&part));
+    k_max_part<<<nb, CL_THREADS, 0, ctx->stream>>>(image, n, part);
+    SDE_CHECK_LAUNCH();
+    k_max_final<<<1, 32, 0, ctx->stream>>>(part, nb, max_dev);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+int sde_image_scale_by_inverse(sde_ctx *ctx, float *image, int64_t n, const float *max_dev) {
+    if (!ctx || !image || n <= 0 || !max_dev) return SDE_EINVAL;
+    k_scale_inv<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(image, n, max_dev);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *box, int nx, int ny,
+               int pnx, int pny, float gain, int nsub, int bsub, float flux, float tflux_in,
+               float *cln, float *res, float *cflux, int *cx, int *cy, volatile int *cancel_flag,
+               sde_clean_result *out) {
+    if (!ctx || !drt || !psf || !cln || !res || nx < 1 || ny < 1 || pnx < 1 || pny < 1 || !out ||
+        (int64_t)nx * ny > INT32_MAX || bsub < 1) {
+        sde_set_error("sde_hogbom: bad arguments");
+        return SDE_EINVAL;
+    }
+    const int nabs = nsub < 0 ? -nsub : nsub;
+    if (nabs >= bsub && (!cflux || !cx || !cy)) {
+        sde_set_error("sde_hogbom: component arrays required");
+        return SDE_EINVAL;
+    }
+    SDE_CUDA_TRY(cudaSetDevice(ctx->device));
+    // PSF peak (pix/pix2drcl.f:146-151)
+    int64_t ip1;
+    SDE_TRY(sde_isamax(ctx, psf, (int64_t)pnx * pny, &ip1));
+    int ipeak = (int)(ip1 - 1);
+    int pmpx = 1 + ipeak % pnx;
+    int pmpy = 1 + (ipeak - pmpx + 1) / pnx;
+    if (pmpx >= pnx) pmpx = pnx / 2;
+    if (pmpy >= pny) pmpy = pny / 2;
+    int per_sm = 0;
+    SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom, CL_THREADS, 0));
+    if (per_sm < 1) {
+        sde_set_error("sde_hogbom: kernel cannot be resident");
+        return SDE_ECUDA;
+    }
+    int64_t npix = (int64_t)nx * ny;
+    int nblocks = ctx->num_sms * (per_sm > 2 ? 2 : per_sm);
+    int64_t want = (npix + 4 * CL_THREADS - 1) / (4 * CL_THREADS);  // small windows: fewer CTAs
+    if (want < nblocks) nblocks = (int)(want < 1 ? 1 : want);
+    Cand *partial;
+    Barrier *bar;
+    float *dout;
+    SDE_TRY(ctx_scratch(ctx, "cl_partial", sizeof(Cand) * 2 * (size_t)nblocks, (void **)&partial));
+    SDE_TRY(ctx_scratch(ctx, "cl_bar", sizeof(Barrier), (void **)&bar));
+    SDE_TRY(ctx_scratch(ctx, "cl_out", 4 * sizeof(float), (void **)&dout));
+    SDE_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(Barrier), ctx->stream));
+    SDE_CUDA_TRY(cudaMemsetAsync(ctx->d_status, 0, sizeof(int) * STATUS_COUNT, ctx->stream));
+    CleanArgs A;
+    A.drt = drt; A.psf = psf; A.box = box; A.cln = cln; A.res = res; A.cflux = cflux;
+    A.cx = cx; A.cy = cy; A.nx = nx; A.ny = ny; A.pnx = pnx; A.pny = pny;
+    A.pmpx = pmpx; A.pmpy = pmpy; A.gain = gain; A.flux = flux; A.tflux_in = tflux_in;
+    A.nsub = nsub; A.bsub = bsub; A.cancel = cancel_flag; A.partial = partial; A.bar = bar;
+    A.status = ctx->d_status; A.out = dout;
+    void *args[] = {&A};
+    SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom, dim3(nblocks), dim3(CL_THREADS),
+                                             args, 0, ctx->stream));
+    float h[4];
+    SDE_CUDA_TRY(cudaMemcpyAsync(h, dout, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    SDE_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(int) * STATUS_COUNT,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    SDE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_status[STATUS_TIMEOUT]) {
+        sde_set_error("sde_hogbom: grid barrier timed out");
+        return SDE_ETIMEDOUT;
+    }
+    int ansub, stopped;
+    memcpy(&ansub, &h[2], 4);
+    memcpy(&stopped, &h[3], 4);
+    out->maxres = h[0];
+    out->tflux = h[1];
+    out->ansub = ansub;
+    if (stopped == 2) return SDE_ECANCELLED;
+    return SDE_OK;
+}

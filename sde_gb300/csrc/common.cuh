@@ -1,0 +1,187 @@
+// common.cuh -- internal declarations shared by the libsdegpu translation units.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/sde_gpu.h"
+
+// ---------------------------------------------------------------------------------------
+// Error handling: every entry point records a message and returns an SDE_E* code.
+void sde_set_error(const char *fmt, ...);
+#define SDE_CUDA_TRY(call)                                                                  \
+    do {                                                                                    \
+        cudaError_t _e = (call);                                                            \
+        if (_e != cudaSuccess) {                                                            \
+            sde_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(_e)); \
+            return _e == cudaErrorMemoryAllocation ? SDE_ENOMEM                             \
+                   : (_e == cudaErrorNoDevice || _e == cudaErrorInsufficientDriver)          \
+                       ? SDE_ENODEV                                                         \
+                       : SDE_ECUDA;                                                         \
+        }                                                                                   \
+    } while (0)
+#define SDE_TRY(call)              \
+    do {                           \
+        int _rc = (call);          \
+        if (_rc != SDE_OK) return _rc; \
+    } while (0)
+#define SDE_CHECK_LAUNCH() SDE_CUDA_TRY(cudaGetLastError())
+
+// ---------------------------------------------------------------------------------------
+// Geometry constants of the tiled gridder.  Tiles are TILE x TILE cells of the gridding
+// frame (GRDH2D's grid before the SUPPU shift); the shared-memory copy of a tile has a
+// halo of HALO = SUPP cells on every side.  A work item is a contiguous range of at most
+// ITEM_MAX sorted visibilities inside one tile; a chunk is at most CHUNK_MAX visibilities
+// of one cell, accumulated in registers by one thread.
+constexpr int TILE = 64;
+constexpr int TILE_LOG2 = 6;
+constexpr int SUPP = 3;                 // 'SF' support (grd/grdcf.f:258)
+constexpr int OSAMP = 128;              // oversampling (grd/grdcf.f:245)
+constexpr int NTAP = 2 * SUPP + 1;      // 7
+constexpr int STILE = TILE + 2 * SUPP;  // 70: shared tile edge (grid and degrid)
+constexpr int CFLEN = 1 + 8 * 129;      // vis/visgrid.f:274
+constexpr int ITEM_MAX = 8192;
+constexpr int CHUNK_MAX = 16;
+constexpr uint32_t KEY_INVALID = 0xFFFFFFFFu;
+
+// per-visibility packed sub-cell offsets: byte0 du_g+64, byte1 dv_g+64 (gridding, FP64
+// cell), byte2 du_d+64, byte3 dv_d+64 (degridding, FP32 cell).  0xFF in byte2 marks a
+// visibility that the degridder handles on its exception path.
+__host__ __device__ inline uint32_t pack_gd(int dug, int dvg, int dud, int dvd) {
+    return (uint32_t)(dug + 64) | ((uint32_t)(dvg + 64) << 8) | ((uint32_t)(dud + 64) << 16) |
+           ((uint32_t)(dvd + 64) << 24);
+}
+constexpr uint32_t GD_EXCEPTION = 0xFFu << 16;
+
+// Exception entries for the degridder: visibilities whose FP32 degridding cell differs
+// from their FP64 gridding cell, that sit within SUPP of the v axis (reflection branch of
+// grd/grddeh2d.f:123-158), whose conjugation flags differ, or that only degrid.
+struct DegridExc {
+    uint32_t orig;     // index in the caller's order
+    int32_t pos;       // sorted position in the plan, -1 if the visibility does not grid
+    int32_t nuc, nvc;  // NINT(UCELL), NINT(VCELL) in GRDDEH2D's FP32 frame
+    int16_t delui, delvi;
+    uint8_t conj;      // USCALE*ULOCAL > 0 (grd/grddeh2d.f:189)
+    uint8_t valid;     // passed GRDDEH2D's bounds (grd/grddeh2d.f:112-114)
+    uint8_t gconj;     // gridding-frame conjugation of this visibility (if pos >= 0)
+    uint8_t pad;
+};
+
+// The exception list is one allocation: entries, then their weights, then their
+// rotations, each section starting on a 16-byte boundary.
+inline size_t exc_wt_off(size_t ne) { return (sizeof(DegridExc) * ne + 15) & ~(size_t)15; }
+inline size_t exc_rot_off(size_t ne) { return (exc_wt_off(ne) + 4 * ne + 15) & ~(size_t)15; }
+inline size_t exc_bytes(size_t ne) { return exc_rot_off(ne) + 8 * ne; }
+
+struct WorkItem {
+    int32_t tile;      // tile id = tv * ntu + tu
+    int32_t cbeg, cend;  // chunk range
+    int32_t vbeg, vend;  // sorted visibility range
+};
+
+// ---------------------------------------------------------------------------------------
+// Context: one device, one stream, grow-only scratch buffers, cached tables.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct sde_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+    int64_t bytes = 0;                     // device bytes owned (buffers + plans)
+    float *d_cf = nullptr;                 // 'SF' gridding function, CFLEN floats
+    float *d_cft = nullptr;                // transposed table [129][8]
+    int *d_status = nullptr;               // device status words (see STATUS_*)
+    int *h_status = nullptr;               // pinned mirror
+    std::unordered_map<std::string, DevBuf> scratch;
+    std::unordered_map<int, float2 *> twiddles;  // N -> exp(+-2 pi i k/N) table
+    CUtensorMap *h_tmap = nullptr;
+};
+
+enum { STATUS_ERR = 0, STATUS_NOWEIGHT = 1, STATUS_TIMEOUT = 2, STATUS_COUNT = 8 };
+
+// scratch buffer by name, grown on demand (contents undefined)
+int ctx_scratch(sde_ctx *ctx, const char *name, size_t bytes, void **out);
+int ctx_alloc(sde_ctx *ctx, void **p, size_t bytes);
+void ctx_free(sde_ctx *ctx, void *p, size_t bytes);
+int ctx_twiddles(sde_ctx *ctx, int n, const float2 **out);
+
+struct sde_plan {
+    sde_ctx *ctx = nullptr;
+    sde_gridspec spec;
+    int doshift = 0;
+    int pitch = 0;            // row pitch (complex elements) of grids the plan writes
+    int ntu = 0, ntv = 0;     // tiles across / down
+    int64_t nvis_in = 0;      // caller's count
+    int64_t nvis = 0;         // gridding visibilities
+    int64_t nitems = 0, nchunks = 0, nexc = 0;
+    // sorted, gridding-valid visibilities
+    float2 *fobs = nullptr;   // observed, in the gridding frame (rotated, conjugated)
+    float2 *fres = nullptr;   // residual, gridding frame
+    float *wt = nullptr;
+    uint32_t *gd = nullptr;   // packed sub-cell offsets
+    uint32_t *orig = nullptr; // caller index of each sorted visibility
+    float2 *rot = nullptr;    // (cos, sin) of the phase rotation (doshift only), sorted
+    uint8_t *gconj = nullptr; // gridding-frame conjugation flag, sorted
+    uint2 *chunks = nullptr;  // {first vis, cell | len << 16}
+    WorkItem *items = nullptr;
+    DegridExc *exc = nullptr; // exception list (includes degrid-only visibilities)
+    float *wt_all = nullptr;  // caller-order weights (for user-frame degridding)
+    float *cf = nullptr;      // gridding function used by this plan (device, CFLEN)
+    float *cft = nullptr;     // transposed table
+    double *d_sums = nullptr; // [0] sum of UVWT (LSUMWT), [1] SUMWT
+    double h_lsumwt = 0.0, h_sumwt = 0.0;
+    bool sums_ready = false;
+    int64_t bytes = 0;
+};
+
+// grid.cu internals used by api.cu
+int plan_build_cft(sde_plan *pl);
+int ctx_build_cft(sde_ctx *ctx);
+int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt);
+int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, float2 *out, int nu, int nv, int pitch,
+                        int uorigin, int vorigin, int supp, float scale);
+int plan_grid_raw(sde_plan *pl, int what, float2 *raw);
+int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vis_out,
+                float *wt_out, unsigned long long *nbad_dev);
+int plan_scatter_residual(sde_plan *pl, float2 *dst);
+int plan_set_vis_dev(sde_plan *pl, const float2 *vis_user);
+int sde_isamax0(sde_ctx *ctx, const float *a, int64_t n, int64_t *index_out);
+
+// ---------------------------------------------------------------------------------------
+// Kernels shared across translation units (host-side launchers).
+int launch_radix_sort_u32(sde_ctx *ctx, uint32_t *keys, uint32_t *vals, int64_t n, int bits,
+                          uint32_t *keys_tmp, uint32_t *vals_tmp);
+int launch_radix_sort_u64(sde_ctx *ctx, uint64_t *keys, uint32_t *vals, int64_t n, int bits,
+                          uint64_t *keys_tmp, uint32_t *vals_tmp);
+int launch_exclusive_scan_u32(sde_ctx *ctx, const uint32_t *in, uint32_t *out, int64_t n,
+                              uint32_t *total_dev);
+int launch_inclusive_max_scan_i32(sde_ctx *ctx, const int32_t *in, int32_t *out, int64_t n);
+
+
+// host restatement of the 'SF' tables (grd/grdcf.f, grd/grdsf.f, grd/grdccf.f)
+double sf_grdsf(double nu);
+void sf_cf_table(float *cf);
+void sf_ccf_table(float *ccf, int ccflen);
+int fftpwr2(int i);
+
+// ---------------------------------------------------------------------------------------
+// Device helpers.
+__device__ __forceinline__ int nint_f(float x) { return (int)roundf(x); }   // half away
+__device__ __forceinline__ int nint_d(double x) { return (int)round(x); }
+
+__device__ __forceinline__ void red_add_f2(float2 *addr, float2 v) {
+    asm volatile("red.relaxed.gpu.global.add.v2.f32 [%0], {%1, %2};" ::"l"(addr), "f"(v.x),
+                 "f"(v.y)
+                 : "memory");
+}
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }

@@ -1,0 +1,615 @@
+// grid.cu -- tiled gridding (GRDH2D) and degridding (GRDDEH2D) over a sde_plan.
+//
+// Gridding: one CTA per work item keeps the item's 64x64-cell tile plus a 3-cell halo in
+// shared memory.  Each thread owns a chunk (<= CHUNK_MAX visibilities of one cell) and
+// accumulates the chunk's full 7x7 complex footprint in registers, then adds it into the
+// shared tile once; the chunk order (colour class, chunk index, cell) makes the 32 chunks
+// of a warp write disjoint cells.  The shared tile is then reduced into the raw grid in
+// HBM with vector red.global.add (only the cells the item touched).
+//
+// Degridding: one CTA per work item stages the model grid's tile (+halo) into shared
+// memory with a single TMA 2-D bulk copy, then each thread interpolates its chunk's
+// visibilities from a register copy of the chunk cell's 7x7 neighbourhood.
+#include <math.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int GRID_THREADS = 128;
+constexpr int CFT_FLOATS = 129 * 8;
+
+// ---------------------------------------------------------------------------------------
+template <bool PSF>
+__global__ void __launch_bounds__(GRID_THREADS, 3)
+    k_grid(const WorkItem *__restrict__ items, const uint2 *__restrict__ chunks,
+           const float2 *__restrict__ fres, const float *__restrict__ wt,
+           const uint32_t *__restrict__ gd, const float *__restrict__ cft_g, float2 *raw,
+           int pitch, int ntu, int nu, int nv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *tile = reinterpret_cast<float2 *>(smem_raw);
+    float *cft = reinterpret_cast<float *>(tile + STILE * STILE);
+    const WorkItem it = items[blockIdx.x];
+    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) tile[k] = make_float2(0.f, 0.f);
+    for (int k = threadIdx.x; k < CFT_FLOATS; k += GRID_THREADS) cft[k] = cft_g[k];
+    __syncthreads();
+    for (int c = it.cbeg + threadIdx.x; c < it.cend; c += GRID_THREADS) {
+        const uint2 ch = chunks[c];
+        const int start = (int)ch.x, cell = (int)(ch.y & 4095u), len = (int)(ch.y >> 16);
+        const int lu = cell & 63, lv = cell >> 6;
+        float ar[NTAP][NTAP];
+        float ai[NTAP][NTAP];
+#pragma unroll
+        for (int b = 0; b < NTAP; b++)
+#pragma unroll
+            for (int a = 0; a < NTAP; a++) {
+                ar[b][a] = 0.f;
+                if (!PSF) ai[b][a] = 0.f;
+            }
+        for (int k = 0; k < len; k++) {
+            const int p = start + k;
+            const uint32_t g = gd[p];
+            const float w = wt[p];
+            const float4 *gu4 = reinterpret_cast<const float4 *>(cft + (g & 0xFFu) * 8);
+            const float4 *gv4 = reinterpret_cast<const float4 *>(cft + ((g >> 8) & 0xFFu) * 8);
+            const float4 u0 = gu4[0], u1 = gu4[1], v0 = gv4[0], v1 = gv4[1];
+            const float gu[NTAP] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z};
+            const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
+            float fr, fi = 0.f;
+            if (PSF) {
+                fr = w;
+            } else {
+                const float2 f = fres[p];
+                fr = w * f.x;
+                fi = w * f.y;
+            }
+            float hr[NTAP], hi[NTAP];
+#pragma unroll
+            for (int a = 0; a < NTAP; a++) {
+                hr[a] = gu[a] * fr;
+                if (!PSF) hi[a] = gu[a] * fi;
+            }
+#pragma unroll
+            for (int b = 0; b < NTAP; b++)
+#pragma unroll
+                for (int a = 0; a < NTAP; a++) {
+                    ar[b][a] = fmaf(gv[b], hr[a], ar[b][a]);
+                    if (!PSF) ai[b][a] = fmaf(gv[b], hi[a], ai[b][a]);
+                }
+        }
+#pragma unroll
+        for (int b = 0; b < NTAP; b++)
+#pragma unroll
+            for (int a = 0; a < NTAP; a++) {
+                float2 *dst = &tile[(lv + b) * STILE + lu + a];
+                atomicAdd(&dst->x, ar[b][a]);
+                if (!PSF) atomicAdd(&dst->y, ai[b][a]);
+            }
+    }
+    __syncthreads();
+    const int tu = it.tile % ntu, tv = it.tile / ntu;
+    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
+        const float2 val = tile[k];
+        if (val.x == 0.f && val.y == 0.f) continue;
+        const int r = k / STILE, cc = k - r * STILE;
+        const int gv0 = tv * TILE + r - SUPP, gu0 = tu * TILE + cc - SUPP;  // 0-based raw
+        if (gv0 < 0 || gv0 >= nv || gu0 < 0 || gu0 >= nu) continue;
+        red_add_f2(&raw[(int64_t)gv0 * pitch + gu0], val);
+    }
+}
+
+// Plan-invariant sums: LSUMWT = sum of UVWT (grd/grdh2d.f:185) and SUMWT (grd/grdh2d.f:157).
+constexpr int RED_T = 256;
+__global__ void __launch_bounds__(RED_T) k_plan_sums(const float *__restrict__ wt,
+                                                      const uint32_t *__restrict__ gd,
+                                                      const float *__restrict__ cft, int64_t n,
+                                                      double *partial) {
+    __shared__ double sh[2][RED_T / 32];
+    double s0 = 0.0, s1 = 0.0;
+    for (int64_t p = (int64_t)blockIdx.x * RED_T + threadIdx.x; p < n; p += (int64_t)gridDim.x * RED_T) {
+        const uint32_t g = gd[p];
+        const float *gu = cft + (g & 0xFFu) * 8, *gv = cft + ((g >> 8) & 0xFFu) * 8;
+        float su = 0.f, sv = 0.f;
+#pragma unroll
+        for (int a = 0; a < NTAP; a++) {
+            su += gu[a];
+            sv += gv[a];
+        }
+        const float w = wt[p];
+        s0 += (double)w * (double)su * (double)sv;
+        s1 += (double)w;
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, d);
+        s1 += __shfl_down_sync(0xffffffffu, s1, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sh[0][threadIdx.x >> 5] = s0;
+        sh[1][threadIdx.x >> 5] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < RED_T / 32; k++) {
+            a += sh[0][k];
+            b += sh[1][k];
+        }
+        partial[2 * blockIdx.x] = a;
+        partial[2 * blockIdx.x + 1] = b;
+    }
+}
+
+__global__ void k_sum_pairs(const double *partial, int n, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < n; k++) {
+            a += partial[2 * k];
+            b += partial[2 * k + 1];
+        }
+        out[0] = a;
+        out[1] = b;
+    }
+}
+
+// Transposed gridding-function table: cft[d][a] = CF(CFOFFSET + (d-64) + OSAMP*(a-SUPP)).
+__global__ void k_build_cft(const float *cf, float *cft) {
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= 129) return;
+    const int center = (SUPP + 1) * OSAMP;  // CFOFFSET - 1 (0-based)
+    for (int a = 0; a < 8; a++)
+        cft[d * 8 + a] = a < NTAP ? cf[center + (d - 64) + OSAMP * (a - SUPP)] : 0.f;
+}
+
+// ---------------------------------------------------------------------------------------
+// Symmetrise, shift left by SUPPU and normalise (grd/grdh2d.f:202-226).  raw and out are
+// [nv][pitch] complex; out(u,v) = scale * R'(u+SUPP, v) for u <= NU-SUPP, else 0, where R'
+// adds conj(R(UC-k, 2VC-v)) into columns UC+k, k = 0..SUPP, UC = UORIGIN+SUPP.
+__global__ void k_finalize(const float2 *__restrict__ raw, float2 *__restrict__ out, int nu,
+                           int nv, int pitch, int uorigin, int vorigin, int supp, float scale) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)nv * pitch) return;
+    const int v0 = (int)(idx / pitch), u0 = (int)(idx - (int64_t)v0 * pitch);
+    if (u0 >= nu) {
+        out[idx] = make_float2(0.f, 0.f);
+        return;
+    }
+    const int u1 = u0 + 1, v1 = v0 + 1;  // 1-based
+    float2 r = make_float2(0.f, 0.f);
+    if (u1 <= nu - supp) {
+        const int U = u1 + supp;            // raw column (1-based)
+        r = raw[(int64_t)v0 * pitch + (U - 1)];
+        const int UC = uorigin + supp, VC = vorigin;
+        const int k = U - UC;
+        if (k >= 0 && k <= supp) {
+            const int dvv = v1 - VC;
+            const int vm = 2 * VC - v1;
+            if (dvv >= -(nv / 2) + 1 && dvv <= nv / 2 - 1 && vm >= 1 && vm <= nv) {
+                const float2 m = raw[(int64_t)(vm - 1) * pitch + (UC - k - 1)];
+                r.x = r.x + m.x;
+                r.y = r.y - m.y;
+            }
+        }
+        r.x *= scale;
+        r.y *= scale;
+    }
+    out[idx] = r;
+}
+
+// ---------------------------------------------------------------------------------------
+// Degridding.
+constexpr int DG_THREADS = 128;
+constexpr int DG_TILE_FLOATS = STILE * STILE * 2;  // 9800 floats, 39200 B
+constexpr uint32_t DG_TX_BYTES = DG_TILE_FLOATS * 4;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// mode 0: residual update in the gridding frame; mode 1: caller-order output (user frame).
+template <int MODE>
+__global__ void __launch_bounds__(DG_THREADS, 3)
+    k_degrid(const __grid_constant__ CUtensorMap tmap, const WorkItem *__restrict__ items,
+             const uint2 *__restrict__ chunks, const uint32_t *__restrict__ gd,
+             const float *__restrict__ cft_g, const float2 *__restrict__ fobs, float2 *fres,
+             const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
+             const uint32_t *__restrict__ orig, const float *__restrict__ wt, float2 *vis_out,
+             float *wt_out, int ntu, int *status) {
+    extern __shared__ __align__(128) unsigned char smem_dg[];
+    float2 *tile = reinterpret_cast<float2 *>(smem_dg);
+    float *cft = reinterpret_cast<float *>(smem_dg + DG_TX_BYTES);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_dg + DG_TX_BYTES + CFT_FLOATS * 4);
+    const WorkItem it = items[blockIdx.x];
+    const int tu = it.tile % ntu, tv = it.tile / ntu;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        asm volatile("fence.proxy.async.shared::cta;");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // box origin: columns tu*64-6 (complex) -> float x = 2*(tu*64-6), rows tv*64-3
+        const int x = 2 * (tu * TILE - 2 * SUPP), y = tv * TILE - SUPP;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                     "r"(DG_TX_BYTES));
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(tile)),
+            "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+            : "memory");
+    }
+    for (int k = threadIdx.x; k < CFT_FLOATS; k += DG_THREADS) cft[k] = cft_g[k];
+    // bounded wait on phase 0 of the barrier
+    {
+        uint32_t done = 0;
+        for (int spin = 0; spin < (1 << 24) && !done; spin++) {
+            asm volatile(
+                "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;"
+                " selp.u32 %0, 1, 0, p; }"
+                : "=r"(done)
+                : "r"(smem_u32(bar))
+                : "memory");
+        }
+        if (!done) {
+            atomicExch(&status[STATUS_TIMEOUT], 1);
+            return;
+        }
+    }
+    __syncthreads();
+    for (int c = it.cbeg + threadIdx.x; c < it.cend; c += DG_THREADS) {
+        const uint2 ch = chunks[c];
+        const int start = (int)ch.x, cell = (int)(ch.y & 4095u), len = (int)(ch.y >> 16);
+        const int lu = cell & 63, lv = cell >> 6;
+        float2 G[NTAP][NTAP];
+#pragma unroll
+        for (int b = 0; b < NTAP; b++)
+#pragma unroll
+            for (int a = 0; a < NTAP; a++) G[b][a] = tile[(lv + b) * STILE + lu + a];
+        for (int k = 0; k < len; k++) {
+            const int p = start + k;
+            const uint32_t g = gd[p];
+            if ((g & GD_EXCEPTION) == GD_EXCEPTION) continue;
+            const float4 *gu4 = reinterpret_cast<const float4 *>(cft + ((g >> 16) & 0xFFu) * 8);
+            const float4 *gv4 = reinterpret_cast<const float4 *>(cft + (g >> 24) * 8);
+            const float4 u0 = gu4[0], u1 = gu4[1], v0 = gv4[0], v1 = gv4[1];
+            const float gu[NTAP] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z};
+            const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
+            float rr = 0.f, ri = 0.f, su = 0.f, sv = 0.f;
+#pragma unroll
+            for (int b = 0; b < NTAP; b++) {
+                float tr = 0.f, ti = 0.f;
+#pragma unroll
+                for (int a = 0; a < NTAP; a++) {
+                    tr = fmaf(gu[a], G[b][a].x, tr);
+                    ti = fmaf(gu[a], G[b][a].y, ti);
+                }
+                rr = fmaf(gv[b], tr, rr);
+                ri = fmaf(gv[b], ti, ri);
+                sv += gv[b];
+                su += gu[b];
+            }
+            const float sw = su * sv;
+            const float inv = 1.0f / sw;
+            float mr = rr * inv, mi = ri * inv;
+            if (MODE == 0) {
+                const float2 o = fobs[p];
+                fres[p] = make_float2(o.x - mr, o.y - mi);
+            } else {
+                if (gconj[p]) mi = -mi;
+                float2 vv = make_float2(mr, mi);
+                if (rot) {
+                    const float2 rt = rot[p];
+                    vv = make_float2(mr * rt.x - mi * rt.y, mr * rt.y + mi * rt.x);
+                }
+                const uint32_t o = orig[p];
+                vis_out[o] = vv;
+                wt_out[o] = wt[p];
+            }
+        }
+    }
+}
+
+// Exception path: GRDDEH2D's loops verbatim (both the axis-reflection branch,
+// grd/grddeh2d.f:123-158, and the plain branch, :163-173), reading the grid from HBM.
+template <int MODE>
+__global__ void k_degrid_exc(const DegridExc *__restrict__ exc, const float *__restrict__ exc_wt,
+                             const float2 *__restrict__ exc_rot, int64_t nexc,
+                             const float2 *__restrict__ grid, int pitch, int nu, int nv,
+                             int uorigin, int vorigin, const float *__restrict__ cf,
+                             int doshift, const float2 *__restrict__ fobs, float2 *fres,
+                             float2 *vis_out, float *wt_out, unsigned long long *nbad) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nexc) return;
+    const DegridExc e = exc[t];
+    if (MODE == 0 && e.pos < 0) return;
+    const float w0 = exc_wt[t];
+    float vr = 0.f, vi = 0.f, sumwt = 0.f;
+    bool ok = false;
+    if (e.valid) {
+        const int cfo = (SUPP + 1) * OSAMP + 1;
+        const int ucen = e.nuc - uorigin, vcen = e.nvc - vorigin;
+#define GAT(U, V) grid[(int64_t)((V)-1) * pitch + ((U)-1)]
+        if (e.nuc <= SUPP) {
+            for (int offu = -SUPP; offu <= SUPP; offu++) {
+                const int delu = e.delui + OSAMP * offu + cfo;
+                if (ucen != -offu) {
+                    const int us = (ucen + offu) >= 0 ? 1 : -1;
+                    const int ui = uorigin + us * (ucen + offu);
+                    for (int offv = -SUPP; offv <= SUPP; offv++) {
+                        const int delv = e.delvi + OSAMP * offv + cfo;
+                        const int vint = vorigin + us * (vcen + offv);
+                        const float uvwt = __fmul_rn(cf[delu - 1], cf[delv - 1]);
+                        if (ui < 1 || ui > nu || vint < 1 || vint > nv) continue;
+                        float2 f = GAT(ui, vint);
+                        if (us <= 0) f.y = -f.y;
+                        vr = __fadd_rn(vr, __fmul_rn(f.x, uvwt));
+                        vi = __fadd_rn(vi, __fmul_rn(f.y, uvwt));
+                        sumwt = __fadd_rn(sumwt, uvwt);
+                    }
+                } else {
+                    for (int offv = -SUPP; offv <= SUPP; offv++) {
+                        const int delv = e.delvi + OSAMP * offv + cfo;
+                        const int vint = vorigin + (vcen + offv);
+                        const float uvwt = __fmul_rn(cf[delu - 1], cf[delv - 1]);
+                        if (vint < 1 || vint > nv) continue;
+                        const float2 f = GAT(uorigin, vint);
+                        vr = __fadd_rn(vr, __fmul_rn(f.x, uvwt));
+                        vi = __fadd_rn(vi, __fmul_rn(f.y, uvwt));
+                        sumwt = __fadd_rn(sumwt, uvwt);
+                    }
+                }
+            }
+        } else {
+            for (int offv = -SUPP; offv <= SUPP; offv++) {
+                const int delv = e.delvi + OSAMP * offv + cfo;
+                const int vint = vorigin + vcen + offv;
+                for (int offu = -SUPP; offu <= SUPP; offu++) {
+                    const int delu = e.delui + OSAMP * offu + cfo;
+                    const int ui = uorigin + ucen + offu;
+                    const float uvwt = __fmul_rn(cf[delu - 1], cf[delv - 1]);
+                    const float2 f = GAT(ui, vint);
+                    vr = __fadd_rn(vr, __fmul_rn(f.x, uvwt));
+                    vi = __fadd_rn(vi, __fmul_rn(f.y, uvwt));
+                    sumwt = __fadd_rn(sumwt, uvwt);
+                }
+            }
+        }
+#undef GAT
+        if (sumwt > 0.0f) {
+            vr = __fdiv_rn(vr, sumwt);
+            vi = __fdiv_rn(vi, sumwt);
+            ok = true;
+        } else {
+            vr = 0.f;
+            vi = 0.f;
+            if (MODE == 1) atomicAdd(nbad, 1ull);
+        }
+        if (e.conj) vi = -vi;
+        const float2 rt = exc_rot[t];
+        const float xr = __fsub_rn(__fmul_rn(vr, rt.x), __fmul_rn(vi, rt.y));
+        const float xi = __fadd_rn(__fmul_rn(vr, rt.y), __fmul_rn(vi, rt.x));
+        vr = xr;
+        vi = xi;
+    }
+    if (MODE == 1) {
+        vis_out[e.orig] = make_float2(vr, vi);
+        wt_out[e.orig] = ok ? fabsf(w0) : -w0;
+    } else {
+        // model in the gridding frame: rotate by (c, -s) when the plan rotates, conjugate
+        float mr = vr, mi = vi;
+        if (doshift) {
+            const float2 rt = exc_rot[t];
+            mr = vr * rt.x + vi * rt.y;
+            mi = -vr * rt.y + vi * rt.x;
+        }
+        if (e.gconj) mi = -mi;
+        const float2 o = fobs[e.pos];
+        fres[e.pos] = make_float2(o.x - mr, o.y - mi);
+    }
+}
+
+// residual back to the caller's frame and order: V = conj?(F) * (c, s), the inverse of
+// F = conj?(V * (c, -s)) applied when the plan was built
+__global__ void k_scatter_vis(const float2 *__restrict__ src, const uint32_t *__restrict__ orig,
+                              const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
+                              int64_t n, float2 *dst) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float2 f = src[p];
+    if (gconj[p]) f.y = -f.y;
+    if (rot) {
+        const float2 r = rot[p];
+        f = make_float2(f.x * r.x - f.y * r.y, f.x * r.y + f.y * r.x);
+    }
+    dst[orig[p]] = f;
+}
+
+// frame transform of the caller's visibilities into the plan's residual (sde_plan_set_vis)
+__global__ void k_set_vis(const float2 *__restrict__ vis_user, const uint32_t *__restrict__ orig,
+                          const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
+                          int64_t n, float2 *fobs, float2 *fres) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float2 v = vis_user[orig[p]];
+    float fr = v.x, fi = v.y;
+    if (rot) {
+        const float2 r = rot[p];  // FVIS = VIS * (c, -s)
+        fr = __fsub_rn(__fmul_rn(v.x, r.x), __fmul_rn(v.y, -r.y));
+        fi = __fadd_rn(__fmul_rn(v.x, -r.y), __fmul_rn(v.y, r.x));
+    }
+    if (gconj[p]) fi = -fi;
+    fobs[p] = make_float2(fr, fi);
+    fres[p] = make_float2(fr, fi);
+}
+
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                    const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                    const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int make_grid_tmap(CUtensorMap *map, const float *grid, int pitch, int nv) {
+    static PFN_encodeTiled fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                         cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+            sde_set_error("cuTensorMapEncodeTiled unavailable");
+            return SDE_ECUDA;
+        }
+        fn = (PFN_encodeTiled)p;
+    }
+    if (((uintptr_t)grid & 15u) != 0 || (pitch * 8) % 16 != 0) {
+        sde_set_error("grid not 16-byte aligned for TMA");
+        return SDE_EINVAL;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)pitch * 2, (cuuint64_t)nv};
+    cuuint64_t strides[1] = {(cuuint64_t)pitch * 8};
+    cuuint32_t box[2] = {(cuuint32_t)(STILE * 2), (cuuint32_t)STILE};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)grid, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        sde_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return SDE_ECUDA;
+    }
+    return SDE_OK;
+}
+
+size_t grid_smem() { return sizeof(float2) * STILE * STILE + sizeof(float) * CFT_FLOATS; }
+size_t degrid_smem() { return DG_TX_BYTES + sizeof(float) * CFT_FLOATS + 16; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+int plan_build_cft(sde_plan *pl) {
+    k_build_cft<<<1, 160, 0, pl->ctx->stream>>>(pl->cf, pl->cft);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+int ctx_build_cft(sde_ctx *ctx) {
+    k_build_cft<<<1, 160, 0, ctx->stream>>>(ctx->d_cf, ctx->d_cft);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+// LSUMWT and SUMWT of the plan (host doubles), computed once.
+int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt) {
+    sde_ctx *ctx = pl->ctx;
+    if (pl->nvis == 0) {
+        *lsumwt = 0.0;
+        *sumwt = 0.0;
+        return SDE_OK;
+    }
+    int nb = ctx->num_sms * 4;
+    double *part;
+    SDE_TRY(ctx_scratch(ctx, "gs_part", sizeof(double) * 2 * (size_t)nb, (void **)&part));
+    k_plan_sums<<<nb, RED_T, 0, ctx->stream>>>(pl->wt, pl->gd, pl->cft, pl->nvis, part);
+    SDE_CHECK_LAUNCH();
+    k_sum_pairs<<<1, 32, 0, ctx->stream>>>(part, nb, pl->d_sums);
+    SDE_CHECK_LAUNCH();
+    double h[2];
+    SDE_CUDA_TRY(cudaMemcpyAsync(h, pl->d_sums, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    SDE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    *lsumwt = h[0];
+    *sumwt = h[1];
+    return SDE_OK;
+}
+
+int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, float2 *out, int nu, int nv, int pitch,
+                        int uorigin, int vorigin, int supp, float scale) {
+    int64_t n = (int64_t)nv * pitch;
+    k_finalize<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(raw, out, nu, nv, pitch, uorigin,
+                                                          vorigin, supp, scale);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+int plan_grid_raw(sde_plan *pl, int what, float2 *raw) {
+    sde_ctx *ctx = pl->ctx;
+    const int nu = pl->spec.nu, nv = pl->spec.nv;
+    SDE_CUDA_TRY(cudaMemsetAsync(raw, 0, sizeof(float2) * (size_t)nv * pl->pitch, ctx->stream));
+    if (pl->nitems == 0) return SDE_OK;
+    static bool attr = false;
+    if (!attr) {
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)grid_smem()));
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)grid_smem()));
+        attr = true;
+    }
+    if (what == SDE_GRID_PSF)
+        k_grid<true><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
+            pl->items, pl->chunks, pl->fres, pl->wt, pl->gd, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+    else
+        k_grid<false><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
+            pl->items, pl->chunks, pl->fres, pl->wt, pl->gd, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+// mode 0: residual update; mode 1: caller-order output
+int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vis_out,
+                float *wt_out, unsigned long long *nbad_dev) {
+    sde_ctx *ctx = pl->ctx;
+    const int nu = pl->spec.nu, nv = pl->spec.nv;
+    static bool attr = false;
+    if (!attr) {
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_degrid<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)degrid_smem()));
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_degrid<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)degrid_smem()));
+        attr = true;
+    }
+    if (pl->nitems > 0) {
+        CUtensorMap map;
+        SDE_TRY(make_grid_tmap(&map, grid, pitch, nv));
+        if (mode == 0)
+            k_degrid<0><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
+                map, pl->items, pl->chunks, pl->gd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot,
+                pl->orig, pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
+        else
+            k_degrid<1><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
+                map, pl->items, pl->chunks, pl->gd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot,
+                pl->orig, pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
+        SDE_CHECK_LAUNCH();
+    }
+    if (pl->nexc > 0) {
+        size_t ne1 = (size_t)pl->nexc;
+        const float *exc_wt = (const float *)((const char *)pl->exc + exc_wt_off(ne1));
+        const float2 *exc_rot = (const float2 *)((const char *)pl->exc + exc_rot_off(ne1));
+        const int T = 128;
+        if (mode == 0)
+            k_degrid_exc<0><<<ceil_div(pl->nexc, T), T, 0, ctx->stream>>>(
+                pl->exc, exc_wt, exc_rot, pl->nexc, (const float2 *)grid, pitch, nu, nv,
+                pl->spec.uorigin, pl->spec.vorigin, pl->cf, pl->doshift, pl->fobs, pl->fres,
+                vis_out, wt_out, nbad_dev);
+        else
+            k_degrid_exc<1><<<ceil_div(pl->nexc, T), T, 0, ctx->stream>>>(
+                pl->exc, exc_wt, exc_rot, pl->nexc, (const float2 *)grid, pitch, nu, nv,
+                pl->spec.uorigin, pl->spec.vorigin, pl->cf, pl->doshift, pl->fobs, pl->fres,
+                vis_out, wt_out, nbad_dev);
+        SDE_CHECK_LAUNCH();
+    }
+    return SDE_OK;
+}
+
+int plan_scatter_residual(sde_plan *pl, float2 *dst) {
+    if (pl->nvis == 0) return SDE_OK;
+    k_scatter_vis<<<ceil_div(pl->nvis, 256), 256, 0, pl->ctx->stream>>>(
+        pl->fres, pl->orig, pl->gconj, pl->rot, pl->nvis, dst);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+int plan_set_vis_dev(sde_plan *pl, const float2 *vis_user) {
+    if (pl->nvis == 0) return SDE_OK;
+    k_set_vis<<<ceil_div(pl->nvis, 256), 256, 0, pl->ctx->stream>>>(vis_user, pl->orig, pl->gconj,
+                                                                  pl->rot, pl->nvis, pl->fobs,
+                                                                  pl->fres);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}

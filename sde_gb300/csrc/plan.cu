@@ -1,0 +1,521 @@
+// plan.cu -- builds a resident, tile-sorted visibility set (sde_plan).
+//
+// For every visibility the plan evaluates, once and with the reference's exact FP64/FP32
+// operations, the cell placement that GRDH2D uses (FP64, grd/grdh2d.f:114-166) and the one
+// GRDDEH2D uses (FP32 cell from FP64 coordinates, grd/grddeh2d.f:92-118).  Visibilities
+// are then sorted by (uv tile, cell), split into same-cell chunks of <= CHUNK_MAX, and the
+// chunks of each work item are ordered by (7x7 colour class, chunk index, cell) so that
+// the 32 chunks a warp flushes at once never overlap.  The observed visibilities are
+// stored already rotated/conjugated into the gridding frame (FVIS of grd/grdh2d.f:125-143),
+// so the per-cycle kernels carry no FP64 or trigonometric work.
+#include <math.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace {
+
+struct GParams {
+    float uscale, uoffset, vscale, voffset;
+    int uorigin, vorigin, nu, nv, supp, osamp;
+    double s[9];
+    int doshift, ntu;
+    double twopi;
+};
+
+struct DGeo {
+    int nud, nvd, dui, dvi;
+    bool valid, conj;
+    float rc, rs;
+};
+
+// GRDDEH2D's per-visibility geometry (grd/grddeh2d.f:92-118): always rotated, FP32 cell.
+__device__ __forceinline__ DGeo degrid_geom(const GParams &p, float u, float v, float w) {
+    DGeo g;
+    double ug = (double)u, vg = (double)v, wg = (double)w;
+    double ul = __dadd_rn(__dadd_rn(__dmul_rn(p.s[0], ug), __dmul_rn(p.s[1], vg)), __dmul_rn(p.s[2], wg));
+    double vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
+    double wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
+    double ph = __dmul_rn(p.twopi, __dsub_rn(wl, wg));
+    g.rc = (float)cos(ph);
+    g.rs = (float)sin(ph);
+    float ucell = __double2float_rn(__dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset));
+    float vcell = __double2float_rn(__dadd_rn(__dmul_rn((double)p.vscale, vl), (double)p.voffset));
+    if (ucell > 0.0f) {
+        ucell = __fadd_rn(ucell, (float)p.uorigin);
+        vcell = __fadd_rn(vcell, (float)p.vorigin);
+    } else {
+        ucell = __fadd_rn(-ucell, (float)p.uorigin);
+        vcell = __fadd_rn(-vcell, (float)p.vorigin);
+    }
+    g.nud = nint_f(ucell);
+    g.nvd = nint_f(vcell);
+    g.valid = !(g.nud + p.supp > p.nu) && !(g.nvd + p.supp > p.nv) && !(g.nvd - p.supp < 1);
+    g.dui = nint_f(__fmul_rn((float)p.osamp, __fsub_rn((float)g.nud, ucell)));
+    g.dvi = nint_f(__fmul_rn((float)p.osamp, __fsub_rn((float)g.nvd, vcell)));
+    g.conj = __dmul_rn((double)p.uscale, ul) > 0.0;
+    return g;
+}
+
+// Per visibility (caller order): gridding key, packed offsets, observed value in the
+// gridding frame, rotation, conjugation flag.
+__global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float *__restrict__ v,
+                            const float *__restrict__ w, const float2 *__restrict__ vis,
+                            const float *__restrict__ wt, int64_t n, uint32_t *keys,
+                            uint32_t *vals, uint32_t *gd, float2 *fobs, float2 *rot,
+                            uint8_t *gconj, unsigned long long *counts) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t nvalid = 0, nexc = 0;
+    if (i < n) {
+        float wi = wt[i];
+        uint32_t key = KEY_INVALID, packed = 0;
+        float2 f = make_float2(0.f, 0.f), r = make_float2(1.f, 0.f);
+        uint8_t gc = 0;
+        if (wi > 0.0f) {
+            float2 vv = vis[i];
+            double ug = (double)u[i], vg = (double)v[i], wg = (double)w[i];
+            double ucell, vcell;
+            float fr, fi;
+            DGeo dg = degrid_geom(p, u[i], v[i], w[i]);
+            if (p.doshift) {
+                double ul = __dadd_rn(__dadd_rn(__dmul_rn(p.s[0], ug), __dmul_rn(p.s[1], vg)), __dmul_rn(p.s[2], wg));
+                double vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
+                double wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
+                double ph = __dmul_rn(p.twopi, __dsub_rn(wl, wg));
+                float c = (float)cos(ph), s = (float)(-sin(ph));
+                fr = __fsub_rn(__fmul_rn(vv.x, c), __fmul_rn(vv.y, s));
+                fi = __fadd_rn(__fmul_rn(vv.x, s), __fmul_rn(vv.y, c));
+                ucell = __dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset);
+                vcell = __dadd_rn(__dmul_rn((double)p.vscale, vl), (double)p.voffset);
+                r = make_float2(dg.rc, dg.rs);
+            } else {
+                fr = vv.x;
+                fi = vv.y;
+                ucell = __dadd_rn(__dmul_rn((double)p.uscale, ug), (double)p.uoffset);
+                vcell = __dadd_rn(__dmul_rn((double)p.vscale, vg), (double)p.voffset);
+            }
+            if (ucell > 0.0) {
+                fi = -fi;
+                gc = 1;
+                ucell = __dadd_rn(ucell, (double)(float)p.uorigin);
+                vcell = __dadd_rn(vcell, (double)(float)p.vorigin);
+            } else {
+                ucell = __dadd_rn(-ucell, (double)(float)p.uorigin);
+                vcell = __dadd_rn(-vcell, (double)(float)p.vorigin);
+            }
+            int nuc = nint_d(ucell), nvc = nint_d(vcell);
+            bool gvalid = !(nuc + 2 * p.supp > p.nu) && !(nvc + p.supp > p.nv) && !(nvc - p.supp < 1);
+            if (gvalid) {
+                int dug = nint_d(__dmul_rn((double)p.osamp, __dsub_rn((double)(float)nuc, ucell)));
+                int dvg = nint_d(__dmul_rn((double)p.osamp, __dsub_rn((double)(float)nvc, vcell)));
+                int ucen = nuc + p.supp, vcen = nvc;  // 1-based, gridding frame
+                int tu = (ucen - 1) >> TILE_LOG2, lu = (ucen - 1) & (TILE - 1);
+                int tv = (vcen - 1) >> TILE_LOG2, lv = (vcen - 1) & (TILE - 1);
+                key = ((uint32_t)(tv * p.ntu + tu) << 12) | ((uint32_t)lv << 6) | (uint32_t)lu;
+                bool exc = !dg.valid || dg.nud != nuc || dg.nvd != nvc || dg.nud <= p.supp ||
+                           dg.conj != (gc != 0);
+                packed = exc ? (pack_gd(dug, dvg, 0, 0) & 0x0000FFFFu) | GD_EXCEPTION
+                             : pack_gd(dug, dvg, dg.dui, dg.dvi);
+                nvalid = 1;
+                nexc = exc;
+                f = make_float2(fr, fi);
+            } else {
+                nexc = 1;  // degrid-only or degrid-invalid: exception path
+            }
+        }
+        keys[i] = key;
+        vals[i] = (uint32_t)i;
+        gd[i] = packed;
+        fobs[i] = f;
+        if (rot) rot[i] = r;
+        gconj[i] = gc;
+    }
+    unsigned mv = __ballot_sync(0xffffffffu, nvalid), me = __ballot_sync(0xffffffffu, nexc);
+    if ((threadIdx.x & 31) == 0) {
+        if (mv) atomicAdd(&counts[0], (unsigned long long)__popc(mv));
+        if (me) atomicAdd(&counts[1], (unsigned long long)__popc(me));
+    }
+}
+
+// Gather the per-visibility arrays into sorted order.
+__global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned long long *counts,
+                              const float2 *__restrict__ fobs_u, const float *__restrict__ wt_u,
+                              const uint32_t *__restrict__ gd_u, const float2 *__restrict__ rot_u,
+                              const uint8_t *__restrict__ gconj_u, float2 *fobs, float2 *fres,
+                              float *wt, uint32_t *gd, uint32_t *orig, float2 *rot, uint8_t *gconj,
+                              uint32_t *pos_of) {
+    int64_t nv = (int64_t)counts[0];
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nv) return;
+    uint32_t i = perm[p];
+    float2 f = fobs_u[i];
+    fobs[p] = f;
+    fres[p] = f;
+    wt[p] = wt_u[i];
+    gd[p] = gd_u[i];
+    orig[p] = i;
+    gconj[p] = gconj_u[i];
+    if (rot) rot[p] = rot_u[i];
+    pos_of[i] = (uint32_t)p;
+}
+
+// flags for the exception compaction
+__global__ void k_exc_flag(const float *__restrict__ wt, const uint32_t *__restrict__ keys_u,
+                           const uint32_t *__restrict__ gd_u, int64_t n, uint32_t *flag) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t f = 0;
+    if (wt[i] > 0.0f) f = (keys_u[i] == KEY_INVALID) || ((gd_u[i] & GD_EXCEPTION) == GD_EXCEPTION);
+    flag[i] = f;
+}
+
+__global__ void k_exc_write(GParams p, const float *__restrict__ u, const float *__restrict__ v,
+                            const float *__restrict__ w, const float *__restrict__ wt,
+                            const uint32_t *__restrict__ keys_u, const uint8_t *__restrict__ gconj_u,
+                            const uint32_t *__restrict__ flag, const uint32_t *__restrict__ slot,
+                            const uint32_t *__restrict__ pos_of, int64_t n, DegridExc *exc,
+                            float *exc_wt, float2 *exc_rot) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !flag[i]) return;
+    DGeo g = degrid_geom(p, u[i], v[i], w[i]);
+    DegridExc e;
+    e.orig = (uint32_t)i;
+    e.pos = keys_u[i] == KEY_INVALID ? -1 : (int32_t)pos_of[i];
+    e.nuc = g.nud;
+    e.nvc = g.nvd;
+    e.delui = (int16_t)g.dui;
+    e.delvi = (int16_t)g.dvi;
+    e.conj = g.conj;
+    e.valid = g.valid;
+    e.gconj = gconj_u[i];
+    e.pad = 0;
+    uint32_t s = slot[i];
+    exc[s] = e;
+    exc_wt[s] = wt[i];
+    exc_rot[s] = make_float2(g.rc, g.rs);
+}
+
+// Run / tile heads over the sorted keys (-1 where not a head) for the max-scans.
+__global__ void k_heads(const uint32_t *__restrict__ keys, const unsigned long long *counts,
+                        int32_t *runhead, int32_t *tilehead) {
+    int64_t nv = (int64_t)counts[0];
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nv) return;
+    uint32_t k = keys[q];
+    bool rh = q == 0 || keys[q - 1] != k;
+    bool th = q == 0 || (keys[q - 1] >> 12) != (k >> 12);
+    runhead[q] = rh ? (int32_t)q : -1;
+    tilehead[q] = th ? (int32_t)q : -1;
+}
+
+__global__ void k_chunk_flags(const unsigned long long *counts, const int32_t *runstart,
+                              const int32_t *tilestart, uint32_t *ihead, uint32_t *chead) {
+    int64_t nv = (int64_t)counts[0];
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nv) return;
+    int32_t rs = runstart[q], ts = tilestart[q];
+    int32_t is = ts + ((int32_t)q - ts) / ITEM_MAX * ITEM_MAX;  // item start
+    int32_t cs = rs > is ? rs : is;                            // run start within item
+    bool ih = ((int32_t)q - ts) % ITEM_MAX == 0;
+    bool ch = ((int32_t)q - cs) % CHUNK_MAX == 0;
+    ihead[q] = ih;
+    chead[q] = ch || ih;
+}
+
+__global__ void k_chunk_write(const uint32_t *__restrict__ keys, const unsigned long long *counts,
+                              const int32_t *runstart, const int32_t *tilestart,
+                              const uint32_t *ihead, const uint32_t *chead,
+                              const uint32_t *item_id, const uint32_t *chunk_id, int jbits,
+                              uint64_t *ckey, uint32_t *cval, uint32_t *cstart, WorkItem *items) {
+    int64_t nv = (int64_t)counts[0];
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nv) return;
+    uint32_t k = keys[q];
+    uint32_t it = item_id[q] + ihead[q] - 1;  // inclusive item index
+    if (ihead[q]) {
+        WorkItem wi;
+        wi.tile = (int32_t)(k >> 12);
+        wi.cbeg = wi.cend = 0;
+        wi.vbeg = (int32_t)q;
+        wi.vend = 0;
+        items[it] = wi;
+    }
+    if (!chead[q]) return;
+    uint32_t c = chunk_id[q];
+    int32_t rs = runstart[q], ts = tilestart[q];
+    int32_t is = ts + ((int32_t)q - ts) / ITEM_MAX * ITEM_MAX;
+    int32_t cs = rs > is ? rs : is;
+    uint32_t j = ((uint32_t)q - (uint32_t)cs) / CHUNK_MAX;
+    uint32_t cell = k & 4095u, lu = cell & 63u, lv = cell >> 6;
+    uint32_t color = (lu % 7u) * 7u + (lv % 7u);
+    ckey[c] = ((uint64_t)it << (6 + jbits + 12)) | ((uint64_t)color << (jbits + 12)) |
+              ((uint64_t)j << 12) | cell;
+    cval[c] = c;
+    cstart[c] = (uint32_t)q;
+}
+
+__global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t *__restrict__ cval,
+                              const uint32_t *__restrict__ cstart, const uint32_t *__restrict__ keys,
+                              int64_t nchunks, int64_t nvalid, int shift_item, uint2 *chunks,
+                              WorkItem *items) {
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    uint32_t orig = cval[c];
+    uint32_t st = cstart[orig];
+    uint32_t en = (int64_t)orig + 1 < nchunks ? cstart[orig + 1] : (uint32_t)nvalid;
+    uint32_t cell = keys[st] & 4095u;
+    chunks[c] = make_uint2(st, cell | ((en - st) << 16));
+    uint32_t it = (uint32_t)(ckey[c] >> shift_item);
+    if (c == 0 || (uint32_t)(ckey[c - 1] >> shift_item) != it) items[it].cbeg = (int32_t)c;
+    if (c == nchunks - 1 || (uint32_t)(ckey[c + 1] >> shift_item) != it) items[it].cend = (int32_t)(c + 1);
+}
+
+__global__ void k_item_vend(WorkItem *items, int64_t nitems, int64_t nvalid) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nitems) return;
+    items[t].vend = t + 1 < nitems ? items[t + 1].vbeg : (int32_t)nvalid;
+}
+
+int bits_for(int64_t maxval) {
+    int b = 1;
+    while (b < 63 && ((int64_t)1 << b) <= maxval) b++;
+    return b;
+}
+
+}  // namespace
+
+int sde_grid_pitch(int nu) { return (nu + 3) & ~3; }
+
+int64_t sde_plan_nvis(const sde_plan *plan) { return plan ? plan->nvis : 0; }
+int64_t sde_plan_bytes(const sde_plan *plan) { return plan ? plan->bytes : 0; }
+
+static int plan_alloc(sde_plan *pl, void **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    int rc = ctx_alloc(pl->ctx, p, bytes);
+    if (rc == SDE_OK) pl->bytes += (int64_t)bytes;
+    return rc;
+}
+
+int sde_plan_destroy(sde_plan *pl) {
+    if (!pl) return SDE_OK;
+    sde_ctx *ctx = pl->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    void *ptrs[] = {pl->fobs, pl->fres, pl->wt, pl->gd, pl->orig, pl->rot, pl->gconj, pl->chunks,
+                    pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    ctx->bytes -= pl->bytes;
+    delete pl;
+    return SDE_OK;
+}
+
+// Upload (or alias) caller arrays; builds everything described at the top of the file.
+int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const float *u,
+                    const float *v, const float *w, const float *vis, const float *wt,
+                    int where, sde_plan **out) {
+    if (!ctx || !spec || !out || nvis < 0 || (nvis > 0 && (!u || !v || !w || !vis || !wt))) {
+        sde_set_error("sde_plan_create: bad arguments");
+        return SDE_EINVAL;
+    }
+    if (spec->supp != SUPP || spec->osamp != OSAMP) {
+        sde_set_error("sde_plan_create: support %d / oversampling %d unsupported (SF needs 3/128)",
+                      spec->supp, spec->osamp);
+        return SDE_EINVAL;
+    }
+    if (spec->nu < 2 * SUPP + 1 || spec->nv < 2 * SUPP + 1 || nvis >= (int64_t)0x7FFFFFFF) {
+        sde_set_error("sde_plan_create: grid %dx%d / %lld visibilities out of range", spec->nu,
+                      spec->nv, (long long)nvis);
+        return SDE_EINVAL;
+    }
+    SDE_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    sde_plan *pl = new sde_plan();
+    pl->ctx = ctx;
+    pl->spec = *spec;
+    pl->doshift = (spec->shift[0] != 1.0) || (spec->shift[4] != 1.0) || (spec->shift[8] != 1.0);
+    pl->pitch = sde_grid_pitch(spec->nu);
+    pl->ntu = (spec->nu + TILE - 1) / TILE;
+    pl->ntv = (spec->nv + TILE - 1) / TILE;
+    pl->nvis_in = nvis;
+    int rc = SDE_OK;
+#define PL_TRY(x)                      \
+    do {                               \
+        rc = (x);                      \
+        if (rc != SDE_OK) goto fail;   \
+    } while (0)
+#define PL_CUDA(x)                                                                   \
+    do {                                                                             \
+        cudaError_t _e = (x);                                                        \
+        if (_e != cudaSuccess) {                                                     \
+            sde_set_error("plan: %s: %s", #x, cudaGetErrorString(_e));               \
+            rc = _e == cudaErrorMemoryAllocation ? SDE_ENOMEM : SDE_ECUDA;           \
+            goto fail;                                                               \
+        }                                                                            \
+    } while (0)
+    {
+        const size_t n = (size_t)(nvis > 0 ? nvis : 1);
+        const float *du = u, *dv = v, *dw = w, *dwt = wt;
+        const float2 *dvis = (const float2 *)vis;
+        if (where == SDE_HOST && nvis > 0) {
+            float *bu, *bv, *bw, *bwt;
+            float2 *bvis;
+            PL_TRY(ctx_scratch(ctx, "pl_u", 4 * n, (void **)&bu));
+            PL_TRY(ctx_scratch(ctx, "pl_v", 4 * n, (void **)&bv));
+            PL_TRY(ctx_scratch(ctx, "pl_w", 4 * n, (void **)&bw));
+            PL_TRY(ctx_scratch(ctx, "pl_wt", 4 * n, (void **)&bwt));
+            PL_TRY(ctx_scratch(ctx, "pl_vis", 8 * n, (void **)&bvis));
+            PL_CUDA(cudaMemcpyAsync(bu, u, 4 * n, cudaMemcpyHostToDevice, st));
+            PL_CUDA(cudaMemcpyAsync(bv, v, 4 * n, cudaMemcpyHostToDevice, st));
+            PL_CUDA(cudaMemcpyAsync(bw, w, 4 * n, cudaMemcpyHostToDevice, st));
+            PL_CUDA(cudaMemcpyAsync(bwt, wt, 4 * n, cudaMemcpyHostToDevice, st));
+            PL_CUDA(cudaMemcpyAsync(bvis, vis, 8 * n, cudaMemcpyHostToDevice, st));
+            du = bu; dv = bv; dw = bw; dwt = bwt; dvis = bvis;
+        }
+        GParams gp;
+        gp.uscale = spec->uscale; gp.uoffset = spec->uoffset;
+        gp.vscale = spec->vscale; gp.voffset = spec->voffset;
+        gp.uorigin = spec->uorigin; gp.vorigin = spec->vorigin;
+        gp.nu = spec->nu; gp.nv = spec->nv; gp.supp = spec->supp; gp.osamp = spec->osamp;
+        memcpy(gp.s, spec->shift, sizeof gp.s);
+        gp.doshift = pl->doshift;
+        gp.ntu = pl->ntu;
+        gp.twopi = (double)(8.0f * atanf(1.0f));  // TWOPI = 8 * ATAN(1.0), REAL (grdh2d.f:91)
+
+        uint32_t *keys, *vals, *ktmp, *vtmp, *gd_u, *pos_of;
+        float2 *fobs_u, *rot_u = nullptr;
+        uint8_t *gconj_u;
+        unsigned long long *counts;
+        PL_TRY(ctx_scratch(ctx, "pl_keys", 4 * n, (void **)&keys));
+        PL_TRY(ctx_scratch(ctx, "pl_vals", 4 * n, (void **)&vals));
+        PL_TRY(ctx_scratch(ctx, "pl_ktmp", 4 * n, (void **)&ktmp));
+        PL_TRY(ctx_scratch(ctx, "pl_vtmp", 4 * n, (void **)&vtmp));
+        PL_TRY(ctx_scratch(ctx, "pl_gd", 4 * n, (void **)&gd_u));
+        PL_TRY(ctx_scratch(ctx, "pl_pos", 4 * n, (void **)&pos_of));
+        PL_TRY(ctx_scratch(ctx, "pl_fobs", 8 * n, (void **)&fobs_u));
+        if (pl->doshift) PL_TRY(ctx_scratch(ctx, "pl_rot", 8 * n, (void **)&rot_u));
+        PL_TRY(ctx_scratch(ctx, "pl_gconj", n, (void **)&gconj_u));
+        PL_TRY(ctx_scratch(ctx, "pl_counts", 64, (void **)&counts));
+        PL_CUDA(cudaMemsetAsync(counts, 0, 64, st));
+        const int T = 256;
+        if (nvis > 0) {
+            k_plan_geom<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dvis, dwt, nvis, keys, vals,
+                                                       gd_u, fobs_u, rot_u, gconj_u, counts);
+            PL_CUDA(cudaGetLastError());
+        }
+        // The user-order keys are needed again by the exception pass: keep a copy.
+        uint32_t *keys_u;
+        PL_TRY(ctx_scratch(ctx, "pl_keys_u", 4 * n, (void **)&keys_u));
+        if (nvis > 0) PL_CUDA(cudaMemcpyAsync(keys_u, keys, 4 * n, cudaMemcpyDeviceToDevice, st));
+        int64_t ntiles = (int64_t)pl->ntu * pl->ntv;
+        int kbits = bits_for((ntiles << 12) + 1);
+        if (kbits > 32) {
+            sde_set_error("plan: grid too large for 32-bit tile keys");
+            rc = SDE_EINVAL;
+            goto fail;
+        }
+        if (nvis > 0) PL_TRY(launch_radix_sort_u32(ctx, keys, vals, nvis, kbits, ktmp, vtmp));
+        unsigned long long hc[2] = {0, 0};
+        PL_CUDA(cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, st));
+        PL_CUDA(cudaStreamSynchronize(st));
+        const int64_t nvalid = (int64_t)hc[0], nexc = (int64_t)hc[1];
+        pl->nvis = nvalid;
+        pl->nexc = nexc;
+        const size_t nv1 = (size_t)(nvalid > 0 ? nvalid : 1);
+        PL_TRY(plan_alloc(pl, (void **)&pl->fobs, 8 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->fres, 8 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->wt, 4 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->gd, 4 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->orig, 4 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->gconj, nv1));
+        if (pl->doshift) PL_TRY(plan_alloc(pl, (void **)&pl->rot, 8 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->d_sums, 4 * sizeof(double)));
+        if (nvalid > 0) {
+            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, fobs_u, dwt, gd_u, rot_u,
+                                                           gconj_u, pl->fobs, pl->fres, pl->wt,
+                                                           pl->gd, pl->orig, pl->rot, pl->gconj,
+                                                           pos_of);
+            PL_CUDA(cudaGetLastError());
+        }
+        // exception list (also carries the GRDDEH2D geometry of non-gridding visibilities)
+        size_t ne1 = (size_t)(nexc > 0 ? nexc : 1);
+        PL_TRY(plan_alloc(pl, (void **)&pl->exc, exc_bytes(ne1)));
+        if (nexc > 0) {
+            uint32_t *flag, *slot;
+            PL_TRY(ctx_scratch(ctx, "pl_flag", 4 * n, (void **)&flag));
+            PL_TRY(ctx_scratch(ctx, "pl_slot", 4 * n, (void **)&slot));
+            k_exc_flag<<<ceil_div(nvis, T), T, 0, st>>>(dwt, keys_u, gd_u, nvis, flag);
+            PL_CUDA(cudaGetLastError());
+            PL_TRY(launch_exclusive_scan_u32(ctx, flag, slot, nvis, nullptr));
+            float *exc_wt = (float *)((char *)pl->exc + exc_wt_off(ne1));
+            float2 *exc_rot = (float2 *)((char *)pl->exc + exc_rot_off(ne1));
+            k_exc_write<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dwt, keys_u, gconj_u, flag,
+                                                       slot, pos_of, nvis, pl->exc, exc_wt, exc_rot);
+            PL_CUDA(cudaGetLastError());
+        }
+        // runs, chunks, work items
+        if (nvalid > 0) {
+            int32_t *runhead, *tilehead;
+            uint32_t *ihead, *chead, *item_id, *chunk_id, *tot;
+            PL_TRY(ctx_scratch(ctx, "pl_runhead", 4 * nv1, (void **)&runhead));
+            PL_TRY(ctx_scratch(ctx, "pl_tilehead", 4 * nv1, (void **)&tilehead));
+            PL_TRY(ctx_scratch(ctx, "pl_ihead", 4 * nv1, (void **)&ihead));
+            PL_TRY(ctx_scratch(ctx, "pl_chead", 4 * nv1, (void **)&chead));
+            PL_TRY(ctx_scratch(ctx, "pl_itemid", 4 * nv1, (void **)&item_id));
+            PL_TRY(ctx_scratch(ctx, "pl_chunkid", 4 * nv1, (void **)&chunk_id));
+            PL_TRY(ctx_scratch(ctx, "pl_tot", 16, (void **)&tot));
+            k_heads<<<ceil_div(nvalid, T), T, 0, st>>>(keys, counts, runhead, tilehead);
+            PL_CUDA(cudaGetLastError());
+            PL_TRY(launch_inclusive_max_scan_i32(ctx, runhead, runhead, nvalid));
+            PL_TRY(launch_inclusive_max_scan_i32(ctx, tilehead, tilehead, nvalid));
+            k_chunk_flags<<<ceil_div(nvalid, T), T, 0, st>>>(counts, runhead, tilehead, ihead, chead);
+            PL_CUDA(cudaGetLastError());
+            PL_TRY(launch_exclusive_scan_u32(ctx, ihead, item_id, nvalid, tot));
+            PL_TRY(launch_exclusive_scan_u32(ctx, chead, chunk_id, nvalid, tot + 1));
+            uint32_t htot[2];
+            PL_CUDA(cudaMemcpyAsync(htot, tot, sizeof htot, cudaMemcpyDeviceToHost, st));
+            PL_CUDA(cudaStreamSynchronize(st));
+            const int64_t nitems = htot[0], nchunks = htot[1];
+            pl->nitems = nitems;
+            pl->nchunks = nchunks;
+            PL_TRY(plan_alloc(pl, (void **)&pl->items, sizeof(WorkItem) * (size_t)nitems));
+            PL_TRY(plan_alloc(pl, (void **)&pl->chunks, sizeof(uint2) * (size_t)nchunks));
+            uint64_t *ckey, *cktmp;
+            uint32_t *cval, *cvtmp, *cstart;
+            PL_TRY(ctx_scratch(ctx, "pl_ckey", 8 * (size_t)nchunks, (void **)&ckey));
+            PL_TRY(ctx_scratch(ctx, "pl_cktmp", 8 * (size_t)nchunks, (void **)&cktmp));
+            PL_TRY(ctx_scratch(ctx, "pl_cval", 4 * (size_t)nchunks, (void **)&cval));
+            PL_TRY(ctx_scratch(ctx, "pl_cvtmp", 4 * (size_t)nchunks, (void **)&cvtmp));
+            PL_TRY(ctx_scratch(ctx, "pl_cstart", 4 * (size_t)nchunks, (void **)&cstart));
+            const int jbits = bits_for(ITEM_MAX / CHUNK_MAX);
+            k_chunk_write<<<ceil_div(nvalid, T), T, 0, st>>>(keys, counts, runhead, tilehead, ihead,
+                                                           chead, item_id, chunk_id, jbits, ckey,
+                                                           cval, cstart, pl->items);
+            PL_CUDA(cudaGetLastError());
+            const int shift_item = 6 + jbits + 12;
+            const int cbits = shift_item + bits_for(nitems);
+            PL_TRY(launch_radix_sort_u64(ctx, ckey, cval, nchunks, cbits, cktmp, cvtmp));
+            k_chunk_final<<<ceil_div(nchunks, T), T, 0, st>>>(ckey, cval, cstart, keys, nchunks,
+                                                            nvalid, shift_item, pl->chunks,
+                                                            pl->items);
+            PL_CUDA(cudaGetLastError());
+            k_item_vend<<<ceil_div(nitems, T), T, 0, st>>>(pl->items, nitems, nvalid);
+            PL_CUDA(cudaGetLastError());
+        }
+        // gridding function: the context's 'SF' table
+        PL_TRY(plan_alloc(pl, (void **)&pl->cf, sizeof(float) * CFLEN));
+        PL_TRY(plan_alloc(pl, (void **)&pl->cft, sizeof(float) * 129 * 8));
+        PL_CUDA(cudaMemcpyAsync(pl->cf, ctx->d_cf, sizeof(float) * CFLEN, cudaMemcpyDeviceToDevice, st));
+        PL_CUDA(cudaMemcpyAsync(pl->cft, ctx->d_cft, sizeof(float) * 129 * 8, cudaMemcpyDeviceToDevice, st));
+        PL_CUDA(cudaStreamSynchronize(st));
+    }
+    ctx->bytes += pl->bytes;
+    *out = pl;
+    return SDE_OK;
+fail:
+    ctx->bytes += pl->bytes;
+    sde_plan_destroy(pl);
+    return rc;
+#undef PL_TRY
+#undef PL_CUDA
+}
