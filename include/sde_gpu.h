@@ -87,6 +87,14 @@ void pix2drcl_(float *drt, float *psf, float *box, int *nx, int *ny, int *pnx, i
 /* Replaces PIXISAMA (source/pix/pixisama.f:231), called by PIX2DRCL (pix/pix2drcl.f:146). */
 int pixisama_(int *n, float *a, int *i);
 
+/* Host-side tables the gridder's callers build (no GPU work):
+ * GRDSF (source/grd/grdsf.f:306), GRDCF (source/grd/grdcf.f:211, called by VISGRID,
+ * vis/visgrid.f:278) and GRDCCF (source/grd/grdccf.f:382, called by IMGGRIDC,
+ * img/imggridc.f:363); codes 'SF' and 'BOX'. */
+double grdsf_(double *nu);
+void grdcf_(char *cfcode, float *cf, int *cfsupp, int *cfosamp, size_t cfcode_len);
+void grdccf_(char *ccfcode, float *ccf, int *ccflen, size_t ccfcode_len);
+
 /* The reference's error channel: COMMON /SYSI/ (include/stdinc.h:64-66).  libsdegpu
  * defines it; a Fortran program's own definition interposes at link time.  errrepor_ and
  * msgput_ are weak defaults (main/err.f:532, main/msg.f:7) that a host program overrides. */
@@ -111,6 +119,15 @@ void *sde_ctx_stream(sde_ctx *ctx);            /* the cudaStream_t all calls run
 int sde_ctx_set_stream(sde_ctx *ctx, void *stream); /* run on a caller's stream instead   */
 /* Device memory owned by the context's pools (bytes), for admission control. */
 int64_t sde_ctx_bytes_in_use(sde_ctx *ctx);
+/* Tracing: with profiling on, every kernel launch is bracketed by CUDA events on the
+ * context's stream; sde_ctx_kernel_stats synchronises and returns the summed device time
+ * (ms) and launch count of one kernel ("grid", "grid_psf", "degrid", "degrid_exc",
+ * "finalize", "col_fft", "row_c2r", "row_r2c", "hogbom", ...).  sde_ctx_launches counts
+ * every kernel the library has launched on this context. */
+int sde_ctx_profile(sde_ctx *ctx, int enable);
+int sde_ctx_kernel_stats(sde_ctx *ctx, const char *kernel, double *total_ms, int64_t *count);
+int sde_ctx_reset_stats(sde_ctx *ctx);
+int64_t sde_ctx_launches(sde_ctx *ctx);
 
 /* Geometry of one gridding/degridding job (the scalar arguments of GRDH2D/GRDDEH2D). */
 typedef struct {

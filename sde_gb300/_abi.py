@@ -60,6 +60,10 @@ SIGNATURES = [
     ("sde_ctx_stream", P, [P]),
     ("sde_ctx_set_stream", I, [P, P]),
     ("sde_ctx_bytes_in_use", I64, [P]),
+    ("sde_ctx_profile", I, [P, I]),
+    ("sde_ctx_kernel_stats", I, [P, C.c_char_p, C.POINTER(C.c_double), C.POINTER(I64)]),
+    ("sde_ctx_reset_stats", I, [P]),
+    ("sde_ctx_launches", I64, [P]),
     ("sde_weights", I, [P, I, P, F, P, P, P, P, I64, F, F, F, F, I, I, I, I, P, P, P,
                         C.POINTER(WStats)]),
     ("sde_plan_create", I, [P, C.POINTER(GridSpec), I64, P, P, P, P, P, I, C.POINTER(P)]),
@@ -89,6 +93,9 @@ SIGNATURES = [
     ("pixcor2d_", None, [P] * 9 + [C.c_size_t]),
     ("pix2drcl_", None, [P] * 19),
     ("pixisama_", I, [P, P, P]),
+    ("grdsf_", C.c_double, [P]),
+    ("grdcf_", None, [P, P, P, P, C.c_size_t]),
+    ("grdccf_", None, [P, P, P, C.c_size_t]),
     ("errrepor_", None, [P, P, P, C.c_size_t, C.c_size_t, C.c_size_t]),
     ("msgput_", None, [P, P, C.c_size_t, C.c_size_t]),
 ]

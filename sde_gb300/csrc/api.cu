@@ -81,6 +81,8 @@ int fftpwr2(int i) {
 
 // ---------------------------------------------------------------------------------------
 // context
+static void drain_events(sde_ctx *c);
+
 int ctx_alloc(sde_ctx *ctx, void **p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
     if (e != cudaSuccess) {
@@ -187,6 +189,7 @@ extern "C" int sde_ctx_destroy(sde_ctx *c) {
     if (!c) return SDE_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    drain_events(c);
     for (auto &kv : c->scratch)
         if (kv.second.p) cudaFree(kv.second.p);
     for (auto &kv : c->twiddles) cudaFree(kv.second);
@@ -223,6 +226,47 @@ extern "C" int sde_ctx_set_stream(sde_ctx *c, void *stream) {
 }
 
 extern "C" int64_t sde_ctx_bytes_in_use(sde_ctx *c) { return c ? c->bytes : 0; }
+
+static void drain_events(sde_ctx *c) {
+    for (auto &e : c->evq) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
+            auto &k = c->kstats[e.name];
+            k.first += ms;
+            k.second += 1;
+        }
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    c->evq.clear();
+}
+
+extern "C" int sde_ctx_profile(sde_ctx *c, int enable) {
+    if (!c) return SDE_EINVAL;
+    c->profile = enable != 0;
+    return SDE_OK;
+}
+
+extern "C" int sde_ctx_kernel_stats(sde_ctx *c, const char *kernel, double *total_ms, int64_t *count) {
+    if (!c || !kernel) return SDE_EINVAL;
+    SDE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    drain_events(c);
+    auto it = c->kstats.find(kernel);
+    if (total_ms) *total_ms = it == c->kstats.end() ? 0.0 : it->second.first;
+    if (count) *count = it == c->kstats.end() ? 0 : it->second.second;
+    return SDE_OK;
+}
+
+extern "C" int sde_ctx_reset_stats(sde_ctx *c) {
+    if (!c) return SDE_EINVAL;
+    SDE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    drain_events(c);
+    c->kstats.clear();
+    c->nlaunch = 0;
+    return SDE_OK;
+}
+
+extern "C" int64_t sde_ctx_launches(sde_ctx *c) { return c ? c->nlaunch : 0; }
 
 // ---------------------------------------------------------------------------------------
 // plan-level operations
@@ -425,6 +469,47 @@ static void fill_spec(sde_gridspec *s, int nu, int nv, float us, float uo, float
     s->supp = SUPP;
     s->osamp = OSAMP;
     memcpy(s->shift, shift, sizeof s->shift);
+}
+
+// GRDSF / GRDCF / GRDCCF (grd/grdsf.f, grd/grdcf.f, grd/grdccf.f): host-side table
+// builders the callers of the gridder use; 'SF' and 'BOX' codes.
+extern "C" double grdsf_(double *nu) { return sf_grdsf(*nu); }
+
+extern "C" void grdcf_(char *cfcode, float *cf, int *cfsupp, int *cfosamp, size_t len) {
+    if (sysi_.error) return;
+    if (len >= 2 && strncmp(cfcode, "SF", 2) == 0) {
+        sf_cf_table(cf);
+        *cfsupp = SUPP;
+        *cfosamp = OSAMP;
+    } else if (len >= 3 && strncmp(cfcode, "BOX", 3) == 0) {
+        const int osamp = 128, supp = 1, off = (supp + 1) * osamp;
+        for (int i = 0; i <= osamp / 2; i++) cf[off + i] = cf[off - i] = 1.0f;
+        for (int i = osamp / 2 + 1; i <= 2 * osamp; i++) cf[off + i] = cf[off - i] = 0.0f;
+        float sum = 0.0f;
+        for (int i = -(supp + 1) * osamp; i <= (supp + 1) * osamp; i++) sum = sum + cf[off + i];
+        for (int i = -(supp + 1) * osamp; i <= (supp + 1) * osamp; i++) cf[off + i] = cf[off + i] / sum;
+        *cfsupp = supp;
+        *cfosamp = osamp;
+    } else {
+        report("Bad argument", "GRDCF", "Cannot make convolution function");
+    }
+}
+
+extern "C" void grdccf_(char *ccfcode, float *ccf, int *ccflen, size_t len) {
+    if (sysi_.error) return;
+    if (len >= 2 && strncmp(ccfcode, "SF", 2) == 0) {
+        sf_ccf_table(ccf, *ccflen);
+    } else if (len >= 3 && strncmp(ccfcode, "BOX", 3) == 0) {
+        const float PI = 3.141592554f;
+        ccf[0] = 1.0f;
+        for (int i = 2; i <= *ccflen; i++) {
+            double nu = (double)(i - 1) / (double)(*ccflen - 1);
+            float x = 0.5f * PI * (float)nu;
+            ccf[i - 1] = sinf(x) / x;
+        }
+    } else {
+        report("Bad argument", "GRDCCF", "Cannot make convolution correction function");
+    }
 }
 
 extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis,
@@ -685,6 +770,7 @@ extern "C" void pixcor2d_(float *in, int *nx, int *ny, float *cf, int *cflen, ch
     cudaStream_t st = ctx->stream;
     cudaMemcpyAsync(di, in, 4 * npix, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dc, cf, 4 * (size_t)*cflen, cudaMemcpyHostToDevice, st);
+    KTimer kt(ctx, "pixcor2d");
     k_pixcor2d<<<ceil_div((int64_t)npix, 256), 256, 0, st>>>(di, *nx, *ny, dc, correct, di, sx, sy, *cenx, *ceny);
     cudaMemcpyAsync(out, di, 4 * npix, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) {

@@ -288,6 +288,7 @@ int sde_image_max(sde_ctx *ctx, const float *image, int64_t n, float *max_dev) {
     int nb = ctx->num_sms * 2;
     float *part;
     SDE_TRY(ctx_scratch(ctx, "max_part", sizeof(float) * (size_t)nb, (void **)&part));
+    KTimer kt(ctx, "image_max");
     k_max_part<<<nb, CL_THREADS, 0, ctx->stream>>>(image, n, part);
     SDE_CHECK_LAUNCH();
     k_max_final<<<1, 32, 0, ctx->stream>>>(part, nb, max_dev);
@@ -297,6 +298,7 @@ int sde_image_max(sde_ctx *ctx, const float *image, int64_t n, float *max_dev) {
 
 int sde_image_scale_by_inverse(sde_ctx *ctx, float *image, int64_t n, const float *max_dev) {
     if (!ctx || !image || n <= 0 || !max_dev) return SDE_EINVAL;
+    KTimer kt(ctx, "scale_inv");
     k_scale_inv<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(image, n, max_dev);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
@@ -350,6 +352,7 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
     A.nsub = nsub; A.bsub = bsub; A.cancel = cancel_flag; A.partial = partial; A.bar = bar;
     A.status = ctx->d_status; A.out = dout;
     void *args[] = {&A};
+    KTimer kt(ctx, "hogbom");
     SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom, dim3(nblocks), dim3(CL_THREADS),
                                              args, 0, ctx->stream));
     float h[4];

@@ -49,14 +49,18 @@ constexpr int ITEM_MAX = 8192;
 constexpr int CHUNK_MAX = 16;
 constexpr uint32_t KEY_INVALID = 0xFFFFFFFFu;
 
-// per-visibility packed sub-cell offsets: byte0 du_g+64, byte1 dv_g+64 (gridding, FP64
-// cell), byte2 du_d+64, byte3 dv_d+64 (degridding, FP32 cell).  0xFF in byte2 marks a
-// visibility that the degridder handles on its exception path.
-__host__ __device__ inline uint32_t pack_gd(int dug, int dvg, int dud, int dvd) {
-    return (uint32_t)(dug + 64) | ((uint32_t)(dvg + 64) << 8) | ((uint32_t)(dud + 64) << 16) |
-           ((uint32_t)(dvd + 64) << 24);
+// Per-visibility geometry words (sorted order):
+//   gdg (uint16): du_g+64 | (dv_g+64) << 8 -- gridding sub-cell offsets (FP64 cell);
+//   gdd (uint32): du_d+64 | (dv_d+64) << 8 | cell << 16 (12-bit tile-local cell of the
+//                 chunk) | GDD_EXCEPTION -- degridding offsets (FP32 cell); visibilities with
+//                 GDD_EXCEPTION set are handled by the degridder's exception path.
+__host__ __device__ inline uint16_t pack_gdg(int dug, int dvg) {
+    return (uint16_t)((uint32_t)(dug + 64) | ((uint32_t)(dvg + 64) << 8));
 }
-constexpr uint32_t GD_EXCEPTION = 0xFFu << 16;
+__host__ __device__ inline uint32_t pack_gdd(int dud, int dvd, uint32_t cell) {
+    return (uint32_t)(dud + 64) | ((uint32_t)(dvd + 64) << 8) | (cell << 16);
+}
+constexpr uint32_t GDD_EXCEPTION = 1u << 31;
 
 // Exception entries for the degridder: visibilities whose FP32 degridding cell differs
 // from their FP64 gridding cell, that sit within SUPP of the v axis (reflection branch of
@@ -104,6 +108,36 @@ struct sde_ctx {
     std::unordered_map<std::string, DevBuf> scratch;
     std::unordered_map<int, float2 *> twiddles;  // N -> exp(+-2 pi i k/N) table
     CUtensorMap *h_tmap = nullptr;
+    // per-kernel CUDA-event timing (sde_ctx_profile) and launch counting
+    bool profile = false;
+    int64_t nlaunch = 0;
+    struct EvPair {
+        const char *name;
+        cudaEvent_t a, b;
+    };
+    std::vector<EvPair> evq;
+    std::unordered_map<std::string, std::pair<double, int64_t>> kstats;
+};
+
+// Scoped timer around one kernel launch on the context's stream: counts the launch and,
+// when profiling is on, records a CUDA event pair that sde_ctx_kernel_stats resolves.
+struct KTimer {
+    sde_ctx *c;
+    cudaEvent_t b = nullptr;
+    const char *name;
+    KTimer(sde_ctx *ctx, const char *n) : c(ctx), name(n) {
+        c->nlaunch++;
+        if (c->profile) {
+            cudaEvent_t a;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, c->stream);
+            c->evq.push_back({name, a, b});
+        }
+    }
+    ~KTimer() {
+        if (b) cudaEventRecord(b, c->stream);
+    }
 };
 
 enum { STATUS_ERR = 0, STATUS_NOWEIGHT = 1, STATUS_TIMEOUT = 2, STATUS_COUNT = 8 };
@@ -127,7 +161,8 @@ struct sde_plan {
     float2 *fobs = nullptr;   // observed, in the gridding frame (rotated, conjugated)
     float2 *fres = nullptr;   // residual, gridding frame
     float *wt = nullptr;
-    uint32_t *gd = nullptr;   // packed sub-cell offsets
+    uint16_t *gdg = nullptr;  // gridding sub-cell offsets
+    uint32_t *gdd = nullptr;  // degridding offsets + cell + exception flag
     uint32_t *orig = nullptr; // caller index of each sorted visibility
     float2 *rot = nullptr;    // (cos, sin) of the phase rotation (doshift only), sorted
     uint8_t *gconj = nullptr; // gridding-frame conjugation flag, sorted

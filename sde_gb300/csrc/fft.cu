@@ -254,14 +254,18 @@ int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, in
     const int cc = col_cols(nv);
     const size_t smc = sizeof(float2) * (size_t)cc * nv;
     SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
-    k_col_fft<<<ceil_div(nu, cc), FFT_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
-                                                                   ilog2(nv), cc, twv, 1, 0, nv);
+    {
+        KTimer kt(ctx, "col_fft");
+        k_col_fft<<<ceil_div(nu, cc), FFT_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
+                                                                       ilog2(nv), cc, twv, 1, 0, nv);
+    }
     SDE_CHECK_LAUNCH();
     CorrParams cp = {nullptr, 0.f, 0.f, 0.f, 0.f};
     if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
     const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;  // 0-based first grid row
     const size_t smr = sizeof(float2) * (size_t)(fnu / 2);
     SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+    KTimer kt(ctx, "row_c2r");
     k_row_c2r<<<ny, FFT_THREADS, smr, ctx->stream>>>((const float2 *)grid, pitch, fnu,
                                                      ilog2(fnu / 2), nx, ny, ibegy, twu, cp,
                                                      scale_dev, image);
@@ -283,12 +287,16 @@ int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fn
     const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;
     const size_t smr = sizeof(float2) * (size_t)(fnu / 2);
     SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
-    k_row_r2c<<<ny, FFT_THREADS, smr, ctx->stream>>>(image, nx, ny, fnu, ilog2(fnu / 2), ibegy, twu,
-                                                     cp, (float2 *)grid, pitch, nu);
+    {
+        KTimer kt(ctx, "row_r2c");
+        k_row_r2c<<<ny, FFT_THREADS, smr, ctx->stream>>>(image, nx, ny, fnu, ilog2(fnu / 2), ibegy,
+                                                         twu, cp, (float2 *)grid, pitch, nu);
+    }
     SDE_CHECK_LAUNCH();
     const int cc = col_cols(nv);
     const size_t smc = sizeof(float2) * (size_t)cc * nv;
     SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
+    KTimer kt(ctx, "col_fft");
     k_col_fft<<<ceil_div(nu, cc), FFT_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
                                                                    ilog2(nv), cc, twv, 0, ibegy,
                                                                    ibegy + ny);

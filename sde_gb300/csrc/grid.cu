@@ -17,75 +17,86 @@
 
 namespace {
 
-constexpr int GRID_THREADS = 128;
+constexpr int GRID_THREADS = 256;
+constexpr int GLANES = 4;                          // lanes per chunk
+constexpr int GGROUPS = GRID_THREADS / GLANES;     // chunks in flight per CTA
 constexpr int CFT_FLOATS = 129 * 8;
 
-// ---------------------------------------------------------------------------------------
+// Gridding.  Lane q of a 4-lane group owns footprint columns q and q+4 (q+4 = 7 is empty)
+// of its chunk's cell and accumulates 7 rows x 2 columns x complex in registers; the chunk's
+// visibilities are read once per group (same addresses: L1 broadcast).  The shared tile
+// receives each chunk's footprint once, through shared-memory atomics (a warp's 8 chunks
+// share a colour class, so their footprints do not overlap).
 template <bool PSF>
-__global__ void __launch_bounds__(GRID_THREADS, 3)
+__global__ void __launch_bounds__(GRID_THREADS, 4)
     k_grid(const WorkItem *__restrict__ items, const uint2 *__restrict__ chunks,
            const float2 *__restrict__ fres, const float *__restrict__ wt,
-           const uint32_t *__restrict__ gd, const float *__restrict__ cft_g, float2 *raw,
+           const uint16_t *__restrict__ gdg, const float *__restrict__ cft_g, float2 *raw,
            int pitch, int ntu, int nu, int nv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *tile = reinterpret_cast<float2 *>(smem_raw);
-    float *cft = reinterpret_cast<float *>(tile + STILE * STILE);
+    float *cft = reinterpret_cast<float *>(tile + STILE * STILE);   // [129][8] rows (v taps)
+    float2 *cfp = reinterpret_cast<float2 *>(cft + CFT_FLOATS);     // [129][4] (col q, col q+4)
     const WorkItem it = items[blockIdx.x];
     for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) tile[k] = make_float2(0.f, 0.f);
     for (int k = threadIdx.x; k < CFT_FLOATS; k += GRID_THREADS) cft[k] = cft_g[k];
+    for (int k = threadIdx.x; k < 129 * 4; k += GRID_THREADS) {
+        const int d = k >> 2, q = k & 3;
+        cfp[k] = make_float2(cft_g[d * 8 + q], q + 4 < NTAP ? cft_g[d * 8 + q + 4] : 0.f);
+    }
     __syncthreads();
-    for (int c = it.cbeg + threadIdx.x; c < it.cend; c += GRID_THREADS) {
+    const int q = threadIdx.x & (GLANES - 1);
+    const int grp = threadIdx.x / GLANES;
+    for (int c = it.cbeg + grp; c < it.cend; c += GGROUPS) {
         const uint2 ch = chunks[c];
         const int start = (int)ch.x, cell = (int)(ch.y & 4095u), len = (int)(ch.y >> 16);
         const int lu = cell & 63, lv = cell >> 6;
-        float ar[NTAP][NTAP];
-        float ai[NTAP][NTAP];
+        float a0r[NTAP], a0i[NTAP], a1r[NTAP], a1i[NTAP];
 #pragma unroll
-        for (int b = 0; b < NTAP; b++)
-#pragma unroll
-            for (int a = 0; a < NTAP; a++) {
-                ar[b][a] = 0.f;
-                if (!PSF) ai[b][a] = 0.f;
+        for (int b = 0; b < NTAP; b++) {
+            a0r[b] = 0.f;
+            a1r[b] = 0.f;
+            if (!PSF) {
+                a0i[b] = 0.f;
+                a1i[b] = 0.f;
             }
+        }
         for (int k = 0; k < len; k++) {
             const int p = start + k;
-            const uint32_t g = gd[p];
+            const uint32_t g = gdg[p];
             const float w = wt[p];
-            const float4 *gu4 = reinterpret_cast<const float4 *>(cft + (g & 0xFFu) * 8);
-            const float4 *gv4 = reinterpret_cast<const float4 *>(cft + ((g >> 8) & 0xFFu) * 8);
-            const float4 u0 = gu4[0], u1 = gu4[1], v0 = gv4[0], v1 = gv4[1];
-            const float gu[NTAP] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z};
+            const float2 gu = cfp[(g & 0xFFu) * 4 + q];
+            const float4 *gv4 = reinterpret_cast<const float4 *>(cft + (g >> 8) * 8);
+            const float4 v0 = gv4[0], v1 = gv4[1];
             const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
-            float fr, fi = 0.f;
-            if (PSF) {
-                fr = w;
-            } else {
+            float fr = w, fi = 0.f;
+            if (!PSF) {
                 const float2 f = fres[p];
                 fr = w * f.x;
                 fi = w * f.y;
             }
-            float hr[NTAP], hi[NTAP];
+            const float h0r = gu.x * fr, h1r = gu.y * fr;
+            const float h0i = gu.x * fi, h1i = gu.y * fi;
 #pragma unroll
-            for (int a = 0; a < NTAP; a++) {
-                hr[a] = gu[a] * fr;
-                if (!PSF) hi[a] = gu[a] * fi;
-            }
-#pragma unroll
-            for (int b = 0; b < NTAP; b++)
-#pragma unroll
-                for (int a = 0; a < NTAP; a++) {
-                    ar[b][a] = fmaf(gv[b], hr[a], ar[b][a]);
-                    if (!PSF) ai[b][a] = fmaf(gv[b], hi[a], ai[b][a]);
+            for (int b = 0; b < NTAP; b++) {
+                a0r[b] = fmaf(gv[b], h0r, a0r[b]);
+                a1r[b] = fmaf(gv[b], h1r, a1r[b]);
+                if (!PSF) {
+                    a0i[b] = fmaf(gv[b], h0i, a0i[b]);
+                    a1i[b] = fmaf(gv[b], h1i, a1i[b]);
                 }
+            }
         }
 #pragma unroll
-        for (int b = 0; b < NTAP; b++)
-#pragma unroll
-            for (int a = 0; a < NTAP; a++) {
-                float2 *dst = &tile[(lv + b) * STILE + lu + a];
-                atomicAdd(&dst->x, ar[b][a]);
-                if (!PSF) atomicAdd(&dst->y, ai[b][a]);
+        for (int b = 0; b < NTAP; b++) {
+            float2 *row = &tile[(lv + b) * STILE + lu];
+            atomicAdd(&row[q].x, a0r[b]);
+            if (!PSF) atomicAdd(&row[q].y, a0i[b]);
+            if (q + 4 < NTAP) {
+                atomicAdd(&row[q + 4].x, a1r[b]);
+                if (!PSF) atomicAdd(&row[q + 4].y, a1i[b]);
             }
+        }
     }
     __syncthreads();
     const int tu = it.tile % ntu, tv = it.tile / ntu;
@@ -102,13 +113,13 @@ __global__ void __launch_bounds__(GRID_THREADS, 3)
 // Plan-invariant sums: LSUMWT = sum of UVWT (grd/grdh2d.f:185) and SUMWT (grd/grdh2d.f:157).
 constexpr int RED_T = 256;
 __global__ void __launch_bounds__(RED_T) k_plan_sums(const float *__restrict__ wt,
-                                                      const uint32_t *__restrict__ gd,
+                                                      const uint16_t *__restrict__ gdg,
                                                       const float *__restrict__ cft, int64_t n,
                                                       double *partial) {
     __shared__ double sh[2][RED_T / 32];
     double s0 = 0.0, s1 = 0.0;
     for (int64_t p = (int64_t)blockIdx.x * RED_T + threadIdx.x; p < n; p += (int64_t)gridDim.x * RED_T) {
-        const uint32_t g = gd[p];
+        const uint32_t g = gdg[p];
         const float *gu = cft + (g & 0xFFu) * 8, *gv = cft + ((g >> 8) & 0xFFu) * 8;
         float su = 0.f, sv = 0.f;
 #pragma unroll
@@ -198,7 +209,7 @@ __global__ void k_finalize(const float2 *__restrict__ raw, float2 *__restrict__ 
 
 // ---------------------------------------------------------------------------------------
 // Degridding.
-constexpr int DG_THREADS = 128;
+constexpr int DG_THREADS = 256;
 constexpr int DG_TILE_FLOATS = STILE * STILE * 2;  // 9800 floats, 39200 B
 constexpr uint32_t DG_TX_BYTES = DG_TILE_FLOATS * 4;
 
@@ -207,14 +218,15 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
 }
 
 // mode 0: residual update in the gridding frame; mode 1: caller-order output (user frame).
+// One thread per visibility of the item (coalesced loads); the 7x7 neighbourhood of its
+// cell is read from the TMA-staged tile, interpolated separably: sum_b gv[b] sum_a gu[a] G.
 template <int MODE>
-__global__ void __launch_bounds__(DG_THREADS, 3)
+__global__ void __launch_bounds__(DG_THREADS, 4)
     k_degrid(const __grid_constant__ CUtensorMap tmap, const WorkItem *__restrict__ items,
-             const uint2 *__restrict__ chunks, const uint32_t *__restrict__ gd,
-             const float *__restrict__ cft_g, const float2 *__restrict__ fobs, float2 *fres,
-             const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
-             const uint32_t *__restrict__ orig, const float *__restrict__ wt, float2 *vis_out,
-             float *wt_out, int ntu, int *status) {
+             const uint32_t *__restrict__ gdd, const float *__restrict__ cft_g,
+             const float2 *__restrict__ fobs, float2 *fres, const uint8_t *__restrict__ gconj,
+             const float2 *__restrict__ rot, const uint32_t *__restrict__ orig,
+             const float *__restrict__ wt, float2 *vis_out, float *wt_out, int ntu, int *status) {
     extern __shared__ __align__(128) unsigned char smem_dg[];
     float2 *tile = reinterpret_cast<float2 *>(smem_dg);
     float *cft = reinterpret_cast<float *>(smem_dg + DG_TX_BYTES);
@@ -239,7 +251,6 @@ __global__ void __launch_bounds__(DG_THREADS, 3)
             : "memory");
     }
     for (int k = threadIdx.x; k < CFT_FLOATS; k += DG_THREADS) cft[k] = cft_g[k];
-    // bounded wait on phase 0 of the barrier
     {
         uint32_t done = 0;
         for (int spin = 0; spin < (1 << 24) && !done; spin++) {
@@ -256,55 +267,46 @@ __global__ void __launch_bounds__(DG_THREADS, 3)
         }
     }
     __syncthreads();
-    for (int c = it.cbeg + threadIdx.x; c < it.cend; c += DG_THREADS) {
-        const uint2 ch = chunks[c];
-        const int start = (int)ch.x, cell = (int)(ch.y & 4095u), len = (int)(ch.y >> 16);
-        const int lu = cell & 63, lv = cell >> 6;
-        float2 G[NTAP][NTAP];
+    for (int p = it.vbeg + threadIdx.x; p < it.vend; p += DG_THREADS) {
+        const uint32_t g = gdd[p];
+        if (g & GDD_EXCEPTION) continue;
+        const int cell = (int)((g >> 16) & 4095u), lu = cell & 63, lv = cell >> 6;
+        const float4 *gu4 = reinterpret_cast<const float4 *>(cft + (g & 0xFFu) * 8);
+        const float4 *gv4 = reinterpret_cast<const float4 *>(cft + ((g >> 8) & 0xFFu) * 8);
+        const float4 u0 = gu4[0], u1 = gu4[1], v0 = gv4[0], v1 = gv4[1];
+        const float gu[NTAP] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z};
+        const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
+        float rr = 0.f, ri = 0.f, su = 0.f, sv = 0.f;
 #pragma unroll
-        for (int b = 0; b < NTAP; b++)
+        for (int b = 0; b < NTAP; b++) {
+            const float2 *row = &tile[(lv + b) * STILE + lu];
+            float tr = 0.f, ti = 0.f;
 #pragma unroll
-            for (int a = 0; a < NTAP; a++) G[b][a] = tile[(lv + b) * STILE + lu + a];
-        for (int k = 0; k < len; k++) {
-            const int p = start + k;
-            const uint32_t g = gd[p];
-            if ((g & GD_EXCEPTION) == GD_EXCEPTION) continue;
-            const float4 *gu4 = reinterpret_cast<const float4 *>(cft + ((g >> 16) & 0xFFu) * 8);
-            const float4 *gv4 = reinterpret_cast<const float4 *>(cft + (g >> 24) * 8);
-            const float4 u0 = gu4[0], u1 = gu4[1], v0 = gv4[0], v1 = gv4[1];
-            const float gu[NTAP] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z};
-            const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
-            float rr = 0.f, ri = 0.f, su = 0.f, sv = 0.f;
-#pragma unroll
-            for (int b = 0; b < NTAP; b++) {
-                float tr = 0.f, ti = 0.f;
-#pragma unroll
-                for (int a = 0; a < NTAP; a++) {
-                    tr = fmaf(gu[a], G[b][a].x, tr);
-                    ti = fmaf(gu[a], G[b][a].y, ti);
-                }
-                rr = fmaf(gv[b], tr, rr);
-                ri = fmaf(gv[b], ti, ri);
-                sv += gv[b];
-                su += gu[b];
+            for (int a = 0; a < NTAP; a++) {
+                const float2 G = row[a];
+                tr = fmaf(gu[a], G.x, tr);
+                ti = fmaf(gu[a], G.y, ti);
             }
-            const float sw = su * sv;
-            const float inv = 1.0f / sw;
-            float mr = rr * inv, mi = ri * inv;
-            if (MODE == 0) {
-                const float2 o = fobs[p];
-                fres[p] = make_float2(o.x - mr, o.y - mi);
-            } else {
-                if (gconj[p]) mi = -mi;
-                float2 vv = make_float2(mr, mi);
-                if (rot) {
-                    const float2 rt = rot[p];
-                    vv = make_float2(mr * rt.x - mi * rt.y, mr * rt.y + mi * rt.x);
-                }
-                const uint32_t o = orig[p];
-                vis_out[o] = vv;
-                wt_out[o] = wt[p];
+            rr = fmaf(gv[b], tr, rr);
+            ri = fmaf(gv[b], ti, ri);
+            sv += gv[b];
+            su += gu[b];
+        }
+        const float inv = 1.0f / (su * sv);
+        float mr = rr * inv, mi = ri * inv;
+        if (MODE == 0) {
+            const float2 o = fobs[p];
+            fres[p] = make_float2(o.x - mr, o.y - mi);
+        } else {
+            if (gconj[p]) mi = -mi;
+            float2 vv = make_float2(mr, mi);
+            if (rot) {
+                const float2 rt = rot[p];
+                vv = make_float2(mr * rt.x - mi * rt.y, mr * rt.y + mi * rt.x);
             }
+            const uint32_t o = orig[p];
+            vis_out[o] = vv;
+            wt_out[o] = wt[p];
         }
     }
 }
@@ -478,7 +480,7 @@ int make_grid_tmap(CUtensorMap *map, const float *grid, int pitch, int nv) {
     return SDE_OK;
 }
 
-size_t grid_smem() { return sizeof(float2) * STILE * STILE + sizeof(float) * CFT_FLOATS; }
+size_t grid_smem() { return sizeof(float2) * STILE * STILE + sizeof(float) * CFT_FLOATS + sizeof(float2) * 129 * 4; }
 size_t degrid_smem() { return DG_TX_BYTES + sizeof(float) * CFT_FLOATS + 16; }
 
 }  // namespace
@@ -507,7 +509,8 @@ int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt) {
     int nb = ctx->num_sms * 4;
     double *part;
     SDE_TRY(ctx_scratch(ctx, "gs_part", sizeof(double) * 2 * (size_t)nb, (void **)&part));
-    k_plan_sums<<<nb, RED_T, 0, ctx->stream>>>(pl->wt, pl->gd, pl->cft, pl->nvis, part);
+    KTimer kt(ctx, "plan_sums");
+    k_plan_sums<<<nb, RED_T, 0, ctx->stream>>>(pl->wt, pl->gdg, pl->cft, pl->nvis, part);
     SDE_CHECK_LAUNCH();
     k_sum_pairs<<<1, 32, 0, ctx->stream>>>(part, nb, pl->d_sums);
     SDE_CHECK_LAUNCH();
@@ -522,6 +525,7 @@ int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt) {
 int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, float2 *out, int nu, int nv, int pitch,
                         int uorigin, int vorigin, int supp, float scale) {
     int64_t n = (int64_t)nv * pitch;
+    KTimer kt(ctx, "finalize");
     k_finalize<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(raw, out, nu, nv, pitch, uorigin,
                                                           vorigin, supp, scale);
     SDE_CHECK_LAUNCH();
@@ -541,12 +545,13 @@ int plan_grid_raw(sde_plan *pl, int what, float2 *raw) {
                                           (int)grid_smem()));
         attr = true;
     }
+    KTimer kt(ctx, what == SDE_GRID_PSF ? "grid_psf" : "grid");
     if (what == SDE_GRID_PSF)
         k_grid<true><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
-            pl->items, pl->chunks, pl->fres, pl->wt, pl->gd, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+            pl->items, pl->chunks, pl->fres, pl->wt, pl->gdg, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
     else
         k_grid<false><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
-            pl->items, pl->chunks, pl->fres, pl->wt, pl->gd, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+            pl->items, pl->chunks, pl->fres, pl->wt, pl->gdg, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
@@ -567,14 +572,15 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
     if (pl->nitems > 0) {
         CUtensorMap map;
         SDE_TRY(make_grid_tmap(&map, grid, pitch, nv));
+        KTimer kt(ctx, "degrid");
         if (mode == 0)
             k_degrid<0><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->chunks, pl->gd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot,
-                pl->orig, pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
+                map, pl->items, pl->gdd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot, pl->orig,
+                pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
         else
             k_degrid<1><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->chunks, pl->gd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot,
-                pl->orig, pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
+                map, pl->items, pl->gdd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot, pl->orig,
+                pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
         SDE_CHECK_LAUNCH();
     }
     if (pl->nexc > 0) {
@@ -582,6 +588,7 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
         const float *exc_wt = (const float *)((const char *)pl->exc + exc_wt_off(ne1));
         const float2 *exc_rot = (const float2 *)((const char *)pl->exc + exc_rot_off(ne1));
         const int T = 128;
+        KTimer kt(ctx, "degrid_exc");
         if (mode == 0)
             k_degrid_exc<0><<<ceil_div(pl->nexc, T), T, 0, ctx->stream>>>(
                 pl->exc, exc_wt, exc_rot, pl->nexc, (const float2 *)grid, pitch, nu, nv,
@@ -599,6 +606,7 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
 
 int plan_scatter_residual(sde_plan *pl, float2 *dst) {
     if (pl->nvis == 0) return SDE_OK;
+    KTimer kt(pl->ctx, "scatter_vis");
     k_scatter_vis<<<ceil_div(pl->nvis, 256), 256, 0, pl->ctx->stream>>>(
         pl->fres, pl->orig, pl->gconj, pl->rot, pl->nvis, dst);
     SDE_CHECK_LAUNCH();
@@ -607,6 +615,7 @@ int plan_scatter_residual(sde_plan *pl, float2 *dst) {
 
 int plan_set_vis_dev(sde_plan *pl, const float2 *vis_user) {
     if (pl->nvis == 0) return SDE_OK;
+    KTimer kt(pl->ctx, "set_vis");
     k_set_vis<<<ceil_div(pl->nvis, 256), 256, 0, pl->ctx->stream>>>(vis_user, pl->orig, pl->gconj,
                                                                   pl->rot, pl->nvis, pl->fobs,
                                                                   pl->fres);

@@ -62,13 +62,14 @@ __device__ __forceinline__ DGeo degrid_geom(const GParams &p, float u, float v, 
 __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float *__restrict__ v,
                             const float *__restrict__ w, const float2 *__restrict__ vis,
                             const float *__restrict__ wt, int64_t n, uint32_t *keys,
-                            uint32_t *vals, uint32_t *gd, float2 *fobs, float2 *rot,
-                            uint8_t *gconj, unsigned long long *counts) {
+                            uint32_t *vals, uint16_t *gdg, uint32_t *gdd, float2 *fobs,
+                            float2 *rot, uint8_t *gconj, unsigned long long *counts) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t nvalid = 0, nexc = 0;
     if (i < n) {
         float wi = wt[i];
-        uint32_t key = KEY_INVALID, packed = 0;
+        uint32_t key = KEY_INVALID, pdd = 0;
+        uint16_t pdg = 0;
         float2 f = make_float2(0.f, 0.f), r = make_float2(1.f, 0.f);
         uint8_t gc = 0;
         if (wi > 0.0f) {
@@ -114,8 +115,9 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
                 key = ((uint32_t)(tv * p.ntu + tu) << 12) | ((uint32_t)lv << 6) | (uint32_t)lu;
                 bool exc = !dg.valid || dg.nud != nuc || dg.nvd != nvc || dg.nud <= p.supp ||
                            dg.conj != (gc != 0);
-                packed = exc ? (pack_gd(dug, dvg, 0, 0) & 0x0000FFFFu) | GD_EXCEPTION
-                             : pack_gd(dug, dvg, dg.dui, dg.dvi);
+                const uint32_t cell = ((uint32_t)lv << 6) | (uint32_t)lu;
+                pdg = pack_gdg(dug, dvg);
+                pdd = exc ? (pack_gdd(0, 0, cell) | GDD_EXCEPTION) : pack_gdd(dg.dui, dg.dvi, cell);
                 nvalid = 1;
                 nexc = exc;
                 f = make_float2(fr, fi);
@@ -125,7 +127,8 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
         }
         keys[i] = key;
         vals[i] = (uint32_t)i;
-        gd[i] = packed;
+        gdg[i] = pdg;
+        gdd[i] = pdd;
         fobs[i] = f;
         if (rot) rot[i] = r;
         gconj[i] = gc;
@@ -140,10 +143,11 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
 // Gather the per-visibility arrays into sorted order.
 __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned long long *counts,
                               const float2 *__restrict__ fobs_u, const float *__restrict__ wt_u,
-                              const uint32_t *__restrict__ gd_u, const float2 *__restrict__ rot_u,
+                              const uint16_t *__restrict__ gdg_u, const uint32_t *__restrict__ gdd_u,
+                              const float2 *__restrict__ rot_u,
                               const uint8_t *__restrict__ gconj_u, float2 *fobs, float2 *fres,
-                              float *wt, uint32_t *gd, uint32_t *orig, float2 *rot, uint8_t *gconj,
-                              uint32_t *pos_of) {
+                              float *wt, uint16_t *gdg, uint32_t *gdd, uint32_t *orig, float2 *rot,
+                              uint8_t *gconj, uint32_t *pos_of) {
     int64_t nv = (int64_t)counts[0];
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
@@ -152,7 +156,8 @@ __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned 
     fobs[p] = f;
     fres[p] = f;
     wt[p] = wt_u[i];
-    gd[p] = gd_u[i];
+    gdg[p] = gdg_u[i];
+    gdd[p] = gdd_u[i];
     orig[p] = i;
     gconj[p] = gconj_u[i];
     if (rot) rot[p] = rot_u[i];
@@ -161,11 +166,11 @@ __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned 
 
 // flags for the exception compaction
 __global__ void k_exc_flag(const float *__restrict__ wt, const uint32_t *__restrict__ keys_u,
-                           const uint32_t *__restrict__ gd_u, int64_t n, uint32_t *flag) {
+                           const uint32_t *__restrict__ gdd_u, int64_t n, uint32_t *flag) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t f = 0;
-    if (wt[i] > 0.0f) f = (keys_u[i] == KEY_INVALID) || ((gd_u[i] & GD_EXCEPTION) == GD_EXCEPTION);
+    if (wt[i] > 0.0f) f = (keys_u[i] == KEY_INVALID) || ((gdd_u[i] & GDD_EXCEPTION) != 0);
     flag[i] = f;
 }
 
@@ -301,7 +306,7 @@ int sde_plan_destroy(sde_plan *pl) {
     sde_ctx *ctx = pl->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    void *ptrs[] = {pl->fobs, pl->fres, pl->wt, pl->gd, pl->orig, pl->rot, pl->gconj, pl->chunks,
+    void *ptrs[] = {pl->fobs, pl->fres, pl->wt, pl->gdg, pl->gdd, pl->orig, pl->rot, pl->gconj, pl->chunks,
                     pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -382,7 +387,8 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
         gp.ntu = pl->ntu;
         gp.twopi = (double)(8.0f * atanf(1.0f));  // TWOPI = 8 * ATAN(1.0), REAL (grdh2d.f:91)
 
-        uint32_t *keys, *vals, *ktmp, *vtmp, *gd_u, *pos_of;
+        uint32_t *keys, *vals, *ktmp, *vtmp, *gdd_u, *pos_of;
+        uint16_t *gdg_u;
         float2 *fobs_u, *rot_u = nullptr;
         uint8_t *gconj_u;
         unsigned long long *counts;
@@ -390,7 +396,8 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
         PL_TRY(ctx_scratch(ctx, "pl_vals", 4 * n, (void **)&vals));
         PL_TRY(ctx_scratch(ctx, "pl_ktmp", 4 * n, (void **)&ktmp));
         PL_TRY(ctx_scratch(ctx, "pl_vtmp", 4 * n, (void **)&vtmp));
-        PL_TRY(ctx_scratch(ctx, "pl_gd", 4 * n, (void **)&gd_u));
+        PL_TRY(ctx_scratch(ctx, "pl_gdg", 2 * n, (void **)&gdg_u));
+        PL_TRY(ctx_scratch(ctx, "pl_gdd", 4 * n, (void **)&gdd_u));
         PL_TRY(ctx_scratch(ctx, "pl_pos", 4 * n, (void **)&pos_of));
         PL_TRY(ctx_scratch(ctx, "pl_fobs", 8 * n, (void **)&fobs_u));
         if (pl->doshift) PL_TRY(ctx_scratch(ctx, "pl_rot", 8 * n, (void **)&rot_u));
@@ -400,7 +407,7 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
         const int T = 256;
         if (nvis > 0) {
             k_plan_geom<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dvis, dwt, nvis, keys, vals,
-                                                       gd_u, fobs_u, rot_u, gconj_u, counts);
+                                                       gdg_u, gdd_u, fobs_u, rot_u, gconj_u, counts);
             PL_CUDA(cudaGetLastError());
         }
         // The user-order keys are needed again by the exception pass: keep a copy.
@@ -425,16 +432,17 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
         PL_TRY(plan_alloc(pl, (void **)&pl->fobs, 8 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->fres, 8 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->wt, 4 * nv1));
-        PL_TRY(plan_alloc(pl, (void **)&pl->gd, 4 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->gdg, 2 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->gdd, 4 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->orig, 4 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->gconj, nv1));
         if (pl->doshift) PL_TRY(plan_alloc(pl, (void **)&pl->rot, 8 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->d_sums, 4 * sizeof(double)));
         if (nvalid > 0) {
-            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, fobs_u, dwt, gd_u, rot_u,
-                                                           gconj_u, pl->fobs, pl->fres, pl->wt,
-                                                           pl->gd, pl->orig, pl->rot, pl->gconj,
-                                                           pos_of);
+            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, fobs_u, dwt, gdg_u, gdd_u,
+                                                           rot_u, gconj_u, pl->fobs, pl->fres,
+                                                           pl->wt, pl->gdg, pl->gdd, pl->orig,
+                                                           pl->rot, pl->gconj, pos_of);
             PL_CUDA(cudaGetLastError());
         }
         // exception list (also carries the GRDDEH2D geometry of non-gridding visibilities)
@@ -444,7 +452,7 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
             uint32_t *flag, *slot;
             PL_TRY(ctx_scratch(ctx, "pl_flag", 4 * n, (void **)&flag));
             PL_TRY(ctx_scratch(ctx, "pl_slot", 4 * n, (void **)&slot));
-            k_exc_flag<<<ceil_div(nvis, T), T, 0, st>>>(dwt, keys_u, gd_u, nvis, flag);
+            k_exc_flag<<<ceil_div(nvis, T), T, 0, st>>>(dwt, keys_u, gdd_u, nvis, flag);
             PL_CUDA(cudaGetLastError());
             PL_TRY(launch_exclusive_scan_u32(ctx, flag, slot, nvis, nullptr));
             float *exc_wt = (float *)((char *)pl->exc + exc_wt_off(ne1));
