@@ -122,7 +122,7 @@ int ctx_twiddles(sde_ctx *ctx, int n, const float2 **out) {
         *out = it->second;
         return SDE_OK;
     }
-    int h = n / 2 > 0 ? n / 2 : 1;
+    int h = n > 0 ? n : 1;  // full period: exp(+2 pi i k/n), k < n
     std::vector<float2> t((size_t)h);
     for (int k = 0; k < h; k++) {
         double a = 2.0 * M_PI * (double)k / (double)n;

@@ -25,98 +25,244 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-__device__ __forceinline__ unsigned brev(unsigned k, int logn) {
-    return logn == 0 ? 0u : (__brev(k) >> (32 - logn));
+// ---- register-resident radix-2/4/8/16 DFTs --------------------------------------------
+// dft<R, INV>(v): v[k] <- sum_r v[r] w^(rk), w = exp(-2 pi i/R) (forward) or exp(+2 pi i/R).
+template <bool INV>
+__device__ __forceinline__ float2 mul_mi(float2 a) {  // a * (-i) forward, a * (+i) inverse
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+template <bool INV>
+__device__ __forceinline__ void dft2(float2 &a, float2 &b) {
+    const float2 t = a;
+    a = make_float2(t.x + b.x, t.y + b.y);
+    b = make_float2(t.x - b.x, t.y - b.y);
+}
+template <bool INV>
+__device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 &v3) {
+    float2 a0 = make_float2(v0.x + v2.x, v0.y + v2.y), a1 = make_float2(v0.x - v2.x, v0.y - v2.y);
+    float2 a2 = make_float2(v1.x + v3.x, v1.y + v3.y), a3 = mul_mi<INV>(make_float2(v1.x - v3.x, v1.y - v3.y));
+    v0 = make_float2(a0.x + a2.x, a0.y + a2.y);
+    v2 = make_float2(a0.x - a2.x, a0.y - a2.y);
+    v1 = make_float2(a1.x + a3.x, a1.y + a3.y);
+    v3 = make_float2(a1.x - a3.x, a1.y - a3.y);
+}
+// constant twiddles exp(-+2 pi i m/16), m = 0..15, used inside dft8/dft16
+__device__ __forceinline__ float2 w16(int m, bool inv) {
+    const float c[4] = {1.0f, 0.92387953251128674f, 0.70710678118654752f, 0.38268343236508977f};
+    m &= 15;
+    float re, im;  // exp(-2 pi i m/16)
+    const int q = m >> 2, r = m & 3;
+    float cr = c[r], sr = r ? c[4 - r] : 0.0f;  // cos, sin of 2 pi r/16
+    // rotate by -q*pi/2
+    switch (q) {
+        case 0: re = cr; im = -sr; break;
+        case 1: re = -sr; im = -cr; break;
+        case 2: re = -cr; im = sr; break;
+        default: re = sr; im = cr; break;
+    }
+    return make_float2(re, inv ? -im : im);
+}
+template <bool INV>
+__device__ __forceinline__ void dft8(float2 *v) {
+    // r = r1 + 4 r2 (r1 < 4, r2 < 2); k = 2 k1 + k2
+#pragma unroll
+    for (int r1 = 0; r1 < 4; r1++) dft2<INV>(v[r1], v[r1 + 4]);  // -> Y[r1][k2] at v[r1 + 4 k2]
+#pragma unroll
+    for (int r1 = 1; r1 < 4; r1++) v[r1 + 4] = cmul(v[r1 + 4], w16(2 * r1, INV));  // w8^(r1 k2)
+    dft4<INV>(v[0], v[1], v[2], v[3]);
+    dft4<INV>(v[4], v[5], v[6], v[7]);
+    // X[2 k1 + k2] = v[k1 + 4 k2]
+    float2 t[8];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++)
+#pragma unroll
+        for (int k2 = 0; k2 < 2; k2++) t[2 * k1 + k2] = v[k1 + 4 * k2];
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = t[k];
+}
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 *v) {
+    // r = r1 + 4 r2; k = 4 k1 + k2
+#pragma unroll
+    for (int r1 = 0; r1 < 4; r1++) dft4<INV>(v[r1], v[r1 + 4], v[r1 + 8], v[r1 + 12]);
+#pragma unroll
+    for (int r1 = 1; r1 < 4; r1++)
+#pragma unroll
+        for (int k2 = 1; k2 < 4; k2++) v[r1 + 4 * k2] = cmul(v[r1 + 4 * k2], w16(r1 * k2, INV));
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) dft4<INV>(v[4 * k2], v[4 * k2 + 1], v[4 * k2 + 2], v[4 * k2 + 3]);
+    float2 t[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; k2++) t[4 * k1 + k2] = v[k1 + 4 * k2];
+#pragma unroll
+    for (int k = 0; k < 16; k++) v[k] = t[k];
+}
+template <int R, bool INV>
+__device__ __forceinline__ void dftR(float2 *v) {
+    if (R == 16) dft16<INV>(v);
+    else if (R == 8) dft8<INV>(v);
+    else if (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+    else dft2<INV>(v[0], v[1]);
 }
 
-// In-place radix-2 DIT over `ncol` independent transforms of length n stored back to back
-// in s (each already in bit-reversed order).  tw[k*tws] = exp(+2 pi i k/n) for k < n/2.
-__device__ void block_fft(float2 *s, int n, int logn, int ncol, const float2 *__restrict__ tw,
-                          int tws, bool inverse) {
-    const int half = n >> 1;
-    const int total = half * ncol;
-    for (int st = 0; st < logn; st++) {
-        const int h = 1 << st;
-        const int step = half >> st;  // W_{2h}^j = W_n^{j n/(2h)}
-        for (int b = threadIdx.x; b < total; b += blockDim.x) {
-            const int col = b / half, bb = b - col * half;
-            const int j = bb & (h - 1);
-            const int i = ((bb >> st) << (st + 1)) + j;
-            float2 w = __ldg(&tw[(size_t)j * step * tws]);
-            if (!inverse) w.y = -w.y;
-            float2 *base = s + (size_t)col * n;
-            const float2 x = base[i], y = base[i + h];
-            const float2 t = cmul(y, w);
-            base[i] = make_float2(x.x + t.x, x.y + t.y);
-            base[i + h] = make_float2(x.x - t.x, x.y - t.y);
+// Shared-memory index of element i of a transform: an XOR swizzle of the low four bits by
+// bits 4..7 spreads the stride-16 stores of the first radix-16 pass over all banks.
+__device__ __forceinline__ int swz(int i) { return i ^ ((i >> 4) & 15); }
+
+// One Stockham pass of radix R over `ncol` transforms of length n = 2^logn stored back to
+// back in s (in place: every thread loads its R inputs, barrier, stores its R outputs,
+// barrier).  tw[t*tws] = exp(+2 pi i t/n), t < n (double-precision table rounded to float).
+template <int R, int LOGR, bool INV>
+__device__ __forceinline__ void stockham_pass(float2 *s, int logn, int logns, int ncol,
+                                              const float2 *__restrict__ tw, int tws) {
+    const int lognb = logn - LOGR, nb = 1 << lognb, ns = 1 << logns;
+    const int total = nb * ncol;
+    const int tshift = logn - logns - LOGR;  // t = jm * r * n/(ns R)
+    for (int base = 0; base < total; base += blockDim.x) {
+        const int b = base + threadIdx.x;
+        float2 v[R];
+        int col = 0, j = 0;
+        if (b < total) {
+            col = b >> lognb;
+            j = b & (nb - 1);
+            const float2 *src = s + ((size_t)col << logn);
+#pragma unroll
+            for (int r = 0; r < R; r++) v[r] = src[swz(j + r * nb)];
+        }
+        __syncthreads();
+        if (b < total) {
+            const int jm = j & (ns - 1);
+            if (jm) {
+#pragma unroll
+                for (int r = 1; r < R; r++) {
+                    float2 w = __ldg(&tw[(size_t)((jm * r) << tshift) * tws]);
+                    if (!INV) w.y = -w.y;
+                    v[r] = cmul(v[r], w);
+                }
+            }
+            dftR<R, INV>(v);
+            float2 *dst = s + ((size_t)col << logn);
+            const int od = ((j >> logns) << (logns + LOGR)) + jm;
+#pragma unroll
+            for (int r = 0; r < R; r++) dst[swz(od + r * ns)] = v[r];
         }
         __syncthreads();
     }
 }
 
+// Full in-place FFT of ncol transforms of length n = 2^logn (2..16384) in smem (swizzled
+// index swz), natural order in and out.  inverse: exp(+), unscaled.
+__device__ void block_fft(float2 *s, int logn, int ncol, const float2 *__restrict__ tw, int tws,
+                          bool inverse) {
+    int logns = 0;
+    while (logns < logn) {
+        const int rem = logn - logns;
+        if (rem >= 4) {
+            if (inverse) stockham_pass<16, 4, true>(s, logn, logns, ncol, tw, tws);
+            else stockham_pass<16, 4, false>(s, logn, logns, ncol, tw, tws);
+            logns += 4;
+        } else if (rem == 3) {
+            if (inverse) stockham_pass<8, 3, true>(s, logn, logns, ncol, tw, tws);
+            else stockham_pass<8, 3, false>(s, logn, logns, ncol, tw, tws);
+            logns += 3;
+        } else if (rem == 2) {
+            if (inverse) stockham_pass<4, 2, true>(s, logn, logns, ncol, tw, tws);
+            else stockham_pass<4, 2, false>(s, logn, logns, ncol, tw, tws);
+            logns += 2;
+        } else {
+            if (inverse) stockham_pass<2, 1, true>(s, logn, logns, ncol, tw, tws);
+            else stockham_pass<2, 1, false>(s, logn, logns, ncol, tw, tws);
+            logns += 1;
+        }
+    }
+}
+
 // Column pass along v, in place on grid [nv][pitch].  inverse: FFTX ISIG=-1 (1/nv);
 // forward: ISIG=+1.  Forward mode treats rows outside [r0, r1) as zero (FFTR2D's padding,
-// fft/fftr2d.f:57-70).
-__global__ void __launch_bounds__(FFT_THREADS) k_col_fft(float2 *grid, int pitch, int nu, int nv,
-                                                          int lognv, int ccols,
+// fft/fftr2d.f:57-70).  A CTA keeps ccols (even, power of two) whole columns in shared
+// memory; rows are read as 16-byte pairs of columns, LB rows in flight per thread.
+constexpr int COL_THREADS = 256;
+constexpr int LB = 16;
+__global__ void __launch_bounds__(COL_THREADS) k_col_fft(float2 *grid, int pitch, int nu, int nv,
+                                                          int lognv, int logcc,
                                                           const float2 *__restrict__ tw,
                                                           int inverse, int r0, int r1) {
     extern __shared__ float2 s[];
+    const int ccols = 1 << logcc;
     const int u0 = blockIdx.x * ccols;
     const int c = (nv + 1) / 2 - 1;
-    const int total = nv * ccols;
-    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-        const int v = idx / ccols, j = idx - v * ccols;
-        const int u = u0 + j;
-        float2 x = make_float2(0.f, 0.f);
-        if (u < nu && (inverse || (v >= r0 && v < r1))) x = grid[(int64_t)v * pitch + u];
-        int k = v - c;
-        if (k < 0) k += nv;
-        s[(size_t)j * nv + brev((unsigned)k, lognv)] = x;
+    const int lp = logcc - 1;               // pairs per row = ccols/2
+    const int total = nv << lp;             // (row, pair) items
+    for (int base = 0; base < total; base += COL_THREADS * LB) {
+        float4 x[LB];
+#pragma unroll
+        for (int i = 0; i < LB; i++) {
+            const int idx = base + i * COL_THREADS + threadIdx.x;
+            const int v = idx >> lp, jp = idx & ((1 << lp) - 1);
+            const int u = u0 + 2 * jp;
+            x[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (idx < total && u < nu && (inverse || (v >= r0 && v < r1)))
+                x[i] = *reinterpret_cast<const float4 *>(&grid[(int64_t)v * pitch + u]);
+        }
+#pragma unroll
+        for (int i = 0; i < LB; i++) {
+            const int idx = base + i * COL_THREADS + threadIdx.x;
+            if (idx >= total) continue;
+            const int v = idx >> lp, jp = idx & ((1 << lp) - 1);
+            int k = v - c;
+            if (k < 0) k += nv;
+            s[((size_t)(2 * jp) << lognv) + swz(k)] = make_float2(x[i].x, x[i].y);
+            s[((size_t)(2 * jp + 1) << lognv) + swz(k)] = make_float2(x[i].z, x[i].w);
+        }
     }
     __syncthreads();
-    block_fft(s, nv, lognv, ccols, tw, 1, inverse != 0);
+    block_fft(s, lognv, ccols, tw, 1, inverse != 0);
     const float sc = inverse ? 1.0f / (float)nv : 1.0f;
-    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-        const int v = idx / ccols, j = idx - v * ccols;
-        const int u = u0 + j;
+    for (int idx = threadIdx.x; idx < total; idx += COL_THREADS) {
+        const int v = idx >> lp, jp = idx & ((1 << lp) - 1);
+        const int u = u0 + 2 * jp;
         if (u >= nu) continue;
         int k = v - c;
         if (k < 0) k += nv;
-        float2 z = s[(size_t)j * nv + k];
+        float2 z0 = s[((size_t)(2 * jp) << lognv) + swz(k)];
+        float2 z1 = s[((size_t)(2 * jp + 1) << lognv) + swz(k)];
         if (inverse) {
-            z.x = z.x * sc;
-            z.y = z.y * sc;
+            z0.x *= sc; z0.y *= sc; z1.x *= sc; z1.y *= sc;
         }
-        grid[(int64_t)v * pitch + u] = z;
+        // grid rows are 16-byte aligned (pitch % 4 == 0), u is even
+        *reinterpret_cast<float4 *>(&grid[(int64_t)v * pitch + u]) = make_float4(z0.x, z0.y, z1.x, z1.y);
     }
 }
 
 struct CorrParams {
-    const float *ccf;  // nullptr: no grid correction
-    float scalex, scaley, cenx, ceny;
+    const float *ccf;    // nullptr: no grid correction
+    const float *corrx;  // CCF(ICFX) for each image column (pix/pixcor2d.f:62)
+    const float *corry;  // CCF(ICFY) for each image row (pix/pixcor2d.f:60)
 };
-
-__device__ __forceinline__ float corr_factor(const CorrParams &cp, int ix1, int iy1) {
-    const int icx = 1 + abs(nint_f(__fmul_rn(cp.scalex, __fsub_rn((float)ix1, cp.cenx))));
-    const int icy = 1 + abs(nint_f(__fmul_rn(cp.scaley, __fsub_rn((float)iy1, cp.ceny))));
-    return __fmul_rn(cp.ccf[icx - 1], cp.ccf[icy - 1]);
-}
 
 // Row pass grid -> image (c2r), one CTA per image row, with grid correction and an
 // optional final scale OUT = s*IN (ARRSCALE by 1/max, pix/pixrscal.f).
 __global__ void __launch_bounds__(FFT_THREADS) k_row_c2r(const float2 *__restrict__ grid,
-                                                          int pitch, int fnu, int logh,
+                                                          int pitch, int fnu, int rows,
                                                           int nx, int ny, int ibegy,
                                                           const float2 *__restrict__ tw,
                                                           CorrParams cp,
                                                           const float *__restrict__ scale_dev,
                                                           float *image) {
     extern __shared__ float2 s[];
-    const int iy = blockIdx.x;
     const int H = fnu >> 1;
-    const float2 *X = grid + (int64_t)(iy + ibegy) * pitch;
-    for (int k = threadIdx.x; k < H; k += blockDim.x) {
+    const int logh = __ffs(H) - 1;
+    const int iy0 = blockIdx.x * rows;
+    for (int t = threadIdx.x; t < H * rows; t += blockDim.x) {
+        const int rr = t >> logh, k = t & (H - 1);
+        const int iy = iy0 + rr;
+        if (iy >= ny) {
+            s[(rr << logh) + swz(k)] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float2 *X = grid + (int64_t)(iy + ibegy) * pitch;
         float2 a = X[k], b = X[H - k];
         if (k == 0) {
             a.y = 0.f;
@@ -127,37 +273,50 @@ __global__ void __launch_bounds__(FFT_THREADS) k_row_c2r(const float2 *__restric
         const float2 d = make_float2(0.5f * (a.x - b.x), 0.5f * (a.y + b.y));
         const float2 B = cmul(d, __ldg(&tw[k]));
         // Z = A + i B
-        s[brev((unsigned)k, logh)] = make_float2(A.x - B.y, A.y + B.x);
+        s[(rr << logh) + swz(k)] = make_float2(A.x - B.y, A.y + B.x);
     }
     __syncthreads();
-    block_fft(s, H, logh, 1, tw, 2, true);
+    block_fft(s, logh, rows, tw, 2, true);
     const float inv = 1.0f / (float)H;
     const int cu = (fnu + 1) / 2 - 1, ioff = (fnu - nx) / 2;
     const float sc = scale_dev ? 1.0f / *scale_dev : 1.0f;
-    float *out = image + (int64_t)iy * nx;
-    for (int ix = threadIdx.x; ix < nx; ix += blockDim.x) {
+    for (int rr = 0; rr < rows; rr++) {
+        const int iy = iy0 + rr;
+        if (iy >= ny) break;
+        float *out = image + (int64_t)iy * nx;
+        const float cfy = cp.ccf ? cp.corry[iy] : 1.0f;
+        for (int ix = threadIdx.x; ix < nx; ix += blockDim.x) {
         int n = ix + ioff - cu;
         if (n < 0) n += fnu;
-        const float2 z = s[n >> 1];
+        const float2 z = s[(rr << logh) + swz(n >> 1)];
         float val = ((n & 1) ? z.y : z.x) * inv;
-        if (cp.ccf) val = __fdiv_rn(val, corr_factor(cp, ix + 1, iy + 1));
+        if (cp.ccf) val = __fdiv_rn(val, __fmul_rn(cp.corrx[ix], cfy));
         if (scale_dev) val = __fadd_rn(__fmul_rn(sc, val), 0.0f);
         out[ix] = val;
+        }
     }
 }
 
 // Row pass image -> grid (r2c), one CTA per image row; grid correction on the way in.
 __global__ void __launch_bounds__(FFT_THREADS) k_row_r2c(const float *__restrict__ image, int nx,
-                                                          int ny, int fnu, int logh, int ibegy,
+                                                          int ny, int fnu, int rows, int ibegy,
                                                           const float2 *__restrict__ tw,
                                                           CorrParams cp, float2 *grid, int pitch,
                                                           int nu) {
     extern __shared__ float2 s[];
-    const int iy = blockIdx.x;
     const int H = fnu >> 1;
+    const int logh = __ffs(H) - 1;
     const int cu = (fnu + 1) / 2 - 1, ioff = (fnu - nx) / 2;
-    const float *row = image + (int64_t)iy * nx;
-    for (int m = threadIdx.x; m < H; m += blockDim.x) {
+    const int iy0 = blockIdx.x * rows;
+    for (int t = threadIdx.x; t < H * rows; t += blockDim.x) {
+        const int rr = t >> logh, m = t & (H - 1);
+        const int iy = iy0 + rr;
+        if (iy >= ny) {
+            s[(rr << logh) + swz(m)] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float cfy = cp.ccf ? cp.corry[iy] : 1.0f;
+        const float *row = image + (int64_t)iy * nx;
         float xv[2];
 #pragma unroll
         for (int e = 0; e < 2; e++) {
@@ -168,35 +327,55 @@ __global__ void __launch_bounds__(FFT_THREADS) k_row_r2c(const float *__restrict
             float val = 0.f;
             if (ix >= 0 && ix < nx) {
                 val = row[ix];
-                if (cp.ccf) val = __fdiv_rn(val, corr_factor(cp, ix + 1, iy + 1));
+                if (cp.ccf) val = __fdiv_rn(val, __fmul_rn(cp.corrx[ix], cfy));
             }
             xv[e] = val;
         }
-        s[brev((unsigned)m, logh)] = make_float2(xv[0], xv[1]);
+        s[(rr << logh) + swz(m)] = make_float2(xv[0], xv[1]);
     }
     __syncthreads();
-    block_fft(s, H, logh, 1, tw, 2, false);
-    float2 *X = grid + (int64_t)(iy + ibegy) * pitch;
-    for (int k = threadIdx.x; k <= H; k += blockDim.x) {
-        const float2 zk = s[k == H ? 0 : k];
-        const float2 zc = s[k == 0 || k == H ? 0 : H - k];
+    block_fft(s, logh, rows, tw, 2, false);
+    for (int rr = 0; rr < rows; rr++) {
+        const int iy = iy0 + rr;
+        if (iy >= ny) break;
+        float2 *X = grid + (int64_t)(iy + ibegy) * pitch;
+        const float2 *sr = s + (rr << logh);
+        for (int k = threadIdx.x; k <= H; k += blockDim.x) {
+        const float2 zk = sr[swz(k == H ? 0 : k)];
+        const float2 zc = sr[swz(k == 0 || k == H ? 0 : H - k)];
         // A = (Z[k] + conj Z[H-k])/2, B = (Z[k] - conj Z[H-k])/(2i), X = A + e^{-2 pi i k/N} B
         const float2 A = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y - zc.y));
         const float2 B = make_float2(0.5f * (zk.y + zc.y), -0.5f * (zk.x - zc.x));
         float2 w = k < H ? __ldg(&tw[k]) : make_float2(-1.f, 0.f);
         w.y = -w.y;
-        const float2 t = cmul(B, w);
-        float2 x = make_float2(A.x + t.x, A.y + t.y);
+        const float2 bw = cmul(B, w);
+        float2 x = make_float2(A.x + bw.x, A.y + bw.y);
         if (k == 0 || k == H) x.y = 0.f;
         X[k] = x;
+        }
     }
 }
 
-int col_cols(int nv) {
+// rows per CTA and threads for the row passes: one radix-16 butterfly per thread per pass,
+// at least 128 threads and 16 KB of shared memory per CTA
+void row_shape(int fnu, int *rows, int *thr) {
+    const int H = fnu / 2;
+    int per = H / 16 < 32 ? 32 : H / 16;
+    int r = 1;
+    while (r * per < 128 || (size_t)r * H * 8 < 16384) r *= 2;
+    if (r * per > FFT_THREADS) r = FFT_THREADS / per > 0 ? FFT_THREADS / per : 1;
+    *rows = r;
+    *thr = r * per > FFT_THREADS ? FFT_THREADS : r * per;
+}
+
+// log2 of the columns per CTA: 128 KB of columns, between 2 and 16 columns
+int col_logcc(int nv) {
     int c = 16384 / nv;
-    if (c < 1) c = 1;
+    if (c < 2) c = 2;
     if (c > 16) c = 16;
-    return c;
+    int l = 0;
+    while ((1 << l) < c) l++;
+    return l;
 }
 
 int ilog2(int n) {
@@ -207,34 +386,42 @@ int ilog2(int n) {
 
 bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
+// Per-axis grid-correction factors CCF(1 + |NINT(SCALE*(I - CEN))|) with PIXCOR2D's REAL
+// arithmetic (pix/pixcor2d.f:44-63), computed on the host once per image shape.
 int corr_params(sde_ctx *ctx, int nx, int ny, CorrParams *cp) {
     int fnx = fftpwr2(nx), fny = fftpwr2(ny);
     int ccflen = 1 + fftpwr2(nx > ny ? nx : ny) / 2;
-    char name[48];
-    snprintf(name, sizeof name, "ccf_%d", ccflen);
+    char name[64];
+    snprintf(name, sizeof name, "ccf_%d_%d", nx, ny);
     auto it = ctx->scratch.find(name);
     float *d = nullptr;
-    if (it == ctx->scratch.end() || it->second.bytes < sizeof(float) * (size_t)ccflen) {
-        SDE_TRY(ctx_scratch(ctx, name, sizeof(float) * (size_t)ccflen, (void **)&d));
-        std::vector<float> h((size_t)ccflen);
+    const size_t need = sizeof(float) * (size_t)(ccflen + nx + ny);
+    if (it == ctx->scratch.end() || it->second.bytes < need) {
+        SDE_TRY(ctx_scratch(ctx, name, need, (void **)&d));
+        std::vector<float> h((size_t)(ccflen + nx + ny));
         sf_ccf_table(h.data(), ccflen);
-        SDE_CUDA_TRY(cudaMemcpy(d, h.data(), sizeof(float) * (size_t)ccflen, cudaMemcpyHostToDevice));
+        const float scalex = (float)(ccflen - 1) * 2.0f / (float)fnx;
+        const float scaley = (float)(ccflen - 1) * 2.0f / (float)fny;
+        const float cenx = (float)((nx + 1) / 2), ceny = (float)((ny + 1) / 2);
+        for (int ix = 1; ix <= nx; ix++)
+            h[(size_t)ccflen + ix - 1] = h[(size_t)abs((int)lroundf(scalex * ((float)ix - cenx)))];
+        for (int iy = 1; iy <= ny; iy++)
+            h[(size_t)ccflen + nx + iy - 1] = h[(size_t)abs((int)lroundf(scaley * ((float)iy - ceny)))];
+        SDE_CUDA_TRY(cudaMemcpy(d, h.data(), need, cudaMemcpyHostToDevice));
     } else {
         d = (float *)it->second.p;
     }
     cp->ccf = d;
-    cp->scalex = (float)(ccflen - 1) * 2.0f / (float)fnx;
-    cp->scaley = (float)(ccflen - 1) * 2.0f / (float)fny;
-    cp->cenx = (float)((nx + 1) / 2);
-    cp->ceny = (float)((ny + 1) / 2);
+    cp->corrx = d + ccflen;
+    cp->corry = d + ccflen + nx;
     return SDE_OK;
 }
 
 int check_fft_args(int nx, int ny, int fnu, int nv, int pitch) {
-    if (!is_pow2(fnu) || !is_pow2(nv) || fnu < 4 || nv < 2 || fnu > 16384 || nv > 16384 || nx < 1 ||
+    if (!is_pow2(fnu) || !is_pow2(nv) || fnu < 4 || nv < 2 || fnu > 8192 || nv > 8192 || nx < 1 ||
         ny < 1 || nx > fnu || ny > nv || pitch < fnu / 2 + 1) {
         sde_set_error("FFT: unsupported sizes nx=%d ny=%d fnu=%d nv=%d pitch=%d (power-of-two "
-                      "FNU/NV up to 16384 required)", nx, ny, fnu, nv, pitch);
+                      "FNU/NV up to 8192 required, as ARRFFTR's MAXGAMMA=13)", nx, ny, fnu, nv, pitch);
         return SDE_EINVAL;
     }
     return SDE_OK;
@@ -251,24 +438,25 @@ int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, in
     const float2 *twv, *twu;
     SDE_TRY(ctx_twiddles(ctx, nv, &twv));
     SDE_TRY(ctx_twiddles(ctx, fnu, &twu));
-    const int cc = col_cols(nv);
+    const int lcc = col_logcc(nv), cc = 1 << lcc;
     const size_t smc = sizeof(float2) * (size_t)cc * nv;
     SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
     {
         KTimer kt(ctx, "col_fft");
-        k_col_fft<<<ceil_div(nu, cc), FFT_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
-                                                                       ilog2(nv), cc, twv, 1, 0, nv);
+        k_col_fft<<<ceil_div(nu, cc), COL_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
+                                                                       ilog2(nv), lcc, twv, 1, 0, nv);
     }
     SDE_CHECK_LAUNCH();
-    CorrParams cp = {nullptr, 0.f, 0.f, 0.f, 0.f};
+    CorrParams cp = {nullptr, nullptr, nullptr};
     if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
     const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;  // 0-based first grid row
-    const size_t smr = sizeof(float2) * (size_t)(fnu / 2);
+    int rows, thr;
+    row_shape(fnu, &rows, &thr);
+    const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
     SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
     KTimer kt(ctx, "row_c2r");
-    k_row_c2r<<<ny, FFT_THREADS, smr, ctx->stream>>>((const float2 *)grid, pitch, fnu,
-                                                     ilog2(fnu / 2), nx, ny, ibegy, twu, cp,
-                                                     scale_dev, image);
+    k_row_c2r<<<ceil_div(ny, rows), thr, smr, ctx->stream>>>((const float2 *)grid, pitch, fnu, rows,
+                                                            nx, ny, ibegy, twu, cp, scale_dev, image);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
@@ -282,23 +470,25 @@ int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fn
     const float2 *twv, *twu;
     SDE_TRY(ctx_twiddles(ctx, nv, &twv));
     SDE_TRY(ctx_twiddles(ctx, fnu, &twu));
-    CorrParams cp = {nullptr, 0.f, 0.f, 0.f, 0.f};
+    CorrParams cp = {nullptr, nullptr, nullptr};
     if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
     const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;
-    const size_t smr = sizeof(float2) * (size_t)(fnu / 2);
+    int rows, thr;
+    row_shape(fnu, &rows, &thr);
+    const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
     SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
     {
         KTimer kt(ctx, "row_r2c");
-        k_row_r2c<<<ny, FFT_THREADS, smr, ctx->stream>>>(image, nx, ny, fnu, ilog2(fnu / 2), ibegy,
-                                                         twu, cp, (float2 *)grid, pitch, nu);
+        k_row_r2c<<<ceil_div(ny, rows), thr, smr, ctx->stream>>>(image, nx, ny, fnu, rows, ibegy, twu,
+                                                                cp, (float2 *)grid, pitch, nu);
     }
     SDE_CHECK_LAUNCH();
-    const int cc = col_cols(nv);
+    const int lcc = col_logcc(nv), cc = 1 << lcc;
     const size_t smc = sizeof(float2) * (size_t)cc * nv;
     SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
     KTimer kt(ctx, "col_fft");
-    k_col_fft<<<ceil_div(nu, cc), FFT_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
-                                                                   ilog2(nv), cc, twv, 0, ibegy,
+    k_col_fft<<<ceil_div(nu, cc), COL_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
+                                                                   ilog2(nv), lcc, twv, 0, ibegy,
                                                                    ibegy + ny);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
