@@ -221,6 +221,24 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
                float tflux_in, float *cln, float *res, float *cflux, int *cx, int *cy,
                volatile int *cancel_flag, sde_clean_result *out);
 
+/* Hogbom CLEAN that allocates nothing.  This entry point has no counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc -- hosts whose device memory
+ * all comes from their own allocator or fixed arena, real-time or embedded loops that forbid
+ * allocation once running, and serving loops that must never block on the allocator.  It
+ * takes the same device arrays and returns the same results as sde_hogbom, on the caller's
+ * stream (a cudaStream_t, 0 for the legacy stream, on the current device).  Its scratch --
+ * partial maxima of at most 1024 CTAs per search, the grid barrier, status words and result
+ * scalars, about 36 KB -- lives in one static device array that every GPU which loads the
+ * library keeps until the process exits.  The first call on a device takes that array's
+ * address (cudaGetSymbolAddress), so make it before any stream capture.  Every call shares
+ * the array and the call clears what must start at zero; calls that overlap on the GPU (two
+ * streams, two host threads) race on it and must be serialised by the caller.  Windows or
+ * PSFs over 2^31-1 pixels are rejected with SDE_EINVAL. */
+int sde_hogbom_noalloc(void *stream, const float *drt, const float *psf, const float *box, int nx,
+                       int ny, int pnx, int pny, float gain, int nsub, int bsub, float flux,
+                       float tflux_in, float *cln, float *res, float *cflux, int *cx, int *cy,
+                       volatile int *cancel_flag, sde_clean_result *out);
+
 /* Index (1-based) of the first strictly largest |a| (PIXISAMA) of a device array. */
 int sde_isamax(sde_ctx *ctx, const float *a, int64_t n, int64_t *index_out);
 

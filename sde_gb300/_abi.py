@@ -84,6 +84,8 @@ SIGNATURES = [
     ("sde_hogbom", I, [P, P, P, P, I, I, I, I, F, I, I, F, F, P, P, P, P, P, P,
                        C.POINTER(CleanResult)]),
     ("sde_isamax", I, [P, P, I64, C.POINTER(I64)]),
+    ("sde_hogbom_noalloc", I, [P, P, P, P, I, I, I, I, F, I, I, F, F, P, P, P, P, P, P,
+                               C.POINTER(CleanResult)]),
     # Fortran-77 drop-in layer (all arguments by reference)
     ("grdh2d_", None, [P] * 24),
     ("grddeh2d_", None, [P] * 22),

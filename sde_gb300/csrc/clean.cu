@@ -11,6 +11,9 @@
 // global (max, first index), so component positions are identical to the reference's.
 #include <cooperative_groups.h>
 #include <math.h>
+#include <string.h>
+
+#include <mutex>
 
 #include "common.cuh"
 
@@ -362,6 +365,139 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
     SDE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     if (ctx->h_status[STATUS_TIMEOUT]) {
         sde_set_error("sde_hogbom: grid barrier timed out");
+        return SDE_ETIMEDOUT;
+    }
+    int ansub, stopped;
+    memcpy(&ansub, &h[2], 4);
+    memcpy(&stopped, &h[3], 4);
+    out->maxres = h[0];
+    out->tflux = h[1];
+    out->ansub = ansub;
+    if (stopped == 2) return SDE_ECANCELLED;
+    return SDE_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Hogbom CLEAN without any device allocation.
+//
+// Some callers cannot call cudaMalloc: code that owns all device memory through its own
+// allocator or a fixed arena, embedded/real-time hosts that forbid allocation after start-up,
+// and serving loops that must not block on the allocator.  For them this entry point runs the
+// same minor cycle as sde_hogbom on arrays the caller already holds, keeping its scratch --
+// the per-CTA partial maxima of the PSF-peak search and of every CLEAN iteration, the grid
+// barrier, the status words and the result scalars -- in one file-scope device array of fixed
+// size.  That array exists on every GPU that loads the library, for the life of the process.
+namespace {
+constexpr int NOALLOC_MAX_CTAS = 1024;  // partial maxima kept per search (~36 KB in all)
+struct NoAllocScratch {
+    Cand isa_part[NOALLOC_MAX_CTAS];
+    int64_t isa_out;
+    Cand partial[2 * NOALLOC_MAX_CTAS];
+    Barrier bar;
+    int status[STATUS_COUNT];
+    float out[4];
+};
+}  // namespace
+
+static __device__ __align__(256) NoAllocScratch g_clean_scratch;
+
+// Host-side copies of g_clean_scratch's device address, one per device.  The array's name in
+// host code only stands in for the symbol; the address every kernel receives comes from
+// cudaGetSymbolAddress, taken once per device with that device current.
+static NoAllocScratch *g_clean_scratch_dev[64];
+static std::mutex g_clean_scratch_mu;
+
+static int clean_scratch_address(int dev, NoAllocScratch **out) {
+    if (dev < 0 || dev >= 64) {
+        sde_set_error("sde_hogbom_noalloc: device %d out of range", dev);
+        return SDE_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(g_clean_scratch_mu);
+    if (!g_clean_scratch_dev[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_clean_scratch);
+        if (e != cudaSuccess || !p) {
+            sde_set_error("sde_hogbom_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? SDE_ENODEV : SDE_ECUDA;
+        }
+        g_clean_scratch_dev[dev] = (NoAllocScratch *)p;
+    }
+    *out = g_clean_scratch_dev[dev];
+    return SDE_OK;
+}
+
+extern "C" int sde_hogbom_noalloc(void *stream, const float *drt, const float *psf,
+                                  const float *box, int nx, int ny, int pnx, int pny, float gain,
+                                  int nsub, int bsub, float flux, float tflux_in, float *cln,
+                                  float *res, float *cflux, int *cx, int *cy,
+                                  volatile int *cancel_flag, sde_clean_result *out) {
+    if (!drt || !psf || !cln || !res || !out || nx < 1 || ny < 1 || pnx < 1 || pny < 1 || bsub < 1) {
+        sde_set_error("sde_hogbom_noalloc: bad arguments");
+        return SDE_EINVAL;
+    }
+    if ((int64_t)nx * ny > INT32_MAX || (int64_t)pnx * pny > INT32_MAX) {
+        sde_set_error("sde_hogbom_noalloc: window %dx%d or PSF %dx%d exceeds 2^31-1 pixels", nx, ny,
+                      pnx, pny);
+        return SDE_EINVAL;
+    }
+    const int nabs = nsub < 0 ? -nsub : nsub;
+    if (nabs >= bsub && (!cflux || !cx || !cy)) {
+        sde_set_error("sde_hogbom_noalloc: component arrays required");
+        return SDE_EINVAL;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, nsm = 0;
+    SDE_CUDA_TRY(cudaGetDevice(&dev));
+    SDE_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    NoAllocScratch *S = nullptr;
+    SDE_TRY(clean_scratch_address(dev, &S));
+    // PSF peak (pix/pix2drcl.f:146-151) with the partials in the static array
+    int nbi = nsm * 2;
+    if (nbi > NOALLOC_MAX_CTAS) nbi = NOALLOC_MAX_CTAS;
+    k_isamax_part<<<nbi, CL_THREADS, 0, st>>>(psf, (int64_t)pnx * pny, S->isa_part);
+    SDE_CHECK_LAUNCH();
+    k_isamax_final<<<1, CL_THREADS, 0, st>>>(S->isa_part, nbi, &S->isa_out);
+    SDE_CHECK_LAUNCH();
+    int64_t ip1 = 0;
+    SDE_CUDA_TRY(cudaMemcpyAsync(&ip1, &S->isa_out, sizeof ip1, cudaMemcpyDeviceToHost, st));
+    SDE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (ip1 == 0) ip1 = 1;  // PIXISAMA's default I = 1
+    const int ipeak = (int)(ip1 - 1);
+    int pmpx = 1 + ipeak % pnx;
+    int pmpy = 1 + (ipeak - pmpx + 1) / pnx;
+    if (pmpx >= pnx) pmpx = pnx / 2;
+    if (pmpy >= pny) pmpy = pny / 2;
+    int per_sm = 0;
+    SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom, CL_THREADS, 0));
+    if (per_sm < 1) {
+        sde_set_error("sde_hogbom_noalloc: kernel cannot be resident");
+        return SDE_ECUDA;
+    }
+    const int64_t npix = (int64_t)nx * ny;
+    int nblocks = nsm * (per_sm > 2 ? 2 : per_sm);
+    const int64_t want = (npix + 4 * CL_THREADS - 1) / (4 * CL_THREADS);
+    if (want < nblocks) nblocks = (int)(want < 1 ? 1 : want);
+    if (nblocks > NOALLOC_MAX_CTAS) nblocks = NOALLOC_MAX_CTAS;
+    // the array keeps the previous call's contents: clear what must start at zero
+    SDE_CUDA_TRY(cudaMemsetAsync(&S->bar, 0, sizeof(Barrier), st));
+    SDE_CUDA_TRY(cudaMemsetAsync(S->status, 0, sizeof(S->status), st));
+    SDE_CUDA_TRY(cudaMemsetAsync(S->out, 0, sizeof(S->out), st));
+    CleanArgs A;
+    A.drt = drt; A.psf = psf; A.box = box; A.cln = cln; A.res = res; A.cflux = cflux;
+    A.cx = cx; A.cy = cy; A.nx = nx; A.ny = ny; A.pnx = pnx; A.pny = pny;
+    A.pmpx = pmpx; A.pmpy = pmpy; A.gain = gain; A.flux = flux; A.tflux_in = tflux_in;
+    A.nsub = nsub; A.bsub = bsub; A.cancel = cancel_flag; A.partial = S->partial; A.bar = &S->bar;
+    A.status = S->status; A.out = S->out;
+    void *args[] = {&A};
+    SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom, dim3(nblocks), dim3(CL_THREADS),
+                                             args, 0, st));
+    float h[4];
+    int hs[STATUS_COUNT];
+    SDE_CUDA_TRY(cudaMemcpyAsync(h, S->out, sizeof h, cudaMemcpyDeviceToHost, st));
+    SDE_CUDA_TRY(cudaMemcpyAsync(hs, S->status, sizeof hs, cudaMemcpyDeviceToHost, st));
+    SDE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hs[STATUS_TIMEOUT]) {
+        sde_set_error("sde_hogbom_noalloc: grid barrier timed out");
         return SDE_ETIMEDOUT;
     }
     int ansub, stopped;
