@@ -46,7 +46,9 @@ constexpr int NTAP = 2 * SUPP + 1;      // 7
 constexpr int STILE = TILE + 2 * SUPP;  // 70: shared tile edge (grid and degrid)
 constexpr int CFLEN = 1 + 8 * 129;      // vis/visgrid.f:274
 constexpr int ITEM_MAX = 8192;
-constexpr int CHUNK_MAX = 16;
+constexpr int CHUNK_MAX = 64;
+constexpr int LBITS = 6;                // chunk length class CHUNK_MAX - len, 0..63
+static_assert(CHUNK_MAX - 1 < (1 << LBITS), "length class field");
 constexpr uint32_t KEY_INVALID = 0xFFFFFFFFu;
 
 // Per-visibility geometry words (sorted order):
@@ -161,7 +163,7 @@ struct sde_plan {
     float2 *fobs = nullptr;   // observed, in the gridding frame (rotated, conjugated)
     float2 *fres = nullptr;   // residual, gridding frame
     float *wt = nullptr;
-    uint16_t *gdg = nullptr;  // gridding sub-cell offsets
+    float2 *wg = nullptr;     // {WT, gdg bits}: the gridder's per-visibility static record
     uint32_t *gdd = nullptr;  // degridding offsets + cell + exception flag
     uint32_t *orig = nullptr; // caller index of each sorted visibility
     float2 *rot = nullptr;    // (cos, sin) of the phase rotation (doshift only), sorted
@@ -217,6 +219,21 @@ __device__ __forceinline__ void red_add_f2(float2 *addr, float2 v) {
     asm volatile("red.relaxed.gpu.global.add.v2.f32 [%0], {%1, %2};" ::"l"(addr), "f"(v.x),
                  "f"(v.y)
                  : "memory");
+}
+
+// Ask the TMA unit to pull elements [first, last) of an array into L2 (no registers, no
+// completion to wait for).  The byte range is shrunk to 16-byte boundaries (the rule of
+// cp.async.bulk.prefetch.L2), so it never reaches outside the array; the elements cut off
+// at either end are simply not prefetched.
+__device__ __forceinline__ void prefetch_l2_range(const void *base, int64_t first, int64_t last,
+                                                  int esize) {
+    uintptr_t a = (reinterpret_cast<uintptr_t>(base) + (uintptr_t)(first * esize) + 15) & ~(uintptr_t)15;
+    const uintptr_t b = (reinterpret_cast<uintptr_t>(base) + (uintptr_t)(last * esize)) & ~(uintptr_t)15;
+    while (a < b) {
+        const uint32_t n = (uint32_t)(b - a < 16384 ? b - a : 16384);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(n) : "memory");
+        a += n;
+    }
 }
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }

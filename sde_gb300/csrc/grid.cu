@@ -1,15 +1,17 @@
 // grid.cu -- tiled gridding (GRDH2D) and degridding (GRDDEH2D) over a sde_plan.
 //
 // Gridding: one CTA per work item keeps the item's 64x64-cell tile plus a 3-cell halo in
-// shared memory.  Each thread owns a chunk (<= CHUNK_MAX visibilities of one cell) and
-// accumulates the chunk's full 7x7 complex footprint in registers, then adds it into the
-// shared tile once; the chunk order (colour class, chunk index, cell) makes the 32 chunks
-// of a warp write disjoint cells.  The shared tile is then reduced into the raw grid in
-// HBM with vector red.global.add (only the cells the item touched).
+// shared memory.  A 4-lane group owns a chunk (<= CHUNK_MAX visibilities of one cell) and
+// accumulates the chunk's 7x7 complex footprint in registers (two columns per lane), then
+// adds it into the shared tile once; the chunk order (colour class, length class, chunk
+// index, cell) makes the 8 chunks of a warp write disjoint cells and have similar lengths.
+// The shared tile is then reduced into the raw grid in HBM with vector red.global.add (only
+// the cells the item touched).
 //
 // Degridding: one CTA per work item stages the model grid's tile (+halo) into shared
-// memory with a single TMA 2-D bulk copy, then each thread interpolates its chunk's
-// visibilities from a register copy of the chunk cell's 7x7 neighbourhood.
+// memory with a single TMA 2-D bulk copy, then a 4-lane group per chunk interpolates the
+// chunk's visibilities from a register copy of the chunk cell's 7x7 neighbourhood (two
+// columns per lane) and reduces the lanes' partial sums with shuffles.
 #include <math.h>
 #include <string.h>
 
@@ -20,7 +22,27 @@ namespace {
 constexpr int GRID_THREADS = 256;
 constexpr int GLANES = 4;                          // lanes per chunk
 constexpr int GGROUPS = GRID_THREADS / GLANES;     // chunks in flight per CTA
-constexpr int CFT_FLOATS = 129 * 8;
+constexpr int GRID_AHEAD = 2;                      // record prefetch distance (visibilities)
+constexpr int GRID_MINB = 4;                       // resident CTAs per SM the kernel is built for
+constexpr int CFT_FLOATS = 129 * 8;                // global table [129][8]
+// Shared copies of the table, strided so that the 8 rows a warp reads at once (one per
+// 4-lane group) fall on 8 different bank positions: v taps [129][12] (two float4 per row),
+// u tap pairs (col q, col q+4) [129][5] float2.
+constexpr int CFV_STRIDE = 12;
+constexpr int CFP_STRIDE = 5;
+constexpr int CFV_FLOATS = 129 * CFV_STRIDE;
+constexpr int CFP_PAIRS = 129 * CFP_STRIDE;
+
+__device__ __forceinline__ void fill_tap_tables(const float *__restrict__ cft_g, float *cfv,
+                                                float2 *cfp, int nthreads) {
+    for (int k = threadIdx.x; k < 129 * 8; k += nthreads)
+        cfv[(k >> 3) * CFV_STRIDE + (k & 7)] = cft_g[k];
+    for (int k = threadIdx.x; k < 129 * 4; k += nthreads) {
+        const int d = k >> 2, q = k & 3;
+        cfp[d * CFP_STRIDE + q] =
+            make_float2(cft_g[d * 8 + q], q + 4 < NTAP ? cft_g[d * 8 + q + 4] : 0.f);
+    }
+}
 
 // Gridding.  Lane q of a 4-lane group owns footprint columns q and q+4 (q+4 = 7 is empty)
 // of its chunk's cell and accumulates 7 rows x 2 columns x complex in registers; the chunk's
@@ -28,22 +50,23 @@ constexpr int CFT_FLOATS = 129 * 8;
 // receives each chunk's footprint once, through shared-memory atomics (a warp's 8 chunks
 // share a colour class, so their footprints do not overlap).
 template <bool PSF>
-__global__ void __launch_bounds__(GRID_THREADS, 4)
+__global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
     k_grid(const WorkItem *__restrict__ items, const uint2 *__restrict__ chunks,
-           const float2 *__restrict__ fres, const float *__restrict__ wt,
-           const uint16_t *__restrict__ gdg, const float *__restrict__ cft_g, float2 *raw,
-           int pitch, int ntu, int nu, int nv) {
+           const float2 *__restrict__ fres, const float2 *__restrict__ wg,
+           const float *__restrict__ cft_g, float2 *raw, int pitch, int ntu, int nu, int nv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *tile = reinterpret_cast<float2 *>(smem_raw);
-    float *cft = reinterpret_cast<float *>(tile + STILE * STILE);   // [129][8] rows (v taps)
-    float2 *cfp = reinterpret_cast<float2 *>(cft + CFT_FLOATS);     // [129][4] (col q, col q+4)
+    float *cft = reinterpret_cast<float *>(tile + STILE * STILE);   // v taps
+    float2 *cfp = reinterpret_cast<float2 *>(cft + CFV_FLOATS);     // u tap pairs
     const WorkItem it = items[blockIdx.x];
-    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) tile[k] = make_float2(0.f, 0.f);
-    for (int k = threadIdx.x; k < CFT_FLOATS; k += GRID_THREADS) cft[k] = cft_g[k];
-    for (int k = threadIdx.x; k < 129 * 4; k += GRID_THREADS) {
-        const int d = k >> 2, q = k & 3;
-        cfp[k] = make_float2(cft_g[d * 8 + q], q + 4 < NTAP ? cft_g[d * 8 + q + 4] : 0.f);
+    if (threadIdx.x == 0) {
+        // the item's chunk list and records stream into L2 while the tile is cleared
+        prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
+        prefetch_l2_range(wg, it.vbeg, it.vend, 8);
+        if (!PSF) prefetch_l2_range(fres, it.vbeg, it.vend, 8);
     }
+    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) tile[k] = make_float2(0.f, 0.f);
+    fill_tap_tables(cft_g, cft, cfp, GRID_THREADS);
     __syncthreads();
     const int q = threadIdx.x & (GLANES - 1);
     const int grp = threadIdx.x / GLANES;
@@ -61,29 +84,46 @@ __global__ void __launch_bounds__(GRID_THREADS, 4)
                 a1i[b] = 0.f;
             }
         }
-        for (int k = 0; k < len; k++) {
-            const int p = start + k;
-            const uint32_t g = gdg[p];
-            const float w = wt[p];
-            const float2 gu = cfp[(g & 0xFFu) * 4 + q];
-            const float4 *gv4 = reinterpret_cast<const float4 *>(cft + (g >> 8) * 8);
-            const float4 v0 = gv4[0], v1 = gv4[1];
-            const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
-            float fr = w, fi = 0.f;
-            if (!PSF) {
-                const float2 f = fres[p];
-                fr = w * f.x;
-                fi = w * f.y;
-            }
-            const float h0r = gu.x * fr, h1r = gu.y * fr;
-            const float h0i = gu.x * fi, h1i = gu.y * fi;
+        // GRID_AHEAD visibilities ahead: their records and values load while this one
+        // accumulates (a register ring, indexed by constants after unrolling)
+        const float2 *pw = wg + start, *pf = fres + start;
+        float2 rb[GRID_AHEAD], fb[GRID_AHEAD];
 #pragma unroll
-            for (int b = 0; b < NTAP; b++) {
-                a0r[b] = fmaf(gv[b], h0r, a0r[b]);
-                a1r[b] = fmaf(gv[b], h1r, a1r[b]);
+        for (int j = 0; j < GRID_AHEAD; j++) {
+            rb[j] = j < len ? pw[j] : make_float2(0.f, 0.f);
+            fb[j] = (!PSF && j < len) ? pf[j] : make_float2(0.f, 0.f);
+        }
+        for (int k = 0; k < len; k += GRID_AHEAD) {
+#pragma unroll
+            for (int j = 0; j < GRID_AHEAD; j++) {
+                if (k + j >= len) break;
+                const float2 rec = rb[j], f = fb[j];
+                if (k + j + GRID_AHEAD < len) {
+                    rb[j] = pw[k + j + GRID_AHEAD];
+                    if (!PSF) fb[j] = pf[k + j + GRID_AHEAD];
+                }
+                const uint32_t g = __float_as_uint(rec.y);
+                const float w = rec.x;
+                const float2 gu = cfp[(g & 0xFFu) * CFP_STRIDE + q];
+                const float4 *gv4 =
+                    reinterpret_cast<const float4 *>(cft + ((g >> 8) & 0xFFu) * CFV_STRIDE);
+                const float4 v0 = gv4[0], v1 = gv4[1];
+                const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
+                float fr = w, fi = 0.f;
                 if (!PSF) {
-                    a0i[b] = fmaf(gv[b], h0i, a0i[b]);
-                    a1i[b] = fmaf(gv[b], h1i, a1i[b]);
+                    fr = w * f.x;
+                    fi = w * f.y;
+                }
+                const float h0r = gu.x * fr, h1r = gu.y * fr;
+                const float h0i = gu.x * fi, h1i = gu.y * fi;
+#pragma unroll
+                for (int b = 0; b < NTAP; b++) {
+                    a0r[b] = fmaf(gv[b], h0r, a0r[b]);
+                    a1r[b] = fmaf(gv[b], h1r, a1r[b]);
+                    if (!PSF) {
+                        a0i[b] = fmaf(gv[b], h0i, a0i[b]);
+                        a1i[b] = fmaf(gv[b], h1i, a1i[b]);
+                    }
                 }
             }
         }
@@ -112,14 +152,14 @@ __global__ void __launch_bounds__(GRID_THREADS, 4)
 
 // Plan-invariant sums: LSUMWT = sum of UVWT (grd/grdh2d.f:185) and SUMWT (grd/grdh2d.f:157).
 constexpr int RED_T = 256;
-__global__ void __launch_bounds__(RED_T) k_plan_sums(const float *__restrict__ wt,
-                                                      const uint16_t *__restrict__ gdg,
+__global__ void __launch_bounds__(RED_T) k_plan_sums(const float2 *__restrict__ wg,
                                                       const float *__restrict__ cft, int64_t n,
                                                       double *partial) {
     __shared__ double sh[2][RED_T / 32];
     double s0 = 0.0, s1 = 0.0;
     for (int64_t p = (int64_t)blockIdx.x * RED_T + threadIdx.x; p < n; p += (int64_t)gridDim.x * RED_T) {
-        const uint32_t g = gdg[p];
+        const float2 rec = wg[p];
+        const uint32_t g = __float_as_uint(rec.y);
         const float *gu = cft + (g & 0xFFu) * 8, *gv = cft + ((g >> 8) & 0xFFu) * 8;
         float su = 0.f, sv = 0.f;
 #pragma unroll
@@ -127,7 +167,7 @@ __global__ void __launch_bounds__(RED_T) k_plan_sums(const float *__restrict__ w
             su += gu[a];
             sv += gv[a];
         }
-        const float w = wt[p];
+        const float w = rec.x;
         s0 += (double)w * (double)su * (double)sv;
         s1 += (double)w;
     }
@@ -217,20 +257,37 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+constexpr int DG_GROUPS = DG_THREADS / 4;          // chunks in flight per CTA
+constexpr int RSUM_FLOATS = 132;                    // 129 row sums, padded
+constexpr size_t DG_CFT_OFF = DG_TX_BYTES;
+constexpr size_t DG_CFP_OFF = DG_CFT_OFF + sizeof(float) * CFV_FLOATS;
+constexpr size_t DG_RSUM_OFF = DG_CFP_OFF + sizeof(float2) * CFP_PAIRS;
+constexpr size_t DG_BAR_OFF = DG_RSUM_OFF + sizeof(float) * RSUM_FLOATS;
+static_assert(DG_CFT_OFF % 16 == 0 && DG_CFP_OFF % 16 == 0 && DG_BAR_OFF % 8 == 0, "layout");
+
 // mode 0: residual update in the gridding frame; mode 1: caller-order output (user frame).
-// One thread per visibility of the item (coalesced loads); the 7x7 neighbourhood of its
-// cell is read from the TMA-staged tile, interpolated separably: sum_b gv[b] sum_a gu[a] G.
+// A 4-lane group per chunk (the chunk's visibilities share one degridding cell, or carry
+// GDD_EXCEPTION and are skipped here).  Lane q holds columns q and q+4 of the cell's 7x7
+// neighbourhood in registers, read once per chunk from the TMA-staged tile, and for each
+// visibility forms sum_b gv[b] G[b][col] per column, then gu[col] times that: a partial
+// sum over its columns.  Four visibilities' partials are reduced across the group with a
+// transposing butterfly (6 shuffles per lane), after which lane q owns visibility q of the
+// four and finishes it: divide by (sum gu)(sum gv) (row sums in the same order as a plain
+// loop), subtract from the observed value or write to the caller's order.
 template <int MODE>
 __global__ void __launch_bounds__(DG_THREADS, 4)
     k_degrid(const __grid_constant__ CUtensorMap tmap, const WorkItem *__restrict__ items,
-             const uint32_t *__restrict__ gdd, const float *__restrict__ cft_g,
-             const float2 *__restrict__ fobs, float2 *fres, const uint8_t *__restrict__ gconj,
-             const float2 *__restrict__ rot, const uint32_t *__restrict__ orig,
-             const float *__restrict__ wt, float2 *vis_out, float *wt_out, int ntu, int *status) {
+             const uint2 *__restrict__ chunks, const uint32_t *__restrict__ gdd,
+             const float *__restrict__ cft_g, const float2 *__restrict__ fobs, float2 *fres,
+             const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
+             const uint32_t *__restrict__ orig, const float *__restrict__ wt, float2 *vis_out,
+             float *wt_out, int ntu, int *status) {
     extern __shared__ __align__(128) unsigned char smem_dg[];
     float2 *tile = reinterpret_cast<float2 *>(smem_dg);
-    float *cft = reinterpret_cast<float *>(smem_dg + DG_TX_BYTES);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_dg + DG_TX_BYTES + CFT_FLOATS * 4);
+    float *cft = reinterpret_cast<float *>(smem_dg + DG_CFT_OFF);
+    float2 *cfp = reinterpret_cast<float2 *>(smem_dg + DG_CFP_OFF);
+    float *rsum = reinterpret_cast<float *>(smem_dg + DG_RSUM_OFF);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_dg + DG_BAR_OFF);
     const WorkItem it = items[blockIdx.x];
     const int tu = it.tile % ntu, tv = it.tile / ntu;
     if (threadIdx.x == 0) {
@@ -249,8 +306,17 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
             " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(tile)),
             "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
             : "memory");
+        prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
+        prefetch_l2_range(gdd, it.vbeg, it.vend, 4);
+        if (MODE == 0) prefetch_l2_range(fobs, it.vbeg, it.vend, 8);
     }
-    for (int k = threadIdx.x; k < CFT_FLOATS; k += DG_THREADS) cft[k] = cft_g[k];
+    fill_tap_tables(cft_g, cft, cfp, DG_THREADS);
+    for (int d = threadIdx.x; d < 129; d += DG_THREADS) {
+        float sacc = 0.f;
+#pragma unroll
+        for (int a = 0; a < NTAP; a++) sacc += cft_g[d * 8 + a];
+        rsum[d] = sacc;
+    }
     {
         uint32_t done = 0;
         for (int spin = 0; spin < (1 << 24) && !done; spin++) {
@@ -267,46 +333,97 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
         }
     }
     __syncthreads();
-    for (int p = it.vbeg + threadIdx.x; p < it.vend; p += DG_THREADS) {
-        const uint32_t g = gdd[p];
-        if (g & GDD_EXCEPTION) continue;
-        const int cell = (int)((g >> 16) & 4095u), lu = cell & 63, lv = cell >> 6;
-        const float4 *gu4 = reinterpret_cast<const float4 *>(cft + (g & 0xFFu) * 8);
-        const float4 *gv4 = reinterpret_cast<const float4 *>(cft + ((g >> 8) & 0xFFu) * 8);
-        const float4 u0 = gu4[0], u1 = gu4[1], v0 = gv4[0], v1 = gv4[1];
-        const float gu[NTAP] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z};
-        const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
-        float rr = 0.f, ri = 0.f, su = 0.f, sv = 0.f;
+    const int q = threadIdx.x & 3;
+    const bool hi2 = (q & 2) != 0, hi1 = (q & 1) != 0;
+    constexpr uint32_t FULL = 0xffffffffu;
+    constexpr uint32_t GDD_PAD = 0x4040u;  // offsets 0, cell 0: a harmless table row
+    // Every lane of a warp runs the same number of group iterations (the loop bounds are
+    // per CTA), so the shuffles below always see all 32 lanes.
+    const int ngroups_iter = (it.cend - it.cbeg + DG_GROUPS - 1) / DG_GROUPS;
+    for (int gi = 0; gi < ngroups_iter; gi++) {
+        const int c = it.cbeg + gi * DG_GROUPS + (threadIdx.x >> 2);
+        const bool live = c < it.cend;
+        const uint2 ch = live ? chunks[c] : make_uint2(0u, 0u);
+        const int start = (int)ch.x, len = live ? (int)(ch.y >> 16) : 0;
+        const int cell = (int)(ch.y & 4095u), lu = cell & 63, lv = cell >> 6;
+        float2 G0[NTAP], G1[NTAP];
 #pragma unroll
         for (int b = 0; b < NTAP; b++) {
             const float2 *row = &tile[(lv + b) * STILE + lu];
-            float tr = 0.f, ti = 0.f;
-#pragma unroll
-            for (int a = 0; a < NTAP; a++) {
-                const float2 G = row[a];
-                tr = fmaf(gu[a], G.x, tr);
-                ti = fmaf(gu[a], G.y, ti);
-            }
-            rr = fmaf(gv[b], tr, rr);
-            ri = fmaf(gv[b], ti, ri);
-            sv += gv[b];
-            su += gu[b];
+            G0[b] = row[q];
+            G1[b] = q + 4 < NTAP ? row[q + 4] : make_float2(0.f, 0.f);
         }
-        const float inv = 1.0f / (su * sv);
-        float mr = rr * inv, mi = ri * inv;
-        if (MODE == 0) {
-            const float2 o = fobs[p];
-            fres[p] = make_float2(o.x - mr, o.y - mi);
-        } else {
-            if (gconj[p]) mi = -mi;
-            float2 vv = make_float2(mr, mi);
-            if (rot) {
-                const float2 rt = rot[p];
-                vv = make_float2(mr * rt.x - mi * rt.y, mr * rt.y + mi * rt.x);
+        // the warp iterates to the longest chunk among its 8 groups
+        int wlen = len;
+#pragma unroll
+        for (int d = 4; d < 32; d <<= 1) wlen = max(wlen, __shfl_xor_sync(FULL, wlen, d));
+        // the next batch's offset words and observed value load during this batch
+        uint32_t gn[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) gn[u] = u < len ? gdd[start + u] : GDD_PAD;
+        float2 obn = make_float2(0.f, 0.f);
+        if (MODE == 0 && q < len) obn = fobs[start + q];
+        for (int k = 0; k < wlen; k += 4) {
+            const int pq = start + k + q;
+            const bool mine = k + q < len;
+            const float2 ob = obn;
+            uint32_t gc[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                gc[u] = gn[u];
+                gn[u] = k + 4 + u < len ? gdd[start + k + 4 + u] : GDD_PAD;
             }
-            const uint32_t o = orig[p];
-            vis_out[o] = vv;
-            wt_out[o] = wt[p];
+            if (MODE == 0 && k + 4 + q < len) obn = fobs[pq + 4];
+            float pr[4], pim[4];
+            uint32_t gq = GDD_PAD;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t g = gc[u];
+                if (u == q) gq = g;
+                const float2 gu = cfp[(g & 0xFFu) * CFP_STRIDE + q];
+                const float4 *gv4 = reinterpret_cast<const float4 *>(cft + ((g >> 8) & 0xFFu) * CFV_STRIDE);
+                const float4 v0 = gv4[0], v1 = gv4[1];
+                const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
+                float c0r = 0.f, c0i = 0.f, c1r = 0.f, c1i = 0.f;
+#pragma unroll
+                for (int b = 0; b < NTAP; b++) {
+                    c0r = fmaf(gv[b], G0[b].x, c0r);
+                    c0i = fmaf(gv[b], G0[b].y, c0i);
+                    c1r = fmaf(gv[b], G1[b].x, c1r);
+                    c1i = fmaf(gv[b], G1[b].y, c1i);
+                }
+                pr[u] = fmaf(gu.y, c1r, gu.x * c0r);
+                pim[u] = fmaf(gu.y, c1i, gu.x * c0i);
+            }
+            // butterfly over lane bit 1: keep visibilities {0,1} (or {2,3}), pass the others
+            float k0r = hi2 ? pr[2] : pr[0], k0i = hi2 ? pim[2] : pim[0];
+            float k1r = hi2 ? pr[3] : pr[1], k1i = hi2 ? pim[3] : pim[1];
+            const float s0r = hi2 ? pr[0] : pr[2], s0i = hi2 ? pim[0] : pim[2];
+            const float s1r = hi2 ? pr[1] : pr[3], s1i = hi2 ? pim[1] : pim[3];
+            k0r += __shfl_xor_sync(FULL, s0r, 2);
+            k0i += __shfl_xor_sync(FULL, s0i, 2);
+            k1r += __shfl_xor_sync(FULL, s1r, 2);
+            k1i += __shfl_xor_sync(FULL, s1i, 2);
+            // butterfly over lane bit 0: keep visibility q
+            float tr = hi1 ? k1r : k0r, ti = hi1 ? k1i : k0i;
+            tr += __shfl_xor_sync(FULL, hi1 ? k0r : k1r, 1);
+            ti += __shfl_xor_sync(FULL, hi1 ? k0i : k1i, 1);
+            if (!mine || (gq & GDD_EXCEPTION)) continue;
+            const float inv = 1.0f / (rsum[gq & 0xFFu] * rsum[(gq >> 8) & 0xFFu]);
+            float mr = tr * inv, mi = ti * inv;
+            if (MODE == 0) {
+                fres[pq] = make_float2(ob.x - mr, ob.y - mi);
+            } else {
+                if (gconj[pq]) mi = -mi;
+                float2 vv = make_float2(mr, mi);
+                if (rot) {
+                    const float2 rt = rot[pq];
+                    vv = make_float2(mr * rt.x - mi * rt.y, mr * rt.y + mi * rt.x);
+                }
+                const uint32_t o = orig[pq];
+                vis_out[o] = vv;
+                wt_out[o] = wt[pq];
+            }
         }
     }
 }
@@ -480,8 +597,10 @@ int make_grid_tmap(CUtensorMap *map, const float *grid, int pitch, int nv) {
     return SDE_OK;
 }
 
-size_t grid_smem() { return sizeof(float2) * STILE * STILE + sizeof(float) * CFT_FLOATS + sizeof(float2) * 129 * 4; }
-size_t degrid_smem() { return DG_TX_BYTES + sizeof(float) * CFT_FLOATS + 16; }
+size_t grid_smem() {
+    return sizeof(float2) * STILE * STILE + sizeof(float) * CFV_FLOATS + sizeof(float2) * CFP_PAIRS;
+}
+size_t degrid_smem() { return DG_BAR_OFF + 16; }
 
 }  // namespace
 
@@ -510,7 +629,7 @@ int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt) {
     double *part;
     SDE_TRY(ctx_scratch(ctx, "gs_part", sizeof(double) * 2 * (size_t)nb, (void **)&part));
     KTimer kt(ctx, "plan_sums");
-    k_plan_sums<<<nb, RED_T, 0, ctx->stream>>>(pl->wt, pl->gdg, pl->cft, pl->nvis, part);
+    k_plan_sums<<<nb, RED_T, 0, ctx->stream>>>(pl->wg, pl->cft, pl->nvis, part);
     SDE_CHECK_LAUNCH();
     k_sum_pairs<<<1, 32, 0, ctx->stream>>>(part, nb, pl->d_sums);
     SDE_CHECK_LAUNCH();
@@ -548,10 +667,10 @@ int plan_grid_raw(sde_plan *pl, int what, float2 *raw) {
     KTimer kt(ctx, what == SDE_GRID_PSF ? "grid_psf" : "grid");
     if (what == SDE_GRID_PSF)
         k_grid<true><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
-            pl->items, pl->chunks, pl->fres, pl->wt, pl->gdg, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+            pl->items, pl->chunks, pl->fres, pl->wg, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
     else
         k_grid<false><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
-            pl->items, pl->chunks, pl->fres, pl->wt, pl->gdg, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+            pl->items, pl->chunks, pl->fres, pl->wg, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
@@ -575,11 +694,11 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
         KTimer kt(ctx, "degrid");
         if (mode == 0)
             k_degrid<0><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->gdd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot, pl->orig,
+                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot, pl->orig,
                 pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
         else
             k_degrid<1><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->gdd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot, pl->orig,
+                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot, pl->orig,
                 pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
         SDE_CHECK_LAUNCH();
     }

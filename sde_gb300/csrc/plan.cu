@@ -146,8 +146,8 @@ __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned 
                               const uint16_t *__restrict__ gdg_u, const uint32_t *__restrict__ gdd_u,
                               const float2 *__restrict__ rot_u,
                               const uint8_t *__restrict__ gconj_u, float2 *fobs, float2 *fres,
-                              float *wt, uint16_t *gdg, uint32_t *gdd, uint32_t *orig, float2 *rot,
-                              uint8_t *gconj, uint32_t *pos_of) {
+                              float *wt, float2 *wg, uint32_t *gdd, uint32_t *orig,
+                              float2 *rot, uint8_t *gconj, uint32_t *pos_of) {
     int64_t nv = (int64_t)counts[0];
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
@@ -156,7 +156,7 @@ __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned 
     fobs[p] = f;
     fres[p] = f;
     wt[p] = wt_u[i];
-    gdg[p] = gdg_u[i];
+    wg[p] = make_float2(wt_u[i], __uint_as_float((uint32_t)gdg_u[i]));
     gdd[p] = gdd_u[i];
     orig[p] = i;
     gconj[p] = gconj_u[i];
@@ -253,10 +253,22 @@ __global__ void k_chunk_write(const uint32_t *__restrict__ keys, const unsigned 
     uint32_t j = ((uint32_t)q - (uint32_t)cs) / CHUNK_MAX;
     uint32_t cell = k & 4095u, lu = cell & 63u, lv = cell >> 6;
     uint32_t color = (lu % 7u) * 7u + (lv % 7u);
-    ckey[c] = ((uint64_t)it << (6 + jbits + 12)) | ((uint64_t)color << (jbits + 12)) |
-              ((uint64_t)j << 12) | cell;
+    ckey[c] = ((uint64_t)it << (6 + LBITS + jbits + 12)) |
+              ((uint64_t)color << (LBITS + jbits + 12)) | ((uint64_t)j << 12) | cell;
     cval[c] = c;
     cstart[c] = (uint32_t)q;
+}
+
+// Length class (CHUNK_MAX - length) of each chunk, above the chunk index in its sort key:
+// within a colour class longer chunks come first, so the 8 chunks that a warp of the
+// gridder or degridder takes together have similar lengths.
+__global__ void k_chunk_len(const uint32_t *__restrict__ cstart, int64_t nchunks, int64_t nvalid,
+                            int lshift, uint64_t *ckey) {
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const uint32_t en = c + 1 < nchunks ? cstart[c + 1] : (uint32_t)nvalid;
+    const uint32_t len = en - cstart[c];
+    ckey[c] |= (uint64_t)(CHUNK_MAX - len) << lshift;
 }
 
 __global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t *__restrict__ cval,
@@ -306,7 +318,7 @@ int sde_plan_destroy(sde_plan *pl) {
     sde_ctx *ctx = pl->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    void *ptrs[] = {pl->fobs, pl->fres, pl->wt, pl->gdg, pl->gdd, pl->orig, pl->rot, pl->gconj, pl->chunks,
+    void *ptrs[] = {pl->fobs, pl->fres, pl->wt, pl->wg, pl->gdd, pl->orig, pl->rot, pl->gconj, pl->chunks,
                     pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -432,7 +444,7 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
         PL_TRY(plan_alloc(pl, (void **)&pl->fobs, 8 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->fres, 8 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->wt, 4 * nv1));
-        PL_TRY(plan_alloc(pl, (void **)&pl->gdg, 2 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->wg, 8 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->gdd, 4 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->orig, 4 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->gconj, nv1));
@@ -441,8 +453,8 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
         if (nvalid > 0) {
             k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, fobs_u, dwt, gdg_u, gdd_u,
                                                            rot_u, gconj_u, pl->fobs, pl->fres,
-                                                           pl->wt, pl->gdg, pl->gdd, pl->orig,
-                                                           pl->rot, pl->gconj, pos_of);
+                                                           pl->wt, pl->wg, pl->gdd,
+                                                           pl->orig, pl->rot, pl->gconj, pos_of);
             PL_CUDA(cudaGetLastError());
         }
         // exception list (also carries the GRDDEH2D geometry of non-gridding visibilities)
@@ -500,7 +512,10 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
                                                            chead, item_id, chunk_id, jbits, ckey,
                                                            cval, cstart, pl->items);
             PL_CUDA(cudaGetLastError());
-            const int shift_item = 6 + jbits + 12;
+            k_chunk_len<<<ceil_div(nchunks, T), T, 0, st>>>(cstart, nchunks, nvalid, jbits + 12,
+                                                          ckey);
+            PL_CUDA(cudaGetLastError());
+            const int shift_item = 6 + LBITS + jbits + 12;
             const int cbits = shift_item + bits_for(nitems);
             PL_TRY(launch_radix_sort_u64(ctx, ckey, cval, nchunks, cbits, cktmp, cvtmp));
             k_chunk_final<<<ceil_div(nchunks, T), T, 0, st>>>(ckey, cval, cstart, keys, nchunks,
