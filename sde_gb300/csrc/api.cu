@@ -322,8 +322,10 @@ extern "C" int sde_plan_degrid_residual(sde_plan *pl, const float *grid, int pit
 extern "C" int sde_plan_reset_residual(sde_plan *pl) {
     if (!pl) return SDE_EINVAL;
     if (pl->nvis > 0)
-        SDE_CUDA_TRY(cudaMemcpyAsync(pl->fres, pl->fobs, sizeof(float2) * (size_t)pl->nvis,
-                                     cudaMemcpyDeviceToDevice, pl->ctx->stream));
+        SDE_CUDA_TRY(cudaMemcpy2DAsync(reinterpret_cast<char *>(pl->rec) + sizeof(float2),
+                                       sizeof(float4), pl->fobs, sizeof(float2), sizeof(float2),
+                                       (size_t)pl->nvis, cudaMemcpyDeviceToDevice,
+                                       pl->ctx->stream));
     return SDE_OK;
 }
 

@@ -161,9 +161,9 @@ struct sde_plan {
     int64_t nitems = 0, nchunks = 0, nexc = 0;
     // sorted, gridding-valid visibilities
     float2 *fobs = nullptr;   // observed, in the gridding frame (rotated, conjugated)
-    float2 *fres = nullptr;   // residual, gridding frame
+    float4 *rec = nullptr;    // {WT, gdg bits, residual re, residual im} (gridding frame):
+                              // the gridder reads one 16-byte record per visibility
     float *wt = nullptr;
-    float2 *wg = nullptr;     // {WT, gdg bits}: the gridder's per-visibility static record
     uint32_t *gdd = nullptr;  // degridding offsets + cell + exception flag
     uint32_t *orig = nullptr; // caller index of each sorted visibility
     float2 *rot = nullptr;    // (cos, sin) of the phase rotation (doshift only), sorted
@@ -234,6 +234,14 @@ __device__ __forceinline__ void prefetch_l2_range(const void *base, int64_t firs
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(n) : "memory");
         a += n;
     }
+}
+
+// The residual half of a plan record.
+__device__ __forceinline__ float2 *rec_res(float4 *rec, int64_t p) {
+    return reinterpret_cast<float2 *>(rec + p) + 1;
+}
+__device__ __forceinline__ float2 rec_res(const float4 *rec, int64_t p) {
+    return reinterpret_cast<const float2 *>(rec + p)[1];
 }
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }

@@ -24,52 +24,83 @@ constexpr int GLANES = 4;                          // lanes per chunk
 constexpr int GGROUPS = GRID_THREADS / GLANES;     // chunks in flight per CTA
 constexpr int GRID_AHEAD = 2;                      // record prefetch distance (visibilities)
 constexpr int GRID_MINB = 4;                       // resident CTAs per SM the kernel is built for
-constexpr int CFT_FLOATS = 129 * 8;                // global table [129][8]
-// Shared copies of the table, strided so that the 8 rows a warp reads at once (one per
-// 4-lane group) fall on 8 different bank positions: v taps [129][12] (two float4 per row),
-// u tap pairs (col q, col q+4) [129][5] float2.
-constexpr int CFV_STRIDE = 12;
-constexpr int CFP_STRIDE = 5;
-constexpr int CFV_FLOATS = 129 * CFV_STRIDE;
-constexpr int CFP_PAIRS = 129 * CFP_STRIDE;
+// Shared copy of the tap table, one layout for both reads a 4-lane group makes per
+// visibility.  A chunk covers a pair of cells (lu0, lu0+1), so its footprint is 8 columns
+// wide; lane q owns window columns q and q+4, which for a visibility in the pair's column
+// off (0 or 1) are taps q-off and q+4-off.  A row holds the taps as 5 pairs,
+// (a0,a4) (a1,a5) (a2,a6) (a3,0) (0,a3): lane q reads pair (q - off) mod 5 as one float2,
+// and the seven v taps are the first 8 floats, read as two float4 by every lane.  Rows are
+// padded to 12 floats (float4 alignment).  (Keeping several bank-staggered copies of the
+// table, one per group of a half-warp, removes its bank conflicts but measured slower: the
+// extra shared memory costs a resident CTA per SM.)
+constexpr int TAP_ROW = 12;
+constexpr int TAP_COPIES = 1;
+constexpr int TAP_STRIDE = TAP_ROW * TAP_COPIES;    // floats per table row
+constexpr int TAP_FLOATS = 129 * TAP_STRIDE;
 
-__device__ __forceinline__ void fill_tap_tables(const float *__restrict__ cft_g, float *cfv,
-                                                float2 *cfp, int nthreads) {
-    for (int k = threadIdx.x; k < 129 * 8; k += nthreads)
-        cfv[(k >> 3) * CFV_STRIDE + (k & 7)] = cft_g[k];
-    for (int k = threadIdx.x; k < 129 * 4; k += nthreads) {
-        const int d = k >> 2, q = k & 3;
-        cfp[d * CFP_STRIDE + q] =
-            make_float2(cft_g[d * 8 + q], q + 4 < NTAP ? cft_g[d * 8 + q + 4] : 0.f);
+__device__ __forceinline__ void fill_tap_table(const float *__restrict__ cft_g, float *tab,
+                                               int nthreads) {
+    // row entry e -> tap index (0 4 1 5 2 6 3 7 | 7 3 | 7 7); tap 7 is the table's zero
+    for (int k = threadIdx.x; k < TAP_FLOATS; k += nthreads) {
+        const int d = k / TAP_STRIDE, e = k % TAP_ROW;
+        const int a = e < 8 ? (e >> 1) + 4 * (e & 1) : (e == 9 ? 3 : 7);
+        tab[k] = cft_g[d * 8 + a];
     }
 }
 
-// Gridding.  Lane q of a 4-lane group owns footprint columns q and q+4 (q+4 = 7 is empty)
-// of its chunk's cell and accumulates 7 rows x 2 columns x complex in registers; the chunk's
-// visibilities are read once per group (same addresses: L1 broadcast).  The shared tile
-// receives each chunk's footprint once, through shared-memory atomics (a warp's 8 chunks
-// share a colour class, so their footprints do not overlap).
+// One visibility's taps from a group's copy of the table: u pair for lane q (g bit 16 is
+// the visibility's column in the cell pair), and v taps.
+struct Taps {
+    float2 gu;
+    float gv[NTAP];
+};
+__device__ __forceinline__ Taps read_taps(const float *tg, int q, uint32_t g) {
+    Taps t;
+    const int off = (int)((g >> 16) & 1u);
+    const int pair = q - off < 0 ? 4 : q - off;
+    t.gu = *reinterpret_cast<const float2 *>(tg + (g & 0xFFu) * TAP_STRIDE + 2 * pair);
+    const float4 *r = reinterpret_cast<const float4 *>(tg + ((g >> 8) & 0xFFu) * TAP_STRIDE);
+    const float4 v0 = r[0], v1 = r[1];
+    t.gv[0] = v0.x;
+    t.gv[1] = v0.z;
+    t.gv[2] = v1.x;
+    t.gv[3] = v1.z;
+    t.gv[4] = v0.y;
+    t.gv[5] = v0.w;
+    t.gv[6] = v1.y;
+    return t;
+}
+
+// Gridding.  A chunk holds visibilities of one cell pair (lu0, lu0+1); its footprint is a
+// 7-row x 8-column window.  Lane q of a 4-lane group owns window columns q and q+4 and
+// accumulates 7 rows x 2 columns x complex in registers; the chunk's visibilities are read
+// once per group (same addresses: L1 broadcast).  The shared tile (real and imaginary
+// planes) receives each chunk's window once, through shared-memory atomics (a warp's 8
+// chunks share a colour class, so their windows do not overlap).
 template <bool PSF>
 __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
     k_grid(const WorkItem *__restrict__ items, const uint2 *__restrict__ chunks,
-           const float2 *__restrict__ fres, const float2 *__restrict__ wg,
-           const float *__restrict__ cft_g, float2 *raw, int pitch, int ntu, int nu, int nv) {
+           const float4 *__restrict__ rec, const float *__restrict__ cft_g, float2 *raw,
+           int pitch, int ntu, int nu, int nv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2 *tile = reinterpret_cast<float2 *>(smem_raw);
-    float *cft = reinterpret_cast<float *>(tile + STILE * STILE);   // v taps
-    float2 *cfp = reinterpret_cast<float2 *>(cft + CFV_FLOATS);     // u tap pairs
+    float *tre = reinterpret_cast<float *>(smem_raw);
+    float *tim = tre + STILE * STILE;
+    float *tab = tim + STILE * STILE;  // tap table
     const WorkItem it = items[blockIdx.x];
     if (threadIdx.x == 0) {
         // the item's chunk list and records stream into L2 while the tile is cleared
         prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
-        prefetch_l2_range(wg, it.vbeg, it.vend, 8);
-        if (!PSF) prefetch_l2_range(fres, it.vbeg, it.vend, 8);
+        prefetch_l2_range(rec, it.vbeg, it.vend, 16);
     }
-    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) tile[k] = make_float2(0.f, 0.f);
-    fill_tap_tables(cft_g, cft, cfp, GRID_THREADS);
+    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
+        tre[k] = 0.f;
+        tim[k] = 0.f;
+    }
+    fill_tap_table(cft_g, tab, GRID_THREADS);
     __syncthreads();
     const int q = threadIdx.x & (GLANES - 1);
     const int grp = threadIdx.x / GLANES;
+    const float *tg = tab + (grp & (TAP_COPIES - 1)) * TAP_ROW;  // this group's copy
     for (int c = it.cbeg + grp; c < it.cend; c += GGROUPS) {
         const uint2 ch = chunks[c];
         const int start = (int)ch.x, cell = (int)(ch.y & 4095u), len = (int)(ch.y >> 16);
@@ -86,33 +117,25 @@ __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
         }
         // GRID_AHEAD visibilities ahead: their records and values load while this one
         // accumulates (a register ring, indexed by constants after unrolling)
-        const float2 *pw = wg + start, *pf = fres + start;
-        float2 rb[GRID_AHEAD], fb[GRID_AHEAD];
+        const float4 *pr = rec + start;
+        float4 rb[GRID_AHEAD];
 #pragma unroll
-        for (int j = 0; j < GRID_AHEAD; j++) {
-            rb[j] = j < len ? pw[j] : make_float2(0.f, 0.f);
-            fb[j] = (!PSF && j < len) ? pf[j] : make_float2(0.f, 0.f);
-        }
+        for (int j = 0; j < GRID_AHEAD; j++) rb[j] = j < len ? pr[j] : make_float4(0.f, 0.f, 0.f, 0.f);
         for (int k = 0; k < len; k += GRID_AHEAD) {
 #pragma unroll
             for (int j = 0; j < GRID_AHEAD; j++) {
                 if (k + j >= len) break;
-                const float2 rec = rb[j], f = fb[j];
-                if (k + j + GRID_AHEAD < len) {
-                    rb[j] = pw[k + j + GRID_AHEAD];
-                    if (!PSF) fb[j] = pf[k + j + GRID_AHEAD];
-                }
-                const uint32_t g = __float_as_uint(rec.y);
-                const float w = rec.x;
-                const float2 gu = cfp[(g & 0xFFu) * CFP_STRIDE + q];
-                const float4 *gv4 =
-                    reinterpret_cast<const float4 *>(cft + ((g >> 8) & 0xFFu) * CFV_STRIDE);
-                const float4 v0 = gv4[0], v1 = gv4[1];
-                const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
+                const float4 r = rb[j];
+                if (k + j + GRID_AHEAD < len) rb[j] = pr[k + j + GRID_AHEAD];
+                const uint32_t g = __float_as_uint(r.y);
+                const float w = r.x;
+                const Taps t = read_taps(tg, q, g);
+                const float2 gu = t.gu;
+                const float *gv = t.gv;
                 float fr = w, fi = 0.f;
                 if (!PSF) {
-                    fr = w * f.x;
-                    fi = w * f.y;
+                    fr = w * r.z;
+                    fi = w * r.w;
                 }
                 const float h0r = gu.x * fr, h1r = gu.y * fr;
                 const float h0i = gu.x * fi, h1i = gu.y * fi;
@@ -129,19 +152,18 @@ __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
         }
 #pragma unroll
         for (int b = 0; b < NTAP; b++) {
-            float2 *row = &tile[(lv + b) * STILE + lu];
-            atomicAdd(&row[q].x, a0r[b]);
-            if (!PSF) atomicAdd(&row[q].y, a0i[b]);
-            if (q + 4 < NTAP) {
-                atomicAdd(&row[q + 4].x, a1r[b]);
-                if (!PSF) atomicAdd(&row[q + 4].y, a1i[b]);
-            }
+            float *rr = &tre[(lv + b) * STILE + lu + q];
+            float *ri = &tim[(lv + b) * STILE + lu + q];
+            atomicAdd(rr, a0r[b]);
+            if (!PSF) atomicAdd(ri, a0i[b]);
+            atomicAdd(rr + 4, a1r[b]);
+            if (!PSF) atomicAdd(ri + 4, a1i[b]);
         }
     }
     __syncthreads();
     const int tu = it.tile % ntu, tv = it.tile / ntu;
     for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
-        const float2 val = tile[k];
+        const float2 val = make_float2(tre[k], tim[k]);
         if (val.x == 0.f && val.y == 0.f) continue;
         const int r = k / STILE, cc = k - r * STILE;
         const int gv0 = tv * TILE + r - SUPP, gu0 = tu * TILE + cc - SUPP;  // 0-based raw
@@ -152,14 +174,14 @@ __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
 
 // Plan-invariant sums: LSUMWT = sum of UVWT (grd/grdh2d.f:185) and SUMWT (grd/grdh2d.f:157).
 constexpr int RED_T = 256;
-__global__ void __launch_bounds__(RED_T) k_plan_sums(const float2 *__restrict__ wg,
+__global__ void __launch_bounds__(RED_T) k_plan_sums(const float4 *__restrict__ rec,
                                                       const float *__restrict__ cft, int64_t n,
                                                       double *partial) {
     __shared__ double sh[2][RED_T / 32];
     double s0 = 0.0, s1 = 0.0;
     for (int64_t p = (int64_t)blockIdx.x * RED_T + threadIdx.x; p < n; p += (int64_t)gridDim.x * RED_T) {
-        const float2 rec = wg[p];
-        const uint32_t g = __float_as_uint(rec.y);
+        const float2 wgp = reinterpret_cast<const float2 *>(rec + p)[0];
+        const uint32_t g = __float_as_uint(wgp.y);
         const float *gu = cft + (g & 0xFFu) * 8, *gv = cft + ((g >> 8) & 0xFFu) * 8;
         float su = 0.f, sv = 0.f;
 #pragma unroll
@@ -167,7 +189,7 @@ __global__ void __launch_bounds__(RED_T) k_plan_sums(const float2 *__restrict__ 
             su += gu[a];
             sv += gv[a];
         }
-        const float w = rec.x;
+        const float w = wgp.x;
         s0 += (double)w * (double)su * (double)sv;
         s1 += (double)w;
     }
@@ -259,17 +281,17 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
 
 constexpr int DG_GROUPS = DG_THREADS / 4;          // chunks in flight per CTA
 constexpr int RSUM_FLOATS = 132;                    // 129 row sums, padded
-constexpr size_t DG_CFT_OFF = DG_TX_BYTES;
-constexpr size_t DG_CFP_OFF = DG_CFT_OFF + sizeof(float) * CFV_FLOATS;
-constexpr size_t DG_RSUM_OFF = DG_CFP_OFF + sizeof(float2) * CFP_PAIRS;
+constexpr size_t DG_TAB_OFF = DG_TX_BYTES;
+constexpr size_t DG_RSUM_OFF = DG_TAB_OFF + sizeof(float) * TAP_FLOATS;
 constexpr size_t DG_BAR_OFF = DG_RSUM_OFF + sizeof(float) * RSUM_FLOATS;
-static_assert(DG_CFT_OFF % 16 == 0 && DG_CFP_OFF % 16 == 0 && DG_BAR_OFF % 8 == 0, "layout");
+static_assert(DG_TAB_OFF % 16 == 0 && DG_BAR_OFF % 8 == 0, "layout");
 
 // mode 0: residual update in the gridding frame; mode 1: caller-order output (user frame).
-// A 4-lane group per chunk (the chunk's visibilities share one degridding cell, or carry
-// GDD_EXCEPTION and are skipped here).  Lane q holds columns q and q+4 of the cell's 7x7
-// neighbourhood in registers, read once per chunk from the TMA-staged tile, and for each
-// visibility forms sum_b gv[b] G[b][col] per column, then gu[col] times that: a partial
+// A 4-lane group per chunk (the chunk's visibilities lie in one cell pair -- their
+// degridding cell is their gridding cell -- or carry GDD_EXCEPTION and are skipped here).
+// Lane q holds columns q and q+4 of the pair's 7x8 neighbourhood window in registers, read
+// once per chunk from the TMA-staged tile, and for each visibility forms
+// sum_b gv[b] G[b][col] per column, then the u tap of that column times that: a partial
 // sum over its columns.  Four visibilities' partials are reduced across the group with a
 // transposing butterfly (6 shuffles per lane), after which lane q owns visibility q of the
 // four and finishes it: divide by (sum gu)(sum gv) (row sums in the same order as a plain
@@ -278,14 +300,13 @@ template <int MODE>
 __global__ void __launch_bounds__(DG_THREADS, 4)
     k_degrid(const __grid_constant__ CUtensorMap tmap, const WorkItem *__restrict__ items,
              const uint2 *__restrict__ chunks, const uint32_t *__restrict__ gdd,
-             const float *__restrict__ cft_g, const float2 *__restrict__ fobs, float2 *fres,
+             const float *__restrict__ cft_g, const float2 *__restrict__ fobs, float4 *rec,
              const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
              const uint32_t *__restrict__ orig, const float *__restrict__ wt, float2 *vis_out,
              float *wt_out, int ntu, int *status) {
     extern __shared__ __align__(128) unsigned char smem_dg[];
     float2 *tile = reinterpret_cast<float2 *>(smem_dg);
-    float *cft = reinterpret_cast<float *>(smem_dg + DG_CFT_OFF);
-    float2 *cfp = reinterpret_cast<float2 *>(smem_dg + DG_CFP_OFF);
+    float *tab = reinterpret_cast<float *>(smem_dg + DG_TAB_OFF);
     float *rsum = reinterpret_cast<float *>(smem_dg + DG_RSUM_OFF);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_dg + DG_BAR_OFF);
     const WorkItem it = items[blockIdx.x];
@@ -310,7 +331,7 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
         prefetch_l2_range(gdd, it.vbeg, it.vend, 4);
         if (MODE == 0) prefetch_l2_range(fobs, it.vbeg, it.vend, 8);
     }
-    fill_tap_tables(cft_g, cft, cfp, DG_THREADS);
+    fill_tap_table(cft_g, tab, DG_THREADS);
     for (int d = threadIdx.x; d < 129; d += DG_THREADS) {
         float sacc = 0.f;
 #pragma unroll
@@ -335,6 +356,8 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
     __syncthreads();
     const int q = threadIdx.x & 3;
     const bool hi2 = (q & 2) != 0, hi1 = (q & 1) != 0;
+    const int grp = threadIdx.x >> 2;
+    const float *tg = tab + (grp & (TAP_COPIES - 1)) * TAP_ROW;  // this group's copy
     constexpr uint32_t FULL = 0xffffffffu;
     constexpr uint32_t GDD_PAD = 0x4040u;  // offsets 0, cell 0: a harmless table row
     // Every lane of a warp runs the same number of group iterations (the loop bounds are
@@ -351,39 +374,34 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
         for (int b = 0; b < NTAP; b++) {
             const float2 *row = &tile[(lv + b) * STILE + lu];
             G0[b] = row[q];
-            G1[b] = q + 4 < NTAP ? row[q + 4] : make_float2(0.f, 0.f);
+            G1[b] = row[q + 4];
         }
         // the warp iterates to the longest chunk among its 8 groups
         int wlen = len;
 #pragma unroll
         for (int d = 4; d < 32; d <<= 1) wlen = max(wlen, __shfl_xor_sync(FULL, wlen, d));
-        // the next batch's offset words and observed value load during this batch
-        uint32_t gn[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) gn[u] = u < len ? gdd[start + u] : GDD_PAD;
+        // lane q loads the offset word and observed value of visibility q of the next batch
+        // (one coalesced load per group); the group shares the words by shuffle
+        const int gbase = threadIdx.x & 28;  // lane of q = 0 in this group
+        uint32_t gqn = q < len ? gdd[start + q] : GDD_PAD;
         float2 obn = make_float2(0.f, 0.f);
         if (MODE == 0 && q < len) obn = fobs[start + q];
         for (int k = 0; k < wlen; k += 4) {
             const int pq = start + k + q;
             const bool mine = k + q < len;
             const float2 ob = obn;
-            uint32_t gc[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                gc[u] = gn[u];
-                gn[u] = k + 4 + u < len ? gdd[start + k + 4 + u] : GDD_PAD;
+            const uint32_t gq = gqn;
+            if (k + 4 + q < len) {
+                gqn = gdd[pq + 4];
+                if (MODE == 0) obn = fobs[pq + 4];
             }
-            if (MODE == 0 && k + 4 + q < len) obn = fobs[pq + 4];
             float pr[4], pim[4];
-            uint32_t gq = GDD_PAD;
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const uint32_t g = gc[u];
-                if (u == q) gq = g;
-                const float2 gu = cfp[(g & 0xFFu) * CFP_STRIDE + q];
-                const float4 *gv4 = reinterpret_cast<const float4 *>(cft + ((g >> 8) & 0xFFu) * CFV_STRIDE);
-                const float4 v0 = gv4[0], v1 = gv4[1];
-                const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
+                const uint32_t g = __shfl_sync(FULL, gq, gbase + u);
+                const Taps t = read_taps(tg, q, g);
+                const float2 gu = t.gu;
+                const float *gv = t.gv;
                 float c0r = 0.f, c0i = 0.f, c1r = 0.f, c1i = 0.f;
 #pragma unroll
                 for (int b = 0; b < NTAP; b++) {
@@ -412,7 +430,7 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
             const float inv = 1.0f / (rsum[gq & 0xFFu] * rsum[(gq >> 8) & 0xFFu]);
             float mr = tr * inv, mi = ti * inv;
             if (MODE == 0) {
-                fres[pq] = make_float2(ob.x - mr, ob.y - mi);
+                *rec_res(rec, pq) = make_float2(ob.x - mr, ob.y - mi);
             } else {
                 if (gconj[pq]) mi = -mi;
                 float2 vv = make_float2(mr, mi);
@@ -435,7 +453,7 @@ __global__ void k_degrid_exc(const DegridExc *__restrict__ exc, const float *__r
                              const float2 *__restrict__ exc_rot, int64_t nexc,
                              const float2 *__restrict__ grid, int pitch, int nu, int nv,
                              int uorigin, int vorigin, const float *__restrict__ cf,
-                             int doshift, const float2 *__restrict__ fobs, float2 *fres,
+                             int doshift, const float2 *__restrict__ fobs, float4 *rec,
                              float2 *vis_out, float *wt_out, unsigned long long *nbad) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nexc) return;
@@ -523,18 +541,18 @@ __global__ void k_degrid_exc(const DegridExc *__restrict__ exc, const float *__r
         }
         if (e.gconj) mi = -mi;
         const float2 o = fobs[e.pos];
-        fres[e.pos] = make_float2(o.x - mr, o.y - mi);
+        *rec_res(rec, e.pos) = make_float2(o.x - mr, o.y - mi);
     }
 }
 
 // residual back to the caller's frame and order: V = conj?(F) * (c, s), the inverse of
 // F = conj?(V * (c, -s)) applied when the plan was built
-__global__ void k_scatter_vis(const float2 *__restrict__ src, const uint32_t *__restrict__ orig,
+__global__ void k_scatter_vis(const float4 *__restrict__ rec, const uint32_t *__restrict__ orig,
                               const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
                               int64_t n, float2 *dst) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    float2 f = src[p];
+    float2 f = rec_res(rec, p);
     if (gconj[p]) f.y = -f.y;
     if (rot) {
         const float2 r = rot[p];
@@ -546,7 +564,7 @@ __global__ void k_scatter_vis(const float2 *__restrict__ src, const uint32_t *__
 // frame transform of the caller's visibilities into the plan's residual (sde_plan_set_vis)
 __global__ void k_set_vis(const float2 *__restrict__ vis_user, const uint32_t *__restrict__ orig,
                           const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
-                          int64_t n, float2 *fobs, float2 *fres) {
+                          int64_t n, float2 *fobs, float4 *rec) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     float2 v = vis_user[orig[p]];
@@ -558,7 +576,7 @@ __global__ void k_set_vis(const float2 *__restrict__ vis_user, const uint32_t *_
     }
     if (gconj[p]) fi = -fi;
     fobs[p] = make_float2(fr, fi);
-    fres[p] = make_float2(fr, fi);
+    *rec_res(rec, p) = make_float2(fr, fi);
 }
 
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -597,9 +615,7 @@ int make_grid_tmap(CUtensorMap *map, const float *grid, int pitch, int nv) {
     return SDE_OK;
 }
 
-size_t grid_smem() {
-    return sizeof(float2) * STILE * STILE + sizeof(float) * CFV_FLOATS + sizeof(float2) * CFP_PAIRS;
-}
+size_t grid_smem() { return sizeof(float) * (2 * STILE * STILE + TAP_FLOATS); }
 size_t degrid_smem() { return DG_BAR_OFF + 16; }
 
 }  // namespace
@@ -629,7 +645,7 @@ int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt) {
     double *part;
     SDE_TRY(ctx_scratch(ctx, "gs_part", sizeof(double) * 2 * (size_t)nb, (void **)&part));
     KTimer kt(ctx, "plan_sums");
-    k_plan_sums<<<nb, RED_T, 0, ctx->stream>>>(pl->wg, pl->cft, pl->nvis, part);
+    k_plan_sums<<<nb, RED_T, 0, ctx->stream>>>(pl->rec, pl->cft, pl->nvis, part);
     SDE_CHECK_LAUNCH();
     k_sum_pairs<<<1, 32, 0, ctx->stream>>>(part, nb, pl->d_sums);
     SDE_CHECK_LAUNCH();
@@ -667,10 +683,10 @@ int plan_grid_raw(sde_plan *pl, int what, float2 *raw) {
     KTimer kt(ctx, what == SDE_GRID_PSF ? "grid_psf" : "grid");
     if (what == SDE_GRID_PSF)
         k_grid<true><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
-            pl->items, pl->chunks, pl->fres, pl->wg, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+            pl->items, pl->chunks, pl->rec, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
     else
         k_grid<false><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
-            pl->items, pl->chunks, pl->fres, pl->wg, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+            pl->items, pl->chunks, pl->rec, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
@@ -694,11 +710,11 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
         KTimer kt(ctx, "degrid");
         if (mode == 0)
             k_degrid<0><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot, pl->orig,
+                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot, pl->orig,
                 pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
         else
             k_degrid<1><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->fres, pl->gconj, pl->rot, pl->orig,
+                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot, pl->orig,
                 pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
         SDE_CHECK_LAUNCH();
     }
@@ -711,12 +727,12 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
         if (mode == 0)
             k_degrid_exc<0><<<ceil_div(pl->nexc, T), T, 0, ctx->stream>>>(
                 pl->exc, exc_wt, exc_rot, pl->nexc, (const float2 *)grid, pitch, nu, nv,
-                pl->spec.uorigin, pl->spec.vorigin, pl->cf, pl->doshift, pl->fobs, pl->fres,
+                pl->spec.uorigin, pl->spec.vorigin, pl->cf, pl->doshift, pl->fobs, pl->rec,
                 vis_out, wt_out, nbad_dev);
         else
             k_degrid_exc<1><<<ceil_div(pl->nexc, T), T, 0, ctx->stream>>>(
                 pl->exc, exc_wt, exc_rot, pl->nexc, (const float2 *)grid, pitch, nu, nv,
-                pl->spec.uorigin, pl->spec.vorigin, pl->cf, pl->doshift, pl->fobs, pl->fres,
+                pl->spec.uorigin, pl->spec.vorigin, pl->cf, pl->doshift, pl->fobs, pl->rec,
                 vis_out, wt_out, nbad_dev);
         SDE_CHECK_LAUNCH();
     }
@@ -727,7 +743,7 @@ int plan_scatter_residual(sde_plan *pl, float2 *dst) {
     if (pl->nvis == 0) return SDE_OK;
     KTimer kt(pl->ctx, "scatter_vis");
     k_scatter_vis<<<ceil_div(pl->nvis, 256), 256, 0, pl->ctx->stream>>>(
-        pl->fres, pl->orig, pl->gconj, pl->rot, pl->nvis, dst);
+        pl->rec, pl->orig, pl->gconj, pl->rot, pl->nvis, dst);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
@@ -737,7 +753,7 @@ int plan_set_vis_dev(sde_plan *pl, const float2 *vis_user) {
     KTimer kt(pl->ctx, "set_vis");
     k_set_vis<<<ceil_div(pl->nvis, 256), 256, 0, pl->ctx->stream>>>(vis_user, pl->orig, pl->gconj,
                                                                   pl->rot, pl->nvis, pl->fobs,
-                                                                  pl->fres);
+                                                                  pl->rec);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }

@@ -145,8 +145,8 @@ __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned 
                               const float2 *__restrict__ fobs_u, const float *__restrict__ wt_u,
                               const uint16_t *__restrict__ gdg_u, const uint32_t *__restrict__ gdd_u,
                               const float2 *__restrict__ rot_u,
-                              const uint8_t *__restrict__ gconj_u, float2 *fobs, float2 *fres,
-                              float *wt, float2 *wg, uint32_t *gdd, uint32_t *orig,
+                              const uint8_t *__restrict__ gconj_u, float2 *fobs, float4 *rec,
+                              float *wt, uint32_t *gdd, uint32_t *orig,
                               float2 *rot, uint8_t *gconj, uint32_t *pos_of) {
     int64_t nv = (int64_t)counts[0];
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -154,9 +154,10 @@ __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned 
     uint32_t i = perm[p];
     float2 f = fobs_u[i];
     fobs[p] = f;
-    fres[p] = f;
     wt[p] = wt_u[i];
-    wg[p] = make_float2(wt_u[i], __uint_as_float((uint32_t)gdg_u[i]));
+    // bit 16: column of the visibility's cell within its chunk's cell pair
+    const uint32_t off = (gdd_u[i] >> 16) & 1u;
+    rec[p] = make_float4(wt_u[i], __uint_as_float((uint32_t)gdg_u[i] | (off << 16)), f.x, f.y);
     gdd[p] = gdd_u[i];
     orig[p] = i;
     gconj[p] = gconj_u[i];
@@ -207,7 +208,7 @@ __global__ void k_heads(const uint32_t *__restrict__ keys, const unsigned long l
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nv) return;
     uint32_t k = keys[q];
-    bool rh = q == 0 || keys[q - 1] != k;
+    bool rh = q == 0 || (keys[q - 1] >> 1) != (k >> 1);  // runs of one cell pair
     bool th = q == 0 || (keys[q - 1] >> 12) != (k >> 12);
     runhead[q] = rh ? (int32_t)q : -1;
     tilehead[q] = th ? (int32_t)q : -1;
@@ -251,8 +252,8 @@ __global__ void k_chunk_write(const uint32_t *__restrict__ keys, const unsigned 
     int32_t is = ts + ((int32_t)q - ts) / ITEM_MAX * ITEM_MAX;
     int32_t cs = rs > is ? rs : is;
     uint32_t j = ((uint32_t)q - (uint32_t)cs) / CHUNK_MAX;
-    uint32_t cell = k & 4095u, lu = cell & 63u, lv = cell >> 6;
-    uint32_t color = (lu % 7u) * 7u + (lv % 7u);
+    uint32_t cell = k & 4094u, lu = cell & 63u, lv = cell >> 6;  // pair's even cell
+    uint32_t color = ((lu >> 1) & 3u) * 7u + (lv % 7u);
     ckey[c] = ((uint64_t)it << (6 + LBITS + jbits + 12)) |
               ((uint64_t)color << (LBITS + jbits + 12)) | ((uint64_t)j << 12) | cell;
     cval[c] = c;
@@ -280,7 +281,7 @@ __global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t 
     uint32_t orig = cval[c];
     uint32_t st = cstart[orig];
     uint32_t en = (int64_t)orig + 1 < nchunks ? cstart[orig + 1] : (uint32_t)nvalid;
-    uint32_t cell = keys[st] & 4095u;
+    uint32_t cell = keys[st] & 4094u;
     chunks[c] = make_uint2(st, cell | ((en - st) << 16));
     uint32_t it = (uint32_t)(ckey[c] >> shift_item);
     if (c == 0 || (uint32_t)(ckey[c - 1] >> shift_item) != it) items[it].cbeg = (int32_t)c;
@@ -318,7 +319,7 @@ int sde_plan_destroy(sde_plan *pl) {
     sde_ctx *ctx = pl->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    void *ptrs[] = {pl->fobs, pl->fres, pl->wt, pl->wg, pl->gdd, pl->orig, pl->rot, pl->gconj, pl->chunks,
+    void *ptrs[] = {pl->fobs, pl->rec, pl->wt, pl->gdd, pl->orig, pl->rot, pl->gconj, pl->chunks,
                     pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -442,9 +443,8 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
         pl->nexc = nexc;
         const size_t nv1 = (size_t)(nvalid > 0 ? nvalid : 1);
         PL_TRY(plan_alloc(pl, (void **)&pl->fobs, 8 * nv1));
-        PL_TRY(plan_alloc(pl, (void **)&pl->fres, 8 * nv1));
+        PL_TRY(plan_alloc(pl, (void **)&pl->rec, 16 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->wt, 4 * nv1));
-        PL_TRY(plan_alloc(pl, (void **)&pl->wg, 8 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->gdd, 4 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->orig, 4 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->gconj, nv1));
@@ -452,8 +452,8 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
         PL_TRY(plan_alloc(pl, (void **)&pl->d_sums, 4 * sizeof(double)));
         if (nvalid > 0) {
             k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, fobs_u, dwt, gdg_u, gdd_u,
-                                                           rot_u, gconj_u, pl->fobs, pl->fres,
-                                                           pl->wt, pl->wg, pl->gdd,
+                                                           rot_u, gconj_u, pl->fobs, pl->rec,
+                                                           pl->wt, pl->gdd,
                                                            pl->orig, pl->rot, pl->gconj, pos_of);
             PL_CUDA(cudaGetLastError());
         }
