@@ -427,6 +427,365 @@ int check_fft_args(int nx, int ny, int fnu, int nv, int pitch) {
     return SDE_OK;
 }
 
+// ---- compile-time-sized transforms ------------------------------------------------------
+// The same Stockham decomposition as block_fft (radix-16 passes, then one radix-8/4/2 pass),
+// with the transform length, the number of transforms in shared memory and the thread
+// count fixed at compile time: every pass unrolls with constant strides, each thread keeps
+// its butterflies' inputs in registers, and the kernels fit 64 registers (4+ resident CTAs
+// of 256 threads per SM).
+
+// v[r] *= w^r (r = 1..R-1) for w = tw[i1] (conjugated for the forward transform), with two
+// table reads: w and w^4 = tw[i4]; the other powers are products (w^2 = w w, w^3 = w^2 w,
+// w^(4a+b) = w^(4a) w^b), at most four roundings from the tabulated values.
+template <int R, bool INV>
+__device__ __forceinline__ void twiddle_powers(float2 *v, const float2 *__restrict__ tw, size_t i1,
+                                               size_t i4) {
+    float2 w1 = __ldg(&tw[i1]);
+    if (!INV) w1.y = -w1.y;
+    v[1] = cmul(v[1], w1);
+    if (R == 2) return;
+    const float2 w2 = cmul(w1, w1);
+    v[2] = cmul(v[2], w2);
+    const float2 w3 = cmul(w2, w1);
+    v[3] = cmul(v[3], w3);
+    if (R == 4) return;
+    float2 w4 = __ldg(&tw[i4]);
+    if (!INV) w4.y = -w4.y;
+    float2 wa = w4;  // w^(4a)
+#pragma unroll
+    for (int a = 1; a < R / 4; a++) {
+        if (a > 1) wa = cmul(wa, w4);
+        v[4 * a] = cmul(v[4 * a], wa);
+        v[4 * a + 1] = cmul(v[4 * a + 1], cmul(wa, w1));
+        v[4 * a + 2] = cmul(v[4 * a + 2], cmul(wa, w2));
+        v[4 * a + 3] = cmul(v[4 * a + 3], cmul(wa, w3));
+    }
+}
+
+// One radix-2^LOGR pass over NT transforms of length 2^LOGN (T threads).
+template <int LOGN, int LOGR, int LOGNS, bool INV, int NT, int T>
+__device__ __forceinline__ void st_pass(float2 *s, const float2 *__restrict__ tw, int tws) {
+    constexpr int R = 1 << LOGR, NB = 1 << (LOGN - LOGR), NS = 1 << LOGNS;
+    constexpr int TOTAL = NB * NT;
+    constexpr int PER = (TOTAL + T - 1) / T;
+    constexpr int TSHIFT = LOGN - LOGNS - LOGR;
+    float2 v[PER][R];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int b = threadIdx.x + i * T;
+        if (TOTAL % T == 0 || b < TOTAL) {
+            const int col = b >> (LOGN - LOGR), j = b & (NB - 1);
+            const float2 *src = s + (col << LOGN);
+#pragma unroll
+            for (int r = 0; r < R; r++) v[i][r] = src[swz(j + r * NB)];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int b = threadIdx.x + i * T;
+        if (TOTAL % T == 0 || b < TOTAL) {
+            const int col = b >> (LOGN - LOGR), j = b & (NB - 1);
+            const int jm = j & (NS - 1);
+            if (LOGNS > 0 && jm)
+                twiddle_powers<R, INV>(v[i], tw, (size_t)(jm << TSHIFT) * tws,
+                                       (size_t)((4 * jm) << TSHIFT) * tws);
+            dftR<R, INV>(v[i]);
+            float2 *dst = s + (col << LOGN);
+            const int od = ((j >> LOGNS) << (LOGNS + LOGR)) + jm;
+#pragma unroll
+            for (int r = 0; r < R; r++) dst[swz(od + r * NS)] = v[i][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <int LOGN, int LOGNS, bool INV, int NT, int T>
+struct StPasses {
+    static __device__ __forceinline__ void run(float2 *s, const float2 *__restrict__ tw, int tws) {
+        constexpr int REM = LOGN - LOGNS;
+        constexpr int LOGR = REM >= 4 ? 4 : REM;
+        st_pass<LOGN, LOGR, LOGNS, INV, NT, T>(s, tw, tws);
+        StPasses<LOGN, LOGNS + LOGR, INV, NT, T>::run(s, tw, tws);
+    }
+};
+template <int LOGN, bool INV, int NT, int T>
+struct StPasses<LOGN, LOGN, INV, NT, T> {
+    static __device__ __forceinline__ void run(float2 *, const float2 *__restrict__, int) {}
+};
+
+// Shapes: columns per CTA and threads for a column transform of length 2^LOGN, rows per CTA
+// and threads for a row transform of half-length 2^LOGH.
+template <int LOGN>
+struct ColShape {
+    static constexpr int N = 1 << LOGN;
+    static constexpr int CC = N >= 4096 ? 2 : (4096 / N > 64 ? 64 : 4096 / N);  // columns
+    static constexpr int T0 = CC * N / 16;
+    static constexpr int T = T0 < 128 ? 128 : (T0 > 1024 ? 1024 : T0);
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)CC * N;
+    static constexpr int MINB = 1024 / T;  // resident CTAs the kernel is built for (64 regs)
+};
+template <int LOGH>
+struct RowShape {
+    static constexpr int H = 1 << LOGH;
+    static constexpr int ROWS = H >= 2048 ? 2 : 4096 / H;
+    static constexpr int T0 = ROWS * H / 16;
+    static constexpr int T = T0 < 128 ? 128 : (T0 > 1024 ? 1024 : T0);
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)ROWS * H;
+    static constexpr int MINB = 1024 / T;
+};
+
+// Column pass along v (as k_col_fft), CC columns per CTA read as 16-byte column pairs.
+template <int LOGN, bool INV>
+__global__ void __launch_bounds__(ColShape<LOGN>::T, ColShape<LOGN>::MINB) k_col_fft_t(float2 *grid, int pitch, int nu,
+                                                                   const float2 *__restrict__ tw,
+                                                                   int r0, int r1) {
+    using S = ColShape<LOGN>;
+    constexpr int N = S::N, CC = S::CC, T = S::T;
+    constexpr int LP = __builtin_ctz(CC) - 1;           // log2(column pairs per row)
+    constexpr int TOTAL = N * CC / 2;                   // (row, pair) items
+    constexpr int PER = (TOTAL + T - 1) / T;
+    extern __shared__ float2 s[];
+    const int u0 = blockIdx.x * CC;
+    const int c = (N + 1) / 2 - 1;
+    float4 x[PER];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int idx = i * T + threadIdx.x;
+        const int v = idx >> LP, jp = idx & ((1 << LP) - 1);
+        const int u = u0 + 2 * jp;
+        x[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if ((TOTAL % T == 0 || idx < TOTAL) && u < nu && (INV || (v >= r0 && v < r1)))
+            x[i] = *reinterpret_cast<const float4 *>(&grid[(int64_t)v * pitch + u]);
+    }
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int idx = i * T + threadIdx.x;
+        if (TOTAL % T != 0 && idx >= TOTAL) continue;
+        const int v = idx >> LP, jp = idx & ((1 << LP) - 1);
+        int k = v - c;
+        if (k < 0) k += N;
+        s[((2 * jp) << LOGN) + swz(k)] = make_float2(x[i].x, x[i].y);
+        s[((2 * jp + 1) << LOGN) + swz(k)] = make_float2(x[i].z, x[i].w);
+    }
+    __syncthreads();
+    StPasses<LOGN, 0, INV, CC, T>::run(s, tw, 1);
+    const float sc = INV ? 1.0f / (float)N : 1.0f;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int idx = i * T + threadIdx.x;
+        if (TOTAL % T != 0 && idx >= TOTAL) continue;
+        const int v = idx >> LP, jp = idx & ((1 << LP) - 1);
+        const int u = u0 + 2 * jp;
+        if (u >= nu) continue;
+        int k = v - c;
+        if (k < 0) k += N;
+        float2 z0 = s[((2 * jp) << LOGN) + swz(k)];
+        float2 z1 = s[((2 * jp + 1) << LOGN) + swz(k)];
+        if (INV) {
+            z0.x *= sc; z0.y *= sc; z1.x *= sc; z1.y *= sc;
+        }
+        *reinterpret_cast<float4 *>(&grid[(int64_t)v * pitch + u]) = make_float4(z0.x, z0.y, z1.x, z1.y);
+    }
+}
+
+// Row pass grid -> image (as k_row_c2r), ROWS rows per CTA, half-length 2^LOGH.
+template <int LOGH>
+__global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB) k_row_c2r_t(const float2 *__restrict__ grid,
+                                                                   int pitch, int nx, int ny,
+                                                                   int ibegy,
+                                                                   const float2 *__restrict__ tw,
+                                                                   CorrParams cp,
+                                                                   const float *__restrict__ scale_dev,
+                                                                   float *image) {
+    using S = RowShape<LOGH>;
+    constexpr int H = S::H, ROWS = S::ROWS, T = S::T, FNU = 2 * H;
+    constexpr int TOTAL = ROWS * H;
+    constexpr int PER = (TOTAL + T - 1) / T;
+    extern __shared__ float2 s[];
+    const int iy0 = blockIdx.x * ROWS;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int t = i * T + threadIdx.x;
+        if (TOTAL % T != 0 && t >= TOTAL) continue;
+        const int rr = t >> LOGH, k = t & (H - 1);
+        const int iy = iy0 + rr;
+        if (iy >= ny) {
+            s[(rr << LOGH) + swz(k)] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float2 *X = grid + (int64_t)(iy + ibegy) * pitch;
+        float2 a = X[k], b = X[H - k];
+        if (k == 0) {
+            a.y = 0.f;
+            b.y = 0.f;
+        }
+        const float2 A = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+        const float2 d = make_float2(0.5f * (a.x - b.x), 0.5f * (a.y + b.y));
+        const float2 B = cmul(d, __ldg(&tw[k]));
+        s[(rr << LOGH) + swz(k)] = make_float2(A.x - B.y, A.y + B.x);
+    }
+    __syncthreads();
+    StPasses<LOGH, 0, true, ROWS, T>::run(s, tw, 2);
+    const float inv = 1.0f / (float)H;
+    const int cu = (FNU + 1) / 2 - 1, ioff = (FNU - nx) / 2;
+    const float sc = scale_dev ? 1.0f / *scale_dev : 1.0f;
+    for (int t = threadIdx.x; t < ROWS * nx; t += T) {
+        const int rr = t / nx, ix = t - rr * nx;
+        const int iy = iy0 + rr;
+        if (iy >= ny) break;
+        int n = ix + ioff - cu;
+        if (n < 0) n += FNU;
+        const float2 z = s[(rr << LOGH) + swz(n >> 1)];
+        float val = ((n & 1) ? z.y : z.x) * inv;
+        if (cp.ccf) val = __fdiv_rn(val, __fmul_rn(cp.corrx[ix], cp.corry[iy]));
+        if (scale_dev) val = __fadd_rn(__fmul_rn(sc, val), 0.0f);
+        image[(int64_t)iy * nx + ix] = val;
+    }
+}
+
+// Row pass image -> grid (as k_row_r2c), ROWS rows per CTA, half-length 2^LOGH.
+template <int LOGH>
+__global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB) k_row_r2c_t(const float *__restrict__ image,
+                                                                   int nx, int ny, int ibegy,
+                                                                   const float2 *__restrict__ tw,
+                                                                   CorrParams cp, float2 *grid,
+                                                                   int pitch) {
+    using S = RowShape<LOGH>;
+    constexpr int H = S::H, ROWS = S::ROWS, T = S::T, FNU = 2 * H;
+    constexpr int TOTAL = ROWS * H;
+    constexpr int PER = (TOTAL + T - 1) / T;
+    extern __shared__ float2 s[];
+    const int cu = (FNU + 1) / 2 - 1, ioff = (FNU - nx) / 2;
+    const int iy0 = blockIdx.x * ROWS;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int t = i * T + threadIdx.x;
+        if (TOTAL % T != 0 && t >= TOTAL) continue;
+        const int rr = t >> LOGH, m = t & (H - 1);
+        const int iy = iy0 + rr;
+        if (iy >= ny) {
+            s[(rr << LOGH) + swz(m)] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float cfy = cp.ccf ? cp.corry[iy] : 1.0f;
+        const float *row = image + (int64_t)iy * nx;
+        float xv[2];
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+            const int k = 2 * m + e;
+            int n = k + cu;
+            if (n >= FNU) n -= FNU;
+            const int ix = n - ioff;
+            float val = 0.f;
+            if (ix >= 0 && ix < nx) {
+                val = row[ix];
+                if (cp.ccf) val = __fdiv_rn(val, __fmul_rn(cp.corrx[ix], cfy));
+            }
+            xv[e] = val;
+        }
+        s[(rr << LOGH) + swz(m)] = make_float2(xv[0], xv[1]);
+    }
+    __syncthreads();
+    StPasses<LOGH, 0, false, ROWS, T>::run(s, tw, 2);
+    for (int t = threadIdx.x; t < ROWS * (H + 1); t += T) {
+        const int rr = t / (H + 1), k = t - rr * (H + 1);
+        const int iy = iy0 + rr;
+        if (iy >= ny) break;
+        float2 *X = grid + (int64_t)(iy + ibegy) * pitch;
+        const float2 *sr = s + (rr << LOGH);
+        const float2 zk = sr[swz(k == H ? 0 : k)];
+        const float2 zc = sr[swz(k == 0 || k == H ? 0 : H - k)];
+        const float2 A = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y - zc.y));
+        const float2 B = make_float2(0.5f * (zk.y + zc.y), -0.5f * (zk.x - zc.x));
+        float2 w = k < H ? __ldg(&tw[k]) : make_float2(-1.f, 0.f);
+        w.y = -w.y;
+        const float2 bw = cmul(B, w);
+        float2 xo = make_float2(A.x + bw.x, A.y + bw.y);
+        if (k == 0 || k == H) xo.y = 0.f;
+        X[k] = xo;
+    }
+}
+
+// Launchers for the compile-time shapes: false if the size has no instance.
+template <int LOGN>
+cudaError_t launch_col_t(float2 *grid, int pitch, int nu, const float2 *tw, bool inverse, int r0,
+                         int r1, cudaStream_t st) {
+    using S = ColShape<LOGN>;
+    const unsigned nb = (unsigned)((nu + S::CC - 1) / S::CC);
+    if (inverse) {
+        cudaError_t e = cudaFuncSetAttribute(k_col_fft_t<LOGN, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+        if (e != cudaSuccess) return e;
+        k_col_fft_t<LOGN, true><<<nb, S::T, S::SMEM, st>>>(grid, pitch, nu, tw, r0, r1);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(k_col_fft_t<LOGN, false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+        if (e != cudaSuccess) return e;
+        k_col_fft_t<LOGN, false><<<nb, S::T, S::SMEM, st>>>(grid, pitch, nu, tw, r0, r1);
+    }
+    return cudaGetLastError();
+}
+
+template <int LOGH>
+cudaError_t launch_c2r_t(const float2 *grid, int pitch, int nx, int ny, int ibegy, const float2 *tw,
+                         CorrParams cp, const float *scale_dev, float *image, cudaStream_t st) {
+    using S = RowShape<LOGH>;
+    cudaError_t e = cudaFuncSetAttribute(k_row_c2r_t<LOGH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)S::SMEM);
+    if (e != cudaSuccess) return e;
+    k_row_c2r_t<LOGH><<<(unsigned)((ny + S::ROWS - 1) / S::ROWS), S::T, S::SMEM, st>>>(
+        grid, pitch, nx, ny, ibegy, tw, cp, scale_dev, image);
+    return cudaGetLastError();
+}
+
+template <int LOGH>
+cudaError_t launch_r2c_t(const float *image, int nx, int ny, int ibegy, const float2 *tw,
+                         CorrParams cp, float2 *grid, int pitch, cudaStream_t st) {
+    using S = RowShape<LOGH>;
+    cudaError_t e = cudaFuncSetAttribute(k_row_r2c_t<LOGH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)S::SMEM);
+    if (e != cudaSuccess) return e;
+    k_row_r2c_t<LOGH><<<(unsigned)((ny + S::ROWS - 1) / S::ROWS), S::T, S::SMEM, st>>>(
+        image, nx, ny, ibegy, tw, cp, grid, pitch);
+    return cudaGetLastError();
+}
+
+#define SDE_LOG_CASES(X) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13)
+
+// Column pass through the compile-time kernels when 2^logn has an instance.
+bool col_fft_t(int logn, float2 *grid, int pitch, int nu, const float2 *tw, bool inverse, int r0,
+               int r1, cudaStream_t st, cudaError_t *err) {
+    switch (logn) {
+#define CASE(L) \
+    case L: *err = launch_col_t<L>(grid, pitch, nu, tw, inverse, r0, r1, st); return true;
+        SDE_LOG_CASES(CASE)
+#undef CASE
+        default: return false;
+    }
+}
+bool c2r_t(int logh, const float2 *grid, int pitch, int nx, int ny, int ibegy, const float2 *tw,
+           CorrParams cp, const float *scale_dev, float *image, cudaStream_t st, cudaError_t *err) {
+    switch (logh) {
+#define CASE(L) \
+    case L: *err = launch_c2r_t<L>(grid, pitch, nx, ny, ibegy, tw, cp, scale_dev, image, st); return true;
+        SDE_LOG_CASES(CASE)
+#undef CASE
+        default: return false;
+    }
+}
+bool r2c_t(int logh, const float *image, int nx, int ny, int ibegy, const float2 *tw, CorrParams cp,
+           float2 *grid, int pitch, cudaStream_t st, cudaError_t *err) {
+    switch (logh) {
+#define CASE(L) \
+    case L: *err = launch_r2c_t<L>(image, nx, ny, ibegy, tw, cp, grid, pitch, st); return true;
+        SDE_LOG_CASES(CASE)
+#undef CASE
+        default: return false;
+    }
+}
+#undef SDE_LOG_CASES
+
 }  // namespace
 
 int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, int fnu, int nv,
@@ -438,26 +797,35 @@ int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, in
     const float2 *twv, *twu;
     SDE_TRY(ctx_twiddles(ctx, nv, &twv));
     SDE_TRY(ctx_twiddles(ctx, fnu, &twu));
-    const int lcc = col_logcc(nv), cc = 1 << lcc;
-    const size_t smc = sizeof(float2) * (size_t)cc * nv;
-    SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
     {
         KTimer kt(ctx, "col_fft");
-        k_col_fft<<<ceil_div(nu, cc), COL_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
-                                                                       ilog2(nv), lcc, twv, 1, 0, nv);
+        cudaError_t e = cudaSuccess;
+        if (!col_fft_t(ilog2(nv), (float2 *)grid, pitch, nu, twv, true, 0, nv, ctx->stream, &e)) {
+            const int lcc = col_logcc(nv), cc = 1 << lcc;
+            const size_t smc = sizeof(float2) * (size_t)cc * nv;
+            SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
+            k_col_fft<<<ceil_div(nu, cc), COL_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
+                                                                           ilog2(nv), lcc, twv, 1, 0, nv);
+            e = cudaGetLastError();
+        }
+        SDE_CUDA_TRY(e);
     }
-    SDE_CHECK_LAUNCH();
     CorrParams cp = {nullptr, nullptr, nullptr};
     if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
     const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;  // 0-based first grid row
-    int rows, thr;
-    row_shape(fnu, &rows, &thr);
-    const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
-    SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
     KTimer kt(ctx, "row_c2r");
-    k_row_c2r<<<ceil_div(ny, rows), thr, smr, ctx->stream>>>((const float2 *)grid, pitch, fnu, rows,
-                                                            nx, ny, ibegy, twu, cp, scale_dev, image);
-    SDE_CHECK_LAUNCH();
+    cudaError_t e = cudaSuccess;
+    if (!c2r_t(ilog2(fnu / 2), (const float2 *)grid, pitch, nx, ny, ibegy, twu, cp, scale_dev, image,
+               ctx->stream, &e)) {
+        int rows, thr;
+        row_shape(fnu, &rows, &thr);
+        const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+        k_row_c2r<<<ceil_div(ny, rows), thr, smr, ctx->stream>>>((const float2 *)grid, pitch, fnu, rows,
+                                                                nx, ny, ibegy, twu, cp, scale_dev, image);
+        e = cudaGetLastError();
+    }
+    SDE_CUDA_TRY(e);
     return SDE_OK;
 }
 
@@ -473,23 +841,33 @@ int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fn
     CorrParams cp = {nullptr, nullptr, nullptr};
     if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
     const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;
-    int rows, thr;
-    row_shape(fnu, &rows, &thr);
-    const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
-    SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
     {
         KTimer kt(ctx, "row_r2c");
-        k_row_r2c<<<ceil_div(ny, rows), thr, smr, ctx->stream>>>(image, nx, ny, fnu, rows, ibegy, twu,
-                                                                cp, (float2 *)grid, pitch, nu);
+        cudaError_t e = cudaSuccess;
+        if (!r2c_t(ilog2(fnu / 2), image, nx, ny, ibegy, twu, cp, (float2 *)grid, pitch, ctx->stream,
+                   &e)) {
+            int rows, thr;
+            row_shape(fnu, &rows, &thr);
+            const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
+            SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+            k_row_r2c<<<ceil_div(ny, rows), thr, smr, ctx->stream>>>(image, nx, ny, fnu, rows, ibegy, twu,
+                                                                    cp, (float2 *)grid, pitch, nu);
+            e = cudaGetLastError();
+        }
+        SDE_CUDA_TRY(e);
     }
-    SDE_CHECK_LAUNCH();
-    const int lcc = col_logcc(nv), cc = 1 << lcc;
-    const size_t smc = sizeof(float2) * (size_t)cc * nv;
-    SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
     KTimer kt(ctx, "col_fft");
-    k_col_fft<<<ceil_div(nu, cc), COL_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
-                                                                   ilog2(nv), lcc, twv, 0, ibegy,
-                                                                   ibegy + ny);
-    SDE_CHECK_LAUNCH();
+    cudaError_t e = cudaSuccess;
+    if (!col_fft_t(ilog2(nv), (float2 *)grid, pitch, nu, twv, false, ibegy, ibegy + ny, ctx->stream,
+                   &e)) {
+        const int lcc = col_logcc(nv), cc = 1 << lcc;
+        const size_t smc = sizeof(float2) * (size_t)cc * nv;
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
+        k_col_fft<<<ceil_div(nu, cc), COL_THREADS, smc, ctx->stream>>>((float2 *)grid, pitch, nu, nv,
+                                                                       ilog2(nv), lcc, twv, 0, ibegy,
+                                                                       ibegy + ny);
+        e = cudaGetLastError();
+    }
+    SDE_CUDA_TRY(e);
     return SDE_OK;
 }
