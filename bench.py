@@ -47,6 +47,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="single", choices=["single", "mosaic", "serve"],
+                    help="single: the large single field (headline); mosaic: config 4 "
+                         "(49 uneven pointings, batched vs per-pointing); serve: config 5 "
+                         "(Poisson stream of jobs, continuous batching)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="single workload: skip the compact mosaic/serve summaries")
     ap.add_argument("--nchan", type=int, default=NCHAN, help="channels (64 = full workload)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -79,7 +85,7 @@ def make_vis_torch(torch, u_d, v_d, seed, device):
     im = torch.zeros(n, dtype=torch.float32, device=device)
     two_pi = 2.0 * math.pi
     for S, ll, mm in zip(flux, l, m):
-        ph = (u_d * float(-two_pi * ll)).add_(v_d * float(-two_pi * mm))
+        ph = (u_d * float(two_pi * ll)).add_(v_d * float(two_pi * mm))  # SDE's sign
         re.add_(torch.cos(ph), alpha=float(S))
         im.add_(torch.sin(ph), alpha=float(S))
         del ph
@@ -414,12 +420,274 @@ def run_gpu(args):
                             "hogbom_%d_iter" % args.clean_iters: hogbom_ms},
         "plan": {"gridding_vis": int(nplan), "bytes": int(plan.nbytes), "ndrop_weighting": int(wst.ndrop)},
     }
-    if rank == 0:
-        print(json.dumps(line))
     plan.close()
     ctx.close()
+    if rank == 0 and not dist and not args.no_extras:
+        # compact batched / served results beside the headline (outside its timed region)
+        try:
+            line["mosaic"] = run_mosaic(args, compact=True)
+        except Exception as e:  # reported, never silently dropped
+            line["mosaic"] = {"error": repr(e)}
+        try:
+            line["serve"] = run_serve(args, compact=True)
+        except Exception as e:
+            line["serve"] = {"error": repr(e)}
+    if rank == 0:
+        print(json.dumps(line))
     if dist:
         tdist.destroy_process_group()
+
+
+MOSAIC_METRIC = "Mvis/s mosaic dirty imaging (49 uneven pointings, batched + CUDA graph)"
+
+
+def _device_vis_fn(torch, dev):
+    """synth.visibilities on the device (FP64 phases), same sign and noise model."""
+    def fn(u, v, flux, l, m, noise, seed):
+        ud = torch.as_tensor(u, device=dev, dtype=torch.float64)
+        vd = torch.as_tensor(v, device=dev, dtype=torch.float64)
+        acc = torch.zeros(len(u), dtype=torch.complex128, device=dev)
+        for S, ll, mm in zip(flux, l, m):
+            acc += float(S) * torch.exp(2j * math.pi * (ud * float(ll) + vd * float(mm)))
+        rng = np.random.default_rng(seed + 2)
+        out = acc.to(torch.complex64).cpu().numpy()
+        if noise > 0:
+            out += (rng.normal(0, noise, len(u)) + 1j * rng.normal(0, noise, len(u))).astype(np.complex64)
+        return out
+    return fn
+
+
+def run_mosaic(args, compact=False):
+    """Config 4: dirty mosaic of 49 uneven pointings.  A step is the dirty imaging pass of
+    the whole mosaic (every pointing gridded, transformed, PSF-normalised, combined)."""
+    import torch
+    from sde_gb300 import mosaic, synth
+    from sde_gb300.imaging import Context
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = Context(local)
+    pts, c = synth.config4(vis_fn=_device_vis_fn(torch, ctx.device))
+    nvis_in = sum(len(p["u"]) for p in pts)
+    tune = mosaic.autotune(ctx, pts, c["cell_arcsec"], reps=3)
+    m = mosaic.Mosaic(ctx, pts, c["cell_arcsec"], opts=tune["best"])
+    nvis = m.nvis
+    steps = max(args.steps if not compact else 20, 1)
+    warm = max(args.warmup, 3)
+
+    def timed(fn):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ctx.stream)
+        for _ in range(steps):
+            fn()
+        e1.record(ctx.stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    graph_ms = timed(lambda: m.dirty(graph=True))
+    clk = clocks.stop()
+    eager_ms = timed(lambda: m.dirty(graph=False))
+    loop_ms = timed(lambda: m.dirty_loop())
+    nodes = m.graph_nodes
+    m.close()
+    # e2e: host arrays -> device, weighting, plans, batch, PSF, dirty mosaic, mosaic to host
+    e2e_ms = []
+    for _ in range(1 if compact else 2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        me = mosaic.Mosaic(ctx, pts, c["cell_arcsec"], opts=tune["best"])
+        me.dirty(graph=False)
+        mos = me.read(-1)
+        torch.cuda.synchronize()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        me.close()
+    h2d = sum(p["u"].nbytes * 3 + p["vis"].nbytes + p["wt"].nbytes for p in pts)
+    res = {
+        "batched_graph": {"ms": graph_ms, "mvis_s": nvis / graph_ms / 1e3,
+                          "dirty_images_s": m.n / graph_ms * 1e3, "graph_nodes": nodes},
+        "batched_eager": {"ms": eager_ms, "mvis_s": nvis / eager_ms / 1e3,
+                          "dirty_images_s": m.n / eager_ms * 1e3},
+        "per_pointing_loop": {"ms": loop_ms, "mvis_s": nvis / loop_ms / 1e3,
+                              "dirty_images_s": m.n / loop_ms * 1e3},
+        "speedup_vs_loop": loop_ms / graph_ms,
+        "autotune": {"chosen": list(tune["best"]),
+                     "table_ms": [[list(k), round(v, 4)] for k, v in tune["table"]]},
+        "nvis": int(nvis), "pointings": m.n,
+        "image_sizes": sorted(int(p["imsize"]) for p in pts),
+        "mosaic_px": [m.layout["mnx"], m.layout["mny"]],
+    }
+    if compact:
+        ctx.close()
+        return res
+    line = {
+        "metric": MOSAIC_METRIC, "value": res["batched_graph"]["mvis_s"], "unit": "Mvis/s",
+        "n_gpus": 1, "steps": steps, "warmup": warm, "ms_per_step": graph_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded config 4: hex mosaic, Gaussian PB 30', log-uniform Nvis, pow2 sizes)",
+        "config": {"workload": "config 4 mosaic: %d pointings, %d vis, images %s, 2\" cells, "
+                               "uniform weighting, linear mosaic %dx%d" % (m.n, nvis_in,
+                                                                         "256-2048", m.layout["mnx"],
+                                                                         m.layout["mny"]),
+                   "l2": "per-pointing visibility records 16 B x %d vis" % nvis},
+        "gpu_launches": int(nodes),
+        "clocks": clk,
+        "e2e": {"value": nvis_in / statistics.mean(e2e_ms) / 1e3, "unit": "Mvis/s",
+                "ms_per_step": statistics.mean(e2e_ms), "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(mos.nbytes),
+                "path": "Mosaic(host pointings): upload, weighting, plans, batch, PSF; dirty; "
+                        "mosaic to host"},
+        "cpu_baseline": _mosaic_cpu_baseline(pts, c) if rank == 0 and not args.no_cpu_baseline else None,
+        "mosaic": res,
+    }
+    ctx.close()
+    return line
+
+
+def _mosaic_cpu_baseline(pts, c, budget_s=12.0):
+    """The reference's per-pointing uvmap (oracle/ C restatement, 1 thread) on a sample of
+    the pointings (smallest images first, until the time budget), Mvis/s over the sample."""
+    from oracle import oracle as O
+    O.lib()
+    order = sorted(range(len(pts)), key=lambda i: (pts[i]["imsize"], len(pts[i]["u"])))
+    done, nv, t_all = [], 0, 0.0
+    for i in order:
+        p = pts[i]
+        par = O.params(p["imsize"], c["cell_arcsec"], fov=1.0, rmode="NONE", vdec=c["dec"])
+        t0 = time.perf_counter()
+        O.uvmap(par, p["u"], p["v"], p["w"], p["vis"], p["wt"])
+        t_all += time.perf_counter() - t0
+        nv += len(p["u"])
+        done.append(i)
+        if t_all > budget_s:
+            break
+    return {"value": nv / t_all / 1e6, "unit": "Mvis/s", "cores": 1, "kind": "port",
+            "sample": "uvmap (uniform weights, PSF, dirty) of %d of %d pointings (%d vis, "
+                      "images %s), oracle/ C restatement, 1 thread"
+                      % (len(done), len(pts), nv, sorted({pts[i]["imsize"] for i in done})),
+            "dirty_images_s": len(done) / t_all}
+
+
+SERVE_METRIC = ("Mvis/s served uvmap jobs (config 5 population, all queued), "
+                "with p50/p99 ms latency at 200 jobs/s Poisson")
+
+
+def run_serve(args, compact=False):
+    """Config 5: uvmap jobs of the seeded config-5 population (27-64 antennas, 1-60
+    integrations, 1-64 channels, 256^2-4096^2, natural or robust R in [-2, 2]) served by
+    slot-parallel continuous batching.  (1) A Poisson stream at 200 jobs/s: p50/p99
+    latency, arrival to dirty image on the host.  (2) Saturation: the same jobs all queued
+    at once, served (several slots) vs serial (one slot, one job at a time): Mvis/s."""
+    import torch
+    from sde_gb300 import serve
+    from sde_gb300._abi import lib
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ntpl = 24 if compact else 48
+    tpl = [serve.make_job(i, vis_fn=_device_vis_fn(torch, dev)) for i in range(ntpl)]
+
+    def pin(j):
+        d = {}
+        for k in ("u", "v", "w", "wt"):
+            d[k] = torch.from_numpy(np.ascontiguousarray(j[k])).pin_memory()
+        d["vis"] = torch.from_numpy(np.asarray(j["vis"], np.complex64).view(np.float32)).pin_memory()
+        return d
+
+    pins = [pin(j) for j in tpl]
+    duration = 2.0 if compact else 5.0
+    rate = serve.CONFIG5["rate_hz"]
+    n_stream = int(rate * duration)
+    rng = np.random.default_rng(serve.synth.SEED_BASE + 56)
+    pick = rng.integers(ntpl, size=n_stream)
+    jobs = [tpl[k] for k in pick]
+    pinned = [pins[k] for k in pick]
+    arrivals = serve.poisson_arrivals(n_stream, rate)
+    nslots = 6
+    srv = serve.Server(nslots=nslots, hbm_budget=64 << 30, device=local)
+    srv.run(jobs[:2 * nslots], None, pinned[:2 * nslots])  # warm-up: tables, allocator
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    rec = srv.run(jobs, arrivals, pinned)
+    clk = clocks.stop()
+    st = serve.summarize(rec)
+    st.update(offered_jobs_s=rate, max_running=srv.max_running,
+              max_reserved_gb=srv.max_reserved / 2 ** 30)
+    nsat = 48 if compact else 96
+    t0 = time.perf_counter()
+    srv.run(jobs[:nsat], None, pinned[:nsat])
+    t_served = time.perf_counter() - t0
+    launches = sum(lib().sde_ctx_launches(sl.ctx.h) for sl in srv.slots)
+    srv.close()
+    one = serve.Server(nslots=1, hbm_budget=64 << 30, device=local)
+    one.run(jobs[:2], None, pinned[:2])
+    t0 = time.perf_counter()
+    one.run(jobs[:nsat], None, pinned[:nsat])
+    t_serial = time.perf_counter() - t0
+    one.close()
+    nv_sat = sum(j["nvis"] for j in jobs[:nsat])
+    res = {
+        "stream": st,
+        "saturated": {"jobs": nsat, "nvis": int(nv_sat), "slots": nslots,
+                      "served_mvis_s": nv_sat / t_served / 1e6, "served_images_s": nsat / t_served,
+                      "serial_mvis_s": nv_sat / t_serial / 1e6, "serial_images_s": nsat / t_serial,
+                      "speedup": t_serial / t_served},
+        "templates": ntpl,
+        "job_nvis_mean": float(np.mean([j["nvis"] for j in jobs])),
+    }
+    if compact:
+        return res
+    h2d = float(np.mean([j["nvis"] * 24 for j in jobs]))
+    d2h = float(np.mean([j["imsize"] ** 2 * 4 for j in jobs]))
+    line = {
+        "metric": SERVE_METRIC, "value": res["saturated"]["served_mvis_s"], "unit": "Mvis/s",
+        "n_gpus": 1, "steps": nsat, "warmup": 2 * nslots,
+        "ms_per_step": t_served / nsat * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded config-5 job population, %d templates)" % ntpl,
+        "config": {"workload": "config 5 served uvmap: Poisson %g jobs/s for %g s (%d jobs), "
+                               "27-64 ants, 1-60 ints, 1-64 ch, 256-4096 px, natural or robust"
+                               % (rate, duration, n_stream), "slots": nslots,
+                   "hbm_budget_gb": 64},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "max": st["max_ms"]},
+        "e2e": {"value": res["saturated"]["served_mvis_s"], "unit": "Mvis/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "path": "host (pinned) job arrays -> weighting, plan, PSF, dirty -> image to host"},
+        "cpu_baseline": _serve_cpu_baseline(tpl) if rank == 0 and not args.no_cpu_baseline else None,
+        "serve": res,
+    }
+    return line
+
+
+def _serve_cpu_baseline(tpl, budget_s=12.0):
+    """uvmap of a sample of the job population with the oracle/ C restatement (1 thread)."""
+    from oracle import oracle as O
+    O.lib()
+    order = sorted(range(len(tpl)), key=lambda i: tpl[i]["nvis"] * max(tpl[i]["imsize"], 1024))
+    nv, t_all, done = 0, 0.0, 0
+    for i in order:
+        j = tpl[i]
+        par = O.params(j["imsize"], j["cell"], fov=1.0,
+                       rmode="NONE" if j["natural"] else "NORM", vdec=j["dec"])
+        t0 = time.perf_counter()
+        O.uvmap(par, j["u"], j["v"], j["w"], j["vis"], j["wt"])
+        t_all += time.perf_counter() - t0
+        nv += j["nvis"]
+        done += 1
+        if t_all > budget_s:
+            break
+    return {"value": nv / t_all / 1e6, "unit": "Mvis/s", "cores": 1, "kind": "port",
+            "sample": "uvmap of the %d cheapest of %d job templates (%d vis), oracle/ C "
+                      "restatement, 1 thread" % (done, len(tpl), nv),
+            "images_s": done / t_all}
 
 
 def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis):
@@ -495,6 +763,14 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "mosaic":
+        line = run_mosaic(args)
+        if line:
+            print(json.dumps(line))
+    elif args.workload == "serve":
+        line = run_serve(args)
+        if line:
+            print(json.dumps(line))
     else:
         run_gpu(args)
 

@@ -162,6 +162,19 @@ int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const 
 int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const float *u,
                     const float *v, const float *w, const float *vis, const float *wt,
                     int where, sde_plan **out);
+/* The same with the plan's sort-bucket sizes chosen by the caller (an autotuner): the
+ * visibilities of one uv tile are cut into work items of at most item_max visibilities
+ * (one CTA each), and the visibilities of one cell pair inside a work item into chunks of
+ * at most chunk_max (one 4-lane group each).  0 selects the default (8192 / 64).  Limits:
+ * chunk_max <= item_max <= 65536, chunk_max <= 4096.  No counterpart in the reference
+ * (GRDH2D walks visibilities in input order). */
+typedef struct {
+    int item_max;
+    int chunk_max;
+} sde_plan_opts;
+int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const float *u,
+                         const float *v, const float *w, const float *vis, const float *wt,
+                         int where, const sde_plan_opts *opts, sde_plan **out);
 int sde_plan_destroy(sde_plan *plan);
 int64_t sde_plan_nvis(const sde_plan *plan);       /* visibilities that grid              */
 int64_t sde_plan_bytes(const sde_plan *plan);
@@ -240,6 +253,43 @@ int sde_hogbom_noalloc(void *stream, const float *drt, const float *psf, const f
                        volatile int *cancel_flag, sde_clean_result *out);
 
 /* Index (1-based) of the first strictly largest |a| (PIXISAMA) of a device array. */
+
+/* ---- Batches of plans: a mosaic's pointings or a group of served jobs ------------------
+ * No counterpart entry point in the reference: task/mosclean.f images its pointings one
+ * after another and forms the linear mosaic (task/mosclean.f:413-432); a batch images all
+ * of them together.  Every plan must come from ctx and hold a power-of-two grid large
+ * enough for its nx[i] x ny[i] image.  The batch owns per plan a grid, a PSF image and a
+ * dirty image (device, row-major nx x ny).
+ *   sde_batch_psf      grid and transform every PSF; records each PSF peak.
+ *   sde_batch_dirty    dirty image of every plan, divided by its PSF peak (uvmap's
+ *                      normalisation, task/uvmap.f:473-483): one persistent gridding launch
+ *                      over all plans' work items, one batched finalize, per shape one
+ *                      batched column FFT and one batched row c2r with grid correction,
+ *                      then the mosaic if one is set.  use_graph != 0: the launch sequence
+ *                      is captured in a CUDA graph on the second call and replayed after.
+ *   sde_batch_dirty_loop  the same images through sde_plan_grid + sde_image_from_grid,
+ *                      one plan at a time (the per-pointing baseline).
+ *   sde_batch_set_mosaic  linear mosaic mnx x mny: pointing i's image centre ((n+1)/2,
+ *                      1-based) lands on mosaic pixel (cx[i], cy[i]); its primary beam is a
+ *                      Gaussian of FWHM fwhm_px[i] pixels; mosaic = sum wt PB I / sum wt PB^2
+ *                      where sum wt PB^2 > clip * its maximum, else 0.
+ *   sde_batch_image    device pointer: i = -1 the mosaic; which 0 the dirty image of plan
+ *                      i, 1 its PSF, 2 its PSF peak (one float). */
+typedef struct sde_batch sde_batch;
+int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, const int *nx, const int *ny,
+                     sde_batch **out);
+int sde_batch_destroy(sde_batch *b);
+int64_t sde_batch_bytes(const sde_batch *b);
+int sde_batch_psf(sde_batch *b);
+int sde_batch_set_mosaic(sde_batch *b, int mnx, int mny, const int *cx, const int *cy,
+                         const float *fwhm_px, const float *wt, float clip);
+int sde_batch_dirty(sde_batch *b, int use_graph);
+int sde_batch_dirty_loop(sde_batch *b);
+int sde_batch_graph_nodes(const sde_batch *b);
+int sde_batch_image(const sde_batch *b, int i, int which, float **dev);
+/* copy n floats of what sde_batch_image names into dst (host or device); synchronises */
+int sde_batch_read(const sde_batch *b, int i, int which, float *dst, int64_t n);
+
 int sde_isamax(sde_ctx *ctx, const float *a, int64_t n, int64_t *index_out);
 
 #ifdef __cplusplus

@@ -36,6 +36,10 @@ class WStats(C.Structure):
                 ("f2", C.c_float), ("d2", C.c_float)]
 
 
+class PlanOpts(C.Structure):
+    _fields_ = [("item_max", C.c_int), ("chunk_max", C.c_int)]
+
+
 class CleanResult(C.Structure):
     _fields_ = [("ansub", C.c_int), ("maxres", C.c_float), ("tflux", C.c_float)]
 
@@ -67,6 +71,8 @@ SIGNATURES = [
     ("sde_weights", I, [P, I, P, F, P, P, P, P, I64, F, F, F, F, I, I, I, I, P, P, P,
                         C.POINTER(WStats)]),
     ("sde_plan_create", I, [P, C.POINTER(GridSpec), I64, P, P, P, P, P, I, C.POINTER(P)]),
+    ("sde_plan_create_opts", I, [P, C.POINTER(GridSpec), I64, P, P, P, P, P, I,
+                                 C.POINTER(PlanOpts), C.POINTER(P)]),
     ("sde_plan_destroy", I, [P]),
     ("sde_plan_nvis", I64, [P]),
     ("sde_plan_bytes", I64, [P]),
@@ -86,6 +92,16 @@ SIGNATURES = [
     ("sde_isamax", I, [P, P, I64, C.POINTER(I64)]),
     ("sde_hogbom_noalloc", I, [P, P, P, P, I, I, I, I, F, I, I, F, F, P, P, P, P, P, P,
                                C.POINTER(CleanResult)]),
+    ("sde_batch_create", I, [P, I, P, P, P, C.POINTER(P)]),
+    ("sde_batch_destroy", I, [P]),
+    ("sde_batch_bytes", I64, [P]),
+    ("sde_batch_psf", I, [P]),
+    ("sde_batch_set_mosaic", I, [P, I, I, P, P, P, P, F]),
+    ("sde_batch_dirty", I, [P, I]),
+    ("sde_batch_dirty_loop", I, [P]),
+    ("sde_batch_graph_nodes", I, [P]),
+    ("sde_batch_image", I, [P, I, I, C.POINTER(P)]),
+    ("sde_batch_read", I, [P, I, I, P, I64]),
     # Fortran-77 drop-in layer (all arguments by reference)
     ("grdh2d_", None, [P] * 24),
     ("grddeh2d_", None, [P] * 22),

@@ -1,0 +1,482 @@
+// batch.cu -- many plans imaged together: the pointings of a mosaic (task/mosclean.f images
+// each pointing, then forms the linear mosaic, task/mosclean.f:413-432) and batches of
+// served imaging jobs.
+//
+// The batch owns, in one device allocation, a raw and a final grid, a PSF image and a dirty
+// image per plan.  Dirty imaging of the whole batch is: one persistent gridding launch over
+// the combined work-item list of all plans (k_grid_batch), one batched finalize, and per
+// shape class (plans with the same grid and image size) one batched column FFT and one
+// batched row c2r with grid correction and the PSF-peak normalisation of uvmap
+// (task/uvmap.f:473-483).  The mosaic adds each pointing's primary-beam-weighted image and
+// weight into a numerator and a denominator and divides.  Because the launch sequence of a
+// batch never changes, it is captured once into a CUDA graph and replayed.
+#include <algorithm>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+
+namespace {
+
+struct MosaicPointing {
+    const float *image;  // dirty image of the pointing (nx x ny, row-major)
+    int nx, ny;
+    int cx, cy;          // mosaic pixel of the image centre pixel ((n+1)/2, 1-based)
+    float pbk;           // 4 ln2 / FWHM^2 (FWHM in pixels): PB = exp(-pbk r^2)
+    float wt;            // pointing weight (SUMWT of the pointing)
+};
+
+// num += wt PB image, den += wt PB^2 over each pointing's pixels (blockIdx.y = pointing)
+__global__ void k_mosaic_accum(const MosaicPointing *__restrict__ pts, int mnx, int mny, float *num,
+                               float *den) {
+    const MosaicPointing p = pts[blockIdx.y];
+    const int64_t npix = (int64_t)p.nx * p.ny;
+    const int cenx = (p.nx + 1) / 2 - 1, ceny = (p.ny + 1) / 2 - 1;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < npix;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int iy = (int)(k / p.nx), ix = (int)(k - (int64_t)iy * p.nx);
+        const int mx = p.cx - 1 + ix - cenx, my = p.cy - 1 + iy - ceny;
+        if (mx < 0 || mx >= mnx || my < 0 || my >= mny) continue;
+        const float dx = (float)(ix - cenx), dy = (float)(iy - ceny);
+        const float pb = expf(-p.pbk * (dx * dx + dy * dy));
+        const int64_t m = (int64_t)my * mnx + mx;
+        atomicAdd(&num[m], p.wt * pb * p.image[k]);
+        atomicAdd(&den[m], p.wt * pb * pb);
+    }
+}
+
+// mosaic = num / den where the summed sensitivity den exceeds clip * max(den) (else 0)
+__global__ void k_mosaic_div(const float *__restrict__ num, const float *__restrict__ den,
+                             int64_t n, const float *__restrict__ denmax, float clip, float *out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float d = den[k];
+    out[k] = (d > 0.f && d > clip * *denmax) ? num[k] / d : 0.f;
+}
+
+__global__ void k_max_batch(float *const *__restrict__ images, const int64_t *__restrict__ npix,
+                                float *out) {
+    // one CTA per image: max over the image (the PSF peak of uvmap, task/uvmap.f:424-441)
+    const float *im = images[blockIdx.x];
+    const int64_t n = npix[blockIdx.x];
+    float m = -INFINITY;
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) m = fmaxf(m, im[k]);
+    for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, d));
+    __shared__ float sm[32];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < blockDim.x / 32 ? sm[threadIdx.x] : -INFINITY;
+        for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, d));
+        if (threadIdx.x == 0) out[blockIdx.x] = m;
+    }
+}
+
+// max of a non-negative array, many CTAs: block maxima meet through atomicMax on the float
+// bit patterns (for x >= 0 the IEEE order is the unsigned-integer order); *out starts at 0
+__global__ void k_max_nonneg(const float *__restrict__ v, int64_t n, unsigned int *out) {
+    float m = 0.f;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, v[k]);
+    for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, d));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+}  // namespace
+
+struct sde_batch {
+    sde_ctx *ctx = nullptr;
+    int n = 0;
+    std::vector<sde_plan *> plans;
+    std::vector<int> nx, ny;
+    std::vector<float2 *> raw, grid;
+    std::vector<float *> psf, image;
+    float *d_peak = nullptr;                   // PSF peak per plan
+    BatchPlan *d_plans = nullptr;
+    int64_t *d_item_start = nullptr;
+    unsigned long long *d_counter = nullptr;
+    FinalizeDesc *d_fin = nullptr;
+    float **d_psf_ptrs = nullptr;
+    int64_t *d_npix = nullptr;
+    int64_t max_cells = 0;
+    size_t raw_bytes = 0;                      // the raw grids are contiguous from raw[0]
+    // shape class (fnu, nv, nx, ny, pitch) -> plan indices
+    std::map<std::tuple<int, int, int, int, int>, std::vector<int>> classes;
+    // mosaic
+    int mnx = 0, mny = 0;
+    float clip = 0.f;
+    MosaicPointing *d_pts = nullptr;
+    float *d_num = nullptr, *d_den = nullptr, *d_denmax = nullptr, *d_mosaic = nullptr;
+    // graph of sde_batch_dirty (+ mosaic)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = nullptr;  // capture stream (the caller's may be the legacy default one)
+    int graph_nodes = 0;
+    int eager_runs = 0;
+    std::vector<void *> allocs;
+    std::vector<size_t> alloc_bytes;
+    int64_t bytes = 0;
+};
+
+namespace {
+
+int batch_alloc(sde_batch *b, void **p, size_t bytes) {
+    bytes = (bytes + 255) & ~(size_t)255;
+    SDE_TRY(ctx_alloc(b->ctx, p, bytes));
+    b->allocs.push_back(*p);
+    b->alloc_bytes.push_back(bytes);
+    b->bytes += (int64_t)bytes;
+    b->ctx->bytes += (int64_t)bytes;
+    return SDE_OK;
+}
+
+// the launches of one gridding pass of every plan (PSF or visibilities)
+int batch_grid(sde_batch *b, int psf) {
+    sde_ctx *ctx = b->ctx;
+    SDE_CUDA_TRY(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), ctx->stream));
+    SDE_CUDA_TRY(cudaMemsetAsync(b->raw[0], 0, b->raw_bytes, ctx->stream));
+    SDE_TRY(launch_grid_batch(ctx, psf, b->d_plans, b->d_item_start, b->n, b->d_counter,
+                              ctx->d_cft, ctx->num_sms * 4));
+    SDE_TRY(launch_finalize_batch(ctx, b->d_fin, b->n, b->max_cells));
+    return SDE_OK;
+}
+
+// grid -> image for every shape class; scale by 1/peak when peaks != NULL
+int batch_fft(sde_batch *b, const std::vector<float *> &out, const float *peaks) {
+    for (auto &kv : b->classes) {
+        const int fnu = std::get<0>(kv.first), nv = std::get<1>(kv.first);
+        const int nx = std::get<2>(kv.first), ny = std::get<3>(kv.first), pitch = std::get<4>(kv.first);
+        std::vector<float2 *> g;
+        std::vector<float *> im;
+        std::vector<const float *> sc;
+        for (int i : kv.second) {
+            g.push_back(b->grid[i]);
+            im.push_back(out[i]);
+            sc.push_back(peaks ? peaks + i : nullptr);
+        }
+        int rc = fft_images_from_grids(b->ctx, (int)g.size(), g.data(), im.data(),
+                                       peaks ? sc.data() : nullptr, pitch, nx, ny, fnu, nv, 1);
+        if (rc == SDE_EINVAL) {
+            // no batched instance for this shape: one transform at a time
+            for (size_t k = 0; k < g.size(); k++)
+                SDE_TRY(sde_image_from_grid(b->ctx, (float *)g[k], pitch, nx, ny, fnu, nv, 1, sc[k],
+                                            im[k]));
+        } else {
+            SDE_TRY(rc);
+        }
+    }
+    return SDE_OK;
+}
+
+int batch_mosaic(sde_batch *b) {
+    if (!b->d_pts) return SDE_OK;
+    sde_ctx *ctx = b->ctx;
+    const int64_t m = (int64_t)b->mnx * b->mny;
+    SDE_CUDA_TRY(cudaMemsetAsync(b->d_num, 0, sizeof(float) * 2 * (size_t)m, ctx->stream));
+    int64_t maxpix = 0;
+    for (int i = 0; i < b->n; i++) maxpix = std::max(maxpix, (int64_t)b->nx[i] * b->ny[i]);
+    {
+        KTimer kt(ctx, "mosaic_accum");
+        const unsigned gx = (unsigned)std::min<int64_t>(ceil_div(maxpix, 256), 4096);
+        k_mosaic_accum<<<dim3(gx, (unsigned)b->n), 256, 0, ctx->stream>>>(b->d_pts, b->mnx, b->mny,
+                                                                        b->d_num, b->d_den);
+        SDE_CHECK_LAUNCH();
+    }
+    {
+        KTimer kt(ctx, "mosaic_div");
+        SDE_CUDA_TRY(cudaMemsetAsync(b->d_denmax, 0, sizeof(float), ctx->stream));
+        k_max_nonneg<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(b->d_den, m,
+                                                                reinterpret_cast<unsigned int *>(b->d_denmax));
+        SDE_CHECK_LAUNCH();
+        k_mosaic_div<<<ceil_div(m, 256), 256, 0, ctx->stream>>>(b->d_num, b->d_den, m, b->d_denmax,
+                                                               b->clip, b->d_mosaic);
+        SDE_CHECK_LAUNCH();
+    }
+    return SDE_OK;
+}
+
+int batch_dirty_launches(sde_batch *b) {
+    SDE_TRY(batch_grid(b, 0));
+    SDE_TRY(batch_fft(b, b->image, b->d_peak));
+    SDE_TRY(batch_mosaic(b));
+    return SDE_OK;
+}
+
+void batch_drop_graph(sde_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_nodes = 0;
+}
+
+}  // namespace
+
+extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, const int *nx,
+                                const int *ny, sde_batch **out) {
+    if (!ctx || n <= 0 || !plans || !nx || !ny || !out) {
+        sde_set_error("sde_batch_create: bad arguments");
+        return SDE_EINVAL;
+    }
+    SDE_CUDA_TRY(cudaSetDevice(ctx->device));
+    sde_batch *b = new sde_batch();
+    b->ctx = ctx;
+    b->n = n;
+    int rc = SDE_OK;
+    std::vector<BatchPlan> hp(n);
+    std::vector<int64_t> start(n + 1, 0);
+    std::vector<FinalizeDesc> hf(n);
+    std::vector<size_t> raw_off(n), img_off(n);
+    size_t raw_total = 0, img_total = 0;
+    for (int i = 0; i < n; i++) {
+        sde_plan *pl = plans[i];
+        if (!pl || pl->ctx != ctx || nx[i] < 1 || ny[i] < 1) {
+            sde_set_error("sde_batch_create: plan %d missing, from another context, or bad image size", i);
+            delete b;
+            return SDE_EINVAL;
+        }
+        const int fnu = 2 * (pl->spec.nu - 1), nv = pl->spec.nv;
+        if (fnu < nx[i] || nv < ny[i] || (fnu & (fnu - 1)) || (nv & (nv - 1))) {
+            sde_set_error("sde_batch_create: plan %d grid %dx%d does not hold a %dx%d image", i,
+                          pl->spec.nu, nv, nx[i], ny[i]);
+            delete b;
+            return SDE_EINVAL;
+        }
+        if (!pl->sums_ready) {
+            rc = plan_sums(pl, &pl->h_lsumwt, &pl->h_sumwt);
+            if (rc != SDE_OK) {
+                delete b;
+                return rc;
+            }
+            pl->sums_ready = true;
+        }
+        if (pl->h_lsumwt == 0.0) {
+            sde_set_error("No weight! (plan %d of the batch)", i);
+            delete b;
+            return SDE_ENOWEIGHT;
+        }
+        b->plans.push_back(pl);
+        b->nx.push_back(nx[i]);
+        b->ny.push_back(ny[i]);
+        const size_t cells = (size_t)nv * pl->pitch;
+        raw_off[i] = raw_total;
+        raw_total += (cells * 8 + 255) & ~(size_t)255;
+        img_off[i] = img_total;
+        img_total += ((size_t)nx[i] * ny[i] * 4 + 255) & ~(size_t)255;
+        b->max_cells = std::max<int64_t>(b->max_cells, (int64_t)cells);
+        start[i + 1] = start[i] + pl->nitems;
+        b->classes[std::make_tuple(fnu, nv, nx[i], ny[i], pl->pitch)].push_back(i);
+    }
+    char *rawmem = nullptr, *gridmem = nullptr, *imgmem = nullptr;
+#define B_TRY(x)                              \
+    do {                                      \
+        rc = (x);                             \
+        if (rc != SDE_OK) goto fail;          \
+    } while (0)
+    B_TRY(batch_alloc(b, (void **)&rawmem, raw_total));
+    B_TRY(batch_alloc(b, (void **)&gridmem, raw_total));
+    B_TRY(batch_alloc(b, (void **)&imgmem, 2 * img_total));
+    B_TRY(batch_alloc(b, (void **)&b->d_peak, sizeof(float) * n));
+    B_TRY(batch_alloc(b, (void **)&b->d_plans, sizeof(BatchPlan) * n));
+    B_TRY(batch_alloc(b, (void **)&b->d_item_start, sizeof(int64_t) * (n + 1)));
+    B_TRY(batch_alloc(b, (void **)&b->d_counter, sizeof(unsigned long long)));
+    B_TRY(batch_alloc(b, (void **)&b->d_fin, sizeof(FinalizeDesc) * n));
+    B_TRY(batch_alloc(b, (void **)&b->d_psf_ptrs, sizeof(float *) * n));
+    B_TRY(batch_alloc(b, (void **)&b->d_npix, sizeof(int64_t) * n));
+    b->raw_bytes = raw_total;
+    for (int i = 0; i < n; i++) {
+        sde_plan *pl = b->plans[i];
+        b->raw.push_back(reinterpret_cast<float2 *>(rawmem + raw_off[i]));
+        b->grid.push_back(reinterpret_cast<float2 *>(gridmem + raw_off[i]));
+        b->psf.push_back(reinterpret_cast<float *>(imgmem + img_off[i]));
+        b->image.push_back(reinterpret_cast<float *>(imgmem + img_total + img_off[i]));
+        hp[i] = BatchPlan{pl->items, pl->chunks, pl->rec, b->raw[i], pl->pitch, pl->ntu, pl->spec.nu,
+                          pl->spec.nv};
+        const float scale = (float)((double)((float)(pl->spec.nu - 1) * (float)pl->spec.nv) / pl->h_lsumwt);
+        hf[i] = FinalizeDesc{b->raw[i], b->grid[i], pl->spec.nu, pl->spec.nv, pl->pitch,
+                             pl->spec.uorigin, pl->spec.vorigin, pl->spec.supp, scale};
+    }
+    {
+        std::vector<int64_t> npix(n);
+        for (int i = 0; i < n; i++) npix[i] = (int64_t)b->nx[i] * b->ny[i];
+        cudaStream_t st = ctx->stream;
+        cudaError_t e = cudaSuccess;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_plans, hp.data(), sizeof(BatchPlan) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_item_start, start.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_fin, hf.data(), sizeof(FinalizeDesc) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_psf_ptrs, b->psf.data(), sizeof(float *) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_npix, npix.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            sde_set_error("sde_batch_create: %s", cudaGetErrorString(e));
+            rc = SDE_ECUDA;
+            goto fail;
+        }
+    }
+    *out = b;
+    return SDE_OK;
+fail:
+    for (size_t k = 0; k < b->allocs.size(); k++) ctx_free(ctx, b->allocs[k], b->alloc_bytes[k]);
+    ctx->bytes -= b->bytes;
+    delete b;
+    return rc;
+#undef B_TRY
+}
+
+extern "C" int sde_batch_destroy(sde_batch *b) {
+    if (!b) return SDE_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    batch_drop_graph(b);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    for (size_t k = 0; k < b->allocs.size(); k++) ctx_free(b->ctx, b->allocs[k], b->alloc_bytes[k]);
+    b->ctx->bytes -= b->bytes;
+    delete b;
+    return SDE_OK;
+}
+
+extern "C" int64_t sde_batch_bytes(const sde_batch *b) { return b ? b->bytes : 0; }
+
+extern "C" int sde_batch_psf(sde_batch *b) {
+    if (!b) return SDE_EINVAL;
+    SDE_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    SDE_TRY(batch_grid(b, 1));
+    SDE_TRY(batch_fft(b, b->psf, nullptr));
+    k_max_batch<<<b->n, 1024, 0, b->ctx->stream>>>(b->d_psf_ptrs, b->d_npix, b->d_peak);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+extern "C" int sde_batch_set_mosaic(sde_batch *b, int mnx, int mny, const int *cx, const int *cy,
+                                    const float *fwhm_px, const float *wt, float clip) {
+    if (!b || mnx < 1 || mny < 1 || !cx || !cy || !fwhm_px || !wt || clip < 0.f) {
+        sde_set_error("sde_batch_set_mosaic: bad arguments");
+        return SDE_EINVAL;
+    }
+    SDE_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    if (b->d_pts && (b->mnx != mnx || b->mny != mny)) {
+        sde_set_error("sde_batch_set_mosaic: the mosaic size is fixed once set");
+        return SDE_EINVAL;
+    }
+    if (!b->d_pts) {
+        SDE_TRY(batch_alloc(b, (void **)&b->d_pts, sizeof(MosaicPointing) * b->n));
+        SDE_TRY(batch_alloc(b, (void **)&b->d_num, sizeof(float) * 2 * (size_t)mnx * mny));
+        SDE_TRY(batch_alloc(b, (void **)&b->d_mosaic, sizeof(float) * (size_t)mnx * mny));
+        SDE_TRY(batch_alloc(b, (void **)&b->d_denmax, sizeof(float)));
+        b->d_den = b->d_num + (size_t)mnx * mny;
+    }
+    std::vector<MosaicPointing> h(b->n);
+    for (int i = 0; i < b->n; i++) {
+        if (!(fwhm_px[i] > 0.f)) {
+            sde_set_error("sde_batch_set_mosaic: FWHM of pointing %d must be > 0", i);
+            return SDE_EINVAL;
+        }
+        h[i] = MosaicPointing{b->image[i], b->nx[i], b->ny[i], cx[i], cy[i],
+                              4.0f * 0.69314718f / (fwhm_px[i] * fwhm_px[i]), wt[i]};
+    }
+    b->mnx = mnx;
+    b->mny = mny;
+    b->clip = clip;
+    SDE_CUDA_TRY(cudaMemcpy(b->d_pts, h.data(), sizeof(MosaicPointing) * b->n, cudaMemcpyHostToDevice));
+    batch_drop_graph(b);  // the captured sequence changes
+    return SDE_OK;
+}
+
+extern "C" int sde_batch_dirty(sde_batch *b, int use_graph) {
+    if (!b) return SDE_EINVAL;
+    sde_ctx *ctx = b->ctx;
+    SDE_CUDA_TRY(cudaSetDevice(ctx->device));
+    if (!use_graph) return batch_dirty_launches(b);
+    if (!b->exec) {
+        if (b->eager_runs == 0) {
+            // the first run allocates the context's twiddle and correction tables; graphs
+            // are captured from the second on
+            SDE_TRY(batch_dirty_launches(b));
+            b->eager_runs++;
+            return SDE_OK;
+        }
+        if (!b->cap) SDE_CUDA_TRY(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
+        // capture on the batch's own stream: the caller's stream may be the legacy default
+        // stream, which cannot be captured; the graph is launched on the caller's stream
+        SDE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        const int prof = ctx->profile;
+        cudaStream_t user = ctx->stream;
+        ctx->profile = 0;  // no timing events inside the graph
+        ctx->stream = b->cap;
+        cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+        int rc = e == cudaSuccess ? batch_dirty_launches(b) : SDE_ECUDA;
+        cudaGraph_t g = nullptr;
+        if (e == cudaSuccess) e = cudaStreamEndCapture(b->cap, &g);
+        ctx->stream = user;
+        ctx->profile = prof;
+        if (rc != SDE_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) {
+            sde_set_error("sde_batch_dirty: capture failed: %s", cudaGetErrorString(e));
+            return SDE_ECUDA;
+        }
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            sde_set_error("sde_batch_dirty: graph instantiate: %s", cudaGetErrorString(e));
+            return SDE_ECUDA;
+        }
+        b->graph = g;
+        size_t nn = 0;
+        cudaGraphGetNodes(g, nullptr, &nn);
+        b->graph_nodes = (int)nn;
+    }
+    SDE_CUDA_TRY(cudaGraphLaunch(b->exec, ctx->stream));
+    return SDE_OK;
+}
+
+// The same images through the single-plan entry points, one pointing after another
+// (sde_plan_grid + sde_image_from_grid per plan): the baseline the batch is compared with.
+extern "C" int sde_batch_dirty_loop(sde_batch *b) {
+    if (!b) return SDE_EINVAL;
+    SDE_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    for (int i = 0; i < b->n; i++) {
+        sde_plan *pl = b->plans[i];
+        SDE_TRY(sde_plan_grid(pl, SDE_GRID_VIS, (float *)b->grid[i], pl->pitch, nullptr));
+        SDE_TRY(sde_image_from_grid(b->ctx, (float *)b->grid[i], pl->pitch, b->nx[i], b->ny[i],
+                                    2 * (pl->spec.nu - 1), pl->spec.nv, 1, b->d_peak + i,
+                                    b->image[i]));
+    }
+    SDE_TRY(batch_mosaic(b));
+    return SDE_OK;
+}
+
+extern "C" int sde_batch_graph_nodes(const sde_batch *b) { return b ? b->graph_nodes : 0; }
+
+extern "C" int sde_batch_image(const sde_batch *b, int i, int which, float **dev) {
+    if (!b || !dev || i < -1 || i >= b->n || (i == -1 && !b->d_mosaic)) return SDE_EINVAL;
+    if (i == -1) {
+        *dev = b->d_mosaic;
+        return SDE_OK;
+    }
+    *dev = which == 1 ? b->psf[i] : (which == 2 ? b->d_peak + i : b->image[i]);
+    return SDE_OK;
+}
+
+extern "C" int sde_batch_read(const sde_batch *b, int i, int which, float *dst, int64_t n) {
+    float *src = nullptr;
+    if (!b || !dst || sde_batch_image(b, i, which, &src) != SDE_OK) {
+        sde_set_error("sde_batch_read: bad arguments");
+        return SDE_EINVAL;
+    }
+    const int64_t have = i == -1 ? (int64_t)b->mnx * b->mny
+                                 : (which == 2 ? 1 : (int64_t)b->nx[i] * b->ny[i]);
+    if (n != have) {
+        sde_set_error("sde_batch_read: %lld floats requested, the image holds %lld", (long long)n,
+                      (long long)have);
+        return SDE_EINVAL;
+    }
+    SDE_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    SDE_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(float) * (size_t)n, cudaMemcpyDefault, b->ctx->stream));
+    SDE_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    return SDE_OK;
+}

@@ -45,10 +45,10 @@ constexpr int OSAMP = 128;              // oversampling (grd/grdcf.f:245)
 constexpr int NTAP = 2 * SUPP + 1;      // 7
 constexpr int STILE = TILE + 2 * SUPP;  // 70: shared tile edge (grid and degrid)
 constexpr int CFLEN = 1 + 8 * 129;      // vis/visgrid.f:274
-constexpr int ITEM_MAX = 8192;
-constexpr int CHUNK_MAX = 64;
-constexpr int LBITS = 6;                // chunk length class CHUNK_MAX - len, 0..63
-static_assert(CHUNK_MAX - 1 < (1 << LBITS), "length class field");
+constexpr int ITEM_MAX = 8192;         // default work-item size (sde_plan_opts.item_max)
+constexpr int CHUNK_MAX = 64;           // default chunk size (sde_plan_opts.chunk_max)
+constexpr int ITEM_LIMIT = 1 << 16;     // largest accepted work-item size
+constexpr int CHUNK_LIMIT = 4096;       // largest accepted chunk size
 constexpr uint32_t KEY_INVALID = 0xFFFFFFFFu;
 
 // Per-visibility geometry words (sorted order):
@@ -159,6 +159,7 @@ struct sde_plan {
     int64_t nvis_in = 0;      // caller's count
     int64_t nvis = 0;         // gridding visibilities
     int64_t nitems = 0, nchunks = 0, nexc = 0;
+    int item_max = ITEM_MAX, chunk_max = CHUNK_MAX;  // sort-bucket sizes of this plan
     // sorted, gridding-valid visibilities
     float2 *fobs = nullptr;   // observed, in the gridding frame (rotated, conjugated)
     float4 *rec = nullptr;    // {WT, gdg bits, residual re, residual im} (gridding frame):
@@ -187,6 +188,39 @@ int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt);
 int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, float2 *out, int nu, int nv, int pitch,
                         int uorigin, int vorigin, int supp, float scale);
 int plan_grid_raw(sde_plan *pl, int what, float2 *raw);
+
+// ---- batches of plans (mosaic pointings, served jobs) -----------------------------------
+// One plan as the persistent gridder sees it.
+struct BatchPlan {
+    const WorkItem *items;
+    const uint2 *chunks;
+    const float4 *rec;
+    float2 *raw;
+    int pitch, ntu, nu, nv;
+};
+// One grid of a batched finalize (Hermitian fold, shift by SUPP, GRDH2D normalisation).
+struct FinalizeDesc {
+    const float2 *raw;
+    float2 *out;
+    int nu, nv, pitch, uorigin, vorigin, supp;
+    float scale;
+};
+// Pointers of up to FFT_MAXB same-shape transforms of one batched FFT launch (blockIdx.y).
+constexpr int FFT_MAXB = 64;
+struct FftBatch {
+    float2 *grid[FFT_MAXB];
+    float *image[FFT_MAXB];
+    const float *scale[FFT_MAXB];
+};
+size_t grid_smem_bytes();
+int launch_grid_batch(sde_ctx *ctx, int psf, const BatchPlan *d_plans, const int64_t *d_item_start,
+                      int nplans, unsigned long long *d_counter, const float *cft, int nctas);
+int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, int n, int64_t max_cells);
+// grid -> image for n same-shape grids (inverse column pass, row c2r with grid correction
+// and scale 1/scales[i] when scales[i] != NULL); SDE_EINVAL if the shape has no batched form
+int fft_images_from_grids(sde_ctx *ctx, int n, float2 *const *grids, float *const *images,
+                          const float *const *scales, int pitch, int nx, int ny, int fnu, int nv,
+                          int correct);
 int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vis_out,
                 float *wt_out, unsigned long long *nbad_dev);
 int plan_scatter_residual(sde_plan *pl, float2 *dst);

@@ -537,9 +537,10 @@ struct RowShape {
 
 // Column pass along v (as k_col_fft), CC columns per CTA read as 16-byte column pairs.
 template <int LOGN, bool INV>
-__global__ void __launch_bounds__(ColShape<LOGN>::T, ColShape<LOGN>::MINB) k_col_fft_t(float2 *grid, int pitch, int nu,
-                                                                   const float2 *__restrict__ tw,
-                                                                   int r0, int r1) {
+__global__ void __launch_bounds__(ColShape<LOGN>::T, ColShape<LOGN>::MINB)
+    k_col_fft_t(const __grid_constant__ FftBatch bt, int pitch, int nu, const float2 *__restrict__ tw,
+                int r0, int r1) {
+    float2 *grid = bt.grid[blockIdx.y];
     using S = ColShape<LOGN>;
     constexpr int N = S::N, CC = S::CC, T = S::T;
     constexpr int LP = __builtin_ctz(CC) - 1;           // log2(column pairs per row)
@@ -591,13 +592,12 @@ __global__ void __launch_bounds__(ColShape<LOGN>::T, ColShape<LOGN>::MINB) k_col
 
 // Row pass grid -> image (as k_row_c2r), ROWS rows per CTA, half-length 2^LOGH.
 template <int LOGH>
-__global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB) k_row_c2r_t(const float2 *__restrict__ grid,
-                                                                   int pitch, int nx, int ny,
-                                                                   int ibegy,
-                                                                   const float2 *__restrict__ tw,
-                                                                   CorrParams cp,
-                                                                   const float *__restrict__ scale_dev,
-                                                                   float *image) {
+__global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB)
+    k_row_c2r_t(const __grid_constant__ FftBatch bt, int pitch, int nx, int ny, int ibegy,
+                const float2 *__restrict__ tw, CorrParams cp) {
+    const float2 *__restrict__ grid = bt.grid[blockIdx.y];
+    const float *__restrict__ scale_dev = bt.scale[blockIdx.y];
+    float *image = bt.image[blockIdx.y];
     using S = RowShape<LOGH>;
     constexpr int H = S::H, ROWS = S::ROWS, T = S::T, FNU = 2 * H;
     constexpr int TOTAL = ROWS * H;
@@ -646,11 +646,11 @@ __global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB) k_row
 
 // Row pass image -> grid (as k_row_r2c), ROWS rows per CTA, half-length 2^LOGH.
 template <int LOGH>
-__global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB) k_row_r2c_t(const float *__restrict__ image,
-                                                                   int nx, int ny, int ibegy,
-                                                                   const float2 *__restrict__ tw,
-                                                                   CorrParams cp, float2 *grid,
-                                                                   int pitch) {
+__global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB)
+    k_row_r2c_t(const __grid_constant__ FftBatch bt, int nx, int ny, int ibegy,
+                const float2 *__restrict__ tw, CorrParams cp, int pitch) {
+    const float *__restrict__ image = bt.image[blockIdx.y];
+    float2 *grid = bt.grid[blockIdx.y];
     using S = RowShape<LOGH>;
     constexpr int H = S::H, ROWS = S::ROWS, T = S::T, FNU = 2 * H;
     constexpr int TOTAL = ROWS * H;
@@ -709,76 +709,76 @@ __global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB) k_row
 
 // Launchers for the compile-time shapes: false if the size has no instance.
 template <int LOGN>
-cudaError_t launch_col_t(float2 *grid, int pitch, int nu, const float2 *tw, bool inverse, int r0,
-                         int r1, cudaStream_t st) {
+cudaError_t launch_col_t(const FftBatch &bt, int nbatch, int pitch, int nu, const float2 *tw,
+                         bool inverse, int r0, int r1, cudaStream_t st) {
     using S = ColShape<LOGN>;
-    const unsigned nb = (unsigned)((nu + S::CC - 1) / S::CC);
+    const dim3 nb((unsigned)((nu + S::CC - 1) / S::CC), (unsigned)nbatch);
     if (inverse) {
         cudaError_t e = cudaFuncSetAttribute(k_col_fft_t<LOGN, true>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
         if (e != cudaSuccess) return e;
-        k_col_fft_t<LOGN, true><<<nb, S::T, S::SMEM, st>>>(grid, pitch, nu, tw, r0, r1);
+        k_col_fft_t<LOGN, true><<<nb, S::T, S::SMEM, st>>>(bt, pitch, nu, tw, r0, r1);
     } else {
         cudaError_t e = cudaFuncSetAttribute(k_col_fft_t<LOGN, false>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
         if (e != cudaSuccess) return e;
-        k_col_fft_t<LOGN, false><<<nb, S::T, S::SMEM, st>>>(grid, pitch, nu, tw, r0, r1);
+        k_col_fft_t<LOGN, false><<<nb, S::T, S::SMEM, st>>>(bt, pitch, nu, tw, r0, r1);
     }
     return cudaGetLastError();
 }
 
 template <int LOGH>
-cudaError_t launch_c2r_t(const float2 *grid, int pitch, int nx, int ny, int ibegy, const float2 *tw,
-                         CorrParams cp, const float *scale_dev, float *image, cudaStream_t st) {
+cudaError_t launch_c2r_t(const FftBatch &bt, int nbatch, int pitch, int nx, int ny, int ibegy,
+                         const float2 *tw, CorrParams cp, cudaStream_t st) {
     using S = RowShape<LOGH>;
     cudaError_t e = cudaFuncSetAttribute(k_row_c2r_t<LOGH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)S::SMEM);
     if (e != cudaSuccess) return e;
-    k_row_c2r_t<LOGH><<<(unsigned)((ny + S::ROWS - 1) / S::ROWS), S::T, S::SMEM, st>>>(
-        grid, pitch, nx, ny, ibegy, tw, cp, scale_dev, image);
+    k_row_c2r_t<LOGH><<<dim3((unsigned)((ny + S::ROWS - 1) / S::ROWS), (unsigned)nbatch), S::T, S::SMEM,
+                        st>>>(bt, pitch, nx, ny, ibegy, tw, cp);
     return cudaGetLastError();
 }
 
 template <int LOGH>
-cudaError_t launch_r2c_t(const float *image, int nx, int ny, int ibegy, const float2 *tw,
-                         CorrParams cp, float2 *grid, int pitch, cudaStream_t st) {
+cudaError_t launch_r2c_t(const FftBatch &bt, int nbatch, int nx, int ny, int ibegy, const float2 *tw,
+                         CorrParams cp, int pitch, cudaStream_t st) {
     using S = RowShape<LOGH>;
     cudaError_t e = cudaFuncSetAttribute(k_row_r2c_t<LOGH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)S::SMEM);
     if (e != cudaSuccess) return e;
-    k_row_r2c_t<LOGH><<<(unsigned)((ny + S::ROWS - 1) / S::ROWS), S::T, S::SMEM, st>>>(
-        image, nx, ny, ibegy, tw, cp, grid, pitch);
+    k_row_r2c_t<LOGH><<<dim3((unsigned)((ny + S::ROWS - 1) / S::ROWS), (unsigned)nbatch), S::T, S::SMEM,
+                        st>>>(bt, nx, ny, ibegy, tw, cp, pitch);
     return cudaGetLastError();
 }
 
 #define SDE_LOG_CASES(X) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13)
 
 // Column pass through the compile-time kernels when 2^logn has an instance.
-bool col_fft_t(int logn, float2 *grid, int pitch, int nu, const float2 *tw, bool inverse, int r0,
-               int r1, cudaStream_t st, cudaError_t *err) {
+bool col_fft_t(int logn, const FftBatch &bt, int nbatch, int pitch, int nu, const float2 *tw,
+               bool inverse, int r0, int r1, cudaStream_t st, cudaError_t *err) {
     switch (logn) {
 #define CASE(L) \
-    case L: *err = launch_col_t<L>(grid, pitch, nu, tw, inverse, r0, r1, st); return true;
+    case L: *err = launch_col_t<L>(bt, nbatch, pitch, nu, tw, inverse, r0, r1, st); return true;
         SDE_LOG_CASES(CASE)
 #undef CASE
         default: return false;
     }
 }
-bool c2r_t(int logh, const float2 *grid, int pitch, int nx, int ny, int ibegy, const float2 *tw,
-           CorrParams cp, const float *scale_dev, float *image, cudaStream_t st, cudaError_t *err) {
+bool c2r_t(int logh, const FftBatch &bt, int nbatch, int pitch, int nx, int ny, int ibegy,
+           const float2 *tw, CorrParams cp, cudaStream_t st, cudaError_t *err) {
     switch (logh) {
 #define CASE(L) \
-    case L: *err = launch_c2r_t<L>(grid, pitch, nx, ny, ibegy, tw, cp, scale_dev, image, st); return true;
+    case L: *err = launch_c2r_t<L>(bt, nbatch, pitch, nx, ny, ibegy, tw, cp, st); return true;
         SDE_LOG_CASES(CASE)
 #undef CASE
         default: return false;
     }
 }
-bool r2c_t(int logh, const float *image, int nx, int ny, int ibegy, const float2 *tw, CorrParams cp,
-           float2 *grid, int pitch, cudaStream_t st, cudaError_t *err) {
+bool r2c_t(int logh, const FftBatch &bt, int nbatch, int nx, int ny, int ibegy, const float2 *tw,
+           CorrParams cp, int pitch, cudaStream_t st, cudaError_t *err) {
     switch (logh) {
 #define CASE(L) \
-    case L: *err = launch_r2c_t<L>(image, nx, ny, ibegy, tw, cp, grid, pitch, st); return true;
+    case L: *err = launch_r2c_t<L>(bt, nbatch, nx, ny, ibegy, tw, cp, pitch, st); return true;
         SDE_LOG_CASES(CASE)
 #undef CASE
         default: return false;
@@ -787,6 +787,47 @@ bool r2c_t(int logh, const float *image, int nx, int ny, int ibegy, const float2
 #undef SDE_LOG_CASES
 
 }  // namespace
+
+int fft_images_from_grids(sde_ctx *ctx, int n, float2 *const *grids, float *const *images,
+                          const float *const *scales, int pitch, int nx, int ny, int fnu, int nv,
+                          int correct) {
+    if (!ctx || n < 0) return SDE_EINVAL;
+    if (n == 0) return SDE_OK;
+    SDE_TRY(check_fft_args(nx, ny, fnu, nv, pitch));
+    const int logn = ilog2(nv), logh = ilog2(fnu / 2);
+    if (logn < 5 || logn > 13 || logh < 5 || logh > 13) {
+        sde_set_error("batched FFT: no compiled shape for fnu=%d nv=%d", fnu, nv);
+        return SDE_EINVAL;
+    }
+    const int nu = fnu / 2 + 1;
+    const float2 *twv, *twu;
+    SDE_TRY(ctx_twiddles(ctx, nv, &twv));
+    SDE_TRY(ctx_twiddles(ctx, fnu, &twu));
+    CorrParams cp = {nullptr, nullptr, nullptr};
+    if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
+    const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;
+    for (int b0 = 0; b0 < n; b0 += FFT_MAXB) {
+        const int nb = n - b0 < FFT_MAXB ? n - b0 : FFT_MAXB;
+        FftBatch bt{};
+        for (int i = 0; i < nb; i++) {
+            bt.grid[i] = grids[b0 + i];
+            bt.image[i] = images[b0 + i];
+            bt.scale[i] = scales ? scales[b0 + i] : nullptr;
+        }
+        cudaError_t e = cudaSuccess;
+        {
+            KTimer kt(ctx, "col_fft_batch");
+            col_fft_t(logn, bt, nb, pitch, nu, twv, true, 0, nv, ctx->stream, &e);
+        }
+        SDE_CUDA_TRY(e);
+        {
+            KTimer kt(ctx, "row_c2r_batch");
+            c2r_t(logh, bt, nb, pitch, nx, ny, ibegy, twu, cp, ctx->stream, &e);
+        }
+        SDE_CUDA_TRY(e);
+    }
+    return SDE_OK;
+}
 
 int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, int fnu, int nv,
                         int correct, const float *scale_dev, float *image) {
@@ -800,7 +841,9 @@ int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, in
     {
         KTimer kt(ctx, "col_fft");
         cudaError_t e = cudaSuccess;
-        if (!col_fft_t(ilog2(nv), (float2 *)grid, pitch, nu, twv, true, 0, nv, ctx->stream, &e)) {
+        FftBatch bt{};
+        bt.grid[0] = (float2 *)grid;
+        if (!col_fft_t(ilog2(nv), bt, 1, pitch, nu, twv, true, 0, nv, ctx->stream, &e)) {
             const int lcc = col_logcc(nv), cc = 1 << lcc;
             const size_t smc = sizeof(float2) * (size_t)cc * nv;
             SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
@@ -815,8 +858,11 @@ int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, in
     const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;  // 0-based first grid row
     KTimer kt(ctx, "row_c2r");
     cudaError_t e = cudaSuccess;
-    if (!c2r_t(ilog2(fnu / 2), (const float2 *)grid, pitch, nx, ny, ibegy, twu, cp, scale_dev, image,
-               ctx->stream, &e)) {
+    FftBatch bt{};
+    bt.grid[0] = (float2 *)grid;
+    bt.image[0] = image;
+    bt.scale[0] = scale_dev;
+    if (!c2r_t(ilog2(fnu / 2), bt, 1, pitch, nx, ny, ibegy, twu, cp, ctx->stream, &e)) {
         int rows, thr;
         row_shape(fnu, &rows, &thr);
         const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
@@ -844,8 +890,10 @@ int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fn
     {
         KTimer kt(ctx, "row_r2c");
         cudaError_t e = cudaSuccess;
-        if (!r2c_t(ilog2(fnu / 2), image, nx, ny, ibegy, twu, cp, (float2 *)grid, pitch, ctx->stream,
-                   &e)) {
+        FftBatch bt{};
+        bt.grid[0] = (float2 *)grid;
+        bt.image[0] = const_cast<float *>(image);
+        if (!r2c_t(ilog2(fnu / 2), bt, 1, nx, ny, ibegy, twu, cp, pitch, ctx->stream, &e)) {
             int rows, thr;
             row_shape(fnu, &rows, &thr);
             const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
@@ -858,8 +906,9 @@ int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fn
     }
     KTimer kt(ctx, "col_fft");
     cudaError_t e = cudaSuccess;
-    if (!col_fft_t(ilog2(nv), (float2 *)grid, pitch, nu, twv, false, ibegy, ibegy + ny, ctx->stream,
-                   &e)) {
+    FftBatch bt{};
+    bt.grid[0] = (float2 *)grid;
+    if (!col_fft_t(ilog2(nv), bt, 1, pitch, nu, twv, false, ibegy, ibegy + ny, ctx->stream, &e)) {
         const int lcc = col_logcc(nv), cc = 1 << lcc;
         const size_t smc = sizeof(float2) * (size_t)cc * nv;
         SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));

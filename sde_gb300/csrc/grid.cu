@@ -77,27 +77,15 @@ __device__ __forceinline__ Taps read_taps(const float *tg, int q, uint32_t g) {
 // once per group (same addresses: L1 broadcast).  The shared tile (real and imaginary
 // planes) receives each chunk's window once, through shared-memory atomics (a warp's 8
 // chunks share a colour class, so their windows do not overlap).
+// Grid one work item: the item's chunks into the shared tile (planar re/im planes, zero on
+// entry; tap table filled), then the touched cells into the raw grid.  Reading the tile
+// back zeroes it, so the next item of a persistent CTA starts from a clean tile once the
+// caller's barrier has passed.
 template <bool PSF>
-__global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
-    k_grid(const WorkItem *__restrict__ items, const uint2 *__restrict__ chunks,
-           const float4 *__restrict__ rec, const float *__restrict__ cft_g, float2 *raw,
-           int pitch, int ntu, int nu, int nv) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *tre = reinterpret_cast<float *>(smem_raw);
-    float *tim = tre + STILE * STILE;
-    float *tab = tim + STILE * STILE;  // tap table
-    const WorkItem it = items[blockIdx.x];
-    if (threadIdx.x == 0) {
-        // the item's chunk list and records stream into L2 while the tile is cleared
-        prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
-        prefetch_l2_range(rec, it.vbeg, it.vend, 16);
-    }
-    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
-        tre[k] = 0.f;
-        tim[k] = 0.f;
-    }
-    fill_tap_table(cft_g, tab, GRID_THREADS);
-    __syncthreads();
+__device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__restrict__ chunks,
+                                          const float4 *__restrict__ rec, const float *tab,
+                                          float *tre, float *tim, float2 *raw, int pitch,
+                                          int ntu, int nu, int nv) {
     const int q = threadIdx.x & (GLANES - 1);
     const int grp = threadIdx.x / GLANES;
     const float *tg = tab + (grp & (TAP_COPIES - 1)) * TAP_ROW;  // this group's copy
@@ -165,10 +153,80 @@ __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
     for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
         const float2 val = make_float2(tre[k], tim[k]);
         if (val.x == 0.f && val.y == 0.f) continue;
+        tre[k] = 0.f;
+        tim[k] = 0.f;
         const int r = k / STILE, cc = k - r * STILE;
         const int gv0 = tv * TILE + r - SUPP, gu0 = tu * TILE + cc - SUPP;  // 0-based raw
         if (gv0 < 0 || gv0 >= nv || gu0 < 0 || gu0 >= nu) continue;
         red_add_f2(&raw[(int64_t)gv0 * pitch + gu0], val);
+    }
+}
+
+// One CTA per work item of one plan.
+template <bool PSF>
+__global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
+    k_grid(const WorkItem *__restrict__ items, const uint2 *__restrict__ chunks,
+           const float4 *__restrict__ rec, const float *__restrict__ cft_g, float2 *raw,
+           int pitch, int ntu, int nu, int nv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *tre = reinterpret_cast<float *>(smem_raw);
+    float *tim = tre + STILE * STILE;
+    float *tab = tim + STILE * STILE;  // tap table
+    const WorkItem it = items[blockIdx.x];
+    if (threadIdx.x == 0) {
+        // the item's chunk list and records stream into L2 while the tile is cleared
+        prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
+        prefetch_l2_range(rec, it.vbeg, it.vend, 16);
+    }
+    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
+        tre[k] = 0.f;
+        tim[k] = 0.f;
+    }
+    fill_tap_table(cft_g, tab, GRID_THREADS);
+    __syncthreads();
+    grid_item<PSF>(it, chunks, rec, tab, tre, tim, raw, pitch, ntu, nu, nv);
+}
+
+// Persistent gridding of many plans (a mosaic's pointings, a batch of served jobs): each
+// CTA fills its tap table once, then takes work items from the combined list of all plans
+// (item_start[p] = first combined index of plan p) through an atomic counter until the
+// list is exhausted.  One launch grids every plan.
+template <bool PSF>
+__global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
+    k_grid_batch(const BatchPlan *__restrict__ plans, const int64_t *__restrict__ item_start,
+                 int nplans, unsigned long long *counter, const float *__restrict__ cft_g) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *tre = reinterpret_cast<float *>(smem_raw);
+    float *tim = tre + STILE * STILE;
+    float *tab = tim + STILE * STILE;
+    __shared__ long long s_next;
+    __shared__ int s_plan;
+    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
+        tre[k] = 0.f;
+        tim[k] = 0.f;
+    }
+    fill_tap_table(cft_g, tab, GRID_THREADS);
+    const int64_t total = item_start[nplans];
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long n = (long long)atomicAdd(counter, 1ull);
+            int p = 0;
+            if (n < total)
+                while (p + 1 < nplans && item_start[p + 1] <= n) p++;
+            s_next = n;
+            s_plan = p;
+        }
+        __syncthreads();
+        const long long n = s_next;
+        if (n >= total) break;
+        const BatchPlan P = plans[s_plan];
+        const WorkItem it = P.items[n - item_start[s_plan]];
+        if (threadIdx.x == 0) {
+            prefetch_l2_range(P.chunks, it.cbeg, it.cend, 8);
+            prefetch_l2_range(P.rec, it.vbeg, it.vend, 16);
+        }
+        grid_item<PSF>(it, P.chunks, P.rec, tab, tre, tim, P.raw, P.pitch, P.ntu, P.nu, P.nv);
+        __syncthreads();
     }
 }
 
@@ -238,15 +296,12 @@ __global__ void k_build_cft(const float *cf, float *cft) {
 // Symmetrise, shift left by SUPPU and normalise (grd/grdh2d.f:202-226).  raw and out are
 // [nv][pitch] complex; out(u,v) = scale * R'(u+SUPP, v) for u <= NU-SUPP, else 0, where R'
 // adds conj(R(UC-k, 2VC-v)) into columns UC+k, k = 0..SUPP, UC = UORIGIN+SUPP.
-__global__ void k_finalize(const float2 *__restrict__ raw, float2 *__restrict__ out, int nu,
-                           int nv, int pitch, int uorigin, int vorigin, int supp, float scale) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)nv * pitch) return;
+// One cell of the final GRDH2D grid from the raw accumulation (index idx of [nv][pitch]).
+__device__ __forceinline__ float2 finalize_cell(const float2 *__restrict__ raw, int64_t idx, int nu,
+                                                int nv, int pitch, int uorigin, int vorigin,
+                                                int supp, float scale) {
     const int v0 = (int)(idx / pitch), u0 = (int)(idx - (int64_t)v0 * pitch);
-    if (u0 >= nu) {
-        out[idx] = make_float2(0.f, 0.f);
-        return;
-    }
+    if (u0 >= nu) return make_float2(0.f, 0.f);
     const int u1 = u0 + 1, v1 = v0 + 1;  // 1-based
     float2 r = make_float2(0.f, 0.f);
     if (u1 <= nu - supp) {
@@ -266,7 +321,22 @@ __global__ void k_finalize(const float2 *__restrict__ raw, float2 *__restrict__ 
         r.x *= scale;
         r.y *= scale;
     }
-    out[idx] = r;
+    return r;
+}
+
+__global__ void k_finalize(const float2 *__restrict__ raw, float2 *__restrict__ out, int nu,
+                           int nv, int pitch, int uorigin, int vorigin, int supp, float scale) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)nv * pitch) return;
+    out[idx] = finalize_cell(raw, idx, nu, nv, pitch, uorigin, vorigin, supp, scale);
+}
+
+// finalize of many grids: blockIdx.y picks the grid, blocks past its size return
+__global__ void k_finalize_batch(const FinalizeDesc *__restrict__ d) {
+    const FinalizeDesc f = d[blockIdx.y];
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)f.nv * f.pitch) return;
+    f.out[idx] = finalize_cell(f.raw, idx, f.nu, f.nv, f.pitch, f.uorigin, f.vorigin, f.supp, f.scale);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -663,6 +733,37 @@ int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, float2 *out, int nu, in
     KTimer kt(ctx, "finalize");
     k_finalize<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(raw, out, nu, nv, pitch, uorigin,
                                                           vorigin, supp, scale);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+size_t grid_smem_bytes() { return grid_smem(); }
+
+int launch_grid_batch(sde_ctx *ctx, int psf, const BatchPlan *d_plans, const int64_t *d_item_start,
+                      int nplans, unsigned long long *d_counter, const float *cft, int nctas) {
+    static bool attr = false;
+    if (!attr) {
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)grid_smem()));
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)grid_smem()));
+        attr = true;
+    }
+    KTimer kt(ctx, psf ? "grid_batch_psf" : "grid_batch");
+    if (psf)
+        k_grid_batch<true><<<nctas, GRID_THREADS, grid_smem(), ctx->stream>>>(d_plans, d_item_start, nplans,
+                                                                             d_counter, cft);
+    else
+        k_grid_batch<false><<<nctas, GRID_THREADS, grid_smem(), ctx->stream>>>(d_plans, d_item_start, nplans,
+                                                                              d_counter, cft);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, int n, int64_t max_cells) {
+    if (n <= 0) return SDE_OK;
+    KTimer kt(ctx, "finalize_batch");
+    k_finalize_batch<<<dim3((unsigned)ceil_div(max_cells, 256), (unsigned)n), 256, 0, ctx->stream>>>(d_desc);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }

@@ -215,15 +215,16 @@ __global__ void k_heads(const uint32_t *__restrict__ keys, const unsigned long l
 }
 
 __global__ void k_chunk_flags(const unsigned long long *counts, const int32_t *runstart,
-                              const int32_t *tilestart, uint32_t *ihead, uint32_t *chead) {
+                              const int32_t *tilestart, int item_max, int chunk_max,
+                              uint32_t *ihead, uint32_t *chead) {
     int64_t nv = (int64_t)counts[0];
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nv) return;
     int32_t rs = runstart[q], ts = tilestart[q];
-    int32_t is = ts + ((int32_t)q - ts) / ITEM_MAX * ITEM_MAX;  // item start
+    int32_t is = ts + ((int32_t)q - ts) / item_max * item_max;  // item start
     int32_t cs = rs > is ? rs : is;                            // run start within item
-    bool ih = ((int32_t)q - ts) % ITEM_MAX == 0;
-    bool ch = ((int32_t)q - cs) % CHUNK_MAX == 0;
+    bool ih = ((int32_t)q - ts) % item_max == 0;
+    bool ch = ((int32_t)q - cs) % chunk_max == 0;
     ihead[q] = ih;
     chead[q] = ch || ih;
 }
@@ -231,7 +232,8 @@ __global__ void k_chunk_flags(const unsigned long long *counts, const int32_t *r
 __global__ void k_chunk_write(const uint32_t *__restrict__ keys, const unsigned long long *counts,
                               const int32_t *runstart, const int32_t *tilestart,
                               const uint32_t *ihead, const uint32_t *chead,
-                              const uint32_t *item_id, const uint32_t *chunk_id, int jbits,
+                              const uint32_t *item_id, const uint32_t *chunk_id, int item_max,
+                              int chunk_max, int lbits, int jbits,
                               uint64_t *ckey, uint32_t *cval, uint32_t *cstart, WorkItem *items) {
     int64_t nv = (int64_t)counts[0];
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -249,13 +251,13 @@ __global__ void k_chunk_write(const uint32_t *__restrict__ keys, const unsigned 
     if (!chead[q]) return;
     uint32_t c = chunk_id[q];
     int32_t rs = runstart[q], ts = tilestart[q];
-    int32_t is = ts + ((int32_t)q - ts) / ITEM_MAX * ITEM_MAX;
+    int32_t is = ts + ((int32_t)q - ts) / item_max * item_max;
     int32_t cs = rs > is ? rs : is;
-    uint32_t j = ((uint32_t)q - (uint32_t)cs) / CHUNK_MAX;
+    uint32_t j = ((uint32_t)q - (uint32_t)cs) / (uint32_t)chunk_max;
     uint32_t cell = k & 4094u, lu = cell & 63u, lv = cell >> 6;  // pair's even cell
     uint32_t color = ((lu >> 1) & 3u) * 7u + (lv % 7u);
-    ckey[c] = ((uint64_t)it << (6 + LBITS + jbits + 12)) |
-              ((uint64_t)color << (LBITS + jbits + 12)) | ((uint64_t)j << 12) | cell;
+    ckey[c] = ((uint64_t)it << (6 + lbits + jbits + 12)) |
+              ((uint64_t)color << (lbits + jbits + 12)) | ((uint64_t)j << 12) | cell;
     cval[c] = c;
     cstart[c] = (uint32_t)q;
 }
@@ -264,12 +266,12 @@ __global__ void k_chunk_write(const uint32_t *__restrict__ keys, const unsigned 
 // within a colour class longer chunks come first, so the 8 chunks that a warp of the
 // gridder or degridder takes together have similar lengths.
 __global__ void k_chunk_len(const uint32_t *__restrict__ cstart, int64_t nchunks, int64_t nvalid,
-                            int lshift, uint64_t *ckey) {
+                            int chunk_max, int lshift, uint64_t *ckey) {
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nchunks) return;
     const uint32_t en = c + 1 < nchunks ? cstart[c + 1] : (uint32_t)nvalid;
     const uint32_t len = en - cstart[c];
-    ckey[c] |= (uint64_t)(CHUNK_MAX - len) << lshift;
+    ckey[c] |= (uint64_t)(chunk_max - (int)len) << lshift;
 }
 
 __global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t *__restrict__ cval,
@@ -332,8 +334,21 @@ int sde_plan_destroy(sde_plan *pl) {
 int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const float *u,
                     const float *v, const float *w, const float *vis, const float *wt,
                     int where, sde_plan **out) {
+    return sde_plan_create_opts(ctx, spec, nvis, u, v, w, vis, wt, where, nullptr, out);
+}
+
+int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const float *u,
+                         const float *v, const float *w, const float *vis, const float *wt,
+                         int where, const sde_plan_opts *opts, sde_plan **out) {
     if (!ctx || !spec || !out || nvis < 0 || (nvis > 0 && (!u || !v || !w || !vis || !wt))) {
         sde_set_error("sde_plan_create: bad arguments");
+        return SDE_EINVAL;
+    }
+    const int item_max = opts && opts->item_max > 0 ? opts->item_max : ITEM_MAX;
+    const int chunk_max = opts && opts->chunk_max > 0 ? opts->chunk_max : CHUNK_MAX;
+    if (item_max > ITEM_LIMIT || chunk_max > CHUNK_LIMIT || chunk_max > item_max) {
+        sde_set_error("sde_plan_create: work item %d / chunk %d out of range (item <= %d, "
+                      "chunk <= %d, chunk <= item)", item_max, chunk_max, ITEM_LIMIT, CHUNK_LIMIT);
         return SDE_EINVAL;
     }
     if (spec->supp != SUPP || spec->osamp != OSAMP) {
@@ -356,6 +371,8 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
     pl->ntu = (spec->nu + TILE - 1) / TILE;
     pl->ntv = (spec->nv + TILE - 1) / TILE;
     pl->nvis_in = nvis;
+    pl->item_max = item_max;
+    pl->chunk_max = chunk_max;
     int rc = SDE_OK;
 #define PL_TRY(x)                      \
     do {                               \
@@ -488,7 +505,8 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
             PL_CUDA(cudaGetLastError());
             PL_TRY(launch_inclusive_max_scan_i32(ctx, runhead, runhead, nvalid));
             PL_TRY(launch_inclusive_max_scan_i32(ctx, tilehead, tilehead, nvalid));
-            k_chunk_flags<<<ceil_div(nvalid, T), T, 0, st>>>(counts, runhead, tilehead, ihead, chead);
+            k_chunk_flags<<<ceil_div(nvalid, T), T, 0, st>>>(counts, runhead, tilehead, pl->item_max,
+                                                           pl->chunk_max, ihead, chead);
             PL_CUDA(cudaGetLastError());
             PL_TRY(launch_exclusive_scan_u32(ctx, ihead, item_id, nvalid, tot));
             PL_TRY(launch_exclusive_scan_u32(ctx, chead, chunk_id, nvalid, tot + 1));
@@ -507,15 +525,17 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
             PL_TRY(ctx_scratch(ctx, "pl_cval", 4 * (size_t)nchunks, (void **)&cval));
             PL_TRY(ctx_scratch(ctx, "pl_cvtmp", 4 * (size_t)nchunks, (void **)&cvtmp));
             PL_TRY(ctx_scratch(ctx, "pl_cstart", 4 * (size_t)nchunks, (void **)&cstart));
-            const int jbits = bits_for(ITEM_MAX / CHUNK_MAX);
+            const int jbits = bits_for(pl->item_max / pl->chunk_max);
+            const int lbits = bits_for(pl->chunk_max - 1);
             k_chunk_write<<<ceil_div(nvalid, T), T, 0, st>>>(keys, counts, runhead, tilehead, ihead,
-                                                           chead, item_id, chunk_id, jbits, ckey,
+                                                           chead, item_id, chunk_id, pl->item_max,
+                                                           pl->chunk_max, lbits, jbits, ckey,
                                                            cval, cstart, pl->items);
             PL_CUDA(cudaGetLastError());
-            k_chunk_len<<<ceil_div(nchunks, T), T, 0, st>>>(cstart, nchunks, nvalid, jbits + 12,
-                                                          ckey);
+            k_chunk_len<<<ceil_div(nchunks, T), T, 0, st>>>(cstart, nchunks, nvalid, pl->chunk_max,
+                                                          jbits + 12, ckey);
             PL_CUDA(cudaGetLastError());
-            const int shift_item = 6 + LBITS + jbits + 12;
+            const int shift_item = 6 + lbits + jbits + 12;
             const int cbits = shift_item + bits_for(nitems);
             PL_TRY(launch_radix_sort_u64(ctx, ckey, cval, nchunks, cbits, cktmp, cvtmp));
             k_chunk_final<<<ceil_div(nchunks, T), T, 0, st>>>(ckey, cval, cstart, keys, nchunks,

@@ -130,7 +130,8 @@ def _ptr(t):
 class Context:
     """A libsdegpu context bound to torch's current CUDA stream."""
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, stream=None):
+        """stream: a torch.cuda.Stream for the library's work (default: the current one)."""
         torch = _torch()
         self.torch = torch
         self.device = torch.device("cuda", device)
@@ -140,7 +141,7 @@ class Context:
         self.h = h
         import weakref
         self._plans = weakref.WeakSet()  # closed before the context goes away
-        self.stream = torch.cuda.current_stream(self.device)
+        self.stream = stream if stream is not None else torch.cuda.current_stream(self.device)
         check(lib().sde_ctx_set_stream(h, C.c_void_p(self.stream.cuda_stream)), "set_stream")
 
     def close(self):
@@ -236,14 +237,21 @@ class Context:
 class Plan:
     """Device-resident, tile-sorted visibilities of one job (sde_plan)."""
 
-    def __init__(self, ctx, geom, u, v, w, vis, wt):
+    def __init__(self, ctx, geom, u, v, w, vis, wt, opts=None):
+        """opts: (item_max, chunk_max) sort-bucket sizes, None for the defaults."""
         self.ctx, self.geom = ctx, geom
         self.nvis_in = int(wt.numel())
         h = C.c_void_p()
         spec = geom.spec()
-        check(lib().sde_plan_create(ctx.h, C.byref(spec), self.nvis_in, _ptr(u), _ptr(v),
-                                    _ptr(w), _ptr(vis), _ptr(wt), _abi.SDE_DEVICE, C.byref(h)),
-              "sde_plan_create")
+        if opts is None:
+            check(lib().sde_plan_create(ctx.h, C.byref(spec), self.nvis_in, _ptr(u), _ptr(v),
+                                        _ptr(w), _ptr(vis), _ptr(wt), _abi.SDE_DEVICE,
+                                        C.byref(h)), "sde_plan_create")
+        else:
+            o = _abi.PlanOpts(int(opts[0]), int(opts[1]))
+            check(lib().sde_plan_create_opts(ctx.h, C.byref(spec), self.nvis_in, _ptr(u), _ptr(v),
+                                             _ptr(w), _ptr(vis), _ptr(wt), _abi.SDE_DEVICE,
+                                             C.byref(o), C.byref(h)), "sde_plan_create_opts")
         self.h = h
         ctx._plans.add(self)
 

@@ -9,8 +9,10 @@ antenna positions; this module follows the same physics with numpy:
     v = -sin(dec) cosH X + sin(dec) sinH Y + cos(dec) Z,
     w =  cos(dec) cosH X - cos(dec) sinH Y + sin(dec) Z, in wavelengths;
   * visibilities of point (and Gaussian) sources
-    V = sum_k S_k exp(-2 pi i (u l_k + v m_k)) (times the Gaussian's transform), plus
-    complex Gaussian noise.
+    V = sum_k S_k exp(+2 pi i (u l_k + v m_k)) (times the Gaussian's transform), plus
+    complex Gaussian noise -- SDE's sign: its direct-transform imaging applies
+    exp(-2 pi i u l) with l = CDELT (I - CRPIX), CDELT < 0 in RA (vis/visdftp2.f:101-107),
+    so a source east of the centre (l > 0) appears left of the centre pixel.
 Visibilities are ordered channel-major, then time, then baseline (AIPS 'TB' order within a
 channel).  Coordinates are float32 wavelengths, visibilities complex64, weights float32,
 matching the reference's SoA layout (Vis/UU, Vis/VV, Vis/WW, Vis/OBS/I/VIS, .../WT).
@@ -78,7 +80,8 @@ def point_sky(n_src, field_arcsec, seed, s_min=1e-4, s_max=1.0, index=-1.5):
 
 
 def visibilities(u, v, flux, l, m, noise_sigma, seed, gauss=None, chunk=1 << 20):
-    """Complex64 visibilities of point sources (+ optional Gaussians (S, l, m, fwhm_rad))."""
+    """Complex64 visibilities of point sources (+ optional Gaussians (S, l, m, fwhm_rad)),
+    SDE's sign convention (module docstring)."""
     n = len(u)
     out = np.empty(n, np.complex64)
     rng = np.random.default_rng(seed + 2)
@@ -87,12 +90,12 @@ def visibilities(u, v, flux, l, m, noise_sigma, seed, gauss=None, chunk=1 << 20)
         vv = v[s0:s0 + chunk].astype(np.float64)
         acc = np.zeros(len(uu), np.complex128)
         for S, ll, mm in zip(flux, l, m):
-            acc += S * np.exp(-2j * np.pi * (uu * ll + vv * mm))
+            acc += S * np.exp(2j * np.pi * (uu * ll + vv * mm))
         if gauss is not None:
             for S, ll, mm, fw in gauss:
                 sig = fw / (2.0 * math.sqrt(2.0 * math.log(2.0)))
                 amp = np.exp(-2.0 * np.pi ** 2 * sig ** 2 * (uu ** 2 + vv ** 2))
-                acc += S * amp * np.exp(-2j * np.pi * (uu * ll + vv * mm))
+                acc += S * amp * np.exp(2j * np.pi * (uu * ll + vv * mm))
         out[s0:s0 + chunk] = acc
     if noise_sigma > 0:
         out += (rng.normal(0, noise_sigma, n) + 1j * rng.normal(0, noise_sigma, n)).astype(
@@ -129,3 +132,64 @@ def config2_uvw(n_chan=64, dt_s=10.0):
 
 CONFIG2 = dict(imsize=4096, cellsize=0.5, vra=0.0, vdec=40.0, fov=1.0, rmode="NORM",
                robust=(0.0, 0.0, 0.0), n_src=200, noise=1e-3)
+
+
+# ---- config 4: a mosaic of uneven pointings -----------------------------------------------
+CONFIG4 = dict(n_point=49, fwhm_arcmin=30.0, spacing_arcmin=15.0, cell_arcsec=2.0,
+               nvis_range=(2e3, 2e6), size_range=(256, 2048), n_src=40, noise=1e-3, dec=40.0,
+               arm_m=5000.0, freq_hz=1.4e9, hours=8.0)
+
+
+def hex_pointings(n, spacing):
+    """n pointing offsets (l, m) on a hexagonal lattice (rows offset by half a spacing,
+    row pitch spacing*sqrt(3)/2), centred on (0, 0)."""
+    side = int(math.ceil(math.sqrt(n)))
+    pts = []
+    for r in range(side):
+        for c in range(side):
+            if len(pts) < n:
+                pts.append(((c + 0.5 * (r % 2)) * spacing, r * spacing * math.sqrt(3.0) / 2.0))
+    pts = np.array(pts)
+    return pts - pts.mean(axis=0)
+
+
+def config4(n_point=None, seed=SEED_BASE + 4, nvis_range=None, size_range=None, vis_fn=None):
+    """Seeded mosaic: per pointing a dict(u, v, w, vis, wt, imsize, l0, m0, pb_fwhm_rad).
+    Pointing i sees the sky through a Gaussian primary beam centred on (l0, m0); its
+    visibilities are phased to its own centre.  vis_fn(u, v, flux, l, m, noise, seed) may
+    replace the numpy visibility sum (e.g. a device version); default: visibilities()."""
+    c = dict(CONFIG4)
+    n_point = c["n_point"] if n_point is None else n_point
+    nvis_range = c["nvis_range"] if nvis_range is None else nvis_range
+    size_range = c["size_range"] if size_range is None else size_range
+    rng = np.random.default_rng(seed)
+    a2r = math.radians(1.0 / 3600.0)
+    fwhm = c["fwhm_arcmin"] * 60.0 * a2r
+    centres = hex_pointings(n_point, c["spacing_arcmin"] * 60.0 * a2r)
+    pos = y_array(27, c["arm_m"], seed)
+    # sky: power-law point sources over the mosaic area (+ one FWHM margin)
+    ext = np.abs(centres).max(axis=0) + fwhm
+    a = -1.5
+    x = rng.uniform(0, 1, c["n_src"])
+    flux = (1e-3 ** a + x * (1.0 ** a - 1e-3 ** a)) ** (1.0 / a)
+    sl = rng.uniform(-ext[0], ext[0], c["n_src"])
+    sm = rng.uniform(-ext[1], ext[1], c["n_src"])
+    lo, hi = math.log(nvis_range[0]), math.log(nvis_range[1])
+    e_lo, e_hi = int(round(math.log2(size_range[0]))), int(round(math.log2(size_range[1])))
+    nbl = 27 * 26 // 2
+    out = []
+    for i, (l0, m0) in enumerate(centres):
+        nvis = int(math.exp(rng.uniform(lo, hi)))
+        imsize = 2 ** int(rng.integers(e_lo, e_hi + 1))
+        nt = max(1, -(-nvis // nbl))
+        u, v, w = uvw_tracks(pos, c["dec"], c["hours"], c["hours"] * 3600.0 / nt, [c["freq_hz"]])
+        u, v, w = u[:nvis], v[:nvis], w[:nvis]
+        dl, dm = sl - l0, sm - m0
+        pb = np.exp(-4.0 * math.log(2.0) * (dl ** 2 + dm ** 2) / fwhm ** 2)
+        keep = pb > 1e-3
+        fn = vis_fn or visibilities
+        vis = fn(u, v, flux[keep] * pb[keep], dl[keep], dm[keep], c["noise"], seed + 100 + i)
+        out.append(dict(u=u, v=v, w=w, vis=np.asarray(vis, np.complex64),
+                        wt=np.ones(len(u), np.float32), imsize=imsize, l0=float(l0),
+                        m0=float(m0), pb_fwhm_rad=fwhm))
+    return out, c
