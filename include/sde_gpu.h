@@ -128,6 +128,13 @@ int sde_ctx_profile(sde_ctx *ctx, int enable);
 int sde_ctx_kernel_stats(sde_ctx *ctx, const char *kernel, double *total_ms, int64_t *count);
 int sde_ctx_reset_stats(sde_ctx *ctx);
 int64_t sde_ctx_launches(sde_ctx *ctx);
+/* Compensated accumulation of the gridding sums across work items (default on): each work
+ * item's shared-memory tile is added into the raw grid with an atomic that returns the
+ * previous value, the rounding error of that FP32 add (TwoSum) goes to a second plane, and
+ * the finalize pass adds the planes.  Off: plain FP32 sums (half the raw-grid memory).
+ * Takes effect for passes started afterwards; batches fix it at sde_batch_create.
+ * No counterpart in the reference (GRDH2D sums every visibility into its cell in REAL). */
+int sde_ctx_set_compensated(sde_ctx *ctx, int on);
 
 /* Geometry of one gridding/degridding job (the scalar arguments of GRDH2D/GRDDEH2D). */
 typedef struct {

@@ -68,6 +68,7 @@ SIGNATURES = [
     ("sde_ctx_kernel_stats", I, [P, C.c_char_p, C.POINTER(C.c_double), C.POINTER(I64)]),
     ("sde_ctx_reset_stats", I, [P]),
     ("sde_ctx_launches", I64, [P]),
+    ("sde_ctx_set_compensated", I, [P, I]),
     ("sde_weights", I, [P, I, P, F, P, P, P, P, I64, F, F, F, F, I, I, I, I, P, P, P,
                         C.POINTER(WStats)]),
     ("sde_plan_create", I, [P, C.POINTER(GridSpec), I64, P, P, P, P, P, I, C.POINTER(P)]),

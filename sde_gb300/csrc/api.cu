@@ -268,6 +268,12 @@ extern "C" int sde_ctx_reset_stats(sde_ctx *c) {
 
 extern "C" int64_t sde_ctx_launches(sde_ctx *c) { return c ? c->nlaunch : 0; }
 
+extern "C" int sde_ctx_set_compensated(sde_ctx *c, int on) {
+    if (!c) return SDE_EINVAL;
+    c->compensated = on != 0;
+    return SDE_OK;
+}
+
 // ---------------------------------------------------------------------------------------
 // plan-level operations
 static int ensure_sums(sde_plan *pl) {
@@ -294,17 +300,20 @@ extern "C" int sde_plan_grid(sde_plan *pl, int what, float *grid, int pitch, flo
         return SDE_ENOWEIGHT;
     }
     float2 *raw;
-    SDE_TRY(ctx_scratch(ctx, "raw_grid", sizeof(float2) * (size_t)nv * pl->pitch, (void **)&raw));
-    SDE_TRY(plan_grid_raw(pl, what, raw));
+    const size_t cells = (size_t)nv * pl->pitch;
+    SDE_TRY(ctx_scratch(ctx, "raw_grid", sizeof(float2) * cells * (ctx->compensated ? 2 : 1),
+                        (void **)&raw));
+    float2 *raw_lo = ctx->compensated ? raw + cells : nullptr;
+    SDE_TRY(plan_grid_raw(pl, what, raw, raw_lo));
     // LSUMWT = FLOAT(NU-1)*FLOAT(NV)/LSUMWT (grd/grdh2d.f:218), applied in FP32
     const float scale = (float)((double)((float)(nu - 1) * (float)nv) / pl->h_lsumwt);
     if (pitch == pl->pitch) {
-        SDE_TRY(grid_finalize_scale(ctx, raw, (float2 *)grid, nu, nv, pitch, pl->spec.uorigin,
+        SDE_TRY(grid_finalize_scale(ctx, raw, raw_lo, (float2 *)grid, nu, nv, pitch, pl->spec.uorigin,
                                     pl->spec.vorigin, pl->spec.supp, scale));
     } else {
         float2 *tmp;
         SDE_TRY(ctx_scratch(ctx, "fin_grid", sizeof(float2) * (size_t)nv * pl->pitch, (void **)&tmp));
-        SDE_TRY(grid_finalize_scale(ctx, raw, tmp, nu, nv, pl->pitch, pl->spec.uorigin,
+        SDE_TRY(grid_finalize_scale(ctx, raw, raw_lo, tmp, nu, nv, pl->pitch, pl->spec.uorigin,
                                     pl->spec.vorigin, pl->spec.supp, scale));
         SDE_CUDA_TRY(cudaMemcpy2DAsync(grid, (size_t)pitch * 8, tmp, (size_t)pl->pitch * 8,
                                        (size_t)nu * 8, nv, cudaMemcpyDeviceToDevice, ctx->stream));

@@ -102,6 +102,7 @@ struct sde_batch {
     int64_t *d_npix = nullptr;
     int64_t max_cells = 0;
     size_t raw_bytes = 0;                      // the raw grids are contiguous from raw[0]
+    bool comp = true;                          // compensated cross-item sums (raw_lo planes)
     // shape class (fnu, nv, nx, ny, pitch) -> plan indices
     std::map<std::tuple<int, int, int, int, int>, std::vector<int>> classes;
     // mosaic
@@ -137,7 +138,7 @@ int batch_grid(sde_batch *b, int psf) {
     sde_ctx *ctx = b->ctx;
     SDE_CUDA_TRY(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), ctx->stream));
     SDE_CUDA_TRY(cudaMemsetAsync(b->raw[0], 0, b->raw_bytes, ctx->stream));
-    SDE_TRY(launch_grid_batch(ctx, psf, b->d_plans, b->d_item_start, b->n, b->d_counter,
+    SDE_TRY(launch_grid_batch(ctx, psf, b->comp, b->d_plans, b->d_item_start, b->n, b->d_counter,
                               ctx->d_cft, ctx->num_sms * 4));
     SDE_TRY(launch_finalize_batch(ctx, b->d_fin, b->n, b->max_cells));
     return SDE_OK;
@@ -224,6 +225,7 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
     sde_batch *b = new sde_batch();
     b->ctx = ctx;
     b->n = n;
+    b->comp = ctx->compensated;
     int rc = SDE_OK;
     std::vector<BatchPlan> hp(n);
     std::vector<int64_t> start(n + 1, 0);
@@ -262,7 +264,7 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
         b->ny.push_back(ny[i]);
         const size_t cells = (size_t)nv * pl->pitch;
         raw_off[i] = raw_total;
-        raw_total += (cells * 8 + 255) & ~(size_t)255;
+        raw_total += (cells * 8 * (b->comp ? 2 : 1) + 255) & ~(size_t)255;
         img_off[i] = img_total;
         img_total += ((size_t)nx[i] * ny[i] * 4 + 255) & ~(size_t)255;
         b->max_cells = std::max<int64_t>(b->max_cells, (int64_t)cells);
@@ -292,10 +294,11 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
         b->grid.push_back(reinterpret_cast<float2 *>(gridmem + raw_off[i]));
         b->psf.push_back(reinterpret_cast<float *>(imgmem + img_off[i]));
         b->image.push_back(reinterpret_cast<float *>(imgmem + img_total + img_off[i]));
-        hp[i] = BatchPlan{pl->items, pl->chunks, pl->rec, b->raw[i], pl->pitch, pl->ntu, pl->spec.nu,
+        float2 *lo = b->comp ? b->raw[i] + (size_t)pl->spec.nv * pl->pitch : nullptr;
+        hp[i] = BatchPlan{pl->items, pl->chunks, pl->rec, b->raw[i], lo, pl->pitch, pl->ntu, pl->spec.nu,
                           pl->spec.nv};
         const float scale = (float)((double)((float)(pl->spec.nu - 1) * (float)pl->spec.nv) / pl->h_lsumwt);
-        hf[i] = FinalizeDesc{b->raw[i], b->grid[i], pl->spec.nu, pl->spec.nv, pl->pitch,
+        hf[i] = FinalizeDesc{b->raw[i], lo, b->grid[i], pl->spec.nu, pl->spec.nv, pl->pitch,
                              pl->spec.uorigin, pl->spec.vorigin, pl->spec.supp, scale};
     }
     {

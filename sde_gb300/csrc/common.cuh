@@ -88,7 +88,11 @@ struct WorkItem {
     int32_t tile;      // tile id = tv * ntu + tu
     int32_t cbeg, cend;  // chunk range
     int32_t vbeg, vend;  // sorted visibility range
+    int32_t dense;     // 1: the item's tile holds >= DENSE_TILE_VIS visibilities
 };
+// A tile this full has many work items, so its cells receive long sums across items: those
+// sums are the ones compensated (sde_ctx_set_compensated).
+constexpr int DENSE_TILE_VIS = 65536;
 
 // ---------------------------------------------------------------------------------------
 // Context: one device, one stream, grow-only scratch buffers, cached tables.
@@ -113,6 +117,8 @@ struct sde_ctx {
     // per-kernel CUDA-event timing (sde_ctx_profile) and launch counting
     bool profile = false;
     int64_t nlaunch = 0;
+    // gridding sums across work items with TwoSum compensation (sde_ctx_set_compensated)
+    bool compensated = true;
     struct EvPair {
         const char *name;
         cudaEvent_t a, b;
@@ -185,9 +191,11 @@ struct sde_plan {
 int plan_build_cft(sde_plan *pl);
 int ctx_build_cft(sde_ctx *ctx);
 int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt);
-int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, float2 *out, int nu, int nv, int pitch,
+int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, const float2 *raw_lo, float2 *out, int nu, int nv, int pitch,
                         int uorigin, int vorigin, int supp, float scale);
-int plan_grid_raw(sde_plan *pl, int what, float2 *raw);
+// raw accumulation of one gridding pass; raw_lo (same shape, may be NULL) receives the
+// rounding errors of the cross-item sums (compensated accumulation)
+int plan_grid_raw(sde_plan *pl, int what, float2 *raw, float2 *raw_lo);
 
 // ---- batches of plans (mosaic pointings, served jobs) -----------------------------------
 // One plan as the persistent gridder sees it.
@@ -196,11 +204,13 @@ struct BatchPlan {
     const uint2 *chunks;
     const float4 *rec;
     float2 *raw;
+    float2 *raw_lo;  // NULL: plain FP32 sums across items
     int pitch, ntu, nu, nv;
 };
 // One grid of a batched finalize (Hermitian fold, shift by SUPP, GRDH2D normalisation).
 struct FinalizeDesc {
     const float2 *raw;
+    const float2 *raw_lo;
     float2 *out;
     int nu, nv, pitch, uorigin, vorigin, supp;
     float scale;
@@ -213,8 +223,9 @@ struct FftBatch {
     const float *scale[FFT_MAXB];
 };
 size_t grid_smem_bytes();
-int launch_grid_batch(sde_ctx *ctx, int psf, const BatchPlan *d_plans, const int64_t *d_item_start,
-                      int nplans, unsigned long long *d_counter, const float *cft, int nctas);
+int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
+                      const int64_t *d_item_start, int nplans, unsigned long long *d_counter,
+                      const float *cft, int nctas);
 int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, int n, int64_t max_cells);
 // grid -> image for n same-shape grids (inverse column pass, row c2r with grid correction
 // and scale 1/scales[i] when scales[i] != NULL); SDE_EINVAL if the shape has no batched form
@@ -248,6 +259,14 @@ int fftpwr2(int i);
 // Device helpers.
 __device__ __forceinline__ int nint_f(float x) { return (int)roundf(x); }   // half away
 __device__ __forceinline__ int nint_d(double x) { return (int)round(x); }
+
+// TwoSum (Knuth): the rounding error of fl(a + b), exactly, in round-to-nearest
+__device__ __forceinline__ float two_sum_err(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float ap = __fsub_rn(s, bp);
+    return __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
 
 __device__ __forceinline__ void red_add_f2(float2 *addr, float2 v) {
     asm volatile("red.relaxed.gpu.global.add.v2.f32 [%0], {%1, %2};" ::"l"(addr), "f"(v.x),

@@ -81,11 +81,11 @@ __device__ __forceinline__ Taps read_taps(const float *tg, int q, uint32_t g) {
 // entry; tap table filled), then the touched cells into the raw grid.  Reading the tile
 // back zeroes it, so the next item of a persistent CTA starts from a clean tile once the
 // caller's barrier has passed.
-template <bool PSF>
+template <bool PSF, bool COMP>
 __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__restrict__ chunks,
                                           const float4 *__restrict__ rec, const float *tab,
-                                          float *tre, float *tim, float2 *raw, int pitch,
-                                          int ntu, int nu, int nv) {
+                                          float *tre, float *tim, float2 *raw, float2 *raw_lo,
+                                          int pitch, int ntu, int nu, int nv) {
     const int q = threadIdx.x & (GLANES - 1);
     const int grp = threadIdx.x / GLANES;
     const float *tg = tab + (grp & (TAP_COPIES - 1)) * TAP_ROW;  // this group's copy
@@ -150,24 +150,54 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
     }
     __syncthreads();
     const int tu = it.tile % ntu, tv = it.tile / ntu;
-    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
-        const float2 val = make_float2(tre[k], tim[k]);
-        if (val.x == 0.f && val.y == 0.f) continue;
-        tre[k] = 0.f;
-        tim[k] = 0.f;
-        const int r = k / STILE, cc = k - r * STILE;
-        const int gv0 = tv * TILE + r - SUPP, gu0 = tu * TILE + cc - SUPP;  // 0-based raw
-        if (gv0 < 0 || gv0 >= nv || gu0 < 0 || gu0 >= nu) continue;
-        red_add_f2(&raw[(int64_t)gv0 * pitch + gu0], val);
+    // flush FLUSH_B cells per thread at a time, so that the compensated path keeps FLUSH_B
+    // returning atomics in flight instead of waiting on each
+    constexpr int FLUSH_B = 4;
+    for (int k0 = threadIdx.x; k0 < STILE * STILE; k0 += FLUSH_B * GRID_THREADS) {
+        float2 val[FLUSH_B];
+        int64_t gi[FLUSH_B];
+#pragma unroll
+        for (int j = 0; j < FLUSH_B; j++) {
+            const int k = k0 + j * GRID_THREADS;
+            gi[j] = -1;
+            val[j] = make_float2(0.f, 0.f);
+            if (k >= STILE * STILE) continue;
+            val[j] = make_float2(tre[k], tim[k]);
+            if (val[j].x == 0.f && val[j].y == 0.f) continue;
+            tre[k] = 0.f;
+            tim[k] = 0.f;
+            const int r = k / STILE, cc = k - r * STILE;
+            const int gv0 = tv * TILE + r - SUPP, gu0 = tu * TILE + cc - SUPP;  // 0-based raw
+            if (gv0 < 0 || gv0 >= nv || gu0 < 0 || gu0 >= nu) continue;
+            gi[j] = (int64_t)gv0 * pitch + gu0;
+        }
+        if (COMP && it.dense) {
+            // compensated sum across items (dense tiles, many items per cell): the atomic
+            // returns the value it added to, so the rounding error of the stored sum is
+            // exact (TwoSum) and goes to raw_lo
+            float2 old[FLUSH_B];
+#pragma unroll
+            for (int j = 0; j < FLUSH_B; j++)
+                if (gi[j] >= 0) old[j] = atomicAdd(&raw[gi[j]], val[j]);
+#pragma unroll
+            for (int j = 0; j < FLUSH_B; j++)
+                if (gi[j] >= 0)
+                    red_add_f2(&raw_lo[gi[j]], make_float2(two_sum_err(old[j].x, val[j].x),
+                                                           two_sum_err(old[j].y, val[j].y)));
+        } else {
+#pragma unroll
+            for (int j = 0; j < FLUSH_B; j++)
+                if (gi[j] >= 0) red_add_f2(&raw[gi[j]], val[j]);
+        }
     }
 }
 
 // One CTA per work item of one plan.
-template <bool PSF>
+template <bool PSF, bool COMP>
 __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
     k_grid(const WorkItem *__restrict__ items, const uint2 *__restrict__ chunks,
            const float4 *__restrict__ rec, const float *__restrict__ cft_g, float2 *raw,
-           int pitch, int ntu, int nu, int nv) {
+           float2 *raw_lo, int pitch, int ntu, int nu, int nv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *tre = reinterpret_cast<float *>(smem_raw);
     float *tim = tre + STILE * STILE;
@@ -184,14 +214,14 @@ __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
     }
     fill_tap_table(cft_g, tab, GRID_THREADS);
     __syncthreads();
-    grid_item<PSF>(it, chunks, rec, tab, tre, tim, raw, pitch, ntu, nu, nv);
+    grid_item<PSF, COMP>(it, chunks, rec, tab, tre, tim, raw, raw_lo, pitch, ntu, nu, nv);
 }
 
 // Persistent gridding of many plans (a mosaic's pointings, a batch of served jobs): each
 // CTA fills its tap table once, then takes work items from the combined list of all plans
 // (item_start[p] = first combined index of plan p) through an atomic counter until the
 // list is exhausted.  One launch grids every plan.
-template <bool PSF>
+template <bool PSF, bool COMP>
 __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
     k_grid_batch(const BatchPlan *__restrict__ plans, const int64_t *__restrict__ item_start,
                  int nplans, unsigned long long *counter, const float *__restrict__ cft_g) {
@@ -225,7 +255,8 @@ __global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
             prefetch_l2_range(P.chunks, it.cbeg, it.cend, 8);
             prefetch_l2_range(P.rec, it.vbeg, it.vend, 16);
         }
-        grid_item<PSF>(it, P.chunks, P.rec, tab, tre, tim, P.raw, P.pitch, P.ntu, P.nu, P.nv);
+        grid_item<PSF, COMP>(it, P.chunks, P.rec, tab, tre, tim, P.raw, P.raw_lo, P.pitch, P.ntu,
+                             P.nu, P.nv);
         __syncthreads();
     }
 }
@@ -297,23 +328,35 @@ __global__ void k_build_cft(const float *cf, float *cft) {
 // [nv][pitch] complex; out(u,v) = scale * R'(u+SUPP, v) for u <= NU-SUPP, else 0, where R'
 // adds conj(R(UC-k, 2VC-v)) into columns UC+k, k = 0..SUPP, UC = UORIGIN+SUPP.
 // One cell of the final GRDH2D grid from the raw accumulation (index idx of [nv][pitch]).
-__device__ __forceinline__ float2 finalize_cell(const float2 *__restrict__ raw, int64_t idx, int nu,
-                                                int nv, int pitch, int uorigin, int vorigin,
-                                                int supp, float scale) {
+__device__ __forceinline__ float2 raw_at(const float2 *__restrict__ raw,
+                                         const float2 *__restrict__ raw_lo, int64_t i) {
+    float2 r = raw[i];
+    if (raw_lo) {
+        const float2 e = raw_lo[i];
+        r.x = r.x + e.x;
+        r.y = r.y + e.y;
+    }
+    return r;
+}
+
+__device__ __forceinline__ float2 finalize_cell(const float2 *__restrict__ raw,
+                                                const float2 *__restrict__ raw_lo, int64_t idx,
+                                                int nu, int nv, int pitch, int uorigin,
+                                                int vorigin, int supp, float scale) {
     const int v0 = (int)(idx / pitch), u0 = (int)(idx - (int64_t)v0 * pitch);
     if (u0 >= nu) return make_float2(0.f, 0.f);
     const int u1 = u0 + 1, v1 = v0 + 1;  // 1-based
     float2 r = make_float2(0.f, 0.f);
     if (u1 <= nu - supp) {
         const int U = u1 + supp;            // raw column (1-based)
-        r = raw[(int64_t)v0 * pitch + (U - 1)];
+        r = raw_at(raw, raw_lo, (int64_t)v0 * pitch + (U - 1));
         const int UC = uorigin + supp, VC = vorigin;
         const int k = U - UC;
         if (k >= 0 && k <= supp) {
             const int dvv = v1 - VC;
             const int vm = 2 * VC - v1;
             if (dvv >= -(nv / 2) + 1 && dvv <= nv / 2 - 1 && vm >= 1 && vm <= nv) {
-                const float2 m = raw[(int64_t)(vm - 1) * pitch + (UC - k - 1)];
+                const float2 m = raw_at(raw, raw_lo, (int64_t)(vm - 1) * pitch + (UC - k - 1));
                 r.x = r.x + m.x;
                 r.y = r.y - m.y;
             }
@@ -324,11 +367,12 @@ __device__ __forceinline__ float2 finalize_cell(const float2 *__restrict__ raw, 
     return r;
 }
 
-__global__ void k_finalize(const float2 *__restrict__ raw, float2 *__restrict__ out, int nu,
-                           int nv, int pitch, int uorigin, int vorigin, int supp, float scale) {
+__global__ void k_finalize(const float2 *__restrict__ raw, const float2 *__restrict__ raw_lo,
+                           float2 *__restrict__ out, int nu, int nv, int pitch, int uorigin,
+                           int vorigin, int supp, float scale) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)nv * pitch) return;
-    out[idx] = finalize_cell(raw, idx, nu, nv, pitch, uorigin, vorigin, supp, scale);
+    out[idx] = finalize_cell(raw, raw_lo, idx, nu, nv, pitch, uorigin, vorigin, supp, scale);
 }
 
 // finalize of many grids: blockIdx.y picks the grid, blocks past its size return
@@ -336,7 +380,8 @@ __global__ void k_finalize_batch(const FinalizeDesc *__restrict__ d) {
     const FinalizeDesc f = d[blockIdx.y];
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)f.nv * f.pitch) return;
-    f.out[idx] = finalize_cell(f.raw, idx, f.nu, f.nv, f.pitch, f.uorigin, f.vorigin, f.supp, f.scale);
+    f.out[idx] = finalize_cell(f.raw, f.raw_lo, idx, f.nu, f.nv, f.pitch, f.uorigin, f.vorigin,
+                               f.supp, f.scale);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -727,11 +772,11 @@ int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt) {
     return SDE_OK;
 }
 
-int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, float2 *out, int nu, int nv, int pitch,
-                        int uorigin, int vorigin, int supp, float scale) {
+int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, const float2 *raw_lo, float2 *out, int nu,
+                        int nv, int pitch, int uorigin, int vorigin, int supp, float scale) {
     int64_t n = (int64_t)nv * pitch;
     KTimer kt(ctx, "finalize");
-    k_finalize<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(raw, out, nu, nv, pitch, uorigin,
+    k_finalize<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(raw, raw_lo, out, nu, nv, pitch, uorigin,
                                                           vorigin, supp, scale);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
@@ -739,23 +784,31 @@ int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, float2 *out, int nu, in
 
 size_t grid_smem_bytes() { return grid_smem(); }
 
-int launch_grid_batch(sde_ctx *ctx, int psf, const BatchPlan *d_plans, const int64_t *d_item_start,
-                      int nplans, unsigned long long *d_counter, const float *cft, int nctas) {
+int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
+                      const int64_t *d_item_start, int nplans, unsigned long long *d_counter,
+                      const float *cft, int nctas) {
     static bool attr = false;
     if (!attr) {
-        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid_batch<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)grid_smem()));
-        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid_batch<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)grid_smem()));
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid_batch<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)grid_smem()));
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid_batch<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)grid_smem()));
         attr = true;
     }
     KTimer kt(ctx, psf ? "grid_batch_psf" : "grid_batch");
-    if (psf)
-        k_grid_batch<true><<<nctas, GRID_THREADS, grid_smem(), ctx->stream>>>(d_plans, d_item_start, nplans,
-                                                                             d_counter, cft);
+    const dim3 g((unsigned)nctas), b(GRID_THREADS);
+    if (psf && comp)
+        k_grid_batch<true, true><<<g, b, grid_smem(), ctx->stream>>>(d_plans, d_item_start, nplans, d_counter, cft);
+    else if (psf)
+        k_grid_batch<true, false><<<g, b, grid_smem(), ctx->stream>>>(d_plans, d_item_start, nplans, d_counter, cft);
+    else if (comp)
+        k_grid_batch<false, true><<<g, b, grid_smem(), ctx->stream>>>(d_plans, d_item_start, nplans, d_counter, cft);
     else
-        k_grid_batch<false><<<nctas, GRID_THREADS, grid_smem(), ctx->stream>>>(d_plans, d_item_start, nplans,
-                                                                              d_counter, cft);
+        k_grid_batch<false, false><<<g, b, grid_smem(), ctx->stream>>>(d_plans, d_item_start, nplans, d_counter, cft);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
@@ -768,26 +821,37 @@ int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, int n, int64
     return SDE_OK;
 }
 
-int plan_grid_raw(sde_plan *pl, int what, float2 *raw) {
+int plan_grid_raw(sde_plan *pl, int what, float2 *raw, float2 *raw_lo) {
     sde_ctx *ctx = pl->ctx;
     const int nu = pl->spec.nu, nv = pl->spec.nv;
     SDE_CUDA_TRY(cudaMemsetAsync(raw, 0, sizeof(float2) * (size_t)nv * pl->pitch, ctx->stream));
+    if (raw_lo)
+        SDE_CUDA_TRY(cudaMemsetAsync(raw_lo, 0, sizeof(float2) * (size_t)nv * pl->pitch, ctx->stream));
     if (pl->nitems == 0) return SDE_OK;
     static bool attr = false;
     if (!attr) {
-        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)grid_smem()));
-        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)grid_smem()));
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)grid_smem()));
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_grid<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)grid_smem()));
         attr = true;
     }
     KTimer kt(ctx, what == SDE_GRID_PSF ? "grid_psf" : "grid");
-    if (what == SDE_GRID_PSF)
-        k_grid<true><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
-            pl->items, pl->chunks, pl->rec, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+    const dim3 g((unsigned)pl->nitems), b(GRID_THREADS);
+    const size_t sm = grid_smem();
+    cudaStream_t st = ctx->stream;
+    if (what == SDE_GRID_PSF && raw_lo)
+        k_grid<true, true><<<g, b, sm, st>>>(pl->items, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
+    else if (what == SDE_GRID_PSF)
+        k_grid<true, false><<<g, b, sm, st>>>(pl->items, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
+    else if (raw_lo)
+        k_grid<false, true><<<g, b, sm, st>>>(pl->items, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
     else
-        k_grid<false><<<(unsigned)pl->nitems, GRID_THREADS, grid_smem(), ctx->stream>>>(
-            pl->items, pl->chunks, pl->rec, pl->cft, raw, pl->pitch, pl->ntu, nu, nv);
+        k_grid<false, false><<<g, b, sm, st>>>(pl->items, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }

@@ -246,6 +246,7 @@ __global__ void k_chunk_write(const uint32_t *__restrict__ keys, const unsigned 
         wi.cbeg = wi.cend = 0;
         wi.vbeg = (int32_t)q;
         wi.vend = 0;
+        wi.dense = 0;
         items[it] = wi;
     }
     if (!chead[q]) return;
@@ -288,6 +289,27 @@ __global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t 
     uint32_t it = (uint32_t)(ckey[c] >> shift_item);
     if (c == 0 || (uint32_t)(ckey[c - 1] >> shift_item) != it) items[it].cbeg = (int32_t)c;
     if (c == nchunks - 1 || (uint32_t)(ckey[c + 1] >> shift_item) != it) items[it].cend = (int32_t)(c + 1);
+}
+
+// dense flag of each work item: its tile's items (contiguous, sorted by tile) together
+// hold >= DENSE_TILE_VIS visibilities
+__global__ void k_item_dense(WorkItem *items, int64_t nitems) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nitems) return;
+    const int32_t tile = items[t].tile;
+    int64_t lo = 0, hi = t;  // first item of the tile
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) / 2;
+        if (items[mid].tile < tile) lo = mid + 1; else hi = mid;
+    }
+    const int64_t first = lo;
+    lo = t;
+    hi = nitems;  // one past the last item of the tile
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) / 2;
+        if (items[mid].tile <= tile) lo = mid + 1; else hi = mid;
+    }
+    items[t].dense = (int64_t)items[lo - 1].vend - items[first].vbeg >= DENSE_TILE_VIS;
 }
 
 __global__ void k_item_vend(WorkItem *items, int64_t nitems, int64_t nvalid) {
@@ -543,6 +565,8 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
                                                             pl->items);
             PL_CUDA(cudaGetLastError());
             k_item_vend<<<ceil_div(nitems, T), T, 0, st>>>(pl->items, nitems, nvalid);
+            PL_CUDA(cudaGetLastError());
+            k_item_dense<<<ceil_div(nitems, T), T, 0, st>>>(pl->items, nitems);
             PL_CUDA(cudaGetLastError());
         }
         // gridding function: the context's 'SF' table
