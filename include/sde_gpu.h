@@ -47,6 +47,14 @@ int sde_version(void);
  * Layer 1: Fortran-77 drop-in entry points (gfortran symbol names).
  * ====================================================================================== */
 
+/* The drop-ins keep the plan of their last GRDH2D/GRDDEH2D call together with a device copy
+ * of the U, V, W, WT it was built from; a call whose U, V, W, WT (compared bitwise on the
+ * device after the upload), grid geometry and gridding function match reuses it and only
+ * loads the new VIS.  No counterpart in the reference.  Statistics, and a call that frees
+ * the cached plan and inputs: */
+int sde_shim_cache_stats(int64_t *hits, int64_t *misses);
+int sde_shim_cache_clear(void);
+
 /* Replaces GRDH2D (source/grd/grdh2d.f:7-9), called by VISGRID (vis/visgrid.f:329). */
 void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
              float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,

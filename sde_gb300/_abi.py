@@ -103,6 +103,8 @@ SIGNATURES = [
     ("sde_batch_graph_nodes", I, [P]),
     ("sde_batch_image", I, [P, I, I, C.POINTER(P)]),
     ("sde_batch_read", I, [P, I, I, P, I64]),
+    ("sde_shim_cache_stats", I, [C.POINTER(I64), C.POINTER(I64)]),
+    ("sde_shim_cache_clear", I, []),
     # Fortran-77 drop-in layer (all arguments by reference)
     ("grdh2d_", None, [P] * 24),
     ("grddeh2d_", None, [P] * 22),

@@ -523,6 +523,132 @@ extern "C" void grdccf_(char *ccfcode, float *ccf, int *ccflen, size_t len) {
     }
 }
 
+// ---- plan cache of the drop-ins ---------------------------------------------------------
+// VISGRID and VISDEGRI call GRDH2D / GRDDEH2D every major cycle with the same U, V, W, WT and
+// new VIS.  The shim keeps the plan of its last call with a device copy of the U, V, W, WT it
+// was built from.  Every call still uploads its arrays; when they are bitwise identical to
+// the cached ones (compared on the device) and the grid geometry and the caller's gridding
+// function are the same, only the visibilities are replaced (the frame transform of
+// sde_plan_set_vis) instead of sorting again.  Any difference rebuilds the plan.
+struct ShimCache {
+    sde_plan *pl = nullptr;
+    sde_gridspec spec{};
+    int64_t nvis = -1;
+    uint64_t cf_hash = 0;
+    float *inputs = nullptr;  // u | v | w | wt of the cached plan (device)
+    size_t cap = 0;           // bytes of inputs
+    int64_t hits = 0, misses = 0;
+};
+static ShimCache g_pc;
+
+__global__ void k_words_differ(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b,
+                               int64_t n, int *flag) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (a[i] != b[i]) {
+            *flag = 1;
+            return;
+        }
+}
+
+static uint64_t hash_floats(const float *x, size_t n) {
+    uint64_t h = 1469598103934665603ull;  // FNV-1a over the bit patterns
+    const unsigned char *b = reinterpret_cast<const unsigned char *>(x);
+    for (size_t i = 0; i < n * sizeof(float); i++) h = (h ^ b[i]) * 1099511628211ull;
+    return h;
+}
+
+static void shim_cache_drop() {
+    if (g_pc.pl) sde_plan_destroy(g_pc.pl);
+    g_pc.pl = nullptr;
+    g_pc.nvis = -1;
+}
+
+// The plan for this call (owned by the cache: callers do not destroy it).  vis may be NULL
+// (GRDDEH2D: VIS is output only).
+static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const float *u,
+                     const float *v, const float *w, const float *vis, const float *wt,
+                     const float *cf, sde_plan **out) {
+    cudaStream_t st = ctx->stream;
+    float *in = nullptr, *dvis = nullptr;
+    const size_t nb = sizeof(float) * (size_t)(n > 0 ? n : 1);
+    SDE_TRY(ctx_scratch(ctx, "shim_in", 4 * nb, (void **)&in));
+    SDE_TRY(ctx_scratch(ctx, "shim_vis", 2 * nb, (void **)&dvis));
+    if (n > 0) {
+        SDE_CUDA_TRY(cudaMemcpyAsync(in, u, nb, cudaMemcpyHostToDevice, st));
+        SDE_CUDA_TRY(cudaMemcpyAsync(in + n, v, nb, cudaMemcpyHostToDevice, st));
+        SDE_CUDA_TRY(cudaMemcpyAsync(in + 2 * n, w, nb, cudaMemcpyHostToDevice, st));
+        SDE_CUDA_TRY(cudaMemcpyAsync(in + 3 * n, wt, nb, cudaMemcpyHostToDevice, st));
+        if (vis) SDE_CUDA_TRY(cudaMemcpyAsync(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
+        else SDE_CUDA_TRY(cudaMemsetAsync(dvis, 0, 2 * nb, st));
+    }
+    const uint64_t h = hash_floats(cf, 2 * (SUPP + 1) * OSAMP + 1);
+    if (g_pc.pl && g_pc.nvis == n && g_pc.cf_hash == h && memcmp(&g_pc.spec, &sp, sizeof sp) == 0) {
+        int *flag = nullptr;
+        SDE_TRY(ctx_scratch(ctx, "shim_flag", sizeof(int), (void **)&flag));
+        SDE_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
+        if (n > 0) {
+            k_words_differ<<<ctx->num_sms * 4, 256, 0, st>>>(reinterpret_cast<const uint32_t *>(in),
+                                                              reinterpret_cast<const uint32_t *>(g_pc.inputs),
+                                                              4 * n, flag);
+            SDE_CHECK_LAUNCH();
+        }
+        int hf = 1;
+        SDE_CUDA_TRY(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SDE_CUDA_TRY(cudaStreamSynchronize(st));
+        if (!hf) {
+            if (n > 0) SDE_TRY(sde_plan_set_vis(g_pc.pl, dvis, SDE_DEVICE));
+            g_pc.hits++;
+            *out = g_pc.pl;
+            return SDE_OK;
+        }
+    }
+    shim_cache_drop();
+    sde_plan *pl = nullptr;
+    SDE_TRY(sde_plan_create(ctx, &sp, n, in, in + n, in + 2 * n, dvis, in + 3 * n, SDE_DEVICE, &pl));
+    int rc = plan_use_table(pl, cf);
+    if (rc == SDE_OK && 4 * nb > g_pc.cap) {
+        if (g_pc.inputs) ctx_free(ctx, g_pc.inputs, g_pc.cap);
+        g_pc.inputs = nullptr;
+        g_pc.cap = 0;
+        rc = ctx_alloc(ctx, (void **)&g_pc.inputs, 4 * nb);
+        if (rc == SDE_OK) g_pc.cap = 4 * nb;
+    }
+    if (rc == SDE_OK && n > 0) {
+        cudaError_t e = cudaMemcpyAsync(g_pc.inputs, in, 4 * nb, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) {
+            sde_set_error("%s", cudaGetErrorString(e));
+            rc = SDE_ECUDA;
+        }
+    }
+    if (rc != SDE_OK) {
+        sde_plan_destroy(pl);
+        return rc;
+    }
+    g_pc.pl = pl;
+    g_pc.spec = sp;
+    g_pc.nvis = n;
+    g_pc.cf_hash = h;
+    g_pc.misses++;
+    *out = pl;
+    return SDE_OK;
+}
+
+extern "C" int sde_shim_cache_stats(int64_t *hits, int64_t *misses) {
+    if (hits) *hits = g_pc.hits;
+    if (misses) *misses = g_pc.misses;
+    return SDE_OK;
+}
+
+extern "C" int sde_shim_cache_clear(void) {
+    std::lock_guard<std::mutex> lk(g_shim_mu);
+    shim_cache_drop();
+    if (g_pc.inputs && g_shim_ctx) ctx_free(g_shim_ctx, g_pc.inputs, g_pc.cap);
+    g_pc.inputs = nullptr;
+    g_pc.cap = 0;
+    return SDE_OK;
+}
+
 extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis,
                         float *uscale, float *uoffset, float *vscale, float *voffset, int *uorigin,
                         int *vorigin, float *gvis, int *psf, int *nu, int *nv, float *gridfnu,
@@ -540,8 +666,7 @@ extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int
     sde_gridspec sp;
     fill_spec(&sp, *nu, *nv, *uscale, *uoffset, *vscale, *voffset, *uorigin, *vorigin, shift);
     sde_plan *pl = nullptr;
-    int rc = sde_plan_create(ctx, &sp, *nvis, u, v, w, vis, wt, SDE_HOST, &pl);
-    if (rc == SDE_OK) rc = plan_use_table(pl, gridfnu);
+    int rc = shim_plan(ctx, sp, *nvis, u, v, w, vis, wt, gridfnu, &pl);
     float2 *dg = nullptr;
     const int pitch = sde_grid_pitch(*nu);
     if (rc == SDE_OK) rc = ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * *nv, (void **)&dg);
@@ -557,7 +682,6 @@ extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int
         }
         *sumwt = sw;
     }
-    sde_plan_destroy(pl);
     if (rc == SDE_ENOWEIGHT)
         report("Bad argument", R, "No weight!");
     else if (rc != SDE_OK)
@@ -581,8 +705,7 @@ extern "C" void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, i
     sde_gridspec sp;
     fill_spec(&sp, *nu, *nv, *uscale, *uoffset, *vscale, *voffset, *uorigin, *vorigin, shift);
     sde_plan *pl = nullptr;
-    int rc = sde_plan_create(ctx, &sp, *nvis, u, v, w, vis, wt, SDE_HOST, &pl);
-    if (rc == SDE_OK) rc = plan_use_table(pl, intfnu);
+    int rc = shim_plan(ctx, sp, *nvis, u, v, w, nullptr, wt, intfnu, &pl);
     float2 *dg = nullptr;
     const int pitch = sde_grid_pitch(*nu);
     if (rc == SDE_OK) rc = ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * *nv, (void **)&dg);
@@ -596,7 +719,6 @@ extern "C" void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, i
     }
     int64_t nbad = 0;
     if (rc == SDE_OK) rc = sde_plan_degrid(pl, (const float *)dg, pitch, vis, wt, SDE_HOST, &nbad);
-    sde_plan_destroy(pl);
     if (rc != SDE_OK) {
         report_rc(rc, R);
         return;

@@ -1,0 +1,205 @@
+"""The Fortran-77 drop-in entry points, called through the C ABI exactly as SDE's VISGRID,
+VISDEGRI, GRDUWT/GRDRUWT, ARRFFTR, IMGGRIDC and IMGCLEAN call them (every argument by
+reference, host arrays), against the oracle's restatement of the same routines.
+
+Bars: weight counts bit-exact; grids 1e-5 of the grid peak; degridded visibilities 1e-5 of
+the largest with identical WT signs; FFTs 1e-5 of the peak (images inside the CRDNHALF
+window); CLEAN components identical.  The plan cache of GRDH2D/GRDDEH2D must give the same
+results as a fresh plan, and rebuild when any input changes.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+P = C.c_void_p
+I = lambda x: C.byref(C.c_int(int(x)))
+F = lambda x: C.byref(C.c_float(float(x)))
+
+
+def _p(a):
+    return a.ctypes.data_as(P)
+
+
+@pytest.fixture(scope="module")
+def L():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from sde_gb300 import _abi
+    lib = _abi.lib()
+    _abi.sysi().error = 0
+    return lib
+
+
+@pytest.fixture(scope="module")
+def case(orc, obs_small):
+    o = obs_small
+    p = orc.params(o["imsize"], o["cell"], fov=1.0, rmode="NONE", vdec=o["vdec"])
+    g = orc.geom(p)
+    cf, _, _ = orc.grdcf()
+    return o, g, cf
+
+
+def _grdh2d(L, o, g, cf, psf=False, u=None):
+    from sde_gb300 import _abi
+    vis = np.ascontiguousarray(o["vis"], np.complex64)
+    wt = np.ascontiguousarray(o["wt"], np.float32).copy()
+    uu = np.ascontiguousarray(o["u"] if u is None else u, np.float32)
+    gvis = np.zeros((g.nv, g.nu), np.complex64)
+    sw = C.c_float()
+    shift = np.ascontiguousarray(list(g.shift), np.float64)
+    L.grdh2d_(_p(vis), _p(wt), _p(uu), _p(o["v"]), _p(o["w"]), I(len(wt)), F(g.uscale), F(0),
+              F(g.vscale), F(0), I(g.uorigin), I(g.vorigin), _p(gvis), I(int(psf)), I(g.nu),
+              I(g.nv), _p(cf), I(3), I(128), _p(cf), I(3), I(128), _p(shift), C.byref(sw))
+    assert _abi.sysi().error == 0
+    return gvis, sw.value
+
+
+def _stats(L):
+    h, m = C.c_int64(), C.c_int64()
+    L.sde_shim_cache_stats(C.byref(h), C.byref(m))
+    return h.value, m.value
+
+
+def test_grdh2d_and_its_plan_cache(L, orc, case):
+    o, g, cf = case
+    shift = np.asarray(list(g.shift))
+    rc, ref, rsw, _ = orc.grdh2d(o["vis"], o["wt"], o["u"], o["v"], o["w"], g.uscale, g.vscale,
+                                 g.uorigin, g.vorigin, g.nu, g.nv, shift, cf=cf)
+    L.sde_shim_cache_clear()
+    h0, m0 = _stats(L)
+    a, sw = _grdh2d(L, o, g, cf)
+    b, _ = _grdh2d(L, o, g, cf)           # same U, V, W, WT: the cached plan
+    h1, m1 = _stats(L)
+    assert (h1 - h0, m1 - m0) == (1, 1)
+    pk = np.abs(ref).max()
+    assert np.abs(a - ref).max() / pk < 1e-5
+    assert np.abs(b - ref).max() / pk < 1e-5
+    assert abs(sw - rsw) <= 1e-6 * abs(rsw)
+    # one U changed: the cache must notice and rebuild
+    u2 = np.array(o["u"], np.float32)
+    u2[len(u2) // 3] *= np.float32(0.97)
+    rc, ref2, _, _ = orc.grdh2d(o["vis"], o["wt"], u2, o["v"], o["w"], g.uscale, g.vscale,
+                                g.uorigin, g.vorigin, g.nu, g.nv, shift, cf=cf)
+    c, _ = _grdh2d(L, o, g, cf, u=u2)
+    h2, m2 = _stats(L)
+    assert m2 - m1 == 1
+    assert np.abs(c - ref2).max() / np.abs(ref2).max() < 1e-5
+    # PSF through the same entry point
+    rc, rpsf, _, _ = orc.grdh2d(o["vis"], o["wt"], o["u"], o["v"], o["w"], g.uscale, g.vscale,
+                                g.uorigin, g.vorigin, g.nu, g.nv, shift, psf=True, cf=cf)
+    d, _ = _grdh2d(L, o, g, cf, psf=True)
+    assert np.abs(d - rpsf).max() / np.abs(rpsf).max() < 1e-5
+
+
+def test_grddeh2d(L, orc, case):
+    from sde_gb300 import _abi
+    o, g, cf = case
+    shift = np.ascontiguousarray(list(g.shift), np.float64)
+    rng = np.random.default_rng(3)
+    gvis = (rng.normal(size=(g.nv, g.nu)) + 1j * rng.normal(size=(g.nv, g.nu))).astype(np.complex64)
+    rvis, rwt, rnb = orc.grddeh2d(np.zeros(len(o["wt"]), np.complex64), o["wt"], o["u"], o["v"],
+                                  o["w"], g.uscale, g.vscale, g.uorigin, g.vorigin, gvis, shift,
+                                  cf=cf)
+    for _ in range(2):  # second call: the cached plan
+        vis = np.zeros(len(o["wt"]), np.complex64)
+        wt = np.ascontiguousarray(o["wt"], np.float32).copy()
+        L.grddeh2d_(_p(vis), _p(wt), _p(o["u"]), _p(o["v"]), _p(o["w"]), I(len(wt)), F(g.uscale),
+                    F(0), F(g.vscale), F(0), I(g.uorigin), I(g.vorigin), _p(gvis), I(g.nu),
+                    I(g.nv), _p(cf), I(3), I(128), _p(cf), I(3), I(128), _p(shift))
+        assert _abi.sysi().error == 0
+        assert np.abs(vis - rvis).max() / np.abs(rvis).max() < 1e-5
+        assert np.array_equal(np.sign(wt), np.sign(rwt))
+
+
+def test_grduwt2d_and_grdruw2d_bit_exact(L, orc, case):
+    from sde_gb300.imaging import Geom
+    o, g0, cf = case
+    g = Geom(o["imsize"], o["cell"], vdec=o["vdec"])  # FOV/CDELT weighting scales in REAL
+    shift = np.ascontiguousarray(list(g.shift), np.float64)
+    n = len(o["wt"])
+    wt = np.ascontiguousarray(o["wt"], np.float32)
+    rnew, rgwt, _ = orc.grduwt2d(wt, o["u"], o["v"], o["w"], g.wuscale, g.wvscale, g.uorigin,
+                                 g.vorigin, g.nu, g.nv, shift)
+    newwt = np.zeros(n, np.float32)
+    gwt = np.zeros((g.nv, g.nu), np.float32)
+    L.grduwt2d_(_p(wt), _p(o["u"]), _p(o["v"]), _p(o["w"]), I(n), F(g.wuscale), F(0),
+                F(g.wvscale), F(0), I(g.uorigin), I(g.vorigin), _p(newwt), _p(gwt), I(g.nu),
+                I(g.nv), _p(shift))
+    assert np.array_equal(newwt.view(np.uint32), rnew.view(np.uint32))
+    assert np.array_equal(gwt.view(np.uint32), rgwt.view(np.uint32))
+    rc, rnew, rgwt, *_ = orc.grdruw2d(wt, o["u"], o["v"], o["w"], g.wuscale, g.wvscale,
+                                      g.uorigin, g.vorigin, g.nu, g.nv, shift, "NORM",
+                                      [0.5, 0.0, 0.0])
+    newwt = np.zeros(n, np.float32)
+    gwt = np.zeros((g.nv, g.nu), np.float32)
+    rob = np.array([0.5, 0.0, 0.0], np.float32)
+    L.grdruw2d_(_p(wt), _p(o["u"]), _p(o["v"]), _p(o["w"]), I(n), F(g.wuscale), F(0),
+                F(g.wvscale), F(0), I(g.uorigin), I(g.vorigin), _p(newwt), _p(gwt), I(g.nu),
+                I(g.nv), _p(shift), b"NORM", _p(rob), F(0.0), C.c_size_t(4))
+    assert np.array_equal(newwt.view(np.uint32), rnew.view(np.uint32))
+    assert np.array_equal(gwt.view(np.uint32), rgwt.view(np.uint32))
+
+
+def _window(n):
+    lo = n // 4 + 1
+    length = min(3 * n // 4 - 1 - lo + 1, n // 2 - 1)
+    return slice(lo - 1, lo - 1 + length)
+
+
+def test_fftr2d_both_directions_and_pixcor2d(L, orc, case):
+    o, g, cf = case
+    n, fnu, nv, nu = g.nx, g.fnu, g.nv, g.nu
+    rng = np.random.default_rng(8)
+    grid = (rng.normal(size=(nv, nu)) + 1j * rng.normal(size=(nv, nu))).astype(np.complex64)
+    rimg, _ = orc.fftr2d(n, n, fnu, nv, -1, xarray=grid)
+    img = np.zeros((n, n), np.float32)
+    x = grid.copy()
+    L.fftr2d_(_p(img), _p(x), None, None, None, I(n), I(n), I(fnu), I(nv), I(-1))
+    assert np.abs(img - rimg).max() / np.abs(rimg).max() < 1e-5
+    image = rng.normal(size=(n, n)).astype(np.float32)
+    _, rgrid = orc.fftr2d(n, n, fnu, nv, 1, rarray=image)
+    x = np.zeros((nv, nu), np.complex64)
+    L.fftr2d_(_p(image), _p(x), None, None, None, I(n), I(n), I(fnu), I(nv), I(1))
+    assert np.abs(x - rgrid).max() / np.abs(rgrid).max() < 1e-5
+    ccflen = 1 + fnu // 2
+    ccf = orc.grdccf(ccflen)
+    rcor = orc.pixcor2d(image, ccf, g.cenx, g.ceny)
+    out = np.zeros_like(image)
+    L.pixcor2d_(_p(image), I(n), I(n), _p(ccf), I(ccflen), b"CORRECT", _p(out), F(g.cenx),
+                F(g.ceny), C.c_size_t(7))
+    w = _window(n)
+    assert np.abs(out - rcor)[w, w].max() / np.abs(rcor[w, w]).max() < 1e-6
+
+
+def test_pix2drcl_and_pixisama_identical(L, orc):
+    rng = np.random.default_rng(4)
+    n = 64
+    yy, xx = np.mgrid[0:2 * n, 0:2 * n]
+    psf = np.exp(-((xx - n + 1) ** 2 + (yy - n + 1) ** 2) / 7.0).astype(np.float32)
+    drt = (0.01 * rng.standard_normal((n - 1, n - 1))).astype(np.float32)
+    for _ in range(4):
+        iy, ix = rng.integers(8, n - 9, 2)
+        drt += rng.uniform(0.2, 1.0) * psf[n - 1 - iy:2 * n - 2 - iy, n - 1 - ix:2 * n - 2 - ix]
+    box = np.ones_like(drt)
+    niter, gain = 150, 0.1
+    r = orc.pix2drcl(drt, psf, box, gain, niter)
+    cln = np.zeros_like(drt)
+    res = np.zeros_like(drt)
+    cflux = np.zeros(niter, np.float32)
+    cx = np.zeros(niter, np.int32)
+    cy = np.zeros(niter, np.int32)
+    ansub, maxres, tflux = C.c_int(), C.c_float(), C.c_float(0.0)
+    L.pix2drcl_(_p(drt), _p(psf), _p(box), I(n - 1), I(n - 1), I(2 * n), I(2 * n), F(gain),
+                I(niter), I(1), F(0.0), _p(cln), _p(res), C.byref(ansub), C.byref(maxres),
+                C.byref(tflux), _p(cflux), _p(cx), _p(cy))
+    assert ansub.value == r["ansub"]
+    k = r["ansub"] if r["ansub"] > 0 else niter
+    assert np.array_equal(cx[:k], r["cx"][:k]) and np.array_equal(cy[:k], r["cy"][:k])
+    assert np.array_equal(cflux[:k], r["cflux"][:k])
+    assert np.array_equal(res, r["res"]) and np.array_equal(cln, r["cln"])
+    a = rng.normal(size=1000).astype(np.float32)
+    assert L.pixisama_(I(a.size), _p(a), I(1)) == orc.pixisama(a)
