@@ -269,6 +269,33 @@ int sde_hogbom_noalloc(void *stream, const float *drt, const float *psf, const f
 
 /* Index (1-based) of the first strictly largest |a| (PIXISAMA) of a device array. */
 
+/* ---- One uvmap job in one call ----------------------------------------------------------
+ * The device work of task/uvmap.f for one job: optional weighting (rmode -1: keep WT, the
+ * natural weights; 0..4 as sde_weights, with the weighting scales wuscale/wvscale =
+ * FOV/CDELT), plan, PSF, PSF peak, dirty image divided by the peak (task/uvmap.f:212-491),
+ * from host (where = SDE_HOST) or device arrays to host or device images (out_where).  WT
+ * is not modified (the weighting works on a copy).  psf may be NULL; if given it receives
+ * the PSF divided by its peak.  Synchronises the context's stream before returning.
+ * No counterpart entry point in the reference (uvmap is a task, not a routine). */
+typedef struct {
+    sde_gridspec spec;
+    int nx, ny;
+    int rmode;
+    float robust[3];
+    float ds;
+    float wuscale, wvscale;
+    int out_where;
+} sde_uvmap_args;
+typedef struct {
+    float psf_peak;
+    float sumwt;
+    int64_t ngrid;  /* visibilities that gridded */
+    int64_t ndrop;  /* dropped by the weighting (off the weighting grid) */
+} sde_uvmap_result;
+int sde_uvmap(sde_ctx *ctx, const sde_uvmap_args *a, int64_t nvis, const float *u, const float *v,
+              const float *w, const float *vis, const float *wt, int where, float *dirty,
+              float *psf, sde_uvmap_result *res);
+
 /* ---- Batches of plans: a mosaic's pointings or a group of served jobs ------------------
  * No counterpart entry point in the reference: task/mosclean.f images its pointings one
  * after another and forms the linear mosaic (task/mosclean.f:413-432); a batch images all

@@ -40,6 +40,17 @@ class PlanOpts(C.Structure):
     _fields_ = [("item_max", C.c_int), ("chunk_max", C.c_int)]
 
 
+class UvmapArgs(C.Structure):
+    _fields_ = [("spec", GridSpec), ("nx", C.c_int), ("ny", C.c_int), ("rmode", C.c_int),
+                ("robust", C.c_float * 3), ("ds", C.c_float), ("wuscale", C.c_float),
+                ("wvscale", C.c_float), ("out_where", C.c_int)]
+
+
+class UvmapResult(C.Structure):
+    _fields_ = [("psf_peak", C.c_float), ("sumwt", C.c_float), ("ngrid", C.c_int64),
+                ("ndrop", C.c_int64)]
+
+
 class CleanResult(C.Structure):
     _fields_ = [("ansub", C.c_int), ("maxres", C.c_float), ("tflux", C.c_float)]
 
@@ -93,6 +104,8 @@ SIGNATURES = [
     ("sde_isamax", I, [P, P, I64, C.POINTER(I64)]),
     ("sde_hogbom_noalloc", I, [P, P, P, P, I, I, I, I, F, I, I, F, F, P, P, P, P, P, P,
                                C.POINTER(CleanResult)]),
+    ("sde_uvmap", I, [P, C.POINTER(UvmapArgs), I64, P, P, P, P, P, I, P, P,
+                      C.POINTER(UvmapResult)]),
     ("sde_batch_create", I, [P, I, P, P, P, C.POINTER(P)]),
     ("sde_batch_destroy", I, [P]),
     ("sde_batch_bytes", I64, [P]),

@@ -83,26 +83,30 @@ int fftpwr2(int i) {
 // context
 static void drain_events(sde_ctx *c);
 
+// Device memory is stream-ordered (cudaMallocAsync / cudaFreeAsync on the context's stream,
+// from the device's pool, which keeps freed memory for reuse): allocating and freeing never
+// synchronises the device, so contexts working on different streams (concurrent jobs) do not
+// stall one another.  Memory used on another stream is synchronised with the context's
+// stream first (the context, batch and table set-up paths do).
 int ctx_alloc(sde_ctx *ctx, void **p, size_t bytes) {
-    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, ctx->stream);
     if (e != cudaSuccess) {
         *p = nullptr;
-        sde_set_error("cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+        sde_set_error("cudaMallocAsync(%zu): %s", bytes, cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? SDE_ENOMEM : SDE_ECUDA;
     }
     return SDE_OK;
 }
 
 void ctx_free(sde_ctx *ctx, void *p, size_t bytes) {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, ctx->stream);
 }
 
 int ctx_scratch(sde_ctx *ctx, const char *name, size_t bytes, void **out) {
     DevBuf &b = ctx->scratch[name];
     if (b.bytes < bytes) {
         if (b.p) {
-            SDE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-            cudaFree(b.p);
+            ctx_free(ctx, b.p, b.bytes);  // stream-ordered: after the work that used it
             ctx->bytes -= (int64_t)b.bytes;
             b.p = nullptr;
             b.bytes = 0;
@@ -130,7 +134,9 @@ int ctx_twiddles(sde_ctx *ctx, int n, const float2 **out) {
     }
     float2 *d;
     SDE_TRY(ctx_alloc(ctx, (void **)&d, sizeof(float2) * (size_t)h));
-    SDE_CUDA_TRY(cudaMemcpy(d, t.data(), sizeof(float2) * (size_t)h, cudaMemcpyHostToDevice));
+    // pageable source: returns once the host data has been staged, so t may go away
+    SDE_CUDA_TRY(cudaMemcpyAsync(d, t.data(), sizeof(float2) * (size_t)h, cudaMemcpyHostToDevice,
+                                 ctx->stream));
     ctx->bytes += (int64_t)(sizeof(float2) * h);
     ctx->twiddles[n] = d;
     *out = d;
@@ -163,6 +169,15 @@ extern "C" int sde_ctx_create(sde_ctx **out, int device) {
     }
     c->own_stream = true;
     c->num_sms = prop.multiProcessorCount;
+    {
+        // the default pool keeps memory freed by cudaFreeAsync for reuse instead of
+        // returning it at every synchronisation
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
     if ((rc = ctx_alloc(c, (void **)&c->d_status, sizeof(int) * STATUS_COUNT)) ||
         (rc = ctx_alloc(c, (void **)&c->d_cf, sizeof(float) * CFLEN)) ||
         (rc = ctx_alloc(c, (void **)&c->d_cft, sizeof(float) * 129 * 8))) {
@@ -175,8 +190,8 @@ extern "C" int sde_ctx_create(sde_ctx **out, int device) {
     }
     float cf[CFLEN];
     sf_cf_table(cf);
-    cudaMemcpy(c->d_cf, cf, sizeof cf, cudaMemcpyHostToDevice);
-    cudaMemset(c->d_status, 0, sizeof(int) * STATUS_COUNT);
+    cudaMemcpyAsync(c->d_cf, cf, sizeof cf, cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(c->d_status, 0, sizeof(int) * STATUS_COUNT, c->stream);
     if ((rc = ctx_build_cft(c)) != SDE_OK || cudaStreamSynchronize(c->stream) != cudaSuccess) {
         sde_ctx_destroy(c);
         return rc ? rc : SDE_ECUDA;
@@ -190,12 +205,12 @@ extern "C" int sde_ctx_destroy(sde_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     drain_events(c);
-    for (auto &kv : c->scratch)
-        if (kv.second.p) cudaFree(kv.second.p);
-    for (auto &kv : c->twiddles) cudaFree(kv.second);
-    if (c->d_status) cudaFree(c->d_status);
-    if (c->d_cf) cudaFree(c->d_cf);
-    if (c->d_cft) cudaFree(c->d_cft);
+    for (auto &kv : c->scratch) ctx_free(c, kv.second.p, kv.second.bytes);
+    for (auto &kv : c->twiddles) ctx_free(c, kv.second, 0);
+    ctx_free(c, c->d_status, 0);
+    ctx_free(c, c->d_cf, 0);
+    ctx_free(c, c->d_cft, 0);
+    if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -204,10 +219,11 @@ extern "C" int sde_ctx_destroy(sde_ctx *c) {
 
 extern "C" int sde_ctx_sync(sde_ctx *c) {
     if (!c) return SDE_EINVAL;
+    SDE_CUDA_TRY(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int) * STATUS_COUNT,
+                                 cudaMemcpyDeviceToHost, c->stream));
     SDE_CUDA_TRY(cudaStreamSynchronize(c->stream));
-    SDE_CUDA_TRY(cudaMemcpy(c->h_status, c->d_status, sizeof(int) * STATUS_COUNT, cudaMemcpyDeviceToHost));
     if (c->h_status[STATUS_TIMEOUT]) {
-        cudaMemset(c->d_status, 0, sizeof(int) * STATUS_COUNT);
+        cudaMemsetAsync(c->d_status, 0, sizeof(int) * STATUS_COUNT, c->stream);
         sde_set_error("a bounded device wait timed out");
         return SDE_ETIMEDOUT;
     }

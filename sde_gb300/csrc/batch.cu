@@ -382,7 +382,9 @@ extern "C" int sde_batch_set_mosaic(sde_batch *b, int mnx, int mny, const int *c
     b->mnx = mnx;
     b->mny = mny;
     b->clip = clip;
-    SDE_CUDA_TRY(cudaMemcpy(b->d_pts, h.data(), sizeof(MosaicPointing) * b->n, cudaMemcpyHostToDevice));
+    SDE_CUDA_TRY(cudaMemcpyAsync(b->d_pts, h.data(), sizeof(MosaicPointing) * b->n,
+                                 cudaMemcpyHostToDevice, b->ctx->stream));
+    SDE_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
     batch_drop_graph(b);  // the captured sequence changes
     return SDE_OK;
 }

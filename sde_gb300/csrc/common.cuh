@@ -229,6 +229,7 @@ int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
 int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, int n, int64_t max_cells);
 // grid -> image for n same-shape grids (inverse column pass, row c2r with grid correction
 // and scale 1/scales[i] when scales[i] != NULL); SDE_EINVAL if the shape has no batched form
+int check_fft_shape(int nx, int ny, int fnu, int nv);  // SDE_EINVAL + message if unsupported
 int fft_images_from_grids(sde_ctx *ctx, int n, float2 *const *grids, float *const *images,
                           const float *const *scales, int pitch, int nx, int ny, int fnu, int nv,
                           int correct);

@@ -407,7 +407,7 @@ int corr_params(sde_ctx *ctx, int nx, int ny, CorrParams *cp) {
             h[(size_t)ccflen + ix - 1] = h[(size_t)abs((int)lroundf(scalex * ((float)ix - cenx)))];
         for (int iy = 1; iy <= ny; iy++)
             h[(size_t)ccflen + nx + iy - 1] = h[(size_t)abs((int)lroundf(scaley * ((float)iy - ceny)))];
-        SDE_CUDA_TRY(cudaMemcpy(d, h.data(), need, cudaMemcpyHostToDevice));
+        SDE_CUDA_TRY(cudaMemcpyAsync(d, h.data(), need, cudaMemcpyHostToDevice, ctx->stream));
     } else {
         d = (float *)it->second.p;
     }
@@ -827,6 +827,10 @@ int fft_images_from_grids(sde_ctx *ctx, int n, float2 *const *grids, float *cons
         SDE_CUDA_TRY(e);
     }
     return SDE_OK;
+}
+
+int check_fft_shape(int nx, int ny, int fnu, int nv) {
+    return check_fft_args(nx, ny, fnu, nv, fnu / 2 + 1);
 }
 
 int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, int fnu, int nv,

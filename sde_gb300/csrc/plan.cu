@@ -342,11 +342,10 @@ int sde_plan_destroy(sde_plan *pl) {
     if (!pl) return SDE_OK;
     sde_ctx *ctx = pl->ctx;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    // stream-ordered frees: after the plan's last use on the context's stream
     void *ptrs[] = {pl->fobs, pl->rec, pl->wt, pl->gdd, pl->orig, pl->rot, pl->gconj, pl->chunks,
                     pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    for (void *p : ptrs) ctx_free(ctx, p, 0);
     ctx->bytes -= pl->bytes;
     delete pl;
     return SDE_OK;

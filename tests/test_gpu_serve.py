@@ -71,3 +71,34 @@ def test_stream_records_and_latency(server, jobs):
     s = summarize(rec)
     assert s["p50_ms"] <= s["p99_ms"] <= s["max_ms"]
     assert s["jobs"] == len(jobs)
+
+
+def test_native_job_equals_uvmap_composition(server, jobs, orc):
+    """sde_uvmap (one native call) gives the image of the host-side uvmap composition and
+    of the oracle's uvmap, for a natural and a robust job."""
+    import torch
+    from sde_gb300.imaging import Geom, uvmap
+    from sde_gb300.serve import run_job
+    ctx = server.slots[0].ctx
+    for j in [x for x in jobs if x["natural"]][:1] + [x for x in jobs if not x["natural"]][:1]:
+        native = run_job(ctx, j, torch)
+        g = Geom(j["imsize"], j["cell"], vdec=j["dec"])
+        t = {k: ctx.tensor(j[k], torch.float32) for k in ("u", "v", "w", "wt")}
+        t["vis"] = ctx.tensor(np.asarray(j["vis"], np.complex64).view(np.float32), torch.float32)
+        with torch.cuda.stream(ctx.stream):
+            if j["natural"]:
+                r = uvmap(ctx, g, t["u"], t["v"], t["w"], t["vis"], t["wt"], weighting=False)
+            else:
+                r = uvmap(ctx, g, t["u"], t["v"], t["w"], t["vis"], t["wt"], rmode="NORM",
+                          robust=(j["robust"], 0.0, 0.0))
+            ctx.stream.synchronize()
+        comp = r["dirty"].cpu().numpy()
+        r["plan"].close()
+        w = _window(j["imsize"])
+        pk = np.abs(comp).max()
+        assert np.abs(native - comp)[w, w].max() / pk < 1e-5
+        if not j["natural"]:
+            p = orc.params(j["imsize"], j["cell"], fov=1.0, rmode="NORM",
+                           robust=(j["robust"], 0.0, 0.0), vdec=j["dec"])
+            rd, *_ = orc.uvmap(p, j["u"], j["v"], j["w"], j["vis"], j["wt"])
+            assert np.abs(native - rd)[w, w].max() / np.abs(rd).max() < 1e-5
