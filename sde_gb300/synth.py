@@ -134,6 +134,18 @@ CONFIG2 = dict(imsize=4096, cellsize=0.5, vra=0.0, vdec=40.0, fov=1.0, rmode="NO
                robust=(0.0, 0.0, 0.0), n_src=200, noise=1e-3)
 
 
+def config3_uvw(n_ant=64, n_time=8640, dt_s=5.0, n_chan=32):
+    """Precision case uv coverage: 64 antennas (2016 baselines) on a Y of 21 km arms,
+    8640 x 5 s (12 h) x 32 channels over 1.2-1.6 GHz = 557,383,680 visibilities, dec +40."""
+    seed = SEED_BASE + 3
+    pos = y_array(n_ant, 21000.0, seed)
+    freqs = 1.2e9 + (np.arange(n_chan) + 0.5) * (0.4e9 / n_chan)
+    return uvw_tracks(pos, 40.0, n_time * dt_s / 3600.0, dt_s, freqs), seed
+
+
+CONFIG3 = dict(imsize=8192, cellsize=0.5, vdec=40.0, n_src=20, noise=1e-3)
+
+
 # ---- config 4: a mosaic of uneven pointings -----------------------------------------------
 CONFIG4 = dict(n_point=49, fwhm_arcmin=30.0, spacing_arcmin=15.0, cell_arcsec=2.0,
                nvis_range=(2e3, 2e6), size_range=(256, 2048), n_src=40, noise=1e-3, dec=40.0,
