@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--clean-iters", type=int, default=200)
+    ap.add_argument("--plan-opts", default=None,
+                    help="item_max,chunk_max of the plan's work items and chunks (library defaults if unset)")
     return ap.parse_args()
 
 
@@ -307,7 +309,8 @@ def run_gpu(args):
     torch.cuda.synchronize()
     weights_ms = ev0.elapsed_time(ev1)
     t0 = time.perf_counter()
-    plan = Plan(ctx, geom, ud, vd, wd, vis, wt)
+    popts = tuple(int(x) for x in args.plan_opts.split(",")) if args.plan_opts else None
+    plan = Plan(ctx, geom, ud, vd, wd, vis, wt, opts=popts)
     torch.cuda.synchronize()
     plan_ms = (time.perf_counter() - t0) * 1e3
     nplan = plan.nvis
@@ -420,7 +423,8 @@ def run_gpu(args):
         "cpu_baseline": cpu_base,
         "once_per_job_ms": {"weights": weights_ms, "plan_build": plan_ms,
                             "hogbom_%d_iter" % args.clean_iters: hogbom_ms},
-        "plan": {"gridding_vis": int(nplan), "bytes": int(plan.nbytes), "ndrop_weighting": int(wst.ndrop)},
+        "plan": dict(gridding_vis=int(nplan), bytes=int(plan.nbytes), ndrop_weighting=int(wst.ndrop),
+                     **_plan_stats(L, plan)),
     }
     plan.close()
     ctx.close()
@@ -690,6 +694,12 @@ def _serve_cpu_baseline(tpl, budget_s=12.0):
             "sample": "uvmap of the %d cheapest of %d job templates (%d vis), oracle/ C "
                       "restatement, 1 thread" % (done, len(tpl), nv),
             "images_s": done / t_all}
+
+
+def _plan_stats(L, plan):
+    a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+    L.sde_plan_stats(plan.h, C.byref(a), C.byref(b), C.byref(c))
+    return {"work_items": a.value, "chunks": b.value, "degrid_exceptions": c.value}
 
 
 def _shim_stats(L):

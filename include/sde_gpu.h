@@ -180,7 +180,7 @@ int sde_plan_create(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, const 
 /* The same with the plan's sort-bucket sizes chosen by the caller (an autotuner): the
  * visibilities of one uv tile are cut into work items of at most item_max visibilities
  * (one CTA each), and the visibilities of one cell pair inside a work item into chunks of
- * at most chunk_max (one 4-lane group each).  0 selects the default (8192 / 64).  Limits:
+ * at most chunk_max (one 4-lane group each).  0 selects the default (16384 / 64).  Limits:
  * chunk_max <= item_max <= 65536, chunk_max <= 4096.  No counterpart in the reference
  * (GRDH2D walks visibilities in input order). */
 typedef struct {
@@ -193,6 +193,9 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
 int sde_plan_destroy(sde_plan *plan);
 int64_t sde_plan_nvis(const sde_plan *plan);       /* visibilities that grid              */
 int64_t sde_plan_bytes(const sde_plan *plan);
+/* work items, chunks and degridding exceptions (GRDDEH2D's reflection branch, FP32/FP64
+ * cell mismatches, degrid-only points) of a plan */
+int sde_plan_stats(const sde_plan *plan, int64_t *nitems, int64_t *nchunks, int64_t *nexc);
 /* Replace the plan's visibilities (same order/length as at creation). */
 int sde_plan_set_vis(sde_plan *plan, const float *vis, int where);
 

@@ -88,6 +88,7 @@ SIGNATURES = [
     ("sde_plan_destroy", I, [P]),
     ("sde_plan_nvis", I64, [P]),
     ("sde_plan_bytes", I64, [P]),
+    ("sde_plan_stats", I, [P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)]),
     ("sde_plan_set_vis", I, [P, P, I]),
     ("sde_grid_pitch", I, [I]),
     ("sde_plan_grid", I, [P, I, P, I, C.POINTER(F)]),

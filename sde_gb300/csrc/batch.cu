@@ -139,7 +139,7 @@ int batch_grid(sde_batch *b, int psf) {
     SDE_CUDA_TRY(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), ctx->stream));
     SDE_CUDA_TRY(cudaMemsetAsync(b->raw[0], 0, b->raw_bytes, ctx->stream));
     SDE_TRY(launch_grid_batch(ctx, psf, b->comp, b->d_plans, b->d_item_start, b->n, b->d_counter,
-                              ctx->d_cft, ctx->num_sms * 4));
+                              ctx->d_cft, ctx->num_sms * grid_ctas_per_sm()));
     SDE_TRY(launch_finalize_batch(ctx, b->d_fin, b->n, b->max_cells));
     return SDE_OK;
 }

@@ -45,7 +45,7 @@ constexpr int OSAMP = 128;              // oversampling (grd/grdcf.f:245)
 constexpr int NTAP = 2 * SUPP + 1;      // 7
 constexpr int STILE = TILE + 2 * SUPP;  // 70: shared tile edge (grid and degrid)
 constexpr int CFLEN = 1 + 8 * 129;      // vis/visgrid.f:274
-constexpr int ITEM_MAX = 8192;         // default work-item size (sde_plan_opts.item_max)
+constexpr int ITEM_MAX = 16384;        // default work-item size (sde_plan_opts.item_max)
 constexpr int CHUNK_MAX = 64;           // default chunk size (sde_plan_opts.chunk_max)
 constexpr int ITEM_LIMIT = 1 << 16;     // largest accepted work-item size
 constexpr int CHUNK_LIMIT = 4096;       // largest accepted chunk size
@@ -65,8 +65,10 @@ __host__ __device__ inline uint32_t pack_gdd(int dud, int dvd, uint32_t cell) {
 constexpr uint32_t GDD_EXCEPTION = 1u << 31;
 
 // Exception entries for the degridder: visibilities whose FP32 degridding cell differs
-// from their FP64 gridding cell, that sit within SUPP of the v axis (reflection branch of
-// grd/grddeh2d.f:123-158), whose conjugation flags differ, or that only degrid.
+// from their FP64 gridding cell, whose conjugation flags differ, that only degrid, or that
+// sit within SUPP of the v axis (reflection branch of grd/grddeh2d.f:123-158) where the
+// tiled degridder cannot stand in for that branch (UORIGIN != 1, or a mirrored row
+// 2*VORIGIN - v outside the grid, whose taps the reference skips).
 struct DegridExc {
     uint32_t orig;     // index in the caller's order
     int32_t pos;       // sorted position in the plan, -1 if the visibility does not grid
@@ -223,6 +225,7 @@ struct FftBatch {
     const float *scale[FFT_MAXB];
 };
 size_t grid_smem_bytes();
+int grid_ctas_per_sm();  // resident persistent gridding CTAs per SM
 int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
                       const int64_t *d_item_start, int nplans, unsigned long long *d_counter,
                       const float *cft, int nctas);

@@ -418,7 +418,8 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
              const float *__restrict__ cft_g, const float2 *__restrict__ fobs, float4 *rec,
              const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
              const uint32_t *__restrict__ orig, const float *__restrict__ wt, float2 *vis_out,
-             float *wt_out, int ntu, int *status) {
+             float *wt_out, int ntu, const float2 *__restrict__ grid, int pitch, int nv,
+             int vorigin, int refl, int *status) {
     extern __shared__ __align__(128) unsigned char smem_dg[];
     float2 *tile = reinterpret_cast<float2 *>(smem_dg);
     float *tab = reinterpret_cast<float *>(smem_dg + DG_TAB_OFF);
@@ -466,6 +467,21 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
         if (!done) {
             atomicExch(&status[STATUS_TIMEOUT], 1);
             return;
+        }
+    }
+    if (refl && tu == 0) {
+        // GRDDEH2D's reflection branch (grd/grddeh2d.f:123-158) in the tile: halo columns
+        // 3..5 stand for u = -3..-1 (left of the v axis; TMA filled them with zeros) and
+        // receive conj(G(-u, 2*VORIGIN - v)), the values that branch reads there
+        for (int k = threadIdx.x; k < STILE * SUPP; k += DG_THREADS) {
+            const int r = k / SUPP, c = SUPP + k % SUPP;    // c = 2*SUPP + u
+            const int vm = 2 * vorigin - (tv * TILE - SUPP + r + 1);  // mirrored 1-based row
+            float2 val = make_float2(0.f, 0.f);
+            if (vm >= 1 && vm <= nv) {
+                const float2 gm = grid[(int64_t)(vm - 1) * pitch + (2 * SUPP - c)];
+                val = make_float2(gm.x, -gm.y);
+            }
+            tile[r * STILE + c] = val;
         }
     }
     __syncthreads();
@@ -561,80 +577,65 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
     }
 }
 
-// Exception path: GRDDEH2D's loops verbatim (both the axis-reflection branch,
-// grd/grddeh2d.f:123-158, and the plain branch, :163-173), reading the grid from HBM.
+// Exception path: GRDDEH2D's taps and weights (the axis-reflection branch,
+// grd/grddeh2d.f:123-158, and the plain branch, :163-173), reading the grid from HBM.  One
+// warp per exception: lane l < 49 evaluates tap (offu, offv) = (l/7 - SUPP, l%7 - SUPP) and
+// the warp sums the products and weights by shuffles.  A mirrored row outside the grid,
+// which the reference's reflection loop reads without a bounds check (undefined there),
+// is left out of both sums.
+constexpr int EXC_THREADS = 128;
 template <int MODE>
-__global__ void k_degrid_exc(const DegridExc *__restrict__ exc, const float *__restrict__ exc_wt,
-                             const float2 *__restrict__ exc_rot, int64_t nexc,
-                             const float2 *__restrict__ grid, int pitch, int nu, int nv,
-                             int uorigin, int vorigin, const float *__restrict__ cf,
-                             int doshift, const float2 *__restrict__ fobs, float4 *rec,
-                             float2 *vis_out, float *wt_out, unsigned long long *nbad) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(EXC_THREADS)
+    k_degrid_exc(const DegridExc *__restrict__ exc, const float *__restrict__ exc_wt,
+                 const float2 *__restrict__ exc_rot, int64_t nexc,
+                 const float2 *__restrict__ grid, int pitch, int nu, int nv,
+                 int uorigin, int vorigin, const float *__restrict__ cf,
+                 int doshift, const float2 *__restrict__ fobs, float4 *rec,
+                 float2 *vis_out, float *wt_out, unsigned long long *nbad) {
+    const int64_t t = ((int64_t)blockIdx.x * EXC_THREADS + threadIdx.x) >> 5;  // per warp
+    const int lane = threadIdx.x & 31;
     if (t >= nexc) return;
     const DegridExc e = exc[t];
     if (MODE == 0 && e.pos < 0) return;
     const float w0 = exc_wt[t];
-    float vr = 0.f, vi = 0.f, sumwt = 0.f;
+    float vr = 0.f, vi = 0.f;
     bool ok = false;
     if (e.valid) {
         const int cfo = (SUPP + 1) * OSAMP + 1;
         const int ucen = e.nuc - uorigin, vcen = e.nvc - vorigin;
-#define GAT(U, V) grid[(int64_t)((V)-1) * pitch + ((U)-1)]
-        if (e.nuc <= SUPP) {
-            for (int offu = -SUPP; offu <= SUPP; offu++) {
-                const int delu = e.delui + OSAMP * offu + cfo;
-                if (ucen != -offu) {
-                    const int us = (ucen + offu) >= 0 ? 1 : -1;
-                    const int ui = uorigin + us * (ucen + offu);
-                    for (int offv = -SUPP; offv <= SUPP; offv++) {
-                        const int delv = e.delvi + OSAMP * offv + cfo;
-                        const int vint = vorigin + us * (vcen + offv);
-                        const float uvwt = __fmul_rn(cf[delu - 1], cf[delv - 1]);
-                        if (ui < 1 || ui > nu || vint < 1 || vint > nv) continue;
-                        float2 f = GAT(ui, vint);
-                        if (us <= 0) f.y = -f.y;
-                        vr = __fadd_rn(vr, __fmul_rn(f.x, uvwt));
-                        vi = __fadd_rn(vi, __fmul_rn(f.y, uvwt));
-                        sumwt = __fadd_rn(sumwt, uvwt);
-                    }
-                } else {
-                    for (int offv = -SUPP; offv <= SUPP; offv++) {
-                        const int delv = e.delvi + OSAMP * offv + cfo;
-                        const int vint = vorigin + (vcen + offv);
-                        const float uvwt = __fmul_rn(cf[delu - 1], cf[delv - 1]);
-                        if (vint < 1 || vint > nv) continue;
-                        const float2 f = GAT(uorigin, vint);
-                        vr = __fadd_rn(vr, __fmul_rn(f.x, uvwt));
-                        vi = __fadd_rn(vi, __fmul_rn(f.y, uvwt));
-                        sumwt = __fadd_rn(sumwt, uvwt);
-                    }
-                }
+        const bool axis = e.nuc <= SUPP;
+        float pr = 0.f, pi = 0.f, pw = 0.f;
+        for (int l = lane; l < NTAP * NTAP; l += 32) {
+            const int offu = l / NTAP - SUPP, offv = l % NTAP - SUPP;
+            const int delu = e.delui + OSAMP * offu + cfo, delv = e.delvi + OSAMP * offv + cfo;
+            const float uvwt = __fmul_rn(cf[delu - 1], cf[delv - 1]);
+            int ui = uorigin + ucen + offu, vint = vorigin + vcen + offv;
+            bool cj = false;
+            if (axis && ucen + offu != 0) {
+                const int us = (ucen + offu) >= 0 ? 1 : -1;
+                ui = uorigin + us * (ucen + offu);
+                vint = vorigin + us * (vcen + offv);
+                cj = us < 0;
             }
-        } else {
-            for (int offv = -SUPP; offv <= SUPP; offv++) {
-                const int delv = e.delvi + OSAMP * offv + cfo;
-                const int vint = vorigin + vcen + offv;
-                for (int offu = -SUPP; offu <= SUPP; offu++) {
-                    const int delu = e.delui + OSAMP * offu + cfo;
-                    const int ui = uorigin + ucen + offu;
-                    const float uvwt = __fmul_rn(cf[delu - 1], cf[delv - 1]);
-                    const float2 f = GAT(ui, vint);
-                    vr = __fadd_rn(vr, __fmul_rn(f.x, uvwt));
-                    vi = __fadd_rn(vi, __fmul_rn(f.y, uvwt));
-                    sumwt = __fadd_rn(sumwt, uvwt);
-                }
-            }
+            if (axis && (ui < 1 || ui > nu || vint < 1 || vint > nv)) continue;
+            float2 f = grid[(int64_t)(vint - 1) * pitch + (ui - 1)];
+            if (cj) f.y = -f.y;
+            pr = __fadd_rn(pr, __fmul_rn(f.x, uvwt));
+            pi = __fadd_rn(pi, __fmul_rn(f.y, uvwt));
+            pw = __fadd_rn(pw, uvwt);
         }
-#undef GAT
-        if (sumwt > 0.0f) {
-            vr = __fdiv_rn(vr, sumwt);
-            vi = __fdiv_rn(vi, sumwt);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            pr += __shfl_xor_sync(0xffffffffu, pr, d);
+            pi += __shfl_xor_sync(0xffffffffu, pi, d);
+            pw += __shfl_xor_sync(0xffffffffu, pw, d);
+        }
+        if (pw > 0.0f) {
+            vr = __fdiv_rn(pr, pw);
+            vi = __fdiv_rn(pi, pw);
             ok = true;
-        } else {
-            vr = 0.f;
-            vi = 0.f;
-            if (MODE == 1) atomicAdd(nbad, 1ull);
+        } else if (MODE == 1 && lane == 0) {
+            atomicAdd(nbad, 1ull);
         }
         if (e.conj) vi = -vi;
         const float2 rt = exc_rot[t];
@@ -643,6 +644,7 @@ __global__ void k_degrid_exc(const DegridExc *__restrict__ exc, const float *__r
         vr = xr;
         vi = xi;
     }
+    if (lane != 0) return;
     if (MODE == 1) {
         vis_out[e.orig] = make_float2(vr, vi);
         wt_out[e.orig] = ok ? fabsf(w0) : -w0;
@@ -783,6 +785,7 @@ int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, const float2 *raw_lo, f
 }
 
 size_t grid_smem_bytes() { return grid_smem(); }
+int grid_ctas_per_sm() { return GRID_MINB; }
 
 int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
                       const int64_t *d_item_start, int nplans, unsigned long long *d_counter,
@@ -876,26 +879,29 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
         if (mode == 0)
             k_degrid<0><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
                 map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot, pl->orig,
-                pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
+                pl->wt, vis_out, wt_out, pl->ntu, (const float2 *)grid, pitch, nv, pl->spec.vorigin,
+                (int)(pl->spec.uorigin == 1), ctx->d_status);
         else
             k_degrid<1><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
                 map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot, pl->orig,
-                pl->wt, vis_out, wt_out, pl->ntu, ctx->d_status);
+                pl->wt, vis_out, wt_out, pl->ntu, (const float2 *)grid, pitch, nv, pl->spec.vorigin,
+                (int)(pl->spec.uorigin == 1), ctx->d_status);
         SDE_CHECK_LAUNCH();
     }
     if (pl->nexc > 0) {
         size_t ne1 = (size_t)pl->nexc;
         const float *exc_wt = (const float *)((const char *)pl->exc + exc_wt_off(ne1));
         const float2 *exc_rot = (const float2 *)((const char *)pl->exc + exc_rot_off(ne1));
-        const int T = 128;
+        const int64_t nb = ceil_div(pl->nexc * 32, EXC_THREADS);
+        const int T = EXC_THREADS;
         KTimer kt(ctx, "degrid_exc");
         if (mode == 0)
-            k_degrid_exc<0><<<ceil_div(pl->nexc, T), T, 0, ctx->stream>>>(
+            k_degrid_exc<0><<<nb, T, 0, ctx->stream>>>(
                 pl->exc, exc_wt, exc_rot, pl->nexc, (const float2 *)grid, pitch, nu, nv,
                 pl->spec.uorigin, pl->spec.vorigin, pl->cf, pl->doshift, pl->fobs, pl->rec,
                 vis_out, wt_out, nbad_dev);
         else
-            k_degrid_exc<1><<<ceil_div(pl->nexc, T), T, 0, ctx->stream>>>(
+            k_degrid_exc<1><<<nb, T, 0, ctx->stream>>>(
                 pl->exc, exc_wt, exc_rot, pl->nexc, (const float2 *)grid, pitch, nu, nv,
                 pl->spec.uorigin, pl->spec.vorigin, pl->cf, pl->doshift, pl->fobs, pl->rec,
                 vis_out, wt_out, nbad_dev);

@@ -113,8 +113,14 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
                 int tu = (ucen - 1) >> TILE_LOG2, lu = (ucen - 1) & (TILE - 1);
                 int tv = (vcen - 1) >> TILE_LOG2, lv = (vcen - 1) & (TILE - 1);
                 key = ((uint32_t)(tv * p.ntu + tu) << 12) | ((uint32_t)lv << 6) | (uint32_t)lu;
-                bool exc = !dg.valid || dg.nud != nuc || dg.nvd != nvc || dg.nud <= p.supp ||
-                           dg.conj != (gc != 0);
+                // GRDDEH2D's reflection branch (NUD <= SUPP) reads conj(G(-u, 2*VORIGIN - v))
+                // left of the v axis; the tiled degridder holds those values in the u = 0
+                // tile's halo, so the branch stays in the tiled path when every mirrored
+                // row lies inside the grid (else the reference skips taps: exception)
+                const bool refl_tiled = p.uorigin == 1 && 2 * p.vorigin - (dg.nvd + p.supp) >= 1 &&
+                                        2 * p.vorigin - (dg.nvd - p.supp) <= p.nv;
+                bool exc = !dg.valid || dg.nud != nuc || dg.nvd != nvc ||
+                           (dg.nud <= p.supp && !refl_tiled) || dg.conj != (gc != 0);
                 const uint32_t cell = ((uint32_t)lv << 6) | (uint32_t)lu;
                 pdg = pack_gdg(dug, dvg);
                 pdd = exc ? (pack_gdd(0, 0, cell) | GDD_EXCEPTION) : pack_gdd(dg.dui, dg.dvi, cell);
@@ -330,6 +336,13 @@ int sde_grid_pitch(int nu) { return (nu + 3) & ~3; }
 
 int64_t sde_plan_nvis(const sde_plan *plan) { return plan ? plan->nvis : 0; }
 int64_t sde_plan_bytes(const sde_plan *plan) { return plan ? plan->bytes : 0; }
+int sde_plan_stats(const sde_plan *plan, int64_t *nitems, int64_t *nchunks, int64_t *nexc) {
+    if (!plan) return SDE_EINVAL;
+    if (nitems) *nitems = plan->nitems;
+    if (nchunks) *nchunks = plan->nchunks;
+    if (nexc) *nexc = plan->nexc;
+    return SDE_OK;
+}
 
 static int plan_alloc(sde_plan *pl, void **p, size_t bytes) {
     if (bytes == 0) bytes = 16;

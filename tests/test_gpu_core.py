@@ -184,6 +184,111 @@ def test_degrid_matches_grddeh2d(gpu_ctx, orc, obs_small, obs_shift, case):
     plan.close()
 
 
+def _reflection_rows_outside(g, u, v):
+    """GRDDEH2D's FP32 cells (grd/grddeh2d.f:103-114): True where a visibility inside the
+    reference's bounds has a mirrored row 2*VORIGIN - (NVC + offv) outside 1..NV."""
+    ul = np.float64(g.uscale) * u.astype(np.float64)
+    vl = (np.float64(g.vscale) * v.astype(np.float64)).astype(np.float32)
+    pos = ul > 0
+    uc = np.where(pos, ul.astype(np.float32) + np.float32(g.uorigin),
+                  -ul.astype(np.float32) + np.float32(g.uorigin))
+    vc = np.where(pos, vl + np.float32(g.vorigin), -vl + np.float32(g.vorigin))
+    nuc = np.floor(uc + 0.5).astype(int)
+    nvc = np.floor(vc + 0.5).astype(int)
+    inside = (nuc + 3 <= g.nu) & (nvc + 3 <= g.nv) & (nvc - 3 >= 1)
+    mirror_out = (2 * g.vorigin - (nvc + 3) < 1) | (2 * g.vorigin - (nvc - 3) > g.nv)
+    return inside & (nuc <= 3) & mirror_out, uc, vc, nuc, nvc, pos
+
+
+def _degrid_skip_outside(orc, g, gvis, uc, vc, nuc, nvc, pos):
+    """The reflection branch in FP64 with taps whose row lies outside the grid left out of
+    the sum and of SUMWT (the GPU's reading of an access the reference leaves undefined)."""
+    cf, supp, osamp = orc.grdcf()
+    cf = np.asarray(cf, np.float64)
+    cfo = (supp + 1) * osamp + 1
+    out = []
+    for a, b, nu_, nv_, p in zip(uc, vc, nuc, nvc, pos):
+        dui = int(np.floor(np.float32(osamp) * (np.float32(nu_) - a) + np.float32(0.5)))
+        dvi = int(np.floor(np.float32(osamp) * (np.float32(nv_) - b) + np.float32(0.5)))
+        ucen, vcen = nu_ - g.uorigin, nv_ - g.vorigin
+        acc, sw = 0j, 0.0
+        for offu in range(-supp, supp + 1):
+            us = 1 if ucen + offu >= 0 else -1
+            ui = g.uorigin + us * (ucen + offu)
+            for offv in range(-supp, supp + 1):
+                vi = g.vorigin + us * (vcen + offv)
+                if vi < 1 or vi > g.nv:
+                    continue
+                wgt = cf[dui + osamp * offu + cfo - 1] * cf[dvi + osamp * offv + cfo - 1]
+                f = complex(gvis[vi - 1, ui - 1])
+                acc += (f if us > 0 else f.conjugate()) * wgt
+                sw += wgt
+        val = acc / sw
+        out.append(val.conjugate() if p else val)
+    return np.array(out)
+
+
+def test_degrid_reflection_branch(gpu_ctx, orc):
+    """GRDDEH2D's axis-reflection branch (grd/grddeh2d.f:123-158): visibilities within SUPP
+    cells of the v axis, over the whole v range.  Those whose mirrored rows 2*VORIGIN - v
+    stay inside the grid are degridded by the tiled kernel (from the u = 0 tile's mirrored
+    halo) and must match the oracle.  Where a mirrored row leaves the grid the reference
+    reads outside GVIS (no bounds check in that loop): those take the exception path, which
+    leaves the outside taps out, and are checked against that rule in FP64."""
+    import ctypes as C
+    from sde_gb300 import _abi
+    from sde_gb300.imaging import Geom, Plan
+    ctx = gpu_ctx
+    g = Geom(64, 8.0, vdec=40.0)
+    rng = np.random.default_rng(21)
+    n = 3000
+    ucell = rng.uniform(-3.45, 3.45, n)
+    vcell = rng.uniform(-27.0, 27.0, n)
+    # rows at the v edges: NVC = 61 / 60 (a mirrored row off the grid / inside) and
+    # NVC = 4 / 3 (tiled / outside GRDDEH2D's bounds)
+    vcell[:40] = np.repeat([29.0, 28.0, -28.0, -29.0], 10) + rng.uniform(-0.3, 0.3, 40)
+    u = (ucell / g.uscale).astype(np.float32)
+    v = (vcell / g.vscale).astype(np.float32)
+    w = rng.uniform(-50, 50, n).astype(np.float32)
+    vis = (rng.normal(size=n) + 1j * rng.normal(size=n)).astype(np.complex64)
+    wt = np.ones(n, np.float32)
+    gvis = (rng.normal(size=(g.nv, g.nu)) + 1j * rng.normal(size=(g.nv, g.nu))).astype(np.complex64)
+    edge, uc, vc, nuc, nvc, pos = _reflection_rows_outside(g, u, v)
+    assert 0 < edge.sum() < 40
+    d = ~edge  # where the reference is defined
+    ref_vis, ref_wt, ref_nbad = orc.grddeh2d(vis[d], wt[d], u[d], v[d], w[d], g.uscale, g.vscale,
+                                             g.uorigin, g.vorigin, gvis, g.shift)
+    t = {k: _dev(ctx, x) for k, x in (("u", u), ("v", v), ("w", w), ("wt", wt), ("vis", vis))}
+    plan = Plan(ctx, g, t["u"], t["v"], t["w"], t["vis"], t["wt"])
+    a, b, nexc = C.c_int64(), C.c_int64(), C.c_int64()
+    _abi.lib().sde_plan_stats(plan.h, C.byref(a), C.byref(b), C.byref(nexc))
+    assert 0 < nexc.value < 40  # only edge rows; the near-axis bulk is tiled
+    gp = np.zeros((g.nv, g.pitch), np.complex64)
+    gp[:, :g.nu] = gvis
+    gd = _dev(ctx, gp)
+    vis_out = t["vis"].clone()
+    wt_out = t["wt"].clone()
+    nbad = plan.degrid(gd, vis_out, wt_out)
+    got_v = vis_out.cpu().numpy()
+    got_w = wt_out.cpu().numpy()
+    assert nbad == ref_nbad
+    assert np.array_equal(got_w[d], ref_wt)
+    scale = np.abs(ref_vis[ref_wt > 0]).max()
+    assert np.abs(got_v[d] - ref_vis).max() / scale < 1e-5
+    e64 = _degrid_skip_outside(orc, g, gvis, uc[edge], vc[edge], nuc[edge], nvc[edge], pos[edge])
+    assert np.all(got_w[edge] > 0)
+    assert np.abs(got_v[edge] - e64).max() / scale < 1e-5
+    # residual form: observed - model, read back in the caller's order
+    plan.degrid_residual(gd)
+    res = t["vis"].clone()
+    plan.residual(res)
+    r = res.cpu().numpy()
+    ok = ref_wt > 0
+    assert np.abs(r[d][ok] - (vis[d] - ref_vis)[ok]).max() / scale < 1e-5
+    assert np.abs(r[edge] - (vis[edge] - e64)).max() / scale < 1e-5
+    plan.close()
+
+
 def test_residual_cycle_consistent(gpu_ctx, orc, obs_small):
     """Residual = observed - model in the gridding frame equals gridding (obs - degrid)."""
     from sde_gb300.imaging import Plan
