@@ -216,7 +216,10 @@ int sde_plan_reset_residual(sde_plan *plan);
 /* Degrid a device grid into user-ordered visibilities exactly as GRDDEH2D does
  * (normalised interpolation, reflection, conjugation, phase rotation, WT sign flags).
  * vis_out/wt_out are device or host pointers per `where` (length = nvis at creation);
- * entries GRDDEH2D would not touch are left unchanged. */
+ * like GRDDEH2D's VIS and WT they are in/out: wt_out holds the WT the plan was made from,
+ * and entries GRDDEH2D would not touch (WT <= 0) are left unchanged.  Host arrays are
+ * uploaded only when the plan has such entries, and WT is copied back only when a point
+ * was not degridded (its WT negated). */
 int sde_plan_degrid(sde_plan *plan, const float *grid, int pitch, float *vis_out,
                     float *wt_out, int where, int64_t *nbad);
 /* Copy the residual visibilities back in the caller's original order (complex64). */

@@ -362,25 +362,34 @@ extern "C" int sde_plan_degrid(sde_plan *pl, const float *grid, int pitch, float
     const size_t n = (size_t)(pl->nvis_in > 0 ? pl->nvis_in : 1);
     float2 *dv = (float2 *)vis_out;
     float *dw = wt_out;
+    const size_t nin = (size_t)pl->nvis_in;
     if (where == SDE_HOST) {
         SDE_TRY(ctx_scratch(ctx, "dg_vis", 8 * n, (void **)&dv));
         SDE_TRY(ctx_scratch(ctx, "dg_wt", 4 * n, (void **)&dw));
-        SDE_CUDA_TRY(cudaMemcpyAsync(dv, vis_out, 8 * (size_t)pl->nvis_in, cudaMemcpyHostToDevice, ctx->stream));
-        SDE_CUDA_TRY(cudaMemcpyAsync(dw, wt_out, 4 * (size_t)pl->nvis_in, cudaMemcpyHostToDevice, ctx->stream));
+        // Every visibility with WT > 0 is written (degridded value, or 0 and WT negated);
+        // only the others keep the caller's values, so VIS and WT go up only if there are
+        // such visibilities.
+        if (pl->nuntouched > 0) {
+            SDE_CUDA_TRY(cudaMemcpyAsync(dv, vis_out, 8 * nin, cudaMemcpyHostToDevice, ctx->stream));
+            SDE_CUDA_TRY(cudaMemcpyAsync(dw, wt_out, 4 * nin, cudaMemcpyHostToDevice, ctx->stream));
+        }
     }
-    unsigned long long *nb;
-    SDE_TRY(ctx_scratch(ctx, "dg_nbad", 8, (void **)&nb));
-    SDE_CUDA_TRY(cudaMemsetAsync(nb, 0, 8, ctx->stream));
+    unsigned long long *nb;  // [0] points not degridded (SUMWT <= 0), [1] WT negated
+    SDE_TRY(ctx_scratch(ctx, "dg_nbad", 16, (void **)&nb));
+    SDE_CUDA_TRY(cudaMemsetAsync(nb, 0, 16, ctx->stream));
     SDE_TRY(plan_degrid(pl, grid, pitch, 1, dv, dw, nb));
-    if (where == SDE_HOST) {
-        SDE_CUDA_TRY(cudaMemcpyAsync(vis_out, dv, 8 * (size_t)pl->nvis_in, cudaMemcpyDeviceToHost, ctx->stream));
-        SDE_CUDA_TRY(cudaMemcpyAsync(wt_out, dw, 4 * (size_t)pl->nvis_in, cudaMemcpyDeviceToHost, ctx->stream));
-    }
+    if (where == SDE_HOST)
+        SDE_CUDA_TRY(cudaMemcpyAsync(vis_out, dv, 8 * nin, cudaMemcpyDeviceToHost, ctx->stream));
     if (nbad || where == SDE_HOST) {
-        unsigned long long h = 0;
-        SDE_CUDA_TRY(cudaMemcpyAsync(&h, nb, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        unsigned long long h[2] = {0, 0};
+        SDE_CUDA_TRY(cudaMemcpyAsync(h, nb, 16, cudaMemcpyDeviceToHost, ctx->stream));
         SDE_TRY(sde_ctx_sync(ctx));
-        if (nbad) *nbad = (int64_t)h;
+        if (nbad) *nbad = (int64_t)h[0];
+        // WT keeps the caller's values (the plan's WT) unless a point was not degridded
+        if (where == SDE_HOST && h[1] > 0) {
+            SDE_CUDA_TRY(cudaMemcpyAsync(wt_out, dw, 4 * nin, cudaMemcpyDeviceToHost, ctx->stream));
+            SDE_TRY(sde_ctx_sync(ctx));
+        }
     }
     return SDE_OK;
 }
@@ -557,14 +566,32 @@ struct ShimCache {
 };
 static ShimCache g_pc;
 
+// flag = 1 if the n words differ anywhere (both arrays 16-byte aligned): 16-byte loads,
+// four in flight per thread, then the tail word by word.
 __global__ void k_words_differ(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b,
                                int64_t n, int *flag) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
-        if (a[i] != b[i]) {
-            *flag = 1;
-            return;
+    const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * blockDim.x;
+    const uint4 *a4 = reinterpret_cast<const uint4 *>(a), *b4 = reinterpret_cast<const uint4 *>(b);
+    uint32_t diff = 0;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        uint4 x[4], y[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            x[k] = a4[i + k * stride];
+            y[k] = b4[i + k * stride];
         }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            diff |= (x[k].x ^ y[k].x) | (x[k].y ^ y[k].y) | (x[k].z ^ y[k].z) | (x[k].w ^ y[k].w);
+    }
+    for (; i < n4; i += stride) {
+        const uint4 x = a4[i], y = b4[i];
+        diff |= (x.x ^ y.x) | (x.y ^ y.y) | (x.z ^ y.z) | (x.w ^ y.w);
+    }
+    for (int64_t j = 4 * n4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride)
+        diff |= a[j] ^ b[j];
+    if (diff) *flag = 1;
 }
 
 static uint64_t hash_floats(const float *x, size_t n) {
@@ -596,7 +623,6 @@ static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const floa
         SDE_CUDA_TRY(cudaMemcpyAsync(in + 2 * n, w, nb, cudaMemcpyHostToDevice, st));
         SDE_CUDA_TRY(cudaMemcpyAsync(in + 3 * n, wt, nb, cudaMemcpyHostToDevice, st));
         if (vis) SDE_CUDA_TRY(cudaMemcpyAsync(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
-        else SDE_CUDA_TRY(cudaMemsetAsync(dvis, 0, 2 * nb, st));
     }
     const uint64_t h = hash_floats(cf, 2 * (SUPP + 1) * OSAMP + 1);
     if (g_pc.pl && g_pc.nvis == n && g_pc.cf_hash == h && memcmp(&g_pc.spec, &sp, sizeof sp) == 0) {
@@ -613,13 +639,15 @@ static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const floa
         SDE_CUDA_TRY(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
         SDE_CUDA_TRY(cudaStreamSynchronize(st));
         if (!hf) {
-            if (n > 0) SDE_TRY(sde_plan_set_vis(g_pc.pl, dvis, SDE_DEVICE));
+            // GRDDEH2D's call passes no visibilities: the plan's are not used there
+            if (n > 0 && vis) SDE_TRY(sde_plan_set_vis(g_pc.pl, dvis, SDE_DEVICE));
             g_pc.hits++;
             *out = g_pc.pl;
             return SDE_OK;
         }
     }
     shim_cache_drop();
+    if (!vis && n > 0) SDE_CUDA_TRY(cudaMemsetAsync(dvis, 0, 2 * nb, st));
     sde_plan *pl = nullptr;
     SDE_TRY(sde_plan_create(ctx, &sp, n, in, in + n, in + 2 * n, dvis, in + 3 * n, SDE_DEVICE, &pl));
     int rc = plan_use_table(pl, cf);

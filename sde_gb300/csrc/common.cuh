@@ -181,6 +181,9 @@ struct sde_plan {
     WorkItem *items = nullptr;
     DegridExc *exc = nullptr; // exception list (includes degrid-only visibilities)
     float *wt_all = nullptr;  // caller-order weights (for user-frame degridding)
+    int32_t *inv = nullptr;   // caller index -> position of the tiled visibilities (-1 else),
+                              // built on the first caller-order degrid
+    int64_t nuntouched = 0;   // caller visibilities with WT <= 0 (GRDDEH2D leaves them as they are)
     float *cf = nullptr;      // gridding function used by this plan (device, CFLEN)
     float *cft = nullptr;     // transposed table
     double *d_sums = nullptr; // [0] sum of UVWT (LSUMWT), [1] SUMWT
@@ -236,6 +239,7 @@ int check_fft_shape(int nx, int ny, int fnu, int nv);  // SDE_EINVAL + message i
 int fft_images_from_grids(sde_ctx *ctx, int n, float2 *const *grids, float *const *images,
                           const float *const *scales, int pitch, int nx, int ny, int fnu, int nv,
                           int correct);
+int plan_inverse(sde_plan *pl);
 int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vis_out,
                 float *wt_out, unsigned long long *nbad_dev);
 int plan_scatter_residual(sde_plan *pl, float2 *dst);

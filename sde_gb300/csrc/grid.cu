@@ -417,9 +417,8 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
              const uint2 *__restrict__ chunks, const uint32_t *__restrict__ gdd,
              const float *__restrict__ cft_g, const float2 *__restrict__ fobs, float4 *rec,
              const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
-             const uint32_t *__restrict__ orig, const float *__restrict__ wt, float2 *vis_out,
-             float *wt_out, int ntu, const float2 *__restrict__ grid, int pitch, int nv,
-             int vorigin, int refl, int *status) {
+             const float *__restrict__ wt, float4 *stage, int ntu, const float2 *__restrict__ grid,
+             int pitch, int nv, int vorigin, int refl, int *status) {
     extern __shared__ __align__(128) unsigned char smem_dg[];
     float2 *tile = reinterpret_cast<float2 *>(smem_dg);
     float *tab = reinterpret_cast<float *>(smem_dg + DG_TAB_OFF);
@@ -563,18 +562,39 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
             if (MODE == 0) {
                 *rec_res(rec, pq) = make_float2(ob.x - mr, ob.y - mi);
             } else {
+                // caller's frame, staged in plan order (k_gather_user puts it in the
+                // caller's order with coalesced writes)
                 if (gconj[pq]) mi = -mi;
                 float2 vv = make_float2(mr, mi);
                 if (rot) {
                     const float2 rt = rot[pq];
                     vv = make_float2(mr * rt.x - mi * rt.y, mr * rt.y + mi * rt.x);
                 }
-                const uint32_t o = orig[pq];
-                vis_out[o] = vv;
-                wt_out[o] = wt[pq];
+                stage[pq] = make_float4(vv.x, vv.y, wt[pq], 0.f);
             }
         }
     }
+}
+
+// Caller index -> plan position of the visibilities the tiled degridder handles (-1 for
+// the others: exceptions, visibilities outside the plan).
+__global__ void k_plan_inverse(const uint32_t *__restrict__ orig, const uint32_t *__restrict__ gdd,
+                               int64_t n, int32_t *inv) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    if (!(gdd[p] & GDD_EXCEPTION)) inv[orig[p]] = (int32_t)p;
+}
+
+// Caller-order output of the tiled degridder: coalesced writes, one 16-byte gather each.
+__global__ void k_gather_user(const int32_t *__restrict__ inv, const float4 *__restrict__ stage,
+                              int64_t n, float2 *vis_out, float *wt_out) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int32_t p = inv[o];
+    if (p < 0) return;
+    const float4 s = stage[p];
+    vis_out[o] = make_float2(s.x, s.y);
+    wt_out[o] = s.z;
 }
 
 // Exception path: GRDDEH2D's taps and weights (the axis-reflection branch,
@@ -648,6 +668,7 @@ __global__ void __launch_bounds__(EXC_THREADS)
     if (MODE == 1) {
         vis_out[e.orig] = make_float2(vr, vi);
         wt_out[e.orig] = ok ? fabsf(w0) : -w0;
+        if (!ok) atomicAdd(nbad + 1, 1ull);  // WT left negated: the caller's WT changes
     } else {
         // model in the gridding frame: rotate by (c, -s) when the plan rotates, conjugate
         float mr = vr, mi = vi;
@@ -859,6 +880,23 @@ int plan_grid_raw(sde_plan *pl, int what, float2 *raw, float2 *raw_lo) {
     return SDE_OK;
 }
 
+// The caller -> plan permutation of the tiled visibilities, built on first use.
+int plan_inverse(sde_plan *pl) {
+    if (pl->inv || pl->nvis_in == 0) return SDE_OK;
+    sde_ctx *ctx = pl->ctx;
+    int32_t *inv = nullptr;
+    SDE_TRY(ctx_alloc(ctx, (void **)&inv, sizeof(int32_t) * (size_t)pl->nvis_in));
+    pl->bytes += (int64_t)(sizeof(int32_t) * (size_t)pl->nvis_in);
+    ctx->bytes += (int64_t)(sizeof(int32_t) * (size_t)pl->nvis_in);
+    SDE_CUDA_TRY(cudaMemsetAsync(inv, 0xFF, sizeof(int32_t) * (size_t)pl->nvis_in, ctx->stream));
+    if (pl->nvis > 0) {
+        k_plan_inverse<<<ceil_div(pl->nvis, 256), 256, 0, ctx->stream>>>(pl->orig, pl->gdd, pl->nvis, inv);
+        SDE_CHECK_LAUNCH();
+    }
+    pl->inv = inv;
+    return SDE_OK;
+}
+
 // mode 0: residual update; mode 1: caller-order output
 int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vis_out,
                 float *wt_out, unsigned long long *nbad_dev) {
@@ -872,21 +910,32 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
                                           (int)degrid_smem()));
         attr = true;
     }
+    float4 *stage = nullptr;
+    if (mode == 1 && pl->nitems > 0) {
+        SDE_TRY(ctx_scratch(ctx, "dg_stage", sizeof(float4) * (size_t)pl->nvis, (void **)&stage));
+        SDE_TRY(plan_inverse(pl));
+    }
     if (pl->nitems > 0) {
         CUtensorMap map;
         SDE_TRY(make_grid_tmap(&map, grid, pitch, nv));
         KTimer kt(ctx, "degrid");
         if (mode == 0)
             k_degrid<0><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot, pl->orig,
-                pl->wt, vis_out, wt_out, pl->ntu, (const float2 *)grid, pitch, nv, pl->spec.vorigin,
+                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot,
+                pl->wt, nullptr, pl->ntu, (const float2 *)grid, pitch, nv, pl->spec.vorigin,
                 (int)(pl->spec.uorigin == 1), ctx->d_status);
         else
             k_degrid<1><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot, pl->orig,
-                pl->wt, vis_out, wt_out, pl->ntu, (const float2 *)grid, pitch, nv, pl->spec.vorigin,
+                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot,
+                pl->wt, stage, pl->ntu, (const float2 *)grid, pitch, nv, pl->spec.vorigin,
                 (int)(pl->spec.uorigin == 1), ctx->d_status);
         SDE_CHECK_LAUNCH();
+        if (mode == 1) {
+            KTimer kg(ctx, "gather_user");
+            k_gather_user<<<ceil_div(pl->nvis_in, 256), 256, 0, ctx->stream>>>(
+                pl->inv, stage, pl->nvis_in, vis_out, wt_out);
+            SDE_CHECK_LAUNCH();
+        }
     }
     if (pl->nexc > 0) {
         size_t ne1 = (size_t)pl->nexc;

@@ -140,9 +140,11 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
         gconj[i] = gc;
     }
     unsigned mv = __ballot_sync(0xffffffffu, nvalid), me = __ballot_sync(0xffffffffu, nexc);
+    const unsigned mt = __ballot_sync(0xffffffffu, i < n && wt[i] > 0.0f);
     if ((threadIdx.x & 31) == 0) {
         if (mv) atomicAdd(&counts[0], (unsigned long long)__popc(mv));
         if (me) atomicAdd(&counts[1], (unsigned long long)__popc(me));
+        if (mt) atomicAdd(&counts[2], (unsigned long long)__popc(mt));
     }
 }
 
@@ -357,7 +359,7 @@ int sde_plan_destroy(sde_plan *pl) {
     cudaSetDevice(ctx->device);
     // stream-ordered frees: after the plan's last use on the context's stream
     void *ptrs[] = {pl->fobs, pl->rec, pl->wt, pl->gdd, pl->orig, pl->rot, pl->gconj, pl->chunks,
-                    pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums};
+                    pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums, pl->inv};
     for (void *p : ptrs) ctx_free(ctx, p, 0);
     ctx->bytes -= pl->bytes;
     delete pl;
@@ -486,10 +488,11 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
             goto fail;
         }
         if (nvis > 0) PL_TRY(launch_radix_sort_u32(ctx, keys, vals, nvis, kbits, ktmp, vtmp));
-        unsigned long long hc[2] = {0, 0};
+        unsigned long long hc[3] = {0, 0, 0};
         PL_CUDA(cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, st));
         PL_CUDA(cudaStreamSynchronize(st));
         const int64_t nvalid = (int64_t)hc[0], nexc = (int64_t)hc[1];
+        pl->nuntouched = nvis - (int64_t)hc[2];
         pl->nvis = nvalid;
         pl->nexc = nexc;
         const size_t nv1 = (size_t)(nvalid > 0 ? nvalid : 1);

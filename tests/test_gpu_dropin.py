@@ -115,6 +115,56 @@ def test_grddeh2d(L, orc, case):
         assert np.array_equal(np.sign(wt), np.sign(rwt))
 
 
+def test_grddeh2d_flagged_and_failed_points(L, orc):
+    """GRDDEH2D leaves VIS and WT of flagged points (WT <= 0) as they are, and zeroes VIS and
+    negates WT of points outside its bounds: the host path uploads and copies back only what
+    those rules need, and must give the oracle's arrays."""
+    from sde_gb300 import _abi
+    from sde_gb300.imaging import Geom
+    g = Geom(64, 8.0, vdec=40.0)
+    rng = np.random.default_rng(12)
+    n = 2000
+    ucell = rng.uniform(-30.0, 30.0, n)
+    vcell = rng.uniform(-27.0, 27.0, n)
+    vcell[:30] = rng.uniform(29.6, 31.0, 30) * np.sign(rng.uniform(-1, 1, 30))  # outside
+    u = (ucell / g.uscale).astype(np.float32)
+    v = (vcell / g.vscale).astype(np.float32)
+    w = rng.uniform(-50, 50, n).astype(np.float32)
+    vis0 = (rng.normal(size=n) + 1j * rng.normal(size=n)).astype(np.complex64)
+    wt0 = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    wt0[30:80] = -wt0[30:80]
+    wt0[80:90] = 0.0
+    gvis = (rng.normal(size=(g.nv, g.nu)) + 1j * rng.normal(size=(g.nv, g.nu))).astype(np.complex64)
+    cf, _, _ = orc.grdcf()
+    shift = np.ascontiguousarray(list(g.shift), np.float64)
+    rvis, rwt, rnb = orc.grddeh2d(vis0, wt0, u, v, w, g.uscale, g.vscale, g.uorigin, g.vorigin,
+                                  gvis, shift, cf=cf)
+    assert (rwt < 0).sum() > 50  # flagged and failed points present
+    for _ in range(2):  # second call: the cached plan
+        vis = vis0.copy()
+        wt = wt0.copy()
+        L.grddeh2d_(_p(vis), _p(wt), _p(u), _p(v), _p(w), I(n), F(g.uscale), F(0), F(g.vscale),
+                    F(0), I(g.uorigin), I(g.vorigin), _p(gvis), I(g.nu), I(g.nv), _p(cf), I(3),
+                    I(128), _p(cf), I(3), I(128), _p(shift))
+        assert _abi.sysi().error == 0
+        assert np.array_equal(wt.view(np.uint32), rwt.view(np.uint32))
+        keep = wt0 <= 0
+        assert np.array_equal(vis[keep], vis0[keep])
+        assert np.abs(vis - rvis).max() / np.abs(rvis[rwt > 0]).max() < 1e-5
+    # all weights positive: nothing is uploaded for VIS/WT; outputs still complete
+    wt1 = np.abs(wt0) + np.float32(0.1)
+    rvis1, rwt1, _ = orc.grddeh2d(vis0, wt1, u, v, w, g.uscale, g.vscale, g.uorigin, g.vorigin,
+                                  gvis, shift, cf=cf)
+    vis = np.full(n, np.complex64(7 + 7j))
+    wt = wt1.copy()
+    L.grddeh2d_(_p(vis), _p(wt), _p(u), _p(v), _p(w), I(n), F(g.uscale), F(0), F(g.vscale), F(0),
+                I(g.uorigin), I(g.vorigin), _p(gvis), I(g.nu), I(g.nv), _p(cf), I(3), I(128),
+                _p(cf), I(3), I(128), _p(shift))
+    assert _abi.sysi().error == 0
+    assert np.array_equal(wt.view(np.uint32), rwt1.view(np.uint32))
+    assert np.abs(vis - rvis1).max() / np.abs(rvis1[rwt1 > 0]).max() < 1e-5
+
+
 def test_grduwt2d_and_grdruw2d_bit_exact(L, orc, case):
     from sde_gb300.imaging import Geom
     o, g0, cf = case
