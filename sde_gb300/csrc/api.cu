@@ -566,14 +566,21 @@ struct ShimCache {
 };
 static ShimCache g_pc;
 
-// flag = 1 if the n words differ anywhere (both arrays 16-byte aligned): 16-byte loads,
-// four in flight per thread, then the tail word by word.
+// flag = 1 if the n words differ anywhere.  a and b have the same alignment modulo 16
+// bytes: the head words up to the first 16-byte boundary go one by one, the body as 16-byte
+// loads (four in flight per thread), the tail word by word.
 __global__ void k_words_differ(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b,
                                int64_t n, int *flag) {
-    const int64_t n4 = n >> 2, stride = (int64_t)gridDim.x * blockDim.x;
-    const uint4 *a4 = reinterpret_cast<const uint4 *>(a), *b4 = reinterpret_cast<const uint4 *>(b);
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t head = (int64_t)((4 - (((uintptr_t)a >> 2) & 3)) & 3);
+    if (head > n) head = n;
     uint32_t diff = 0;
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < head) diff |= a[tid] ^ b[tid];
+    const int64_t n4 = (n - head) >> 2;
+    const uint4 *a4 = reinterpret_cast<const uint4 *>(a + head);
+    const uint4 *b4 = reinterpret_cast<const uint4 *>(b + head);
+    int64_t i = tid;
     for (; i + 3 * stride < n4; i += 4 * stride) {
         uint4 x[4], y[4];
 #pragma unroll
@@ -589,8 +596,7 @@ __global__ void k_words_differ(const uint32_t *__restrict__ a, const uint32_t *_
         const uint4 x = a4[i], y = b4[i];
         diff |= (x.x ^ y.x) | (x.y ^ y.y) | (x.z ^ y.z) | (x.w ^ y.w);
     }
-    for (int64_t j = 4 * n4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride)
-        diff |= a[j] ^ b[j];
+    for (int64_t j = head + 4 * n4 + tid; j < n; j += stride) diff |= a[j] ^ b[j];
     if (diff) *flag = 1;
 }
 
@@ -609,38 +615,76 @@ static void shim_cache_drop() {
 
 // The plan for this call (owned by the cache: callers do not destroy it).  vis may be NULL
 // (GRDDEH2D: VIS is output only).
+// Copies of the drop-ins' inputs run on a second stream so that work on the context's stream
+// overlaps them: the cached plan takes the new visibilities (set_vis) while U, V, W, WT are
+// still arriving, each array is compared as soon as it has arrived, and a caller's extra
+// upload (GRDDEH2D's model grid) follows the inputs while the comparison runs.
+struct ShimStreams {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev[7] = {};
+};
+static ShimStreams g_ss;
+
+static int shim_streams() {
+    if (g_ss.copy) return SDE_OK;
+    SDE_CUDA_TRY(cudaStreamCreateWithFlags(&g_ss.copy, cudaStreamNonBlocking));
+    for (auto &e : g_ss.ev) SDE_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return SDE_OK;
+}
+
+struct Upload2D {  // an extra host -> device 2-D copy issued behind the inputs
+    void *dst;
+    size_t dpitch;
+    const void *src;
+    size_t spitch, width, rows;
+};
+
 static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const float *u,
                      const float *v, const float *w, const float *vis, const float *wt,
-                     const float *cf, sde_plan **out) {
+                     const float *cf, sde_plan **out, const Upload2D *extra = nullptr) {
     cudaStream_t st = ctx->stream;
+    SDE_TRY(shim_streams());
+    cudaStream_t cs = g_ss.copy;
     float *in = nullptr, *dvis = nullptr;
     const size_t nb = sizeof(float) * (size_t)(n > 0 ? n : 1);
     SDE_TRY(ctx_scratch(ctx, "shim_in", 4 * nb, (void **)&in));
     SDE_TRY(ctx_scratch(ctx, "shim_vis", 2 * nb, (void **)&dvis));
-    if (n > 0) {
-        SDE_CUDA_TRY(cudaMemcpyAsync(in, u, nb, cudaMemcpyHostToDevice, st));
-        SDE_CUDA_TRY(cudaMemcpyAsync(in + n, v, nb, cudaMemcpyHostToDevice, st));
-        SDE_CUDA_TRY(cudaMemcpyAsync(in + 2 * n, w, nb, cudaMemcpyHostToDevice, st));
-        SDE_CUDA_TRY(cudaMemcpyAsync(in + 3 * n, wt, nb, cudaMemcpyHostToDevice, st));
-        if (vis) SDE_CUDA_TRY(cudaMemcpyAsync(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
-    }
+    int *flag = nullptr;
+    SDE_TRY(ctx_scratch(ctx, "shim_flag", sizeof(int), (void **)&flag));
     const uint64_t h = hash_floats(cf, 2 * (SUPP + 1) * OSAMP + 1);
-    if (g_pc.pl && g_pc.nvis == n && g_pc.cf_hash == h && memcmp(&g_pc.spec, &sp, sizeof sp) == 0) {
-        int *flag = nullptr;
-        SDE_TRY(ctx_scratch(ctx, "shim_flag", sizeof(int), (void **)&flag));
-        SDE_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
-        if (n > 0) {
-            k_words_differ<<<ctx->num_sms * 4, 256, 0, st>>>(reinterpret_cast<const uint32_t *>(in),
-                                                              reinterpret_cast<const uint32_t *>(g_pc.inputs),
-                                                              4 * n, flag);
+    const bool cached = g_pc.pl && g_pc.nvis == n && g_pc.cf_hash == h &&
+                        memcmp(&g_pc.spec, &sp, sizeof sp) == 0;
+    SDE_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    if (n > 0 && vis) SDE_CUDA_TRY(cudaMemcpyAsync(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
+    // the copy stream follows everything queued so far (scratch allocations, earlier users
+    // of the buffers, the visibilities' copy)
+    SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[0], st));
+    SDE_CUDA_TRY(cudaStreamWaitEvent(cs, g_ss.ev[0], 0));
+    if (n > 0 && vis && cached) SDE_TRY(sde_plan_set_vis(g_pc.pl, dvis, SDE_DEVICE));  // speculative
+    const float *src[4] = {u, v, w, wt};
+    for (int k = 0; k < 4 && n > 0; k++) {
+        SDE_CUDA_TRY(cudaMemcpyAsync(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
+        SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[1 + k], cs));
+    }
+    if (extra)
+        SDE_CUDA_TRY(cudaMemcpy2DAsync(extra->dst, extra->dpitch, extra->src, extra->spitch,
+                                       extra->width, extra->rows, cudaMemcpyHostToDevice, cs));
+    SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[5], cs));
+    if (cached) {
+        for (int k = 0; k < 4 && n > 0; k++) {
+            SDE_CUDA_TRY(cudaStreamWaitEvent(st, g_ss.ev[1 + k], 0));
+            k_words_differ<<<ctx->num_sms * 4, 256, 0, st>>>(
+                reinterpret_cast<const uint32_t *>(in + k * n),
+                reinterpret_cast<const uint32_t *>(g_pc.inputs + k * n), n, flag);
             SDE_CHECK_LAUNCH();
         }
+    }
+    SDE_CUDA_TRY(cudaStreamWaitEvent(st, g_ss.ev[5], 0));
+    if (cached) {
         int hf = 1;
         SDE_CUDA_TRY(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
         SDE_CUDA_TRY(cudaStreamSynchronize(st));
         if (!hf) {
-            // GRDDEH2D's call passes no visibilities: the plan's are not used there
-            if (n > 0 && vis) SDE_TRY(sde_plan_set_vis(g_pc.pl, dvis, SDE_DEVICE));
             g_pc.hits++;
             *out = g_pc.pl;
             return SDE_OK;
@@ -749,18 +793,12 @@ extern "C" void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, i
     sde_gridspec sp;
     fill_spec(&sp, *nu, *nv, *uscale, *uoffset, *vscale, *voffset, *uorigin, *vorigin, shift);
     sde_plan *pl = nullptr;
-    int rc = shim_plan(ctx, sp, *nvis, u, v, w, nullptr, wt, intfnu, &pl);
     float2 *dg = nullptr;
     const int pitch = sde_grid_pitch(*nu);
-    if (rc == SDE_OK) rc = ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * *nv, (void **)&dg);
-    if (rc == SDE_OK) {
-        cudaError_t e = cudaMemcpy2DAsync(dg, (size_t)pitch * 8, gvis, (size_t)*nu * 8, (size_t)*nu * 8,
-                                          *nv, cudaMemcpyHostToDevice, ctx->stream);
-        if (e != cudaSuccess) {
-            sde_set_error("%s", cudaGetErrorString(e));
-            rc = SDE_ECUDA;
-        }
-    }
+    int rc = ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * *nv, (void **)&dg);
+    // the model grid goes up behind U, V, W, WT, while they are compared with the cached plan's
+    const Upload2D gup{dg, (size_t)pitch * 8, gvis, (size_t)*nu * 8, (size_t)*nu * 8, (size_t)*nv};
+    if (rc == SDE_OK) rc = shim_plan(ctx, sp, *nvis, u, v, w, nullptr, wt, intfnu, &pl, &gup);
     int64_t nbad = 0;
     if (rc == SDE_OK) rc = sde_plan_degrid(pl, (const float *)dg, pitch, vis, wt, SDE_HOST, &nbad);
     if (rc != SDE_OK) {

@@ -395,6 +395,7 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
 }
 
 constexpr int DG_GROUPS = DG_THREADS / 4;          // chunks in flight per CTA
+constexpr int DG_PREFETCH = 4096;                  // visibilities prefetched into L2 per item
 constexpr int RSUM_FLOATS = 132;                    // 129 row sums, padded
 constexpr size_t DG_TAB_OFF = DG_TX_BYTES;
 constexpr size_t DG_RSUM_OFF = DG_TAB_OFF + sizeof(float) * TAP_FLOATS;
@@ -443,8 +444,11 @@ __global__ void __launch_bounds__(DG_THREADS, 4)
             "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
             : "memory");
         prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
-        prefetch_l2_range(gdd, it.vbeg, it.vend, 4);
-        if (MODE == 0) prefetch_l2_range(fobs, it.vbeg, it.vend, 8);
+        // the first DG_PREFETCH visibilities' words only: whole items of all resident CTAs
+        // would not fit in L2 together (measured: the full range evicts what it fetched)
+        const int pf_end = min(it.vend, it.vbeg + DG_PREFETCH);
+        prefetch_l2_range(gdd, it.vbeg, pf_end, 4);
+        if (MODE == 0) prefetch_l2_range(fobs, it.vbeg, pf_end, 8);
     }
     fill_tap_table(cft_g, tab, DG_THREADS);
     for (int d = threadIdx.x; d < 129; d += DG_THREADS) {
