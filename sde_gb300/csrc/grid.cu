@@ -22,7 +22,6 @@ namespace {
 constexpr int GRID_THREADS = 256;
 constexpr int GLANES = 4;                          // lanes per chunk
 constexpr int GGROUPS = GRID_THREADS / GLANES;     // chunks in flight per CTA
-constexpr int GRID_AHEAD = 2;                      // record prefetch distance (visibilities)
 constexpr int GRID_MINB = 4;                       // resident CTAs per SM the kernel is built for
 // Shared copy of the tap table, one layout for both reads a 4-lane group makes per
 // visibility.  A chunk covers a pair of cells (lu0, lu0+1), so its footprint is 8 columns
@@ -73,8 +72,8 @@ __device__ __forceinline__ Taps read_taps(const float *tg, int q, uint32_t g) {
 
 // Gridding.  A chunk holds visibilities of one cell pair (lu0, lu0+1); its footprint is a
 // 7-row x 8-column window.  Lane q of a 4-lane group owns window columns q and q+4 and
-// accumulates 7 rows x 2 columns x complex in registers; the chunk's visibilities are read
-// once per group (same addresses: L1 broadcast).  The shared tile (real and imaginary
+// accumulates 7 rows x 2 columns x complex in registers; the group's lanes load four
+// consecutive records at a time and share them by shuffle.  The shared tile (real and imaginary
 // planes) receives each chunk's window once, through shared-memory atomics (a warp's 8
 // chunks share a colour class, so their windows do not overlap).
 // Grid one work item: the item's chunks into the shared tile (planar re/im planes, zero on
@@ -86,13 +85,26 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
                                           const float4 *__restrict__ rec, const float *tab,
                                           float *tre, float *tim, float2 *raw, float2 *raw_lo,
                                           int pitch, int ntu, int nu, int nv) {
+    // Cooperative record loads: lane q of a group loads record k+q of its chunk (one
+    // 64-byte run per group instead of one record broadcast to four lanes), and the group
+    // exchanges each visibility's weighted value and offset word by shuffle.  Every lane of
+    // a warp runs the same number of chunk rounds and visibility steps (the warp's longest
+    // chunk; shorter chunks read zero-weight records), so full-warp shuffles are safe.
     const int q = threadIdx.x & (GLANES - 1);
     const int grp = threadIdx.x / GLANES;
-    const float *tg = tab + (grp & (TAP_COPIES - 1)) * TAP_ROW;  // this group's copy
-    for (int c = it.cbeg + grp; c < it.cend; c += GGROUPS) {
-        const uint2 ch = chunks[c];
-        const int start = (int)ch.x, cell = (int)(ch.y & 4095u), len = (int)(ch.y >> 16);
+    const int gbase = threadIdx.x & 28;
+    const float *tg = tab;
+    constexpr uint32_t FULL = 0xffffffffu;
+    const int rounds = (it.cend - it.cbeg + GGROUPS - 1) / GGROUPS;
+    for (int rr = 0; rr < rounds; rr++) {
+        const int c = it.cbeg + rr * GGROUPS + grp;
+        const bool live = c < it.cend;
+        const uint2 ch = live ? chunks[c] : make_uint2(0u, 0u);
+        const int start = (int)ch.x, cell = (int)(ch.y & 4095u), len = live ? (int)(ch.y >> 16) : 0;
         const int lu = cell & 63, lv = cell >> 6;
+        int wlen = len;
+#pragma unroll
+        for (int d = 4; d < 32; d <<= 1) wlen = max(wlen, __shfl_xor_sync(FULL, wlen, d));
         float a0r[NTAP], a0i[NTAP], a1r[NTAP], a1i[NTAP];
 #pragma unroll
         for (int b = 0; b < NTAP; b++) {
@@ -103,48 +115,42 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
                 a1i[b] = 0.f;
             }
         }
-        // GRID_AHEAD visibilities ahead: their records and values load while this one
-        // accumulates (a register ring, indexed by constants after unrolling)
         const float4 *pr = rec + start;
-        float4 rb[GRID_AHEAD];
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 cur = q < len ? pr[q] : zero;
+        for (int k = 0; k < wlen; k += GLANES) {
+            const float4 nxt = k + GLANES + q < len ? pr[k + GLANES + q] : zero;
+            const uint32_t gq = __float_as_uint(cur.y);
+            const float frq = PSF ? cur.x : cur.x * cur.z, fiq = PSF ? 0.f : cur.x * cur.w;
 #pragma unroll
-        for (int j = 0; j < GRID_AHEAD; j++) rb[j] = j < len ? pr[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int k = 0; k < len; k += GRID_AHEAD) {
-#pragma unroll
-            for (int j = 0; j < GRID_AHEAD; j++) {
-                if (k + j >= len) break;
-                const float4 r = rb[j];
-                if (k + j + GRID_AHEAD < len) rb[j] = pr[k + j + GRID_AHEAD];
-                const uint32_t g = __float_as_uint(r.y);
-                const float w = r.x;
+            for (int u = 0; u < GLANES; u++) {
+                const uint32_t g = __shfl_sync(FULL, gq, gbase + u);
+                const float fr = __shfl_sync(FULL, frq, gbase + u);
+                const float fi = PSF ? 0.f : __shfl_sync(FULL, fiq, gbase + u);
                 const Taps t = read_taps(tg, q, g);
                 const float2 gu = t.gu;
-                const float *gv = t.gv;
-                float fr = w, fi = 0.f;
-                if (!PSF) {
-                    fr = w * r.z;
-                    fi = w * r.w;
-                }
                 const float h0r = gu.x * fr, h1r = gu.y * fr;
                 const float h0i = gu.x * fi, h1i = gu.y * fi;
 #pragma unroll
                 for (int b = 0; b < NTAP; b++) {
-                    a0r[b] = fmaf(gv[b], h0r, a0r[b]);
-                    a1r[b] = fmaf(gv[b], h1r, a1r[b]);
+                    a0r[b] = fmaf(t.gv[b], h0r, a0r[b]);
+                    a1r[b] = fmaf(t.gv[b], h1r, a1r[b]);
                     if (!PSF) {
-                        a0i[b] = fmaf(gv[b], h0i, a0i[b]);
-                        a1i[b] = fmaf(gv[b], h1i, a1i[b]);
+                        a0i[b] = fmaf(t.gv[b], h0i, a0i[b]);
+                        a1i[b] = fmaf(t.gv[b], h1i, a1i[b]);
                     }
                 }
             }
+            cur = nxt;
         }
+        if (!live) continue;
 #pragma unroll
         for (int b = 0; b < NTAP; b++) {
-            float *rr = &tre[(lv + b) * STILE + lu + q];
+            float *rr_ = &tre[(lv + b) * STILE + lu + q];
             float *ri = &tim[(lv + b) * STILE + lu + q];
-            atomicAdd(rr, a0r[b]);
+            atomicAdd(rr_, a0r[b]);
             if (!PSF) atomicAdd(ri, a0i[b]);
-            atomicAdd(rr + 4, a1r[b]);
+            atomicAdd(rr_ + 4, a1r[b]);
             if (!PSF) atomicAdd(ri + 4, a1i[b]);
         }
     }
