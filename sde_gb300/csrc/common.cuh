@@ -228,7 +228,11 @@ struct FftBatch {
     const float *scale[FFT_MAXB];
 };
 size_t grid_smem_bytes();
-int grid_ctas_per_sm();  // resident persistent gridding CTAs per SM
+int grid_ctas_per_sm();
+// 2-D FP32 tensor map for cp.async.bulk.tensor (grid.cu): width floats x rows, row pitch in
+// bytes, box box_w x box_h; out-of-range elements read as zero and are not written
+int encode_tmap_f32_2d(CUtensorMap *map, const void *base, uint64_t width, uint64_t rows,
+                       uint64_t row_bytes, uint32_t box_w, uint32_t box_h);  // resident persistent gridding CTAs per SM
 int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
                       const int64_t *d_item_start, int nplans, unsigned long long *d_counter,
                       const float *cft, int nctas);

@@ -707,6 +707,223 @@ __global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB)
     }
 }
 
+// ---- column pass fed by TMA -----------------------------------------------------------
+// Two columns per CTA, held in shared memory as (col0, col1) complex pairs, one float4 per
+// row: TMA box loads bring the 16 bytes of each row in (no load instructions, no L1
+// wavefronts per row), every thread runs its radix-16 butterfly on both columns with one
+// set of twiddles, and TMA box stores write the columns back.  The first pass reads in row
+// order (FFTX1D's cyclic shift and, forward, the rows outside the image read as zero), the
+// middle passes use an XOR swizzle for float4 elements, and the last pass writes in row
+// order (inverse: times 1/N).  The tensor map's width (2*NU floats) keeps the loads of the
+// padding column at zero and the stores out of it.
+__device__ __forceinline__ int swz4(int i) { return i ^ ((i >> 4) & 7); }
+
+template <int R, bool INV>
+__device__ __forceinline__ void twiddle_powers2(float2 *a, float2 *b, const float2 *__restrict__ tw,
+                                                size_t i1, size_t i4) {
+    float2 w1 = __ldg(&tw[i1]);
+    if (!INV) w1.y = -w1.y;
+    a[1] = cmul(a[1], w1);
+    b[1] = cmul(b[1], w1);
+    if (R == 2) return;
+    const float2 w2 = cmul(w1, w1);
+    a[2] = cmul(a[2], w2);
+    b[2] = cmul(b[2], w2);
+    const float2 w3 = cmul(w2, w1);
+    a[3] = cmul(a[3], w3);
+    b[3] = cmul(b[3], w3);
+    if (R == 4) return;
+    float2 w4 = __ldg(&tw[i4]);
+    if (!INV) w4.y = -w4.y;
+    float2 wa = w4;
+#pragma unroll
+    for (int q = 1; q < R / 4; q++) {
+        if (q > 1) wa = cmul(wa, w4);
+        const float2 x1 = cmul(wa, w1), x2 = cmul(wa, w2), x3 = cmul(wa, w3);
+        a[4 * q] = cmul(a[4 * q], wa);
+        b[4 * q] = cmul(b[4 * q], wa);
+        a[4 * q + 1] = cmul(a[4 * q + 1], x1);
+        b[4 * q + 1] = cmul(b[4 * q + 1], x1);
+        a[4 * q + 2] = cmul(a[4 * q + 2], x2);
+        b[4 * q + 2] = cmul(b[4 * q + 2], x2);
+        a[4 * q + 3] = cmul(a[4 * q + 3], x3);
+        b[4 * q + 3] = cmul(b[4 * q + 3], x3);
+    }
+}
+
+template <int LOGN, int LOGR, int LOGNS, bool INV, int T, bool FIRST, bool LAST>
+__device__ __forceinline__ void st_pass2(float4 *s, const float2 *__restrict__ tw, int r0, int r1) {
+    constexpr int N = 1 << LOGN, R = 1 << LOGR, NB = 1 << (LOGN - LOGR), NS = 1 << LOGNS;
+    constexpr int PER = (NB + T - 1) / T;
+    constexpr int TSHIFT = LOGN - LOGNS - LOGR;
+    constexpr int C = N / 2 - 1;  // (N+1)/2 - 1 for even N
+    float2 a[PER][R], b[PER][R];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int j = threadIdx.x + i * T;
+        if (NB % T == 0 || j < NB) {
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int idx = j + r * NB;
+                float4 x;
+                if (FIRST) {
+                    const int v = (idx + C) & (N - 1);
+                    x = s[v];
+                    if (!INV && (v < r0 || v >= r1)) x = make_float4(0.f, 0.f, 0.f, 0.f);
+                } else {
+                    x = s[swz4(idx)];
+                }
+                a[i][r] = make_float2(x.x, x.y);
+                b[i][r] = make_float2(x.z, x.w);
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int j = threadIdx.x + i * T;
+        if (NB % T == 0 || j < NB) {
+            const int jm = j & (NS - 1);
+            if (LOGNS > 0 && jm)
+                twiddle_powers2<R, INV>(a[i], b[i], tw, (size_t)(jm << TSHIFT), (size_t)((4 * jm) << TSHIFT));
+            dftR<R, INV>(a[i]);
+            dftR<R, INV>(b[i]);
+            const int od = ((j >> LOGNS) << (LOGNS + LOGR)) + jm;
+            const float sc = INV ? 1.0f / (float)N : 1.0f;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int p = od + r * NS;
+                if (LAST) {
+                    float4 y = make_float4(a[i][r].x, a[i][r].y, b[i][r].x, b[i][r].y);
+                    if (INV) {
+                        y.x *= sc; y.y *= sc; y.z *= sc; y.w *= sc;
+                    }
+                    s[(p + C) & (N - 1)] = y;
+                } else {
+                    s[swz4(p)] = make_float4(a[i][r].x, a[i][r].y, b[i][r].x, b[i][r].y);
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <int LOGN, int LOGNS, bool INV, int T>
+struct St2Passes {
+    static __device__ __forceinline__ void run(float4 *s, const float2 *__restrict__ tw, int r0, int r1) {
+        constexpr int REM = LOGN - LOGNS;
+        constexpr int LOGR = REM >= 4 ? 4 : REM;
+        st_pass2<LOGN, LOGR, LOGNS, INV, T, LOGNS == 0, LOGNS + LOGR == LOGN>(s, tw, r0, r1);
+        St2Passes<LOGN, LOGNS + LOGR, INV, T>::run(s, tw, r0, r1);
+    }
+};
+template <int LOGN, bool INV, int T>
+struct St2Passes<LOGN, LOGN, INV, T> {
+    static __device__ __forceinline__ void run(float4 *, const float2 *__restrict__, int, int) {}
+};
+
+template <int LOGN>
+struct ColTma {
+    static constexpr int N = 1 << LOGN;
+    static constexpr int T = N / 16 < 128 ? 128 : N / 16;  // one radix-16 butterfly per thread
+    static constexpr int BOX = N < 256 ? N : 256;          // rows per TMA box
+    static constexpr size_t SMEM = sizeof(float4) * (size_t)N + 16;
+    static constexpr int MINB = 2 * SMEM <= 227 * 1024 ? 2 : 1;  // resident CTAs (shared memory)
+};
+
+template <int LOGN, bool INV>
+__global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
+    k_col_fft_tma(const __grid_constant__ CUtensorMap tmap, const float2 *__restrict__ tw, int r0,
+                  int r1, int *status) {
+    using S = ColTma<LOGN>;
+    constexpr int N = S::N, BOX = S::BOX;
+    extern __shared__ __align__(128) unsigned char smem_ct[];
+    float4 *s = reinterpret_cast<float4 *>(smem_ct);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_ct + sizeof(float4) * (size_t)N);
+    const uint32_t sb = (uint32_t)__cvta_generic_to_shared(s);
+    const uint32_t bb = (uint32_t)__cvta_generic_to_shared(bar);
+    const int x = 4 * blockIdx.x;  // first float of this CTA's two complex columns
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bb));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        asm volatile("fence.proxy.async.shared::cta;");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bb),
+                     "r"((uint32_t)(sizeof(float4) * N)));
+        for (int b = 0; b < N / BOX; b++)
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                " [%0], [%1, {%2, %3}], [%4];" ::"r"(sb + (uint32_t)(b * BOX * sizeof(float4))),
+                "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(b * BOX), "r"(bb)
+                : "memory");
+    }
+    {
+        uint32_t done = 0;
+        for (int spin = 0; spin < (1 << 24) && !done; spin++) {
+            asm volatile(
+                "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;"
+                " selp.u32 %0, 1, 0, p; }"
+                : "=r"(done)
+                : "r"(bb)
+                : "memory");
+        }
+        if (!done) {
+            atomicExch(&status[STATUS_TIMEOUT], 1);
+            return;
+        }
+    }
+    St2Passes<LOGN, 0, INV, S::T>::run(s, tw, r0, r1);
+    // the last pass's generic stores must be visible to the bulk copies that read them
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < N / BOX; b++)
+            asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                             reinterpret_cast<uint64_t>(&tmap)),
+                         "r"(x), "r"(b * BOX), "r"(sb + (uint32_t)(b * BOX * sizeof(float4)))
+                         : "memory");
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    }
+}
+
+template <int LOGN>
+cudaError_t launch_col_tma(const CUtensorMap &map, int nu, const float2 *tw, bool inverse, int r0,
+                           int r1, int *status, cudaStream_t st) {
+    using S = ColTma<LOGN>;
+    const unsigned nb = (unsigned)((nu + 1) / 2);
+    if (inverse) {
+        cudaError_t e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+        if (e != cudaSuccess) return e;
+        k_col_fft_tma<LOGN, true><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+        if (e != cudaSuccess) return e;
+        k_col_fft_tma<LOGN, false><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status);
+    }
+    return cudaGetLastError();
+}
+
+// Column pass of one grid through the TMA kernel when 2^logn has an instance (2048..8192).
+bool col_fft_tma(sde_ctx *ctx, int logn, float2 *grid, int pitch, int nu, int nv, const float2 *tw,
+                 bool inverse, int r0, int r1, cudaError_t *err, int *rc) {
+    if (logn < 11 || logn > 13) return false;
+    CUtensorMap map;
+    *rc = encode_tmap_f32_2d(&map, grid, (uint64_t)nu * 2, (uint64_t)nv, (uint64_t)pitch * 8, 4,
+                             (uint32_t)(nv < 256 ? nv : 256));
+    if (*rc != SDE_OK) return true;
+    switch (logn) {
+        case 11: *err = launch_col_tma<11>(map, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
+        case 12: *err = launch_col_tma<12>(map, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
+        default: *err = launch_col_tma<13>(map, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
+    }
+    return true;
+}
+
 // Launchers for the compile-time shapes: false if the size has no instance.
 template <int LOGN>
 cudaError_t launch_col_t(const FftBatch &bt, int nbatch, int pitch, int nu, const float2 *tw,
@@ -847,7 +1064,10 @@ int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, in
         cudaError_t e = cudaSuccess;
         FftBatch bt{};
         bt.grid[0] = (float2 *)grid;
-        if (!col_fft_t(ilog2(nv), bt, 1, pitch, nu, twv, true, 0, nv, ctx->stream, &e)) {
+        int trc = SDE_OK;
+        if (col_fft_tma(ctx, ilog2(nv), (float2 *)grid, pitch, nu, nv, twv, true, 0, nv, &e, &trc)) {
+            SDE_TRY(trc);
+        } else if (!col_fft_t(ilog2(nv), bt, 1, pitch, nu, twv, true, 0, nv, ctx->stream, &e)) {
             const int lcc = col_logcc(nv), cc = 1 << lcc;
             const size_t smc = sizeof(float2) * (size_t)cc * nv;
             SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
@@ -912,7 +1132,11 @@ int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fn
     cudaError_t e = cudaSuccess;
     FftBatch bt{};
     bt.grid[0] = (float2 *)grid;
-    if (!col_fft_t(ilog2(nv), bt, 1, pitch, nu, twv, false, ibegy, ibegy + ny, ctx->stream, &e)) {
+    int trc = SDE_OK;
+    if (col_fft_tma(ctx, ilog2(nv), (float2 *)grid, pitch, nu, nv, twv, false, ibegy, ibegy + ny, &e,
+                    &trc)) {
+        SDE_TRY(trc);
+    } else if (!col_fft_t(ilog2(nv), bt, 1, pitch, nu, twv, false, ibegy, ibegy + ny, ctx->stream, &e)) {
         const int lcc = col_logcc(nv), cc = 1 << lcc;
         const size_t smc = sizeof(float2) * (size_t)cc * nv;
         SDE_CUDA_TRY(cudaFuncSetAttribute(k_col_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));

@@ -727,13 +727,25 @@ __global__ void k_set_vis(const float2 *__restrict__ vis_user, const uint32_t *_
     *rec_res(rec, p) = make_float2(fr, fi);
 }
 
-typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                    const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                    const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
 int make_grid_tmap(CUtensorMap *map, const float *grid, int pitch, int nv) {
-    static PFN_encodeTiled fn = nullptr;
+    return encode_tmap_f32_2d(map, grid, (uint64_t)pitch * 2, (uint64_t)nv, (uint64_t)pitch * 8,
+                              STILE * 2, STILE);
+}
+
+size_t grid_smem() { return sizeof(float) * (2 * STILE * STILE + TAP_FLOATS); }
+size_t degrid_smem() { return DG_BAR_OFF + 16; }
+
+}  // namespace
+
+// A 2-D FP32 tensor map (width floats x rows, row pitch in bytes, box box_w x box_h) for
+// cp.async.bulk.tensor; out-of-range elements read as zero and are not written.
+int encode_tmap_f32_2d(CUtensorMap *map, const void *base, uint64_t width, uint64_t rows,
+                       uint64_t row_bytes, uint32_t box_w, uint32_t box_h) {
+    typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                      const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                      const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                      CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeTiledFn fn = nullptr;
     if (!fn) {
         cudaDriverEntryPointQueryResult q;
         void *p = nullptr;
@@ -743,18 +755,18 @@ int make_grid_tmap(CUtensorMap *map, const float *grid, int pitch, int nv) {
             sde_set_error("cuTensorMapEncodeTiled unavailable");
             return SDE_ECUDA;
         }
-        fn = (PFN_encodeTiled)p;
+        fn = (EncodeTiledFn)p;
     }
-    if (((uintptr_t)grid & 15u) != 0 || (pitch * 8) % 16 != 0) {
-        sde_set_error("grid not 16-byte aligned for TMA");
+    if (((uintptr_t)base & 15u) != 0 || row_bytes % 16 != 0 || (box_w * 4) % 16 != 0) {
+        sde_set_error("array not 16-byte aligned for TMA");
         return SDE_EINVAL;
     }
-    cuuint64_t dims[2] = {(cuuint64_t)pitch * 2, (cuuint64_t)nv};
-    cuuint64_t strides[1] = {(cuuint64_t)pitch * 8};
-    cuuint32_t box[2] = {(cuuint32_t)(STILE * 2), (cuuint32_t)STILE};
+    cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)row_bytes};
+    cuuint32_t box[2] = {box_w, box_h};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)grid, dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides,
+                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         sde_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -762,11 +774,6 @@ int make_grid_tmap(CUtensorMap *map, const float *grid, int pitch, int nv) {
     }
     return SDE_OK;
 }
-
-size_t grid_smem() { return sizeof(float) * (2 * STILE * STILE + TAP_FLOATS); }
-size_t degrid_smem() { return DG_BAR_OFF + 16; }
-
-}  // namespace
 
 // ---------------------------------------------------------------------------------------
 int plan_build_cft(sde_plan *pl) {

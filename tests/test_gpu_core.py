@@ -78,7 +78,10 @@ def test_grid_matches_grdh2d(gpu_ctx, orc, obs_small, obs_shift, case, psf):
     plan.close()
 
 
-@pytest.mark.parametrize("n,fnu", [(256, 256), (200, 256), (128, 128)])
+# 2048 and up: the column pass fed by TMA (two columns per CTA); 1800 in 2048: the forward
+# pass's rows outside the image
+@pytest.mark.parametrize("n,fnu", [(256, 256), (200, 256), (128, 128), (2048, 2048), (1800, 2048),
+                                   (4096, 4096), (8192, 8192)])
 def test_fft_both_directions(gpu_ctx, orc, n, fnu):
     ctx = gpu_ctx
     from sde_gb300.imaging import fftpwr2
