@@ -805,14 +805,22 @@ def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis):
     dt = (time.perf_counter() - t0) / args.e2e_steps
     gb = nu * nv * 8
     img = n * n * 4
-    h2d = 24 * nvis + gb + img + img + img + (24 + 12) * nvis + gb
-    d2h = gb + img + gb + img + img + gb + 12 * nvis
+    # grdh2d_: VIS, WT, U, V, W up, grid down; fftr2d_(-1): grid up, image and the
+    # column-transformed grid down; pixcor2d_ x2: image up and down; fftr2d_(+1): image up,
+    # grid down; grddeh2d_: U, V, W, WT and the model grid up, VIS down -- plus VIS and WT up
+    # when some WT <= 0 (the points GRDDEH2D leaves as they are), and WT down when a point
+    # was not degridded (WT negated)
+    flagged = bool((hwt <= 0).any().item())
+    negated = bool(((hwt2 < 0) & (hwt > 0)).any().item())
+    h2d = 24 * nvis + gb + img + img + img + 16 * nvis + gb + (12 * nvis if flagged else 0)
+    d2h = gb + img + gb + img + img + gb + 8 * nvis + (4 * nvis if negated else 0)
     return {"value": nvis / dt / 1e6, "unit": "Mvis/s", "ms_per_step": dt * 1e3,
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "path": "grdh2d_ -> fftr2d_(-1) -> pixcor2d_ x2 -> fftr2d_(+1) -> grddeh2d_, pinned "
                     "host arrays; every call uploads its inputs and downloads its outputs; "
                     "GRDH2D/GRDDEH2D reuse their tile plan when U, V, W, WT are bitwise "
                     "unchanged (compared on the device)",
+            "flagged_wt": flagged, "negated_wt": negated,
             "plan_cache": _shim_stats(L)}
 
 
