@@ -79,44 +79,47 @@ def test_grid_matches_grdh2d(gpu_ctx, orc, obs_small, obs_shift, case, psf):
 
 
 # 2048 and up: the column pass fed by TMA (two columns per CTA); 1800 in 2048: the forward
-# pass's rows outside the image
-@pytest.mark.parametrize("n,fnu", [(256, 256), (200, 256), (128, 128), (2048, 2048), (1800, 2048),
-                                   (4096, 4096), (8192, 8192)])
-def test_fft_both_directions(gpu_ctx, orc, n, fnu):
+# pass's rows outside the image; FFTs of 4096 and 8192: the row passes on row pairs fed by
+# bulk copies (3600 wide: an image narrower than the FFT; 4095 rows: a pair with one row)
+@pytest.mark.parametrize("n,fnu,ny", [(256, 256, 256), (200, 256, 200), (128, 128, 128),
+                                      (2048, 2048, 2048), (1800, 2048, 1800), (4096, 4096, 4096),
+                                      (3600, 4096, 4095), (8192, 8192, 8192)])
+def test_fft_both_directions(gpu_ctx, orc, n, fnu, ny):
     ctx = gpu_ctx
     from sde_gb300.imaging import fftpwr2
-    rng = np.random.default_rng(n)
+    rng = np.random.default_rng(n + ny)
+    nx = n
     nv, nu = fnu, fnu // 2 + 1
     pitch = (nu + 3) & ~3
     X = (rng.standard_normal((nv, nu)) + 1j * rng.standard_normal((nv, nu))).astype(np.complex64)
-    ref_img, _ = orc.fftr2d(n, n, fnu, nv, -1, xarray=X)
+    ref_img, _ = orc.fftr2d(nx, ny, fnu, nv, -1, xarray=X)
     Xp = np.zeros((nv, pitch), np.complex64)
     Xp[:, :nu] = X
     grid = _dev(ctx, Xp)
-    img = ctx.empty((n, n), ctx.torch.float32)
+    img = ctx.empty((ny, nx), ctx.torch.float32)
 
     class G:
         pass
     gg = G()
-    gg.pitch, gg.nx, gg.ny, gg.fnu, gg.nv = pitch, n, n, fnu, nv
+    gg.pitch, gg.nx, gg.ny, gg.fnu, gg.nv = pitch, nx, ny, fnu, nv
     ctx.image_from_grid(gg, grid, img, correct=False)
     assert rel_err(img.cpu().numpy(), ref_img) < 2e-6
     # forward
-    im = rng.standard_normal((n, n)).astype(np.float32)
-    _, refX = orc.fftr2d(n, n, fnu, nv, +1, rarray=im)
+    im = rng.standard_normal((ny, nx)).astype(np.float32)
+    _, refX = orc.fftr2d(nx, ny, fnu, nv, +1, rarray=im)
     grid2 = ctx.zeros((nv, pitch), ctx.torch.complex64)
     ctx.grid_from_image(gg, _dev(ctx, im), grid2, correct=False)
     assert rel_err(grid2.cpu().numpy()[:, :nu], refX) < 2e-6
     # with the grid correction fused
-    ccflen = 1 + fftpwr2(n) // 2
+    ccflen = 1 + fftpwr2(max(nx, ny)) // 2
     ccf = orc.grdccf(ccflen)
-    cen = float((n + 1) // 2)
+    cenx, ceny = float((nx + 1) // 2), float((ny + 1) // 2)
     ctx.image_from_grid(gg, _dev(ctx, Xp), img, correct=True)
-    ref_c = orc.pixcor2d(ref_img, ccf, cen, cen)
-    w = _window(n)
-    assert rel_err(img.cpu().numpy()[w, w], ref_c[w, w]) < 2e-6
-    corrected = orc.pixcor2d(im, ccf, cen, cen)
-    _, refX2 = orc.fftr2d(n, n, fnu, nv, +1, rarray=corrected)
+    ref_c = orc.pixcor2d(ref_img, ccf, cenx, ceny)
+    wx, wy = _window(nx), _window(ny)
+    assert rel_err(img.cpu().numpy()[wy, wx], ref_c[wy, wx]) < 2e-6
+    corrected = orc.pixcor2d(im, ccf, cenx, ceny)
+    _, refX2 = orc.fftr2d(nx, ny, fnu, nv, +1, rarray=corrected)
     ctx.grid_from_image(gg, _dev(ctx, im), grid2, correct=True)
     assert rel_err(grid2.cpu().numpy()[:, :nu], refX2) < 2e-6
 
