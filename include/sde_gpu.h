@@ -305,8 +305,8 @@ int sde_uvmap(sde_ctx *ctx, const sde_uvmap_args *a, int64_t nvis, const float *
 /* ---- Batches of plans: a mosaic's pointings or a group of served jobs ------------------
  * No counterpart entry point in the reference: task/mosclean.f images its pointings one
  * after another and forms the linear mosaic (task/mosclean.f:413-432); a batch images all
- * of them together.  Every plan must come from ctx and hold a power-of-two grid large
- * enough for its nx[i] x ny[i] image.  The batch owns per plan a grid, a PSF image and a
+ * of them together.  At most 65535 plans; every plan must come from ctx and hold a
+ * power-of-two grid large enough for its nx[i] x ny[i] image.  The batch owns per plan a grid, a PSF image and a
  * dirty image (device, row-major nx x ny).
  *   sde_batch_psf      grid and transform every PSF; records each PSF peak.
  *   sde_batch_dirty    dirty image of every plan, divided by its PSF peak (uvmap's
@@ -320,7 +320,8 @@ int sde_uvmap(sde_ctx *ctx, const sde_uvmap_args *a, int64_t nvis, const float *
  *   sde_batch_set_mosaic  linear mosaic mnx x mny: pointing i's image centre ((n+1)/2,
  *                      1-based) lands on mosaic pixel (cx[i], cy[i]); its primary beam is a
  *                      Gaussian of FWHM fwhm_px[i] pixels; mosaic = sum wt PB I / sum wt PB^2
- *                      where sum wt PB^2 > clip * its maximum, else 0.
+ *                      where sum wt PB^2 > clip * its maximum, else 0 (the denominator
+ *                      and its clip are formed here, once per layout).
  *   sde_batch_image    device pointer: i = -1 the mosaic; which 0 the dirty image of plan
  *                      i, 1 its PSF, 2 its PSF peak (one float). */
 typedef struct sde_batch sde_batch;

@@ -25,34 +25,70 @@ struct MosaicPointing {
     int cx, cy;          // mosaic pixel of the image centre pixel ((n+1)/2, 1-based)
     float pbk;           // 4 ln2 / FWHM^2 (FWHM in pixels): PB = exp(-pbk r^2)
     float wt;            // pointing weight (SUMWT of the pointing)
+    int64_t block0;      // first block of this pointing in the flattened launches
 };
 
-// num += wt PB image, den += wt PB^2 over each pointing's pixels (blockIdx.y = pointing)
-__global__ void k_mosaic_accum(const MosaicPointing *__restrict__ pts, int mnx, int mny, float *num,
-                               float *den) {
-    const MosaicPointing p = pts[blockIdx.y];
-    const int64_t npix = (int64_t)p.nx * p.ny;
+// Flattened over the pointings' pixels: blk[b] = the pointing of block b, 1024 pixels per
+// block.  The primary beam of a pixel of pointing p and its mosaic pixel.
+struct MosaicPixel {
+    bool in;
+    int64_t m;  // mosaic index
+    float pb;
+    int64_t k;  // pixel of the pointing's image
+};
+__device__ __forceinline__ MosaicPixel mosaic_pixel(const MosaicPointing &p, int64_t k, int mnx, int mny) {
+    MosaicPixel r{false, 0, 0.f, k};
+    if (k >= (int64_t)p.nx * p.ny) return r;
     const int cenx = (p.nx + 1) / 2 - 1, ceny = (p.ny + 1) / 2 - 1;
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < npix;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        const int iy = (int)(k / p.nx), ix = (int)(k - (int64_t)iy * p.nx);
-        const int mx = p.cx - 1 + ix - cenx, my = p.cy - 1 + iy - ceny;
-        if (mx < 0 || mx >= mnx || my < 0 || my >= mny) continue;
-        const float dx = (float)(ix - cenx), dy = (float)(iy - ceny);
-        const float pb = expf(-p.pbk * (dx * dx + dy * dy));
-        const int64_t m = (int64_t)my * mnx + mx;
-        atomicAdd(&num[m], p.wt * pb * p.image[k]);
-        atomicAdd(&den[m], p.wt * pb * pb);
+    const int iy = (int)(k / p.nx), ix = (int)(k - (int64_t)iy * p.nx);
+    const int mx = p.cx - 1 + ix - cenx, my = p.cy - 1 + iy - ceny;
+    if (mx < 0 || mx >= mnx || my < 0 || my >= mny) return r;
+    const float dx = (float)(ix - cenx), dy = (float)(iy - ceny);
+    r.in = true;
+    r.m = (int64_t)my * mnx + mx;
+    r.pb = expf(-p.pbk * (dx * dx + dy * dy));
+    return r;
+}
+
+// num += wt PB image over every pointing's pixels (task/mosclean.f:413-432's numerator)
+__global__ void __launch_bounds__(256) k_mosaic_num(const MosaicPointing *__restrict__ pts,
+                                                    const uint16_t *__restrict__ blk, int mnx, int mny,
+                                                    float *num) {
+    const MosaicPointing p = pts[blk[blockIdx.x]];
+    const int64_t base = (int64_t)(blockIdx.x - p.block0) * BATCH_BLOCK_CELLS;
+#pragma unroll
+    for (int j = 0; j < BATCH_BLOCK_CELLS / 256; j++) {
+        const MosaicPixel q = mosaic_pixel(p, base + j * 256 + threadIdx.x, mnx, mny);
+        if (q.in) atomicAdd(&num[q.m], p.wt * q.pb * p.image[q.k]);
     }
 }
 
-// mosaic = num / den where the summed sensitivity den exceeds clip * max(den) (else 0)
-__global__ void k_mosaic_div(const float *__restrict__ num, const float *__restrict__ den,
-                             int64_t n, const float *__restrict__ denmax, float clip, float *out) {
+// den += wt PB^2 (the denominator; once per layout)
+__global__ void __launch_bounds__(256) k_mosaic_den(const MosaicPointing *__restrict__ pts,
+                                                    const uint16_t *__restrict__ blk, int mnx, int mny,
+                                                    float *den) {
+    const MosaicPointing p = pts[blk[blockIdx.x]];
+    const int64_t base = (int64_t)(blockIdx.x - p.block0) * BATCH_BLOCK_CELLS;
+#pragma unroll
+    for (int j = 0; j < BATCH_BLOCK_CELLS / 256; j++) {
+        const MosaicPixel q = mosaic_pixel(p, base + j * 256 + threadIdx.x, mnx, mny);
+        if (q.in) atomicAdd(&den[q.m], p.wt * q.pb * q.pb);
+    }
+}
+
+// den -> 1/den where den > clip * max(den), else 0 (in place)
+__global__ void k_mosaic_invden(float *den, int64_t n, const float *__restrict__ denmax, float clip) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const float d = den[k];
-    out[k] = (d > 0.f && d > clip * *denmax) ? num[k] / d : 0.f;
+    den[k] = (d > 0.f && d > clip * *denmax) ? 1.0f / d : 0.f;
+}
+
+__global__ void k_mosaic_scale(const float *__restrict__ num, const float *__restrict__ invden,
+                               int64_t n, float *out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    out[k] = num[k] * invden[k];
 }
 
 __global__ void k_max_batch(float *const *__restrict__ images, const int64_t *__restrict__ npix,
@@ -98,6 +134,8 @@ struct sde_batch {
     int64_t *d_item_start = nullptr;
     unsigned long long *d_counter = nullptr;
     FinalizeDesc *d_fin = nullptr;
+    uint16_t *d_fin_blk = nullptr;             // grid of each block of the flattened finalize
+    int64_t fin_nblk = 0;
     float **d_psf_ptrs = nullptr;
     int64_t *d_npix = nullptr;
     int64_t max_cells = 0;
@@ -109,7 +147,11 @@ struct sde_batch {
     int mnx = 0, mny = 0;
     float clip = 0.f;
     MosaicPointing *d_pts = nullptr;
-    float *d_num = nullptr, *d_den = nullptr, *d_denmax = nullptr, *d_mosaic = nullptr;
+    uint16_t *d_pts_blk = nullptr;             // pointing of each block of the mosaic launches
+    int64_t pts_nblk = 0;
+    // num = sum wt PB I (per pass); invden = 1 / sum wt PB^2 where that sum passes the clip,
+    // else 0 (fixed by the layout: computed once in sde_batch_set_mosaic)
+    float *d_num = nullptr, *d_invden = nullptr, *d_denmax = nullptr, *d_mosaic = nullptr;
     // graph of sde_batch_dirty (+ mosaic)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -140,7 +182,7 @@ int batch_grid(sde_batch *b, int psf) {
     SDE_CUDA_TRY(cudaMemsetAsync(b->raw[0], 0, b->raw_bytes, ctx->stream));
     SDE_TRY(launch_grid_batch(ctx, psf, b->comp, b->d_plans, b->d_item_start, b->n, b->d_counter,
                               ctx->d_cft, ctx->num_sms * grid_ctas_per_sm()));
-    SDE_TRY(launch_finalize_batch(ctx, b->d_fin, b->n, b->max_cells));
+    SDE_TRY(launch_finalize_batch(ctx, b->d_fin, b->d_fin_blk, b->fin_nblk));
     return SDE_OK;
 }
 
@@ -175,24 +217,16 @@ int batch_mosaic(sde_batch *b) {
     if (!b->d_pts) return SDE_OK;
     sde_ctx *ctx = b->ctx;
     const int64_t m = (int64_t)b->mnx * b->mny;
-    SDE_CUDA_TRY(cudaMemsetAsync(b->d_num, 0, sizeof(float) * 2 * (size_t)m, ctx->stream));
-    int64_t maxpix = 0;
-    for (int i = 0; i < b->n; i++) maxpix = std::max(maxpix, (int64_t)b->nx[i] * b->ny[i]);
+    SDE_CUDA_TRY(cudaMemsetAsync(b->d_num, 0, sizeof(float) * (size_t)m, ctx->stream));
     {
         KTimer kt(ctx, "mosaic_accum");
-        const unsigned gx = (unsigned)std::min<int64_t>(ceil_div(maxpix, 256), 4096);
-        k_mosaic_accum<<<dim3(gx, (unsigned)b->n), 256, 0, ctx->stream>>>(b->d_pts, b->mnx, b->mny,
-                                                                        b->d_num, b->d_den);
+        k_mosaic_num<<<(unsigned)b->pts_nblk, 256, 0, ctx->stream>>>(b->d_pts, b->d_pts_blk, b->mnx,
+                                                                    b->mny, b->d_num);
         SDE_CHECK_LAUNCH();
     }
     {
         KTimer kt(ctx, "mosaic_div");
-        SDE_CUDA_TRY(cudaMemsetAsync(b->d_denmax, 0, sizeof(float), ctx->stream));
-        k_max_nonneg<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(b->d_den, m,
-                                                                reinterpret_cast<unsigned int *>(b->d_denmax));
-        SDE_CHECK_LAUNCH();
-        k_mosaic_div<<<ceil_div(m, 256), 256, 0, ctx->stream>>>(b->d_num, b->d_den, m, b->d_denmax,
-                                                               b->clip, b->d_mosaic);
+        k_mosaic_scale<<<ceil_div(m, 256), 256, 0, ctx->stream>>>(b->d_num, b->d_invden, m, b->d_mosaic);
         SDE_CHECK_LAUNCH();
     }
     return SDE_OK;
@@ -219,6 +253,10 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
                                 const int *ny, sde_batch **out) {
     if (!ctx || n <= 0 || !plans || !nx || !ny || !out) {
         sde_set_error("sde_batch_create: bad arguments");
+        return SDE_EINVAL;
+    }
+    if (n > 65535) {  // the flattened launches index plans with 16 bits
+        sde_set_error("sde_batch_create: at most 65535 plans per batch");
         return SDE_EINVAL;
     }
     SDE_CUDA_TRY(cudaSetDevice(ctx->device));
@@ -285,6 +323,9 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
     B_TRY(batch_alloc(b, (void **)&b->d_item_start, sizeof(int64_t) * (n + 1)));
     B_TRY(batch_alloc(b, (void **)&b->d_counter, sizeof(unsigned long long)));
     B_TRY(batch_alloc(b, (void **)&b->d_fin, sizeof(FinalizeDesc) * n));
+    for (int i = 0; i < n; i++)
+        b->fin_nblk += ceil_div((int64_t)b->plans[i]->spec.nv * b->plans[i]->pitch, BATCH_BLOCK_CELLS);
+    B_TRY(batch_alloc(b, (void **)&b->d_fin_blk, sizeof(uint16_t) * (size_t)b->fin_nblk));
     B_TRY(batch_alloc(b, (void **)&b->d_psf_ptrs, sizeof(float *) * n));
     B_TRY(batch_alloc(b, (void **)&b->d_npix, sizeof(int64_t) * n));
     b->raw_bytes = raw_total;
@@ -299,16 +340,23 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
                           pl->spec.nv};
         const float scale = (float)((double)((float)(pl->spec.nu - 1) * (float)pl->spec.nv) / pl->h_lsumwt);
         hf[i] = FinalizeDesc{b->raw[i], lo, b->grid[i], pl->spec.nu, pl->spec.nv, pl->pitch,
-                             pl->spec.uorigin, pl->spec.vorigin, pl->spec.supp, scale};
+                             pl->spec.uorigin, pl->spec.vorigin, pl->spec.supp, scale, 0};
     }
     {
         std::vector<int64_t> npix(n);
         for (int i = 0; i < n; i++) npix[i] = (int64_t)b->nx[i] * b->ny[i];
+        std::vector<uint16_t> fblk((size_t)b->fin_nblk);
+        for (int i = 0, k = 0; i < n; i++) {
+            hf[i].block0 = k;
+            const int64_t nb = ceil_div((int64_t)hf[i].nv * hf[i].pitch, BATCH_BLOCK_CELLS);
+            for (int64_t j = 0; j < nb; j++) fblk[(size_t)k++] = (uint16_t)i;
+        }
         cudaStream_t st = ctx->stream;
         cudaError_t e = cudaSuccess;
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_plans, hp.data(), sizeof(BatchPlan) * n, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_item_start, start.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_fin, hf.data(), sizeof(FinalizeDesc) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_fin_blk, fblk.data(), sizeof(uint16_t) * fblk.size(), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_psf_ptrs, b->psf.data(), sizeof(float *) * n, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_npix, npix.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -364,27 +412,44 @@ extern "C" int sde_batch_set_mosaic(sde_batch *b, int mnx, int mny, const int *c
         return SDE_EINVAL;
     }
     if (!b->d_pts) {
+        for (int i = 0; i < b->n; i++)
+            b->pts_nblk += ceil_div((int64_t)b->nx[i] * b->ny[i], BATCH_BLOCK_CELLS);
         SDE_TRY(batch_alloc(b, (void **)&b->d_pts, sizeof(MosaicPointing) * b->n));
+        SDE_TRY(batch_alloc(b, (void **)&b->d_pts_blk, sizeof(uint16_t) * (size_t)b->pts_nblk));
         SDE_TRY(batch_alloc(b, (void **)&b->d_num, sizeof(float) * 2 * (size_t)mnx * mny));
         SDE_TRY(batch_alloc(b, (void **)&b->d_mosaic, sizeof(float) * (size_t)mnx * mny));
         SDE_TRY(batch_alloc(b, (void **)&b->d_denmax, sizeof(float)));
-        b->d_den = b->d_num + (size_t)mnx * mny;
+        b->d_invden = b->d_num + (size_t)mnx * mny;
     }
     std::vector<MosaicPointing> h(b->n);
-    for (int i = 0; i < b->n; i++) {
+    std::vector<uint16_t> pblk((size_t)b->pts_nblk);
+    for (int i = 0, k = 0; i < b->n; i++) {
         if (!(fwhm_px[i] > 0.f)) {
             sde_set_error("sde_batch_set_mosaic: FWHM of pointing %d must be > 0", i);
             return SDE_EINVAL;
         }
         h[i] = MosaicPointing{b->image[i], b->nx[i], b->ny[i], cx[i], cy[i],
-                              4.0f * 0.69314718f / (fwhm_px[i] * fwhm_px[i]), wt[i]};
+                              4.0f * 0.69314718f / (fwhm_px[i] * fwhm_px[i]), wt[i], k};
+        const int64_t nb = ceil_div((int64_t)b->nx[i] * b->ny[i], BATCH_BLOCK_CELLS);
+        for (int64_t j = 0; j < nb; j++) pblk[(size_t)k++] = (uint16_t)i;
     }
     b->mnx = mnx;
     b->mny = mny;
     b->clip = clip;
-    SDE_CUDA_TRY(cudaMemcpyAsync(b->d_pts, h.data(), sizeof(MosaicPointing) * b->n,
-                                 cudaMemcpyHostToDevice, b->ctx->stream));
-    SDE_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    cudaStream_t st = b->ctx->stream;
+    SDE_CUDA_TRY(cudaMemcpyAsync(b->d_pts, h.data(), sizeof(MosaicPointing) * b->n, cudaMemcpyHostToDevice, st));
+    SDE_CUDA_TRY(cudaMemcpyAsync(b->d_pts_blk, pblk.data(), sizeof(uint16_t) * pblk.size(), cudaMemcpyHostToDevice, st));
+    // the denominator and its clip depend on the layout only
+    const int64_t m = (int64_t)mnx * mny;
+    SDE_CUDA_TRY(cudaMemsetAsync(b->d_invden, 0, sizeof(float) * (size_t)m, st));
+    k_mosaic_den<<<(unsigned)b->pts_nblk, 256, 0, st>>>(b->d_pts, b->d_pts_blk, mnx, mny, b->d_invden);
+    SDE_CHECK_LAUNCH();
+    SDE_CUDA_TRY(cudaMemsetAsync(b->d_denmax, 0, sizeof(float), st));
+    k_max_nonneg<<<b->ctx->num_sms * 4, 256, 0, st>>>(b->d_invden, m, reinterpret_cast<unsigned int *>(b->d_denmax));
+    SDE_CHECK_LAUNCH();
+    k_mosaic_invden<<<ceil_div(m, 256), 256, 0, st>>>(b->d_invden, m, b->d_denmax, clip);
+    SDE_CHECK_LAUNCH();
+    SDE_CUDA_TRY(cudaStreamSynchronize(st));
     batch_drop_graph(b);  // the captured sequence changes
     return SDE_OK;
 }

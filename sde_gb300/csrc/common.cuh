@@ -219,7 +219,10 @@ struct FinalizeDesc {
     float2 *out;
     int nu, nv, pitch, uorigin, vorigin, supp;
     float scale;
+    int64_t block0;  // first block of this grid in the flattened launch
 };
+// Cells (pixels) per block of the flattened batch launches: 256 threads x 4.
+constexpr int BATCH_BLOCK_CELLS = 1024;
 // Pointers of up to FFT_MAXB same-shape transforms of one batched FFT launch (blockIdx.y).
 constexpr int FFT_MAXB = 64;
 struct FftBatch {
@@ -236,7 +239,8 @@ int encode_tmap_f32_2d(CUtensorMap *map, const void *base, uint64_t width, uint6
 int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
                       const int64_t *d_item_start, int nplans, unsigned long long *d_counter,
                       const float *cft, int nctas);
-int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, int n, int64_t max_cells);
+// finalize of n grids in one flattened launch: blk[b] = the grid of block b (nblk blocks)
+int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, const uint16_t *blk, int64_t nblk);
 // grid -> image for n same-shape grids (inverse column pass, row c2r with grid correction
 // and scale 1/scales[i] when scales[i] != NULL); SDE_EINVAL if the shape has no batched form
 int check_fft_shape(int nx, int ny, int fnu, int nv);  // SDE_EINVAL + message if unsupported

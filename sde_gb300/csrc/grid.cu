@@ -382,12 +382,18 @@ __global__ void k_finalize(const float2 *__restrict__ raw, const float2 *__restr
 }
 
 // finalize of many grids: blockIdx.y picks the grid, blocks past its size return
-__global__ void k_finalize_batch(const FinalizeDesc *__restrict__ d) {
-    const FinalizeDesc f = d[blockIdx.y];
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)f.nv * f.pitch) return;
-    f.out[idx] = finalize_cell(f.raw, f.raw_lo, idx, f.nu, f.nv, f.pitch, f.uorigin, f.vorigin,
-                               f.supp, f.scale);
+__global__ void __launch_bounds__(256) k_finalize_batch(const FinalizeDesc *__restrict__ d,
+                                                         const uint16_t *__restrict__ blk) {
+    const FinalizeDesc f = d[blk[blockIdx.x]];
+    const int64_t base = (int64_t)(blockIdx.x - f.block0) * BATCH_BLOCK_CELLS;
+    const int64_t ncell = (int64_t)f.nv * f.pitch;
+#pragma unroll
+    for (int j = 0; j < BATCH_BLOCK_CELLS / 256; j++) {
+        const int64_t idx = base + j * 256 + threadIdx.x;
+        if (idx < ncell)
+            f.out[idx] = finalize_cell(f.raw, f.raw_lo, idx, f.nu, f.nv, f.pitch, f.uorigin,
+                                       f.vorigin, f.supp, f.scale);
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -854,10 +860,10 @@ int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
     return SDE_OK;
 }
 
-int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, int n, int64_t max_cells) {
-    if (n <= 0) return SDE_OK;
+int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, const uint16_t *blk, int64_t nblk) {
+    if (nblk <= 0) return SDE_OK;
     KTimer kt(ctx, "finalize_batch");
-    k_finalize_batch<<<dim3((unsigned)ceil_div(max_cells, 256), (unsigned)n), 256, 0, ctx->stream>>>(d_desc);
+    k_finalize_batch<<<(unsigned)nblk, 256, 0, ctx->stream>>>(d_desc, blk);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
