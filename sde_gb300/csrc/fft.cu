@@ -836,10 +836,17 @@ struct ColTma {
     static constexpr int MINB = 2 * SMEM <= 227 * 1024 ? 2 : 1;  // resident CTAs (shared memory)
 };
 
+// tensor maps of up to TMA_MAXB same-shape grids of one launch (blockIdx.y)
+constexpr int TMA_MAXB = 16;
+struct TmaBatch {
+    CUtensorMap map[TMA_MAXB];
+};
+
 template <int LOGN, bool INV>
 __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
-    k_col_fft_tma(const __grid_constant__ CUtensorMap tmap, const float2 *__restrict__ tw, int r0,
+    k_col_fft_tma(const __grid_constant__ TmaBatch tb, const float2 *__restrict__ tw, int r0,
                   int r1, int *status) {
+    const CUtensorMap *tmap = &tb.map[blockIdx.y];
     using S = ColTma<LOGN>;
     constexpr int N = S::N, BOX = S::BOX;
     extern __shared__ __align__(128) unsigned char smem_ct[];
@@ -861,7 +868,7 @@ __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
             asm volatile(
                 "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(sb + (uint32_t)(b * BOX * sizeof(float4))),
-                "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(b * BOX), "r"(bb)
+                "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(b * BOX), "r"(bb)
                 : "memory");
     }
     {
@@ -886,7 +893,7 @@ __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
     if (threadIdx.x == 0) {
         for (int b = 0; b < N / BOX; b++)
             asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
-                             reinterpret_cast<uint64_t>(&tmap)),
+                             reinterpret_cast<uint64_t>(tmap)),
                          "r"(x), "r"(b * BOX), "r"(sb + (uint32_t)(b * BOX * sizeof(float4)))
                          : "memory");
         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
@@ -895,10 +902,10 @@ __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
 }
 
 template <int LOGN>
-cudaError_t launch_col_tma(const CUtensorMap &map, int nu, const float2 *tw, bool inverse, int r0,
-                           int r1, int *status, cudaStream_t st) {
+cudaError_t launch_col_tma(const TmaBatch &map, int nbatch, int nu, const float2 *tw, bool inverse,
+                           int r0, int r1, int *status, cudaStream_t st) {
     using S = ColTma<LOGN>;
-    const unsigned nb = (unsigned)((nu + 1) / 2);
+    const dim3 nb((unsigned)((nu + 1) / 2), (unsigned)nbatch);
     if (inverse) {
         cudaError_t e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, true>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
@@ -913,18 +920,25 @@ cudaError_t launch_col_tma(const CUtensorMap &map, int nu, const float2 *tw, boo
     return cudaGetLastError();
 }
 
-// Column pass of one grid through the TMA kernel when 2^logn has an instance (2048..8192).
-bool col_fft_tma(sde_ctx *ctx, int logn, float2 *grid, int pitch, int nu, int nv, const float2 *tw,
-                 bool inverse, int r0, int r1, cudaError_t *err, int *rc) {
+// Column pass of n same-shape grids through the TMA kernel when 2^logn has an instance
+// (2048..8192), TMA_MAXB grids per launch.
+bool col_fft_tma(sde_ctx *ctx, int logn, float2 *const *grids, int n, int pitch, int nu, int nv,
+                 const float2 *tw, bool inverse, int r0, int r1, cudaError_t *err, int *rc) {
     if (logn < 11 || logn > 13) return false;
-    CUtensorMap map;
-    *rc = encode_tmap_f32_2d(&map, grid, (uint64_t)nu * 2, (uint64_t)nv, (uint64_t)pitch * 8, 4,
-                             (uint32_t)(nv < 256 ? nv : 256));
-    if (*rc != SDE_OK) return true;
-    switch (logn) {
-        case 11: *err = launch_col_tma<11>(map, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
-        case 12: *err = launch_col_tma<12>(map, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
-        default: *err = launch_col_tma<13>(map, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
+    *rc = SDE_OK;
+    *err = cudaSuccess;
+    for (int b0 = 0; b0 < n && *rc == SDE_OK && *err == cudaSuccess; b0 += TMA_MAXB) {
+        const int nb = n - b0 < TMA_MAXB ? n - b0 : TMA_MAXB;
+        TmaBatch tb;
+        for (int i = 0; i < nb && *rc == SDE_OK; i++)
+            *rc = encode_tmap_f32_2d(&tb.map[i], grids[b0 + i], (uint64_t)nu * 2, (uint64_t)nv,
+                                     (uint64_t)pitch * 8, 4, (uint32_t)(nv < 256 ? nv : 256));
+        if (*rc != SDE_OK) break;
+        switch (logn) {
+            case 11: *err = launch_col_tma<11>(tb, nb, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
+            case 12: *err = launch_col_tma<12>(tb, nb, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
+            default: *err = launch_col_tma<13>(tb, nb, nu, tw, inverse, r0, r1, ctx->d_status, ctx->stream); break;
+        }
     }
     return true;
 }
@@ -1130,10 +1144,10 @@ cudaError_t launch_c2r_pair(const FftBatch &bt, int nbatch, int pitch, int nx, i
         bt, pitch, nx, ny, ibegy, tw, cp, status);
     return cudaGetLastError();
 }
-// Whether the row-pair c2r kernel applies: half-lengths 2048 and 4096, grid rows that start
+// Whether the row-pair c2r kernel applies: half-lengths 1024..4096, grid rows that start
 // on 16-byte boundaries (pitch even, 16-byte aligned grids), image rows of whole float4s.
 static bool row_pair_ok(int logh, const FftBatch &bt, int nbatch, int pitch, int nx) {
-    if (logh != 11 && logh != 12) return false;
+    if (logh < 10 || logh > 12) return false;
     if ((pitch & 1) || (nx & 3)) return false;
     for (int b = 0; b < nbatch; b++)
         if (((uintptr_t)bt.grid[b] & 15u) || ((uintptr_t)bt.image[b] & 15u)) return false;
@@ -1200,8 +1214,9 @@ bool col_fft_t(int logn, const FftBatch &bt, int nbatch, int pitch, int nu, cons
 bool c2r_t(int logh, const FftBatch &bt, int nbatch, int pitch, int nx, int ny, int ibegy,
            const float2 *tw, CorrParams cp, cudaStream_t st, cudaError_t *err, int *status) {
     if (status && row_pair_ok(logh, bt, nbatch, pitch, nx)) {
-        *err = logh == 11 ? launch_c2r_pair<11>(bt, nbatch, pitch, nx, ny, ibegy, tw, cp, status, st)
-                          : launch_c2r_pair<12>(bt, nbatch, pitch, nx, ny, ibegy, tw, cp, status, st);
+        *err = logh == 10   ? launch_c2r_pair<10>(bt, nbatch, pitch, nx, ny, ibegy, tw, cp, status, st)
+               : logh == 11 ? launch_c2r_pair<11>(bt, nbatch, pitch, nx, ny, ibegy, tw, cp, status, st)
+                            : launch_c2r_pair<12>(bt, nbatch, pitch, nx, ny, ibegy, tw, cp, status, st);
         return true;
     }
     switch (logh) {
@@ -1255,7 +1270,11 @@ int fft_images_from_grids(sde_ctx *ctx, int n, float2 *const *grids, float *cons
         cudaError_t e = cudaSuccess;
         {
             KTimer kt(ctx, "col_fft_batch");
-            col_fft_t(logn, bt, nb, pitch, nu, twv, true, 0, nv, ctx->stream, &e);
+            int trc = SDE_OK;
+            if (col_fft_tma(ctx, logn, bt.grid, nb, pitch, nu, nv, twv, true, 0, nv, &e, &trc))
+                SDE_TRY(trc);
+            else
+                col_fft_t(logn, bt, nb, pitch, nu, twv, true, 0, nv, ctx->stream, &e);
         }
         SDE_CUDA_TRY(e);
         {
@@ -1286,7 +1305,8 @@ int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, in
         FftBatch bt{};
         bt.grid[0] = (float2 *)grid;
         int trc = SDE_OK;
-        if (col_fft_tma(ctx, ilog2(nv), (float2 *)grid, pitch, nu, nv, twv, true, 0, nv, &e, &trc)) {
+        float2 *g1 = (float2 *)grid;
+        if (col_fft_tma(ctx, ilog2(nv), &g1, 1, pitch, nu, nv, twv, true, 0, nv, &e, &trc)) {
             SDE_TRY(trc);
         } else if (!col_fft_t(ilog2(nv), bt, 1, pitch, nu, twv, true, 0, nv, ctx->stream, &e)) {
             const int lcc = col_logcc(nv), cc = 1 << lcc;
@@ -1354,8 +1374,8 @@ int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fn
     FftBatch bt{};
     bt.grid[0] = (float2 *)grid;
     int trc = SDE_OK;
-    if (col_fft_tma(ctx, ilog2(nv), (float2 *)grid, pitch, nu, nv, twv, false, ibegy, ibegy + ny, &e,
-                    &trc)) {
+    float2 *g1 = (float2 *)grid;
+    if (col_fft_tma(ctx, ilog2(nv), &g1, 1, pitch, nu, nv, twv, false, ibegy, ibegy + ny, &e, &trc)) {
         SDE_TRY(trc);
     } else if (!col_fft_t(ilog2(nv), bt, 1, pitch, nu, twv, false, ibegy, ibegy + ny, ctx->stream, &e)) {
         const int lcc = col_logcc(nv), cc = 1 << lcc;

@@ -58,6 +58,36 @@ def test_batch_equals_single_plan_path(gpu_ctx, pointings):
     m.close()
 
 
+def test_batch_large_images_equal_single_plan_path(gpu_ctx):
+    """Pointings of 1024^2 to 4096^2: the batched column pass through TMA (several grids of
+    one shape per launch) and the row-pair c2r pass, against the single-plan path."""
+    from sde_gb300 import synth
+    from sde_gb300.imaging import Geom, uvmap
+    from sde_gb300.mosaic import Mosaic
+    pts, c = synth.config4(n_point=7, seed=synth.SEED_BASE + 5, nvis_range=(2e4, 6e4),
+                           size_range=(1024, 4096))
+    sizes = [p["imsize"] for p in pts]
+    assert {1024, 2048, 4096} <= set(sizes) and sizes.count(2048) >= 2
+    ctx = gpu_ctx
+    m = Mosaic(ctx, pts, c["cell_arcsec"])
+    m.dirty(graph=True)
+    m.dirty(graph=True)  # the captured graph
+    torch = ctx.torch
+    seen = set()
+    for i, p in enumerate(pts):
+        if p["imsize"] in seen:
+            continue
+        seen.add(p["imsize"])
+        g = Geom(p["imsize"], c["cell_arcsec"])
+        t = {k: ctx.tensor(p[k], torch.float32) for k in ("u", "v", "w", "wt")}
+        t["vis"] = ctx.tensor(np.asarray(p["vis"], np.complex64).view(np.float32), torch.float32)
+        r = uvmap(ctx, g, t["u"], t["v"], t["w"], t["vis"], t["wt"], rmode="UNIFORM")
+        ctx.sync()
+        _close(m.read(i), r["dirty"].cpu().numpy())
+        r["plan"].close()
+    m.close()
+
+
 def test_batch_graph_and_loop_agree(gpu_ctx, pointings):
     from sde_gb300.mosaic import Mosaic
     pts, c = pointings
