@@ -308,15 +308,28 @@ __global__ void __launch_bounds__(RED_T) k_plan_sums(const float4 *__restrict__ 
     }
 }
 
-__global__ void k_sum_pairs(const double *partial, int n, double *out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int k = 0; k < n; k++) {
-            a += partial[2 * k];
-            b += partial[2 * k + 1];
+// The partial pairs summed in a fixed order by one block: thread t takes partials t, t+256,
+// ..., then a fixed tree over the threads (deterministic for a given partial count).
+__global__ void __launch_bounds__(RED_T) k_sum_pairs(const double *partial, int n, double *out) {
+    __shared__ double sh[2][RED_T];
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < n; k += RED_T) {
+        a += partial[2 * k];
+        b += partial[2 * k + 1];
+    }
+    sh[0][threadIdx.x] = a;
+    sh[1][threadIdx.x] = b;
+    __syncthreads();
+    for (int s = RED_T / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + s];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + s];
         }
-        out[0] = a;
-        out[1] = b;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sh[0][0];
+        out[1] = sh[1][0];
     }
 }
 
@@ -802,13 +815,13 @@ int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt) {
         *sumwt = 0.0;
         return SDE_OK;
     }
-    int nb = ctx->num_sms * 4;
+    const int nb = (int)std::min<int64_t>(ctx->num_sms * 4, ceil_div(pl->nvis, RED_T));
     double *part;
-    SDE_TRY(ctx_scratch(ctx, "gs_part", sizeof(double) * 2 * (size_t)nb, (void **)&part));
+    SDE_TRY(ctx_scratch(ctx, "gs_part", sizeof(double) * 2 * (size_t)(ctx->num_sms * 4), (void **)&part));
     KTimer kt(ctx, "plan_sums");
     k_plan_sums<<<nb, RED_T, 0, ctx->stream>>>(pl->rec, pl->cft, pl->nvis, part);
     SDE_CHECK_LAUNCH();
-    k_sum_pairs<<<1, 32, 0, ctx->stream>>>(part, nb, pl->d_sums);
+    k_sum_pairs<<<1, RED_T, 0, ctx->stream>>>(part, nb, pl->d_sums);
     SDE_CHECK_LAUNCH();
     double h[2];
     SDE_CUDA_TRY(cudaMemcpyAsync(h, pl->d_sums, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));

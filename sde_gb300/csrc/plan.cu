@@ -589,7 +589,6 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         PL_TRY(plan_alloc(pl, (void **)&pl->cft, sizeof(float) * 129 * 8));
         PL_CUDA(cudaMemcpyAsync(pl->cf, ctx->d_cf, sizeof(float) * CFLEN, cudaMemcpyDeviceToDevice, st));
         PL_CUDA(cudaMemcpyAsync(pl->cft, ctx->d_cft, sizeof(float) * 129 * 8, cudaMemcpyDeviceToDevice, st));
-        PL_CUDA(cudaStreamSynchronize(st));
     }
     ctx->bytes += pl->bytes;
     *out = pl;
