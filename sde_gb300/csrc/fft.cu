@@ -107,6 +107,35 @@ __device__ __forceinline__ void dftR(float2 *v) {
     else dft2<INV>(v[0], v[1]);
 }
 
+// bulk copy of nbytes (multiple of 16, both addresses 16-byte aligned) into shared memory
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t nbytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(src)), "r"(nbytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool bar_wait_bounded(uint32_t bar) {
+    uint32_t done = 0;
+    for (int spin = 0; spin < (1 << 24) && !done; spin++) {
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;"
+            " selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar)
+            : "memory");
+    }
+    return done != 0;
+}
+
+__device__ __forceinline__ void bar_init_one(uint32_t bar) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        asm volatile("fence.proxy.async.shared::cta;");
+    }
+    __syncthreads();
+}
+
 // Shared-memory index of element i of a transform: an XOR swizzle of the low four bits by
 // bits 4..7 spreads the stride-16 stores of the first radix-16 pass over all banks.
 __device__ __forceinline__ int swz(int i) { return i ^ ((i >> 4) & 15); }
@@ -531,7 +560,7 @@ struct RowShape {
     static constexpr int ROWS = H >= 2048 ? 2 : 4096 / H;
     static constexpr int T0 = ROWS * H / 16;
     static constexpr int T = T0 < 128 ? 128 : (T0 > 1024 ? 1024 : T0);
-    static constexpr size_t SMEM = sizeof(float2) * (size_t)ROWS * H;
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)ROWS * H + 16;  // + an mbarrier
     static constexpr int MINB = 1024 / T;
 };
 
@@ -648,18 +677,68 @@ __global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB)
 template <int LOGH>
 __global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB)
     k_row_r2c_t(const __grid_constant__ FftBatch bt, int nx, int ny, int ibegy,
-                const float2 *__restrict__ tw, CorrParams cp, int pitch) {
+                const float2 *__restrict__ tw, CorrParams cp, int pitch, int *status) {
     const float *__restrict__ image = bt.image[blockIdx.y];
     float2 *grid = bt.grid[blockIdx.y];
     using S = RowShape<LOGH>;
     constexpr int H = S::H, ROWS = S::ROWS, T = S::T, FNU = 2 * H;
     constexpr int TOTAL = ROWS * H;
     constexpr int PER = (TOTAL + T - 1) / T;
-    extern __shared__ float2 s[];
+    extern __shared__ __align__(16) float2 s[];
     const int cu = (FNU + 1) / 2 - 1, ioff = (FNU - nx) / 2;
     const int iy0 = blockIdx.x * ROWS;
-    // the CTA's image rows start on their way to L2 while the first loads are issued
-    // (measured: 0.107 -> 0.099 ms at 4096^2)
+    if (ROWS == 2 && status) {
+        // the CTA's image rows come in by bulk copy (row rr at floats [rr*FNU, rr*FNU+nx) of
+        // s); every thread reads its inputs from there, then the FFT layout overwrites it
+        // (measured: 0.099 -> 0.088 ms at 4096^2 against the L2-prefetch path below)
+        const float *stg = reinterpret_cast<const float *>(s);
+        const uint32_t sb = (uint32_t)__cvta_generic_to_shared(s);
+        const uint32_t bb = (uint32_t)__cvta_generic_to_shared(s + ROWS * H);
+        const bool two = iy0 + 1 < ny;
+        bar_init_one(bb);
+        if (threadIdx.x == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bb),
+                         "r"((uint32_t)((two ? 2 : 1) * nx * sizeof(float))));
+            bulk_g2s(sb, image + (int64_t)iy0 * nx, nx * sizeof(float), bb);
+            if (two) bulk_g2s(sb + FNU * sizeof(float), image + (int64_t)(iy0 + 1) * nx, nx * sizeof(float), bb);
+        }
+        if (!bar_wait_bounded(bb)) {
+            atomicExch(&status[STATUS_TIMEOUT], 1);
+            return;
+        }
+        float2 xin[PER];
+#pragma unroll
+        for (int i = 0; i < PER; i++) {
+            const int t = i * T + threadIdx.x;
+            const int rr = t >> LOGH, m = t & (H - 1);
+            const int iy = iy0 + rr;
+            xin[i] = make_float2(0.f, 0.f);
+            if (iy >= ny) continue;
+            const float cfy = cp.ccf ? cp.corry[iy] : 1.0f;
+            float xv[2];
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                int n = 2 * m + e + cu;
+                if (n >= FNU) n -= FNU;
+                const int ix = n - ioff;
+                float val = 0.f;
+                if (ix >= 0 && ix < nx) {
+                    val = stg[rr * FNU + ix];
+                    if (cp.ccf) val = __fdiv_rn(val, __fmul_rn(cp.corrx[ix], cfy));
+                }
+                xv[e] = val;
+            }
+            xin[i] = make_float2(xv[0], xv[1]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < PER; i++) {
+            const int t = i * T + threadIdx.x;
+            s[((t >> LOGH) << LOGH) + swz(t & (H - 1))] = xin[i];
+        }
+    } else {
+    // rows that do not start on 16-byte boundaries: the CTA's image rows start on their way
+    // to L2 while the first loads are issued (0.107 -> 0.099 ms at 4096^2)
     if (threadIdx.x == 0)
         for (int rr = 0; rr < ROWS; rr++)
             if (iy0 + rr < ny) prefetch_l2_range(image + (int64_t)(iy0 + rr) * nx, 0, nx, 4);
@@ -690,6 +769,7 @@ __global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB)
             xv[e] = val;
         }
         s[(rr << LOGH) + swz(m)] = make_float2(xv[0], xv[1]);
+    }
     }
     __syncthreads();
     StPasses<LOGH, 0, false, ROWS, T>::run(s, tw, 2);
@@ -1021,35 +1101,6 @@ struct RowPair {
     static constexpr int MINB = T <= 128 ? 4 : 2;
 };
 
-// bulk copy of nbytes (multiple of 16, both addresses 16-byte aligned) into shared memory
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t nbytes, uint32_t bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(src)), "r"(nbytes), "r"(bar)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool bar_wait_bounded(uint32_t bar) {
-    uint32_t done = 0;
-    for (int spin = 0; spin < (1 << 24) && !done; spin++) {
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;"
-            " selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(bar)
-            : "memory");
-    }
-    return done != 0;
-}
-
-__device__ __forceinline__ void bar_init_one(uint32_t bar) {
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
-        asm volatile("fence.mbarrier_init.release.cluster;");
-        asm volatile("fence.proxy.async.shared::cta;");
-    }
-    __syncthreads();
-}
-
 // c2r first-pass input: FFTR's pre-step of element k for both staged grid rows
 template <int H>
 struct C2rRead {
@@ -1188,13 +1239,13 @@ cudaError_t launch_c2r_t(const FftBatch &bt, int nbatch, int pitch, int nx, int 
 
 template <int LOGH>
 cudaError_t launch_r2c_t(const FftBatch &bt, int nbatch, int nx, int ny, int ibegy, const float2 *tw,
-                         CorrParams cp, int pitch, cudaStream_t st) {
+                         CorrParams cp, int pitch, int *status, cudaStream_t st) {
     using S = RowShape<LOGH>;
     cudaError_t e = cudaFuncSetAttribute(k_row_r2c_t<LOGH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)S::SMEM);
     if (e != cudaSuccess) return e;
     k_row_r2c_t<LOGH><<<dim3((unsigned)((ny + S::ROWS - 1) / S::ROWS), (unsigned)nbatch), S::T, S::SMEM,
-                        st>>>(bt, nx, ny, ibegy, tw, cp, pitch);
+                        st>>>(bt, nx, ny, ibegy, tw, cp, pitch, status);
     return cudaGetLastError();
 }
 
@@ -1228,10 +1279,14 @@ bool c2r_t(int logh, const FftBatch &bt, int nbatch, int pitch, int nx, int ny, 
     }
 }
 bool r2c_t(int logh, const FftBatch &bt, int nbatch, int nx, int ny, int ibegy, const float2 *tw,
-           CorrParams cp, int pitch, cudaStream_t st, cudaError_t *err) {
+           CorrParams cp, int pitch, cudaStream_t st, cudaError_t *err, int *status) {
+    // image rows staged by bulk copy when they start on 16-byte boundaries
+    bool staged = status && (nx & 3) == 0;
+    for (int b = 0; b < nbatch && staged; b++) staged = ((uintptr_t)bt.image[b] & 15u) == 0;
+    int *st_status = staged ? status : nullptr;
     switch (logh) {
 #define CASE(L) \
-    case L: *err = launch_r2c_t<L>(bt, nbatch, nx, ny, ibegy, tw, cp, pitch, st); return true;
+    case L: *err = launch_r2c_t<L>(bt, nbatch, nx, ny, ibegy, tw, cp, pitch, st_status, st); return true;
         SDE_LOG_CASES(CASE)
 #undef CASE
         default: return false;
@@ -1358,7 +1413,7 @@ int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fn
         FftBatch bt{};
         bt.grid[0] = (float2 *)grid;
         bt.image[0] = const_cast<float *>(image);
-        if (!r2c_t(ilog2(fnu / 2), bt, 1, nx, ny, ibegy, twu, cp, pitch, ctx->stream, &e)) {
+        if (!r2c_t(ilog2(fnu / 2), bt, 1, nx, ny, ibegy, twu, cp, pitch, ctx->stream, &e, ctx->d_status)) {
             int rows, thr;
             row_shape(fnu, &rows, &thr);
             const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
