@@ -362,7 +362,8 @@ def run_gpu(args):
     clk = clocks.stop()
     launches = L.sde_ctx_launches(ctx.h)
     kern = {}
-    for name in ("grid", "finalize", "col_fft", "row_c2r", "row_r2c", "degrid", "degrid_exc"):
+    for name in ("grid", "fold_lo", "finalize", "col_fft_fin", "col_fft", "row_c2r", "row_r2c", "degrid",
+                 "degrid_exc"):
         tot, cnt = C.c_double(), C.c_int64()
         L.sde_ctx_kernel_stats(ctx.h, name.encode(), C.byref(tot), C.byref(cnt))
         if cnt.value:

@@ -207,6 +207,15 @@ int sde_plan_set_vis(sde_plan *plan, const float *vis, int where);
 #define SDE_GRID_PSF 1
 int sde_grid_pitch(int nu);
 int sde_plan_grid(sde_plan *plan, int what, float *grid, int pitch, float *sumwt);
+/* Dirty image (SDE_GRID_VIS) or PSF (SDE_GRID_PSF) of the plan into image (device, ny x nx,
+ * row-major): GRDH2D's grid then FFTR2D's inverse (fft/fftr2d.f:64-90), with PIXCOR2D's
+ * correction when correct != 0 and divided by *scale_dev when scale_dev != NULL -- what
+ * sde_plan_grid followed by sde_image_from_grid gives, with GRDH2D's finalize applied inside
+ * the column pass instead of as a pass of its own.  The column-transformed grid is left in
+ * grid ([nv][pitch] complex64) when grid != NULL.  Asynchronous; sumwt as in sde_plan_grid.
+ * No counterpart entry point in the reference (uvmap calls GRDH2D, then FFTR2D). */
+int sde_plan_image(sde_plan *plan, int what, int nx, int ny, int correct, const float *scale_dev,
+                   float *image, float *grid, int pitch, float *sumwt);
 
 /* Degrid a device grid ([nv][pitch] complex64, GRDDEH2D layout) at the plan's
  * visibilities and update the residual: residual = observed - model.  Asynchronous. */

@@ -92,6 +92,7 @@ SIGNATURES = [
     ("sde_plan_set_vis", I, [P, P, I]),
     ("sde_grid_pitch", I, [I]),
     ("sde_plan_grid", I, [P, I, P, I, C.POINTER(F)]),
+    ("sde_plan_image", I, [P, I, I, I, I, P, P, P, I, C.POINTER(F)]),
     ("sde_plan_degrid_residual", I, [P, P, I]),
     ("sde_plan_reset_residual", I, [P]),
     ("sde_plan_degrid", I, [P, P, I, P, P, I, C.POINTER(I64)]),

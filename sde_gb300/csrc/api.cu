@@ -300,6 +300,26 @@ static int ensure_sums(sde_plan *pl) {
     return SDE_OK;
 }
 
+// Raw accumulation of one gridding pass of pl in the context's scratch; the compensation
+// plane, when on, is folded in (*raw_lo = nullptr after) or left for finalize.
+static int plan_raw_pass(sde_plan *pl, int what, float2 **raw, float2 **raw_lo) {
+    sde_ctx *ctx = pl->ctx;
+    const size_t cells = (size_t)pl->spec.nv * pl->pitch;
+    SDE_TRY(ctx_scratch(ctx, "raw_grid", sizeof(float2) * cells * (ctx->compensated ? 2 : 1), (void **)raw));
+    *raw_lo = ctx->compensated ? *raw + cells : nullptr;
+    // the compensation plane stays zero between passes (the fold re-zeroes what a pass
+    // wrote); it is cleared only when the scratch is new
+    const bool lo_clean = *raw_lo && ctx->lo_clean == *raw_lo;
+    ctx->lo_clean = nullptr;
+    SDE_TRY(plan_grid_raw(pl, what, *raw, *raw_lo, lo_clean));
+    SDE_TRY(plan_fold_lo(pl, *raw, *raw_lo));
+    if (*raw_lo && pl->core_lo) {
+        ctx->lo_clean = *raw_lo;
+        *raw_lo = nullptr;  // folded into raw
+    }
+    return SDE_OK;
+}
+
 extern "C" int sde_plan_grid(sde_plan *pl, int what, float *grid, int pitch, float *sumwt) {
     if (!pl || !grid || pitch < pl->spec.nu || (what != SDE_GRID_VIS && what != SDE_GRID_PSF)) {
         sde_set_error("sde_plan_grid: bad arguments");
@@ -315,12 +335,8 @@ extern "C" int sde_plan_grid(sde_plan *pl, int what, float *grid, int pitch, flo
         sde_set_error("No weight!");
         return SDE_ENOWEIGHT;
     }
-    float2 *raw;
-    const size_t cells = (size_t)nv * pl->pitch;
-    SDE_TRY(ctx_scratch(ctx, "raw_grid", sizeof(float2) * cells * (ctx->compensated ? 2 : 1),
-                        (void **)&raw));
-    float2 *raw_lo = ctx->compensated ? raw + cells : nullptr;
-    SDE_TRY(plan_grid_raw(pl, what, raw, raw_lo));
+    float2 *raw, *raw_lo;
+    SDE_TRY(plan_raw_pass(pl, what, &raw, &raw_lo));
     // LSUMWT = FLOAT(NU-1)*FLOAT(NV)/LSUMWT (grd/grdh2d.f:218), applied in FP32
     const float scale = (float)((double)((float)(nu - 1) * (float)nv) / pl->h_lsumwt);
     if (pitch == pl->pitch) {
@@ -334,6 +350,42 @@ extern "C" int sde_plan_grid(sde_plan *pl, int what, float *grid, int pitch, flo
         SDE_CUDA_TRY(cudaMemcpy2DAsync(grid, (size_t)pitch * 8, tmp, (size_t)pl->pitch * 8,
                                        (size_t)nu * 8, nv, cudaMemcpyDeviceToDevice, ctx->stream));
     }
+    if (sumwt) *sumwt = (float)pl->h_sumwt;
+    return SDE_OK;
+}
+
+extern "C" int sde_plan_image(sde_plan *pl, int what, int nx, int ny, int correct,
+                              const float *scale_dev, float *image, float *grid, int pitch,
+                              float *sumwt) {
+    if (!pl || !image || nx < 1 || ny < 1 || (grid && pitch < pl->spec.nu) ||
+        (what != SDE_GRID_VIS && what != SDE_GRID_PSF)) {
+        sde_set_error("sde_plan_image: bad arguments");
+        return SDE_EINVAL;
+    }
+    sde_ctx *ctx = pl->ctx;
+    SDE_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int nu = pl->spec.nu, nv = pl->spec.nv, fnu = 2 * (nu - 1);
+    SDE_TRY(check_fft_shape(nx, ny, fnu, nv));
+    SDE_TRY(ensure_sums(pl));
+    float2 *g = (float2 *)grid;
+    if (!g || pitch != pl->pitch)
+        SDE_TRY(ctx_scratch(ctx, "img_grid", sizeof(float2) * (size_t)nv * pl->pitch, (void **)&g));
+    if (pl->h_lsumwt == 0.0) {
+        SDE_CUDA_TRY(cudaMemsetAsync(image, 0, sizeof(float) * (size_t)nx * ny, ctx->stream));
+        if (grid) SDE_CUDA_TRY(cudaMemset2DAsync(grid, (size_t)pitch * 8, 0, (size_t)nu * 8, nv, ctx->stream));
+        if (sumwt) *sumwt = (float)pl->h_sumwt;
+        sde_set_error("No weight!");
+        return SDE_ENOWEIGHT;
+    }
+    float2 *raw, *raw_lo;
+    SDE_TRY(plan_raw_pass(pl, what, &raw, &raw_lo));
+    // LSUMWT = FLOAT(NU-1)*FLOAT(NV)/LSUMWT (grd/grdh2d.f:218), applied in FP32
+    const float scale = (float)((double)((float)(nu - 1) * (float)nv) / pl->h_lsumwt);
+    SDE_TRY(image_from_raw(ctx, raw, raw_lo, nu, nv, pl->spec.uorigin, pl->spec.vorigin, pl->spec.supp,
+                           scale, (float *)g, pl->pitch, nx, ny, fnu, correct, scale_dev, image));
+    if (grid && (float2 *)grid != g)
+        SDE_CUDA_TRY(cudaMemcpy2DAsync(grid, (size_t)pitch * 8, g, (size_t)pl->pitch * 8, (size_t)nu * 8, nv,
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
     if (sumwt) *sumwt = (float)pl->h_sumwt;
     return SDE_OK;
 }

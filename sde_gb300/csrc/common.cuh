@@ -44,6 +44,13 @@ constexpr int SUPP = 3;                 // 'SF' support (grd/grdcf.f:258)
 constexpr int OSAMP = 128;              // oversampling (grd/grdcf.f:245)
 constexpr int NTAP = 2 * SUPP + 1;      // 7
 constexpr int STILE = TILE + 2 * SUPP;  // 70: shared tile edge (grid and degrid)
+// The raw gridding accumulation keeps GRDH2D's raw column U (1-based, grd/grdh2d.f:177-187)
+// at index U, so final column u (0-based) sits at raw index u + SUPP + 1 = u + 4 and any two
+// final columns (u, u+1), u even, start on a 16-byte boundary of the raw row (TMA boxes).
+constexpr int RAW_SHIFT = SUPP + 1;
+// Row pitch (complex elements) of a plan's raw and final grids: a multiple of 4 (16-byte
+// rows for TMA) with room for raw index NU.
+inline int plan_pitch(int nu) { return (nu + 4) & ~3; }
 constexpr int CFLEN = 1 + 8 * 129;      // vis/visgrid.f:274
 constexpr int ITEM_MAX = 16384;        // default work-item size (sde_plan_opts.item_max)
 constexpr int CHUNK_MAX = 64;           // default chunk size (sde_plan_opts.chunk_max)
@@ -121,6 +128,7 @@ struct sde_ctx {
     int64_t nlaunch = 0;
     // gridding sums across work items with TwoSum compensation (sde_ctx_set_compensated)
     bool compensated = true;
+    const void *lo_clean = nullptr;  // compensation plane of the raw-grid scratch known to be zero
     struct EvPair {
         const char *name;
         cudaEvent_t a, b;
@@ -181,6 +189,8 @@ struct sde_plan {
     WorkItem *items = nullptr;
     DegridExc *exc = nullptr; // exception list (includes degrid-only visibilities)
     float *wt_all = nullptr;  // caller-order weights (for user-frame degridding)
+    uint8_t *core_lo = nullptr;  // (ntu+1) x (ntv+1) raw-grid cores where the compensation
+                                 // plane can be non-zero (dense tiles' footprints)
     int32_t *inv = nullptr;   // caller index -> position of the tiled visibilities (-1 else),
                               // built on the first caller-order degrid
     int64_t nuntouched = 0;   // caller visibilities with WT <= 0 (GRDDEH2D leaves them as they are)
@@ -200,7 +210,16 @@ int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, const float2 *raw_lo, f
                         int uorigin, int vorigin, int supp, float scale);
 // raw accumulation of one gridding pass; raw_lo (same shape, may be NULL) receives the
 // rounding errors of the cross-item sums (compensated accumulation)
-int plan_grid_raw(sde_plan *pl, int what, float2 *raw, float2 *raw_lo);
+int plan_grid_raw(sde_plan *pl, int what, float2 *raw, float2 *raw_lo, bool lo_clean = false);
+// Add the compensation plane into the raw grid where it can be non-zero (the plan's dense
+// cores) and zero it there: afterwards raw alone is the compensated sum and raw_lo is zero.
+int plan_fold_lo(sde_plan *pl, float2 *raw, float2 *raw_lo);
+// Image of a gridding pass from the raw accumulation (fft.cu): finalize fused into the
+// column pass where it is TMA-fed (raw_lo must then be folded, i.e. nullptr), else finalize
+// into grid and the usual passes; grid receives the column-transformed grid.
+int image_from_raw(sde_ctx *ctx, const float2 *raw, const float2 *raw_lo, int nu, int nv,
+                   int uorigin, int vorigin, int supp, float scale, float *grid, int pitch, int nx,
+                   int ny, int fnu, int correct, const float *scale_dev, float *image);
 
 // ---- batches of plans (mosaic pointings, served jobs) -----------------------------------
 // One plan as the persistent gridder sees it.

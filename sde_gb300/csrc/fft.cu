@@ -836,8 +836,35 @@ __device__ __forceinline__ void twiddle_powers2(float2 *a, float2 *b, const floa
     }
 }
 
-template <int LOGN, int LOGR, int LOGNS, bool INV, int T, bool FIRST, bool LAST>
-__device__ __forceinline__ void st_pass2(float4 *s, const float2 *__restrict__ tw, int r0, int r1) {
+// GRDH2D's finalize (grd/grdh2d.f:202-226) applied while a column pass reads its input from
+// the raw accumulation: out(u, v) = scale * (R(u+SUPP+1, v) + conj(R(UC-k, 2VC-v)) for the
+// k = 0..SUPP columns next to the axis), 0 for u+1 > NU-SUPP; R is stored at raw index U
+// (RAW_SHIFT) and already holds the folded compensation plane.  nullptr raw: no finalize.
+struct FinParams {
+    const float2 *raw;
+    int raw_pitch, nu, nv, uorigin, vorigin, supp;
+    float scale;
+};
+__device__ __forceinline__ float2 fin_cell(const FinParams &f, float2 r, int u, int v) {
+    const int u1 = u + 1, v1 = v + 1;
+    if (u1 > f.nu - f.supp) return make_float2(0.f, 0.f);
+    const int U = u1 + f.supp, UC = f.uorigin + f.supp, k = U - UC;
+    if (k >= 0 && k <= f.supp) {
+        const int dvv = v1 - f.vorigin, vm = 2 * f.vorigin - v1;
+        if (dvv >= -(f.nv / 2) + 1 && dvv <= f.nv / 2 - 1 && vm >= 1 && vm <= f.nv) {
+            const float2 m = f.raw[(int64_t)(vm - 1) * f.raw_pitch + (UC - k)];
+            r.x = r.x + m.x;
+            r.y = r.y - m.y;
+        }
+    }
+    r.x *= f.scale;
+    r.y *= f.scale;
+    return r;
+}
+
+template <int LOGN, int LOGR, int LOGNS, bool INV, int T, bool FIRST, bool LAST, bool FIN = false>
+__device__ __forceinline__ void st_pass2(float4 *s, const float2 *__restrict__ tw, int r0, int r1,
+                                         const FinParams *fp = nullptr, int u0 = 0) {
     constexpr int N = 1 << LOGN, R = 1 << LOGR, NB = 1 << (LOGN - LOGR), NS = 1 << LOGNS;
     constexpr int PER = (NB + T - 1) / T;
     constexpr int TSHIFT = LOGN - LOGNS - LOGR;
@@ -855,6 +882,11 @@ __device__ __forceinline__ void st_pass2(float4 *s, const float2 *__restrict__ t
                     const int v = (idx + C) & (N - 1);
                     x = s[v];
                     if (!INV && (v < r0 || v >= r1)) x = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (FIN) {
+                        const float2 c0 = fin_cell(*fp, make_float2(x.x, x.y), u0, v);
+                        const float2 c1 = fin_cell(*fp, make_float2(x.z, x.w), u0 + 1, v);
+                        x = make_float4(c0.x, c0.y, c1.x, c1.y);
+                    }
                 } else {
                     x = s[swz4(idx)];
                 }
@@ -893,18 +925,21 @@ __device__ __forceinline__ void st_pass2(float4 *s, const float2 *__restrict__ t
     __syncthreads();
 }
 
-template <int LOGN, int LOGNS, bool INV, int T>
+template <int LOGN, int LOGNS, bool INV, int T, bool FIN>
 struct St2Passes {
-    static __device__ __forceinline__ void run(float4 *s, const float2 *__restrict__ tw, int r0, int r1) {
+    static __device__ __forceinline__ void run(float4 *s, const float2 *__restrict__ tw, int r0, int r1,
+                                               const FinParams *fp, int u0) {
         constexpr int REM = LOGN - LOGNS;
         constexpr int LOGR = REM >= 4 ? 4 : REM;
-        st_pass2<LOGN, LOGR, LOGNS, INV, T, LOGNS == 0, LOGNS + LOGR == LOGN>(s, tw, r0, r1);
-        St2Passes<LOGN, LOGNS + LOGR, INV, T>::run(s, tw, r0, r1);
+        st_pass2<LOGN, LOGR, LOGNS, INV, T, LOGNS == 0, LOGNS + LOGR == LOGN, FIN && LOGNS == 0>(
+            s, tw, r0, r1, fp, u0);
+        St2Passes<LOGN, LOGNS + LOGR, INV, T, FIN>::run(s, tw, r0, r1, fp, u0);
     }
 };
-template <int LOGN, bool INV, int T>
-struct St2Passes<LOGN, LOGN, INV, T> {
-    static __device__ __forceinline__ void run(float4 *, const float2 *__restrict__, int, int) {}
+template <int LOGN, bool INV, int T, bool FIN>
+struct St2Passes<LOGN, LOGN, INV, T, FIN> {
+    static __device__ __forceinline__ void run(float4 *, const float2 *__restrict__, int, int,
+                                               const FinParams *, int) {}
 };
 
 template <int LOGN>
@@ -922,11 +957,16 @@ struct TmaBatch {
     CUtensorMap map[TMA_MAXB];
 };
 
-template <int LOGN, bool INV>
+// FIN: the input is GRDH2D's raw accumulation (tensor map tb.map[blockIdx.y], boxes at raw
+// index u + RAW_SHIFT) finalized on the way in (fp); the output goes to tb.map[blockIdx.y +
+// store_off] (the final grid).
+template <int LOGN, bool INV, bool FIN>
 __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
     k_col_fft_tma(const __grid_constant__ TmaBatch tb, const float2 *__restrict__ tw, int r0,
-                  int r1, int *status) {
+                  int r1, int *status, int store_off, FinParams fp) {
     const CUtensorMap *tmap = &tb.map[blockIdx.y];
+    const CUtensorMap *smap = &tb.map[blockIdx.y + store_off];
+    const int xl = 4 * blockIdx.x + (FIN ? 2 * RAW_SHIFT : 0);  // load box: raw index u0+4
     using S = ColTma<LOGN>;
     constexpr int N = S::N, BOX = S::BOX;
     extern __shared__ __align__(128) unsigned char smem_ct[];
@@ -948,7 +988,7 @@ __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
             asm volatile(
                 "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(sb + (uint32_t)(b * BOX * sizeof(float4))),
-                "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(b * BOX), "r"(bb)
+                "l"(reinterpret_cast<uint64_t>(tmap)), "r"(xl), "r"(b * BOX), "r"(bb)
                 : "memory");
     }
     {
@@ -966,14 +1006,14 @@ __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
             return;
         }
     }
-    St2Passes<LOGN, 0, INV, S::T>::run(s, tw, r0, r1);
+    St2Passes<LOGN, 0, INV, S::T, FIN>::run(s, tw, r0, r1, &fp, 2 * blockIdx.x);
     // the last pass's generic stores must be visible to the bulk copies that read them
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int b = 0; b < N / BOX; b++)
             asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
-                             reinterpret_cast<uint64_t>(tmap)),
+                             reinterpret_cast<uint64_t>(smap)),
                          "r"(x), "r"(b * BOX), "r"(sb + (uint32_t)(b * BOX * sizeof(float4)))
                          : "memory");
         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
@@ -983,19 +1023,25 @@ __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
 
 template <int LOGN>
 cudaError_t launch_col_tma(const TmaBatch &map, int nbatch, int nu, const float2 *tw, bool inverse,
-                           int r0, int r1, int *status, cudaStream_t st) {
+                           int r0, int r1, int *status, cudaStream_t st, const FinParams *fin = nullptr) {
     using S = ColTma<LOGN>;
     const dim3 nb((unsigned)((nu + 1) / 2), (unsigned)nbatch);
-    if (inverse) {
-        cudaError_t e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, true>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    cudaError_t e;
+    if (fin) {
+        e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)S::SMEM);
         if (e != cudaSuccess) return e;
-        k_col_fft_tma<LOGN, true><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status);
+        k_col_fft_tma<LOGN, true, true><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status, nbatch, *fin);
+    } else if (inverse) {
+        e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)S::SMEM);
+        if (e != cudaSuccess) return e;
+        k_col_fft_tma<LOGN, true, false><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status, 0, FinParams{});
     } else {
-        cudaError_t e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, false>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+        e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)S::SMEM);
         if (e != cudaSuccess) return e;
-        k_col_fft_tma<LOGN, false><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status);
+        k_col_fft_tma<LOGN, false, false><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status, 0, FinParams{});
     }
     return cudaGetLastError();
 }
@@ -1345,6 +1391,32 @@ int check_fft_shape(int nx, int ny, int fnu, int nv) {
     return check_fft_args(nx, ny, fnu, nv, fnu / 2 + 1);
 }
 
+// The row c2r pass of a column-transformed grid into the image (FFTR2D's second half, with
+// PIXCOR2D's correction and the PSF-peak scale when asked).
+static int c2r_pass(sde_ctx *ctx, const float *grid, int pitch, int nx, int ny, int fnu, int nv,
+                    int correct, const float *scale_dev, float *image, const float2 *twu) {
+    CorrParams cp = {nullptr, nullptr, nullptr};
+    if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
+    const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;  // 0-based first grid row
+    KTimer kt(ctx, "row_c2r");
+    cudaError_t e = cudaSuccess;
+    FftBatch bt{};
+    bt.grid[0] = (float2 *)grid;
+    bt.image[0] = image;
+    bt.scale[0] = scale_dev;
+    if (!c2r_t(ilog2(fnu / 2), bt, 1, pitch, nx, ny, ibegy, twu, cp, ctx->stream, &e, ctx->d_status)) {
+        int rows, thr;
+        row_shape(fnu, &rows, &thr);
+        const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
+        SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+        k_row_c2r<<<ceil_div(ny, rows), thr, smr, ctx->stream>>>((const float2 *)grid, pitch, fnu, rows,
+                                                                nx, ny, ibegy, twu, cp, scale_dev, image);
+        e = cudaGetLastError();
+    }
+    SDE_CUDA_TRY(e);
+    return SDE_OK;
+}
+
 int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, int fnu, int nv,
                         int correct, const float *scale_dev, float *image) {
     if (!ctx || !grid || !image) return SDE_EINVAL;
@@ -1373,26 +1445,43 @@ int sde_image_from_grid(sde_ctx *ctx, float *grid, int pitch, int nx, int ny, in
         }
         SDE_CUDA_TRY(e);
     }
-    CorrParams cp = {nullptr, nullptr, nullptr};
-    if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
-    const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;  // 0-based first grid row
-    KTimer kt(ctx, "row_c2r");
-    cudaError_t e = cudaSuccess;
-    FftBatch bt{};
-    bt.grid[0] = (float2 *)grid;
-    bt.image[0] = image;
-    bt.scale[0] = scale_dev;
-    if (!c2r_t(ilog2(fnu / 2), bt, 1, pitch, nx, ny, ibegy, twu, cp, ctx->stream, &e, ctx->d_status)) {
-        int rows, thr;
-        row_shape(fnu, &rows, &thr);
-        const size_t smr = sizeof(float2) * (size_t)(fnu / 2) * rows;
-        SDE_CUDA_TRY(cudaFuncSetAttribute(k_row_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
-        k_row_c2r<<<ceil_div(ny, rows), thr, smr, ctx->stream>>>((const float2 *)grid, pitch, fnu, rows,
-                                                                nx, ny, ibegy, twu, cp, scale_dev, image);
-        e = cudaGetLastError();
+    return c2r_pass(ctx, grid, pitch, nx, ny, fnu, nv, correct, scale_dev, image, twu);
+}
+
+// The dirty image (or PSF) of a plan pass straight from the raw accumulation: where the
+// column pass is TMA-fed (2048..8192 rows) it applies GRDH2D's finalize to its input and
+// writes the column-transformed grid to grid; otherwise finalize into grid, then the column
+// pass.  Then the row c2r pass.
+int image_from_raw(sde_ctx *ctx, const float2 *raw, const float2 *raw_lo, int nu, int nv,
+                   int uorigin, int vorigin, int supp, float scale, float *grid, int pitch, int nx,
+                   int ny, int fnu, int correct, const float *scale_dev, float *image) {
+    SDE_TRY(check_fft_args(nx, ny, fnu, nv, pitch));
+    const int logn = ilog2(nv);
+    if (raw_lo || logn < 11 || logn > 13 || nu != fnu / 2 + 1) {
+        SDE_TRY(grid_finalize_scale(ctx, raw, raw_lo, (float2 *)grid, nu, nv, pitch, uorigin, vorigin,
+                                    supp, scale));
+        return sde_image_from_grid(ctx, grid, pitch, nx, ny, fnu, nv, correct, scale_dev, image);
     }
-    SDE_CUDA_TRY(e);
-    return SDE_OK;
+    const float2 *twv, *twu;
+    SDE_TRY(ctx_twiddles(ctx, nv, &twv));
+    SDE_TRY(ctx_twiddles(ctx, fnu, &twu));
+    {
+        KTimer kt(ctx, "col_fft_fin");
+        TmaBatch tb;
+        SDE_TRY(encode_tmap_f32_2d(&tb.map[0], raw, (uint64_t)pitch * 2, (uint64_t)nv, (uint64_t)pitch * 8, 4,
+                                   256));
+        SDE_TRY(encode_tmap_f32_2d(&tb.map[1], grid, (uint64_t)nu * 2, (uint64_t)nv, (uint64_t)pitch * 8, 4,
+                                   256));
+        const FinParams fp{raw, pitch, nu, nv, uorigin, vorigin, supp, scale};
+        cudaError_t e;
+        switch (logn) {
+            case 11: e = launch_col_tma<11>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fp); break;
+            case 12: e = launch_col_tma<12>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fp); break;
+            default: e = launch_col_tma<13>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fp); break;
+        }
+        SDE_CUDA_TRY(e);
+    }
+    return c2r_pass(ctx, grid, pitch, nx, ny, fnu, nv, correct, scale_dev, image, twu);
 }
 
 int sde_grid_from_image(sde_ctx *ctx, const float *image, int nx, int ny, int fnu, int nv,

@@ -173,9 +173,10 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
             tre[k] = 0.f;
             tim[k] = 0.f;
             const int r = k / STILE, cc = k - r * STILE;
-            const int gv0 = tv * TILE + r - SUPP, gu0 = tu * TILE + cc - SUPP;  // 0-based raw
+            // GRDH2D's 0-based raw cell; stored at raw index gu0 + 1 (RAW_SHIFT = SUPP + 1)
+            const int gv0 = tv * TILE + r - SUPP, gu0 = tu * TILE + cc - SUPP;
             if (gv0 < 0 || gv0 >= nv || gu0 < 0 || gu0 >= nu) continue;
-            gi[j] = (int64_t)gv0 * pitch + gu0;
+            gi[j] = (int64_t)gv0 * pitch + gu0 + 1;
         }
         if (COMP && it.dense) {
             // compensated sum across items (dense tiles, many items per cell): the atomic
@@ -367,15 +368,15 @@ __device__ __forceinline__ float2 finalize_cell(const float2 *__restrict__ raw,
     const int u1 = u0 + 1, v1 = v0 + 1;  // 1-based
     float2 r = make_float2(0.f, 0.f);
     if (u1 <= nu - supp) {
-        const int U = u1 + supp;            // raw column (1-based)
-        r = raw_at(raw, raw_lo, (int64_t)v0 * pitch + (U - 1));
+        const int U = u1 + supp;            // GRDH2D's raw column (1-based) = raw index
+        r = raw_at(raw, raw_lo, (int64_t)v0 * pitch + U);
         const int UC = uorigin + supp, VC = vorigin;
         const int k = U - UC;
         if (k >= 0 && k <= supp) {
             const int dvv = v1 - VC;
             const int vm = 2 * VC - v1;
             if (dvv >= -(nv / 2) + 1 && dvv <= nv / 2 - 1 && vm >= 1 && vm <= nv) {
-                const float2 m = raw_at(raw, raw_lo, (int64_t)(vm - 1) * pitch + (UC - k - 1));
+                const float2 m = raw_at(raw, raw_lo, (int64_t)(vm - 1) * pitch + (UC - k));
                 r.x = r.x + m.x;
                 r.y = r.y - m.y;
             }
@@ -384,6 +385,43 @@ __device__ __forceinline__ float2 finalize_cell(const float2 *__restrict__ raw,
         r.y *= scale;
     }
     return r;
+}
+
+// The compensation plane folded into the raw grid over one marked core (see k_core_lo):
+// raw = raw + lo where lo != 0 (the add finalize would do), lo = 0.  A core row is 32 pairs
+// of cells starting at an even raw index (16-byte aligned: the pitch is a multiple of 4);
+// each thread loads 8 pairs before touching any.
+__global__ void __launch_bounds__(256) k_fold_lo(float2 *raw, float2 *raw_lo, const uint8_t *__restrict__ core,
+                                                 int ncu, int nv, int pitch) {
+    if (!core[blockIdx.x]) return;
+    const int cu = blockIdx.x % ncu, cv = blockIdx.x / ncu;
+    const int r0 = cv * TILE - SUPP, i0 = cu * TILE - (SUPP - 1);
+    float4 *raw4 = reinterpret_cast<float4 *>(raw);
+    float4 *lo4 = reinterpret_cast<float4 *>(raw_lo);
+    constexpr int PAIRS = TILE * TILE / 2 / 256;  // 8
+    float4 e[PAIRS];
+    int64_t q[PAIRS];
+#pragma unroll
+    for (int j = 0; j < PAIRS; j++) {
+        const int k = threadIdx.x + j * 256;
+        const int r = r0 + (k >> 5), i = i0 + 2 * (k & 31);
+        q[j] = -1;
+        e[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (r < 0 || r >= nv || i < 0 || i >= pitch) continue;
+        q[j] = ((int64_t)r * pitch + i) >> 1;
+        e[j] = lo4[q[j]];
+    }
+#pragma unroll
+    for (int j = 0; j < PAIRS; j++) {
+        if (q[j] < 0 || (e[j].x == 0.f && e[j].y == 0.f && e[j].z == 0.f && e[j].w == 0.f)) continue;
+        float4 h = raw4[q[j]];
+        h.x = h.x + e[j].x;
+        h.y = h.y + e[j].y;
+        h.z = h.z + e[j].z;
+        h.w = h.w + e[j].w;
+        raw4[q[j]] = h;
+        lo4[q[j]] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 }
 
 __global__ void k_finalize(const float2 *__restrict__ raw, const float2 *__restrict__ raw_lo,
@@ -881,11 +919,11 @@ int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, const uint16
     return SDE_OK;
 }
 
-int plan_grid_raw(sde_plan *pl, int what, float2 *raw, float2 *raw_lo) {
+int plan_grid_raw(sde_plan *pl, int what, float2 *raw, float2 *raw_lo, bool lo_clean) {
     sde_ctx *ctx = pl->ctx;
     const int nu = pl->spec.nu, nv = pl->spec.nv;
     SDE_CUDA_TRY(cudaMemsetAsync(raw, 0, sizeof(float2) * (size_t)nv * pl->pitch, ctx->stream));
-    if (raw_lo)
+    if (raw_lo && !lo_clean)
         SDE_CUDA_TRY(cudaMemsetAsync(raw_lo, 0, sizeof(float2) * (size_t)nv * pl->pitch, ctx->stream));
     if (pl->nitems == 0) return SDE_OK;
     static bool attr = false;
@@ -930,6 +968,16 @@ int plan_inverse(sde_plan *pl) {
         SDE_CHECK_LAUNCH();
     }
     pl->inv = inv;
+    return SDE_OK;
+}
+
+int plan_fold_lo(sde_plan *pl, float2 *raw, float2 *raw_lo) {
+    if (!raw_lo || !pl->core_lo) return SDE_OK;
+    sde_ctx *ctx = pl->ctx;
+    KTimer kt(ctx, "fold_lo");
+    const int ncu = pl->ntu + 1, ncv = pl->ntv + 1;
+    k_fold_lo<<<ncu * ncv, 256, 0, ctx->stream>>>(raw, raw_lo, pl->core_lo, ncu, pl->spec.nv, pl->pitch);
+    SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
 

@@ -59,11 +59,9 @@ extern "C" int sde_uvmap(sde_ctx *ctx, const sde_uvmap_args *a, int64_t nvis, co
     if (rc == SDE_OK && a->out_where == SDE_HOST)
         rc = ctx_scratch(ctx, "job_dirty", sizeof(float) * (size_t)npix, (void **)&ddirty);
     float sw = 0.0f;
-    if (rc == SDE_OK) rc = sde_plan_grid(pl, SDE_GRID_PSF, grid, pitch, &sw);
-    if (rc == SDE_OK) rc = sde_image_from_grid(ctx, grid, pitch, a->nx, a->ny, fnu, nv, 1, nullptr, dpsf);
+    if (rc == SDE_OK) rc = sde_plan_image(pl, SDE_GRID_PSF, a->nx, a->ny, 1, nullptr, dpsf, grid, pitch, &sw);
     if (rc == SDE_OK) rc = sde_image_max(ctx, dpsf, npix, peak);
-    if (rc == SDE_OK) rc = sde_plan_grid(pl, SDE_GRID_VIS, grid, pitch, nullptr);
-    if (rc == SDE_OK) rc = sde_image_from_grid(ctx, grid, pitch, a->nx, a->ny, fnu, nv, 1, peak, ddirty);
+    if (rc == SDE_OK) rc = sde_plan_image(pl, SDE_GRID_VIS, a->nx, a->ny, 1, peak, ddirty, grid, pitch, nullptr);
     if (rc == SDE_OK && psf) rc = sde_image_scale_by_inverse(ctx, dpsf, npix, peak);
     if (rc == SDE_OK) {
         cudaError_t e = cudaSuccess;

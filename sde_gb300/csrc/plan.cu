@@ -301,6 +301,20 @@ __global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t 
 
 // dense flag of each work item: its tile's items (contiguous, sorted by tile) together
 // hold >= DENSE_TILE_VIS visibilities
+// Raw-grid cores of the compensation plane: the footprint of a tile (tu, tv) (its 64x64
+// cells and 3-cell halo, raw rows [64 tv - 3, 64 tv + 67), raw indices [64 tu - 2,
+// 64 tu + 68)) lies in cores (tu, tv), (tu+1, tv), (tu, tv+1), (tu+1, tv+1), where core
+// (cu, cv) is raw rows [64 cv - 3, 64 cv + 61) x raw indices [64 cu - 2, 64 cu + 62).
+__global__ void k_core_lo(const WorkItem *items, int64_t nitems, int ntu, uint8_t *core) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nitems || !items[t].dense) return;
+    const int tu = items[t].tile % ntu, tv = items[t].tile / ntu, ncu = ntu + 1;
+    core[tv * ncu + tu] = 1;
+    core[tv * ncu + tu + 1] = 1;
+    core[(tv + 1) * ncu + tu] = 1;
+    core[(tv + 1) * ncu + tu + 1] = 1;
+}
+
 __global__ void k_item_dense(WorkItem *items, int64_t nitems) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nitems) return;
@@ -359,7 +373,7 @@ int sde_plan_destroy(sde_plan *pl) {
     cudaSetDevice(ctx->device);
     // stream-ordered frees: after the plan's last use on the context's stream
     void *ptrs[] = {pl->fobs, pl->rec, pl->wt, pl->gdd, pl->orig, pl->rot, pl->gconj, pl->chunks,
-                    pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums, pl->inv};
+                    pl->items, pl->exc, pl->wt_all, pl->cf, pl->cft, pl->d_sums, pl->inv, pl->core_lo};
     for (void *p : ptrs) ctx_free(ctx, p, 0);
     ctx->bytes -= pl->bytes;
     delete pl;
@@ -403,7 +417,7 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
     pl->ctx = ctx;
     pl->spec = *spec;
     pl->doshift = (spec->shift[0] != 1.0) || (spec->shift[4] != 1.0) || (spec->shift[8] != 1.0);
-    pl->pitch = sde_grid_pitch(spec->nu);
+    pl->pitch = plan_pitch(spec->nu);
     pl->ntu = (spec->nu + TILE - 1) / TILE;
     pl->ntv = (spec->nv + TILE - 1) / TILE;
     pl->nvis_in = nvis;
@@ -582,6 +596,11 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
             k_item_vend<<<ceil_div(nitems, T), T, 0, st>>>(pl->items, nitems, nvalid);
             PL_CUDA(cudaGetLastError());
             k_item_dense<<<ceil_div(nitems, T), T, 0, st>>>(pl->items, nitems);
+            PL_CUDA(cudaGetLastError());
+            const size_t ncore = (size_t)(pl->ntu + 1) * (pl->ntv + 1);
+            PL_TRY(plan_alloc(pl, (void **)&pl->core_lo, ncore));
+            PL_CUDA(cudaMemsetAsync(pl->core_lo, 0, ncore, st));
+            k_core_lo<<<ceil_div(nitems, T), T, 0, st>>>(pl->items, nitems, pl->ntu, pl->core_lo);
             PL_CUDA(cudaGetLastError());
         }
         // gridding function: the context's 'SF' table

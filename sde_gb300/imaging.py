@@ -280,6 +280,19 @@ class Plan:
                                   _ptr(out), self.geom.pitch, C.byref(sw)), "sde_plan_grid")
         return sw.value
 
+    def image(self, image, grid=None, psf=False, correct=True, scale_dev=None, sumwt=False):
+        """Dirty image (or PSF) of the plan into image (sde_plan_image: GRDH2D then FFTR2D's
+        inverse with PIXCOR2D's correction, divided by scale_dev[0] if given; the finalize
+        runs inside the column pass).  grid, if given, receives the column-transformed grid.
+        Returns GRDH2D's SUMWT when sumwt (a synchronisation), else None."""
+        sw = C.c_float() if sumwt else None
+        check(lib().sde_plan_image(self.h, _abi.SDE_GRID_PSF if psf else _abi.SDE_GRID_VIS,
+                                   self.geom.nx, self.geom.ny, int(correct),
+                                   None if scale_dev is None else _ptr(scale_dev), _ptr(image),
+                                   None if grid is None else _ptr(grid), self.geom.pitch,
+                                   C.byref(sw) if sumwt else None), "sde_plan_image")
+        return sw.value if sumwt else None
+
     def grid_async(self, out, psf=False):
         check(lib().sde_plan_grid(self.h, _abi.SDE_GRID_PSF if psf else _abi.SDE_GRID_VIS,
                                   _ptr(out), self.geom.pitch, None), "sde_plan_grid")
@@ -317,12 +330,10 @@ def uvmap(ctx, geom, u, v, w, vis, wt, rmode="UNIFORM", robust=(0.0, 0.0, 0.0), 
     psf = ctx.image_buffer(geom)
     dirty = ctx.image_buffer(geom)
     maxpsf = ctx.zeros(1, torch.float32)
-    sumwt = plan.grid(grid, psf=True)
-    ctx.image_from_grid(geom, grid, psf)
+    sumwt = plan.image(psf, grid, psf=True, sumwt=True)
     ctx.image_max(psf, maxpsf)
     ctx.scale_by_inverse(psf, maxpsf)
-    plan.grid(grid, psf=False)
-    ctx.image_from_grid(geom, grid, dirty, scale_dev=maxpsf)
+    plan.image(dirty, grid, scale_dev=maxpsf)
     return dict(dirty=dirty, psf=psf, maxpsf=maxpsf, sumwt=sumwt, plan=plan, wstats=wst,
                 grid=grid)
 
@@ -363,8 +374,7 @@ class MajorCycle:
         self.model = ctx.zeros((geom.ny, geom.nx), ctx.torch.float32)
 
     def grid_step(self):
-        self.plan.grid_async(self.grid)
-        self.ctx.image_from_grid(self.geom, self.grid, self.dirty, scale_dev=self.maxpsf)
+        self.plan.image(self.dirty, self.grid, scale_dev=self.maxpsf)
         return self.dirty
 
     def degrid_step(self, model_image):

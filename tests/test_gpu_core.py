@@ -148,6 +148,39 @@ def test_uvmap_matches_reference(gpu_ctx, orc, obs_small, obs_shift, case, rmode
     res["plan"].close()
 
 
+@pytest.mark.parametrize("imsize,cell", [(256, 2.0), (2048, 0.25)])
+def test_plan_image_equals_grid_then_fft(gpu_ctx, obs_small, imsize, cell):
+    """sde_plan_image (GRDH2D's finalize inside the column pass where that pass is TMA-fed,
+    2048 rows and up) gives the image and column-transformed grid of sde_plan_grid +
+    sde_image_from_grid, for the PSF and the PSF-normalised dirty image.  Two gridding passes
+    differ at FP32 rounding (work items meet in the raw grid through atomic adds in no fixed
+    order), so the bars are the image bars: 1e-5 of the peak inside the CLEAN window, 5e-3
+    over the image (grid correction amplifies rounding at the corners), 1e-5 of the grid peak."""
+    from sde_gb300.imaging import Geom, Plan
+    o = obs_small
+    ctx = gpu_ctx
+    g = Geom(imsize, cell, vdec=o["vdec"])
+    t = {k: _dev(ctx, o[k]) for k in ("u", "v", "w", "wt", "vis")}
+    plan = Plan(ctx, g, t["u"], t["v"], t["w"], t["vis"], t["wt"])
+    torch = ctx.torch
+    for psf in (True, False):
+        peak = ctx.zeros(1, torch.float32) + 0.5
+        ga, gb = ctx.grid_buffer(g), ctx.grid_buffer(g)
+        ia, ib = ctx.image_buffer(g), ctx.image_buffer(g)
+        sw_a = plan.grid(ga, psf=psf)
+        ctx.image_from_grid(g, ga, ia, scale_dev=None if psf else peak)
+        sw_b = plan.image(ib, gb, psf=psf, scale_dev=None if psf else peak, sumwt=True)
+        ctx.sync()
+        assert sw_a == sw_b
+        a, b = ia.cpu().numpy(), ib.cpu().numpy()
+        w = _window(imsize)
+        pk = np.abs(a).max()
+        assert np.abs(a - b)[w, w].max() / pk < 1e-5
+        assert np.abs(a - b).max() / pk < 5e-3
+        assert float((ga - gb).abs().max()) / float(ga.abs().max()) < 1e-5
+    plan.close()
+
+
 @pytest.mark.parametrize("case", ["small", "shift"])
 def test_degrid_matches_grddeh2d(gpu_ctx, orc, obs_small, obs_shift, case):
     from sde_gb300.imaging import Plan
