@@ -50,19 +50,6 @@ __device__ __forceinline__ MosaicPixel mosaic_pixel(const MosaicPointing &p, int
     return r;
 }
 
-// num += wt PB image over every pointing's pixels (task/mosclean.f:413-432's numerator)
-__global__ void __launch_bounds__(256) k_mosaic_num(const MosaicPointing *__restrict__ pts,
-                                                    const uint16_t *__restrict__ blk, int mnx, int mny,
-                                                    float *num) {
-    const MosaicPointing p = pts[blk[blockIdx.x]];
-    const int64_t base = (int64_t)(blockIdx.x - p.block0) * BATCH_BLOCK_CELLS;
-#pragma unroll
-    for (int j = 0; j < BATCH_BLOCK_CELLS / 256; j++) {
-        const MosaicPixel q = mosaic_pixel(p, base + j * 256 + threadIdx.x, mnx, mny);
-        if (q.in) atomicAdd(&num[q.m], p.wt * q.pb * p.image[q.k]);
-    }
-}
-
 // den += wt PB^2 (the denominator; once per layout)
 __global__ void __launch_bounds__(256) k_mosaic_den(const MosaicPointing *__restrict__ pts,
                                                     const uint16_t *__restrict__ blk, int mnx, int mny,
@@ -84,11 +71,42 @@ __global__ void k_mosaic_invden(float *den, int64_t n, const float *__restrict__
     den[k] = (d > 0.f && d > clip * *denmax) ? 1.0f / d : 0.f;
 }
 
-__global__ void k_mosaic_scale(const float *__restrict__ num, const float *__restrict__ invden,
-                               int64_t n, float *out) {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    out[k] = num[k] * invden[k];
+// The mosaic by gather: block = one MOS_TILE x MOS_TILE tile of the mosaic; every pixel sums
+// wt PB I over the tile's pointings (in pointing order) and takes the stored 1/den.
+constexpr int MOS_TILE = 64;
+__global__ void __launch_bounds__(256) k_mosaic_gather(const MosaicPointing *__restrict__ pts,
+                                                       const int32_t *__restrict__ tstart,
+                                                       const uint16_t *__restrict__ tpts, int mtx, int mnx,
+                                                       int mny, const float *__restrict__ invden, float *out) {
+    const int tx = blockIdx.x % mtx, ty = blockIdx.x / mtx;
+    const int p0 = tstart[blockIdx.x], p1 = tstart[blockIdx.x + 1];
+    constexpr int PER = MOS_TILE * MOS_TILE / 256;
+    float acc[PER];
+#pragma unroll
+    for (int j = 0; j < PER; j++) acc[j] = 0.f;
+    for (int pi = p0; pi < p1; pi++) {
+        const MosaicPointing p = pts[tpts[pi]];
+        const int cenx = (p.nx + 1) / 2 - 1, ceny = (p.ny + 1) / 2 - 1;
+        const int ox = p.cx - 1 - cenx, oy = p.cy - 1 - ceny;  // mosaic pixel of image (0, 0)
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int k = threadIdx.x + j * 256;
+            const int mx = tx * MOS_TILE + (k & (MOS_TILE - 1)), my = ty * MOS_TILE + k / MOS_TILE;
+            const int ix = mx - ox, iy = my - oy;
+            if (ix < 0 || ix >= p.nx || iy < 0 || iy >= p.ny) continue;
+            const float dx = (float)(ix - cenx), dy = (float)(iy - ceny);
+            const float pb = expf(-p.pbk * (dx * dx + dy * dy));
+            acc[j] += p.wt * pb * p.image[(int64_t)iy * p.nx + ix];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const int k = threadIdx.x + j * 256;
+        const int mx = tx * MOS_TILE + (k & (MOS_TILE - 1)), my = ty * MOS_TILE + k / MOS_TILE;
+        if (mx >= mnx || my >= mny) continue;
+        const int64_t m = (int64_t)my * mnx + mx;
+        out[m] = acc[j] * invden[m];
+    }
 }
 
 __global__ void k_max_batch(float *const *__restrict__ images, const int64_t *__restrict__ npix,
@@ -149,6 +167,10 @@ struct sde_batch {
     MosaicPointing *d_pts = nullptr;
     uint16_t *d_pts_blk = nullptr;             // pointing of each block of the mosaic launches
     int64_t pts_nblk = 0;
+    // per MOS_TILE x MOS_TILE mosaic tile, the pointings whose image covers it (CSR)
+    int mtx = 0, mty = 0;
+    int32_t *d_tile_start = nullptr;
+    uint16_t *d_tile_pts = nullptr;
     // num = sum wt PB I (per pass); invden = 1 / sum wt PB^2 where that sum passes the clip,
     // else 0 (fixed by the layout: computed once in sde_batch_set_mosaic)
     float *d_num = nullptr, *d_invden = nullptr, *d_denmax = nullptr, *d_mosaic = nullptr;
@@ -216,19 +238,10 @@ int batch_fft(sde_batch *b, const std::vector<float *> &out, const float *peaks)
 int batch_mosaic(sde_batch *b) {
     if (!b->d_pts) return SDE_OK;
     sde_ctx *ctx = b->ctx;
-    const int64_t m = (int64_t)b->mnx * b->mny;
-    SDE_CUDA_TRY(cudaMemsetAsync(b->d_num, 0, sizeof(float) * (size_t)m, ctx->stream));
-    {
-        KTimer kt(ctx, "mosaic_accum");
-        k_mosaic_num<<<(unsigned)b->pts_nblk, 256, 0, ctx->stream>>>(b->d_pts, b->d_pts_blk, b->mnx,
-                                                                    b->mny, b->d_num);
-        SDE_CHECK_LAUNCH();
-    }
-    {
-        KTimer kt(ctx, "mosaic_div");
-        k_mosaic_scale<<<ceil_div(m, 256), 256, 0, ctx->stream>>>(b->d_num, b->d_invden, m, b->d_mosaic);
-        SDE_CHECK_LAUNCH();
-    }
+    KTimer kt(ctx, "mosaic_gather");
+    k_mosaic_gather<<<(unsigned)(b->mtx * b->mty), 256, 0, ctx->stream>>>(
+        b->d_pts, b->d_tile_start, b->d_tile_pts, b->mtx, b->mnx, b->mny, b->d_invden, b->d_mosaic);
+    SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
 
@@ -436,7 +449,34 @@ extern "C" int sde_batch_set_mosaic(sde_batch *b, int mnx, int mny, const int *c
     b->mnx = mnx;
     b->mny = mny;
     b->clip = clip;
+    // per mosaic tile, the pointings whose image covers it (in pointing order)
+    const int mtx = (mnx + MOS_TILE - 1) / MOS_TILE, mty = (mny + MOS_TILE - 1) / MOS_TILE;
+    std::vector<std::vector<uint16_t>> lists((size_t)mtx * mty);
+    for (int i = 0; i < b->n; i++) {
+        const int ox = cx[i] - 1 - ((b->nx[i] + 1) / 2 - 1), oy = cy[i] - 1 - ((b->ny[i] + 1) / 2 - 1);
+        const int x0 = std::max(ox, 0), x1 = std::min(ox + b->nx[i], mnx);
+        const int y0 = std::max(oy, 0), y1 = std::min(oy + b->ny[i], mny);
+        if (x0 >= x1 || y0 >= y1) continue;
+        for (int ty = y0 / MOS_TILE; ty <= (y1 - 1) / MOS_TILE; ty++)
+            for (int tx = x0 / MOS_TILE; tx <= (x1 - 1) / MOS_TILE; tx++)
+                lists[(size_t)ty * mtx + tx].push_back((uint16_t)i);
+    }
+    std::vector<int32_t> tstart(lists.size() + 1, 0);
+    std::vector<uint16_t> tpts;
+    for (size_t t = 0; t < lists.size(); t++) {
+        tpts.insert(tpts.end(), lists[t].begin(), lists[t].end());
+        tstart[t + 1] = (int32_t)tpts.size();
+    }
+    if (tpts.empty()) tpts.push_back(0);
+    if (!b->d_tile_start) {
+        SDE_TRY(batch_alloc(b, (void **)&b->d_tile_start, sizeof(int32_t) * tstart.size()));
+        SDE_TRY(batch_alloc(b, (void **)&b->d_tile_pts, sizeof(uint16_t) * (size_t)b->n * mtx * mty));
+    }
+    b->mtx = mtx;
+    b->mty = mty;
     cudaStream_t st = b->ctx->stream;
+    SDE_CUDA_TRY(cudaMemcpyAsync(b->d_tile_start, tstart.data(), sizeof(int32_t) * tstart.size(), cudaMemcpyHostToDevice, st));
+    SDE_CUDA_TRY(cudaMemcpyAsync(b->d_tile_pts, tpts.data(), sizeof(uint16_t) * tpts.size(), cudaMemcpyHostToDevice, st));
     SDE_CUDA_TRY(cudaMemcpyAsync(b->d_pts, h.data(), sizeof(MosaicPointing) * b->n, cudaMemcpyHostToDevice, st));
     SDE_CUDA_TRY(cudaMemcpyAsync(b->d_pts_blk, pblk.data(), sizeof(uint16_t) * pblk.size(), cudaMemcpyHostToDevice, st));
     // the denominator and its clip depend on the layout only
