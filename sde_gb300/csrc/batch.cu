@@ -153,12 +153,18 @@ struct sde_batch {
     unsigned long long *d_counter = nullptr;
     FinalizeDesc *d_fin = nullptr;
     uint16_t *d_fin_blk = nullptr;             // grid of each block of the flattened finalize
-    int64_t fin_nblk = 0;
+    int64_t fin_nblk = 0;                      // (plans whose shape has no fused column pass)
+    std::vector<FinalizeDesc> hfin;            // host copy: the fused column passes' parameters
+    int2 *d_fold = nullptr;                    // (plan, core) pairs of the compensation fold
+    int64_t fold_n = 0;
     float **d_psf_ptrs = nullptr;
     int64_t *d_npix = nullptr;
     int64_t max_cells = 0;
-    size_t raw_bytes = 0;                      // the raw grids are contiguous from raw[0]
+    // raw grids: every plan's hi plane, contiguous from raw[0] (hi_bytes), then (comp) every
+    // plan's compensation plane; raw_bytes covers both
+    size_t raw_bytes = 0, hi_bytes = 0;
     bool comp = true;                          // compensated cross-item sums (raw_lo planes)
+    bool lo_clean = false;                     // compensation planes all zero (folded)
     // shape class (fnu, nv, nx, ny, pitch) -> plan indices
     std::map<std::tuple<int, int, int, int, int>, std::vector<int>> classes;
     // mosaic
@@ -198,12 +204,20 @@ int batch_alloc(sde_batch *b, void **p, size_t bytes) {
 }
 
 // the launches of one gridding pass of every plan (PSF or visibilities)
+// The compensation planes are written only inside the plans' marked cores and the fold
+// zeroes what it adds, so after the first pass only the hi planes are cleared.  Grids of a
+// shape with a fused column pass are finalized inside it (batch_fft).
 int batch_grid(sde_batch *b, int psf) {
     sde_ctx *ctx = b->ctx;
     SDE_CUDA_TRY(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), ctx->stream));
-    SDE_CUDA_TRY(cudaMemsetAsync(b->raw[0], 0, b->raw_bytes, ctx->stream));
+    SDE_CUDA_TRY(cudaMemsetAsync(b->raw[0], 0, b->lo_clean ? b->hi_bytes : b->raw_bytes, ctx->stream));
+    b->lo_clean = false;
     SDE_TRY(launch_grid_batch(ctx, psf, b->comp, b->d_plans, b->d_item_start, b->n, b->d_counter,
                               ctx->d_cft, ctx->num_sms * grid_ctas_per_sm()));
+    if (b->comp) {
+        SDE_TRY(launch_fold_lo_batch(ctx, b->d_plans, b->d_fold, b->fold_n));
+        b->lo_clean = true;
+    }
     SDE_TRY(launch_finalize_batch(ctx, b->d_fin, b->d_fin_blk, b->fin_nblk));
     return SDE_OK;
 }
@@ -213,6 +227,19 @@ int batch_fft(sde_batch *b, const std::vector<float *> &out, const float *peaks)
     for (auto &kv : b->classes) {
         const int fnu = std::get<0>(kv.first), nv = std::get<1>(kv.first);
         const int nx = std::get<2>(kv.first), ny = std::get<3>(kv.first), pitch = std::get<4>(kv.first);
+        if (fin_fused_shape(fnu / 2 + 1, nv)) {
+            std::vector<FinalizeDesc> fd;
+            std::vector<float *> im;
+            std::vector<const float *> sc;
+            for (int i : kv.second) {
+                fd.push_back(b->hfin[i]);
+                im.push_back(out[i]);
+                sc.push_back(peaks ? peaks + i : nullptr);
+            }
+            SDE_TRY(fft_images_from_raw(b->ctx, (int)fd.size(), fd.data(), im.data(),
+                                        peaks ? sc.data() : nullptr, nx, ny, 1));
+            continue;
+        }
         std::vector<float2 *> g;
         std::vector<float *> im;
         std::vector<const float *> sc;
@@ -282,7 +309,7 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
     std::vector<int64_t> start(n + 1, 0);
     std::vector<FinalizeDesc> hf(n);
     std::vector<size_t> raw_off(n), img_off(n);
-    size_t raw_total = 0, img_total = 0;
+    size_t raw_total = 0, img_total = 0;  // raw_total: the hi planes (the grids have the same layout)
     for (int i = 0; i < n; i++) {
         sde_plan *pl = plans[i];
         if (!pl || pl->ctx != ctx || nx[i] < 1 || ny[i] < 1) {
@@ -315,7 +342,7 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
         b->ny.push_back(ny[i]);
         const size_t cells = (size_t)nv * pl->pitch;
         raw_off[i] = raw_total;
-        raw_total += (cells * 8 * (b->comp ? 2 : 1) + 255) & ~(size_t)255;
+        raw_total += (cells * 8 + 255) & ~(size_t)255;
         img_off[i] = img_total;
         img_total += ((size_t)nx[i] * ny[i] * 4 + 255) & ~(size_t)255;
         b->max_cells = std::max<int64_t>(b->max_cells, (int64_t)cells);
@@ -328,7 +355,7 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
         rc = (x);                             \
         if (rc != SDE_OK) goto fail;          \
     } while (0)
-    B_TRY(batch_alloc(b, (void **)&rawmem, raw_total));
+    B_TRY(batch_alloc(b, (void **)&rawmem, raw_total * (b->comp ? 2 : 1)));
     B_TRY(batch_alloc(b, (void **)&gridmem, raw_total));
     B_TRY(batch_alloc(b, (void **)&imgmem, 2 * img_total));
     B_TRY(batch_alloc(b, (void **)&b->d_peak, sizeof(float) * n));
@@ -337,22 +364,26 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
     B_TRY(batch_alloc(b, (void **)&b->d_counter, sizeof(unsigned long long)));
     B_TRY(batch_alloc(b, (void **)&b->d_fin, sizeof(FinalizeDesc) * n));
     for (int i = 0; i < n; i++)
-        b->fin_nblk += ceil_div((int64_t)b->plans[i]->spec.nv * b->plans[i]->pitch, BATCH_BLOCK_CELLS);
-    B_TRY(batch_alloc(b, (void **)&b->d_fin_blk, sizeof(uint16_t) * (size_t)b->fin_nblk));
+        if (!fin_fused_shape(b->plans[i]->spec.nu, b->plans[i]->spec.nv))
+            b->fin_nblk += ceil_div((int64_t)b->plans[i]->spec.nv * b->plans[i]->pitch, BATCH_BLOCK_CELLS);
+    if (b->fin_nblk > 0)
+        B_TRY(batch_alloc(b, (void **)&b->d_fin_blk, sizeof(uint16_t) * (size_t)b->fin_nblk));
     B_TRY(batch_alloc(b, (void **)&b->d_psf_ptrs, sizeof(float *) * n));
     B_TRY(batch_alloc(b, (void **)&b->d_npix, sizeof(int64_t) * n));
-    b->raw_bytes = raw_total;
+    b->hi_bytes = raw_total;
+    b->raw_bytes = raw_total * (b->comp ? 2 : 1);
     for (int i = 0; i < n; i++) {
         sde_plan *pl = b->plans[i];
         b->raw.push_back(reinterpret_cast<float2 *>(rawmem + raw_off[i]));
         b->grid.push_back(reinterpret_cast<float2 *>(gridmem + raw_off[i]));
         b->psf.push_back(reinterpret_cast<float *>(imgmem + img_off[i]));
         b->image.push_back(reinterpret_cast<float *>(imgmem + img_total + img_off[i]));
-        float2 *lo = b->comp ? b->raw[i] + (size_t)pl->spec.nv * pl->pitch : nullptr;
+        float2 *lo = b->comp ? reinterpret_cast<float2 *>(rawmem + raw_total + raw_off[i]) : nullptr;
         hp[i] = BatchPlan{pl->items, pl->chunks, pl->rec, b->raw[i], lo, pl->pitch, pl->ntu, pl->spec.nu,
                           pl->spec.nv};
         const float scale = (float)((double)((float)(pl->spec.nu - 1) * (float)pl->spec.nv) / pl->h_lsumwt);
-        hf[i] = FinalizeDesc{b->raw[i], lo, b->grid[i], pl->spec.nu, pl->spec.nv, pl->pitch,
+        // the compensation planes are folded into raw before the finalize reads it
+        hf[i] = FinalizeDesc{b->raw[i], nullptr, b->grid[i], pl->spec.nu, pl->spec.nv, pl->pitch,
                              pl->spec.uorigin, pl->spec.vorigin, pl->spec.supp, scale, 0};
     }
     {
@@ -361,15 +392,43 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
         std::vector<uint16_t> fblk((size_t)b->fin_nblk);
         for (int i = 0, k = 0; i < n; i++) {
             hf[i].block0 = k;
+            if (fin_fused_shape(hf[i].nu, hf[i].nv)) continue;
             const int64_t nb = ceil_div((int64_t)hf[i].nv * hf[i].pitch, BATCH_BLOCK_CELLS);
             for (int64_t j = 0; j < nb; j++) fblk[(size_t)k++] = (uint16_t)i;
         }
         cudaStream_t st = ctx->stream;
         cudaError_t e = cudaSuccess;
+        // the (plan, core) pairs to fold: the plans' marked cores (read back once)
+        std::vector<int2> fold;
+        if (b->comp) {
+            for (int i = 0; i < n && e == cudaSuccess; i++) {
+                const sde_plan *pl = b->plans[i];
+                if (!pl->core_lo) continue;
+                const int ncu = pl->ntu + 1, ncv = pl->ntv + 1;
+                if (ncu > 0xFFFF || ncv > 0x7FFF) {
+                    sde_set_error("sde_batch_create: plan %d grid too large for the batch fold", i);
+                    rc = SDE_EINVAL;
+                    goto fail;
+                }
+                std::vector<uint8_t> core((size_t)ncu * ncv);
+                e = cudaMemcpyAsync(core.data(), pl->core_lo, core.size(), cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                for (int cv = 0; cv < ncv && e == cudaSuccess; cv++)
+                    for (int cu = 0; cu < ncu; cu++)
+                        if (core[(size_t)cv * ncu + cu]) fold.push_back(make_int2(i, cu | (cv << 16)));
+            }
+        }
+        if (e == cudaSuccess && !fold.empty()) {
+            b->fold_n = (int64_t)fold.size();
+            rc = batch_alloc(b, (void **)&b->d_fold, sizeof(int2) * fold.size());
+            if (rc != SDE_OK) goto fail;
+            e = cudaMemcpyAsync(b->d_fold, fold.data(), sizeof(int2) * fold.size(), cudaMemcpyHostToDevice, st);
+        }
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_plans, hp.data(), sizeof(BatchPlan) * n, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_item_start, start.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_fin, hf.data(), sizeof(FinalizeDesc) * n, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_fin_blk, fblk.data(), sizeof(uint16_t) * fblk.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && !fblk.empty())
+            e = cudaMemcpyAsync(b->d_fin_blk, fblk.data(), sizeof(uint16_t) * fblk.size(), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_psf_ptrs, b->psf.data(), sizeof(float *) * n, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_npix, npix.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -379,6 +438,7 @@ extern "C" int sde_batch_create(sde_ctx *ctx, int n, sde_plan *const *plans, con
             goto fail;
         }
     }
+    b->hfin = hf;
     *out = b;
     return SDE_OK;
 fail:

@@ -250,19 +250,27 @@ struct FftBatch {
     const float *scale[FFT_MAXB];
 };
 size_t grid_smem_bytes();
-int grid_ctas_per_sm();
+int grid_ctas_per_sm();  // resident persistent gridding CTAs per SM
 // 2-D FP32 tensor map for cp.async.bulk.tensor (grid.cu): width floats x rows, row pitch in
 // bytes, box box_w x box_h; out-of-range elements read as zero and are not written
 int encode_tmap_f32_2d(CUtensorMap *map, const void *base, uint64_t width, uint64_t rows,
-                       uint64_t row_bytes, uint32_t box_w, uint32_t box_h);  // resident persistent gridding CTAs per SM
+                       uint64_t row_bytes, uint32_t box_w, uint32_t box_h);
 int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
                       const int64_t *d_item_start, int nplans, unsigned long long *d_counter,
                       const float *cft, int nctas);
 // finalize of n grids in one flattened launch: blk[b] = the grid of block b (nblk blocks)
 int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, const uint16_t *blk, int64_t nblk);
+// compensation planes of a batch folded into their raw grids: block b folds core cores[b].y
+// (cu | cv << 16) of plan cores[b].x (its raw and raw_lo)
+int launch_fold_lo_batch(sde_ctx *ctx, const BatchPlan *d_plans, const int2 *cores, int64_t ncores);
+int check_fft_shape(int nx, int ny, int fnu, int nv);  // SDE_EINVAL + message if unsupported
+// batched images from raw accumulations (fft.cu; EINVAL when the shape has no fused path;
+// fin_fused_shape says which grids have one)
+bool fin_fused_shape(int nu, int nv);
+int fft_images_from_raw(sde_ctx *ctx, int n, const FinalizeDesc *fd, float *const *images,
+                        const float *const *scales, int nx, int ny, int correct);
 // grid -> image for n same-shape grids (inverse column pass, row c2r with grid correction
 // and scale 1/scales[i] when scales[i] != NULL); SDE_EINVAL if the shape has no batched form
-int check_fft_shape(int nx, int ny, int fnu, int nv);  // SDE_EINVAL + message if unsupported
 int fft_images_from_grids(sde_ctx *ctx, int n, float2 *const *grids, float *const *images,
                           const float *const *scales, int pitch, int nx, int ny, int fnu, int nv,
                           int correct);

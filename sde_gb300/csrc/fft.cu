@@ -845,6 +845,10 @@ struct FinParams {
     int raw_pitch, nu, nv, uorigin, vorigin, supp;
     float scale;
 };
+constexpr int FIN_MAXB = 8;  // grids per finalize-fused column launch (load + store maps)
+struct FinBatch {
+    FinParams f[FIN_MAXB];
+};
 __device__ __forceinline__ float2 fin_cell(const FinParams &f, float2 r, int u, int v) {
     const int u1 = u + 1, v1 = v + 1;
     if (u1 > f.nu - f.supp) return make_float2(0.f, 0.f);
@@ -963,7 +967,8 @@ struct TmaBatch {
 template <int LOGN, bool INV, bool FIN>
 __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
     k_col_fft_tma(const __grid_constant__ TmaBatch tb, const float2 *__restrict__ tw, int r0,
-                  int r1, int *status, int store_off, FinParams fp) {
+                  int r1, int *status, int store_off, const __grid_constant__ FinBatch fb) {
+    const FinParams &fp = fb.f[FIN ? blockIdx.y : 0];
     const CUtensorMap *tmap = &tb.map[blockIdx.y];
     const CUtensorMap *smap = &tb.map[blockIdx.y + store_off];
     const int xl = 4 * blockIdx.x + (FIN ? 2 * RAW_SHIFT : 0);  // load box: raw index u0+4
@@ -1023,7 +1028,7 @@ __global__ void __launch_bounds__(ColTma<LOGN>::T, ColTma<LOGN>::MINB)
 
 template <int LOGN>
 cudaError_t launch_col_tma(const TmaBatch &map, int nbatch, int nu, const float2 *tw, bool inverse,
-                           int r0, int r1, int *status, cudaStream_t st, const FinParams *fin = nullptr) {
+                           int r0, int r1, int *status, cudaStream_t st, const FinBatch *fin = nullptr) {
     using S = ColTma<LOGN>;
     const dim3 nb((unsigned)((nu + 1) / 2), (unsigned)nbatch);
     cudaError_t e;
@@ -1036,12 +1041,12 @@ cudaError_t launch_col_tma(const TmaBatch &map, int nbatch, int nu, const float2
         e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)S::SMEM);
         if (e != cudaSuccess) return e;
-        k_col_fft_tma<LOGN, true, false><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status, 0, FinParams{});
+        k_col_fft_tma<LOGN, true, false><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status, 0, FinBatch{});
     } else {
         e = cudaFuncSetAttribute(k_col_fft_tma<LOGN, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)S::SMEM);
         if (e != cudaSuccess) return e;
-        k_col_fft_tma<LOGN, false, false><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status, 0, FinParams{});
+        k_col_fft_tma<LOGN, false, false><<<nb, S::T, S::SMEM, st>>>(map, tw, r0, r1, status, 0, FinBatch{});
     }
     return cudaGetLastError();
 }
@@ -1387,6 +1392,70 @@ int fft_images_from_grids(sde_ctx *ctx, int n, float2 *const *grids, float *cons
     return SDE_OK;
 }
 
+bool fin_fused_shape(int nu, int nv) {
+    const int logn = ilog2(nv);
+    return logn >= 11 && logn <= 13 && (1 << logn) == nv && nu >= 2;
+}
+
+// Images of n same-shape gridding passes straight from their raw accumulations (compensation
+// planes already folded: every fd[i].raw_lo is NULL): finalize-fused TMA column passes,
+// FIN_MAXB grids per launch (fd[i].out receives the finalized, column-transformed grid), then
+// the batched row c2r pass.  Shapes without a fused column pass: EINVAL.
+int fft_images_from_raw(sde_ctx *ctx, int n, const FinalizeDesc *fd, float *const *images,
+                        const float *const *scales, int nx, int ny, int correct) {
+    if (!ctx || n < 0) return SDE_EINVAL;
+    if (n == 0) return SDE_OK;
+    const int nu = fd[0].nu, nv = fd[0].nv, pitch = fd[0].pitch, fnu = 2 * (nu - 1);
+    for (int i = 0; i < n; i++)
+        if (fd[i].raw_lo || fd[i].nu != nu || fd[i].nv != nv || fd[i].pitch != pitch) return SDE_EINVAL;
+    SDE_TRY(check_fft_args(nx, ny, fnu, nv, pitch));
+    if (!fin_fused_shape(nu, nv)) return SDE_EINVAL;
+    const int logn = ilog2(nv), logh = ilog2(fnu / 2);
+    const float2 *twv, *twu;
+    SDE_TRY(ctx_twiddles(ctx, nv, &twv));
+    SDE_TRY(ctx_twiddles(ctx, fnu, &twu));
+    CorrParams cp = {nullptr, nullptr, nullptr};
+    if (correct) SDE_TRY(corr_params(ctx, nx, ny, &cp));
+    const int ibegy = (nv + 1) / 2 - (ny + 1) / 2;
+    {
+        KTimer kt(ctx, "col_fft_fin_batch");
+        for (int b0 = 0; b0 < n; b0 += FIN_MAXB) {
+            const int nb = n - b0 < FIN_MAXB ? n - b0 : FIN_MAXB;
+            TmaBatch tb;
+            FinBatch fb{};
+            for (int i = 0; i < nb; i++) {
+                const FinalizeDesc &f = fd[b0 + i];
+                SDE_TRY(encode_tmap_f32_2d(&tb.map[i], f.raw, (uint64_t)pitch * 2, (uint64_t)nv,
+                                           (uint64_t)pitch * 8, 4, 256));
+                SDE_TRY(encode_tmap_f32_2d(&tb.map[nb + i], f.out, (uint64_t)nu * 2, (uint64_t)nv,
+                                           (uint64_t)pitch * 8, 4, 256));
+                fb.f[i] = FinParams{f.raw, pitch, nu, nv, f.uorigin, f.vorigin, f.supp, f.scale};
+            }
+            cudaError_t e;
+            switch (logn) {
+                case 11: e = launch_col_tma<11>(tb, nb, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fb); break;
+                case 12: e = launch_col_tma<12>(tb, nb, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fb); break;
+                default: e = launch_col_tma<13>(tb, nb, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fb); break;
+            }
+            SDE_CUDA_TRY(e);
+        }
+    }
+    for (int b0 = 0; b0 < n; b0 += FFT_MAXB) {
+        const int nb = n - b0 < FFT_MAXB ? n - b0 : FFT_MAXB;
+        FftBatch bt{};
+        for (int i = 0; i < nb; i++) {
+            bt.grid[i] = fd[b0 + i].out;
+            bt.image[i] = images[b0 + i];
+            bt.scale[i] = scales ? scales[b0 + i] : nullptr;
+        }
+        cudaError_t e = cudaSuccess;
+        KTimer kt(ctx, "row_c2r_batch");
+        c2r_t(logh, bt, nb, pitch, nx, ny, ibegy, twu, cp, ctx->stream, &e, ctx->d_status);
+        SDE_CUDA_TRY(e);
+    }
+    return SDE_OK;
+}
+
 int check_fft_shape(int nx, int ny, int fnu, int nv) {
     return check_fft_args(nx, ny, fnu, nv, fnu / 2 + 1);
 }
@@ -1472,12 +1541,13 @@ int image_from_raw(sde_ctx *ctx, const float2 *raw, const float2 *raw_lo, int nu
                                    256));
         SDE_TRY(encode_tmap_f32_2d(&tb.map[1], grid, (uint64_t)nu * 2, (uint64_t)nv, (uint64_t)pitch * 8, 4,
                                    256));
-        const FinParams fp{raw, pitch, nu, nv, uorigin, vorigin, supp, scale};
+        FinBatch fb{};
+        fb.f[0] = FinParams{raw, pitch, nu, nv, uorigin, vorigin, supp, scale};
         cudaError_t e;
         switch (logn) {
-            case 11: e = launch_col_tma<11>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fp); break;
-            case 12: e = launch_col_tma<12>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fp); break;
-            default: e = launch_col_tma<13>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fp); break;
+            case 11: e = launch_col_tma<11>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fb); break;
+            case 12: e = launch_col_tma<12>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fb); break;
+            default: e = launch_col_tma<13>(tb, 1, nu, twv, true, 0, nv, ctx->d_status, ctx->stream, &fb); break;
         }
         SDE_CUDA_TRY(e);
     }

@@ -391,10 +391,7 @@ __device__ __forceinline__ float2 finalize_cell(const float2 *__restrict__ raw,
 // raw = raw + lo where lo != 0 (the add finalize would do), lo = 0.  A core row is 32 pairs
 // of cells starting at an even raw index (16-byte aligned: the pitch is a multiple of 4);
 // each thread loads 8 pairs before touching any.
-__global__ void __launch_bounds__(256) k_fold_lo(float2 *raw, float2 *raw_lo, const uint8_t *__restrict__ core,
-                                                 int ncu, int nv, int pitch) {
-    if (!core[blockIdx.x]) return;
-    const int cu = blockIdx.x % ncu, cv = blockIdx.x / ncu;
+__device__ __forceinline__ void fold_core(float2 *raw, float2 *raw_lo, int cu, int cv, int nv, int pitch) {
     const int r0 = cv * TILE - SUPP, i0 = cu * TILE - (SUPP - 1);
     float4 *raw4 = reinterpret_cast<float4 *>(raw);
     float4 *lo4 = reinterpret_cast<float4 *>(raw_lo);
@@ -422,6 +419,20 @@ __global__ void __launch_bounds__(256) k_fold_lo(float2 *raw, float2 *raw_lo, co
         raw4[q[j]] = h;
         lo4[q[j]] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
+}
+
+__global__ void __launch_bounds__(256) k_fold_lo(float2 *raw, float2 *raw_lo, const uint8_t *__restrict__ core,
+                                                 int ncu, int nv, int pitch) {
+    if (!core[blockIdx.x]) return;
+    fold_core(raw, raw_lo, blockIdx.x % ncu, blockIdx.x / ncu, nv, pitch);
+}
+
+// the marked cores of many grids, one block per (grid, core) pair of the list
+__global__ void __launch_bounds__(256) k_fold_lo_batch(const BatchPlan *__restrict__ d,
+                                                       const int2 *__restrict__ cores) {
+    const int2 c = cores[blockIdx.x];
+    const BatchPlan &p = d[c.x];
+    fold_core(p.raw, p.raw_lo, c.y & 0xFFFF, c.y >> 16, p.nv, p.pitch);
 }
 
 __global__ void k_finalize(const float2 *__restrict__ raw, const float2 *__restrict__ raw_lo,
@@ -915,6 +926,14 @@ int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, const uint16
     if (nblk <= 0) return SDE_OK;
     KTimer kt(ctx, "finalize_batch");
     k_finalize_batch<<<(unsigned)nblk, 256, 0, ctx->stream>>>(d_desc, blk);
+    SDE_CHECK_LAUNCH();
+    return SDE_OK;
+}
+
+int launch_fold_lo_batch(sde_ctx *ctx, const BatchPlan *d_plans, const int2 *cores, int64_t ncores) {
+    if (ncores <= 0) return SDE_OK;
+    KTimer kt(ctx, "fold_lo_batch");
+    k_fold_lo_batch<<<(unsigned)ncores, 256, 0, ctx->stream>>>(d_plans, cores);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
