@@ -350,6 +350,43 @@ int sde_batch_read(const sde_batch *b, int i, int which, float *dst, int64_t n);
 
 int sde_isamax(sde_ctx *ctx, const float *a, int64_t n, int64_t *index_out);
 
+/* Visibilities from a FITS random-groups file: the FTS branch of
+ * VISGET(NAME, FILENAME, STOKES, ...) (vis/visget.f:5, 40-46 -> FILGRPGE, VISSTD), for one
+ * Stokes parameter, into the arrays sde_plan_create takes.
+ *   sde_uvfits_open     parses the header (host only, no CUDA call) and checks what
+ *                       fts/ftsgrpre.f and vis/visstd.f check, with their messages
+ *                       ('Not a groups file', 'No groups!', 'Cannot read N-bit files',
+ *                       'First axis not COMPLEX', 'No stokes axes', 'No frequency',
+ *                       'PTYPE=UU not in header', 'Unable to read such data'); groups that
+ *                       hold more than one COMPLEX x STOKES block (several channels or IFs)
+ *                       are refused.
+ *   sde_uvfits_read     reads every group: u, v, w (nread floats each, wavelengths: PTYPE
+ *                       UU/VV/WW in seconds are scaled by SNGL(FREQ)), vis (nread complex64
+ *                       pairs), wt (nread floats) of Stokes stokes ('I', 'V', 'Q' or 'U';
+ *                       after RR/LL/RL/LR -> I/V/Q/U conversion, vis/visconvs.f,
+ *                       visconv2.f, visconvp.f), to host or device arrays of ngroups
+ *                       entries per where.  A file shorter than GCOUNT groups gives
+ *                       nread < ngroups and the reference's warning through msgput_
+ *                       (fts/ftsgrpre.f:254-258).  Synchronises. */
+typedef struct sde_uvfits sde_uvfits;
+typedef struct sde_uvfits_desc {
+    int64_t ngroups;         /* GCOUNT */
+    int64_t ngroups_in_file; /* whole groups the file holds (<= ngroups) */
+    int npar;                /* PCOUNT */
+    int bitpix;              /* 16, 32 or -32 */
+    int ncomplex;            /* 3: (re, im, wt); 2: (re, im) with a WEIGHT parameter */
+    int nstokes;
+    int iquv;                /* Stokes axis CRVAL > 0: no conversion, planes by position */
+    int uvw_scaled;          /* 1: u, v, w scaled by SNGL(FREQ); 0: already in wavelengths */
+    double freq;             /* CRVAL + (1 - CRPIX) * CDELT of the FREQ axis */
+    double ra, dec;          /* CRVAL of the RA and DEC axes (0 when absent) */
+} sde_uvfits_desc;
+int sde_uvfits_open(const char *path, sde_uvfits **out);
+int sde_uvfits_describe(const sde_uvfits *f, sde_uvfits_desc *d);
+int sde_uvfits_read(sde_ctx *ctx, const sde_uvfits *f, int stokes, float *u, float *v, float *w,
+                    float *vis, float *wt, int where, int64_t *nread);
+int sde_uvfits_close(sde_uvfits *f);
+
 #ifdef __cplusplus
 }
 #endif

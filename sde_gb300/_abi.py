@@ -65,6 +65,14 @@ I = C.c_int
 I64 = C.c_int64
 F = C.c_float
 
+
+class UvfitsDesc(C.Structure):
+    """sde_uvfits_desc of include/sde_gpu.h."""
+    _fields_ = [("ngroups", C.c_int64), ("ngroups_in_file", C.c_int64), ("npar", C.c_int),
+                ("bitpix", C.c_int), ("ncomplex", C.c_int), ("nstokes", C.c_int),
+                ("iquv", C.c_int), ("uvw_scaled", C.c_int), ("freq", C.c_double),
+                ("ra", C.c_double), ("dec", C.c_double)]
+
 # (name, restype, argtypes) of every exported function declared in include/sde_gpu.h
 SIGNATURES = [
     ("sde_last_error", C.c_char_p, []),
@@ -118,6 +126,10 @@ SIGNATURES = [
     ("sde_batch_graph_nodes", I, [P]),
     ("sde_batch_image", I, [P, I, I, C.POINTER(P)]),
     ("sde_batch_read", I, [P, I, I, P, I64]),
+    ("sde_uvfits_open", I, [C.c_char_p, C.POINTER(P)]),
+    ("sde_uvfits_describe", I, [P, C.POINTER(UvfitsDesc)]),
+    ("sde_uvfits_read", I, [P, P, I, P, P, P, P, P, I, C.POINTER(I64)]),
+    ("sde_uvfits_close", I, [P]),
     ("sde_shim_cache_stats", I, [C.POINTER(I64), C.POINTER(I64)]),
     ("sde_shim_cache_clear", I, []),
     # Fortran-77 drop-in layer (all arguments by reference)
