@@ -264,6 +264,42 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
                float tflux_in, float *cln, float *res, float *cflux, int *cx, int *cy,
                volatile int *cancel_flag, sde_clean_result *out);
 
+/* Clark CLEAN, the default algorithm of SDE's clean task: the CLARK branch of
+ * task/clean.f:146-205 and IMGCCLEA (img/imgcclea.f) on device arrays.
+ *   dirty, psf  N x N images from uvmap (N a power of two, 64..8192; CRPIX = (N+1)/2, so
+ *               IMGMAKEX's phase shift is zero).
+ *   window      CRDHALF with BLC/TRC unset: w = N/2 pixels from N/4+1 on both axes;
+ *               comp (initial components, updated), resid (final residual) and box (NULL
+ *               = 1.0 everywhere) are w x w.
+ *   transfer    XFR = FFTR2D(PSF) on the N x N grid; IMGRESID's residual
+ *               DIRTY - FFTR2D^-1(FFTR2D(comp) * XFR) runs on it after each minor cycle.
+ *   minor cycle PIX2DRCC on the list of the Numcl largest |residual| (PIXRABSH histogram,
+ *               PIXFLIM limit, at least EXTSIDE * max |residual|, PIX2DRLI order), with
+ *               the Bpatch x Bpatch beam patch (IMGSUBPS) and EXTSIDE the largest |PSF|
+ *               outside it (PIXREXTS).
+ *   cl/cx/cy    device arrays of niter entries for the component list (NULL: scratch).
+ * numcl <= 32768 (the task's default); niter > 0; biter = first iteration number (1, or
+ * NITER+1 of a restarted run).  An empty list ends the loop (the reference would read an
+ * unwritten list entry).  Messages: 'Zero range in values', 'Too many points', 'Limit in
+ * absolute value < 0.0'.  Synchronises once per major cycle. */
+typedef struct {
+    int niter;
+    float gain, flux;
+    int numcl, bpatch, biter;
+} sde_clark_params;
+#define SDE_CLARK_TRACE 64
+typedef struct {
+    int aniter, ncycles, window, blc, last_anl;
+    float maxres, tflux, extside, last_slim;
+    /* IMGCCLEA's message per major cycle (img/imgcclea.f:276-278), first 64 cycles:
+     * list length, components so far, PIX2DRCC's MAXRES, total flux */
+    int t_anl[SDE_CLARK_TRACE], t_aniter[SDE_CLARK_TRACE];
+    float t_maxres[SDE_CLARK_TRACE], t_tflux[SDE_CLARK_TRACE];
+} sde_clark_result;
+int sde_clark(sde_ctx *ctx, const float *dirty, const float *psf, int n, const float *box,
+              const sde_clark_params *p, float *comp, float *resid, float *cl, int *cx, int *cy,
+              sde_clark_result *out);
+
 /* Hogbom CLEAN that allocates nothing.  This entry point has no counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc -- hosts whose device memory
  * all comes from their own allocator or fixed arena, real-time or embedded loops that forbid

@@ -83,6 +83,9 @@ def lib():
                                    C.c_float, C.c_int, C.c_int, C.c_float, f32p, f32p,
                                    C.POINTER(C.c_int), C.POINTER(C.c_float),
                                    C.POINTER(C.c_float), f32p, i32p, i32p]
+        L.orc_clark.restype = C.c_int
+        L.orc_clark.argtypes = [f32p, f32p, C.c_int, C.c_void_p, C.POINTER(ClarkParams), f32p, f32p,
+                                f32p, i32p, i32p, C.POINTER(ClarkResult)]
         L.orc_make_geom.argtypes = [C.POINTER(UvmapParams), C.POINTER(Geom)]
         L.orc_uvmap.argtypes = [C.POINTER(UvmapParams), C.c_int, f32p, f32p, f32p, c64p, f32p,
                                 f32p, f32p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -238,6 +241,44 @@ def pix2drcl(drt, psf, box, gain, nsub, bsub=1, flux=0.0, tflux=0.0):
                        C.byref(ansub), C.byref(maxres), C.byref(tf), cflux, cx, cy)
     return dict(cln=cln, res=res, ansub=ansub.value, maxres=maxres.value, tflux=tf.value,
                 cflux=cflux, cx=cx, cy=cy)
+
+
+class ClarkParams(C.Structure):
+    _fields_ = [("niter", C.c_int), ("gain", C.c_float), ("flux", C.c_float), ("numcl", C.c_int),
+                ("bpatch", C.c_int)]
+
+
+class ClarkResult(C.Structure):
+    _fields_ = [("aniter", C.c_int), ("ncycles", C.c_int), ("window", C.c_int), ("blc", C.c_int),
+                ("last_anl", C.c_int), ("maxres", C.c_float), ("tflux", C.c_float),
+                ("extside", C.c_float), ("last_slim", C.c_float),
+                ("t_anl", C.c_int * 64), ("t_aniter", C.c_int * 64),
+                ("t_maxres", C.c_float * 64), ("t_tflux", C.c_float * 64)]
+
+
+def clark(dirty, psf, niter=100, gain=0.1, flux=0.0, numcl=32768, bpatch=128, box=None):
+    """Clark CLEAN of an N x N dirty image (task/clean.f CLARK branch + img/imgcclea.f).
+    Returns dict(comp, resid (window w x w), cl, cx, cy, rc, and the result fields)."""
+    dirty, psf = _f32(dirty), _f32(psf)
+    n = dirty.shape[0]
+    w = n // 2
+    comp = np.zeros((w, w), np.float32)
+    resid = np.zeros((w, w), np.float32)
+    cl = np.zeros(niter, np.float32)
+    cx = np.zeros(niter, np.int32)
+    cy = np.zeros(niter, np.int32)
+    p = ClarkParams(niter, gain, flux, numcl, bpatch)
+    r = ClarkResult()
+    boxp = None
+    if box is not None:
+        box = _f32(box)
+        boxp = box.ctypes.data_as(C.c_void_p)
+    rc = lib().orc_clark(dirty, psf, n, boxp, C.byref(p), comp, resid, cl, cx, cy, C.byref(r))
+    out = dict(comp=comp, resid=resid, cl=cl, cx=cx, cy=cy, rc=rc)
+    out.update({k: getattr(r, k) for k, _ in r._fields_ if not k.startswith("t_")})
+    nc = min(r.ncycles, 64)
+    out["trace"] = [(r.t_anl[i], r.t_aniter[i], r.t_maxres[i], r.t_tflux[i]) for i in range(nc)]
+    return out
 
 
 def uvmap(p, u, v, w, vis, wt):

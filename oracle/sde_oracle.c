@@ -1225,3 +1225,230 @@ void orc64_dft_image(const orc_geom *g, int nvis, const float *u, const float *v
         }
     }
 }
+
+/* ---------------------------------------------------------------------------------------
+ * Clark CLEAN: the CLARK branch of task/clean.f:146-205 (CRDHALF window, IMGMAKEX,
+ * IMGSUBPS) and IMGCCLEA's major/minor cycle loop (img/imgcclea.f:210-290).
+ */
+
+/* crd/crdhalf.f:21-41 with the task's BLC = TRC unset: the inner half of an axis */
+static void orc_crdhalf_axis(int n, int *blc, int *trc) {
+    int b = 1, t = 1;
+    if (n > 1) {
+        b = n / 4 + 1;
+        t = 3 * n / 4;
+        int idel = t - b + 1 < n / 2 ? t - b + 1 : n / 2;
+        t = b + idel - 1;
+    }
+    *blc = b;
+    *trc = t;
+}
+
+/* pix/pixrabsh.f:18-40.  INDEX = NINT((|A|-BASE)/INCR) is 0 for values near the minimum;
+ * the reference then writes HIST(0), outside HIST(1..NB): those values are in no bin. */
+static int orc_pixrabsh(const float *a, int64_t n, int nb, int *hist, float *base, float *incr) {
+    float amax = fabsf(a[0]), amin = amax;
+    for (int64_t i = 0; i < n; i++) {
+        float x = fabsf(a[i]);
+        amax = amax > x ? amax : x;
+        amin = amin < x ? amin : x;
+    }
+    if (amax == amin) return -1; /* 'Zero range in values' */
+    for (int i = 0; i < nb; i++) hist[i] = 0;
+    *base = amin;
+    *incr = (amax - amin) / (float)(nb - 1);
+    for (int64_t i = 0; i < n; i++) {
+        int index = orc_nint_f((fabsf(a[i]) - *base) / *incr);
+        if (index >= 1 && index <= nb) hist[index - 1]++;
+    }
+    return 0;
+}
+
+/* pix/pixflim.f:16-30; -2 = 'Too many points' */
+static int orc_pixflim(const int *hist, int nb, int nl, int *slim) {
+    int ntotal = 0;
+    *slim = 1;
+    for (int i = nb; i >= 1; i--) {
+        ntotal += hist[i - 1];
+        if (ntotal >= nl) {
+            *slim = i + 1;
+            break;
+        }
+    }
+    return *slim > nb ? -2 : 0;
+}
+
+/* pix/pix2drli.f:17-31: pixels with |A| > SLIM in storage order, at most NL */
+static int orc_pix2drli(const float *a, int nx, int ny, float slim, float *al, int *xl, int *yl, int nl) {
+    int anl = 0;
+    for (int iy = 1; iy <= ny; iy++)
+        for (int ix = 1; ix <= nx; ix++) {
+            float v = a[(size_t)(iy - 1) * nx + (ix - 1)];
+            if (fabsf(v) > slim) {
+                al[anl] = v;
+                xl[anl] = ix;
+                yl[anl] = iy;
+                anl++;
+                if (anl >= nl) return anl;
+            }
+        }
+    return anl;
+}
+
+/* pix/pix2drcc.f:66-140 with SPEED = 1 and GSUB = BSUB (IMGCCLEA's call); cl/cx/cy are
+ * 1-based component lists (index ISUB - 1).  Returns ANSUB. */
+static int orc_pix2drcc(float *drtl, const int *xl, const int *yl, int nl, const float *psf, int pnx,
+                        int pny, float gain, int nsub, int bsub, float flux, float slim, float *cl,
+                        int *cx, int *cy, float *maxres, float *tflux) {
+    int ipeak = orc_pixisama(pnx * pny, psf, 1) - 1;
+    int pmpx = 1 + ipeak % pnx;
+    int pmpy = 1 + (ipeak - pmpx + 1) / pnx;
+    float smn = 0.0f;
+    int isub;
+    for (isub = bsub; isub <= abs(nsub); isub++) {
+        smn = smn + 1.0f / (float)isub; /* FLOAT(ISUB)**SPEED with SPEED = 1.0 */
+        int ip = orc_pixisama(nl, drtl, 1);
+        int pmx = xl[ip - 1], pmy = yl[ip - 1];
+        *maxres = drtl[ip - 1];
+        if (flux < 0.0f && *maxres < 0.0f) return isub - 1;
+        if (nsub < 0 && *maxres < 0.0f) return isub - 1;
+        float lim = slim * smn;
+        if (fabsf(flux) > lim) lim = fabsf(flux);
+        if (fabsf(*maxres) <= lim) return isub - 1;
+        float pntsub = gain * *maxres;
+        *tflux = *tflux + pntsub;
+        cl[isub - 1] = pntsub;
+        cx[isub - 1] = pmx;
+        cy[isub - 1] = pmy;
+        int offx = pmpx + pmx, offy = pmpy + pmy;
+        for (int i = 0; i < nl; i++) {
+            int px = offx - xl[i], py = offy - yl[i];
+            if (px >= 1 && px <= pnx && py >= 1 && py <= pny)
+                drtl[i] = drtl[i] - pntsub * psf[(size_t)(py - 1) * pnx + (px - 1)];
+        }
+    }
+    int ip = orc_pixisama(nl, drtl, 1);
+    *maxres = drtl[ip - 1];
+    return nsub;
+}
+
+/* img/imgresid.f:13-16: RES = DRT - IMGFFT(IMGFFT(MODEL) * XFR) on the transfer
+ * function's grid (fnu x nv), PIXXMULT's complex product in REAL */
+static void orc_imgresid(const float *model, const float *drt, const float *xfr, float *res, int nx,
+                         int ny, int fnu, int nv, float *mvis) {
+    const size_t nxf = (size_t)(fnu / 2 + 1) * nv;
+    orc_fftr2d((float *)model, mvis, nx, ny, fnu, nv, +1);
+    for (size_t k = 0; k < nxf; k++) {
+        float a = mvis[2 * k], b = mvis[2 * k + 1], c = xfr[2 * k], d = xfr[2 * k + 1];
+        mvis[2 * k] = a * c - b * d;
+        mvis[2 * k + 1] = a * d + b * c;
+    }
+    orc_fftr2d(res, mvis, nx, ny, fnu, nv, -1);
+    for (size_t k = 0; k < (size_t)nx * ny; k++) res[k] = drt[k] - res[k];
+}
+
+int orc_clark(const float *dirty, const float *psf, int n, const float *box, const orc_clark_params *p,
+              float *comp, float *resid, float *cl, int *cx, int *cy, orc_clark_result *r) {
+    memset(r, 0, sizeof *r);
+    if (n < 4 || (n & (n - 1)) || p->niter <= 0 || p->numcl <= 0 || p->bpatch <= 0) return -10;
+    /* window (task/clean.f:146-157) */
+    int blc, trc;
+    orc_crdhalf_axis(n, &blc, &trc);
+    const int w = trc - blc + 1;
+    const size_t nw = (size_t)w * w;
+    float *drt = (float *)malloc(sizeof(float) * nw);
+    for (int y = 0; y < w; y++)
+        for (int x = 0; x < w; x++) drt[(size_t)y * w + x] = dirty[(size_t)(y + blc - 1) * n + (x + blc - 1)];
+    /* XFR (img/imgmakex.f: IMGFFT, then ARRPHASE by ((N+1)/2 - CRPIX)/N = 0 for CRPIX = (N+1)/2) */
+    const int fnu = n, nv = n, nu = n / 2 + 1;
+    float *xfr = (float *)malloc(sizeof(float) * 2 * (size_t)nu * nv);
+    float *mvis = (float *)malloc(sizeof(float) * 2 * (size_t)nu * nv);
+    orc_fftr2d((float *)psf, xfr, n, n, fnu, nv, +1);
+    /* beam patch and exterior sidelobe (img/imgsubps.f:28-33, pix/pixrexts.f) */
+    const int rp = (n + 1) / 2, bp = p->bpatch;
+    int pb0 = rp - bp / 2 + 1, pb1 = rp + bp / 2;
+    if (pb0 < 1) pb0 = 1;
+    if (pb1 > n) pb1 = n;
+    const int pw = pb1 - pb0 + 1;
+    float *spsf = (float *)malloc(sizeof(float) * (size_t)pw * pw);
+    float ext = 0.0f;
+    for (int y = 1; y <= n; y++)
+        for (int x = 1; x <= n; x++) {
+            float v = psf[(size_t)(y - 1) * n + (x - 1)];
+            if (x >= pb0 && x <= pb1 && y >= pb0 && y <= pb1)
+                spsf[(size_t)(y - pb0) * pw + (x - pb0)] = v;
+            else if (fabsf(v) > ext)
+                ext = fabsf(v);
+        }
+    r->extside = ext;
+    /* lists */
+    const int nl = p->numcl, nb = 1024;
+    float *al = (float *)malloc(sizeof(float) * nl);
+    int *xl = (int *)malloc(sizeof(int) * nl), *yl = (int *)malloc(sizeof(int) * nl);
+    int *hist = (int *)malloc(sizeof(int) * nb);
+    int rc = 0, riter = 1, aniter = 0;
+    float maxres = 0.0f, tflux = 0.0f;
+    orc_imgresid(comp, drt, xfr, resid, w, w, fnu, nv, mvis);
+    for (;;) {
+        if (box)
+            for (size_t k = 0; k < nw; k++) resid[k] = resid[k] * box[k];
+        float amax = resid[0], amin = resid[0];
+        for (size_t k = 0; k < nw; k++) {
+            if (resid[k] > amax) amax = resid[k];
+            if (resid[k] < amin) amin = resid[k];
+        }
+        maxres = fabsf(amax) > fabsf(amin) ? fabsf(amax) : fabsf(amin);
+        float base, incr;
+        int slimi;
+        if ((rc = orc_pixrabsh(resid, (int64_t)nw, nb, hist, &base, &incr)) != 0) break;
+        if ((rc = orc_pixflim(hist, nb, nl, &slimi)) != 0) break;
+        float slim = incr * (float)(slimi - 1) + base + 0.5f * incr;
+        if (slim < 0.0f) {
+            rc = -3; /* 'Limit in absolute value < 0.0' */
+            break;
+        }
+        float es = fabsf(ext * maxres);
+        slim = slim > es ? slim : es;
+        int anl = orc_pix2drli(resid, w, w, slim, al, xl, yl, nl);
+        r->last_anl = anl;
+        r->last_slim = slim;
+        if (anl == 0) {
+            /* PIX2DRCC would read DRTL(1), never written: stop with nothing subtracted */
+            aniter = riter - 1;
+            break;
+        }
+        aniter = orc_pix2drcc(al, xl, yl, anl, spsf, pw, pw, p->gain, p->niter, riter, p->flux, slim, cl, cx, cy,
+                              &maxres, &tflux);
+        /* pix/pix2drma.f:17-21 */
+        for (int i = riter; i <= aniter; i++) {
+            int ix = cx[i - 1], iy = cy[i - 1];
+            if (ix >= 1 && ix <= w && iy >= 1 && iy <= w)
+                comp[(size_t)(iy - 1) * w + (ix - 1)] = comp[(size_t)(iy - 1) * w + (ix - 1)] + cl[i - 1];
+        }
+        riter = aniter + 1;
+        orc_imgresid(comp, drt, xfr, resid, w, w, fnu, nv, mvis);
+        if (r->ncycles < ORC_CLARK_TRACE) {
+            r->t_anl[r->ncycles] = anl;
+            r->t_aniter[r->ncycles] = aniter;
+            r->t_maxres[r->ncycles] = maxres;
+            r->t_tflux[r->ncycles] = tflux;
+        }
+        r->ncycles++;
+        if (maxres <= 0.0f && p->flux <= 0.0f) break;
+        if (!(fabsf(maxres) > p->flux && aniter < abs(p->niter))) break;
+    }
+    r->aniter = aniter;
+    r->maxres = maxres;
+    r->tflux = tflux;
+    r->window = w;
+    r->blc = blc;
+    free(drt);
+    free(xfr);
+    free(mvis);
+    free(spsf);
+    free(al);
+    free(xl);
+    free(yl);
+    free(hist);
+    return rc;
+}

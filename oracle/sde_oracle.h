@@ -106,6 +106,28 @@ int orc_uvmap(const orc_uvmap_params *p, int nvis, const float *u, const float *
 int orc_vismodel(const orc_uvmap_params *p, int nvis, const float *u, const float *v,
                  const float *w, float *vis, float *wt, const float *image);
 
+/* Clark CLEAN of an N x N dirty image with its N x N PSF (the CLARK branch of task/clean.f
+ * and img/imgcclea.f): window = CRDHALF's inner half (w = N/2 pixels from N/4+1), beam patch
+ * bpatch, list size numcl.  comp (w x w) is the initial component image and is updated;
+ * resid (w x w) receives the final residual; cl/cx/cy (niter entries) the component list.
+ * Returns 0, -1 'Zero range in values', -2 'Too many points', -3 negative limit, -10 bad
+ * arguments. */
+typedef struct {
+    int niter;
+    float gain, flux;
+    int numcl, bpatch;
+} orc_clark_params;
+#define ORC_CLARK_TRACE 64
+typedef struct {
+    int aniter, ncycles, window, blc, last_anl;
+    float maxres, tflux, extside, last_slim;
+    /* IMGCCLEA's per-cycle message (img/imgcclea.f:276-278): ANL, ANITER, MAXRES, TFLUX */
+    int t_anl[ORC_CLARK_TRACE], t_aniter[ORC_CLARK_TRACE];
+    float t_maxres[ORC_CLARK_TRACE], t_tflux[ORC_CLARK_TRACE];
+} orc_clark_result;
+int orc_clark(const float *dirty, const float *psf, int n, const float *box, const orc_clark_params *p,
+              float *comp, float *resid, float *cl, int *cx, int *cy, orc_clark_result *r);
+
 /* ---- FP64 oracle: same algorithms in double, plus a direct DFT --------------------- */
 int  orc64_grdh2d(const float *vis, const float *wt, const float *u, const float *v,
                   const float *w, int nvis, const orc_geom *g, int psf, double *gvis);

@@ -66,6 +66,21 @@ I64 = C.c_int64
 F = C.c_float
 
 
+class ClarkParams(C.Structure):
+    """sde_clark_params of include/sde_gpu.h."""
+    _fields_ = [("niter", C.c_int), ("gain", C.c_float), ("flux", C.c_float), ("numcl", C.c_int),
+                ("bpatch", C.c_int), ("biter", C.c_int)]
+
+
+class ClarkResult(C.Structure):
+    """sde_clark_result of include/sde_gpu.h."""
+    _fields_ = [("aniter", C.c_int), ("ncycles", C.c_int), ("window", C.c_int), ("blc", C.c_int),
+                ("last_anl", C.c_int), ("maxres", C.c_float), ("tflux", C.c_float),
+                ("extside", C.c_float), ("last_slim", C.c_float),
+                ("t_anl", C.c_int * 64), ("t_aniter", C.c_int * 64),
+                ("t_maxres", C.c_float * 64), ("t_tflux", C.c_float * 64)]
+
+
 class UvfitsDesc(C.Structure):
     """sde_uvfits_desc of include/sde_gpu.h."""
     _fields_ = [("ngroups", C.c_int64), ("ngroups_in_file", C.c_int64), ("npar", C.c_int),
@@ -126,6 +141,8 @@ SIGNATURES = [
     ("sde_batch_graph_nodes", I, [P]),
     ("sde_batch_image", I, [P, I, I, C.POINTER(P)]),
     ("sde_batch_read", I, [P, I, I, P, I64]),
+    ("sde_clark", I, [P, P, P, I, P, C.POINTER(ClarkParams), P, P, P, P, P,
+                      C.POINTER(ClarkResult)]),
     ("sde_uvfits_open", I, [C.c_char_p, C.POINTER(P)]),
     ("sde_uvfits_describe", I, [P, C.POINTER(UvfitsDesc)]),
     ("sde_uvfits_read", I, [P, P, I, P, P, P, P, P, I, C.POINTER(I64)]),

@@ -360,6 +360,31 @@ def hogbom(ctx, geom, dirty, psf, niter, gain=0.1, flux=0.0):
     return ctx.hogbom(drt, psf, niter, gain, flux)
 
 
+def clark(ctx, dirty, psf, niter=100, gain=0.1, flux=0.0, numcl=32768, bpatch=128, box=None,
+          comp=None, biter=1):
+    """task/clean.f CLARK path with IMGCCLEA (sde_clark): N x N dirty image and PSF (device
+    tensors) -> components and residual over CRDHALF's N/2 window, the component list, and
+    the per-major-cycle trace (ANL, ANITER, MAXRES, TFLUX).  The defaults are clean.inf's."""
+    torch = ctx.torch
+    n = int(dirty.shape[0])
+    w = n // 2
+    if comp is None:
+        comp = ctx.zeros((w, w), torch.float32)
+    resid = ctx.empty((w, w), torch.float32)
+    cl = ctx.zeros(niter, torch.float32)
+    cx = ctx.zeros(niter, torch.int32)
+    cy = ctx.zeros(niter, torch.int32)
+    p = _abi.ClarkParams(int(niter), float(gain), float(flux), int(numcl), int(bpatch), int(biter))
+    r = _abi.ClarkResult()
+    check(lib().sde_clark(ctx.h, _ptr(dirty), _ptr(psf), n, _ptr(box), C.byref(p), _ptr(comp),
+                          _ptr(resid), _ptr(cl), _ptr(cx), _ptr(cy), C.byref(r)), "sde_clark")
+    out = dict(comp=comp, resid=resid, cl=cl, cx=cx, cy=cy)
+    out.update({k: getattr(r, k) for k, _ in r._fields_ if not k.startswith("t_")})
+    nc = min(r.ncycles, 64)
+    out["trace"] = [(r.t_anl[i], r.t_aniter[i], r.t_maxres[i], r.t_tflux[i]) for i in range(nc)]
+    return out
+
+
 class MajorCycle:
     """One CLEAN major cycle as the reference composes it (task/mosclean.f:227-364):
     grid the residual -> dirty image -> Hogbom minor cycle -> model image -> degrid ->
