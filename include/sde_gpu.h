@@ -264,6 +264,25 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
                float tflux_in, float *cln, float *res, float *cflux, int *cx, int *cy,
                volatile int *cancel_flag, sde_clean_result *out);
 
+/* Direct Fourier transforms (the DFT options of uvmap and vismodel) on device arrays:
+ *   sde_dft_image  VISDFT3D for a 2-D image (vis/visdft3d.f; task/uvmap.f:416-418):
+ *                  dirty(ix,iy) = RNORM sum_k WT_k Re(V_k E), psf = RNORM sum_k WT_k Re(E),
+ *                  E = exp(-i CF (u DX (ix-RX) + v DY (iy-RY))), CF = 2 pi^2/180, RNORM =
+ *                  1/sum WT over WT > 0 ('No valid data' when that sum is 0); dirty or psf
+ *                  may be NULL.
+ *   sde_dft_vis    IMGDFT2D (img/imgdft2d.f; task/vismodel.f:75): V_k = sum I(ix,iy) conj(E)
+ *                  for WT_k > 0; other points keep their VIS.
+ * images [ny][nx] float32, vis complex64 pairs, refx/refy the 1-based reference pixel (a
+ * multiple of 1/2), deltx/delty degrees per pixel; nx, ny, |refx|, |refy| <= 8192.  Phases
+ * are exact to FP32 rounding (no rotation recurrence) and sums over visibilities are
+ * compensated, so both are accurate to ~1e-7 of the peak. */
+int sde_dft_image(sde_ctx *ctx, int64_t nvis, const float *u, const float *v, const float *vis,
+                  const float *wt, int nx, int ny, double refx, double deltx, double refy,
+                  double delty, float *dirty, float *psf);
+int sde_dft_vis(sde_ctx *ctx, const float *image, int nx, int ny, double refx, double deltx,
+                double refy, double delty, int64_t nvis, const float *u, const float *v,
+                const float *wt, float *vis);
+
 /* Clark CLEAN, the default algorithm of SDE's clean task: the CLARK branch of
  * task/clean.f:146-205 and IMGCCLEA (img/imgcclea.f) on device arrays.
  *   dirty, psf  N x N images from uvmap (N a power of two, 64..8192; CRPIX = (N+1)/2, so

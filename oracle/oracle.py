@@ -83,6 +83,16 @@ def lib():
                                    C.c_float, C.c_int, C.c_int, C.c_float, f32p, f32p,
                                    C.POINTER(C.c_int), C.POINTER(C.c_float),
                                    C.POINTER(C.c_float), f32p, i32p, i32p]
+        L.orc_visdft2d.restype = C.c_int
+        L.orc_visdft2d.argtypes = [c64p, C.c_int, f32p, f32p, f32p, f32p, f32p, C.c_int, C.c_int,
+                                   C.c_float, C.c_float, C.c_float, C.c_float]
+        L.orc_imgdft2d.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                   c64p, C.c_int, f32p, f32p, f32p]
+        L.orc64_visdft2d.restype = C.c_int
+        L.orc64_visdft2d.argtypes = [c64p, C.c_int, f32p, f32p, f32p, f64p, f64p, C.c_int, C.c_int,
+                                     C.c_double, C.c_double, C.c_double, C.c_double]
+        L.orc64_imgdft2d.argtypes = [f32p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                     C.c_double, c128p, C.c_int, f32p, f32p, f32p]
         L.orc_clark.restype = C.c_int
         L.orc_clark.argtypes = [f32p, f32p, C.c_int, C.c_void_p, C.POINTER(ClarkParams), f32p, f32p,
                                 f32p, i32p, i32p, C.POINTER(ClarkResult)]
@@ -279,6 +289,30 @@ def clark(dirty, psf, niter=100, gain=0.1, flux=0.0, numcl=32768, bpatch=128, bo
     nc = min(r.ncycles, 64)
     out["trace"] = [(r.t_anl[i], r.t_aniter[i], r.t_maxres[i], r.t_tflux[i]) for i in range(nc)]
     return out
+
+
+def visdft2d(vis, wt, u, v, nx, ny, refx, deltx, refy, delty, fp64=False):
+    """VISDFT3D (2-D): (image, psf, rc); fp64 = exact phases in double."""
+    vis, wt, u, v = _c64(vis), _f32(wt), _f32(u), _f32(v)
+    dt = np.float64 if fp64 else np.float32
+    img = np.zeros((ny, nx), dt)
+    psf = np.zeros((ny, nx), dt)
+    f = lib().orc64_visdft2d if fp64 else lib().orc_visdft2d
+    rc = f(vis, len(wt), wt, u, v, img, psf, nx, ny, refx, deltx, refy, delty)
+    return img, psf, rc
+
+
+def imgdft2d(image, refx, deltx, refy, delty, wt, u, v, vis_in=None, fp64=False):
+    """IMGDFT2D: visibilities of a model image; points with WT <= 0 keep vis_in."""
+    image, wt, u, v = _f32(image), _f32(wt), _f32(u), _f32(v)
+    ny, nx = image.shape
+    if fp64:
+        vis = np.zeros(len(wt), np.complex128) if vis_in is None else np.asarray(vis_in, np.complex128).copy()
+        lib().orc64_imgdft2d(image, nx, ny, refx, deltx, refy, delty, vis, len(wt), wt, u, v)
+    else:
+        vis = np.zeros(len(wt), np.complex64) if vis_in is None else _c64(vis_in).copy()
+        lib().orc_imgdft2d(image, nx, ny, refx, deltx, refy, delty, vis, len(wt), wt, u, v)
+    return vis
 
 
 def uvmap(p, u, v, w, vis, wt):

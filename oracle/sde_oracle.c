@@ -1452,3 +1452,124 @@ int orc_clark(const float *dirty, const float *psf, int n, const float *box, con
     free(hist);
     return rc;
 }
+
+/* ---------------------------------------------------------------------------------------
+ * Direct Fourier transforms of uvmap's and vismodel's DFT options.
+ */
+
+/* vis/visdft3d.f:24-77 for a 2-D image (NZ = 1, REFZ = 1): dirty and PSF by the reference's
+ * FP32 rotation recurrence (CFACTXYZ *= CROTX along x, CFACTYZ *= CROTY along y).
+ * refx/refy 1-based reference pixel, deltx/delty in degrees.  Returns -1 ('No valid data'). */
+int orc_visdft2d(const float *vis, int nvis, const float *wt, const float *u, const float *v, float *image,
+                 float *psf, int nx, int ny, float refx, float deltx, float refy, float delty) {
+    const float cf = 2.0f * (4.0f * atanf(1.0f)) * (4.0f * atanf(1.0f)) / 180.0f;
+    for (size_t k = 0; k < (size_t)nx * ny; k++) image[k] = psf[k] = 0.0f;
+    float rnorm = 0.0f;
+    for (int i = 0; i < nvis; i++)
+        if (wt[i] > 0.0f) rnorm = rnorm + wt[i];
+    if (!(rnorm > 0.0f)) return -1;
+    rnorm = 1.0f / rnorm;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        /* the z term vanishes: W * DELTZ * (1 - REFZ) with REFZ = 1 */
+        float phase = cf * (u[i] * deltx * (1.0f - refx) + v[i] * delty * (1.0f - refy));
+        float fr = rnorm * wt[i] * cosf(phase), fi = rnorm * wt[i] * -sinf(phase);
+        phase = cf * u[i] * deltx;
+        const float rxr = cosf(phase), rxi = -sinf(phase);
+        phase = cf * v[i] * delty;
+        const float ryr = cosf(phase), ryi = -sinf(phase);
+        const float vr = vis[2 * i], vi = vis[2 * i + 1];
+        for (int iy = 0; iy < ny; iy++) {
+            float xr = fr, xi = fi;
+            for (int ix = 0; ix < nx; ix++) {
+                const size_t o = (size_t)iy * nx + ix;
+                image[o] = image[o] + (vr * xr - vi * xi);
+                psf[o] = psf[o] + xr;
+                const float tr = xr * rxr - xi * rxi, ti = xr * rxi + xi * rxr;
+                xr = tr;
+                xi = ti;
+            }
+            const float tr = fr * ryr - fi * ryi, ti = fr * ryi + fi * ryr;
+            fr = tr;
+            fi = ti;
+        }
+    }
+    return 0;
+}
+
+/* img/imgdft2d.f:21-42: model image -> visibilities by the same recurrence (sign +);
+ * points with WT <= 0 keep their VIS */
+void orc_imgdft2d(const float *image, int nx, int ny, float refx, float deltx, float refy, float delty,
+                  float *vis, int nvis, const float *wt, const float *u, const float *v) {
+    const float cf = (8.0f * atanf(1.0f)) * (8.0f * atanf(1.0f)) / 360.0f;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        float sr = 0.0f, si = 0.0f;
+        float phase = cf * (u[i] * deltx * (1.0f - refx) + v[i] * delty * (1.0f - refy));
+        float fr = cosf(phase), fi = sinf(phase);
+        phase = cf * u[i] * deltx;
+        const float rxr = cosf(phase), rxi = sinf(phase);
+        phase = cf * v[i] * delty;
+        const float ryr = cosf(phase), ryi = sinf(phase);
+        for (int iy = 0; iy < ny; iy++) {
+            float xr = fr, xi = fi;
+            for (int ix = 0; ix < nx; ix++) {
+                const float a = image[(size_t)iy * nx + ix];
+                sr = sr + a * xr;
+                si = si + a * xi;
+                const float tr = xr * rxr - xi * rxi, ti = xr * rxi + xi * rxr;
+                xr = tr;
+                xi = ti;
+            }
+            const float tr = fr * ryr - fi * ryi, ti = fr * ryi + fi * ryr;
+            fr = tr;
+            fi = ti;
+        }
+        vis[2 * i] = sr;
+        vis[2 * i + 1] = si;
+    }
+}
+
+/* the same two transforms in FP64 with exact phases (the accuracy reference) */
+int orc64_visdft2d(const float *vis, int nvis, const float *wt, const float *u, const float *v, double *image,
+                   double *psf, int nx, int ny, double refx, double deltx, double refy, double delty) {
+    const double d2r = M_PI / 180.0;
+    double rn = 0.0;
+    for (int i = 0; i < nvis; i++)
+        if (wt[i] > 0.0f) rn += wt[i];
+    if (!(rn > 0.0)) return -1;
+    for (size_t k = 0; k < (size_t)nx * ny; k++) image[k] = psf[k] = 0.0;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        const double c = wt[i] / rn;
+        for (int iy = 0; iy < ny; iy++)
+            for (int ix = 0; ix < nx; ix++) {
+                const double ph = -2.0 * M_PI * d2r * ((double)u[i] * deltx * (ix + 1 - refx) +
+                                                       (double)v[i] * delty * (iy + 1 - refy));
+                const size_t o = (size_t)iy * nx + ix;
+                image[o] += c * ((double)vis[2 * i] * cos(ph) - (double)vis[2 * i + 1] * sin(ph));
+                psf[o] += c * cos(ph);
+            }
+    }
+    return 0;
+}
+
+void orc64_imgdft2d(const float *image, int nx, int ny, double refx, double deltx, double refy, double delty,
+                    double *vis, int nvis, const float *wt, const float *u, const float *v) {
+    const double d2r = M_PI / 180.0;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        double sr = 0.0, si = 0.0;
+        for (int iy = 0; iy < ny; iy++)
+            for (int ix = 0; ix < nx; ix++) {
+                const double a = image[(size_t)iy * nx + ix];
+                if (a == 0.0) continue;
+                const double ph = 2.0 * M_PI * d2r * ((double)u[i] * deltx * (ix + 1 - refx) +
+                                                      (double)v[i] * delty * (iy + 1 - refy));
+                sr += a * cos(ph);
+                si += a * sin(ph);
+            }
+        vis[2 * i] = sr;
+        vis[2 * i + 1] = si;
+    }
+}

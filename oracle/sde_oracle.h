@@ -128,6 +128,19 @@ typedef struct {
 int orc_clark(const float *dirty, const float *psf, int n, const float *box, const orc_clark_params *p,
               float *comp, float *resid, float *cl, int *cx, int *cy, orc_clark_result *r);
 
+/* Direct Fourier transforms (uvmap's and vismodel's DFT options), FP32 as the reference
+ * computes them (rotation recurrences) and FP64 with exact phases.  Images [ny][nx], vis
+ * complex pairs, refx/refy 1-based reference pixel, deltx/delty degrees. */
+int  orc_visdft2d(const float *vis, int nvis, const float *wt, const float *u, const float *v, float *image,
+                  float *psf, int nx, int ny, float refx, float deltx, float refy, float delty);
+void orc_imgdft2d(const float *image, int nx, int ny, float refx, float deltx, float refy, float delty,
+                  float *vis, int nvis, const float *wt, const float *u, const float *v);
+int  orc64_visdft2d(const float *vis, int nvis, const float *wt, const float *u, const float *v,
+                    double *image, double *psf, int nx, int ny, double refx, double deltx, double refy,
+                    double delty);
+void orc64_imgdft2d(const float *image, int nx, int ny, double refx, double deltx, double refy,
+                    double delty, double *vis, int nvis, const float *wt, const float *u, const float *v);
+
 /* ---- FP64 oracle: same algorithms in double, plus a direct DFT --------------------- */
 int  orc64_grdh2d(const float *vis, const float *wt, const float *u, const float *v,
                   const float *w, int nvis, const orc_geom *g, int psf, double *gvis);

@@ -91,6 +91,7 @@ class Geom:
         cdelt_u = f32(1.0) / (D2R * (f32(fftpwr2(n)) * delt_ra))
         cdelt_v = f32(1.0) / (D2R * (f32(fftpwr2(n)) * delt_dec))
         self.cdelt_u, self.cdelt_v = cdelt_u, cdelt_v
+        self.deltx, self.delty = float(delt_ra), float(delt_dec)  # image CDELT, degrees
         self.uscale = f32(1.0) / cdelt_u
         self.vscale = f32(1.0) / cdelt_v
         self.wuscale = f32(fov) / cdelt_u  # GRDUWT: WTFOV / CDELT (grd/grduwt.f:115)
@@ -358,6 +359,33 @@ def hogbom(ctx, geom, dirty, psf, niter, gain=0.1, flux=0.0):
     lo, hi = geom.window()
     drt = dirty[lo:hi, lo:hi].contiguous()
     return ctx.hogbom(drt, psf, niter, gain, flux)
+
+
+def dft_image(ctx, u, v, vis, wt, nx, ny, refx, deltx, refy, delty, dirty=True, psf=True):
+    """VISDFT3D (2-D) on device tensors (sde_dft_image): dict(dirty, psf) [ny][nx]."""
+    torch = ctx.torch
+    out = {"dirty": ctx.empty((ny, nx), torch.float32) if dirty else None,
+           "psf": ctx.empty((ny, nx), torch.float32) if psf else None}
+    check(lib().sde_dft_image(ctx.h, int(wt.numel()), _ptr(u), _ptr(v), _ptr(vis), _ptr(wt), nx, ny,
+                              float(refx), float(deltx), float(refy), float(delty),
+                              _ptr(out["dirty"]), _ptr(out["psf"])), "sde_dft_image")
+    return out
+
+
+def dft_vis(ctx, image, refx, deltx, refy, delty, u, v, wt, vis):
+    """IMGDFT2D on device tensors (sde_dft_vis): vis (complex64) updated where wt > 0."""
+    ny, nx = int(image.shape[0]), int(image.shape[1])
+    check(lib().sde_dft_vis(ctx.h, _ptr(image), nx, ny, float(refx), float(deltx), float(refy),
+                            float(delty), int(wt.numel()), _ptr(u), _ptr(v), _ptr(wt), _ptr(vis)),
+          "sde_dft_vis")
+    return vis
+
+
+def uvmap_dft(ctx, geom, u, v, vis, wt):
+    """uvmap with DFT = T (task/uvmap.f:416-418): VISDFT into the image geometry (CDELT =
+    -/+ CELLSIZE/3600, CRPIX = (N+1)/2), normalised by the sum of weights."""
+    return dft_image(ctx, u, v, vis, wt, geom.nx, geom.ny, geom.cenx, geom.deltx, geom.ceny,
+                     geom.delty)
 
 
 def clark(ctx, dirty, psf, niter=100, gain=0.1, flux=0.0, numcl=32768, bpatch=128, box=None,
