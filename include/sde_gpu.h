@@ -283,6 +283,17 @@ int sde_dft_vis(sde_ctx *ctx, const float *image, int nx, int ny, double refx, d
                 double refy, double delty, int64_t nvis, const float *u, const float *v,
                 const float *wt, float *vis);
 
+/* MODIMG2D (mod/modimg2d.f, via MODIMG, mod/modimg.f): ncomp model components added into the
+ * device image [ny][nx].  types: 4 characters per component (POIN, GAUS, DISK, RECT, SPHE,
+ * SHEL, PLOR); flux, ra, dec (offsets from the reference pixel), bmaj, bmin (arcsec), bpa
+ * (degrees): host arrays; refx/refy 1-based, deltx/delty arcsec per pixel (3600 * CDELT).
+ * Messages: 'Zero increment in X/Y', 'Major axis zero', 'Minor axis zero', 'Unknown model
+ * type XXXX for component N' (all components are checked before any is added).
+ * Synchronises. */
+int sde_model_image(sde_ctx *ctx, int ncomp, const char *types, const float *flux, const float *ra,
+                    const float *dec, const float *bmaj, const float *bmin, const float *bpa, int nx,
+                    int ny, float refx, float deltx, float refy, float delty, float *image);
+
 /* Clark CLEAN, the default algorithm of SDE's clean task: the CLARK branch of
  * task/clean.f:146-205 and IMGCCLEA (img/imgcclea.f) on device arrays.
  *   dirty, psf  N x N images from uvmap (N a power of two, 64..8192; CRPIX = (N+1)/2, so

@@ -93,6 +93,9 @@ def lib():
                                      C.c_double, C.c_double, C.c_double, C.c_double]
         L.orc64_imgdft2d.argtypes = [f32p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                      C.c_double, c128p, C.c_int, f32p, f32p, f32p]
+        L.orc_modimg2d.restype = C.c_int
+        L.orc_modimg2d.argtypes = [C.c_int, i32p, f32p, f32p, f32p, f32p, f32p, f32p, f32p, C.c_int,
+                                   C.c_int, C.c_float, C.c_float, C.c_float, C.c_float]
         L.orc_clark.restype = C.c_int
         L.orc_clark.argtypes = [f32p, f32p, C.c_int, C.c_void_p, C.POINTER(ClarkParams), f32p, f32p,
                                 f32p, i32p, i32p, C.POINTER(ClarkResult)]
@@ -313,6 +316,20 @@ def imgdft2d(image, refx, deltx, refy, delty, wt, u, v, vis_in=None, fp64=False)
         vis = np.zeros(len(wt), np.complex64) if vis_in is None else _c64(vis_in).copy()
         lib().orc_imgdft2d(image, nx, ny, refx, deltx, refy, delty, vis, len(wt), wt, u, v)
     return vis
+
+
+MODEL_TYPES = ["POIN", "GAUS", "DISK", "RECT", "SPHE", "SHEL", "PLOR"]
+
+
+def modimg2d(comps, nx, ny, refx, deltx, refy, delty, image=None):
+    """comps: list of (type, flux, ra, dec, bmaj, bmin, bpa), offsets/sizes in arcsec.
+    Returns (image, rc)."""
+    img = np.zeros((ny, nx), np.float32) if image is None else _f32(image).copy()
+    col = lambda j: np.array([c[j] for c in comps], np.float32)  # noqa: E731
+    types = np.array([MODEL_TYPES.index(c[0][:4]) for c in comps], np.int32)
+    rc = lib().orc_modimg2d(len(comps), types, col(1), col(2), col(3), col(4), col(5), col(6), img, nx, ny,
+                            refx, deltx, refy, delty)
+    return img, rc
 
 
 def uvmap(p, u, v, w, vis, wt):

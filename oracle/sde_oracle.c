@@ -1573,3 +1573,85 @@ void orc64_imgdft2d(const float *image, int nx, int ny, double refx, double delt
         vis[2 * i + 1] = si;
     }
 }
+
+/* mod/modimg2d.f:29-232: components added into an image.  type: 0 POIN, 1 GAUS, 2 DISK,
+ * 3 RECT, 4 SPHE, 5 SHEL, 6 PLOR; ra/dec offsets and deltx/delty in arcsec (MODIMG passes
+ * 3600 * CDELT).  Returns 0, or -1 zero increment, -2 zero axis, -3 unknown type. */
+int orc_modimg2d(int ncomp, const int *type, const float *flux, const float *ra, const float *dec,
+                 const float *bmaj, const float *bmin, const float *bpa, float *image, int nx, int ny,
+                 float refx, float deltx, float refy, float delty) {
+    const float pi = 3.14159265358979323846f;
+    if (deltx == 0.0f || delty == 0.0f) return -1;
+    for (int c = 0; c < ncomp; c++) {
+        const int t = type[c];
+        if (t < 0 || t > 6) return -3;
+        if (t == 0) {
+            int ix = orc_nint_f(refx + ra[c] / deltx), iy = orc_nint_f(refy + dec[c] / delty);
+            if (ix >= 1 && ix <= nx && iy >= 1 && iy <= ny) image[(size_t)(iy - 1) * nx + ix - 1] += flux[c];
+            continue;
+        }
+        if (bmaj[c] == 0.0f || bmin[c] == 0.0f) return -2;
+        const float cospa = cosf(pi * bpa[c] / 180.0f), sinpa = sinf(pi * bpa[c] / 180.0f);
+        float rnorm = 0.0f, fact = 0.0f, dr = 0.0f;
+        if (t == 1) {
+            rnorm = (atanf(1.0f) / logf(2.0f)) * bmaj[c] * bmin[c] / (deltx * delty);
+            rnorm = 1.0f / fabsf(rnorm);
+            fact = 4.0f * logf(2.0f);
+        } else if (t == 2) {
+            rnorm = atanf(1.0f) * bmaj[c] * bmin[c] / (deltx * delty);
+            rnorm = flux[c] / fabsf(rnorm);
+        } else if (t == 3) {
+            rnorm = bmaj[c] * bmin[c] / (deltx * delty);
+            rnorm = 1.0f / fabsf(rnorm);
+        } else if (t == 4) {
+            rnorm = 4.0f * 1.5f * deltx * delty / (pi * bmaj[c] * bmin[c]);
+            rnorm = flux[c] * fabsf(rnorm);
+        } else if (t == 5) {
+            dr = 2.0f * sqrtf(fabsf(deltx * delty) / (bmaj[c] * bmin[c]));
+        } else {
+            fact = powf(4.0f, 1.0f / 3.0f) - 1.0f;
+            rnorm = fabsf(deltx * delty) * fact / (atanf(1.0f) * 2.0f * bmaj[c] * bmin[c]);
+        }
+        for (int pass = (t == 5 ? 0 : 1); pass < 2; pass++) {
+            for (int iy = 1; iy <= ny; iy++) {
+                const float dy = ((float)iy - refy) * delty - dec[c];
+                for (int ix = 1; ix <= nx; ix++) {
+                    const float dx = ((float)ix - refx) * deltx - ra[c];
+                    const float dmaj = dx * sinpa + dy * cospa;
+                    const float dmin = -dx * cospa + dy * sinpa;
+                    float *a = image + (size_t)(iy - 1) * nx + ix - 1;
+                    const float qa = dmaj / bmaj[c], qb = dmin / bmin[c];
+                    if (t == 1) {
+                        const float r = qa * qa + qb * qb;
+                        *a = *a + flux[c] * rnorm * expf(-fact * r);
+                    } else if (t == 2) {
+                        if (qa * qa + qb * qb < 0.25f) *a = *a + rnorm;
+                    } else if (t == 3) {
+                        if (fabsf(dmaj) < 0.5f * bmaj[c] && fabsf(dmin) < 0.5f * bmin[c]) *a = *a + flux[c] * rnorm;
+                    } else if (t == 4) {
+                        const float r = qa * qa + qb * qb;
+                        if (r < 0.25f) *a = *a + rnorm * sqrtf(1.0f - 4.0f * r);
+                    } else if (t == 5) {
+                        const float r = sqrtf(4.0f * (qa * qa + qb * qb));
+                        float rmin = r - dr / 2.0f;
+                        if (r - dr / 2.0f < 1.0f) {
+                            rmin = rmin > 0.0f ? rmin : 0.0f;
+                            const float rmax = r + dr / 2.0f, rmax1 = rmax < 1.0f ? rmax : 1.0f;
+                            if (rmax > rmin) {
+                                const float num = sqrtf(1.0f - rmin * rmin) - sqrtf(1.0f - rmax1 * rmax1);
+                                const float den = 2 * pi * pi * (rmax * rmax - rmin * rmin);
+                                if (pass == 0) rnorm = rnorm + num / den;
+                                else *a = *a + rnorm * num / den;
+                            }
+                        }
+                    } else {
+                        const float r = (qa * qa + qb * qb) * 4.0f;
+                        *a = *a + flux[c] * rnorm * powf(fact * r + 1.0f, -1.5f);
+                    }
+                }
+            }
+            if (t == 5 && pass == 0) rnorm = flux[c] / rnorm;
+        }
+    }
+    return 0;
+}

@@ -141,6 +141,12 @@ int  orc64_visdft2d(const float *vis, int nvis, const float *wt, const float *u,
 void orc64_imgdft2d(const float *image, int nx, int ny, double refx, double deltx, double refy,
                     double delty, double *vis, int nvis, const float *wt, const float *u, const float *v);
 
+/* MODIMG2D (mod/modimg2d.f): components added into image [ny][nx]; type 0 POIN, 1 GAUS,
+ * 2 DISK, 3 RECT, 4 SPHE, 5 SHEL, 6 PLOR; offsets and increments in arcsec. */
+int orc_modimg2d(int ncomp, const int *type, const float *flux, const float *ra, const float *dec,
+                 const float *bmaj, const float *bmin, const float *bpa, float *image, int nx, int ny,
+                 float refx, float deltx, float refy, float delty);
+
 /* ---- FP64 oracle: same algorithms in double, plus a direct DFT --------------------- */
 int  orc64_grdh2d(const float *vis, const float *wt, const float *u, const float *v,
                   const float *w, int nvis, const orc_geom *g, int psf, double *gvis);

@@ -141,6 +141,7 @@ SIGNATURES = [
     ("sde_batch_graph_nodes", I, [P]),
     ("sde_batch_image", I, [P, I, I, C.POINTER(P)]),
     ("sde_batch_read", I, [P, I, I, P, I64]),
+    ("sde_model_image", I, [P, I, C.c_char_p, P, P, P, P, P, P, I, I, F, F, F, F, P]),
     ("sde_dft_image", I, [P, I64, P, P, P, P, I, I, C.c_double, C.c_double, C.c_double,
                           C.c_double, P, P]),
     ("sde_dft_vis", I, [P, P, I, I, C.c_double, C.c_double, C.c_double, C.c_double, I64, P, P,

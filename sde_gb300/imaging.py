@@ -361,6 +361,21 @@ def hogbom(ctx, geom, dirty, psf, niter, gain=0.1, flux=0.0):
     return ctx.hogbom(drt, psf, niter, gain, flux)
 
 
+def model_image(ctx, comps, nx, ny, refx, deltx, refy, delty, image=None):
+    """MODIMG2D (sde_model_image): comps = [(type, flux, ra, dec, bmaj, bmin, bpa), ...] with
+    offsets/axes in arcsec and the position angle in degrees, added into image (a zeroed
+    device image by default); deltx/delty arcsec per pixel."""
+    if image is None:
+        image = ctx.zeros((ny, nx), ctx.torch.float32)
+    n = len(comps)
+    types = "".join(str(c[0])[:4].ljust(4) for c in comps).encode()
+    cols = [np.ascontiguousarray([float(c[j]) for c in comps], np.float32) for j in range(1, 7)]
+    ptr = [a.ctypes.data_as(C.c_void_p) for a in cols]
+    check(lib().sde_model_image(ctx.h, n, types, *ptr, nx, ny, float(refx), float(deltx), float(refy),
+                                float(delty), _ptr(image)), "sde_model_image")
+    return image
+
+
 def dft_image(ctx, u, v, vis, wt, nx, ny, refx, deltx, refy, delty, dirty=True, psf=True):
     """VISDFT3D (2-D) on device tensors (sde_dft_image): dict(dirty, psf) [ny][nx]."""
     torch = ctx.torch
