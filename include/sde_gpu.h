@@ -67,6 +67,13 @@ void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, f
                float *gvis, int *nu, int *nv, float *intfnu, int *suppu, int *osampu,
                float *intfnv, int *suppv, int *osampv, double *shift);
 
+/* Replaces GRDQH2D (source/grd/grdqh2d.f:7-9), called by VISGRID for the 'BOX' gridding
+ * function (vis/visgrid.f:154-158): nearest-cell gridding with the shift matrix's phase
+ * rotation, u = 0 column folded, shift one column left and (NU-1)*NV/LSUMWT. */
+void grdqh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+              float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin, float *gvis,
+              int *psf, int *nu, int *nv, double *shift, float *sumwt);
+
 /* Replaces GRDUWT2D (source/grd/grduwt2d.f:7-8), called by GRDUWT (grd/grduwt.f:122). */
 void grduwt2d_(float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
                float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
@@ -282,6 +289,14 @@ int sde_dft_image(sde_ctx *ctx, int64_t nvis, const float *u, const float *v, co
 int sde_dft_vis(sde_ctx *ctx, const float *image, int nx, int ny, double refx, double deltx,
                 double refy, double delty, int64_t nvis, const float *u, const float *v,
                 const float *wt, float *vis);
+
+/* GRDQH2D on device arrays (the 'BOX' gridder): vis complex64 pairs (ignored for psf), grid
+ * [nv][pitch] complex64 (NU columns written), shift the host 3x3 DOUBLE matrix (column-major,
+ * as CRDSHIFT makes it).  SDE_ENOWEIGHT ('No weight!') leaves the folded, unnormalised grid. */
+int sde_grid_box(sde_ctx *ctx, int64_t nvis, const float *vis, const float *wt, const float *u,
+                 const float *v, const float *w, float uscale, float uoffset, float vscale,
+                 float voffset, int uorigin, int vorigin, int psf, int nu, int nv,
+                 const double *shift, float *grid, int pitch, float *sumwt);
 
 /* MODIMG2D (mod/modimg2d.f, via MODIMG, mod/modimg.f): ncomp model components added into the
  * device image [ny][nx].  types: 4 characters per component (POIN, GAUS, DISK, RECT, SPHE,

@@ -93,6 +93,10 @@ def lib():
                                      C.c_double, C.c_double, C.c_double, C.c_double]
         L.orc64_imgdft2d.argtypes = [f32p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                      C.c_double, c128p, C.c_int, f32p, f32p, f32p]
+        L.orc_grdqh2d.restype = C.c_int
+        L.orc_grdqh2d.argtypes = [c64p, f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float,
+                                  C.c_float, C.c_int, C.c_int, c64p, C.c_int, C.c_int, C.c_int, f64p,
+                                  C.POINTER(C.c_float)]
         L.orc_modimg2d.restype = C.c_int
         L.orc_modimg2d.argtypes = [C.c_int, i32p, f32p, f32p, f32p, f32p, f32p, f32p, f32p, C.c_int,
                                    C.c_int, C.c_float, C.c_float, C.c_float, C.c_float]
@@ -316,6 +320,16 @@ def imgdft2d(image, refx, deltx, refy, delty, wt, u, v, vis_in=None, fp64=False)
         vis = np.zeros(len(wt), np.complex64) if vis_in is None else _c64(vis_in).copy()
         lib().orc_imgdft2d(image, nx, ny, refx, deltx, refy, delty, vis, len(wt), wt, u, v)
     return vis
+
+
+def grdqh2d(vis, wt, u, v, w, g, psf=False):
+    """GRDQH2D with the geometry g (orc_geom): (grid [nv][nu] complex64, sumwt, rc)."""
+    grid = np.zeros((g.nv, g.nu), np.complex64)
+    sw = C.c_float()
+    shift = np.ascontiguousarray(np.array(list(g.shift), np.float64))
+    rc = lib().orc_grdqh2d(_c64(vis), _f32(wt), _f32(u), _f32(v), _f32(w), len(wt), g.uscale, 0.0, g.vscale, 0.0,
+                           g.uorigin, g.vorigin, grid, int(psf), g.nu, g.nv, shift, C.byref(sw))
+    return grid, sw.value, rc
 
 
 MODEL_TYPES = ["POIN", "GAUS", "DISK", "RECT", "SPHE", "SHEL", "PLOR"]

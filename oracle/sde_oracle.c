@@ -1655,3 +1655,66 @@ int orc_modimg2d(int ncomp, const int *type, const float *flux, const float *ra,
     }
     return 0;
 }
+
+/* grd/grdqh2d.f:64-133 -- 'BOX' gridding: nearest cell, sequential REAL sums in visibility
+ * order; gvis [nv][nu] complex; shift DOUBLE 3x3 column-major.  Returns -1 'No weight!'
+ * (grid left folded and unnormalised). */
+int orc_grdqh2d(const float *vis, const float *wt, const float *u, const float *v, const float *w, int nvis,
+                float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin, float *gvis,
+                int psf, int nu, int nv, const double *shift, float *sumwt) {
+    const float twopi = 8.0f * atanf(1.0f);
+    for (size_t k = 0; k < (size_t)2 * nu * nv; k++) gvis[k] = 0.0f;
+    float lsumwt = 0.0f;
+    *sumwt = 0.0f;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        const float ul = (float)(shift[0] * u[i] + shift[1] * v[i] + shift[2] * w[i]);
+        const float vl = (float)(shift[3] * u[i] + shift[4] * v[i] + shift[5] * w[i]);
+        const float wl = (float)(shift[6] * u[i] + shift[7] * v[i] + shift[8] * w[i]);
+        const float phase = twopi * (wl - w[i]);
+        const float c = cosf(phase), s = -sinf(phase);
+        float fr = vis[2 * i] * c - vis[2 * i + 1] * s, fi = vis[2 * i] * s + vis[2 * i + 1] * c;
+        float ucell = uscale * ul + uoffset, vcell = vscale * vl + voffset;
+        *sumwt = *sumwt + wt[i];
+        if (ucell > 0.0f) {
+            fi = -fi;
+            ucell = ucell + (float)uorigin;
+            vcell = vcell + (float)vorigin;
+        } else {
+            ucell = -ucell + (float)uorigin;
+            vcell = -vcell + (float)vorigin;
+        }
+        if (psf) {
+            fr = 1.0f;
+            fi = 0.0f;
+        }
+        const int ug = orc_nint_f(ucell) + 1, vg = orc_nint_f(vcell);
+        if (ug < 1 || ug > nu || vg < 1 || vg > nv) continue;
+        float *g = gvis + 2 * ((size_t)(vg - 1) * nu + (ug - 1));
+        g[0] = g[0] + wt[i] * fr;
+        g[1] = g[1] + wt[i] * fi;
+        lsumwt = lsumwt + wt[i];
+    }
+    const int uz = uorigin + 1, vz = vorigin;
+    for (int off = 0; off <= nv / 2 - 1; off++) {
+        if (vz + off > nv || vz - off < 1) continue;
+        float *p = gvis + 2 * ((size_t)(vz + off - 1) * nu + (uz - 1));
+        float *m = gvis + 2 * ((size_t)(vz - off - 1) * nu + (uz - 1));
+        p[0] = p[0] + m[0];
+        p[1] = p[1] - m[1];
+        m[0] = p[0];
+        m[1] = -p[1];
+    }
+    if (lsumwt == 0.0f) return -1;
+    lsumwt = (float)(nu - 1) * (float)nv / lsumwt;
+    for (int vg = 0; vg < nv; vg++) {
+        float *row = gvis + 2 * (size_t)vg * nu;
+        for (int ug = 0; ug < nu - 1; ug++) {
+            row[2 * ug] = lsumwt * row[2 * ug + 2];
+            row[2 * ug + 1] = lsumwt * row[2 * ug + 3];
+        }
+        row[2 * (nu - 1)] = 0.0f;
+        row[2 * (nu - 1) + 1] = 0.0f;
+    }
+    return 0;
+}

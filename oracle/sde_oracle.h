@@ -141,6 +141,11 @@ int  orc64_visdft2d(const float *vis, int nvis, const float *wt, const float *u,
 void orc64_imgdft2d(const float *image, int nx, int ny, double refx, double deltx, double refy,
                     double delty, double *vis, int nvis, const float *wt, const float *u, const float *v);
 
+/* GRDQH2D (grd/grdqh2d.f): 'BOX' gridding into gvis [nv][nu] complex. */
+int orc_grdqh2d(const float *vis, const float *wt, const float *u, const float *v, const float *w, int nvis,
+                float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin, float *gvis,
+                int psf, int nu, int nv, const double *shift, float *sumwt);
+
 /* MODIMG2D (mod/modimg2d.f): components added into image [ny][nx]; type 0 POIN, 1 GAUS,
  * 2 DISK, 3 RECT, 4 SPHE, 5 SHEL, 6 PLOR; offsets and increments in arcsec. */
 int orc_modimg2d(int ncomp, const int *type, const float *flux, const float *ra, const float *dec,

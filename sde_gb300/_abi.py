@@ -141,6 +141,7 @@ SIGNATURES = [
     ("sde_batch_graph_nodes", I, [P]),
     ("sde_batch_image", I, [P, I, I, C.POINTER(P)]),
     ("sde_batch_read", I, [P, I, I, P, I64]),
+    ("sde_grid_box", I, [P, I64, P, P, P, P, P, F, F, F, F, I, I, I, I, I, P, P, I, C.POINTER(F)]),
     ("sde_model_image", I, [P, I, C.c_char_p, P, P, P, P, P, P, I, I, F, F, F, F, P]),
     ("sde_dft_image", I, [P, I64, P, P, P, P, I, I, C.c_double, C.c_double, C.c_double,
                           C.c_double, P, P]),
@@ -157,6 +158,7 @@ SIGNATURES = [
     # Fortran-77 drop-in layer (all arguments by reference)
     ("grdh2d_", None, [P] * 24),
     ("grddeh2d_", None, [P] * 22),
+    ("grdqh2d_", None, [P] * 18),
     ("grduwt2d_", None, [P] * 16),
     ("grdruw2d_", None, [P] * 19 + [C.c_size_t]),
     ("fftr2d_", None, [P] * 10),

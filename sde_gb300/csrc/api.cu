@@ -828,6 +828,56 @@ extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int
         report_rc(rc, R);
 }
 
+// GRDQH2D (grd/grdqh2d.f), VISGRID's gridder for the 'BOX' function (vis/visgrid.f:154-158)
+extern "C" void grdqh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+                         float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin, float *gvis,
+                         int *psf, int *nu, int *nv, double *shift, float *sumwt) {
+    if (sysi_.error) return;
+    std::lock_guard<std::mutex> lk(g_shim_mu);
+    const char *R = "GRDQH2D";
+    sde_ctx *ctx = shim_ctx();
+    if (!ctx) {
+        report("No GPU", R, sde_last_error());
+        return;
+    }
+    const int64_t n = *nvis > 0 ? *nvis : 0;
+    const size_t nb = (size_t)(n > 0 ? n : 1);
+    float *din = nullptr, *dg = nullptr;
+    int rc = ctx_scratch(ctx, "box_in", sizeof(float) * nb * 6, (void **)&din);
+    if (rc == SDE_OK) rc = ctx_scratch(ctx, "box_grid", sizeof(float2) * (size_t)*nu * *nv, (void **)&dg);
+    float *dvis = din, *dwt = din + 2 * nb, *du = dwt + nb, *dv = du + nb, *dw = dv + nb;
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    if (rc == SDE_OK && n > 0) {
+        e = cudaMemcpyAsync(dvis, vis, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dwt, wt, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(du, u, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dw, w, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) {
+            sde_set_error("%s", cudaGetErrorString(e));
+            rc = SDE_ECUDA;
+        }
+    }
+    float sw = 0.0f;
+    if (rc == SDE_OK)
+        rc = grid_box(ctx, n, dvis, dwt, du, dv, dw, *uscale, *uoffset, *vscale, *voffset, *uorigin, *vorigin, *psf,
+                      *nu, *nv, shift, dg, *nu, &sw, nullptr);
+    if (rc == SDE_OK || rc == SDE_ENOWEIGHT) {
+        e = cudaMemcpyAsync(gvis, dg, sizeof(float2) * (size_t)*nu * *nv, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess && rc == SDE_OK) {
+            sde_set_error("%s", cudaGetErrorString(e));
+            rc = SDE_ECUDA;
+        }
+        *sumwt = sw;
+    }
+    if (rc == SDE_ENOWEIGHT)
+        report("Bad argument", R, "No weight!");
+    else if (rc != SDE_OK)
+        report_rc(rc, R);
+}
+
 extern "C" void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis,
                           float *uscale, float *uoffset, float *vscale, float *voffset,
                           int *uorigin, int *vorigin, float *gvis, int *nu, int *nv, float *intfnu,

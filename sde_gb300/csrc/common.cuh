@@ -264,6 +264,10 @@ int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, const uint16
 // (cu | cv << 16) of plan cores[b].x (its raw and raw_lo)
 int launch_fold_lo_batch(sde_ctx *ctx, const BatchPlan *d_plans, const int2 *cores, int64_t ncores);
 int check_fft_shape(int nx, int ny, int fnu, int nv);  // SDE_EINVAL + message if unsupported
+// GRDQH2D on device arrays (box.cu); shift is the host 3x3 DOUBLE matrix, column-major
+int grid_box(sde_ctx *ctx, int64_t nvis, const float *vis, const float *wt, const float *u, const float *v,
+             const float *w, float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin,
+             int psf, int nu, int nv, const double *shift, float *grid, int pitch, float *sumwt, int64_t *ngrid);
 // batched images from raw accumulations (fft.cu; EINVAL when the shape has no fused path;
 // fin_fused_shape says which grids have one)
 bool fin_fused_shape(int nu, int nv);
