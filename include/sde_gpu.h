@@ -74,6 +74,22 @@ void grdqh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, fl
               float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin, float *gvis,
               int *psf, int *nu, int *nv, double *shift, float *sumwt);
 
+/* Replace GRDH23D (source/grd/grdh23d.f:5-8) and GRDDEH23 (source/grd/grddeh23.f:5-8), the
+ * slow-Z gridder and degridder VISGRID (vis/visgrid.f:219-226) and VISDEGRI
+ * (vis/visdegri.f:154-160) call for N----SIN third axes: the 2-D window on NZ planes, plane iz
+ * rotated by exp(-/+i TWOPI WLOCAL DTOR CELLZ (iz-REFZ)); GVIS [NZ][NV][NU] complex; tables
+ * of 2*(SUPP+1)*OSAMP+1 floats (any support and oversampling). */
+void grdh23d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+              float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin, float *gvis,
+              int *psf, int *nu, int *nv, float *gridfnu, int *suppu, int *osampu, float *gridfnv,
+              int *suppv, int *osampv, int *nz, float *cellz, float *refz, double *shift,
+              float *sumwt);
+void grddeh23_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+               float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
+               float *gvis, int *nu, int *nv, float *intfnu, int *suppu, int *osampu,
+               float *intfnv, int *suppv, int *osampv, int *nz, float *cellz, float *refz,
+               double *shift);
+
 /* Replaces GRDUWT2D (source/grd/grduwt2d.f:7-8), called by GRDUWT (grd/grduwt.f:122). */
 void grduwt2d_(float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
                float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,

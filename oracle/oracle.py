@@ -93,6 +93,15 @@ def lib():
                                      C.c_double, C.c_double, C.c_double, C.c_double]
         L.orc64_imgdft2d.argtypes = [f32p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                      C.c_double, c128p, C.c_int, f32p, f32p, f32p]
+        L.orc_grdh23d.restype = C.c_int
+        L.orc_grdh23d.argtypes = [c64p, f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float,
+                                  C.c_float, C.c_int, C.c_int, c64p, C.c_int, C.c_int, C.c_int, f32p, C.c_int,
+                                  C.c_int, f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, f64p,
+                                  C.POINTER(C.c_float)]
+        L.orc_grddeh23.restype = C.c_int
+        L.orc_grddeh23.argtypes = [c64p, f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float,
+                                   C.c_float, C.c_int, C.c_int, c64p, C.c_int, C.c_int, f32p, C.c_int, C.c_int,
+                                   f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, f64p]
         L.orc_grdqh2d.restype = C.c_int
         L.orc_grdqh2d.argtypes = [c64p, f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float,
                                   C.c_float, C.c_int, C.c_int, c64p, C.c_int, C.c_int, C.c_int, f64p,
@@ -330,6 +339,29 @@ def grdqh2d(vis, wt, u, v, w, g, psf=False):
     rc = lib().orc_grdqh2d(_c64(vis), _f32(wt), _f32(u), _f32(v), _f32(w), len(wt), g.uscale, 0.0, g.vscale, 0.0,
                            g.uorigin, g.vorigin, grid, int(psf), g.nu, g.nv, shift, C.byref(sw))
     return grid, sw.value, rc
+
+
+def grdh23d(vis, wt, u, v, w, g, cf, nz, cellz, refz, psf=False):
+    """GRDH23D with geometry g and the SF table cf: (grid [nz][nv][nu] complex64, sumwt, rc)."""
+    grid = np.zeros((nz, g.nv, g.nu), np.complex64)
+    sw = C.c_float()
+    shift = np.ascontiguousarray(np.array(list(g.shift), np.float64))
+    rc = lib().orc_grdh23d(_c64(vis), _f32(wt), _f32(u), _f32(v), _f32(w), len(wt), g.uscale, 0.0, g.vscale, 0.0,
+                           g.uorigin, g.vorigin, grid, int(psf), g.nu, g.nv, _f32(cf), 3, 128, _f32(cf), 3, 128,
+                           nz, cellz, refz, shift, C.byref(sw))
+    return grid, sw.value, rc
+
+
+def grddeh23(vis, wt, u, v, w, g, cf, grid, cellz, refz):
+    """GRDDEH23: (vis, wt, nbad) with the model cube grid [nz][nv][nu]."""
+    vis = _c64(vis).copy()
+    wt = _f32(wt).copy()
+    shift = np.ascontiguousarray(np.array(list(g.shift), np.float64))
+    nz = grid.shape[0]
+    nbad = lib().orc_grddeh23(vis, wt, _f32(u), _f32(v), _f32(w), len(wt), g.uscale, 0.0, g.vscale, 0.0, g.uorigin,
+                              g.vorigin, np.ascontiguousarray(grid, np.complex64), g.nu, g.nv, _f32(cf), 3, 128,
+                              _f32(cf), 3, 128, nz, cellz, refz, shift)
+    return vis, wt, nbad
 
 
 MODEL_TYPES = ["POIN", "GAUS", "DISK", "RECT", "SPHE", "SHEL", "PLOR"]

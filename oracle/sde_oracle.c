@@ -1718,3 +1718,219 @@ int orc_grdqh2d(const float *vis, const float *wt, const float *u, const float *
     }
     return 0;
 }
+
+/* grd/grdh23d.f:39-147 -- slow-Z gridding: gvis [nz][nv][nu] complex; tables of
+ * 2*(supp+1)*osamp+1 floats.  Returns -1 'No weight!' (grid left unfolded). */
+int orc_grdh23d(const float *vis, const float *wt, const float *u, const float *v, const float *w, int nvis,
+                float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin, float *gvis,
+                int psf, int nu, int nv, const float *fnu, int suppu, int osampu, const float *fnv, int suppv,
+                int osampv, int nz, float cellz, float refz, const double *shift, float *sumwt) {
+    const float twopi = 8.0f * atanf(1.0f), dtor = twopi / 360.0f;
+    const int cfou = (suppu + 1) * osampu + 1, cfov = (suppv + 1) * osampv + 1;
+#define G3(uu, vv, zz) (gvis + 2 * (((size_t)(zz) - 1) * nv * nu + ((size_t)(vv) - 1) * nu + ((uu) - 1)))
+    for (size_t k = 0; k < (size_t)2 * nu * nv * nz; k++) gvis[k] = 0.0f;
+    float lsumwt = 0.0f;
+    *sumwt = 0.0f;
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        *sumwt = *sumwt + wt[i];
+        const float ul = (float)(shift[0] * u[i] + shift[1] * v[i] + shift[2] * w[i]);
+        const float vl = (float)(shift[3] * u[i] + shift[4] * v[i] + shift[5] * w[i]);
+        float wl = (float)(shift[6] * u[i] + shift[7] * v[i] + shift[8] * w[i]);
+        float phase = twopi * (wl - w[i]);
+        float c = cosf(phase), s = -sinf(phase);
+        float fr = vis[2 * i] * c - vis[2 * i + 1] * s, fi = vis[2 * i] * s + vis[2 * i + 1] * c;
+        float ucell = uscale * ul + uoffset, vcell = vscale * vl + voffset;
+        if (ucell > 0.0f) {
+            fi = -fi;
+            ucell = ucell + (float)uorigin;
+            vcell = vcell + (float)vorigin;
+        } else {
+            ucell = -ucell + (float)uorigin;
+            vcell = -vcell + (float)vorigin;
+            wl = -wl;
+        }
+        if (psf) {
+            fr = 1.0f;
+            fi = 0.0f;
+        }
+        const int nuc = orc_nint_f(ucell), nvc = orc_nint_f(vcell);
+        if (nuc + 2 * suppu > nu || nvc + suppv > nv || nvc - suppv < 1) continue;
+        const int delui = orc_nint_f((float)osampu * ((float)nuc - ucell));
+        const int delvi = orc_nint_f((float)osampv * ((float)nvc - vcell));
+        const int uzero = nuc + suppu, vzero = nvc;
+        for (int iz = 1; iz <= nz; iz++) {
+            phase = -twopi * wl * dtor * cellz * ((float)iz - refz);
+            c = cosf(phase);
+            s = -sinf(phase);
+            const float rr = fr * c - fi * s, ri = fr * s + fi * c;
+            for (int ov = -suppv; ov <= suppv; ov++) {
+                const int delv = delvi + osampv * ov + cfov;
+                for (int ou = -suppu; ou <= suppu; ou++) {
+                    const int delu = delui + osampu * ou + cfou;
+                    const float uvwt = wt[i] * fnu[delu - 1] * fnv[delv - 1];
+                    float *g = G3(uzero + ou, vzero + ov, iz);
+                    g[0] = g[0] + uvwt * rr;
+                    g[1] = g[1] + uvwt * ri;
+                    lsumwt = lsumwt + uvwt;
+                }
+            }
+        }
+    }
+    if (lsumwt == 0.0f) return -1;
+    const int uz = uorigin + suppu, vz = vorigin;
+    for (int iz = 1; iz <= nz; iz++)
+        for (int ov = -nv / 2 + 1; ov <= nv / 2 - 1; ov++)
+            for (int ou = 1; ou <= suppu; ou++) {
+                if (vz + ov < 1 || vz + ov > nv || vz - ov < 1 || vz - ov > nv || uz - ou < 1) continue;
+                float *a = G3(uz + ou, vz + ov, iz), *b = G3(uz - ou, vz - ov, iz);
+                a[0] = a[0] + b[0];
+                a[1] = a[1] - b[1];
+            }
+    for (int iz = 1; iz <= nz; iz++)
+        for (int ov = 0; ov <= nv / 2 - 1; ov++) {
+            if (vz + ov > nv || vz - ov < 1) continue;
+            float *a = G3(uz, vz + ov, iz), *b = G3(uz, vz - ov, iz);
+            a[0] = a[0] + b[0];
+            a[1] = a[1] - b[1];
+            b[0] = a[0];
+            b[1] = -a[1];
+        }
+    lsumwt = (float)(nu - 1) * (float)nv * (float)nz / lsumwt;
+    for (int iz = 1; iz <= nz; iz++)
+        for (int vg = 1; vg <= nv; vg++) {
+            for (int ug = 1; ug <= nu - suppu; ug++) {
+                float *a = G3(ug, vg, iz), *b = G3(ug + suppu, vg, iz);
+                a[0] = lsumwt * b[0];
+                a[1] = lsumwt * b[1];
+            }
+            for (int ug = nu - suppu + 1; ug <= nu; ug++) G3(ug, vg, iz)[0] = G3(ug, vg, iz)[1] = 0.0f;
+        }
+#undef G3
+    return 0;
+}
+
+/* grd/grddeh23.f:45-190 -- slow-Z degridding in the reference's loop and operation order;
+ * reads outside the grid (the reference's mirrored rows) read 0.  Returns NBAD. */
+int orc_grddeh23(float *vis, float *wt, const float *u, const float *v, const float *w, int nvis, float uscale,
+                 float uoffset, float vscale, float voffset, int uorigin, int vorigin, const float *gvis, int nu,
+                 int nv, const float *fnu, int suppu, int osampu, const float *fnv, int suppv, int osampv, int nz,
+                 float cellz, float refz, const double *shift) {
+    const float twopi = 8.0f * atanf(1.0f), dtor = twopi / 360.0f;
+    const int cfou = (suppu + 1) * osampu + 1, cfov = (suppv + 1) * osampv + 1;
+    int nbad = 0;
+    float *crr = (float *)malloc(sizeof(float) * nz), *cri = (float *)malloc(sizeof(float) * nz);
+    for (int i = 0; i < nvis; i++) {
+        if (wt[i] <= 0.0f) continue;
+        float ar = 0.0f, ai = 0.0f, sumwt = 0.0f;
+        vis[2 * i] = vis[2 * i + 1] = 0.0f;
+        wt[i] = -wt[i];
+        const float ul = (float)(shift[0] * u[i] + shift[1] * v[i] + shift[2] * w[i]);
+        const float vl = (float)(shift[3] * u[i] + shift[4] * v[i] + shift[5] * w[i]);
+        float wl = (float)(shift[6] * u[i] + shift[7] * v[i] + shift[8] * w[i]);
+        float phase = twopi * (wl - w[i]);
+        const float rotr = cosf(phase), roti = sinf(phase);
+        float ucell = uscale * ul + uoffset, vcell = vscale * vl + voffset;
+        if (ucell > 0.0f) {
+            ucell = ucell + (float)uorigin;
+            vcell = vcell + (float)vorigin;
+        } else {
+            ucell = -ucell + (float)uorigin;
+            vcell = -vcell + (float)vorigin;
+            wl = -wl;
+        }
+        const int nuc = orc_nint_f(ucell), nvc = orc_nint_f(vcell);
+        if (nuc + suppu > nu || nvc + suppv > nv || nvc - suppv < 1) continue;
+        const int delui = orc_nint_f((float)osampu * ((float)nuc - ucell));
+        const int delvi = orc_nint_f((float)osampv * ((float)nvc - vcell));
+        const int ucen = nuc - uorigin, vcen = nvc - vorigin;
+        for (int iz = 1; iz <= nz; iz++) {
+            phase = -twopi * wl * dtor * cellz * ((float)iz - refz);
+            crr[iz - 1] = cosf(phase);
+            cri[iz - 1] = sinf(phase);
+        }
+#define GAT(uu, vv, zz, R, I)                                                                              \
+    do {                                                                                                   \
+        if ((uu) < 1 || (uu) > nu || (vv) < 1 || (vv) > nv) {                                              \
+            R = 0.0f;                                                                                      \
+            I = 0.0f;                                                                                      \
+        } else {                                                                                           \
+            const float *q_ = gvis + 2 * (((size_t)(zz) - 1) * nv * nu + ((size_t)(vv) - 1) * nu + ((uu) - 1)); \
+            R = q_[0];                                                                                     \
+            I = q_[1];                                                                                     \
+        }                                                                                                  \
+    } while (0)
+        if (nuc <= suppu) {
+            for (int ou = -suppu; ou <= suppu; ou++) {
+                const int delu = delui + osampu * ou + cfou;
+                if (ucen != -ou) {
+                    const int us = (ucen + ou) >= 0 ? 1 : -1;
+                    const int ui = uorigin + us * (ucen + ou);
+                    for (int ov = -suppv; ov <= suppv; ov++) {
+                        const int delv = delvi + osampv * ov + cfov;
+                        const int vi = vorigin + us * (vcen + ov);
+                        const float uvwt = fnu[delu - 1] * fnv[delv - 1];
+                        sumwt = sumwt + uvwt;
+                        for (int iz = 1; iz <= nz; iz++) {
+                            float gr, gi;
+                            GAT(ui, vi, iz, gr, gi);
+                            if (us < 0) gi = -gi;
+                            const float pr = gr * crr[iz - 1] - gi * cri[iz - 1], pi_ = gr * cri[iz - 1] + gi * crr[iz - 1];
+                            ar = ar + pr * uvwt;
+                            ai = ai + pi_ * uvwt;
+                        }
+                    }
+                } else {
+                    for (int ov = -suppv; ov <= suppv; ov++) {
+                        const int delv = delvi + osampv * ov + cfov;
+                        const int vi = vorigin + (vcen + ov);
+                        const float uvwt = fnu[delu - 1] * fnv[delv - 1];
+                        sumwt = sumwt + uvwt;
+                        for (int iz = 1; iz <= nz; iz++) {
+                            float gr, gi;
+                            GAT(uorigin, vi, iz, gr, gi);
+                            gr = gr * uvwt;
+                            gi = gi * uvwt;
+                            ar = ar + (gr * crr[iz - 1] - gi * cri[iz - 1]);
+                            ai = ai + (gr * cri[iz - 1] + gi * crr[iz - 1]);
+                        }
+                    }
+                }
+            }
+        } else {
+            for (int ov = -suppv; ov <= suppv; ov++) {
+                const int delv = delvi + osampv * ov + cfov;
+                const int vi = vorigin + vcen + ov;
+                for (int ou = -suppu; ou <= suppu; ou++) {
+                    const int delu = delui + osampu * ou + cfou;
+                    const int ui = uorigin + ucen + ou;
+                    const float uvwt = fnu[delu - 1] * fnv[delv - 1];
+                    sumwt = sumwt + uvwt;
+                    for (int iz = 1; iz <= nz; iz++) {
+                        float gr, gi;
+                        GAT(ui, vi, iz, gr, gi);
+                        gr = gr * uvwt;
+                        gi = gi * uvwt;
+                        ar = ar + (gr * crr[iz - 1] - gi * cri[iz - 1]);
+                        ai = ai + (gr * cri[iz - 1] + gi * crr[iz - 1]);
+                    }
+                }
+            }
+        }
+#undef GAT
+        if (sumwt > 0.0f) {
+            ar = ar / sumwt;
+            ai = ai / sumwt;
+            wt[i] = fabsf(wt[i]);
+        } else {
+            nbad++;
+            ar = ai = 0.0f;
+        }
+        if (uscale * ul > 0.0f) ai = -ai;
+        vis[2 * i] = ar * rotr - ai * roti;
+        vis[2 * i + 1] = ar * roti + ai * rotr;
+    }
+    free(crr);
+    free(cri);
+    return nbad;
+}

@@ -141,6 +141,17 @@ int  orc64_visdft2d(const float *vis, int nvis, const float *wt, const float *u,
 void orc64_imgdft2d(const float *image, int nx, int ny, double refx, double deltx, double refy,
                     double delty, double *vis, int nvis, const float *wt, const float *u, const float *v);
 
+/* GRDH23D / GRDDEH23 (grd/grdh23d.f, grd/grddeh23.f): slow-Z gridding and degridding,
+ * gvis [nz][nv][nu] complex, tables of 2*(supp+1)*osamp+1 floats. */
+int orc_grdh23d(const float *vis, const float *wt, const float *u, const float *v, const float *w, int nvis,
+                float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin, float *gvis,
+                int psf, int nu, int nv, const float *fnu, int suppu, int osampu, const float *fnv, int suppv,
+                int osampv, int nz, float cellz, float refz, const double *shift, float *sumwt);
+int orc_grddeh23(float *vis, float *wt, const float *u, const float *v, const float *w, int nvis, float uscale,
+                 float uoffset, float vscale, float voffset, int uorigin, int vorigin, const float *gvis, int nu,
+                 int nv, const float *fnu, int suppu, int osampu, const float *fnv, int suppv, int osampv, int nz,
+                 float cellz, float refz, const double *shift);
+
 /* GRDQH2D (grd/grdqh2d.f): 'BOX' gridding into gvis [nv][nu] complex. */
 int orc_grdqh2d(const float *vis, const float *wt, const float *u, const float *v, const float *w, int nvis,
                 float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin, float *gvis,

@@ -159,6 +159,8 @@ SIGNATURES = [
     ("grdh2d_", None, [P] * 24),
     ("grddeh2d_", None, [P] * 22),
     ("grdqh2d_", None, [P] * 18),
+    ("grdh23d_", None, [P] * 27),
+    ("grddeh23_", None, [P] * 25),
     ("grduwt2d_", None, [P] * 16),
     ("grdruw2d_", None, [P] * 19 + [C.c_size_t]),
     ("fftr2d_", None, [P] * 10),

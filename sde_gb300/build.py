@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libsdegpu.so")
-SOURCES = ["api.cu", "sort.cu", "weights.cu", "plan.cu", "grid.cu", "fft.cu", "clean.cu", "batch.cu", "jobs.cu", "uvfits.cu", "clark.cu", "dft.cu", "model.cu", "box.cu"]
+SOURCES = ["api.cu", "sort.cu", "weights.cu", "plan.cu", "grid.cu", "fft.cu", "clean.cu", "batch.cu", "jobs.cu", "uvfits.cu", "clark.cu", "dft.cu", "model.cu", "box.cu", "slowz.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]

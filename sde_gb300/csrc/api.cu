@@ -828,6 +828,120 @@ extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int
         report_rc(rc, R);
 }
 
+// Host arrays of a slow-Z call on the device: vis, wt, u, v, w, both tables (uploads in order)
+static int h23_upload(sde_ctx *ctx, int64_t n, const float *vis, const float *wt, const float *u,
+                      const float *v, const float *w, const float *fnu, int lu, const float *fnv, int lv,
+                      float **d) {
+    const size_t nb = (size_t)(n > 0 ? n : 1);
+    SDE_TRY(ctx_scratch(ctx, "h23_in", sizeof(float) * (nb * 6 + (size_t)lu + (size_t)lv), (void **)d));
+    float *p = *d;
+    const float *src[7] = {vis, wt, u, v, w, fnu, fnv};
+    const size_t len[7] = {2 * (size_t)n, (size_t)n, (size_t)n, (size_t)n, (size_t)n, (size_t)lu, (size_t)lv};
+    const size_t off[7] = {0, 2 * nb, 3 * nb, 4 * nb, 5 * nb, 6 * nb, 6 * nb + (size_t)lu};
+    for (int i = 0; i < 7; i++)
+        if (len[i]) SDE_CUDA_TRY(cudaMemcpyAsync(p + off[i], src[i], sizeof(float) * len[i], cudaMemcpyHostToDevice,
+                                                 ctx->stream));
+    return SDE_OK;
+}
+
+// GRDH23D (grd/grdh23d.f), VISGRID's slow-Z gridder (vis/visgrid.f:219-226)
+extern "C" void grdh23d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+                         float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin, float *gvis,
+                         int *psf, int *nu, int *nv, float *gridfnu, int *suppu, int *osampu, float *gridfnv,
+                         int *suppv, int *osampv, int *nz, float *cellz, float *refz, double *shift, float *sumwt) {
+    if (sysi_.error) return;
+    std::lock_guard<std::mutex> lk(g_shim_mu);
+    const char *R = "GRDH23D";
+    sde_ctx *ctx = shim_ctx();
+    if (!ctx) {
+        report("No GPU", R, sde_last_error());
+        return;
+    }
+    const int64_t n = *nvis > 0 ? *nvis : 0;
+    const size_t nb = (size_t)(n > 0 ? n : 1);
+    const int lu = 2 * (*suppu + 1) * *osampu + 1, lv = 2 * (*suppv + 1) * *osampv + 1;
+    const size_t cells = (size_t)*nu * *nv * (*nz > 0 ? *nz : 0);
+    float *d = nullptr, *dg = nullptr;
+    int rc = (*nu < 2 || *nv < 2 || *nz < 1 || *suppu < 0 || *suppv < 0 || *osampu < 1 || *osampv < 1) ? SDE_EINVAL
+                                                                                                    : SDE_OK;
+    if (rc == SDE_EINVAL) sde_set_error("bad grid or table sizes");
+    if (rc == SDE_OK) rc = h23_upload(ctx, n, vis, wt, u, v, w, gridfnu, lu, gridfnv, lv, &d);
+    if (rc == SDE_OK) rc = ctx_scratch(ctx, "h23_grid", sizeof(float2) * cells, (void **)&dg);
+    float sw = 0.0f;
+    if (rc == SDE_OK)
+        rc = grid_h23d(ctx, n, d, d + 2 * nb, d + 3 * nb, d + 4 * nb, d + 5 * nb, *uscale, *uoffset, *vscale, *voffset,
+                       *uorigin, *vorigin, *psf, *nu, *nv, d + 6 * nb, *suppu, *osampu, d + 6 * nb + lu, *suppv,
+                       *osampv, *nz, *cellz, *refz, shift, dg, &sw);
+    if (rc == SDE_OK || rc == SDE_ENOWEIGHT) {
+        cudaError_t e = cudaMemcpyAsync(gvis, dg, sizeof(float2) * cells, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess && rc == SDE_OK) {
+            sde_set_error("%s", cudaGetErrorString(e));
+            rc = SDE_ECUDA;
+        }
+        *sumwt = sw;
+    }
+    if (rc == SDE_ENOWEIGHT)
+        report("Bad argument", R, "No weight!");
+    else if (rc != SDE_OK)
+        report_rc(rc, R);
+}
+
+// GRDDEH23 (grd/grddeh23.f), VISDEGRI's slow-Z degridder (vis/visdegri.f:154-160)
+extern "C" void grddeh23_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
+                          float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin, float *gvis,
+                          int *nu, int *nv, float *intfnu, int *suppu, int *osampu, float *intfnv, int *suppv,
+                          int *osampv, int *nz, float *cellz, float *refz, double *shift) {
+    if (sysi_.error) return;
+    std::lock_guard<std::mutex> lk(g_shim_mu);
+    const char *R = "GRDDEH23";
+    sde_ctx *ctx = shim_ctx();
+    if (!ctx) {
+        report("No GPU", R, sde_last_error());
+        return;
+    }
+    const int64_t n = *nvis > 0 ? *nvis : 0;
+    const size_t nb = (size_t)(n > 0 ? n : 1);
+    const int lu = 2 * (*suppu + 1) * *osampu + 1, lv = 2 * (*suppv + 1) * *osampv + 1;
+    const size_t cells = (size_t)*nu * *nv * (*nz > 0 ? *nz : 0);
+    float *d = nullptr, *dg = nullptr;
+    int rc = (*nu < 2 || *nv < 2 || *nz < 1 || *suppu < 0 || *suppv < 0 || *osampu < 1 || *osampv < 1) ? SDE_EINVAL
+                                                                                                    : SDE_OK;
+    if (rc == SDE_EINVAL) sde_set_error("bad grid or table sizes");
+    if (rc == SDE_OK) rc = h23_upload(ctx, n, vis, wt, u, v, w, intfnu, lu, intfnv, lv, &d);
+    if (rc == SDE_OK) rc = ctx_scratch(ctx, "h23_mgrid", sizeof(float2) * cells, (void **)&dg);
+    if (rc == SDE_OK) {
+        cudaError_t e = cudaMemcpyAsync(dg, gvis, sizeof(float2) * cells, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) {
+            sde_set_error("%s", cudaGetErrorString(e));
+            rc = SDE_ECUDA;
+        }
+    }
+    int64_t nbad = 0;
+    if (rc == SDE_OK)
+        rc = degrid_h23(ctx, n, d, d + 2 * nb, d + 3 * nb, d + 4 * nb, d + 5 * nb, *uscale, *uoffset, *vscale, *voffset,
+                        *uorigin, *vorigin, dg, *nu, *nv, d + 6 * nb, *suppu, *osampu, d + 6 * nb + lu, *suppv,
+                        *osampv, *nz, *cellz, *refz, shift, &nbad);
+    if (rc == SDE_OK && n > 0) {
+        cudaError_t e = cudaMemcpyAsync(vis, d, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(wt, d + 2 * nb, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) {
+            sde_set_error("%s", cudaGetErrorString(e));
+            rc = SDE_ECUDA;
+        }
+    }
+    if (rc != SDE_OK) {
+        report_rc(rc, R);
+        return;
+    }
+    if (nbad > 0) {  // grd/grddeh23.f:185-189
+        char m[96];
+        snprintf(m, sizeof m, "%7lld points were not successfully degridded", (long long)nbad);
+        msgput_(m, "W", strlen(m), 1);
+    }
+}
+
 // GRDQH2D (grd/grdqh2d.f), VISGRID's gridder for the 'BOX' function (vis/visgrid.f:154-158)
 extern "C" void grdqh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
                          float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin, float *gvis,

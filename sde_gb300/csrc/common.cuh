@@ -264,6 +264,16 @@ int launch_finalize_batch(sde_ctx *ctx, const FinalizeDesc *d_desc, const uint16
 // (cu | cv << 16) of plan cores[b].x (its raw and raw_lo)
 int launch_fold_lo_batch(sde_ctx *ctx, const BatchPlan *d_plans, const int2 *cores, int64_t ncores);
 int check_fft_shape(int nx, int ny, int fnu, int nv);  // SDE_EINVAL + message if unsupported
+// GRDH23D / GRDDEH23 on device arrays (slowz.cu): grid [nz][nv][nu] complex, tables of
+// 2*(supp+1)*osamp+1 floats, shift the host 3x3 DOUBLE matrix
+int grid_h23d(sde_ctx *ctx, int64_t nvis, const float *vis, const float *wt, const float *u, const float *v,
+              const float *w, float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin,
+              int psf, int nu, int nv, const float *fnu, int suppu, int osampu, const float *fnv, int suppv,
+              int osampv, int nz, float cellz, float refz, const double *shift, float *grid, float *sumwt);
+int degrid_h23(sde_ctx *ctx, int64_t nvis, float *vis, float *wt, const float *u, const float *v, const float *w,
+               float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin, const float *grid,
+               int nu, int nv, const float *fnu, int suppu, int osampu, const float *fnv, int suppv, int osampv,
+               int nz, float cellz, float refz, const double *shift, int64_t *nbad);
 // GRDQH2D on device arrays (box.cu); shift is the host 3x3 DOUBLE matrix, column-major
 int grid_box(sde_ctx *ctx, int64_t nvis, const float *vis, const float *wt, const float *u, const float *v,
              const float *w, float uscale, float uoffset, float vscale, float voffset, int uorigin, int vorigin,
