@@ -314,6 +314,28 @@ int sde_grid_box(sde_ctx *ctx, int64_t nvis, const float *vis, const float *wt, 
                  float voffset, int uorigin, int vorigin, int psf, int nu, int nv,
                  const double *shift, float *grid, int pitch, float *sumwt);
 
+/* Ungridded robust weighting: uvmap's slow weighting (GridWeights = F, task/uvmap.f:283-290),
+ * GRDURUWT (grd/grduruwt.f) with GRDURUW2 (grd/grduruw2.f).  Host arrays; the neighbour
+ * search runs on the GPU.  Each point's local weight is the summed WT of the points (either
+ * conjugation) inside the ellipse of radii |IDELT/(WTFOV SQRT(PI))| around it, found through
+ * GRDURUW2's bin plane of linked lists (built in the reference's order, so the sums are its
+ * REAL sums); newwt = WT / (sum F2 + D2) with rmode 1 NORM (F2 = (5*10^-R)^2 / mean sum,
+ * D2 = 1), 2 ABS (F2 = R^2, D2 = 2 DS^2), 3 NONE (F2 = 1, D2 = 0).  Points with WT <= 0, and
+ * points off the bin plane, keep their WT.  nbu/nbv: bin plane size (<= 0: GRDEUSZ0's
+ * estimate).  shift: the 3x3 DOUBLE matrix from CRDSHIFT.  Messages: 'Unrecognized RMODE',
+ * 'Bad size for binning array', 'Problems with binsize calcs', 'Zero WTSUM'.  Saving or
+ * reading summed weights (SAVEWEIGHTS/READWEIGHTS) is not provided. */
+typedef struct {
+    int nbu, nbv;
+    int64_t ndrop, nsel;
+    float uradius, vradius, f2, d2;
+    double sumlocwt;
+} sde_uruwt_stats;
+int sde_weights_ungridded(sde_ctx *ctx, int64_t nvis, const float *u, const float *v, const float *w,
+                          const float *wt, float idelt_u, float idelt_v, float wtfov, int rmode,
+                          const float *robust, float ds, const double *shift, int nbu, int nbv,
+                          float *newwt, sde_uruwt_stats *stats);
+
 /* MODIMG2D (mod/modimg2d.f, via MODIMG, mod/modimg.f): ncomp model components added into the
  * device image [ny][nx].  types: 4 characters per component (POIN, GAUS, DISK, RECT, SPHE,
  * SHEL, PLOR); flux, ra, dec (offsets from the reference pixel), bmaj, bmin (arcsec), bpa

@@ -93,6 +93,9 @@ def lib():
                                      C.c_double, C.c_double, C.c_double, C.c_double]
         L.orc64_imgdft2d.argtypes = [f32p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                      C.c_double, c128p, C.c_int, f32p, f32p, f32p]
+        L.orc_grduruwt.restype = C.c_int
+        L.orc_grduruwt.argtypes = [f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
+                                   C.c_float, C.c_float, f64p, C.c_int, C.c_int, f32p, f64p]
         L.orc_grdh23d.restype = C.c_int
         L.orc_grdh23d.argtypes = [c64p, f32p, f32p, f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float,
                                   C.c_float, C.c_int, C.c_int, c64p, C.c_int, C.c_int, C.c_int, f32p, C.c_int,
@@ -339,6 +342,17 @@ def grdqh2d(vis, wt, u, v, w, g, psf=False):
     rc = lib().orc_grdqh2d(_c64(vis), _f32(wt), _f32(u), _f32(v), _f32(w), len(wt), g.uscale, 0.0, g.vscale, 0.0,
                            g.uorigin, g.vorigin, grid, int(psf), g.nu, g.nv, shift, C.byref(sw))
     return grid, sw.value, rc
+
+
+def grduruwt(u, v, w, wt, idelt_u, idelt_v, shift, wtfov=1.0, rmode="NORM", robust=0.0, ds=0.0, nbu=0, nbv=0):
+    """GRDURUWT/GRDURUW2: (newwt, rc, stats dict)."""
+    newwt = np.zeros(len(wt), np.float32)
+    st = np.zeros(7, np.float64)
+    rc = lib().orc_grduruwt(_f32(u), _f32(v), _f32(w), _f32(wt), len(wt), idelt_u, idelt_v, wtfov,
+                            {"NORM": 1, "ABS": 2, "NONE": 3}[rmode], robust, ds,
+                            np.ascontiguousarray(shift, np.float64), nbu, nbv, newwt, st)
+    keys = ("nbu", "nbv", "ndrop", "nsel", "uradius", "vradius", "f2")
+    return newwt, rc, dict(zip(keys, st.tolist()))
 
 
 def grdh23d(vis, wt, u, v, w, g, cf, nz, cellz, refz, psf=False):

@@ -1934,3 +1934,210 @@ int orc_grddeh23(float *vis, float *wt, const float *u, const float *v, const fl
     free(cri);
     return nbad;
 }
+
+/* ---------------------------------------------------------------------------------------
+ * GRDURUWT (grd/grduruwt.f) with GRDURUW2 (grd/grduruw2.f): ungridded robust weighting.
+ */
+static int orc_utlgint(float f) { /* utl/utlgint.f */
+    if (f >= 0.0f) return (int)f;
+    int i = (int)f;
+    return ((float)i == f) ? i : i - 1;
+}
+static int orc_utllint(float f) { /* utl/utllint.f */
+    int i = (int)f;
+    if (f >= 0.0f) return ((float)i == f) ? i : i + 1;
+    return i;
+}
+
+/* rmode 1 NORM, 2 ABS, 3 NONE; nbu/nbv <= 0: GRDEUSZ0's estimate.  newwt: the weights
+ * GRDURUWT leaves (ARRCOPY of NEWWT).  Returns 0, -1 zero WTSUM, -2 bad bin size, -3 bin
+ * calculation, -4 bad RMODE.  stats (7): nbu, nbv, ndrop, nsel, uradius, vradius, f2. */
+int orc_grduruwt(const float *u, const float *v, const float *w, const float *wt_in, int nvis, float idelt_u,
+                 float idelt_v, float wtfov, int rmode, float robust, float ds, const double *shift, int nbu,
+                 int nbv, float *newwt, double *stats) {
+    const float pi = 3.1415927f, bineps = 0.1f;
+    if (rmode < 1 || rmode > 3) return -4;
+    float *wt = (float *)malloc(sizeof(float) * (nvis > 0 ? nvis : 1));
+    memcpy(wt, wt_in, sizeof(float) * (size_t)nvis);
+    const float urad = fabsf(idelt_u / (wtfov * sqrtf(pi))), vrad = fabsf(idelt_v / (wtfov * sqrtf(pi)));
+    const int doshift = shift[0] != 1.0 || shift[4] != 1.0 || shift[8] != 1.0;
+#define ORC_LOCAL(k, U0, V0)                                                          \
+    do {                                                                              \
+        if (doshift) {                                                                \
+            U0 = (float)(shift[0] * u[k] + shift[1] * v[k] + shift[2] * w[k]);        \
+            V0 = (float)(shift[3] * u[k] + shift[4] * v[k] + shift[5] * w[k]);        \
+        } else {                                                                      \
+            U0 = u[k];                                                                \
+            V0 = v[k];                                                                \
+        }                                                                             \
+    } while (0)
+    float umax = -1.0f, vmax = -1.0f;
+    for (int k = 0; k < nvis; k++) {
+        if (wt[k] <= 0.0f) continue;
+        float u0, v0;
+        ORC_LOCAL(k, u0, v0);
+        if (fabsf(u0) > umax) umax = fabsf(u0);
+        if (fabsf(v0) > vmax) vmax = fabsf(v0);
+    }
+    if (nbu <= 0) { /* grd/grdeusz0.f:58-64 */
+        int nun = orc_utllint(7.6f + bineps), nup = orc_utllint(7.6f * umax / urad + bineps);
+        int nvb = 2 * orc_utllint(7.6f * vmax / vrad + bineps);
+        nbu = nun + nup < 1000 ? nun + nup : 1000;
+        nbv = nvb < 2000 ? nvb : 2000;
+    }
+    if (nbv <= 0) nbv = 2 * nbu;
+    if (nbu < 2 || nbv < 2) {
+        free(wt);
+        return -2;
+    }
+    int uorigin;
+    float du = 0.0f;
+    for (uorigin = 1; uorigin <= nbu - 1; uorigin++) {
+        du = umax / ((float)(nbu - uorigin) - bineps);
+        if (((float)uorigin - bineps) * du > urad) break;
+    }
+    if (uorigin > nbu - 1) uorigin = nbu - 1;
+    if (urad / du + bineps > (float)uorigin && (nbu - uorigin) > uorigin) {
+        free(wt);
+        return -3;
+    }
+    const int vorigin = nbv / 2;
+    const float dv = vmax / ((float)vorigin - bineps), uscale = 1.0f / du, vscale = 1.0f / dv;
+    const float ur2 = urad * urad, vr2 = vrad * vrad;
+    int *head = (int *)calloc((size_t)nbu * nbv, sizeof(int));
+    int *links = (int *)calloc((size_t)(nvis > 0 ? nvis : 1), sizeof(int));
+    float *bsum = (float *)calloc((size_t)(nvis > 0 ? nvis : 1), sizeof(float));
+    long long ndrop = 0;
+#define HEAD(i, j) head[((size_t)(j) - 1) * nbu + ((i) - 1)]
+    for (int k = 0; k < nvis; k++) {
+        newwt[k] = wt[k];
+        if (wt[k] <= 0.0f) continue;
+        float u0, v0;
+        ORC_LOCAL(k, u0, v0);
+        float uc = uscale * u0, vc = vscale * v0;
+        if (uc < 0.0f) {
+            uc = -uc;
+            vc = -vc;
+        }
+        int ub = orc_utlgint(uc) + uorigin + 1, vb = orc_utlgint(vc) + vorigin + 1;
+        int ub1 = orc_utlgint(-uc) + uorigin + 1, vb1 = orc_utlgint(-vc) + vorigin + 1;
+        if (ub < 1 || ub > nbu || vb < 1 || vb > nbv) {
+            ndrop++;
+            wt[k] = -1.0f;
+        } else {
+            int l = HEAD(ub, vb);
+            HEAD(ub, vb) = k + 1;
+            links[k] = l;
+            if (ub1 >= 1 && ub1 <= nbu && vb1 >= 1 && vb1 <= nbv) HEAD(ub1, vb1) = k + 1;
+            bsum[k] = l == 0 ? wt[k] : wt[k] + bsum[l - 1];
+        }
+    }
+#define ELL(a, b) ((a) * (a) / ur2 + (b) * (b) / vr2)
+    double sumloc = 0.0;
+    long long nsel = 0;
+    int rc = 0;
+    for (int k = 0; k < nvis && rc == 0; k++) {
+        if (wt[k] <= 0.0f) continue;
+        float u0, v0;
+        ORC_LOCAL(k, u0, v0);
+        if (u0 < 0.0f) {
+            u0 = -u0;
+            v0 = -v0;
+        }
+        int ub = orc_utlgint((u0 - urad) * uscale) + uorigin + 1, ub1 = orc_utlgint((u0 + urad) * uscale) + uorigin + 1;
+        int vb = orc_utlgint((v0 - vrad) * vscale) + vorigin + 1, vb1 = orc_utlgint((v0 + vrad) * vscale) + vorigin + 1;
+        ub = ub < 1 ? 1 : (ub > nbu ? nbu : ub);
+        ub1 = ub1 < 1 ? 1 : (ub1 > nbu ? nbu : ub1);
+        vb = vb < 1 ? 1 : (vb > nbv ? nbv : vb);
+        vb1 = vb1 < 1 ? 1 : (vb1 > nbv ? nbv : vb1);
+        float wtsum = 0.0f;
+        for (int j = vb; j <= vb1; j++)
+            for (int i = ub; i <= ub1; i++) {
+                if (HEAD(i, j) == 0) continue;
+                const float UB = (float)(i - uorigin - 1) * du, VB = (float)(j - vorigin) * dv;
+                int take = 0;
+                if (UB + du < u0) {
+                    if (VB - dv > v0) {
+                        if (ELL(UB - u0, VB - v0) <= 1.0f) take = 1;
+                        else if (ELL(UB + du - u0, VB - dv - v0) >= 1.0f) take = -1;
+                    } else if (VB < v0) {
+                        if (ELL(UB - u0, VB - dv - v0) <= 1.0f) take = 1;
+                        else if (ELL(UB + du - u0, VB - v0) >= 1.0f) take = -1;
+                    } else if (ELL(UB - u0, VB - v0) <= 1.0f && ELL(UB - u0, VB - dv - v0) <= 1.0f) {
+                        take = 1;
+                    }
+                } else if (UB > u0) {
+                    if (VB - dv > v0) {
+                        if (ELL(UB + du - u0, VB - v0) <= 1.0f) take = 1;
+                        else if (ELL(UB - u0, VB - dv - v0) >= 1.0f) take = -1;
+                    } else if (VB < v0) {
+                        if (ELL(UB + du - u0, VB - dv - v0) <= 1.0f) take = 1;
+                        else if (ELL(UB - u0, VB - v0) >= 1.0f) take = -1;
+                    } else if (ELL(UB + du - u0, VB - v0) <= 1.0f && ELL(UB + du - u0, VB - dv - v0) <= 1.0f) {
+                        take = 1;
+                    }
+                } else {
+                    if (VB - dv > v0) {
+                        if (ELL(UB - u0, VB - v0) <= 1.0f && ELL(UB + du - u0, VB - v0) <= 1.0f) take = 1;
+                    } else if (VB < v0) {
+                        if (ELL(UB - u0, VB - dv - v0) <= 1.0f && ELL(UB + du - u0, VB - dv - v0) <= 1.0f) take = 1;
+                    } else if (ELL(UB - u0, VB - v0) <= 1.0f && ELL(UB + du - u0, VB - v0) <= 1.0f &&
+                               ELL(UB + du - u0, VB - dv - v0) <= 1.0f && ELL(UB - u0, VB - dv - v0) <= 1.0f) {
+                        take = 1;
+                    }
+                }
+                if (take < 0) continue;
+                if (take > 0) {
+                    wtsum = wtsum + bsum[HEAD(i, j) - 1];
+                    continue;
+                }
+                const int posbin = i > uorigin;
+                for (int l = HEAD(i, j); l != 0; l = links[l - 1]) {
+                    float ut, vt;
+                    ORC_LOCAL(l - 1, ut, vt);
+                    if (posbin ? ut < 0.0f : ut > 0.0f) {
+                        ut = -ut;
+                        vt = -vt;
+                    }
+                    if (ELL(ut - u0, vt - v0) < 1.0f) wtsum = wtsum + wt[l - 1];
+                }
+            }
+        if (wtsum == 0.0f) {
+            rc = -1;
+            break;
+        }
+        newwt[k] = wtsum;
+        sumloc += wtsum;
+        nsel++;
+    }
+#undef ELL
+#undef HEAD
+#undef ORC_LOCAL
+    float f2 = 1.0f, d2 = 0.0f;
+    if (rc == 0) {
+        if (rmode == 1) {
+            const float t = 5.0f * powf(10.0f, -robust);
+            f2 = (float)((double)(t * t) / (sumloc / (double)nsel));
+            d2 = 1.0f;
+        } else if (rmode == 2) {
+            f2 = robust * robust;
+            d2 = 2.0f * (ds * ds);
+        }
+        for (int k = 0; k < nvis; k++)
+            if (wt[k] > 0.0f) newwt[k] = wt[k] / (newwt[k] * f2 + d2);
+    }
+    if (stats) {
+        stats[0] = nbu;
+        stats[1] = nbv;
+        stats[2] = (double)ndrop;
+        stats[3] = (double)nsel;
+        stats[4] = urad;
+        stats[5] = vrad;
+        stats[6] = f2;
+    }
+    free(wt);
+    free(head);
+    free(links);
+    free(bsum);
+    return rc;
+}

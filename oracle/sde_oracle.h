@@ -141,6 +141,12 @@ int  orc64_visdft2d(const float *vis, int nvis, const float *wt, const float *u,
 void orc64_imgdft2d(const float *image, int nx, int ny, double refx, double deltx, double refy,
                     double delty, double *vis, int nvis, const float *wt, const float *u, const float *v);
 
+/* GRDURUWT + GRDURUW2 (grd/grduruwt.f, grd/grduruw2.f): ungridded robust weighting.
+ * rmode 1 NORM, 2 ABS, 3 NONE; stats (7 doubles): nbu, nbv, ndrop, nsel, uradius, vradius, f2. */
+int orc_grduruwt(const float *u, const float *v, const float *w, const float *wt_in, int nvis, float idelt_u,
+                 float idelt_v, float wtfov, int rmode, float robust, float ds, const double *shift, int nbu,
+                 int nbv, float *newwt, double *stats);
+
 /* GRDH23D / GRDDEH23 (grd/grdh23d.f, grd/grddeh23.f): slow-Z gridding and degridding,
  * gvis [nz][nv][nu] complex, tables of 2*(supp+1)*osamp+1 floats. */
 int orc_grdh23d(const float *vis, const float *wt, const float *u, const float *v, const float *w, int nvis,

@@ -81,6 +81,13 @@ class ClarkResult(C.Structure):
                 ("t_maxres", C.c_float * 64), ("t_tflux", C.c_float * 64)]
 
 
+class UruwtStats(C.Structure):
+    """sde_uruwt_stats of include/sde_gpu.h."""
+    _fields_ = [("nbu", C.c_int), ("nbv", C.c_int), ("ndrop", C.c_int64), ("nsel", C.c_int64),
+                ("uradius", C.c_float), ("vradius", C.c_float), ("f2", C.c_float), ("d2", C.c_float),
+                ("sumlocwt", C.c_double)]
+
+
 class UvfitsDesc(C.Structure):
     """sde_uvfits_desc of include/sde_gpu.h."""
     _fields_ = [("ngroups", C.c_int64), ("ngroups_in_file", C.c_int64), ("npar", C.c_int),
@@ -141,6 +148,8 @@ SIGNATURES = [
     ("sde_batch_graph_nodes", I, [P]),
     ("sde_batch_image", I, [P, I, I, C.POINTER(P)]),
     ("sde_batch_read", I, [P, I, I, P, I64]),
+    ("sde_weights_ungridded", I, [P, I64, P, P, P, P, F, F, F, I, P, F, P, I, I, P,
+                                  C.POINTER(UruwtStats)]),
     ("sde_grid_box", I, [P, I64, P, P, P, P, P, F, F, F, F, I, I, I, I, I, P, P, I, C.POINTER(F)]),
     ("sde_model_image", I, [P, I, C.c_char_p, P, P, P, P, P, P, I, I, F, F, F, F, P]),
     ("sde_dft_image", I, [P, I64, P, P, P, P, I, I, C.c_double, C.c_double, C.c_double,

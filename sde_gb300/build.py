@@ -15,9 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libsdegpu.so")
-SOURCES = ["api.cu", "sort.cu", "weights.cu", "plan.cu", "grid.cu", "fft.cu", "clean.cu", "batch.cu", "jobs.cu", "uvfits.cu", "clark.cu", "dft.cu", "model.cu", "box.cu", "slowz.cu"]
+SOURCES = ["api.cu", "sort.cu", "weights.cu", "plan.cu", "grid.cu", "fft.cu", "clean.cu", "batch.cu", "jobs.cu", "uvfits.cu", "clark.cu", "dft.cu", "model.cu", "box.cu", "slowz.cu", "uruwt.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]
 
 

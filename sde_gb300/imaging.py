@@ -361,6 +361,25 @@ def hogbom(ctx, geom, dirty, psf, niter, gain=0.1, flux=0.0):
     return ctx.hogbom(drt, psf, niter, gain, flux)
 
 
+def weights_ungridded(ctx, geom, u, v, w, wt, rmode="NORM", robust=0.0, ds=0.0, wtfov=1.0, nbu=0, nbv=0):
+    """uvmap's slow weighting (GRDURUWT with GRDURUW2, sde_weights_ungridded) on host arrays:
+    the weighting plane's cell (IDELT) is the gridding plane's 1/uscale, 1/vscale.  Returns
+    (newwt, stats dict)."""
+    n = len(wt)
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    u, v, w, wt = f32(u), f32(v), f32(w), f32(wt)
+    newwt = np.empty(n, np.float32)
+    st = _abi.UruwtStats()
+    rob = (C.c_float * 3)(float(robust), 0.0, 0.0)
+    shift = np.ascontiguousarray(geom.shift, np.float64)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(lib().sde_weights_ungridded(ctx.h, n, p(u), p(v), p(w), p(wt), float(1.0 / geom.uscale),
+                                      float(1.0 / geom.vscale), float(wtfov),
+                                      {"NORM": 1, "ABS": 2, "NONE": 3}[rmode], rob, float(ds), p(shift),
+                                      int(nbu), int(nbv), p(newwt), C.byref(st)), "sde_weights_ungridded")
+    return newwt, {k: getattr(st, k) for k, _ in st._fields_}
+
+
 def model_image(ctx, comps, nx, ny, refx, deltx, refy, delty, image=None):
     """MODIMG2D (sde_model_image): comps = [(type, flux, ra, dec, bmaj, bmin, bpa), ...] with
     offsets/axes in arcsec and the position angle in degrees, added into image (a zeroed
