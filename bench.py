@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="single workload: skip the compact mosaic/serve summaries")
     ap.add_argument("--nchan", type=int, default=NCHAN, help="channels (64 = full workload)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--clean-iters", type=int, default=200)
     ap.add_argument("--plan-opts", default=None,

@@ -691,6 +691,9 @@ struct Upload2D {  // an extra host -> device 2-D copy issued behind the inputs
     size_t spitch, width, rows;
 };
 
+static int shim_plan_build(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const float *in, const float *dvis,
+                           const float *cf, uint64_t h, sde_plan **out);
+
 static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const float *u,
                      const float *v, const float *w, const float *vis, const float *wt,
                      const float *cf, sde_plan **out, const Upload2D *extra = nullptr) {
@@ -742,8 +745,17 @@ static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const floa
             return SDE_OK;
         }
     }
-    shim_cache_drop();
     if (!vis && n > 0) SDE_CUDA_TRY(cudaMemsetAsync(dvis, 0, 2 * nb, st));
+    return shim_plan_build(ctx, sp, n, in, dvis, cf, h, out);
+}
+
+// A new plan from the device copies of U, V, W, WT (in, 4n floats) and VIS, kept in the cache
+// with its inputs.
+static int shim_plan_build(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const float *in, const float *dvis,
+                           const float *cf, uint64_t h, sde_plan **out) {
+    cudaStream_t st = ctx->stream;
+    const size_t nb = sizeof(float) * (size_t)(n > 0 ? n : 1);
+    shim_cache_drop();
     sde_plan *pl = nullptr;
     SDE_TRY(sde_plan_create(ctx, &sp, n, in, in + n, in + 2 * n, dvis, in + 3 * n, SDE_DEVICE, &pl));
     int rc = plan_use_table(pl, cf);
@@ -789,6 +801,71 @@ extern "C" int sde_shim_cache_clear(void) {
     return SDE_OK;
 }
 
+// GRDH2D against the cached plan while its inputs are still arriving: VIS goes up first and
+// the cached plan grids it, and the grid comes down, while U, V, W, WT are uploaded and
+// compared on the copy stream.  If one of them changed, the plan is rebuilt and the grid
+// made and returned again (GVIS and SUMWT are outputs only).  *done = 0: no cached plan.
+static int shim_grid_speculative(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const float *vis, const float *wt,
+                                 const float *u, const float *v, const float *w, const float *cf, int psf,
+                                 float *gvis, int nu, int nv, float *sumwt, int *done) {
+    *done = 0;
+    const uint64_t h = hash_floats(cf, 2 * (SUPP + 1) * OSAMP + 1);
+    if (!(g_pc.pl && n > 0 && g_pc.nvis == n && g_pc.cf_hash == h && memcmp(&g_pc.spec, &sp, sizeof sp) == 0))
+        return SDE_OK;
+    cudaStream_t st = ctx->stream;
+    SDE_TRY(shim_streams());
+    cudaStream_t cs = g_ss.copy;
+    const size_t nb = sizeof(float) * (size_t)n;
+    float *in = nullptr, *dvis = nullptr;
+    float2 *dg = nullptr;
+    int *flag = nullptr;
+    const int pitch = sde_grid_pitch(nu);
+    SDE_TRY(ctx_scratch(ctx, "shim_in", 4 * nb, (void **)&in));
+    SDE_TRY(ctx_scratch(ctx, "shim_vis", 2 * nb, (void **)&dvis));
+    SDE_TRY(ctx_scratch(ctx, "shim_flag", sizeof(int), (void **)&flag));
+    SDE_TRY(ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * nv, (void **)&dg));
+    SDE_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    SDE_CUDA_TRY(cudaMemcpyAsync(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
+    SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[0], st));
+    SDE_CUDA_TRY(cudaStreamWaitEvent(cs, g_ss.ev[0], 0));
+    // the grid of the cached plan and its way back on the main stream ...
+    sde_plan *pl = g_pc.pl;
+    if (!psf) SDE_TRY(sde_plan_set_vis(pl, dvis, SDE_DEVICE));
+    float sw = 0.0f;
+    int rc = sde_plan_grid(pl, psf ? SDE_GRID_PSF : SDE_GRID_VIS, (float *)dg, pitch, &sw);
+    if (rc != SDE_OK && rc != SDE_ENOWEIGHT) return rc;
+    SDE_CUDA_TRY(cudaMemcpy2DAsync(gvis, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, (size_t)nv,
+                                   cudaMemcpyDeviceToHost, st));
+    // ... while U, V, W, WT go up and are compared on the copy stream
+    const float *src[4] = {u, v, w, wt};
+    for (int k = 0; k < 4; k++) {
+        SDE_CUDA_TRY(cudaMemcpyAsync(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
+        k_words_differ<<<ctx->num_sms * 4, 256, 0, cs>>>(reinterpret_cast<const uint32_t *>(in + k * n),
+                                                        reinterpret_cast<const uint32_t *>(g_pc.inputs + k * n), n,
+                                                        flag);
+        SDE_CHECK_LAUNCH();
+    }
+    int hf = 1;
+    SDE_CUDA_TRY(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, cs));
+    SDE_CUDA_TRY(cudaStreamSynchronize(cs));
+    SDE_CUDA_TRY(cudaStreamSynchronize(st));
+    *done = 1;
+    if (!hf) {
+        g_pc.hits++;
+        *sumwt = sw;
+        return rc;
+    }
+    // an input changed: a new plan from the arrived inputs, the grid again
+    SDE_TRY(shim_plan_build(ctx, sp, n, in, dvis, cf, h, &pl));
+    rc = sde_plan_grid(pl, psf ? SDE_GRID_PSF : SDE_GRID_VIS, (float *)dg, pitch, &sw);
+    if (rc != SDE_OK && rc != SDE_ENOWEIGHT) return rc;
+    SDE_CUDA_TRY(cudaMemcpy2DAsync(gvis, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, (size_t)nv,
+                                   cudaMemcpyDeviceToHost, st));
+    SDE_CUDA_TRY(cudaStreamSynchronize(st));
+    *sumwt = sw;
+    return rc;
+}
+
 extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis,
                         float *uscale, float *uoffset, float *vscale, float *voffset, int *uorigin,
                         int *vorigin, float *gvis, int *psf, int *nu, int *nv, float *gridfnu,
@@ -805,6 +882,17 @@ extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int
     }
     sde_gridspec sp;
     fill_spec(&sp, *nu, *nv, *uscale, *uoffset, *vscale, *voffset, *uorigin, *vorigin, shift);
+    int done = 0;
+    float ssw = 0.0f;
+    int rs = shim_grid_speculative(ctx, sp, *nvis, vis, wt, u, v, w, gridfnu, *psf, gvis, *nu, *nv, &ssw, &done);
+    if (done || rs != SDE_OK) {
+        if (rs == SDE_OK || rs == SDE_ENOWEIGHT) *sumwt = ssw;
+        if (rs == SDE_ENOWEIGHT)
+            report("Bad argument", R, "No weight!");
+        else if (rs != SDE_OK)
+            report_rc(rs, R);
+        return;
+    }
     sde_plan *pl = nullptr;
     int rc = shim_plan(ctx, sp, *nvis, u, v, w, vis, wt, gridfnu, &pl);
     float2 *dg = nullptr;
@@ -992,6 +1080,88 @@ extern "C" void grdqh2d_(float *vis, float *wt, float *u, float *v, float *w, in
         report_rc(rc, R);
 }
 
+// GRDDEH2D against the cached plan while its inputs are still arriving.  WT goes up first and
+// is compared with the cached plan's: when it matches and that plan has no points with
+// WT <= 0 (whose VIS the caller keeps), every VIS is written whatever U, V, W turn out to be,
+// so the model grid goes up next, the degrid runs and VIS comes down while U, V, W are
+// uploaded and compared on the copy stream (the two directions of the link at once).  If U,
+// V or W changed, the plan is rebuilt and VIS written again.  *done = 0: not attempted
+// (no cached plan, WT changed, or flagged points): the caller takes the ordinary path.
+static int shim_degrid_speculative(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const float *u, const float *v,
+                                   const float *w, float *wt, const float *cf, const float *gvis, int nu, int nv,
+                                   float *vis, int64_t *nbad, int *done) {
+    *done = 0;
+    const uint64_t h = hash_floats(cf, 2 * (SUPP + 1) * OSAMP + 1);
+    if (!(g_pc.pl && n > 0 && g_pc.nvis == n && g_pc.cf_hash == h && memcmp(&g_pc.spec, &sp, sizeof sp) == 0 &&
+          g_pc.pl->nuntouched == 0))
+        return SDE_OK;
+    cudaStream_t st = ctx->stream;
+    SDE_TRY(shim_streams());
+    cudaStream_t cs = g_ss.copy;
+    const size_t nb = sizeof(float) * (size_t)n;
+    float *in = nullptr, *dvis = nullptr, *dw = nullptr;
+    float2 *dv = nullptr, *dg = nullptr;
+    int *flag = nullptr;
+    unsigned long long *cnt = nullptr;
+    const int pitch = sde_grid_pitch(nu);
+    SDE_TRY(ctx_scratch(ctx, "shim_in", 4 * nb, (void **)&in));
+    SDE_TRY(ctx_scratch(ctx, "shim_flag2", 2 * sizeof(int), (void **)&flag));
+    SDE_TRY(ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * nv, (void **)&dg));
+    SDE_TRY(ctx_scratch(ctx, "dg_vis", 2 * nb, (void **)&dv));
+    SDE_TRY(ctx_scratch(ctx, "dg_wt", nb, (void **)&dw));
+    SDE_TRY(ctx_scratch(ctx, "dg_nbad", 16, (void **)&cnt));
+    SDE_CUDA_TRY(cudaMemsetAsync(flag, 0, 2 * sizeof(int), st));
+    SDE_CUDA_TRY(cudaMemsetAsync(cnt, 0, 16, st));
+    SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[0], st));
+    SDE_CUDA_TRY(cudaStreamWaitEvent(cs, g_ss.ev[0], 0));
+    // WT first, compared on the copy stream
+    SDE_CUDA_TRY(cudaMemcpyAsync(in + 3 * n, wt, nb, cudaMemcpyHostToDevice, cs));
+    k_words_differ<<<ctx->num_sms * 4, 256, 0, cs>>>(reinterpret_cast<const uint32_t *>(in + 3 * n),
+                                                    reinterpret_cast<const uint32_t *>(g_pc.inputs + 3 * n), n,
+                                                    flag);
+    SDE_CHECK_LAUNCH();
+    int fw = 1;
+    SDE_CUDA_TRY(cudaMemcpyAsync(&fw, flag, sizeof(int), cudaMemcpyDeviceToHost, cs));
+    SDE_CUDA_TRY(cudaStreamSynchronize(cs));
+    if (fw) return SDE_OK;  // WT changed: the ordinary path
+    // the model grid, the degrid with the cached plan and VIS down on the main stream ...
+    SDE_CUDA_TRY(cudaMemcpy2DAsync(dg, (size_t)pitch * 8, gvis, (size_t)nu * 8, (size_t)nu * 8, (size_t)nv,
+                                   cudaMemcpyHostToDevice, st));
+    SDE_TRY(plan_degrid(g_pc.pl, (const float *)dg, pitch, 1, dv, dw, cnt));
+    SDE_CUDA_TRY(cudaMemcpyAsync(vis, dv, 2 * nb, cudaMemcpyDeviceToHost, st));
+    // ... while U, V, W go up and are compared on the copy stream
+    const float *src[3] = {u, v, w};
+    for (int k = 0; k < 3; k++) {
+        SDE_CUDA_TRY(cudaMemcpyAsync(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
+        k_words_differ<<<ctx->num_sms * 4, 256, 0, cs>>>(reinterpret_cast<const uint32_t *>(in + k * n),
+                                                        reinterpret_cast<const uint32_t *>(g_pc.inputs + k * n), n,
+                                                        flag + 1);
+        SDE_CHECK_LAUNCH();
+    }
+    int fuvw = 1;
+    SDE_CUDA_TRY(cudaMemcpyAsync(&fuvw, flag + 1, sizeof(int), cudaMemcpyDeviceToHost, cs));
+    unsigned long long hc[2] = {0, 0};
+    SDE_CUDA_TRY(cudaMemcpyAsync(hc, cnt, 16, cudaMemcpyDeviceToHost, st));
+    SDE_CUDA_TRY(cudaStreamSynchronize(cs));
+    SDE_CUDA_TRY(cudaStreamSynchronize(st));
+    *done = 1;
+    if (!fuvw) {
+        g_pc.hits++;
+        *nbad = (int64_t)hc[0];
+        if (hc[1] > 0) {  // points not degridded: WT negated
+            SDE_CUDA_TRY(cudaMemcpyAsync(wt, dw, nb, cudaMemcpyDeviceToHost, st));
+            SDE_CUDA_TRY(cudaStreamSynchronize(st));
+        }
+        return SDE_OK;
+    }
+    // U, V or W changed: a new plan from the arrived inputs, then the ordinary degrid
+    SDE_TRY(ctx_scratch(ctx, "shim_vis", 2 * nb, (void **)&dvis));
+    SDE_CUDA_TRY(cudaMemsetAsync(dvis, 0, 2 * nb, st));
+    sde_plan *pl = nullptr;
+    SDE_TRY(shim_plan_build(ctx, sp, n, in, dvis, cf, h, &pl));
+    return sde_plan_degrid(pl, (const float *)dg, pitch, vis, wt, SDE_HOST, nbad);
+}
+
 extern "C" void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis,
                           float *uscale, float *uoffset, float *vscale, float *voffset,
                           int *uorigin, int *vorigin, float *gvis, int *nu, int *nv, float *intfnu,
@@ -1011,12 +1181,16 @@ extern "C" void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, i
     sde_plan *pl = nullptr;
     float2 *dg = nullptr;
     const int pitch = sde_grid_pitch(*nu);
-    int rc = ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * *nv, (void **)&dg);
-    // the model grid goes up behind U, V, W, WT, while they are compared with the cached plan's
-    const Upload2D gup{dg, (size_t)pitch * 8, gvis, (size_t)*nu * 8, (size_t)*nu * 8, (size_t)*nv};
-    if (rc == SDE_OK) rc = shim_plan(ctx, sp, *nvis, u, v, w, nullptr, wt, intfnu, &pl, &gup);
     int64_t nbad = 0;
-    if (rc == SDE_OK) rc = sde_plan_degrid(pl, (const float *)dg, pitch, vis, wt, SDE_HOST, &nbad);
+    int done = 0;
+    int rc = shim_degrid_speculative(ctx, sp, *nvis, u, v, w, wt, intfnu, gvis, *nu, *nv, vis, &nbad, &done);
+    if (rc == SDE_OK && !done) {
+        rc = ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * *nv, (void **)&dg);
+        // the model grid goes up behind U, V, W, WT, while they are compared with the cached plan's
+        const Upload2D gup{dg, (size_t)pitch * 8, gvis, (size_t)*nu * 8, (size_t)*nu * 8, (size_t)*nv};
+        if (rc == SDE_OK) rc = shim_plan(ctx, sp, *nvis, u, v, w, nullptr, wt, intfnu, &pl, &gup);
+        if (rc == SDE_OK) rc = sde_plan_degrid(pl, (const float *)dg, pitch, vis, wt, SDE_HOST, &nbad);
+    }
     if (rc != SDE_OK) {
         report_rc(rc, R);
         return;

@@ -253,3 +253,58 @@ def test_pix2drcl_and_pixisama_identical(L, orc):
     assert np.array_equal(res, r["res"]) and np.array_equal(cln, r["cln"])
     a = rng.normal(size=1000).astype(np.float32)
     assert L.pixisama_(I(a.size), _p(a), I(1)) == orc.pixisama(a)
+
+
+def test_grddeh2d_speculation(L, orc):
+    """A cached plan with no flagged points lets GRDDEH2D degrid and return VIS while U, V, W
+    are still arriving (WT compared first).  The results must equal the oracle's when the
+    plan still holds (including points outside the grid, whose WT comes back negated) and
+    when U changed under an unchanged WT (the plan is rebuilt and VIS written again)."""
+    from sde_gb300 import _abi
+    from sde_gb300.imaging import Geom
+    g = Geom(64, 8.0, vdec=40.0)
+    rng = np.random.default_rng(21)
+    n = 3000
+    ucell = rng.uniform(-30.0, 30.0, n)
+    vcell = rng.uniform(-27.0, 27.0, n)
+    vcell[:25] = rng.uniform(29.6, 31.0, 25) * np.sign(rng.uniform(-1, 1, 25))  # outside
+    u = (ucell / g.uscale).astype(np.float32)
+    v = (vcell / g.vscale).astype(np.float32)
+    w = rng.uniform(-50, 50, n).astype(np.float32)
+    wt0 = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    gvis = (rng.normal(size=(g.nv, g.nu)) + 1j * rng.normal(size=(g.nv, g.nu))).astype(np.complex64)
+    cf, _, _ = orc.grdcf()
+    shift = np.ascontiguousarray(list(g.shift), np.float64)
+
+    def call(uu):
+        vis = np.full(n, np.complex64(5 - 5j))
+        wt = wt0.copy()
+        L.grddeh2d_(_p(vis), _p(wt), _p(uu), _p(v), _p(w), I(n), F(g.uscale), F(0), F(g.vscale), F(0),
+                    I(g.uorigin), I(g.vorigin), _p(gvis), I(g.nu), I(g.nv), _p(cf), I(3), I(128), _p(cf),
+                    I(3), I(128), _p(shift))
+        assert _abi.sysi().error == 0
+        return vis, wt
+
+    def check(uu, vis, wt):
+        rvis, rwt, _ = orc.grddeh2d(np.zeros(n, np.complex64), wt0, uu, v, w, g.uscale, g.vscale, g.uorigin,
+                                    g.vorigin, gvis, shift, cf=cf)
+        assert np.array_equal(wt.view(np.uint32), rwt.view(np.uint32))
+        assert np.abs(vis - rvis).max() / np.abs(rvis[rwt > 0]).max() < 1e-5
+        return rwt
+
+    h0, m0 = _stats(L)
+    for _ in range(3):  # the first call builds the plan; then two speculative hits
+        vis, wt = call(u)
+        rwt = check(u, vis, wt)
+    assert (rwt < 0).sum() >= 20  # points outside: WT negated on the speculative path too
+    h1, m1 = _stats(L)
+    assert h1 - h0 == 2 and m1 - m0 == 1
+    u2 = u.copy()
+    u2[100] = np.float32(u2[100] * 0.5)  # U changes, WT does not: speculate, then rebuild
+    vis, wt = call(u2)
+    check(u2, vis, wt)
+    h2, m2 = _stats(L)
+    assert m2 - m1 == 1
+    vis, wt = call(u2)  # and the rebuilt plan is reused
+    check(u2, vis, wt)
+    assert _stats(L)[0] - h2 == 1
