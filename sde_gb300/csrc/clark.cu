@@ -5,20 +5,26 @@
 //   |residual| histogram of 1024 bins (PIXRABSH)               k_clark_hist
 //   the list limit (PIXFLIM, ARRFLIM, EXTSIDE)                 k_clark_limit
 //   the list of pixels above it, in storage order (PIX2DRLI)   k_clark_count / _scan / _emit
-//   the minor cycle on the list (PIX2DRCC)                     k_clark_minor: one CTA
+//   the minor cycle on the list (PIX2DRCC)                     k_clark_minor: one cluster
 //   the components into the model image (PIX2DRMA)             k_clark_addcomp
 //   residual = dirty - IFFT(FFT(model) * XFR) (IMGRESID)       FFTR2D passes + k_clark_cmul/_sub
 // The host reads back the cycle's scalars once per major cycle for IMGCCLEA's stop test.
 #include <string.h>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
 constexpr int CL_NB = 1024;        // histogram bins (arr/arrabshi.f:34 NB = 1024)
-constexpr int CL_T = 1024;         // minor-cycle threads (one CTA)
-constexpr int CL_PER = 32;         // list entries per thread held in registers
-constexpr int CL_MAXNL = CL_T * CL_PER;
+constexpr int CL_T = 1024;         // minor-cycle threads per CTA
+constexpr int CL_CTAS = 8;         // minor-cycle CTAs: one thread-block cluster
+constexpr int CL_PER = 4;          // list entries per thread held in registers
+constexpr int CL_SLICE = CL_T * CL_PER;           // entries per CTA
+constexpr int CL_MAXNL = CL_CTAS * CL_SLICE;      // 32768
 constexpr int CL_CHUNK = 4096;     // pixels per block of the list compaction (256 x 16)
 
 struct ClarkState {
@@ -245,30 +251,55 @@ __device__ __forceinline__ unsigned long long isama_key(float v, int i) {
     return ((unsigned long long)__float_as_uint(fabsf(v)) << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)i);
 }
 
-// pix/pix2drcc.f:66-140 with SPEED = 1 and GSUB = BSUB: one CTA.  Thread t holds list
-// entries t*CL_PER .. t*CL_PER+31 (consecutive in storage order, so spatially compact) in
-// registers, their positions in shared memory (entry (t, j) at spos[j*CL_T + t]: no bank
-// conflicts), and their bounding box: an iteration whose beam patch misses the box leaves
-// the thread's entries alone, and a thread rescans its local maximum only after one of its
-// entries changed.  One barrier per iteration: warp maxima go to one of two slot sets
-// (alternating), and every warp reduces the 32 slots itself.
+// pix/pix2drcc.f:66-140 with SPEED = 1 and GSUB = BSUB on a cluster of CL_CTAS CTAs.  CTA r
+// holds list entries r*CL_SLICE ..; its thread t holds CL_PER consecutive ones (storage order,
+// so spatially compact) in registers, their positions in shared memory (entry (t, j) at
+// spos[j*CL_T + t]), the beam patch in shared memory when it fits, and the bounding box of
+// its entries: an iteration whose beam patch misses the box leaves them alone, and a thread
+// rescans its local maximum only after one of its entries changed.  An iteration's argmax
+// (PIXISAMA: the largest |v|, then the first index): warp shuffles, one __syncthreads, the
+// CTA's best into its slot in CTA 0's shared memory, one cluster barrier, every warp reduces
+// the CL_CTAS slots.  Slots alternate between two sets, so no second barrier is needed.
+struct ClSlot {
+    unsigned long long key;
+    float val;
+    int pos;
+};
+
+__device__ __forceinline__ void slot_max(unsigned long long &k, float &v, int &p, int width) {
+    for (int d = width / 2; d > 0; d >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, d);
+        const float ov = __shfl_xor_sync(0xffffffffu, v, d);
+        const int op = __shfl_xor_sync(0xffffffffu, p, d);
+        if (ok > k) {
+            k = ok;
+            v = ov;
+            p = op;
+        }
+    }
+}
+
 template <bool PSF_SMEM>
-__global__ void __launch_bounds__(CL_T, 1)
+__global__ void __cluster_dims__(CL_CTAS, 1, 1) __launch_bounds__(CL_T, 1)
     k_clark_minor(const float *__restrict__ al, const int *__restrict__ pl, ClarkState *st,
                   const float *__restrict__ psf_g, int pw, int ph, float gain, int nsub, int bsub,
                   float flux, float *cl, int *cx, int *cy) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
     extern __shared__ __align__(16) unsigned char smem[];
     int *spos = reinterpret_cast<int *>(smem);
-    float *spsf = reinterpret_cast<float *>(smem + sizeof(int) * CL_MAXNL);
+    float *spsf = reinterpret_cast<float *>(smem + sizeof(int) * CL_SLICE);
     __shared__ unsigned long long skey[2][32];
     __shared__ float sval[2][32];
+    __shared__ int spo[2][32];
+    __shared__ ClSlot cslot[2][CL_CTAS];  // CTA 0's copy is the cluster's
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const int anl = st->anl;
+    const int anl = st->anl, base = rank * CL_SLICE;
     float v[CL_PER];
-    int bx0 = 0x7FFF, bx1 = -1, by0 = 0x7FFF, by1 = -1;  // bounding box of the thread's entries
+    int bx0 = 0x7FFF, bx1 = -1, by0 = 0x7FFF, by1 = -1;
 #pragma unroll
     for (int j = 0; j < CL_PER; j++) {
-        const int i = t * CL_PER + j;
+        const int i = base + t * CL_PER + j;
         const int q = i < anl ? pl[i] : (0x7FFF | (0x7FFF << 16));  // never inside the patch
         v[j] = i < anl ? al[i] : 0.f;
         spos[j * CL_T + t] = q;
@@ -285,61 +316,70 @@ __global__ void __launch_bounds__(CL_T, 1)
         for (int k = t; k < pw * ph; k += CL_T) spsf[k] = psf_g[k];
         psf = spsf;
     }
-    __syncthreads();
+    ClSlot *c0 = cluster.map_shared_rank(&cslot[0][0], 0);
+    cluster.sync();
     const float slim = st->slim;
     const int pmpx = st->pmpx, pmpy = st->pmpy;
     float tflux = st->tflux, smn = 0.f, maxres = 0.f;
     int ansub = nsub, buf = 0;
     unsigned long long lbest = 0ull;
     float lbv = 0.f;
+    int lpos = 0;
     bool rescan = true;
-    auto argmax = [&](float *val) -> int {
+    // the cluster's argmax: value into *val, packed position into *pos
+    auto argmax = [&](float *val, int *pos) {
         if (rescan) {
             lbest = 0ull;
             lbv = 0.f;
+            lpos = 0;
 #pragma unroll
             for (int j = 0; j < CL_PER; j++) {
-                const unsigned long long k = isama_key(v[j], t * CL_PER + j);
+                const unsigned long long k = isama_key(v[j], base + t * CL_PER + j);
                 if (k > lbest) {
                     lbest = k;
                     lbv = v[j];
+                    lpos = spos[j * CL_T + t];
                 }
             }
             rescan = false;
         }
-        unsigned long long best = lbest;
+        unsigned long long k = lbest;
         float bv = lbv;
-        for (int d = 16; d > 0; d >>= 1) {
-            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, best, d);
-            const float ov = __shfl_xor_sync(0xffffffffu, bv, d);
-            if (ok > best) {
-                best = ok;
-                bv = ov;
-            }
-        }
+        int bp = lpos;
+        slot_max(k, bv, bp, 32);
         if (lane == 0) {
-            skey[buf][warp] = best;
+            skey[buf][warp] = k;
             sval[buf][warp] = bv;
+            spo[buf][warp] = bp;
         }
         __syncthreads();
-        best = skey[buf][lane];
-        bv = sval[buf][lane];
-        for (int d = 16; d > 0; d >>= 1) {
-            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, best, d);
-            const float ov = __shfl_xor_sync(0xffffffffu, bv, d);
-            if (ok > best) {
-                best = ok;
-                bv = ov;
-            }
+        if (warp == 0) {
+            k = skey[buf][lane];
+            bv = sval[buf][lane];
+            bp = spo[buf][lane];
+            slot_max(k, bv, bp, 32);
+            if (lane == 0) c0[buf * CL_CTAS + rank] = ClSlot{k, bv, bp};
         }
+        cluster.sync();
+        if (lane < CL_CTAS) {
+            const ClSlot c = c0[buf * CL_CTAS + lane];
+            k = c.key;
+            bv = c.val;
+            bp = c.pos;
+        } else {
+            k = 0ull;
+            bv = 0.f;
+            bp = 0;
+        }
+        slot_max(k, bv, bp, 32);
         buf ^= 1;
         *val = bv;
-        return (int)(0xFFFFFFFFu - (unsigned)(best & 0xFFFFFFFFull));
+        *pos = bp;
     };
-    int isub;
+    int isub, pp = 0;
     for (isub = bsub; isub <= abs(nsub); isub++) {
         smn = __fadd_rn(smn, __fdiv_rn(1.0f, (float)isub));
-        const int ip = argmax(&maxres);
+        argmax(&maxres, &pp);
         if ((flux < 0.f && maxres < 0.f) || (nsub < 0 && maxres < 0.f) ||
             fabsf(maxres) <= fmaxf(__fmul_rn(slim, smn), fabsf(flux))) {
             ansub = isub - 1;
@@ -347,8 +387,8 @@ __global__ void __launch_bounds__(CL_T, 1)
         }
         const float pntsub = __fmul_rn(gain, maxres);
         tflux = __fadd_rn(tflux, pntsub);
-        const int pp = spos[(ip % CL_PER) * CL_T + ip / CL_PER], pmx = pp & 0xFFFF, pmy = pp >> 16;
-        if (t == 0) {
+        const int pmx = pp & 0xFFFF, pmy = pp >> 16;
+        if (rank == 0 && t == 0) {
             cl[isub - 1] = pntsub;
             cx[isub - 1] = pmx;
             cy[isub - 1] = pmy;
@@ -367,8 +407,9 @@ __global__ void __launch_bounds__(CL_T, 1)
             }
         }
     }
-    if (isub > abs(nsub)) argmax(&maxres);  // pix/pix2drcc.f:133-135
-    if (t == 0) {
+    if (isub > abs(nsub)) argmax(&maxres, &pp);  // pix/pix2drcc.f:133-135
+    cluster.sync();  // no CTA leaves while another may still read CTA 0's slots
+    if (rank == 0 && t == 0) {
         st->aniter = ansub;
         st->maxres = maxres;
         st->tflux = tflux;
@@ -515,7 +556,7 @@ extern "C" int sde_clark(sde_ctx *ctx, const float *dirty, const float *psf, int
     k_clark_patch<<<1, 1024, 0, st>>>(psf, n, b0, b1, spsf, pw, dst);
     SDE_CHECK_LAUNCH();
     // minor-cycle kernel: positions (+ beam patch when it fits) in shared memory
-    const size_t sm_pos = sizeof(int) * CL_MAXNL, sm_psf = sizeof(float) * (size_t)pw * pw;
+    const size_t sm_pos = sizeof(int) * CL_SLICE, sm_psf = sizeof(float) * (size_t)pw * pw;
     const bool psf_smem = sm_pos + sm_psf <= 200u * 1024u;
     const size_t sm = sm_pos + (psf_smem ? sm_psf : 0);
     if (psf_smem)
@@ -554,10 +595,10 @@ extern "C" int sde_clark(sde_ctx *ctx, const float *dirty, const float *psf, int
             // TFLUX carries over the cycles (img/imgcclea.f:251)
             SDE_CUDA_TRY(cudaMemcpyAsync(&d->tflux, &tflux, sizeof(float), cudaMemcpyHostToDevice, st));
             if (psf_smem)
-                k_clark_minor<true><<<1, CL_T, sm, st>>>(al, pl, dst, spsf, pw, pw, p->gain, p->niter, riter, p->flux,
+                k_clark_minor<true><<<CL_CTAS, CL_T, sm, st>>>(al, pl, dst, spsf, pw, pw, p->gain, p->niter, riter, p->flux,
                                                          lcl, lcx, lcy);
             else
-                k_clark_minor<false><<<1, CL_T, sm, st>>>(al, pl, dst, spsf, pw, pw, p->gain, p->niter, riter,
+                k_clark_minor<false><<<CL_CTAS, CL_T, sm, st>>>(al, pl, dst, spsf, pw, pw, p->gain, p->niter, riter,
                                                           p->flux, lcl, lcx, lcy);
             SDE_CHECK_LAUNCH();
             k_clark_addcomp<<<1, 1, 0, st>>>(lcl, lcx, lcy, riter, dst, comp, w, w);
