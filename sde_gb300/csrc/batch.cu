@@ -72,31 +72,68 @@ __global__ void k_mosaic_invden(float *den, int64_t n, const float *__restrict__
 }
 
 // The mosaic by gather: block = one MOS_TILE x MOS_TILE tile of the mosaic; every pixel sums
-// wt PB I over the tile's pointings (in pointing order) and takes the stored 1/den.
+// wt PB I over the tile's pointings (in pointing order) and takes the stored 1/den.  The
+// tile's pointing descriptors are staged in shared memory, and pointings are taken two at a
+// time with both images' loads issued before either is added (the sum keeps pointing order).
 constexpr int MOS_TILE = 64;
-__global__ void __launch_bounds__(256) k_mosaic_gather(const MosaicPointing *__restrict__ pts,
+constexpr int MOS_STAGE = 64;  // pointings of a tile staged in shared memory
+// mosaic pixel (tx, ty, k) in image p: the 0-based image pixel, false when outside the image
+__device__ __forceinline__ bool mos_pix(const MosaicPointing &p, int tx, int ty, int k, int *ix, int *iy) {
+    const int ox = p.cx - 1 - ((p.nx + 1) / 2 - 1), oy = p.cy - 1 - ((p.ny + 1) / 2 - 1);
+    *ix = tx * MOS_TILE + (k & (MOS_TILE - 1)) - ox;
+    *iy = ty * MOS_TILE + k / MOS_TILE - oy;
+    return *ix >= 0 && *ix < p.nx && *iy >= 0 && *iy < p.ny;
+}
+
+// the image values of the thread's pixels (0 outside the image); loads only, so that both
+// pointings' loads are in flight before any is used
+__device__ __forceinline__ void mos_load(const MosaicPointing &p, int tx, int ty, float *val) {
+    constexpr int PER = MOS_TILE * MOS_TILE / 256;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        int ix, iy;
+        val[j] = mos_pix(p, tx, ty, threadIdx.x + j * 256, &ix, &iy) ? p.image[(int64_t)iy * p.nx + ix] : 0.f;
+    }
+}
+
+// acc += wt PB I over the thread's pixels inside image p
+__device__ __forceinline__ void mos_add(const MosaicPointing &p, int tx, int ty, const float *val, float *acc) {
+    constexpr int PER = MOS_TILE * MOS_TILE / 256;
+    const int cenx = (p.nx + 1) / 2 - 1, ceny = (p.ny + 1) / 2 - 1;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        int ix, iy;
+        if (!mos_pix(p, tx, ty, threadIdx.x + j * 256, &ix, &iy)) continue;
+        const float dx = (float)(ix - cenx), dy = (float)(iy - ceny);
+        const float pb = expf(-p.pbk * (dx * dx + dy * dy));
+        acc[j] += p.wt * pb * val[j];
+    }
+}
+
+__global__ void __launch_bounds__(256, 3) k_mosaic_gather(const MosaicPointing *__restrict__ pts,
                                                        const int32_t *__restrict__ tstart,
                                                        const uint16_t *__restrict__ tpts, int mtx, int mnx,
                                                        int mny, const float *__restrict__ invden, float *out) {
+    __shared__ MosaicPointing sp[MOS_STAGE];
     const int tx = blockIdx.x % mtx, ty = blockIdx.x / mtx;
-    const int p0 = tstart[blockIdx.x], p1 = tstart[blockIdx.x + 1];
+    const int p0 = tstart[blockIdx.x], cnt = tstart[blockIdx.x + 1] - p0;
+    for (int i = threadIdx.x; i < cnt && i < MOS_STAGE; i += blockDim.x) sp[i] = pts[tpts[p0 + i]];
+    __syncthreads();
     constexpr int PER = MOS_TILE * MOS_TILE / 256;
     float acc[PER];
 #pragma unroll
     for (int j = 0; j < PER; j++) acc[j] = 0.f;
-    for (int pi = p0; pi < p1; pi++) {
-        const MosaicPointing p = pts[tpts[pi]];
-        const int cenx = (p.nx + 1) / 2 - 1, ceny = (p.ny + 1) / 2 - 1;
-        const int ox = p.cx - 1 - cenx, oy = p.cy - 1 - ceny;  // mosaic pixel of image (0, 0)
-#pragma unroll
-        for (int j = 0; j < PER; j++) {
-            const int k = threadIdx.x + j * 256;
-            const int mx = tx * MOS_TILE + (k & (MOS_TILE - 1)), my = ty * MOS_TILE + k / MOS_TILE;
-            const int ix = mx - ox, iy = my - oy;
-            if (ix < 0 || ix >= p.nx || iy < 0 || iy >= p.ny) continue;
-            const float dx = (float)(ix - cenx), dy = (float)(iy - ceny);
-            const float pb = expf(-p.pbk * (dx * dx + dy * dy));
-            acc[j] += p.wt * pb * p.image[(int64_t)iy * p.nx + ix];
+    for (int pi = 0; pi < cnt; pi += 2) {
+        const MosaicPointing pa = pi < MOS_STAGE ? sp[pi] : pts[tpts[p0 + pi]];
+        float va[PER], vb[PER];
+        mos_load(pa, tx, ty, va);
+        if (pi + 1 < cnt) {
+            const MosaicPointing pb = pi + 1 < MOS_STAGE ? sp[pi + 1] : pts[tpts[p0 + pi + 1]];
+            mos_load(pb, tx, ty, vb);
+            mos_add(pa, tx, ty, va, acc);
+            mos_add(pb, tx, ty, vb, acc);
+        } else {
+            mos_add(pa, tx, ty, va, acc);
         }
     }
 #pragma unroll
