@@ -6,14 +6,22 @@
 // scalings (fts/ftsgrpre.f:229-243), takes u, v, w to wavelengths (vis/visstd.f:135-202),
 // converts the correlations to Stokes (vis/visconvs.f, visconv2.f, visconvp.f) and keeps one
 // Stokes parameter's VIS and WT (vis/visstd.f:260-314).  The file is read while the previous
-// chunk is copied and decoded.
+// chunk is copied and decoded, each chunk by a pool of reader threads (pread of disjoint
+// slices), so the read is not bound by one thread's copy out of the page cache.
+#include <errno.h>
+#include <fcntl.h>
 #include <stdio.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -29,6 +37,104 @@ struct sde_uvfits {
 };
 
 namespace {
+
+// ---------------------------------------------------------------------------------------
+// Chunk reader: a chunk's bytes are split into one slice per thread and read with pread on
+// one descriptor (the calling thread reads slice 0).  The result is the length of the chunk's
+// contiguous prefix that was read: a short slice is the end of the file, and what follows it
+// is not counted, as a sequential read would stop there.
+class ChunkReader {
+  public:
+    ChunkReader(int fd, int nthreads) : fd_(fd), n_(nthreads), got_((size_t)nthreads, 0) {
+        try {
+            for (int t = 1; t < n_; t++) th_.emplace_back([this, t] { worker(t); });
+        } catch (...) {
+            finish();  // the threads that did start are joined before the error propagates
+            throw;
+        }
+    }
+    ~ChunkReader() { finish(); }
+    // len bytes at file offset off into dst; the contiguous bytes read, or -1 on a read error
+    int64_t read(uint8_t *dst, int64_t off, int64_t len) {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            dst_ = dst;
+            off_ = off;
+            len_ = len;
+            pending_ = n_ - 1;
+            err_ = false;
+            gen_++;
+        }
+        cv_.notify_all();
+        slice(0);
+        {
+            std::unique_lock<std::mutex> l(m_);
+            done_.wait(l, [this] { return pending_ == 0; });
+        }
+        if (err_) return -1;
+        int64_t total = 0;
+        for (int t = 0; t < n_; t++) {
+            total += got_[(size_t)t];
+            if (got_[(size_t)t] < bound(t + 1) - bound(t)) break;
+        }
+        return total;
+    }
+
+  private:
+    void finish() {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            stop_ = true;
+            gen_++;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+        th_.clear();
+    }
+    int64_t bound(int t) const { return len_ * t / n_; }
+    void slice(int t) {
+        const int64_t a = bound(t), b = bound(t + 1);
+        int64_t done = 0;
+        while (a + done < b) {
+            const ssize_t r = pread(fd_, dst_ + a + done, (size_t)(b - a - done), (off_t)(off_ + a + done));
+            if (r < 0 && errno == EINTR) continue;
+            if (r < 0) err_ = true;
+            if (r <= 0) break;
+            done += r;
+        }
+        got_[(size_t)t] = done;
+    }
+    void worker(int t) {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> l(m_);
+                cv_.wait(l, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (stop_) return;
+            }
+            slice(t);
+            std::lock_guard<std::mutex> l(m_);
+            if (--pending_ == 0) done_.notify_one();
+        }
+    }
+    const int fd_, n_;
+    std::vector<int64_t> got_;
+    std::vector<std::thread> th_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+    int pending_ = 0;
+    std::atomic<bool> err_{false};
+    uint8_t *dst_ = nullptr;
+    int64_t off_ = 0, len_ = 0;
+};
+
+int reader_threads() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    return (int)std::min(8u, std::max(1u, hw));
+}
 
 // ---------------------------------------------------------------------------------------
 // Header.  80-character cards in 2880-byte blocks up to END; "KEYWORD = value / comment".
@@ -448,7 +554,8 @@ extern "C" int sde_uvfits_read(sde_ctx *ctx, const sde_uvfits *f, int stokes, fl
     SDE_TRY(ctx_scratch(ctx, "uvf_chunk1", cbytes, (void **)&dbuf[1]));
     uint8_t *hbuf[2] = {nullptr, nullptr};
     cudaEvent_t ev[2] = {nullptr, nullptr};
-    FILE *fp = nullptr;
+    int fd = -1;
+    std::unique_ptr<ChunkReader> rd;
     int rc = SDE_OK;
     int64_t done = 0;
     cudaError_t e = cudaHostAlloc((void **)&hbuf[0], cbytes, cudaHostAllocDefault);
@@ -460,9 +567,17 @@ extern "C" int sde_uvfits_read(sde_ctx *ctx, const sde_uvfits *f, int stokes, fl
         rc = SDE_ECUDA;
     }
     if (rc == SDE_OK) {
-        fp = fopen(f->path.c_str(), "rb");
-        if (!fp || fseek(fp, (long)f->data_off, SEEK_SET) != 0) {
+        fd = open(f->path.c_str(), O_RDONLY);
+        if (fd < 0) {
             sde_set_error("sde_uvfits_read: cannot read %s", f->path.c_str());
+            rc = SDE_EINVAL;
+        }
+    }
+    if (rc == SDE_OK) {
+        try {
+            rd.reset(new ChunkReader(fd, reader_threads()));
+        } catch (...) {
+            sde_set_error("sde_uvfits_read: cannot start the reader threads");
             rc = SDE_EINVAL;
         }
     }
@@ -471,7 +586,13 @@ extern "C" int sde_uvfits_read(sde_ctx *ctx, const sde_uvfits *f, int stokes, fl
         // the buffer's previous copy has finished before the file overwrites it
         e = cudaEventSynchronize(ev[k]);
         if (e != cudaSuccess) break;
-        const int64_t got = (int64_t)fread(hbuf[k], gbytes, (size_t)want, fp);
+        const int64_t gotb = rd->read(hbuf[k], f->data_off + done * (int64_t)gbytes, want * (int64_t)gbytes);
+        if (gotb < 0) {
+            sde_set_error("sde_uvfits_read: cannot read %s", f->path.c_str());
+            rc = SDE_EINVAL;
+            break;
+        }
+        const int64_t got = gotb / (int64_t)gbytes;  // whole groups only, as fread counts them
         if (got > 0) {
             e = cudaMemcpyAsync(dbuf[k], hbuf[k], (size_t)got * gbytes, cudaMemcpyHostToDevice, st);
             if (e == cudaSuccess) e = cudaEventRecord(ev[k], st);
@@ -507,7 +628,8 @@ extern "C" int sde_uvfits_read(sde_ctx *ctx, const sde_uvfits *f, int stokes, fl
         sde_set_error("sde_uvfits_read: %s", cudaGetErrorString(es));
         rc = SDE_ECUDA;
     }
-    if (fp) fclose(fp);
+    rd.reset();
+    if (fd >= 0) close(fd);
     for (int k = 0; k < 2; k++) {
         if (ev[k]) cudaEventDestroy(ev[k]);
         if (hbuf[k]) cudaFreeHost(hbuf[k]);
