@@ -308,3 +308,99 @@ def test_grddeh2d_speculation(L, orc):
     vis, wt = call(u2)  # and the rebuilt plan is reused
     check(u2, vis, wt)
     assert _stats(L)[0] - h2 == 1
+
+
+def _edge_geom(orc, n, seed):
+    from sde_gb300.imaging import Geom
+    g = Geom(64, 8.0, vdec=40.0)
+    rng = np.random.default_rng(seed)
+    u = (rng.uniform(-30.0, 30.0, max(n, 1)) / g.uscale).astype(np.float32)
+    v = (rng.uniform(-27.0, 27.0, max(n, 1)) / g.vscale).astype(np.float32)
+    w = rng.uniform(-50, 50, max(n, 1)).astype(np.float32)
+    vis = (rng.normal(size=max(n, 1)) + 1j * rng.normal(size=max(n, 1))).astype(np.complex64)
+    cf, _, _ = orc.grdcf()
+    return g, u, v, w, vis, cf, np.ascontiguousarray(list(g.shift), np.float64)
+
+
+def test_grdh2d_without_weight_is_the_references_error(L, orc, capfd):
+    """GRDH2D stops with 'No weight!' (grd/grdh2d.f:195-197) when nothing is gridded: no
+    visibilities, every weight flagged, every point off the grid, and a cached plan whose new
+    call has every weight zeroed (the speculative path has already returned a grid and must
+    write it again).  GVIS comes back zero and SUMWT 0, as the oracle's; the error flag is
+    set and the message is the reference's."""
+    from sde_gb300 import _abi
+    n = 2000
+    g, u, v, w, vis, cf, shift = _edge_geom(orc, n, 31)
+    wt_ok = np.random.default_rng(32).uniform(0.5, 2.0, n).astype(np.float32)
+    wt_flag = -wt_ok
+    wt_flag[::3] = 0.0
+    u_off = (np.full(n, 40.0) / g.uscale).astype(np.float32)  # NINT(UCELL) + 2 SUPPU > NU
+
+    def call(nn, uu, wt):
+        gvis = np.full((g.nv, g.nu), np.complex64(7 + 7j))
+        sw = C.c_float(-1.0)
+        wt = np.ascontiguousarray(wt, np.float32).copy()
+        _abi.sysi().error = 0
+        L.grdh2d_(_p(vis), _p(wt), _p(uu), _p(v), _p(w), I(nn), F(g.uscale), F(0), F(g.vscale), F(0),
+                  I(g.uorigin), I(g.vorigin), _p(gvis), I(0), I(g.nu), I(g.nv), _p(cf), I(3), I(128), _p(cf),
+                  I(3), I(128), _p(shift), C.byref(sw))
+        err = _abi.sysi().error
+        _abi.sysi().error = 0
+        return gvis, sw.value, err
+
+    def no_weight(nn, uu, wt):
+        capfd.readouterr()
+        gvis, sw, err = call(nn, uu, wt)
+        rc, rg, rsw, _ = orc.grdh2d(vis[:nn], wt[:nn], uu[:nn], v[:nn], w[:nn], g.uscale, g.vscale, g.uorigin,
+                                    g.vorigin, g.nu, g.nv, shift, cf=cf)
+        assert rc == 1 and rsw == 0.0 and not rg.any()  # the oracle's ENOWEIGHT
+        assert err == 1 and "No weight!" in capfd.readouterr().err
+        assert not gvis.any() and sw == 0.0
+
+    no_weight(0, u, wt_ok)
+    no_weight(n, u, wt_flag)
+    no_weight(n, u_off, wt_ok)
+    # a cached plan, then the same U, V, W with every weight zero
+    for _ in range(2):
+        gvis, sw, err = call(n, u, wt_ok)
+        assert err == 0
+    rc, rg, rsw, _ = orc.grdh2d(vis, wt_ok, u, v, w, g.uscale, g.vscale, g.uorigin, g.vorigin, g.nu, g.nv,
+                                shift, cf=cf)
+    # SUMWT: the reference adds WT in sequence in REAL; the GPU sums in double and rounds once,
+    # so the two differ by the sequential sum's rounding (~sqrt(n) 2^-24 relative)
+    assert rc == 0 and abs(sw - rsw) <= 1e-5 * rsw
+    assert np.abs(gvis - rg).max() / np.abs(rg).max() < 1e-5
+    no_weight(n, u, np.zeros(n, np.float32))
+    gvis, sw, err = call(n, u, wt_ok)  # and the next call grids again
+    assert err == 0 and np.abs(gvis - rg).max() / np.abs(rg).max() < 1e-5
+
+
+def test_grddeh2d_empty_flagged_and_off_grid(L, orc):
+    """GRDDEH2D with no visibilities writes nothing; with every weight flagged VIS and WT keep
+    the caller's values; with every point off the grid each VIS is 0 and its WT negated
+    (grd/grddeh2d.f) -- bit for bit the oracle's in each case, with no error."""
+    from sde_gb300 import _abi
+    n = 1500
+    g, u, v, w, vis0, cf, shift = _edge_geom(orc, n, 41)
+    rng = np.random.default_rng(42)
+    gvis = (rng.normal(size=(g.nv, g.nu)) + 1j * rng.normal(size=(g.nv, g.nu))).astype(np.complex64)
+    wt_ok = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    wt_flag = -wt_ok
+    wt_flag[::4] = 0.0
+    u_off = (np.full(n, 40.0) / g.uscale).astype(np.float32)
+    for nn, uu, wt0 in ((0, u, wt_ok), (n, u, wt_flag), (n, u_off, wt_ok)):
+        vis = vis0.copy()
+        wt = wt0.copy()
+        _abi.sysi().error = 0
+        L.grddeh2d_(_p(vis), _p(wt), _p(uu), _p(v), _p(w), I(nn), F(g.uscale), F(0), F(g.vscale), F(0),
+                    I(g.uorigin), I(g.vorigin), _p(gvis), I(g.nu), I(g.nv), _p(cf), I(3), I(128), _p(cf),
+                    I(3), I(128), _p(shift))
+        assert _abi.sysi().error == 0
+        if nn == 0:
+            assert np.array_equal(vis.view(np.uint32), vis0.view(np.uint32))
+            assert np.array_equal(wt.view(np.uint32), wt0.view(np.uint32))
+            continue
+        rvis, rwt, _ = orc.grddeh2d(vis0, wt0, uu, v, w, g.uscale, g.vscale, g.uorigin, g.vorigin, gvis, shift,
+                                    cf=cf)
+        assert np.array_equal(wt.view(np.uint32), rwt.view(np.uint32))
+        assert np.array_equal(vis.view(np.uint32), rvis.view(np.uint32))
