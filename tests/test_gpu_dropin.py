@@ -404,3 +404,42 @@ def test_grddeh2d_empty_flagged_and_off_grid(L, orc):
                                     cf=cf)
         assert np.array_equal(wt.view(np.uint32), rwt.view(np.uint32))
         assert np.array_equal(vis.view(np.uint32), rvis.view(np.uint32))
+
+
+@pytest.mark.parametrize("nflag", ["empty", "flagged"])
+def test_weights_on_empty_and_flagged_inputs(L, orc, case, nflag):
+    """GRDUWT2D and GRDRUW2D (every robust mode) with no visibilities, or with every weight
+    flagged: the weight grid is zero, as the oracle's, and no NEWWT is written (both routines
+    skip WT <= 0: grd/grduwt2d.f:118, grd/grdruw2d.f:197), so the caller's values stay; no
+    error (GRDRUW2D's NORM factor is 0/0 there and is used by no point)."""
+    from sde_gb300 import _abi
+    from sde_gb300.imaging import Geom
+    o, _, _ = case
+    g = Geom(o["imsize"], o["cell"], vdec=o["vdec"])
+    shift = np.ascontiguousarray(list(g.shift), np.float64)
+    n = 0 if nflag == "empty" else len(o["wt"])
+    wt = -np.abs(np.ascontiguousarray(o["wt"], np.float32))
+    wt[::5] = 0.0
+    args = (wt[:n], o["u"][:n], o["v"][:n], o["w"][:n], g.wuscale, g.wvscale, g.uorigin, g.vorigin, g.nu, g.nv,
+            shift)
+
+    def run(fn, *extra):
+        newwt = np.full(max(n, 1), np.float32(3.5))
+        gwt = np.full((g.nv, g.nu), np.float32(9.0))
+        _abi.sysi().error = 0
+        fn(_p(wt), _p(o["u"]), _p(o["v"]), _p(o["w"]), I(n), F(g.wuscale), F(0), F(g.wvscale), F(0),
+           I(g.uorigin), I(g.vorigin), _p(newwt), _p(gwt), I(g.nu), I(g.nv), _p(shift), *extra)
+        assert _abi.sysi().error == 0
+        return newwt[:n], gwt
+
+    _, rgwt, _ = orc.grduwt2d(*args)
+    newwt, gwt = run(L.grduwt2d_)
+    assert not rgwt.any() and not gwt.any()
+    assert (newwt == np.float32(3.5)).all()
+    for mode, rob in (("NORM", [0.5, 0.0, 0.0]), ("ABS", [0.0, 1.0, 0.0]), ("NONE", [0.0, 0.0, 0.0])):
+        rc, _, rgwt, *_ = orc.grdruw2d(*args, mode, rob)
+        assert rc == 0
+        newwt, gwt = run(L.grdruw2d_, mode.ljust(4).encode(), _p(np.array(rob, np.float32)), F(0.0),
+                         C.c_size_t(4))
+        assert not rgwt.any() and not gwt.any(), mode
+        assert (newwt == np.float32(3.5)).all(), mode
