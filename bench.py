@@ -35,6 +35,23 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+def max_over_ranks(x, tdist=None, device=None):
+    """x on a single process; with a process group up, the largest x over all ranks (the
+    slowest replica sets the whole job's time)."""
+    if tdist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mvis(nvis_per_rank, world, seconds_per_step):
+    """Whole-job Mvis/s of `world` replicas that each process nvis_per_rank visibilities per
+    step, timed by the slowest replica (weak scaling)."""
+    return nvis_per_rank * world / seconds_per_step / 1e6
+
+
 METRIC = "Mvis/s grid+degrid @4096^2 (one CLEAN major cycle per step)"
 IMSIZE, CELL, VDEC = 4096, 0.5, 40.0
 NCHAN = 64
@@ -369,12 +386,9 @@ def run_gpu(args):
         if cnt.value:
             kern[name] = {"ms_avg": tot.value / cnt.value, "launches": cnt.value}
     L.sde_ctx_profile(ctx.h, 0)
-    if dist:
-        t = torch.tensor([elapsed_ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, tdist if dist else None, dev)
     ms_per_step = elapsed_ms / args.steps
-    value = nvis * world / (ms_per_step / 1e3) / 1e6
+    value = whole_job_mvis(nvis, world, ms_per_step / 1e3)
 
     # ---- roofline for the dominant kernel --------------------------------------------
     peaks = {}
@@ -407,8 +421,9 @@ def run_gpu(args):
 
     # ---- e2e through the Fortran drop-in ABI on pinned host arrays ---------------------
     e2e = None
-    if rank == 0 and args.e2e_steps > 0:
-        e2e = run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis)
+    if args.e2e_steps > 0:  # every replica, timed by the slowest
+        e2e = run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis,
+                      tdist if dist else None, dev, world)
 
     line = {
         "metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": world,
@@ -745,8 +760,9 @@ def run_precision(args):
     }
 
 
-def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis):
-    """Same step through grdh2d_/fftr2d_/pixcor2d_/grddeh2d_ with pinned host buffers."""
+def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis, tdist=None, dev=None, world=1):
+    """Same step through grdh2d_/fftr2d_/pixcor2d_/grddeh2d_ with pinned host buffers; with a
+    process group, every replica runs it and the slowest one's time counts."""
     from sde_gb300 import _abi
     P = C.c_void_p
 
@@ -799,11 +815,13 @@ def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis):
 
     step()  # warm-up (allocates the shim's device buffers)
     torch.cuda.synchronize()
+    if tdist is not None:
+        tdist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         step()
     torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / args.e2e_steps
+    dt = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, tdist, dev)
     gb = nu * nv * 8
     img = n * n * 4
     # grdh2d_: VIS, WT, U, V, W up, grid down; fftr2d_(-1): grid up, image and the
@@ -815,7 +833,7 @@ def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis):
     negated = bool(((hwt2 < 0) & (hwt > 0)).any().item())
     h2d = 24 * nvis + gb + img + img + img + 16 * nvis + gb + (12 * nvis if flagged else 0)
     d2h = gb + img + gb + img + img + gb + 8 * nvis + (4 * nvis if negated else 0)
-    return {"value": nvis / dt / 1e6, "unit": "Mvis/s", "ms_per_step": dt * 1e3,
+    return {"value": whole_job_mvis(nvis, world, dt), "unit": "Mvis/s", "ms_per_step": dt * 1e3,
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "path": "grdh2d_ -> fftr2d_(-1) -> pixcor2d_ x2 -> fftr2d_(+1) -> grddeh2d_, pinned "
                     "host arrays; every call uploads its inputs and downloads its outputs; "

@@ -47,7 +47,11 @@ int sde_version(void);
  * Layer 1: Fortran-77 drop-in entry points (gfortran symbol names).
  * ====================================================================================== */
 
-/* The drop-ins keep the plan of their last GRDH2D/GRDDEH2D call together with a device copy
+/* The drop-ins run on one library context, created by the first drop-in call on the device
+ * named by the environment variable SDE_DEVICE, or else on the calling thread's current CUDA
+ * device (device 0 unless the program selected another).
+ *
+ * The drop-ins keep the plan of their last GRDH2D/GRDDEH2D call together with a device copy
  * of the U, V, W, WT it was built from; a call whose U, V, W, WT (compared bitwise on the
  * device after the upload), grid geometry and gridding function match reuses it and only
  * loads the new VIS.  No counterpart in the reference.  Statistics, and a call that frees

@@ -496,10 +496,17 @@ __attribute__((weak)) void msgput_(const char *msg, const char *type, size_t lms
 static std::mutex g_shim_mu;
 static sde_ctx *g_shim_ctx = nullptr;
 
+// The drop-ins' context: on device SDE_DEVICE if set, else on the calling thread's current
+// device (0 unless the caller chose another), created by the first drop-in call.
 static sde_ctx *shim_ctx() {
     if (!g_shim_ctx) {
         const char *d = getenv("SDE_DEVICE");
-        if (sde_ctx_create(&g_shim_ctx, d ? atoi(d) : 0) != SDE_OK) g_shim_ctx = nullptr;
+        int dev = 0;
+        if (d)
+            dev = atoi(d);
+        else if (cudaGetDevice(&dev) != cudaSuccess)
+            dev = 0;
+        if (sde_ctx_create(&g_shim_ctx, dev) != SDE_OK) g_shim_ctx = nullptr;
     }
     return g_shim_ctx;
 }
