@@ -65,11 +65,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="single",
-                    choices=["single", "mosaic", "serve", "precision"],
+                    choices=["single", "mosaic", "serve", "precision", "clark"],
                     help="single: the large single field (headline); mosaic: config 4 "
                          "(49 uneven pointings, batched vs per-pointing); serve: config 5 "
                          "(Poisson stream of jobs, continuous batching); precision: config 3 "
-                         "(557 M vis at 8192^2: dirty image error vs the FP64 oracle)")
+                         "(557 M vis at 8192^2: dirty image error vs the FP64 oracle); clark: "
+                         "Clark CLEAN of a 4096^2 dirty image (clean task's default algorithm)")
     ap.add_argument("--no-extras", action="store_true",
                     help="single workload: skip the compact mosaic/serve summaries")
     ap.add_argument("--nchan", type=int, default=NCHAN, help="channels (64 = full workload)")
@@ -760,6 +761,76 @@ def run_precision(args):
     }
 
 
+CLARK_KW = dict(niter=5000, gain=0.1, flux=0.0, numcl=32768, bpatch=128)
+
+
+def run_clark(args):
+    """Clark CLEAN (task/clean.f CLARK branch with IMGCCLEA) of the dirty image of a seeded
+    27-antenna Y-array observation (8 h, 4 channels, four point sources and a Gaussian) at
+    4096^2 and 0.25"; a step is one whole CLEAN of 5000 iterations from the same dirty image
+    and PSF (minor cycles on the device, image-plane residual by FFT each major cycle)."""
+    import torch
+    from sde_gb300 import synth
+    from sde_gb300._abi import lib
+    from sde_gb300.imaging import Context, Geom, clark, uvmap
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if rank != 0:
+        return None
+    torch.cuda.set_device(local)
+    n, cell, ntime, nchan, dec, seed = 4096, 0.25, 192, 4, 40.0, 7
+    pos = synth.y_array(27, 3000.0, seed)
+    u, v, w = synth.uvw_tracks(pos, dec, 8.0, 8.0 * 3600.0 / ntime, 1.4e9 * (1.0 + 0.05 * np.arange(nchan)))
+    as2r = math.radians(1.0 / 3600.0)
+    fov = n * cell * as2r
+    vis = synth.visibilities(u, v, np.array([1.0, 0.3, 0.1, 0.05]), np.array([0.0, 0.12, -0.2, 0.3]) * fov,
+                             np.array([0.0, -0.08, 0.15, -0.25]) * fov, 1e-3, seed,
+                             gauss=[(0.2, -0.1 * fov, -0.2 * fov, 8 * cell * as2r)])
+    ctx = Context(local)
+    g = Geom(n, cell, vdec=dec)
+    t = {k: ctx.tensor(a) for k, a in (("u", u), ("v", v), ("w", w), ("vis", vis),
+                                       ("wt", np.ones(len(u), np.float32)))}
+    r = uvmap(ctx, g, t["u"], t["v"], t["w"], t["vis"], t["wt"], rmode="UNIFORM")
+    dirty, psf = r["dirty"], r["psf"]
+    for _ in range(max(1, args.warmup)):
+        res = clark(ctx, dirty, psf, **CLARK_KW)
+    ctx.sync()
+    L = lib()
+    L.sde_ctx_reset_stats(ctx.h)
+    L.sde_ctx_profile(ctx.h, 1)
+    steps = max(1, min(args.steps, 10))
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        res = clark(ctx, dirty, psf, **CLARK_KW)
+        ctx.sync()
+        times.append(time.perf_counter() - t0)
+    kern = {}
+    for k in ("clark_select", "clark_minor", "clark_cmul", "clark_sub", "col_fft", "row_c2r", "row_r2c"):
+        tot, cnt = C.c_double(), C.c_int64()
+        L.sde_ctx_kernel_stats(ctx.h, k.encode(), C.byref(tot), C.byref(cnt))
+        if cnt.value:
+            kern[k] = {"ms_per_clean": tot.value / steps, "launches_per_clean": cnt.value // steps}
+    L.sde_ctx_profile(ctx.h, 0)
+    ms = statistics.median(times) * 1e3
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        dn, pn = dirty.cpu().numpy(), psf.cpu().numpy()
+        t0 = time.perf_counter()
+        ro = O.clark(dn, pn, **CLARK_KW)
+        cpu = {"value": (time.perf_counter() - t0) * 1e3, "unit": "ms per CLEAN", "cores": 1, "kind": "port",
+               "sample": "the same CLEAN (same dirty image and PSF) by the oracle C restatement, 1 thread",
+               "aniter": int(ro["aniter"]), "ncycles": int(ro["ncycles"])}
+    return {"metric": "ms per Clark CLEAN (4096^2, 5000 iterations)", "value": ms, "unit": "ms",
+            "higher_is_better": False, "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup),
+            "dtype": "f32", "data": "synthetic (seeded 27-antenna Y array, 8 h x 4 ch, 4 points + Gaussian)",
+            "config": {"workload": "Clark CLEAN of a 4096^2 dirty image, %d vis, uniform weighting" % len(u),
+                       **CLARK_KW},
+            "aniter": int(res["aniter"]), "ncycles": int(res["ncycles"]), "kernels": kern,
+            "ms_each": [round(x * 1e3, 3) for x in times], "cpu_baseline": cpu}
+
+
 def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis, tdist=None, dev=None, world=1):
     """Same step through grdh2d_/fftr2d_/pixcor2d_/grddeh2d_ with pinned host buffers; with a
     process group, every replica runs it and the slowest one's time counts."""
@@ -857,6 +928,10 @@ def main():
             print(json.dumps(line))
     elif args.workload == "precision":
         line = run_precision(args)
+        if line:
+            print(json.dumps(line))
+    elif args.workload == "clark":
+        line = run_clark(args)
         if line:
             print(json.dumps(line))
     else:

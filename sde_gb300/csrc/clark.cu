@@ -446,43 +446,47 @@ __global__ void k_clark_sub(const float *__restrict__ drt, float *res, int64_t n
         res[k] = __fsub_rn(drt[k], res[k]);
 }
 
-// beam-patch peak (PIXISAMA over the patch, pix/pix2drcc.f:63-66) and the largest |PSF|
-// outside the patch (pix/pixrexts.f), one block
-__global__ void k_clark_patch(const float *__restrict__ psf, int n, int b0, int b1, const float *__restrict__ spsf,
-                              int pw, ClarkState *st) {
+// beam-patch peak (PIXISAMA over the patch, pix/pix2drcc.f:63-66), one block; clears the
+// largest |PSF| outside the patch, which k_clark_ext then takes over the whole PSF
+__global__ void k_clark_patch(const float *__restrict__ spsf, int pw, ClarkState *st) {
     __shared__ unsigned long long sk[32];
-    __shared__ float se[32];
     unsigned long long best = 0ull;
-    float ext = 0.f;
     for (int k = threadIdx.x; k < pw * pw; k += blockDim.x) {
         const unsigned long long key = isama_key(spsf[k], k);
         best = key > best ? key : best;
     }
-    for (int64_t k = threadIdx.x; k < (int64_t)n * n; k += blockDim.x) {
-        const int x = (int)(k % n) + 1, y = (int)(k / n) + 1;
-        if (!(x >= b0 && x <= b1 && y >= b0 && y <= b1)) ext = fmaxf(ext, fabsf(psf[k]));
-    }
     for (int d = 16; d > 0; d >>= 1) {
         const unsigned long long o = __shfl_xor_sync(0xffffffffu, best, d);
         best = o > best ? o : best;
-        ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, d));
     }
-    if ((threadIdx.x & 31) == 0) {
-        sk[threadIdx.x >> 5] = best;
-        se[threadIdx.x >> 5] = ext;
-    }
+    if ((threadIdx.x & 31) == 0) sk[threadIdx.x >> 5] = best;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
-            best = sk[w] > best ? sk[w] : best;
-            ext = fmaxf(ext, se[w]);
-        }
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) best = sk[w] > best ? sk[w] : best;
         const int ip = (int)(0xFFFFFFFFu - (unsigned)(best & 0xFFFFFFFFull));
         st->pmpx = 1 + ip % pw;
         st->pmpy = 1 + ip / pw;
-        st->extside = ext;
+        st->extside = 0.f;
         st->tflux = 0.f;
     }
+}
+
+// the largest |PSF| outside the patch [b0, b1]^2 (pix/pixrexts.f): blocks over rows, threads
+// over columns; the maximum is order-free, so an atomic max on the float's bits (|PSF| >= 0
+// orders as an unsigned integer) gives the same value as a sequential scan; NaN is skipped
+// as fmaxf would skip it
+__global__ void __launch_bounds__(256) k_clark_ext(const float *__restrict__ psf, int n, int b0, int b1,
+                                                   ClarkState *st) {
+    float ext = 0.f;
+    for (int y = blockIdx.x; y < n; y += gridDim.x) {
+        const bool inrows = y + 1 >= b0 && y + 1 <= b1;
+        const float *row = psf + (size_t)y * n;
+        for (int x = threadIdx.x; x < n; x += blockDim.x)
+            if (!(inrows && x + 1 >= b0 && x + 1 <= b1)) ext = fmaxf(ext, fabsf(row[x]));
+    }
+    for (int d = 16; d > 0; d >>= 1) ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, d));
+    if ((threadIdx.x & 31) == 0 && ext > 0.f)
+        atomicMax(reinterpret_cast<unsigned int *>(&st->extside), __float_as_uint(ext));
 }
 
 int fail(const char *m) {
@@ -553,7 +557,8 @@ extern "C" int sde_clark(sde_ctx *ctx, const float *dirty, const float *psf, int
     SDE_CUDA_TRY(cudaMemcpy2DAsync(spsf, sizeof(float) * pw, psf + (size_t)(b0 - 1) * n + (b0 - 1),
                                    sizeof(float) * n, sizeof(float) * pw, pw, cudaMemcpyDeviceToDevice, st));
     SDE_TRY(sde_grid_from_image(ctx, psf, n, n, n, n, 0, (float *)xfr, pitch));
-    k_clark_patch<<<1, 1024, 0, st>>>(psf, n, b0, b1, spsf, pw, dst);
+    k_clark_patch<<<1, 1024, 0, st>>>(spsf, pw, dst);
+    k_clark_ext<<<std::min(n, ctx->num_sms * 8), 256, 0, st>>>(psf, n, b0, b1, dst);
     SDE_CHECK_LAUNCH();
     // minor-cycle kernel: positions (+ beam patch when it fits) in shared memory
     const size_t sm_pos = sizeof(int) * CL_SLICE, sm_psf = sizeof(float) * (size_t)pw * pw;
