@@ -76,19 +76,23 @@ def parse():
     ap.add_argument("--nchan", type=int, default=NCHAN, help="channels (64 = full workload)")
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="single workload: skip the dirty image's error against the FP64 oracle")
     ap.add_argument("--clean-iters", type=int, default=200)
     ap.add_argument("--plan-opts", default=None,
                     help="item_max,chunk_max of the plan's work items and chunks (library defaults if unset)")
     return ap.parse_args()
 
 
-def workload_config(nchan, nvis):
+def workload_config(nchan, nvis, world=1):
+    """The workload's config, identical in both arms (a replica per rank when world > 1)."""
     return {"workload": "large single field: 27-antenna Y (21 km arms), 8 h x 10 s x %d ch "
                         "1.2-1.6 GHz, %d vis, 200 power-law sources + noise, robust NORM R=0, "
                         "4096^2 @ 0.5\" (grid 2049x4096)" % (nchan, nvis),
             "nvis": nvis, "imsize": IMSIZE, "cellsize_arcsec": CELL, "grid": [2049, 4096],
             "kernel": "SF prolate spheroidal 7x7, 128x oversampled",
-            "l2": "inputs 1.55 GB > 129 MB L2 (no flush needed)"}
+            "l2": "inputs 1.55 GB > 129 MB L2 (no flush needed)",
+            "parallelism": "replicas x%d" % world if world > 1 else "single job"}
 
 
 # ------------------------------------------------------------------------------------------
@@ -215,50 +219,129 @@ def reference_times(u, v, w, vis, wt, shift_geom, sample_frac, oracle_mod, fft_f
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU path timed on this host's cores."""
+    """--impl reference: the reference's CPU path (the oracle's C restatement, 1 thread like
+    SDE) on this host, over ONE FULL major cycle of the workload -- every one of the
+    visibilities gridded (GRDH2D) and degridded (GRDDEH2D) once, the inverse FFT with grid
+    correction of the gridded residual, and the correction and forward FFT of the model.
+    GRDH2D's visibility loop is split into K consecutive ranges, one per timed step (the
+    accumulation is the oracle's orc_grdh2d_acc, so the grid is that of one pass over all of
+    them), and each step degrids the same range; step 0 also transforms the model and the
+    last step finalizes the grid and transforms it.  The K steps together are exactly one
+    unsampled major cycle, so ms_per_step = cycle time / K is measured, not extrapolated.
+    Warm-up steps grid and degrid the first range into a scratch grid."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from oracle import oracle as O
+    from sde_gb300 import synth
     O.lib()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    t_setup = time.perf_counter()
     u, v, w, seed = make_uvw(args.nchan)
     nvis = len(u)
-    # bounded sample: one channel's worth of visibilities, spread over all channels
-    nsamp = min(nvis, 1010880)
-    idx = np.linspace(0, nvis - 1, nsamp).astype(np.int64)
-    us, vs, ws = u[idx], v[idx], w[idx]
-    vis = make_vis_numpy_sample(u, v, seed, idx)
-    wt = np.ones(nsamp, np.float32)
+    flux, l, m = synth.point_sky(NSRC, IMSIZE * CELL, seed)
+    vis = O.point_vis(u, v, flux, l, m)  # the same sky in double on the host's threads
+    rng = np.random.default_rng(seed + 2)
+    vis += (rng.normal(0, 1e-3, nvis) + 1j * rng.normal(0, 1e-3, nvis)).astype(np.complex64)
     p = O.params(IMSIZE, CELL, fov=1.0, rmode="NORM", vdec=VDEC)
     g = O.geom(p)
-    rc, wt, *_ = O.grdruw2d(wt, us, vs, ws, g.uscale, g.vscale, g.uorigin, g.vorigin, g.nu, g.nv,
-                            np.array(list(g.shift)), "NORM", [0.0, 0.0, 0.0])
-    scale = nvis / nsamp
-    times = []
-    for k in range(args.warmup + args.steps):
-        t = reference_times(us, vs, ws, vis, wt, g, nsamp / nvis, O)
-        if k >= args.warmup:
-            times.append(t)
-    per = {k: statistics.mean(t[k] for t in times) for k in times[0]}
-    step_s = (per["grid"] + per["degrid"]) * scale + per["fft"]
-    value = nvis / step_s / 1e6
+    shift = np.array(list(g.shift))
+    # once per job, outside the timing (as the GPU arm's weighting)
+    rc, wt, *_ = O.grdruw2d(np.ones(nvis, np.float32), u, v, w, g.uscale, g.vscale, g.uorigin,
+                            g.vorigin, g.nu, g.nv, shift, "NORM", [0.0, 0.0, 0.0])
+    cf, _, _ = O.grdcf()
+    ccf = O.grdccf(1 + g.fnu // 2)
+    model = np.zeros((IMSIZE, IMSIZE), np.float32)
+    model[IMSIZE // 2 - 1, IMSIZE // 2 - 1] = 1.0
+    setup_s = time.perf_counter() - t_setup
+    K = max(1, args.steps)
+    cuts = [nvis * k // K for k in range(K + 1)]
+
+    def degrid(mgrid, a, b):
+        out, _, _ = O.grddeh2d(vis[a:b], wt[a:b], u[a:b], v[a:b], w[a:b], g.uscale, g.vscale,
+                               g.uorigin, g.vorigin, mgrid, shift, cf=cf)
+        return vis[a:b] - out  # residual = observed - model (ARRSUBTR)
+
+    # warm-up: the first range into a scratch grid, degridded from an empty model grid
+    zero_grid = np.zeros((g.nv, g.nu), np.complex64)
+    for _ in range(args.warmup):
+        W = O.Grdh2dParts(g, cf)
+        W.add(vis, wt, u, v, w, cuts[0], cuts[1])
+        degrid(zero_grid, cuts[0], cuts[1])
+    P = O.Grdh2dParts(g, cf)
+    comp = {"grid": 0.0, "degrid": 0.0, "fft": 0.0}
+    step_s = []
+    mgrid = None
+    for k in range(K):
+        t0 = time.perf_counter()
+        if k == 0:
+            mc = O.pixcor2d(model, ccf, g.cenx, g.ceny)  # IMGGRIDC, then IMGFFT (r2c)
+            _, mgrid = O.fftr2d(IMSIZE, IMSIZE, g.fnu, g.nv, +1, rarray=mc)
+        t1 = time.perf_counter()
+        P.add(vis, wt, u, v, w, cuts[k], cuts[k + 1])
+        t2 = time.perf_counter()
+        degrid(mgrid, cuts[k], cuts[k + 1])
+        t3 = time.perf_counter()
+        if k == K - 1:
+            rc = P.end()
+            img, _ = O.fftr2d(IMSIZE, IMSIZE, g.fnu, g.nv, -1, xarray=P.grid)
+            img = O.pixcor2d(img, ccf, g.cenx, g.ceny)
+        t4 = time.perf_counter()
+        comp["fft"] += (t1 - t0) + (t4 - t3)
+        comp["grid"] += t2 - t1
+        comp["degrid"] += t3 - t2
+        step_s.append(t4 - t0)
+    total = sum(step_s)
+    value = nvis / total / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mvis/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": workload_config(args.nchan, nvis),
+        "ms_per_step": total / K * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uv tracks, power-law sky, noise)",
+        "config": workload_config(args.nchan, nvis, world),
         "cpu_baseline": {"value": value, "unit": "Mvis/s", "cores": 1, "kind": "port",
-                         "sample": "grid+degrid of %d of %d visibilities (every %.0fth) on the "
-                                   "full 4096^2 grid, scaled x%.1f, plus the full-size FFTs "
-                                   "and grid corrections; C restatement of the reference "
-                                   "(oracle/), gcc -O2, single-threaded like SDE"
-                                   % (nsamp, nvis, scale, scale),
-                         "components_s": per, "cpu": _cpu_model()},
+                         "sample": "none: one full major cycle over all %d visibilities (GRDH2D's "
+                                   "loop split into %d consecutive ranges, one per step) on the "
+                                   "full 4096^2 grid, with the full-size FFTs and corrections; "
+                                   "C restatement of the reference (oracle/), gcc -O2, "
+                                   "single-threaded like SDE" % (nvis, K),
+                         "components_s": comp, "cycle_s": total, "cpu": _cpu_model()},
         "e2e": {"value": value, "unit": "Mvis/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "setup_s": setup_s,
     }
     print(json.dumps(line))
+
+
+def precision_vs_fp64(geom, u, v, w, vis, wt, dirty, psf):
+    """The GPU's PSF-normalised dirty image and PSF of the workload against the FP64 oracle
+    (oracle/: the same gridder, inverse FFT and correction in double, on the host's threads,
+    with the GPU's reweighted WT): max |GPU - FP64| over CRDNHALF's window and over the whole
+    image, as a fraction of the FP64 image's peak."""
+    from oracle import oracle as O
+    O.lib()
+    p = O.params(IMSIZE, CELL, fov=1.0, rmode="NORM", vdec=VDEC)
+    og = O.geom(p)
+    t0 = time.perf_counter()
+    p64 = O.uvmap_image64_mt(og, u, v, w, vis, wt, True)
+    d64 = O.uvmap_image64_mt(og, u, v, w, vis, wt, False)
+    secs = time.perf_counter() - t0
+    pk = p64.max()
+    d64 /= pk
+    p64 /= pk
+    lo, hi = geom.window()
+    W = slice(lo, hi)
+    dpk = np.abs(d64).max()
+    out = {"dirty_window": float(np.abs(dirty - d64)[W, W].max() / dpk),
+           "dirty_image": float(np.abs(dirty - d64).max() / dpk),
+           "psf_window": float(np.abs(psf - p64)[W, W].max()),
+           "psf_image": float(np.abs(psf - p64).max()),
+           "bar": 1e-5, "unit": "fraction of the FP64 image peak",
+           "oracle": "FP64 restatement of GRDH2D + FFTR2D(-1) + PIXCOR2D (oracle/), %d host threads, %.1f s"
+                     % (max(1, min(os.cpu_count() or 1, 64)), secs),
+           "window": [lo, hi]}
+    out["within_bar"] = out["dirty_window"] <= 1e-5 and out["psf_window"] <= 1e-5
+    return out
 
 
 def _cpu_model():
@@ -340,13 +423,30 @@ def run_gpu(args):
     ctx.image_from_grid(geom, grid, psf)
     ctx.image_max(psf, maxpsf)
     ctx.scale_by_inverse(psf, maxpsf)
+    torch.cuda.synchronize()
+    psf_ms = (time.perf_counter() - t0) * 1e3 - plan_ms
     mc = MajorCycle(ctx, geom, plan, maxpsf, psf)
     mc.grid_step()
+    dirty0 = mc.dirty.clone()  # the observed field's dirty image (checked against FP64 below)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    cl = hogbom(ctx, geom, mc.dirty, psf, args.clean_iters, 0.1)
-    torch.cuda.synchronize()
-    hogbom_ms = (time.perf_counter() - t0) * 1e3
+    L = lib()
+
+    def timed_hogbom():
+        """wall time of one Hogbom call through the library, and k_hogbom's device time"""
+        L.sde_ctx_reset_stats(ctx.h)
+        L.sde_ctx_profile(ctx.h, 1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = hogbom(ctx, geom, mc.dirty, psf, args.clean_iters, 0.1)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) * 1e3
+        tot, cnt = C.c_double(), C.c_int64()
+        L.sde_ctx_kernel_stats(ctx.h, b"hogbom", C.byref(tot), C.byref(cnt))
+        L.sde_ctx_profile(ctx.h, 0)
+        return r, wall, tot.value
+
+    cl, hogbom_first_ms, hogbom_first_kernel_ms = timed_hogbom()
+    cl, hogbom_ms, hogbom_kernel_ms = timed_hogbom()
     model = components_image(ctx, geom, cl["cln"])
     torch.cuda.synchronize()
 
@@ -359,7 +459,6 @@ def run_gpu(args):
     torch.cuda.synchronize()
     if dist:
         tdist.barrier()
-    L = lib()
     L.sde_ctx_reset_stats(ctx.h)
     L.sde_ctx_profile(ctx.h, 1)
     clocks = ClockSampler(local)
@@ -420,6 +519,21 @@ def run_gpu(args):
                                      "achieved_gbs": (48 * nvis + 2 * grid_bytes) / (pair_ms / 1e3) / 1e9,
                                      "frac": (48 * nvis + 2 * grid_bytes) / (pair_ms / 1e3) / 1e9 / hbm_peak}}
 
+    # ---- one whole imaging job: weighting, plan, PSF, then 5 major cycles, each a step
+    # (grid + dirty image + model FFT + degrid) and a Hogbom minor cycle -------------------
+    ncyc = 5
+    job_ms = weights_ms + plan_ms + psf_ms + ncyc * (ms_per_step + hogbom_ms)
+    job = {"cycles": ncyc, "clean_iters_per_cycle": args.clean_iters, "ms": job_ms,
+           "mvis_s": whole_job_mvis(nvis * ncyc, world, job_ms / 1e3),
+           "parts_ms": {"weights": weights_ms, "plan_build": plan_ms, "psf": psf_ms,
+                        "major_cycle_steps": ncyc * ms_per_step, "hogbom": ncyc * hogbom_ms}}
+
+    # ---- the dirty image's error against the FP64 oracle at full size (rank 0) -----------
+    prec = None
+    if rank == 0 and not dist and not args.no_precision:
+        prec = precision_vs_fp64(geom, u, v, w, vis.cpu().numpy(), wt.cpu().numpy(),
+                                 dirty0.cpu().numpy(), psf.cpu().numpy())
+
     # ---- e2e through the Fortran drop-in ABI on pinned host arrays ---------------------
     e2e = None
     if args.e2e_steps > 0:  # every replica, timed by the slowest
@@ -431,15 +545,20 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uv tracks, power-law sky, noise)",
-        "config": dict(workload_config(args.nchan, nvis), parallelism="replicas" if world > 1 else "1 GPU"),
+        "config": workload_config(args.nchan, nvis, world),
         "gpu_launches": int(launches),
         "roofline": roofline,
         "kernels_ms": kern,
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu_base,
-        "once_per_job_ms": {"weights": weights_ms, "plan_build": plan_ms,
-                            "hogbom_%d_iter" % args.clean_iters: hogbom_ms},
+        "once_per_job_ms": {"weights": weights_ms, "plan_build": plan_ms, "psf": psf_ms,
+                            "hogbom_%d_iter" % args.clean_iters: hogbom_ms,
+                            "hogbom_kernel_%d_iter" % args.clean_iters: hogbom_kernel_ms,
+                            "hogbom_first_call": hogbom_first_ms,
+                            "hogbom_first_call_kernel": hogbom_first_kernel_ms},
+        "job": job,
+        "precision": prec,
         "plan": dict(gridding_vis=int(nplan), bytes=int(plan.nbytes), ndrop_weighting=int(wst.ndrop),
                      **_plan_stats(L, plan)),
     }
@@ -731,7 +850,8 @@ def run_precision(args):
     algorithm in double on the host); max |error| over the CRDNHALF window and the image as
     a fraction of the FP64 peak."""
     import torch
-    from sde_gb300 import precision, synth
+    from oracle import precision
+    from sde_gb300 import synth
     from sde_gb300.imaging import Context
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)

@@ -36,7 +36,7 @@ extern "C" {
 #define SDE_ECUDA 3       /* CUDA runtime error                                          */
 #define SDE_ENOWEIGHT 4   /* gridder found no weight (grd/grdh2d.f:195-197 'No weight!') */
 #define SDE_ETIMEDOUT 5   /* a bounded device wait gave up                                */
-#define SDE_EBADMODE 6    /* unrecognised RMODE (grd/grdruw2d.f:361)                      */
+#define SDE_EBADMODE 6    /* unrecognised RMODE (grd/grdruw2d.f:190-192)                      */
 #define SDE_ENODEV 7      /* no CUDA device                                               */
 #define SDE_ECANCELLED 8  /* stopped by the interrupt flag (SYSINTRP analogue)            */
 
@@ -59,13 +59,13 @@ int sde_version(void);
 int sde_shim_cache_stats(int64_t *hits, int64_t *misses);
 int sde_shim_cache_clear(void);
 
-/* Replaces GRDH2D (source/grd/grdh2d.f:7-9), called by VISGRID (vis/visgrid.f:329). */
+/* Replaces GRDH2D (source/grd/grdh2d.f:7-9), called by VISGRID (vis/visgrid.f:160-164). */
 void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
              float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
              float *gvis, int *psf, int *nu, int *nv, float *gridfnu, int *suppu, int *osampu,
              float *gridfnv, int *suppv, int *osampv, double *shift, float *sumwt);
 
-/* Replaces GRDDEH2D (source/grd/grddeh2d.f:7-9), called by VISDEGRI (vis/visdegri.f:81). */
+/* Replaces GRDDEH2D (source/grd/grddeh2d.f:7-9), called by VISDEGRI (vis/visdegri.f:135-139). */
 void grddeh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
                float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
                float *gvis, int *nu, int *nv, float *intfnu, int *suppu, int *osampu,
@@ -78,9 +78,9 @@ void grdqh2d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, fl
               float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin, float *gvis,
               int *psf, int *nu, int *nv, double *shift, float *sumwt);
 
-/* Replace GRDH23D (source/grd/grdh23d.f:5-8) and GRDDEH23 (source/grd/grddeh23.f:5-8), the
- * slow-Z gridder and degridder VISGRID (vis/visgrid.f:219-226) and VISDEGRI
- * (vis/visdegri.f:154-160) call for N----SIN third axes: the 2-D window on NZ planes, plane iz
+/* Replace GRDH23D (source/grd/grdh23d.f:7-10) and GRDDEH23 (source/grd/grddeh23.f:7-10), the
+ * slow-Z gridder and degridder VISGRID (vis/visgrid.f:220-226) and VISDEGRI
+ * (vis/visdegri.f:154-159) call for N----SIN third axes: the 2-D window on NZ planes, plane iz
  * rotated by exp(-/+i TWOPI WLOCAL DTOR CELLZ (iz-REFZ)); GVIS [NZ][NV][NU] complex; tables
  * of 2*(SUPP+1)*OSAMP+1 floats (any support and oversampling). */
 void grdh23d_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
@@ -94,38 +94,38 @@ void grddeh23_(float *vis, float *wt, float *u, float *v, float *w, int *nvis, f
                float *intfnv, int *suppv, int *osampv, int *nz, float *cellz, float *refz,
                double *shift);
 
-/* Replaces GRDUWT2D (source/grd/grduwt2d.f:7-8), called by GRDUWT (grd/grduwt.f:122). */
+/* Replaces GRDUWT2D (source/grd/grduwt2d.f:7-8), called by GRDUWT (grd/grduwt.f:122-126). */
 void grduwt2d_(float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
                float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
                float *newwt, float *gwt, int *nu, int *nv, double *shift);
 
-/* Replaces GRDRUW2D (source/grd/grdruw2d.f:177-179), called by GRDRUWT (grd/grdruwt.f:346). */
+/* Replaces GRDRUW2D (source/grd/grdruw2d.f:7-9), called by GRDRUWT (grd/grdruwt.f:172-176). */
 void grdruw2d_(float *wt, float *u, float *v, float *w, int *nvis, float *uscale,
                float *uoffset, float *vscale, float *voffset, int *uorigin, int *vorigin,
                float *newwt, float *gwt, int *nu, int *nv, double *shift, char *rmode,
                float *robust, float *ds, size_t rmode_len);
 
-/* Replaces FFTR2D (source/fft/fftr2d.f:7-8), called by ARRFFTR (arr/arrfftr.f:139).
+/* Replaces FFTR2D (source/fft/fftr2d.f:7-8), called by ARRFFTR (arr/arrfftr.f:139-140).
  * WORK, WORK2 and RWORK are accepted for signature compatibility and not touched. */
 void fftr2d_(float *rarray, float *xarray, float *work, float *work2, float *rwork, int *nx,
              int *ny, int *fnu, int *nv, int *dir);
 
-/* Replaces PIXCOR2D (source/pix/pixcor2d.f:7-8), called by IMGGRIDC (img/imggridc.f:384). */
+/* Replaces PIXCOR2D (source/pix/pixcor2d.f:7-8), called by IMGGRIDC (img/imggridc.f:96-97). */
 void pixcor2d_(float *in, int *nx, int *ny, float *cf, int *cflen, char *mode, float *out,
                float *cenx, float *ceny, size_t mode_len);
 
-/* Replaces PIX2DRCL (source/pix/pix2drcl.f:78-80), called by IMGCLEAN (img/imgclean.f:186). */
+/* Replaces PIX2DRCL (source/pix/pix2drcl.f:7-9), called by IMGCLEAN (img/imgclean.f:186). */
 void pix2drcl_(float *drt, float *psf, float *box, int *nx, int *ny, int *pnx, int *pny,
                float *gain, int *nsub, int *bsub, float *flux, float *cln, float *res,
                int *ansub, float *maxres, float *tflux, float *cflux, int *cx, int *cy);
 
-/* Replaces PIXISAMA (source/pix/pixisama.f:231), called by PIX2DRCL (pix/pix2drcl.f:146). */
+/* Replaces PIXISAMA (source/pix/pixisama.f:7), called by PIX2DRCL (pix/pix2drcl.f:75,87,135). */
 int pixisama_(int *n, float *a, int *i);
 
 /* Host-side tables the gridder's callers build (no GPU work):
- * GRDSF (source/grd/grdsf.f:306), GRDCF (source/grd/grdcf.f:211, called by VISGRID,
- * vis/visgrid.f:278) and GRDCCF (source/grd/grdccf.f:382, called by IMGGRIDC,
- * img/imggridc.f:363); codes 'SF' and 'BOX'. */
+ * GRDSF (source/grd/grdsf.f:7), GRDCF (source/grd/grdcf.f:7, called by VISGRID,
+ * vis/visgrid.f:100) and GRDCCF (source/grd/grdccf.f:7, called by IMGGRIDC,
+ * img/imggridc.f:75); codes 'SF' and 'BOX'. */
 double grdsf_(double *nu);
 void grdcf_(char *cfcode, float *cf, int *cfsupp, int *cfosamp, size_t cfcode_len);
 void grdccf_(char *ccfcode, float *ccf, int *ccflen, size_t ccfcode_len);
@@ -281,7 +281,7 @@ int sde_image_scale_by_inverse(sde_ctx *ctx, float *image, int64_t n, const floa
 /* Hogbom CLEAN (PIX2DRCL) on device arrays: drt, box, cln, res [ny][nx]; psf [pny][pnx];
  * cflux/cx/cy device arrays of |nsub| entries.  One persistent launch runs every
  * iteration; scalars come back in *out (host) after an internal synchronisation.
- * cancel_flag (host pinned or NULL) is polled like SYSINTRP (pix/pix2drcl.f:165). */
+ * cancel_flag (host pinned or NULL) is polled like SYSINTRP (pix/pix2drcl.f:94-99). */
 typedef struct {
     int ansub;
     float maxres, tflux;
@@ -352,7 +352,7 @@ int sde_model_image(sde_ctx *ctx, int ncomp, const char *types, const float *flu
                     int ny, float refx, float deltx, float refy, float delty, float *image);
 
 /* Clark CLEAN, the default algorithm of SDE's clean task: the CLARK branch of
- * task/clean.f:146-205 and IMGCCLEA (img/imgcclea.f) on device arrays.
+ * task/clean.f:147-205 and IMGCCLEA (img/imgcclea.f) on device arrays.
  *   dirty, psf  N x N images from uvmap (N a power of two, 64..8192; CRPIX = (N+1)/2, so
  *               IMGMAKEX's phase shift is zero).
  *   window      CRDHALF with BLC/TRC unset: w = N/2 pixels from N/4+1 on both axes;
@@ -394,8 +394,11 @@ int sde_clark(sde_ctx *ctx, const float *dirty, const float *psf, int n, const f
  * takes the same device arrays and returns the same results as sde_hogbom, on the caller's
  * stream (a cudaStream_t, 0 for the legacy stream, on the current device).  Its scratch --
  * partial maxima of at most 1024 CTAs per search, the grid barrier, status words and result
- * scalars, about 36 KB -- lives in one static device array that every GPU which loads the
- * library keeps until the process exits.  The first call on a device takes that array's
+ * scalars, about 36 KB -- lives in one static device array that comes with the library's
+ * device code: a GPU gets it when the library's module is loaded there (with CUDA's lazy
+ * module loading, at the first call on that GPU) and keeps it until the process exits, so
+ * make the first call at start-up, before an arena has taken all device memory.  The first
+ * call on a device, and the first after the caller resets it, also takes that array's
  * address (cudaGetSymbolAddress), so make it before any stream capture.  Every call shares
  * the array and the call clears what must start at zero; calls that overlap on the GPU (two
  * streams, two host threads) race on it and must be serialised by the caller.  Windows or
@@ -474,7 +477,7 @@ int sde_batch_read(const sde_batch *b, int i, int which, float *dst, int64_t n);
 int sde_isamax(sde_ctx *ctx, const float *a, int64_t n, int64_t *index_out);
 
 /* Visibilities from a FITS random-groups file: the FTS branch of
- * VISGET(NAME, FILENAME, STOKES, ...) (vis/visget.f:5, 40-46 -> FILGRPGE, VISSTD), for one
+ * VISGET(NAME, FILENAME, STOKES, ...) (vis/visget.f:7, 60-68 -> FILGRPGE, VISSTD), for one
  * Stokes parameter, into the arrays sde_plan_create takes.
  *   sde_uvfits_open     parses the header (host only, no CUDA call) and checks what
  *                       fts/ftsgrpre.f and vis/visstd.f check, with their messages

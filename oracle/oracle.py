@@ -122,6 +122,15 @@ def lib():
                                    f32p, f32p]
         L.orc64_uvmap_image.argtypes = [C.POINTER(Geom), C.c_int, f32p, f32p, f32p, c64p, f32p,
                                         C.c_int, f64p]
+        L.orc_point_vis_mt.argtypes = [C.c_int64, f32p, f32p, C.c_int, f64p, f64p, f64p, c64p, C.c_int]
+        L.orc_grdh2d_acc.argtypes = [c64p, f32p, f32p, f32p, f32p, C.c_int, C.c_int, C.c_float, C.c_float,
+                                     C.c_float, C.c_float, C.c_int, C.c_int, c64p, C.c_int, C.c_int,
+                                     C.c_int, f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, f64p,
+                                     C.POINTER(C.c_float), C.POINTER(C.c_double)]
+        L.orc_grdh2d_end.restype = C.c_int
+        L.orc_grdh2d_end.argtypes = [c64p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]
+        L.orc64_uvmap_image_mt.argtypes = [C.POINTER(Geom), C.c_int, f32p, f32p, f32p, c64p,
+                                           f32p, C.c_int, f64p, C.c_int]
         L.orc64_fftr2d_inv.argtypes = [c128p, f64p, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc64_dft_image.argtypes = [C.POINTER(Geom), C.c_int, f32p, f32p, c64p, f32p,
                                       C.c_int, f64p]
@@ -414,6 +423,49 @@ def uvmap_image64(g, u, v, w, vis, wt, psf):
     img = np.zeros((g.ny, g.nx), np.float64)
     lib().orc64_uvmap_image(C.byref(g), len(wt), _f32(u), _f32(v), _f32(w), _c64(vis),
                             _f32(wt), int(psf), img)
+    return img
+
+
+def point_vis(u, v, flux, l, m, nthreads=None):
+    """sum_k S_k exp(+2 pi i (u l_k + v m_k)) in double -> complex64, on host threads."""
+    nthreads = nthreads or max(1, min(os.cpu_count() or 1, 64))
+    u, v = _f32(u), _f32(v)
+    out = np.empty(len(u), np.complex64)
+    f64 = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+    lib().orc_point_vis_mt(len(u), u, v, len(flux), f64(flux), f64(l), f64(m), out, int(nthreads))
+    return out
+
+
+class Grdh2dParts:
+    """GRDH2D over consecutive visibility ranges (orc_grdh2d_acc / orc_grdh2d_end): the grid
+    equals one orc_grdh2d call over all of them."""
+
+    def __init__(self, g, cf=None, psf=False):
+        if cf is None:
+            cf, _, _ = grdcf()
+        self.g, self.cf, self.psf = g, cf, int(psf)
+        self.grid = np.zeros((g.nv, g.nu), np.complex64)
+        self.sw, self.lsw = C.c_float(0.0), C.c_double(0.0)
+        self.shift = np.ascontiguousarray(np.array(list(g.shift)), np.float64)
+
+    def add(self, vis, wt, u, v, w, i0, i1):
+        g = self.g
+        lib().orc_grdh2d_acc(_c64(vis), _f32(wt), _f32(u), _f32(v), _f32(w), int(i0), int(i1),
+                             g.uscale, 0.0, g.vscale, 0.0, g.uorigin, g.vorigin, self.grid,
+                             self.psf, g.nu, g.nv, self.cf, 3, 128, self.cf, 3, 128, self.shift,
+                             C.byref(self.sw), C.byref(self.lsw))
+
+    def end(self):
+        g = self.g
+        return lib().orc_grdh2d_end(self.grid, g.nu, g.nv, g.uorigin, g.vorigin, 3, self.lsw.value)
+
+
+def uvmap_image64_mt(g, u, v, w, vis, wt, psf, nthreads=None):
+    """uvmap_image64 on host threads (the same grid; used at full benchmark sizes)."""
+    nthreads = nthreads or max(1, min(os.cpu_count() or 1, 64))
+    img = np.zeros((g.ny, g.nx), np.float64)
+    lib().orc64_uvmap_image_mt(C.byref(g), len(wt), _f32(u), _f32(v), _f32(w), _c64(vis),
+                               _f32(wt), int(psf), img, int(nthreads))
     return img
 
 

@@ -1,5 +1,8 @@
 """Dirty-image error against the FP64 oracle on dense uv coverage.
 
+TEST INFRASTRUCTURE (a checker): used by tests/test_gpu_precision.py and by bench.py's
+precision legs; the product package never imports it.
+
 The uv coverage of the large single field (27 antennas, 8 h x 10 s x 64 channels) imaged
 on a small grid puts tens to thousands of visibilities in each cell, where the way cell sums
 are formed decides the error.  GRDH2D adds every visibility into its cell in REAL
@@ -17,9 +20,10 @@ import math
 
 import numpy as np
 
-from . import synth
-from ._abi import lib
-from .imaging import Geom, uvmap
+from oracle import oracle as O
+from sde_gb300 import synth
+from sde_gb300._abi import lib
+from sde_gb300.imaging import Geom, uvmap
 
 
 def dense_case(stride=8, n_src=20, seed_offset=0):
@@ -40,7 +44,6 @@ def _window(n):
 
 def study(ctx, data, imsize=512, cell=4.0, vdec=40.0, reference=True):
     """Errors vs the FP64 oracle (natural weights, uvmap normalisation by the PSF peak)."""
-    from oracle import oracle as O
     O.lib()
     torch = ctx.torch
     u, v, w, vis, wt = data

@@ -27,7 +27,7 @@ int orc_fftpwr2(int i) {
     return p;
 }
 
-/* grd/grdsf.f:338-372: prolate spheroidal m=6, alpha=1 rational approximation */
+/* grd/grdsf.f:46-73: prolate spheroidal m=6, alpha=1 rational approximation */
 double orc_grdsf(double nu) {
     static const double P[2][5] = {
         {8.203343e-2, -3.644705e-1, 6.278660e-1, -5.335581e-1, 2.312756e-1},
@@ -53,7 +53,7 @@ double orc_grdsf(double nu) {
     return (bot != 0.0) ? top / bot : 0.0;
 }
 
-/* grd/grdcf.f:245-294.  code_sf: 1 = 'SF', 0 = 'BOX'.  cf must hold 1+8*129 floats
+/* grd/grdcf.f:41-90.  code_sf: 1 = 'SF', 0 = 'BOX'.  cf must hold 1+8*129 floats
  * (vis/visgrid.f CFLEN); CF(CFOFFSET+I) == cf[CFOFFSET-1+I]. */
 void orc_grdcf(int code_sf, float *cf, int *cfsupp, int *cfosamp) {
     int osamp = 128, supp, off;
@@ -89,7 +89,7 @@ void orc_grdcf(int code_sf, float *cf, int *cfsupp, int *cfosamp) {
     *cfosamp = osamp;
 }
 
-/* grd/grdccf.f:423-427 ('SF' branch); 'BOX' (grdccf.f:417-422) uses SINC(0.5*PI*NU). */
+/* grd/grdccf.f:48-52 ('SF' branch); 'BOX' (grd/grdccf.f:42-47) uses SINC(0.5*PI*NU). */
 void orc_grdccf(int code_sf, float *ccf, int ccflen) {
     if (code_sf) {
         for (int i = 1; i <= ccflen; i++) {
@@ -152,7 +152,7 @@ static int doshift_of(const double *shift) {
     return (SH(1, 1) != 1.0) || (SH(2, 2) != 1.0) || (SH(3, 3) != 1.0);
 }
 
-/* FP32 uv -> cell for the weighting routines: grd/grduwt2d.f:92-111 (and grdruw2d.f:304-323).
+/* FP32 uv -> cell for the weighting routines: grd/grduwt2d.f:92-111 (and grd/grdruw2d.f:134-153).
  * Returns 0 and the 1-based cell if on the grid, else -1. */
 static int wcell(const float *u, const float *v, const float *w, int i, float uscale,
                  float uoffset, float vscale, float voffset, int uorigin, int vorigin,
@@ -228,7 +228,7 @@ void orc_grduwt2d(const float *wt, const float *u, const float *v, const float *
     if (ndrop) *ndrop = nd;
 }
 
-/* grd/grdruw2d.f:257-419 (robust weighting).  rmode: "NORM", "ABS", "NONE", "AZ-NORM". */
+/* grd/grdruw2d.f:97-242 (robust weighting).  rmode: "NORM", "ABS", "NONE", "AZ-NORM". */
 int orc_grdruw2d(const float *wt, const float *u, const float *v, const float *w, int nvis,
                  float uscale, float uoffset, float vscale, float voffset, int uorigin,
                  int vorigin, float *newwt, float *gwt, int nu, int nv, const double *shift,
@@ -314,21 +314,23 @@ int orc_grdruw2d(const float *wt, const float *u, const float *v, const float *w
     return ORC_OK;
 }
 
-/* grd/grdh2d.f:89-226 -- the 2-D gridder (shifted by SUPPU, symmetrised, normalised). */
-int orc_grdh2d(const float *vis, const float *wt, const float *u, const float *v, const float *w,
-               int nvis, float uscale, float uoffset, float vscale, float voffset, int uorigin,
-               int vorigin, float *gvis, int psf, int nu, int nv, const float *gridfnu, int suppu,
-               int osampu, const float *gridfnv, int suppv, int osampv, const double *shift,
-               float *sumwt, double *lsumwt_out) {
+/* grd/grdh2d.f:89-226 -- the 2-D gridder (shifted by SUPPU, symmetrised, normalised).
+ * Written as three parts -- zero the grid, accumulate visibilities i0..i1-1 in order
+ * (grdh2d.f:110-189), finalize (grdh2d.f:195-226) -- so that a caller may split the
+ * visibility loop into consecutive ranges and get the grid of one pass over all of them. */
+#define GRE(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu)]
+#define GIM(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu) + 1]
+void orc_grdh2d_acc(const float *vis, const float *wt, const float *u, const float *v,
+                    const float *w, int i0, int nvis, float uscale, float uoffset, float vscale,
+                    float voffset, int uorigin, int vorigin, float *gvis, int psf, int nu, int nv,
+                    const float *gridfnu, int suppu, int osampu, const float *gridfnv, int suppv,
+                    int osampv, const double *shift, float *sumwt_acc, double *lsumwt_acc) {
     const double twopi = (double)(8.0f * atanf(1.0f));
     const int cfoffset = (suppu + 1) * osampu + 1;
     const int doshift = doshift_of(shift);
-    for (size_t k = 0; k < 2 * (size_t)nu * nv; k++) gvis[k] = 0.0f;
-    double lsumwt = 0.0;
-    float swt = 0.0f;
-#define GRE(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu)]
-#define GIM(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu) + 1]
-    for (int i = 0; i < nvis; i++) {
+    double lsumwt = *lsumwt_acc;
+    float swt = *sumwt_acc;
+    for (int i = i0; i < nvis; i++) {
         if (wt[i] <= 0.0f) continue;
         double ug = (double)u[i], vg = (double)v[i], wg = (double)w[i];
         double ucell, vcell;
@@ -383,8 +385,12 @@ int orc_grdh2d(const float *vis, const float *wt, const float *u, const float *v
             }
         }
     }
-    if (sumwt) *sumwt = swt;
-    if (lsumwt_out) *lsumwt_out = lsumwt;
+    *sumwt_acc = swt;
+    *lsumwt_acc = lsumwt;
+}
+
+int orc_grdh2d_end(float *gvis, int nu, int nv, int uorigin, int vorigin, int suppu,
+                   double lsumwt) {
     if (lsumwt == 0.0) return ORC_ENOWEIGHT;
     /* Symmetrize: grd/grdh2d.f:202-214 */
     int ucen = uorigin + suppu, vcen = vorigin;
@@ -411,9 +417,25 @@ int orc_grdh2d(const float *vis, const float *wt, const float *u, const float *v
             GIM(ug, vg) = 0.0f;
         }
     }
+    return ORC_OK;
+}
 #undef GRE
 #undef GIM
-    return ORC_OK;
+
+int orc_grdh2d(const float *vis, const float *wt, const float *u, const float *v, const float *w,
+               int nvis, float uscale, float uoffset, float vscale, float voffset, int uorigin,
+               int vorigin, float *gvis, int psf, int nu, int nv, const float *gridfnu, int suppu,
+               int osampu, const float *gridfnv, int suppv, int osampv, const double *shift,
+               float *sumwt, double *lsumwt_out) {
+    for (size_t k = 0; k < 2 * (size_t)nu * nv; k++) gvis[k] = 0.0f;
+    double lsumwt = 0.0;
+    float swt = 0.0f;
+    orc_grdh2d_acc(vis, wt, u, v, w, 0, nvis, uscale, uoffset, vscale, voffset, uorigin, vorigin,
+                   gvis, psf, nu, nv, gridfnu, suppu, osampu, gridfnv, suppv, osampv, shift, &swt,
+                   &lsumwt);
+    if (sumwt) *sumwt = swt;
+    if (lsumwt_out) *lsumwt_out = lsumwt;
+    return orc_grdh2d_end(gvis, nu, nv, uorigin, vorigin, suppu, lsumwt);
 }
 
 /* grd/grddeh2d.f:77-200 -- the 2-D degridder. */
@@ -516,7 +538,7 @@ void orc_grddeh2d(float *vis, float *wt, const float *u, const float *v, const f
     if (nbad_out) *nbad_out = nbad;
 }
 
-/* fft/fftx.f:261-452 -- radix-2 complex FFT with quarter-length tables (Newman/AIPS). */
+/* fft/fftx.f:84-275 -- radix-2 complex FFT with quarter-length tables (Newman/AIPS). */
 void orc_fftx(float *x, float *wk, int m, int isig) {
 #define X1(i) x[2 * ((i)-1)]
 #define X2(i) x[2 * ((i)-1) + 1]
@@ -649,7 +671,7 @@ void orc_fftx(float *x, float *wk, int m, int isig) {
 #undef W2
 }
 
-/* fft/fftx1d.f:508-547 (power-of-two branch) */
+/* fft/fftx1d.f:57-92 (power-of-two branch) */
 void orc_fftx1d(float *xarray, float *xwork, float *xwork2, int nx, int dir) {
     int icen = (nx + 1) / 2, ioff = nx - icen + 1;
     for (int ix = 1; ix <= icen - 1; ix++) {
@@ -736,7 +758,7 @@ void orc_fftr(float *R, float *C, float *work, int n, int f) {
 #undef CC
 }
 
-/* fft/fftr1d.f:253-299 (power-of-two branch).  rwork needs nx+2 floats, xwork nx/2 complex. */
+/* fft/fftr1d.f:63-109 (power-of-two branch).  rwork needs nx+2 floats, xwork nx/2 complex. */
 void orc_fftr1d(float *rarray, float *xarray, float *rwork, float *xwork, int nx, int dir) {
     int icen = (nx + 1) / 2;
     if (dir > 0) {
@@ -754,7 +776,7 @@ void orc_fftr1d(float *rarray, float *xarray, float *rwork, float *xwork, int nx
     }
 }
 
-/* fft/fftr1d2.f:137-184 */
+/* fft/fftr1d2.f:41-84 */
 void orc_fftr1d2(float *rarray, float *xarray, float *xwork, float *xwork2, float *rwork,
                  int nx, int fnu, int dir) {
     if (dir > 0) {
@@ -835,7 +857,7 @@ void orc_pixcor2d(const float *in, int nx, int ny, const float *cf, int cflen, i
     }
 }
 
-/* pix/pixisama.f:269-277 -- first index of strictly greatest |A|, 1-based; I if none */
+/* pix/pixisama.f:45-53 -- first index of strictly greatest |A|, 1-based; I if none */
 int orc_pixisama(int n, const float *a, int i) {
     int r = i;
     float maxval = 0.0f;
@@ -848,7 +870,7 @@ int orc_pixisama(int n, const float *a, int i) {
     return r;
 }
 
-/* pix/pix2drcl.f:134-215 -- Hogbom CLEAN minor cycle.  A PSF read whose flat
+/* pix/pix2drcl.f:67-142 -- Hogbom CLEAN minor cycle.  A PSF read whose flat
  * column-major offset falls outside the PSF array reads 0 (the reference reads
  * whatever memory follows; no caller in the reference does that). */
 void orc_pix2drcl(const float *drt, const float *psf, const float *box, int nx, int ny, int pnx,
@@ -906,7 +928,7 @@ void orc_pixrscal(const float *in, float scale, float offset, float *out, int64_
  * Task-level drivers.
  * img/imgmake.f (CDELT = -/+ CELLSIZE/3600, CRPIX = (N+1)/2), fft/fftconja.f:159-163 and
  * fft/fftconj.f (FNU = pow2(N), NU = FNU/2+1, CDELT = 1/(D2R*WIDTH), RPIX = 1, (NV+1)/2),
- * vis/visgrid.f:317-322 (USCALE = 1/CDELT, UORIGIN = NINT(RPIX)). */
+ * vis/visgrid.f:148-153 (USCALE = 1/CDELT, UORIGIN = NINT(RPIX)). */
 void orc_make_geom(const orc_uvmap_params *p, orc_geom *g) {
     const float PI = 3.141592654f;
     const float D2R = PI / 180.0f;
@@ -1227,7 +1249,7 @@ void orc64_dft_image(const orc_geom *g, int nvis, const float *u, const float *v
 }
 
 /* ---------------------------------------------------------------------------------------
- * Clark CLEAN: the CLARK branch of task/clean.f:146-205 (CRDHALF window, IMGMAKEX,
+ * Clark CLEAN: the CLARK branch of task/clean.f:147-205 (CRDHALF window, IMGMAKEX,
  * IMGSUBPS) and IMGCCLEA's major/minor cycle loop (img/imgcclea.f:210-290).
  */
 
@@ -2140,4 +2162,268 @@ int orc_grduruwt(const float *u, const float *v, const float *w, const float *wt
     free(links);
     free(bsum);
     return rc;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Threaded FP64 oracle for full-size images (64.7 M visibilities at 4096^2): the same
+ * gridder, inverse transform and correction as orc64_uvmap_image, split over host threads.
+ * Gridding: thread t owns the grid rows of 64-row bands b with b mod T == t and scans every
+ * visibility, adding only the taps of its rows, so each cell still sums its contributions
+ * in visibility order -- the grid equals the serial orc64_grdh2d's bit for bit.  LSUMWT is
+ * summed by one more thread in the serial loop's order.  Columns and rows of the transform
+ * are independent and split over threads. */
+#include <pthread.h>
+
+typedef struct {
+    const orc_geom *g;
+    const float *vis, *wt, *u, *v, *w;
+    int nvis, psf, t, nt;
+    const float *cf;
+    int supp, osamp;
+    double *gvis;
+    double lsumwt;
+} g64_job;
+
+/* the per-visibility geometry of orc64_grdh2d; returns 0 when the point is skipped */
+static int g64_cell(const g64_job *J, int i, double *fr, double *fi, int *nuc, int *nvc, int *delui,
+                    int *delvi) {
+    const orc_geom *g = J->g;
+    const double *shift = g->shift;
+    const int cfoffset = (J->supp + 1) * J->osamp + 1;
+    if (J->wt[i] <= 0.0f) return 0;
+    double ug = J->u[i], vg = J->v[i], wg = J->w[i], ucell, vcell;
+    if (doshift_of(shift)) {
+        double ul = SH(1, 1) * ug + SH(2, 1) * vg + SH(3, 1) * wg;
+        double vl = SH(1, 2) * ug + SH(2, 2) * vg + SH(3, 2) * wg;
+        double wl = SH(1, 3) * ug + SH(2, 3) * vg + SH(3, 3) * wg;
+        double ph = 2.0 * M_PI * (wl - wg), c = cos(ph), s = -sin(ph);
+        double a = J->vis[2 * i], b = J->vis[2 * i + 1];
+        *fr = a * c - b * s;
+        *fi = a * s + b * c;
+        ucell = (double)g->uscale * ul;
+        vcell = (double)g->vscale * vl;
+    } else {
+        *fr = J->vis[2 * i];
+        *fi = J->vis[2 * i + 1];
+        ucell = (double)g->uscale * ug;
+        vcell = (double)g->vscale * vg;
+    }
+    if (ucell > 0.0) {
+        *fi = -*fi;
+        ucell += g->uorigin;
+        vcell += g->vorigin;
+    } else {
+        ucell = -ucell + g->uorigin;
+        vcell = -vcell + g->vorigin;
+    }
+    if (J->psf) { *fr = 1.0; *fi = 0.0; }
+    *nuc = orc_nint_d(ucell);
+    *nvc = orc_nint_d(vcell);
+    if (*nuc + 2 * J->supp > g->nu || *nvc + J->supp > g->nv || *nvc - J->supp < 1) return 0;
+    *delui = orc_nint_d((double)J->osamp * ((double)*nuc - ucell)) + cfoffset;
+    *delvi = orc_nint_d((double)J->osamp * ((double)*nvc - vcell)) + cfoffset;
+    return 1;
+}
+
+static void *g64_rows(void *arg) {
+    g64_job *J = (g64_job *)arg;
+    const int nu = J->g->nu, supp = J->supp, osamp = J->osamp;
+    const float *cf = J->cf;
+    for (int i = 0; i < J->nvis; i++) {
+        double fr, fi;
+        int nuc, nvc, delui, delvi;
+        if (!g64_cell(J, i, &fr, &fi, &nuc, &nvc, &delui, &delvi)) continue;
+        if (J->t == J->nt) { /* the LSUMWT thread */
+            for (int offv = -supp; offv <= supp; offv++)
+                for (int offu = -supp; offu <= supp; offu++)
+                    J->lsumwt += (double)J->wt[i] * (double)cf[delui + osamp * offu - 1] *
+                                 (double)cf[delvi + osamp * offv - 1];
+            continue;
+        }
+        for (int offv = -supp; offv <= supp; offv++) {
+            const int vv = nvc + offv;
+            if (((vv - 1) / 64) % J->nt != J->t) continue;
+            double *row = J->gvis + 2 * (size_t)(vv - 1) * (size_t)nu;
+            for (int offu = -supp; offu <= supp; offu++) {
+                double uvwt = (double)J->wt[i] * (double)cf[delui + osamp * offu - 1] *
+                              (double)cf[delvi + osamp * offv - 1];
+                const size_t k = (size_t)(nuc + supp + offu - 1);
+                row[2 * k] += uvwt * fr;
+                row[2 * k + 1] += uvwt * fi;
+            }
+        }
+    }
+    return NULL;
+}
+
+typedef struct {
+    const double *x;
+    double *xt, *image;
+    int nx, ny, fnu, nv, t, nt, phase;
+} f64_job;
+
+static void *f64_part(void *arg) {
+    f64_job *J = (f64_job *)arg;
+    const int nu = J->fnu / 2 + 1, nv = J->nv, fnu = J->fnu;
+    if (J->phase == 0) { /* columns */
+        double *col = (double *)malloc(2 * (size_t)nv * sizeof(double));
+        const int cv = (nv + 1) / 2 - 1;
+        for (int ix = J->t; ix < nu; ix += J->nt) {
+            for (int j = 0; j < nv; j++) {
+                int src = (j + cv) % nv;
+                col[2 * j] = J->x[2 * ((size_t)src * nu + ix)];
+                col[2 * j + 1] = J->x[2 * ((size_t)src * nu + ix) + 1];
+            }
+            fft64(col, nv, +1);
+            for (int j = 0; j < nv; j++) {
+                int dst = (j + cv) % nv;
+                J->xt[2 * ((size_t)dst * nu + ix)] = col[2 * j] / nv;
+                J->xt[2 * ((size_t)dst * nu + ix) + 1] = col[2 * j + 1] / nv;
+            }
+        }
+        free(col);
+    } else { /* rows */
+        double *row = (double *)malloc(2 * (size_t)fnu * sizeof(double));
+        const int cu = (fnu + 1) / 2 - 1;
+        const int ibegy = (nv + 1) / 2 - (J->ny + 1) / 2 + 1;
+        for (int iy = J->t; iy < J->ny; iy += J->nt) {
+            const double *xr = J->xt + 2 * (size_t)(iy + ibegy - 1) * nu;
+            for (int k = 0; k < fnu; k++) {
+                double re, im;
+                if (k == 0) { re = xr[0]; im = 0.0; }
+                else if (k == fnu / 2) { re = xr[2 * k]; im = 0.0; }
+                else if (k < fnu / 2) { re = xr[2 * k]; im = xr[2 * k + 1]; }
+                else { re = xr[2 * (fnu - k)]; im = -xr[2 * (fnu - k) + 1]; }
+                row[2 * k] = re;
+                row[2 * k + 1] = im;
+            }
+            fft64(row, fnu, +1);
+            const int ioff = (fnu - J->nx) / 2;
+            for (int ix = 0; ix < J->nx; ix++) {
+                int n = ((ix + ioff) - cu + fnu) % fnu;
+                J->image[(size_t)iy * J->nx + ix] = row[2 * n] / fnu;
+            }
+        }
+        free(row);
+    }
+    return NULL;
+}
+
+void orc64_uvmap_image_mt(const orc_geom *g, int nvis, const float *u, const float *v,
+                          const float *w, const float *vis, const float *wt, int psf,
+                          double *image, int nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    const int nu = g->nu, nv = g->nv;
+    double *gvis = (double *)calloc(2 * (size_t)nu * nv, sizeof(double));
+    float cf[1 + 8 * 129];
+    int supp, osamp;
+    orc_grdcf(1, cf, &supp, &osamp);
+    g64_job *jobs = (g64_job *)calloc((size_t)nthreads + 1, sizeof(g64_job));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads + 1, sizeof(pthread_t));
+    for (int t = 0; t <= nthreads; t++) {
+        g64_job J = {g, vis, wt, u, v, w, nvis, psf, t, nthreads, cf, supp, osamp, gvis, 0.0};
+        jobs[t] = J;
+        pthread_create(&th[t], NULL, g64_rows, &jobs[t]);
+    }
+    for (int t = 0; t <= nthreads; t++) pthread_join(th[t], NULL);
+    const double lsumwt = jobs[nthreads].lsumwt;
+    if (lsumwt == 0.0) {
+        memset(image, 0, sizeof(double) * (size_t)g->nx * g->ny);
+        free(gvis); free(jobs); free(th);
+        return;
+    }
+    /* symmetrise, shift left by SUPPU and normalise: orc64_grdh2d's serial tail */
+#define GRE(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu)]
+#define GIM(uu, vv) gvis[2 * (((size_t)(uu)-1) + (size_t)((vv)-1) * (size_t)nu) + 1]
+    int ucen = g->uorigin + supp, vcen = g->vorigin;
+    for (int offv = -nv / 2 + 1; offv <= nv / 2 - 1; offv++)
+        for (int offu = 1; offu <= supp; offu++) {
+            GRE(ucen + offu, vcen + offv) += GRE(ucen - offu, vcen - offv);
+            GIM(ucen + offu, vcen + offv) -= GIM(ucen - offu, vcen - offv);
+        }
+    for (int offv = 0; offv <= nv / 2 - 1; offv++) {
+        GRE(ucen, vcen + offv) += GRE(ucen, vcen - offv);
+        GIM(ucen, vcen + offv) -= GIM(ucen, vcen - offv);
+        GRE(ucen, vcen - offv) = GRE(ucen, vcen + offv);
+        GIM(ucen, vcen - offv) = -GIM(ucen, vcen + offv);
+    }
+    double scale = (double)(nu - 1) * (double)nv / lsumwt;
+    for (int vg = 1; vg <= nv; vg++) {
+        for (int ug = 1; ug <= nu - supp; ug++) {
+            GRE(ug, vg) = scale * GRE(ug + supp, vg);
+            GIM(ug, vg) = scale * GIM(ug + supp, vg);
+        }
+        for (int ug = nu - supp + 1; ug <= nu; ug++) { GRE(ug, vg) = 0.0; GIM(ug, vg) = 0.0; }
+    }
+#undef GRE
+#undef GIM
+    double *xt = (double *)malloc(2 * (size_t)nu * nv * sizeof(double));
+    f64_job *fj = (f64_job *)calloc((size_t)nthreads, sizeof(f64_job));
+    for (int phase = 0; phase < 2; phase++) {
+        for (int t = 0; t < nthreads; t++) {
+            f64_job J = {gvis, xt, image, g->nx, g->ny, g->fnu, nv, t, nthreads, phase};
+            fj[t] = J;
+            pthread_create(&th[t], NULL, f64_part, &fj[t]);
+        }
+        for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    }
+    free(xt);
+    free(gvis);
+    free(fj);
+    free(jobs);
+    free(th);
+    int ccflen = 1 + orc_fftpwr2(g->nx > g->ny ? g->nx : g->ny) / 2;
+    int fnx = orc_fftpwr2(g->nx), fny = orc_fftpwr2(g->ny);
+    double sx = (double)(ccflen - 1) * 2.0 / fnx, sy = (double)(ccflen - 1) * 2.0 / fny;
+    for (int iy = 1; iy <= g->ny; iy++) {
+        int icy = 1 + abs(orc_nint_d(sy * (iy - g->ceny)));
+        double cy = orc_grdsf((double)(icy - 1) / (double)(ccflen - 1));
+        for (int ix = 1; ix <= g->nx; ix++) {
+            int icx = 1 + abs(orc_nint_d(sx * (ix - g->cenx)));
+            double cx = orc_grdsf((double)(icx - 1) / (double)(ccflen - 1));
+            image[(size_t)(iy - 1) * g->nx + (ix - 1)] /= (cx * cy);
+        }
+    }
+}
+
+/* Visibilities of point sources, V = sum_k S_k exp(+2 pi i (u l_k + v m_k)) in double, stored
+ * complex64 -- the benchmark's synthetic sky for the CPU runs (the sign of SDE's direct
+ * transform, vis/visdftp2.f:101-107), on nthreads host threads over contiguous ranges. */
+typedef struct {
+    int64_t i0, i1;
+    const float *u, *v;
+    int nsrc;
+    const double *flux, *l, *m;
+    float *out;
+} pv_job;
+
+static void *pv_part(void *arg) {
+    pv_job *J = (pv_job *)arg;
+    const double tp = 2.0 * M_PI;
+    for (int64_t i = J->i0; i < J->i1; i++) {
+        double re = 0.0, im = 0.0, uu = J->u[i], vv = J->v[i];
+        for (int k = 0; k < J->nsrc; k++) {
+            double ph = tp * (uu * J->l[k] + vv * J->m[k]);
+            re += J->flux[k] * cos(ph);
+            im += J->flux[k] * sin(ph);
+        }
+        J->out[2 * i] = (float)re;
+        J->out[2 * i + 1] = (float)im;
+    }
+    return NULL;
+}
+
+void orc_point_vis_mt(int64_t n, const float *u, const float *v, int nsrc, const double *flux,
+                      const double *l, const double *m, float *out, int nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    pv_job jobs[256];
+    for (int t = 0; t < nthreads; t++) {
+        pv_job J = {n * t / nthreads, n * (t + 1) / nthreads, u, v, nsrc, flux, l, m, out};
+        jobs[t] = J;
+        pthread_create(&th[t], NULL, pv_part, &jobs[t]);
+    }
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
 }

@@ -13,8 +13,8 @@
  *
  * Documented deviations from the reference source:
  *   - FFTX's bit-reverse table is sized to M (reference IBITRV(4096) overflows at
- *     M = 8192, fft/fftx.f:289), and FFTX/FFTR tables are recomputed on every call
- *     (the reference keeps them in non-SAVEd locals, fft/fftx.f:289-292, fft/fftr.f:87).
+ *     M = 8192, fft/fftx.f:112), and FFTX/FFTR tables are recomputed on every call
+ *     (the reference keeps them in non-SAVEd locals, fft/fftx.f:112-115, fft/fftr.f:87).
  */
 #ifndef SDE_ORACLE_H
 #define SDE_ORACLE_H
@@ -26,15 +26,15 @@ extern "C" {
 /* error codes returned where the reference calls ERRREPOR */
 #define ORC_OK 0
 #define ORC_ENOWEIGHT 1   /* grd/grdh2d.f:195-197 'No weight!'          */
-#define ORC_EBADMODE 2    /* grd/grdruw2d.f:361 'Unrecognized RMODE'      */
+#define ORC_EBADMODE 2    /* grd/grdruw2d.f:191 'Unrecognized RMODE'      */
 #define ORC_EBADARG 3
 
-double orc_grdsf(double nu);                                   /* grd/grdsf.f:306-375   */
+double orc_grdsf(double nu);                                   /* grd/grdsf.f:7-76      */
 int    orc_fftpwr2(int i);                                     /* fft/fftpwr2.f:7-42    */
 int    orc_nint_f(float x);                                    /* Fortran NINT(REAL)    */
 int    orc_nint_d(double x);                                   /* Fortran NINT(DOUBLE)  */
-void   orc_grdcf(int code_sf, float *cf, int *cfsupp, int *cfosamp); /* grd/grdcf.f:211-299 */
-void   orc_grdccf(int code_sf, float *ccf, int ccflen);        /* grd/grdccf.f:382-443  */
+void   orc_grdcf(int code_sf, float *cf, int *cfsupp, int *cfosamp); /* grd/grdcf.f:7-95    */
+void   orc_grdccf(int code_sf, float *ccf, int ccflen);        /* grd/grdccf.f:7-68     */
 void   orc_crdshift(double vra_deg, double vdec_deg, double ira_deg, double idec_deg,
                     float vrota3_deg, double *shift);          /* crd/crdshift.f:7-169  */
 
@@ -46,20 +46,29 @@ int orc_grdruw2d(const float *wt, const float *u, const float *v, const float *w
                  float uscale, float uoffset, float vscale, float voffset, int uorigin,
                  int vorigin, float *newwt, float *gwt, int nu, int nv, const double *shift,
                  const char *rmode, const float *robust, float ds, int *ndrop,
-                 double *sumwt_out, double *sumlocwt_out, float *f2_out); /* grd/grdruw2d.f:177-422 */
+                 double *sumwt_out, double *sumlocwt_out, float *f2_out); /* grd/grdruw2d.f:7-252 */
 
 int orc_grdh2d(const float *vis, const float *wt, const float *u, const float *v, const float *w,
                int nvis, float uscale, float uoffset, float vscale, float voffset, int uorigin,
                int vorigin, float *gvis, int psf, int nu, int nv, const float *gridfnu, int suppu,
                int osampu, const float *gridfnv, int suppv, int osampv, const double *shift,
-               float *sumwt, double *lsumwt_out);              /* grd/grdh2d.f:7-229    */
+               float *sumwt, double *lsumwt_out);
+/* GRDH2D in parts: accumulate visibilities i0..nvis-1 into a zeroed grid (sums carried in
+ * *sumwt_acc / *lsumwt_acc), then finalize with the total LSUMWT */
+void orc_grdh2d_acc(const float *vis, const float *wt, const float *u, const float *v,
+                    const float *w, int i0, int nvis, float uscale, float uoffset, float vscale,
+                    float voffset, int uorigin, int vorigin, float *gvis, int psf, int nu, int nv,
+                    const float *gridfnu, int suppu, int osampu, const float *gridfnv, int suppv,
+                    int osampv, const double *shift, float *sumwt_acc, double *lsumwt_acc);
+int  orc_grdh2d_end(float *gvis, int nu, int nv, int uorigin, int vorigin, int suppu,
+                    double lsumwt);              /* grd/grdh2d.f:7-229    */
 void orc_grddeh2d(float *vis, float *wt, const float *u, const float *v, const float *w, int nvis,
                   float uscale, float uoffset, float vscale, float voffset, int uorigin,
                   int vorigin, const float *gvis, int nu, int nv, const float *intfnu, int suppu,
                   int osampu, const float *intfnv, int suppv, int osampv, const double *shift,
                   int *nbad);                                  /* grd/grddeh2d.f:7-204  */
 
-void orc_fftx(float *x, float *w, int m, int isig);            /* fft/fftx.f:261-452    */
+void orc_fftx(float *x, float *w, int m, int isig);            /* fft/fftx.f:84-275     */
 void orc_fftx1d(float *xarray, float *xwork, float *xwork2, int nx, int dir); /* fft/fftx1d.f */
 void orc_fftr(float *r, float *c, float *work, int n, int f);  /* fft/fftr.f:60-176     */
 void orc_fftr1d(float *rarray, float *xarray, float *rwork, float *xwork, int nx, int dir);
@@ -69,7 +78,7 @@ void orc_fftr2d(float *rarray, float *xarray, int nx, int ny, int fnu, int nv, i
 
 void orc_pixcor2d(const float *in, int nx, int ny, const float *cf, int cflen, int correct,
                   float *out, float cenx, float ceny);         /* pix/pixcor2d.f:7-71   */
-int  orc_pixisama(int n, const float *a, int i);               /* pix/pixisama.f:231-288 */
+int  orc_pixisama(int n, const float *a, int i);               /* pix/pixisama.f:7-64 */
 void orc_pix2drcl(const float *drt, const float *psf, const float *box, int nx, int ny, int pnx,
                   int pny, float gain, int nsub, int bsub, float flux, float *cln, float *res,
                   int *ansub, float *maxres, float *tflux, float *cflux, int *cx, int *cy);
@@ -173,6 +182,13 @@ int orc_modimg2d(int ncomp, const int *type, const float *flux, const float *ra,
 int  orc64_grdh2d(const float *vis, const float *wt, const float *u, const float *v,
                   const float *w, int nvis, const orc_geom *g, int psf, double *gvis);
 void orc64_fftr2d_inv(const double *xarray, double *image, int nx, int ny, int fnu, int nv);
+/* orc64_uvmap_image on nthreads host threads (identical grid; independent FFT lines) */
+/* point-source visibilities in double -> complex64 on nthreads threads (benchmark data) */
+void orc_point_vis_mt(int64_t n, const float *u, const float *v, int nsrc, const double *flux,
+                      const double *l, const double *m, float *out, int nthreads);
+void orc64_uvmap_image_mt(const orc_geom *g, int nvis, const float *u, const float *v,
+                          const float *w, const float *vis, const float *wt, int psf,
+                          double *image, int nthreads);
 void orc64_uvmap_image(const orc_geom *g, int nvis, const float *u, const float *v,
                        const float *w, const float *vis, const float *wt, int psf,
                        double *image);

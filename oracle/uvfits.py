@@ -1,5 +1,5 @@
 """CPU restatement of SDE's visibility load from a FITS random-groups file (the FTS branch of
-VISGET, vis/visget.f:40-46: FILGRPGE -> FTSGRPRE, then VISSTD), in numpy.
+VISGET, vis/visget.f:60-68: FILGRPGE -> FTSGRPRE, then VISSTD), in numpy.
 
 TEST INFRASTRUCTURE: only tests/ import this module.  The product (sde_gb300, libsdegpu's
 sde_uvfits_*) never imports or calls it.

@@ -28,8 +28,8 @@ extern "C" int sde_version(void) { return 1; }
 // ---------------------------------------------------------------------------------------
 // 'SF' tables on the host: the prolate spheroidal function m=6, alpha=1 by F. Schwab's
 // rational approximation (as in grd/grdsf.f), the gridding function (1-nu^2) psi(nu)
-// sampled 128x over support 3 and normalised to unit sum (grd/grdcf.f:257-294), and the
-// grid-correction table psi((i-1)/(CCFLEN-1)) (grd/grdccf.f:423-427).
+// sampled 128x over support 3 and normalised to unit sum (grd/grdcf.f:53-64, 84-90), and the
+// grid-correction table psi((i-1)/(CCFLEN-1)) (grd/grdccf.f:48-52).
 double sf_grdsf(double nu) {
     static const double P[2][5] = {
         {8.203343e-2, -3.644705e-1, 6.278660e-1, -5.335581e-1, 2.312756e-1},
@@ -1289,7 +1289,7 @@ extern "C" void grdruw2d_(float *wt, float *u, float *v, float *w, int *nvis, fl
     else if (fstr_eq(rmode, rmode_len, "NONE"))
         m = 4;
     else {
-        // the reference grids first, then rejects the mode (grd/grdruw2d.f:361)
+        // the reference grids first, then rejects the mode (grd/grdruw2d.f:190-192)
         report("Logic error", "GRDRUW2D", "Unrecognized RMODE");
         return;
     }

@@ -1,5 +1,5 @@
 // clark.cu -- Clark CLEAN (the default algorithm of SDE's clean task): the CLARK branch of
-// task/clean.f:146-205 (CRDHALF window, IMGMAKEX transfer function, IMGSUBPS beam patch and
+// task/clean.f:147-205 (CRDHALF window, IMGMAKEX transfer function, IMGSUBPS beam patch and
 // exterior sidelobe) and IMGCCLEA's loop (img/imgcclea.f:210-290).  A major cycle is:
 //   residual *= box, its extrema (ARRSTAT)                     k_clark_stats
 //   |residual| histogram of 1024 bins (PIXRABSH)               k_clark_hist

@@ -1,8 +1,8 @@
 // clean.cu -- Hogbom CLEAN minor cycle (PIX2DRCL), PIXISAMA, and the uvmap PSF-peak
 // normalisation (ARRSTAT max + ARRSCALE by 1/max).
 //
-// PIX2DRCL (pix/pix2drcl.f:138-203): RES = DRT*BOX; per iteration the first index of the
-// strictly largest |RES| (PIXISAMA, pix/pixisama.f:269-277), stop tests, component record,
+// PIX2DRCL (pix/pix2drcl.f:67-130): RES = DRT*BOX; per iteration the first index of the
+// strictly largest |RES| (PIXISAMA, pix/pixisama.f:45-53), stop tests, component record,
 // then RES -= (PNTSUB*PSF(OFFX-IX,OFFY-IY))*BOX over the whole window in FP32.  Here one
 // cooperative persistent launch runs every iteration: each CTA owns a contiguous slice of
 // the window, applies the previous component's subtraction to it with the same FP32
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
         g = block_best(g);
         // PIXISAMA returns 1 (index 0) when no |value| exceeds 0
         // every |value| >= 0 beats the -1 sentinel, so when nothing exceeds 0 the winner
-        // is index 0 -- PIXISAMA's default of 1 (pix/pixisama.f:269)
+        // is index 0 -- PIXISAMA's default of 1 (pix/pixisama.f:45)
         const int32_t ip = g.idx;
         const int pmx = 1 + ip % A.nx, pmy = 1 + ip / A.nx;
         maxres = g.v;
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
         if (stopped) A.out[0] = maxres;
     }
     if (!stopped) {
-        // final PIXISAMA over the residual (pix/pix2drcl.f:206-209)
+        // final PIXISAMA over the residual (pix/pix2drcl.f:134-138)
         Cand g{-1.0f, INT32_MAX, 0.0f};
         for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
             g = better(g, A.partial[cur * gridDim.x + b]);
@@ -322,7 +322,7 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
         return SDE_EINVAL;
     }
     SDE_CUDA_TRY(cudaSetDevice(ctx->device));
-    // PSF peak (pix/pix2drcl.f:146-151)
+    // PSF peak (pix/pix2drcl.f:73-80)
     int64_t ip1;
     SDE_TRY(sde_isamax(ctx, psf, (int64_t)pnx * pny, &ip1));
     int ipeak = (int)(ip1 - 1);
@@ -403,17 +403,53 @@ static __device__ __align__(256) NoAllocScratch g_clean_scratch;
 
 // Host-side copies of g_clean_scratch's device address, one per device.  The array's name in
 // host code only stands in for the symbol; the address every kernel receives comes from
-// cudaGetSymbolAddress, taken once per device with that device current.
+// cudaGetSymbolAddress, taken with that device current the first time the device is used.
+// It is taken again when the device's current context has changed since (a caller's
+// cudaDeviceReset destroys the primary context, and the next one loads the module, and with
+// it the array, anew -- possibly at another address).
 static NoAllocScratch *g_clean_scratch_dev[64];
+static unsigned long long g_clean_scratch_ctx[64];
 static std::mutex g_clean_scratch_mu;
+
+// unique ID of the calling thread's current CUDA context (driver API, resolved at run time)
+static int current_context_id(unsigned long long *id) {
+    typedef CUresult (*GetCurrentFn)(CUcontext *);
+    typedef CUresult (*GetIdFn)(CUcontext, unsigned long long *);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) !=
+                cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) !=
+                cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b) {
+            sde_set_error("sde_hogbom_noalloc: driver context queries unavailable");
+            return SDE_ECUDA;
+        }
+        get_current = (GetCurrentFn)a;
+        get_id = (GetIdFn)b;
+    }
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, id) != CUDA_SUCCESS) {
+        sde_set_error("sde_hogbom_noalloc: no current CUDA context");
+        return SDE_ECUDA;
+    }
+    return SDE_OK;
+}
 
 static int clean_scratch_address(int dev, NoAllocScratch **out) {
     if (dev < 0 || dev >= 64) {
         sde_set_error("sde_hogbom_noalloc: device %d out of range", dev);
         return SDE_EINVAL;
     }
+    // make the device's primary context current on this thread (no allocation)
+    SDE_CUDA_TRY(cudaSetDevice(dev));
+    unsigned long long id = 0;
+    SDE_TRY(current_context_id(&id));
     std::lock_guard<std::mutex> lk(g_clean_scratch_mu);
-    if (!g_clean_scratch_dev[dev]) {
+    if (!g_clean_scratch_dev[dev] || g_clean_scratch_ctx[dev] != id) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_clean_scratch);
         if (e != cudaSuccess || !p) {
@@ -421,6 +457,7 @@ static int clean_scratch_address(int dev, NoAllocScratch **out) {
             return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? SDE_ENODEV : SDE_ECUDA;
         }
         g_clean_scratch_dev[dev] = (NoAllocScratch *)p;
+        g_clean_scratch_ctx[dev] = id;
     }
     *out = g_clean_scratch_dev[dev];
     return SDE_OK;
@@ -451,7 +488,7 @@ extern "C" int sde_hogbom_noalloc(void *stream, const float *drt, const float *p
     SDE_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     NoAllocScratch *S = nullptr;
     SDE_TRY(clean_scratch_address(dev, &S));
-    // PSF peak (pix/pix2drcl.f:146-151) with the partials in the static array
+    // PSF peak (pix/pix2drcl.f:73-80) with the partials in the static array
     int nbi = nsm * 2;
     if (nbi > NOALLOC_MAX_CTAS) nbi = NOALLOC_MAX_CTAS;
     k_isamax_part<<<nbi, CL_THREADS, 0, st>>>(psf, (int64_t)pnx * pny, S->isa_part);

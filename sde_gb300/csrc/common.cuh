@@ -40,8 +40,8 @@ void sde_set_error(const char *fmt, ...);
 // of one cell, accumulated in registers by one thread.
 constexpr int TILE = 64;
 constexpr int TILE_LOG2 = 6;
-constexpr int SUPP = 3;                 // 'SF' support (grd/grdcf.f:258)
-constexpr int OSAMP = 128;              // oversampling (grd/grdcf.f:245)
+constexpr int SUPP = 3;                 // 'SF' support (grd/grdcf.f:54)
+constexpr int OSAMP = 128;              // oversampling (grd/grdcf.f:41)
 constexpr int NTAP = 2 * SUPP + 1;      // 7
 constexpr int STILE = TILE + 2 * SUPP;  // 70: shared tile edge (grid and degrid)
 // The raw gridding accumulation keeps GRDH2D's raw column U (1-based, grd/grdh2d.f:177-187)
@@ -51,7 +51,7 @@ constexpr int RAW_SHIFT = SUPP + 1;
 // Row pitch (complex elements) of a plan's raw and final grids: a multiple of 4 (16-byte
 // rows for TMA) with room for raw index NU.
 inline int plan_pitch(int nu) { return (nu + 4) & ~3; }
-constexpr int CFLEN = 1 + 8 * 129;      // vis/visgrid.f:274
+constexpr int CFLEN = 1 + 8 * 129;      // vis/visgrid.f:105
 constexpr int ITEM_MAX = 16384;        // default work-item size (sde_plan_opts.item_max)
 constexpr int CHUNK_MAX = 64;           // default chunk size (sde_plan_opts.chunk_max)
 constexpr int ITEM_LIMIT = 1 << 16;     // largest accepted work-item size

@@ -1,5 +1,5 @@
 // uvfits.cu -- visibilities from a FITS random-groups file (the FTS branch of VISGET,
-// vis/visget.f:40-46) straight into the SoA arrays the plans take: the header is parsed on the
+// vis/visget.f:60-68) straight into the SoA arrays the plans take: the header is parsed on the
 // host (the checks of fts/ftsgrpre.f and vis/visstd.f, with their messages), the group records
 // are read into two pinned host buffers in turn and copied to the device, and one kernel per
 // chunk decodes the big-endian words (fts/fti.c fticr_), applies the parameter and array

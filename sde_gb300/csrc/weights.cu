@@ -1,11 +1,11 @@
 // weights.cu -- uniform (GRDUWT2D) and robust (GRDRUW2D) weighting, bit-exact.
 //
-// Pass 1 of the reference (grd/grduwt2d.f:90-115, grd/grdruw2d.f:302-329) adds WT into the
+// Pass 1 of the reference (grd/grduwt2d.f:90-115, grd/grdruw2d.f:132-159) adds WT into the
 // density grid GWT(UCEN,VCEN) sequentially in FP32, in visibility order.  Here each
 // visibility's cell key is computed with the reference's exact FP32/FP64 operations (no
 // FMA contraction), the (key, WT) pairs are sorted stably, and one thread sums each
 // cell's run in order: the same additions in the same order, so GWT is bit-identical.
-// Pass 2 (grd/grduwt2d.f:118-160, grd/grdruw2d.f:366-412) is an element-wise gather.
+// Pass 2 (grd/grduwt2d.f:118-160, grd/grdruw2d.f:196-242) is an element-wise gather.
 #include <math.h>
 #include <string.h>
 
@@ -20,7 +20,7 @@ struct WParams {
     int doshift;
 };
 
-// FP32 uv -> cell of the weighting routines (grd/grduwt2d.f:92-111, grdruw2d.f:368-387).
+// FP32 uv -> cell of the weighting routines (grd/grduwt2d.f:92-111, grd/grdruw2d.f:198-217).
 __device__ __forceinline__ bool wcell(const WParams &p, float u, float v, float w, int &uc,
                                       int &vc, float &ul, float &vl) {
     float ucell, vcell;
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_sumwt_part(const uint32_t *vals
     if (threadIdx.x == 0) partial[blockIdx.x] = r;
 }
 
-// partial[b] = sum over cells in block b's range of (double)(g*g), g > 0 (grdruw2d.f:339-345)
+// partial[b] = sum over cells in block b's range of (double)(g*g), g > 0 (grd/grdruw2d.f:168-175)
 __global__ void __launch_bounds__(RED_THREADS) k_sumlocwt_part(const float *gwt, int64_t ncell,
                                                                 int per_thread, double *partial) {
     int64_t base = ((int64_t)blockIdx.x * RED_THREADS + threadIdx.x) * per_thread;
@@ -149,7 +149,7 @@ struct AzParams {
     double ratio;  // SUMLOCWT / SUMWT
 };
 
-// Pass 2.  uniform: grd/grduwt2d.f:146-158; robust: grd/grdruw2d.f:395-410.
+// Pass 2.  uniform: grd/grduwt2d.f:146-158; robust: grd/grdruw2d.f:225-240.
 __global__ void k_newwt(WParams p, int robust, float f2, float d2, AzParams az,
                         const float *wt, const float *__restrict__ u, const float *__restrict__ v,
                         const float *__restrict__ w, const float *__restrict__ gwt, int64_t n,
@@ -280,7 +280,7 @@ int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const 
         SDE_CUDA_TRY(cudaMemcpyAsync(hcounts, counts, sizeof hcounts, cudaMemcpyDeviceToHost, st));
         SDE_CUDA_TRY(cudaStreamSynchronize(st));
     }
-    // robust parameters on the host, with the reference's REAL/DOUBLE mix (grdruw2d.f:276-363)
+    // robust parameters on the host, with the reference's REAL/DOUBLE mix (grd/grdruw2d.f:106-193)
     float rob = robust ? robust[0] : 0.0f;
     if (rmode == 3) {
         rob = (robust[0] + robust[1]) / 2.0f;

@@ -1,7 +1,7 @@
 """Host-side mirror of the SDE task flow for the imaging hot path, over libsdegpu.
 
   make_geom   IMGMAKE + FFTCONJA/FFTCONJ + VISGRID scalars (img/imgmake.f, fft/fftconja.f,
-              fft/fftconj.f, vis/visgrid.f:314-322) in the reference's REAL arithmetic
+              fft/fftconj.f, vis/visgrid.f:148-153) in the reference's REAL arithmetic
   crdshift    the FP64 phase-centre rotation matrix (crd/crdshift.f:95-160)
   Context     one device + stream (torch's current stream) + the library context
   Plan        a device-resident, tile-sorted visibility set (sde_plan)

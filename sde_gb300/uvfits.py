@@ -1,4 +1,4 @@
-"""Visibilities from FITS random-groups files (VISGET's FTS branch, vis/visget.f:40-46)
+"""Visibilities from FITS random-groups files (VISGET's FTS branch, vis/visget.f:60-68)
 through libsdegpu's loader: the file is read in chunks into pinned memory, copied to the
 device and decoded there (sde_uvfits_* in include/sde_gpu.h).
 

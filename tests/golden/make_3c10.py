@@ -82,6 +82,19 @@ def read_uv(path):
                 ra=np.float64(h["CRVAL5"]), dec=np.float64(h["CRVAL6"]), freq=np.float64(freq))
 
 
+
+def reference_root():
+    """The reference tree: $SDE_REFERENCE, else the benchmark's reference_path (None if
+    neither names an existing directory)."""
+    import json
+    root = os.environ.get("SDE_REFERENCE")
+    if not root:
+        try:
+            root = json.load(open(os.path.join(HERE, "..", "..", "BASELINE.json")))["reference_path"]
+        except (OSError, ValueError, KeyError):
+            root = None
+    return root if root and os.path.isdir(root) else None
+
 def main(reqdata):
     uv = read_uv(os.path.join(reqdata, "3C10UV.FTS"))
     dmap, hm = read_image(os.path.join(reqdata, "3C10MAP.FTS"))
@@ -93,4 +106,10 @@ def main(reqdata):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/reqdata")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    else:
+        root = reference_root()
+        if root is None:
+            sys.exit("no reference tree: pass path/to/reqdata or set SDE_REFERENCE")
+        main(os.path.join(root, "reqdata"))

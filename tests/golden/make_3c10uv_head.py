@@ -14,6 +14,19 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 NGROUPS = 300
 
 
+
+def reference_root():
+    """The reference tree: $SDE_REFERENCE, else the benchmark's reference_path (None if
+    neither names an existing directory)."""
+    import json
+    root = os.environ.get("SDE_REFERENCE")
+    if not root:
+        try:
+            root = json.load(open(os.path.join(HERE, "..", "..", "BASELINE.json")))["reference_path"]
+        except (OSError, ValueError, KeyError):
+            root = None
+    return root if root and os.path.isdir(root) else None
+
 def main(reqdata):
     raw = open(os.path.join(reqdata, "3C10UV.FTS"), "rb").read()
     cards, i = [], 0
@@ -40,4 +53,10 @@ def main(reqdata):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/reqdata")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    else:
+        root = reference_root()
+        if root is None:
+            sys.exit("no reference tree: pass path/to/reqdata or set SDE_REFERENCE")
+        main(os.path.join(root, "reqdata"))

@@ -81,3 +81,45 @@ def test_window_is_crdnhalf():
     g = Geom(4096, 0.5)
     lo, hi = g.window()
     assert (lo, hi - lo) == (1024, 2047)
+
+
+def _oracle_cf(orc, code_sf):
+    cf = np.zeros(1 + 8 * 129, np.float32)
+    s, o = C.c_int(), C.c_int()
+    orc.lib().orc_grdcf(code_sf, cf, C.byref(s), C.byref(o))
+    return cf, s.value, o.value
+
+
+def test_library_gridding_tables_equal_the_oracle(orc):
+    """The library's host-side GRDCF ('SF' and 'BOX'), GRDCCF ('SF' and 'BOX') and GRDSF
+    (grd/grdcf.f:41-90, grd/grdccf.f:42-52, grd/grdsf.f:46-73) -- the tables a caller of the
+    drop-ins builds -- equal the oracle's restatement bit for bit; an unknown code reports
+    through ERRREPOR and leaves ERROR set."""
+    L = _abi.lib()
+    P = C.c_void_p
+    for code, code_sf, supp_ref in ((b"SF", 1, 3), (b"BOX", 0, 1)):
+        ref, rs, ro = _oracle_cf(orc, code_sf)
+        cf = np.full(1 + 8 * 129, np.nan, np.float32)
+        cfs, cfo = C.c_int(-1), C.c_int(-1)
+        # only the table's used span is written: (SUPP+1)*OSAMP on each side of the centre
+        L.grdcf_(code, cf.ctypes.data_as(P), C.byref(cfs), C.byref(cfo), len(code))
+        assert (cfs.value, cfo.value) == (rs, ro) == (supp_ref, 128)
+        n = 2 * (supp_ref + 1) * 128 + 1
+        assert np.array_equal(cf[:n].view(np.uint32), ref[:n].view(np.uint32)), code
+    for ccflen in (33, 257, 2049, 4097):
+        for code, code_sf in ((b"SF", 1), (b"BOX", 0)):
+            ref = np.zeros(ccflen, np.float32)
+            orc.lib().orc_grdccf(code_sf, ref, ccflen)
+            got = np.zeros(ccflen, np.float32)
+            L.grdccf_(code, got.ctypes.data_as(P), C.byref(C.c_int(ccflen)), len(code))
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (code, ccflen)
+    for nu in np.linspace(-0.1, 1.1, 1201):
+        x = C.c_double(float(nu))
+        assert L.grdsf_(C.byref(x)) == orc.lib().orc_grdsf(float(nu))
+    s = _abi.sysi()
+    try:
+        cf = np.zeros(1 + 8 * 129, np.float32)
+        L.grdcf_(b"XYZ", cf.ctypes.data_as(P), C.byref(C.c_int()), C.byref(C.c_int()), 3)
+        assert s.error != 0
+    finally:
+        s.error = 0

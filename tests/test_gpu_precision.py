@@ -8,7 +8,7 @@ pytestmark = pytest.mark.gpu
 
 
 def test_dense_cells_stay_within_1e5_of_fp64(gpu_ctx):
-    from sde_gb300 import precision
+    from oracle import precision
     data = precision.dense_case(stride=64)      # ~1.0 M visibilities
     r = precision.study(gpu_ctx, data, imsize=256, cell=8.0)
     assert r["vis_per_cell"]["max"] > 1000

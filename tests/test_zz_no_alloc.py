@@ -88,11 +88,25 @@ def test_noalloc_hogbom_matches_allocating_entry_point():
 
 
 def test_noalloc_rejects_oversized_window():
-    from sde_gb300 import _abi
-    L = _abi.lib()
-    r = _abi.CleanResult()
-    one = C.c_void_p(16)  # never dereferenced: the size check comes first
-    rc = L.sde_hogbom_noalloc(None, one, one, None, 65536, 65536, 3, 3, 0.1, 10, 1, 0.0, 0.0,
-                              one, one, one, one, one, None, C.byref(r))
-    assert rc == _abi.SDE_EINVAL
-    assert "2^31-1" in _abi.last_error()
+    """The size check runs before any device work.  It is exercised in a child process that
+    sees no GPU, so that if the check ever moved below the launches the call would fail with a
+    device error instead of launching kernels on the placeholder addresses."""
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import ctypes as C, sys\n"
+        "sys.path.insert(0, %r)\n"
+        "from sde_gb300 import _abi\n"
+        "L = _abi.lib()\n"
+        "r = _abi.CleanResult()\n"
+        "one = C.c_void_p(16)\n"
+        "rc = L.sde_hogbom_noalloc(None, one, one, None, 65536, 65536, 3, 3, 0.1, 10, 1, 0.0, 0.0,\n"
+        "                          one, one, one, one, one, None, C.byref(r))\n"
+        "assert rc == _abi.SDE_EINVAL, rc\n"
+        "assert '2^31-1' in _abi.last_error(), _abi.last_error()\n"
+        "print('ok')\n" % os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
