@@ -19,81 +19,89 @@
 
 namespace {
 
-constexpr int GRID_THREADS = 256;
+// ---------------------------------------------------------------------------------------
+// Gridding (GRDH2D's 7x7 accumulation, grd/grdh2d.f:168-189).
+//
+// A chunk holds visibilities of one cell pair (lu0, lu0+1); its footprint is a 7-row x
+// 8-column window.  A 4-lane group owns a chunk: lane q holds window columns q and q+4 over
+// the 7 rows in registers (14 complex sums) for the whole chunk and adds them into the
+// work item's shared tile once, at the end (shared-memory atomics: the 8 chunks of a warp
+// share a colour class, so their windows do not overlap).  The group's lanes load four
+// consecutive records at a time (one 64-byte run) and exchange weight x value and the
+// offset word by shuffle.
+//
+// A CTA is TEAMS independent teams of 256 threads, one CTA per SM, persistent: the teams
+// share one copy of the tap tables (filled once) and each team owns a shared tile, takes
+// work items from an atomic counter and synchronises with its own named barrier, so a
+// team waiting at its item's end does not hold the others.  The tables are laid out so
+// that no read has a bank conflict:
+//   v table: per offset row d (0..128) 4 copies of the 7 v taps (+ a zero), 32 bytes each
+//     in a 128-byte row; group g reads copy g mod 4, so the 4 groups of a half-warp read
+//     4 different 32-byte octets (measured on GB300 with a probe of this access pattern: a
+//     128-bit shared load of 4-lane groups takes the minimum 2 wavefronts this way, and
+//     3.5 with 2 copies in 64-byte rows);
+//   u table: per (d, column-in-pair off) row 4 copies of the 4 pairs (t'_q, t'_{q+4}),
+//     t'_j = tap j - off for window column j (zero outside 0..6); lane q of group g reads
+//     pair q of copy g mod 4: the 4 groups of a half-warp (the unit of a 64-bit load) read
+//     the 4 different 32-byte octets of one 128-byte row (2 wavefronts, the minimum).
+constexpr int TEAMS = 3;
+constexpr int TEAM_THREADS = 256;
+constexpr int GRID_THREADS = TEAMS * TEAM_THREADS;
 constexpr int GLANES = 4;                          // lanes per chunk
-constexpr int GGROUPS = GRID_THREADS / GLANES;     // chunks in flight per CTA
-constexpr int GRID_MINB = 4;                       // resident CTAs per SM the kernel is built for
-// Shared copy of the tap table, one layout for both reads a 4-lane group makes per
-// visibility.  A chunk covers a pair of cells (lu0, lu0+1), so its footprint is 8 columns
-// wide; lane q owns window columns q and q+4, which for a visibility in the pair's column
-// off (0 or 1) are taps q-off and q+4-off.  A row holds the taps as 5 pairs,
-// (a0,a4) (a1,a5) (a2,a6) (a3,0) (0,a3): lane q reads pair (q - off) mod 5 as one float2,
-// and the seven v taps are the first 8 floats, read as two float4 by every lane.  Rows are
-// padded to 12 floats (float4 alignment).  (Keeping several bank-staggered copies of the
-// table, one per group of a half-warp, removes its bank conflicts but measured slower: the
-// extra shared memory costs a resident CTA per SM.)
-constexpr int TAP_ROW = 12;
-constexpr int TAP_COPIES = 1;
-constexpr int TAP_STRIDE = TAP_ROW * TAP_COPIES;    // floats per table row
-constexpr int TAP_FLOATS = 129 * TAP_STRIDE;
+constexpr int GGROUPS = TEAM_THREADS / GLANES;     // chunks in flight per team
+constexpr int VT_ROW = 32;                         // floats per v-table row (4 copies x 8)
+constexpr int VT_FLOATS = 129 * VT_ROW;
+constexpr int UT_ROW = 32;                         // floats per u-table row (4 copies x 4 pairs)
+constexpr int UT_FLOATS = 2 * 129 * UT_ROW;
+constexpr int GTAB_FLOATS = VT_FLOATS + UT_FLOATS;
+constexpr int GTILE_FLOATS = 2 * STILE * STILE;    // a team's tile: re and im planes
+constexpr int NPAIR = (NTAP + 1) / 2;              // window rows taken in pairs
 
-__device__ __forceinline__ void fill_tap_table(const float *__restrict__ cft_g, float *tab,
-                                               int nthreads) {
-    // row entry e -> tap index (0 4 1 5 2 6 3 7 | 7 3 | 7 7); tap 7 is the table's zero
-    for (int k = threadIdx.x; k < TAP_FLOATS; k += nthreads) {
-        const int d = k / TAP_STRIDE, e = k % TAP_ROW;
-        const int a = e < 8 ? (e >> 1) + 4 * (e & 1) : (e == 9 ? 3 : 7);
-        tab[k] = cft_g[d * 8 + a];
+// cft_g[d * 8 + a] = tap a (0..6) of offset row d; cft_g[d * 8 + 7] = 0
+__device__ __forceinline__ void fill_tap_tables(const float *__restrict__ cft_g, float *vt, float *ut) {
+    for (int k = threadIdx.x; k < VT_FLOATS; k += blockDim.x)
+        vt[k] = cft_g[(k / VT_ROW) * 8 + (k & 7)];
+    for (int k = threadIdx.x; k < UT_FLOATS; k += blockDim.x) {
+        const int r = k / UT_ROW, d = r >> 1, off = r & 1, e = k & 7;  // e: pair e/2, half e&1
+        const int a = (e >> 1) + 4 * (e & 1) - off;
+        ut[k] = a >= 0 && a < NTAP ? cft_g[d * 8 + a] : 0.f;
     }
 }
 
-// One visibility's taps from a group's copy of the table: u pair for lane q (g bit 16 is
-// the visibility's column in the cell pair), and v taps.
-struct Taps {
-    float2 gu;
-    float gv[NTAP];
-};
-__device__ __forceinline__ Taps read_taps(const float *tg, int q, uint32_t g) {
-    Taps t;
-    const int off = (int)((g >> 16) & 1u);
-    const int pair = q - off < 0 ? 4 : q - off;
-    t.gu = *reinterpret_cast<const float2 *>(tg + (g & 0xFFu) * TAP_STRIDE + 2 * pair);
-    const float4 *r = reinterpret_cast<const float4 *>(tg + ((g >> 8) & 0xFFu) * TAP_STRIDE);
-    const float4 v0 = r[0], v1 = r[1];
-    t.gv[0] = v0.x;
-    t.gv[1] = v0.z;
-    t.gv[2] = v1.x;
-    t.gv[3] = v1.z;
-    t.gv[4] = v0.y;
-    t.gv[5] = v0.w;
-    t.gv[6] = v1.y;
-    return t;
+// the team's named barrier (0 is __syncthreads)
+__device__ __forceinline__ void team_sync(int team) {
+    asm volatile("bar.sync %0, %1;" ::"r"(team + 1), "r"(TEAM_THREADS) : "memory");
 }
 
-// Gridding.  A chunk holds visibilities of one cell pair (lu0, lu0+1); its footprint is a
-// 7-row x 8-column window.  Lane q of a 4-lane group owns window columns q and q+4 and
-// accumulates 7 rows x 2 columns x complex in registers; the group's lanes load four
-// consecutive records at a time and share them by shuffle.  The shared tile (real and imaginary
-// planes) receives each chunk's window once, through shared-memory atomics (a warp's 8
-// chunks share a colour class, so their windows do not overlap).
-// Grid one work item: the item's chunks into the shared tile (planar re/im planes, zero on
-// entry; tap table filled), then the touched cells into the raw grid.  Reading the tile
-// back zeroes it, so the next item of a persistent CTA starts from a clean tile once the
-// caller's barrier has passed.
+// 1 on every thread of the team when pred holds on all of them
+__device__ __forceinline__ int team_and(int team, int pred) {
+    int r;
+    asm volatile(
+        "{ .reg .pred pi, po; setp.ne.s32 pi, %1, 0; bar.red.and.pred po, %2, %3, pi;"
+        " selp.s32 %0, 1, 0, po; }"
+        : "=r"(r)
+        : "r"(pred), "r"(team + 1), "r"(TEAM_THREADS)
+        : "memory");
+    return r;
+}
+
+// Grid one work item: its chunks into the team's shared tile (planar re/im planes, zero on
+// entry), then the touched cells into the raw grid.  Reading the tile back zeroes it, so
+// the next item starts from a clean tile once the team barrier after the flush has passed.
 template <bool PSF, bool COMP>
 __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__restrict__ chunks,
-                                          const float4 *__restrict__ rec, const float *tab,
-                                          float *tre, float *tim, float2 *raw, float2 *raw_lo,
-                                          int pitch, int ntu, int nu, int nv) {
-    // Cooperative record loads: lane q of a group loads record k+q of its chunk (one
-    // 64-byte run per group instead of one record broadcast to four lanes), and the group
-    // exchanges each visibility's weighted value and offset word by shuffle.  Every lane of
-    // a warp runs the same number of chunk rounds and visibility steps (the warp's longest
-    // chunk; shorter chunks read zero-weight records), so full-warp shuffles are safe.
-    const int q = threadIdx.x & (GLANES - 1);
-    const int grp = threadIdx.x / GLANES;
-    const int gbase = threadIdx.x & 28;
-    const float *tg = tab;
+                                          const float4 *__restrict__ rec, const float *vt,
+                                          const float *ut, float *tre, float *tim, float2 *raw,
+                                          float2 *raw_lo, int pitch, int ntu, int nu, int nv,
+                                          int tid, int team) {
+    // Every lane of a warp runs the same number of chunk rounds and visibility steps (the
+    // warp's longest chunk; shorter chunks read zero-weight records, whose offset word 0
+    // reads table row 0), so full-warp shuffles are safe.
+    const int q = tid & (GLANES - 1);
+    const int grp = tid / GLANES;
+    const int gbase = threadIdx.x & (32 - GLANES);  // lane of q = 0 in this group
+    const float *vcopy = vt + (grp & 3) * 8;
+    const float *ucopy = ut + (grp & 3) * 8 + 2 * q;
     constexpr uint32_t FULL = 0xffffffffu;
     const int rounds = (it.cend - it.cbeg + GGROUPS - 1) / GGROUPS;
     for (int rr = 0; rr < rounds; rr++) {
@@ -104,15 +112,18 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
         const int lu = cell & 63, lv = cell >> 6;
         int wlen = len;
 #pragma unroll
-        for (int d = 4; d < 32; d <<= 1) wlen = max(wlen, __shfl_xor_sync(FULL, wlen, d));
-        float a0r[NTAP], a0i[NTAP], a1r[NTAP], a1i[NTAP];
+        for (int d = GLANES; d < 32; d <<= 1) wlen = max(wlen, __shfl_xor_sync(FULL, wlen, d));
+        // window rows in pairs (0,1) (2,3) (4,5) (6,-): one packed FMA (__ffma2_rn, two
+        // round-to-nearest FMAs) per pair; the v-table row's zero fills the seventh pair's
+        // second half
+        float2 A0r[NPAIR], A0i[NPAIR], A1r[NPAIR], A1i[NPAIR];
 #pragma unroll
-        for (int b = 0; b < NTAP; b++) {
-            a0r[b] = 0.f;
-            a1r[b] = 0.f;
+        for (int p = 0; p < NPAIR; p++) {
+            A0r[p] = make_float2(0.f, 0.f);
+            A1r[p] = make_float2(0.f, 0.f);
             if (!PSF) {
-                a0i[b] = 0.f;
-                a1i[b] = 0.f;
+                A0i[p] = make_float2(0.f, 0.f);
+                A1i[p] = make_float2(0.f, 0.f);
             }
         }
         const float4 *pr = rec + start;
@@ -127,17 +138,26 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
                 const uint32_t g = __shfl_sync(FULL, gq, gbase + u);
                 const float fr = __shfl_sync(FULL, frq, gbase + u);
                 const float fi = PSF ? 0.f : __shfl_sync(FULL, fiq, gbase + u);
-                const Taps t = read_taps(tg, q, g);
-                const float2 gu = t.gu;
+                const float2 gu = *reinterpret_cast<const float2 *>(
+                    ucopy + ((g & 0xFFu) * 2 + ((g >> 16) & 1u)) * UT_ROW);
+                const float4 *vr = reinterpret_cast<const float4 *>(vcopy + ((g >> 8) & 0xFFu) * VT_ROW);
+                const float4 v0 = vr[0], v1 = vr[1];
+                const float2 P[NPAIR] = {make_float2(v0.x, v0.y), make_float2(v0.z, v0.w),
+                                         make_float2(v1.x, v1.y), make_float2(v1.z, v1.w)};
                 const float h0r = gu.x * fr, h1r = gu.y * fr;
-                const float h0i = gu.x * fi, h1i = gu.y * fi;
+                const float2 H0r = make_float2(h0r, h0r), H1r = make_float2(h1r, h1r);
 #pragma unroll
-                for (int b = 0; b < NTAP; b++) {
-                    a0r[b] = fmaf(t.gv[b], h0r, a0r[b]);
-                    a1r[b] = fmaf(t.gv[b], h1r, a1r[b]);
-                    if (!PSF) {
-                        a0i[b] = fmaf(t.gv[b], h0i, a0i[b]);
-                        a1i[b] = fmaf(t.gv[b], h1i, a1i[b]);
+                for (int p = 0; p < NPAIR; p++) {
+                    A0r[p] = __ffma2_rn(P[p], H0r, A0r[p]);
+                    A1r[p] = __ffma2_rn(P[p], H1r, A1r[p]);
+                }
+                if (!PSF) {
+                    const float h0i = gu.x * fi, h1i = gu.y * fi;
+                    const float2 H0i = make_float2(h0i, h0i), H1i = make_float2(h1i, h1i);
+#pragma unroll
+                    for (int p = 0; p < NPAIR; p++) {
+                        A0i[p] = __ffma2_rn(P[p], H0i, A0i[p]);
+                        A1i[p] = __ffma2_rn(P[p], H1i, A1i[p]);
                     }
                 }
             }
@@ -148,23 +168,24 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
         for (int b = 0; b < NTAP; b++) {
             float *rr_ = &tre[(lv + b) * STILE + lu + q];
             float *ri = &tim[(lv + b) * STILE + lu + q];
-            atomicAdd(rr_, a0r[b]);
-            if (!PSF) atomicAdd(ri, a0i[b]);
-            atomicAdd(rr_ + 4, a1r[b]);
-            if (!PSF) atomicAdd(ri + 4, a1i[b]);
+            const int p = b >> 1;
+            atomicAdd(rr_, (b & 1) ? A0r[p].y : A0r[p].x);
+            if (!PSF) atomicAdd(ri, (b & 1) ? A0i[p].y : A0i[p].x);
+            atomicAdd(rr_ + 4, (b & 1) ? A1r[p].y : A1r[p].x);
+            if (!PSF) atomicAdd(ri + 4, (b & 1) ? A1i[p].y : A1i[p].x);
         }
     }
-    __syncthreads();
+    team_sync(team);
     const int tu = it.tile % ntu, tv = it.tile / ntu;
     // flush FLUSH_B cells per thread at a time, so that the compensated path keeps FLUSH_B
     // returning atomics in flight instead of waiting on each
     constexpr int FLUSH_B = 4;
-    for (int k0 = threadIdx.x; k0 < STILE * STILE; k0 += FLUSH_B * GRID_THREADS) {
+    for (int k0 = tid; k0 < STILE * STILE; k0 += FLUSH_B * TEAM_THREADS) {
         float2 val[FLUSH_B];
         int64_t gi[FLUSH_B];
 #pragma unroll
         for (int j = 0; j < FLUSH_B; j++) {
-            const int k = k0 + j * GRID_THREADS;
+            const int k = k0 + j * TEAM_THREADS;
             gi[j] = -1;
             val[j] = make_float2(0.f, 0.f);
             if (k >= STILE * STILE) continue;
@@ -199,72 +220,86 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
     }
 }
 
-// One CTA per work item of one plan.
+// Persistent gridding of one plan: every team takes work items from an atomic counter
+// until the list is exhausted.
 template <bool PSF, bool COMP>
-__global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
-    k_grid(const WorkItem *__restrict__ items, const uint2 *__restrict__ chunks,
-           const float4 *__restrict__ rec, const float *__restrict__ cft_g, float2 *raw,
-           float2 *raw_lo, int pitch, int ntu, int nu, int nv) {
+__global__ void __launch_bounds__(GRID_THREADS, 1)
+    k_grid(const WorkItem *__restrict__ items, int64_t nitems, unsigned long long *counter,
+           const uint2 *__restrict__ chunks, const float4 *__restrict__ rec,
+           const float *__restrict__ cft_g, float2 *raw, float2 *raw_lo, int pitch, int ntu, int nu,
+           int nv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *tre = reinterpret_cast<float *>(smem_raw);
+    float *vt = reinterpret_cast<float *>(smem_raw);
+    float *ut = vt + VT_FLOATS;
+    const int team = threadIdx.x / TEAM_THREADS, tid = threadIdx.x % TEAM_THREADS;
+    float *tre = ut + UT_FLOATS + team * GTILE_FLOATS;
     float *tim = tre + STILE * STILE;
-    float *tab = tim + STILE * STILE;  // tap table
-    const WorkItem it = items[blockIdx.x];
-    if (threadIdx.x == 0) {
-        // the item's chunk list and records stream into L2 while the tile is cleared
-        prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
-        prefetch_l2_range(rec, it.vbeg, it.vend, 16);
-    }
-    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
+    __shared__ long long s_next[TEAMS];
+    for (int k = tid; k < STILE * STILE; k += TEAM_THREADS) {
         tre[k] = 0.f;
         tim[k] = 0.f;
     }
-    fill_tap_table(cft_g, tab, GRID_THREADS);
+    fill_tap_tables(cft_g, vt, ut);
     __syncthreads();
-    grid_item<PSF, COMP>(it, chunks, rec, tab, tre, tim, raw, raw_lo, pitch, ntu, nu, nv);
+    for (;;) {
+        if (tid == 0) s_next[team] = (long long)atomicAdd(counter, 1ull);
+        team_sync(team);
+        const long long n = s_next[team];
+        if (n >= nitems) break;
+        const WorkItem it = items[n];
+        if (tid == 0) {
+            // the item's chunk list and records stream into L2 while the first chunks run
+            prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
+            prefetch_l2_range(rec, it.vbeg, it.vend, 16);
+        }
+        grid_item<PSF, COMP>(it, chunks, rec, vt, ut, tre, tim, raw, raw_lo, pitch, ntu, nu, nv, tid, team);
+        team_sync(team);
+    }
 }
 
-// Persistent gridding of many plans (a mosaic's pointings, a batch of served jobs): each
-// CTA fills its tap table once, then takes work items from the combined list of all plans
-// (item_start[p] = first combined index of plan p) through an atomic counter until the
-// list is exhausted.  One launch grids every plan.
+// Persistent gridding of many plans (a mosaic's pointings, a batch of served jobs): the
+// same, over the combined work-item list of all plans (item_start[p] = first combined index
+// of plan p).  One launch grids every plan.
 template <bool PSF, bool COMP>
-__global__ void __launch_bounds__(GRID_THREADS, GRID_MINB)
+__global__ void __launch_bounds__(GRID_THREADS, 1)
     k_grid_batch(const BatchPlan *__restrict__ plans, const int64_t *__restrict__ item_start,
                  int nplans, unsigned long long *counter, const float *__restrict__ cft_g) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *tre = reinterpret_cast<float *>(smem_raw);
+    float *vt = reinterpret_cast<float *>(smem_raw);
+    float *ut = vt + VT_FLOATS;
+    const int team = threadIdx.x / TEAM_THREADS, tid = threadIdx.x % TEAM_THREADS;
+    float *tre = ut + UT_FLOATS + team * GTILE_FLOATS;
     float *tim = tre + STILE * STILE;
-    float *tab = tim + STILE * STILE;
-    __shared__ long long s_next;
-    __shared__ int s_plan;
-    for (int k = threadIdx.x; k < STILE * STILE; k += GRID_THREADS) {
+    __shared__ long long s_next[TEAMS];
+    __shared__ int s_plan[TEAMS];
+    for (int k = tid; k < STILE * STILE; k += TEAM_THREADS) {
         tre[k] = 0.f;
         tim[k] = 0.f;
     }
-    fill_tap_table(cft_g, tab, GRID_THREADS);
+    fill_tap_tables(cft_g, vt, ut);
+    __syncthreads();
     const int64_t total = item_start[nplans];
     for (;;) {
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             const long long n = (long long)atomicAdd(counter, 1ull);
             int p = 0;
             if (n < total)
                 while (p + 1 < nplans && item_start[p + 1] <= n) p++;
-            s_next = n;
-            s_plan = p;
+            s_next[team] = n;
+            s_plan[team] = p;
         }
-        __syncthreads();
-        const long long n = s_next;
+        team_sync(team);
+        const long long n = s_next[team];
         if (n >= total) break;
-        const BatchPlan P = plans[s_plan];
-        const WorkItem it = P.items[n - item_start[s_plan]];
-        if (threadIdx.x == 0) {
+        const BatchPlan P = plans[s_plan[team]];
+        const WorkItem it = P.items[n - item_start[s_plan[team]]];
+        if (tid == 0) {
             prefetch_l2_range(P.chunks, it.cbeg, it.cend, 8);
             prefetch_l2_range(P.rec, it.vbeg, it.vend, 16);
         }
-        grid_item<PSF, COMP>(it, P.chunks, P.rec, tab, tre, tim, P.raw, P.raw_lo, P.pitch, P.ntu,
-                             P.nu, P.nv);
-        __syncthreads();
+        grid_item<PSF, COMP>(it, P.chunks, P.rec, vt, ut, tre, tim, P.raw, P.raw_lo, P.pitch, P.ntu,
+                             P.nu, P.nv, tid, team);
+        team_sync(team);
     }
 }
 
@@ -459,196 +494,221 @@ __global__ void __launch_bounds__(256) k_finalize_batch(const FinalizeDesc *__re
 }
 
 // ---------------------------------------------------------------------------------------
-// Degridding.
-constexpr int DG_THREADS = 256;
+// Degridding (GRDDEH2D, grd/grddeh2d.f:119-193).
+//
+// Persistent, TEAMS teams of 256 threads per CTA and one CTA per SM, like the gridder: the
+// CTA fills the gridder's tap tables and the tap row sums once; each team takes work items
+// from an atomic counter and stages the item's model tile + halo in its own shared buffer
+// with one TMA 2-D bulk load (cp.async.bulk.tensor, the team's mbarrier, bounded wait).  A
+// 4-lane group owns a chunk (the chunk's visibilities lie in one cell pair -- their
+// degridding cell is their gridding cell -- or carry GDD_EXCEPTION and are skipped here):
+// lane q holds columns q and q+4 of the pair's 7x8 neighbourhood window in registers, read
+// once per chunk, and for each visibility forms sum_b gv[b] G[b][col] per column, then the u
+// tap of that column times that: a partial sum over its columns.  Four visibilities'
+// partials are reduced across the group with a transposing butterfly (6 shuffles per
+// lane), after which lane q owns visibility q of the four and finishes it: divide by
+// (sum gu)(sum gv) (row sums in the same order as a plain loop), subtract from the observed
+// value or stage it for the caller's order.
+constexpr int DG_THREADS = GRID_THREADS;
+constexpr int DG_GROUPS = TEAM_THREADS / 4;        // chunks in flight per team
 constexpr int DG_TILE_FLOATS = STILE * STILE * 2;  // 9800 floats, 39200 B
 constexpr uint32_t DG_TX_BYTES = DG_TILE_FLOATS * 4;
+constexpr size_t DG_TILE_STRIDE = (DG_TX_BYTES + 127) / 128 * 128;  // TMA destinations: 128-byte aligned
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-constexpr int DG_GROUPS = DG_THREADS / 4;          // chunks in flight per CTA
 constexpr int DG_PREFETCH = 4096;                  // visibilities prefetched into L2 per item
 constexpr int RSUM_FLOATS = 132;                    // 129 row sums, padded
-constexpr size_t DG_TAB_OFF = DG_TX_BYTES;
-constexpr size_t DG_RSUM_OFF = DG_TAB_OFF + sizeof(float) * TAP_FLOATS;
+constexpr size_t DG_VT_OFF = (size_t)TEAMS * DG_TILE_STRIDE;
+constexpr size_t DG_UT_OFF = DG_VT_OFF + sizeof(float) * VT_FLOATS;
+constexpr size_t DG_RSUM_OFF = DG_UT_OFF + sizeof(float) * UT_FLOATS;
 constexpr size_t DG_BAR_OFF = DG_RSUM_OFF + sizeof(float) * RSUM_FLOATS;
-static_assert(DG_TAB_OFF % 16 == 0 && DG_BAR_OFF % 8 == 0, "layout");
+static_assert(DG_TILE_STRIDE % 128 == 0 && DG_VT_OFF % 16 == 0 && DG_UT_OFF % 16 == 0 &&
+                  DG_BAR_OFF % 8 == 0, "layout");
 
 // mode 0: residual update in the gridding frame; mode 1: caller-order output (user frame).
-// A 4-lane group per chunk (the chunk's visibilities lie in one cell pair -- their
-// degridding cell is their gridding cell -- or carry GDD_EXCEPTION and are skipped here).
-// Lane q holds columns q and q+4 of the pair's 7x8 neighbourhood window in registers, read
-// once per chunk from the TMA-staged tile, and for each visibility forms
-// sum_b gv[b] G[b][col] per column, then the u tap of that column times that: a partial
-// sum over its columns.  Four visibilities' partials are reduced across the group with a
-// transposing butterfly (6 shuffles per lane), after which lane q owns visibility q of the
-// four and finishes it: divide by (sum gu)(sum gv) (row sums in the same order as a plain
-// loop), subtract from the observed value or write to the caller's order.
 template <int MODE>
-__global__ void __launch_bounds__(DG_THREADS, 4)
+__global__ void __launch_bounds__(DG_THREADS, 1)
     k_degrid(const __grid_constant__ CUtensorMap tmap, const WorkItem *__restrict__ items,
-             const uint2 *__restrict__ chunks, const uint32_t *__restrict__ gdd,
-             const float *__restrict__ cft_g, const float2 *__restrict__ fobs, float4 *rec,
-             const uint8_t *__restrict__ gconj, const float2 *__restrict__ rot,
-             const float *__restrict__ wt, float4 *stage, int ntu, const float2 *__restrict__ grid,
-             int pitch, int nv, int vorigin, int refl, int *status) {
+             int64_t nitems, unsigned long long *counter, const uint2 *__restrict__ chunks,
+             const uint32_t *__restrict__ gdd, const float *__restrict__ cft_g,
+             const float2 *__restrict__ fobs, float4 *rec, const uint8_t *__restrict__ gconj,
+             const float2 *__restrict__ rot, const float *__restrict__ wt, float4 *stage, int ntu,
+             const float2 *__restrict__ grid, int pitch, int nv, int vorigin, int refl,
+             int *status) {
     extern __shared__ __align__(128) unsigned char smem_dg[];
-    float2 *tile = reinterpret_cast<float2 *>(smem_dg);
-    float *tab = reinterpret_cast<float *>(smem_dg + DG_TAB_OFF);
+    const int team = threadIdx.x / TEAM_THREADS, tid = threadIdx.x % TEAM_THREADS;
+    float2 *tile = reinterpret_cast<float2 *>(smem_dg + (size_t)team * DG_TILE_STRIDE);
+    float *vt = reinterpret_cast<float *>(smem_dg + DG_VT_OFF);
+    float *ut = reinterpret_cast<float *>(smem_dg + DG_UT_OFF);
     float *rsum = reinterpret_cast<float *>(smem_dg + DG_RSUM_OFF);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_dg + DG_BAR_OFF);
-    const WorkItem it = items[blockIdx.x];
-    const int tu = it.tile % ntu, tv = it.tile / ntu;
-    if (threadIdx.x == 0) {
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_dg + DG_BAR_OFF) + team;
+    __shared__ long long s_next[TEAMS];
+    if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
         asm volatile("fence.mbarrier_init.release.cluster;");
-        asm volatile("fence.proxy.async.shared::cta;");
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        // box origin: columns tu*64-6 (complex) -> float x = 2*(tu*64-6), rows tv*64-3
-        const int x = 2 * (tu * TILE - 2 * SUPP), y = tv * TILE - SUPP;
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                     "r"(DG_TX_BYTES));
-        asm volatile(
-            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-            " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(tile)),
-            "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
-            : "memory");
-        prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
-        // the first DG_PREFETCH visibilities' words only: whole items of all resident CTAs
-        // would not fit in L2 together (measured: the full range evicts what it fetched)
-        const int pf_end = min(it.vend, it.vbeg + DG_PREFETCH);
-        prefetch_l2_range(gdd, it.vbeg, pf_end, 4);
-        if (MODE == 0) prefetch_l2_range(fobs, it.vbeg, pf_end, 8);
-    }
-    fill_tap_table(cft_g, tab, DG_THREADS);
+    fill_tap_tables(cft_g, vt, ut);
     for (int d = threadIdx.x; d < 129; d += DG_THREADS) {
         float sacc = 0.f;
 #pragma unroll
         for (int a = 0; a < NTAP; a++) sacc += cft_g[d * 8 + a];
         rsum[d] = sacc;
     }
-    {
-        uint32_t done = 0;
-        for (int spin = 0; spin < (1 << 24) && !done; spin++) {
-            asm volatile(
-                "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;"
-                " selp.u32 %0, 1, 0, p; }"
-                : "=r"(done)
-                : "r"(smem_u32(bar))
-                : "memory");
-        }
-        if (!done) {
-            atomicExch(&status[STATUS_TIMEOUT], 1);
-            return;
-        }
-    }
-    if (refl && tu == 0) {
-        // GRDDEH2D's reflection branch (grd/grddeh2d.f:123-158) in the tile: halo columns
-        // 3..5 stand for u = -3..-1 (left of the v axis; TMA filled them with zeros) and
-        // receive conj(G(-u, 2*VORIGIN - v)), the values that branch reads there
-        for (int k = threadIdx.x; k < STILE * SUPP; k += DG_THREADS) {
-            const int r = k / SUPP, c = SUPP + k % SUPP;    // c = 2*SUPP + u
-            const int vm = 2 * vorigin - (tv * TILE - SUPP + r + 1);  // mirrored 1-based row
-            float2 val = make_float2(0.f, 0.f);
-            if (vm >= 1 && vm <= nv) {
-                const float2 gm = grid[(int64_t)(vm - 1) * pitch + (2 * SUPP - c)];
-                val = make_float2(gm.x, -gm.y);
-            }
-            tile[r * STILE + c] = val;
-        }
-    }
     __syncthreads();
-    const int q = threadIdx.x & 3;
+    const int q = tid & 3;
     const bool hi2 = (q & 2) != 0, hi1 = (q & 1) != 0;
-    const int grp = threadIdx.x >> 2;
-    const float *tg = tab + (grp & (TAP_COPIES - 1)) * TAP_ROW;  // this group's copy
+    const int grp = tid >> 2;
+    const int gbase = threadIdx.x & 28;  // lane of q = 0 in this group
+    const float *vcopy = vt + (grp & 3) * 8;
+    const float *ucopy = ut + (grp & 3) * 8 + 2 * q;
     constexpr uint32_t FULL = 0xffffffffu;
     constexpr uint32_t GDD_PAD = 0x4040u;  // offsets 0, cell 0: a harmless table row
-    // Every lane of a warp runs the same number of group iterations (the loop bounds are
-    // per CTA), so the shuffles below always see all 32 lanes.
-    const int ngroups_iter = (it.cend - it.cbeg + DG_GROUPS - 1) / DG_GROUPS;
-    for (int gi = 0; gi < ngroups_iter; gi++) {
-        const int c = it.cbeg + gi * DG_GROUPS + (threadIdx.x >> 2);
-        const bool live = c < it.cend;
-        const uint2 ch = live ? chunks[c] : make_uint2(0u, 0u);
-        const int start = (int)ch.x, len = live ? (int)(ch.y >> 16) : 0;
-        const int cell = (int)(ch.y & 4095u), lu = cell & 63, lv = cell >> 6;
-        float2 G0[NTAP], G1[NTAP];
-#pragma unroll
-        for (int b = 0; b < NTAP; b++) {
-            const float2 *row = &tile[(lv + b) * STILE + lu];
-            G0[b] = row[q];
-            G1[b] = row[q + 4];
+    for (uint32_t iter = 0;; iter++) {
+        if (tid == 0) s_next[team] = (long long)atomicAdd(counter, 1ull);
+        team_sync(team);  // also: the team's reads of its previous tile are done
+        const long long n = s_next[team];
+        if (n >= nitems) break;
+        const WorkItem it = items[n];
+        const int tu = it.tile % ntu, tv = it.tile / ntu;
+        if (tid == 0) {
+            // the previous item's generic-proxy writes to the tile (reflection halo) are
+            // ordered before this async-proxy write
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            // box origin: columns tu*64-6 (complex) -> float x = 2*(tu*64-6), rows tv*64-3
+            const int x = 2 * (tu * TILE - 2 * SUPP), y = tv * TILE - SUPP;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                         "r"(DG_TX_BYTES));
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(tile)),
+                "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+                : "memory");
+            prefetch_l2_range(chunks, it.cbeg, it.cend, 8);
+            // the first DG_PREFETCH visibilities' words only: whole items of all resident
+            // teams would not fit in L2 together (measured: the full range evicts what it
+            // fetched)
+            const int pf_end = min(it.vend, it.vbeg + DG_PREFETCH);
+            prefetch_l2_range(gdd, it.vbeg, pf_end, 4);
+            if (MODE == 0) prefetch_l2_range(fobs, it.vbeg, pf_end, 8);
         }
-        // the warp iterates to the longest chunk among its 8 groups
-        int wlen = len;
-#pragma unroll
-        for (int d = 4; d < 32; d <<= 1) wlen = max(wlen, __shfl_xor_sync(FULL, wlen, d));
-        // lane q loads the offset word and observed value of visibility q of the next batch
-        // (one coalesced load per group); the group shares the words by shuffle
-        const int gbase = threadIdx.x & 28;  // lane of q = 0 in this group
-        uint32_t gqn = q < len ? gdd[start + q] : GDD_PAD;
-        float2 obn = make_float2(0.f, 0.f);
-        if (MODE == 0 && q < len) obn = fobs[start + q];
-        for (int k = 0; k < wlen; k += 4) {
-            const int pq = start + k + q;
-            const bool mine = k + q < len;
-            const float2 ob = obn;
-            const uint32_t gq = gqn;
-            if (k + 4 + q < len) {
-                gqn = gdd[pq + 4];
-                if (MODE == 0) obn = fobs[pq + 4];
+        {
+            uint32_t done = 0;
+            const uint32_t parity = iter & 1u;
+            for (int spin = 0; spin < (1 << 24) && !done; spin++) {
+                asm volatile(
+                    "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;"
+                    " selp.u32 %0, 1, 0, p; }"
+                    : "=r"(done)
+                    : "r"(smem_u32(bar)), "r"(parity)
+                    : "memory");
             }
-            float pr[4], pim[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const uint32_t g = __shfl_sync(FULL, gq, gbase + u);
-                const Taps t = read_taps(tg, q, g);
-                const float2 gu = t.gu;
-                const float *gv = t.gv;
-                float c0r = 0.f, c0i = 0.f, c1r = 0.f, c1i = 0.f;
-#pragma unroll
-                for (int b = 0; b < NTAP; b++) {
-                    c0r = fmaf(gv[b], G0[b].x, c0r);
-                    c0i = fmaf(gv[b], G0[b].y, c0i);
-                    c1r = fmaf(gv[b], G1[b].x, c1r);
-                    c1i = fmaf(gv[b], G1[b].y, c1i);
-                }
-                pr[u] = fmaf(gu.y, c1r, gu.x * c0r);
-                pim[u] = fmaf(gu.y, c1i, gu.x * c0i);
+            if (!team_and(team, done != 0)) {
+                if (tid == 0) atomicExch(&status[STATUS_TIMEOUT], 1);
+                return;
             }
-            // butterfly over lane bit 1: keep visibilities {0,1} (or {2,3}), pass the others
-            float k0r = hi2 ? pr[2] : pr[0], k0i = hi2 ? pim[2] : pim[0];
-            float k1r = hi2 ? pr[3] : pr[1], k1i = hi2 ? pim[3] : pim[1];
-            const float s0r = hi2 ? pr[0] : pr[2], s0i = hi2 ? pim[0] : pim[2];
-            const float s1r = hi2 ? pr[1] : pr[3], s1i = hi2 ? pim[1] : pim[3];
-            k0r += __shfl_xor_sync(FULL, s0r, 2);
-            k0i += __shfl_xor_sync(FULL, s0i, 2);
-            k1r += __shfl_xor_sync(FULL, s1r, 2);
-            k1i += __shfl_xor_sync(FULL, s1i, 2);
-            // butterfly over lane bit 0: keep visibility q
-            float tr = hi1 ? k1r : k0r, ti = hi1 ? k1i : k0i;
-            tr += __shfl_xor_sync(FULL, hi1 ? k0r : k1r, 1);
-            ti += __shfl_xor_sync(FULL, hi1 ? k0i : k1i, 1);
-            if (!mine || (gq & GDD_EXCEPTION)) continue;
-            const float inv = 1.0f / (rsum[gq & 0xFFu] * rsum[(gq >> 8) & 0xFFu]);
-            float mr = tr * inv, mi = ti * inv;
-            if (MODE == 0) {
-                *rec_res(rec, pq) = make_float2(ob.x - mr, ob.y - mi);
-            } else {
-                // caller's frame, staged in plan order (k_gather_user puts it in the
-                // caller's order with coalesced writes)
-                if (gconj[pq]) mi = -mi;
-                float2 vv = make_float2(mr, mi);
-                if (rot) {
-                    const float2 rt = rot[pq];
-                    vv = make_float2(mr * rt.x - mi * rt.y, mr * rt.y + mi * rt.x);
+        }
+        if (refl && tu == 0) {
+            // GRDDEH2D's reflection branch (grd/grddeh2d.f:123-158) in the tile: halo columns
+            // 3..5 stand for u = -3..-1 (left of the v axis; TMA filled them with zeros) and
+            // receive conj(G(-u, 2*VORIGIN - v)), the values that branch reads there
+            for (int k = tid; k < STILE * SUPP; k += TEAM_THREADS) {
+                const int r = k / SUPP, c = SUPP + k % SUPP;    // c = 2*SUPP + u
+                const int vm = 2 * vorigin - (tv * TILE - SUPP + r + 1);  // mirrored 1-based row
+                float2 val = make_float2(0.f, 0.f);
+                if (vm >= 1 && vm <= nv) {
+                    const float2 gm = grid[(int64_t)(vm - 1) * pitch + (2 * SUPP - c)];
+                    val = make_float2(gm.x, -gm.y);
                 }
-                stage[pq] = make_float4(vv.x, vv.y, wt[pq], 0.f);
+                tile[r * STILE + c] = val;
+            }
+            team_sync(team);
+        }
+        // Every lane of a warp runs the same number of group iterations (the loop bounds are
+        // per item), so the shuffles below always see all 32 lanes.
+        const int ngroups_iter = (it.cend - it.cbeg + DG_GROUPS - 1) / DG_GROUPS;
+        for (int gi = 0; gi < ngroups_iter; gi++) {
+            const int c = it.cbeg + gi * DG_GROUPS + grp;
+            const bool live = c < it.cend;
+            const uint2 ch = live ? chunks[c] : make_uint2(0u, 0u);
+            const int start = (int)ch.x, len = live ? (int)(ch.y >> 16) : 0;
+            const int cell = (int)(ch.y & 4095u), lu = cell & 63, lv = cell >> 6;
+            float2 G0[NTAP], G1[NTAP];
+#pragma unroll
+            for (int b = 0; b < NTAP; b++) {
+                const float2 *row = &tile[(lv + b) * STILE + lu];
+                G0[b] = row[q];
+                G1[b] = row[q + 4];
+            }
+            // the warp iterates to the longest chunk among its 8 groups
+            int wlen = len;
+#pragma unroll
+            for (int d = 4; d < 32; d <<= 1) wlen = max(wlen, __shfl_xor_sync(FULL, wlen, d));
+            // lane q loads the offset word and observed value of visibility q of the next
+            // batch (one coalesced load per group); the group shares the words by shuffle
+            uint32_t gqn = q < len ? gdd[start + q] : GDD_PAD;
+            float2 obn = make_float2(0.f, 0.f);
+            if (MODE == 0 && q < len) obn = fobs[start + q];
+            for (int k = 0; k < wlen; k += 4) {
+                const int pq = start + k + q;
+                const bool mine = k + q < len;
+                const float2 ob = obn;
+                const uint32_t gq = gqn;
+                if (k + 4 + q < len) {
+                    gqn = gdd[pq + 4];
+                    if (MODE == 0) obn = fobs[pq + 4];
+                }
+                float pr[4], pim[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t g = __shfl_sync(FULL, gq, gbase + u);
+                    const float2 gu = *reinterpret_cast<const float2 *>(
+                        ucopy + ((g & 0xFFu) * 2 + ((g >> 16) & 1u)) * UT_ROW);
+                    const float4 *vr = reinterpret_cast<const float4 *>(vcopy + ((g >> 8) & 0xFFu) * VT_ROW);
+                    const float4 v0 = vr[0], v1 = vr[1];
+                    const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
+                    float c0r = 0.f, c0i = 0.f, c1r = 0.f, c1i = 0.f;
+#pragma unroll
+                    for (int b = 0; b < NTAP; b++) {
+                        c0r = fmaf(gv[b], G0[b].x, c0r);
+                        c0i = fmaf(gv[b], G0[b].y, c0i);
+                        c1r = fmaf(gv[b], G1[b].x, c1r);
+                        c1i = fmaf(gv[b], G1[b].y, c1i);
+                    }
+                    pr[u] = fmaf(gu.y, c1r, gu.x * c0r);
+                    pim[u] = fmaf(gu.y, c1i, gu.x * c0i);
+                }
+                // butterfly over lane bit 1: keep visibilities {0,1} (or {2,3}), pass the others
+                float k0r = hi2 ? pr[2] : pr[0], k0i = hi2 ? pim[2] : pim[0];
+                float k1r = hi2 ? pr[3] : pr[1], k1i = hi2 ? pim[3] : pim[1];
+                const float s0r = hi2 ? pr[0] : pr[2], s0i = hi2 ? pim[0] : pim[2];
+                const float s1r = hi2 ? pr[1] : pr[3], s1i = hi2 ? pim[1] : pim[3];
+                k0r += __shfl_xor_sync(FULL, s0r, 2);
+                k0i += __shfl_xor_sync(FULL, s0i, 2);
+                k1r += __shfl_xor_sync(FULL, s1r, 2);
+                k1i += __shfl_xor_sync(FULL, s1i, 2);
+                // butterfly over lane bit 0: keep visibility q
+                float tr = hi1 ? k1r : k0r, ti = hi1 ? k1i : k0i;
+                tr += __shfl_xor_sync(FULL, hi1 ? k0r : k1r, 1);
+                ti += __shfl_xor_sync(FULL, hi1 ? k0i : k1i, 1);
+                if (!mine || (gq & GDD_EXCEPTION)) continue;
+                const float inv = 1.0f / (rsum[gq & 0xFFu] * rsum[(gq >> 8) & 0xFFu]);
+                float mr = tr * inv, mi = ti * inv;
+                if (MODE == 0) {
+                    *rec_res(rec, pq) = make_float2(ob.x - mr, ob.y - mi);
+                } else {
+                    // caller's frame, staged in plan order (k_gather_user puts it in the
+                    // caller's order with coalesced writes)
+                    if (gconj[pq]) mi = -mi;
+                    float2 vv = make_float2(mr, mi);
+                    if (rot) {
+                        const float2 rt = rot[pq];
+                        vv = make_float2(mr * rt.x - mi * rt.y, mr * rt.y + mi * rt.x);
+                    }
+                    stage[pq] = make_float4(vv.x, vv.y, wt[pq], 0.f);
+                }
             }
         }
     }
@@ -800,8 +860,8 @@ int make_grid_tmap(CUtensorMap *map, const float *grid, int pitch, int nv) {
                               STILE * 2, STILE);
 }
 
-size_t grid_smem() { return sizeof(float) * (2 * STILE * STILE + TAP_FLOATS); }
-size_t degrid_smem() { return DG_BAR_OFF + 16; }
+size_t grid_smem() { return sizeof(float) * (GTAB_FLOATS + TEAMS * GTILE_FLOATS); }
+size_t degrid_smem() { return DG_BAR_OFF + 8 * TEAMS; }
 
 }  // namespace
 
@@ -891,7 +951,7 @@ int grid_finalize_scale(sde_ctx *ctx, const float2 *raw, const float2 *raw_lo, f
 }
 
 size_t grid_smem_bytes() { return grid_smem(); }
-int grid_ctas_per_sm() { return GRID_MINB; }
+int grid_ctas_per_sm() { return 1; }
 
 int launch_grid_batch(sde_ctx *ctx, int psf, int comp, const BatchPlan *d_plans,
                       const int64_t *d_item_start, int nplans, unsigned long long *d_counter,
@@ -957,18 +1017,23 @@ int plan_grid_raw(sde_plan *pl, int what, float2 *raw, float2 *raw_lo, bool lo_c
                                           (int)grid_smem()));
         attr = true;
     }
+    unsigned long long *counter;
+    SDE_TRY(ctx_scratch(ctx, "grid_counter", sizeof(unsigned long long), (void **)&counter));
+    SDE_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
     KTimer kt(ctx, what == SDE_GRID_PSF ? "grid_psf" : "grid");
-    const dim3 g((unsigned)pl->nitems), b(GRID_THREADS);
+    const int64_t want = (int64_t)ctx->num_sms;
+    const dim3 g((unsigned)(pl->nitems < want ? pl->nitems : want)), b(GRID_THREADS);
     const size_t sm = grid_smem();
     cudaStream_t st = ctx->stream;
+    const int64_t ni = pl->nitems;
     if (what == SDE_GRID_PSF && raw_lo)
-        k_grid<true, true><<<g, b, sm, st>>>(pl->items, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
+        k_grid<true, true><<<g, b, sm, st>>>(pl->items, ni, counter, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
     else if (what == SDE_GRID_PSF)
-        k_grid<true, false><<<g, b, sm, st>>>(pl->items, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
+        k_grid<true, false><<<g, b, sm, st>>>(pl->items, ni, counter, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
     else if (raw_lo)
-        k_grid<false, true><<<g, b, sm, st>>>(pl->items, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
+        k_grid<false, true><<<g, b, sm, st>>>(pl->items, ni, counter, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
     else
-        k_grid<false, false><<<g, b, sm, st>>>(pl->items, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
+        k_grid<false, false><<<g, b, sm, st>>>(pl->items, ni, counter, pl->chunks, pl->rec, pl->cft, raw, raw_lo, pl->pitch, pl->ntu, nu, nv);
     SDE_CHECK_LAUNCH();
     return SDE_OK;
 }
@@ -1021,17 +1086,22 @@ int plan_degrid(sde_plan *pl, const float *grid, int pitch, int mode, float2 *vi
     if (pl->nitems > 0) {
         CUtensorMap map;
         SDE_TRY(make_grid_tmap(&map, grid, pitch, nv));
+        unsigned long long *counter;
+        SDE_TRY(ctx_scratch(ctx, "degrid_counter", sizeof(unsigned long long), (void **)&counter));
+        SDE_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
+        const int64_t want = (int64_t)ctx->num_sms;
+        const unsigned nb = (unsigned)(pl->nitems < want ? pl->nitems : want);
         KTimer kt(ctx, "degrid");
         if (mode == 0)
-            k_degrid<0><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot,
-                pl->wt, nullptr, pl->ntu, (const float2 *)grid, pitch, nv, pl->spec.vorigin,
-                (int)(pl->spec.uorigin == 1), ctx->d_status);
+            k_degrid<0><<<nb, DG_THREADS, degrid_smem(), ctx->stream>>>(
+                map, pl->items, pl->nitems, counter, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec,
+                pl->gconj, pl->rot, pl->wt, nullptr, pl->ntu, (const float2 *)grid, pitch, nv,
+                pl->spec.vorigin, (int)(pl->spec.uorigin == 1), ctx->d_status);
         else
-            k_degrid<1><<<(unsigned)pl->nitems, DG_THREADS, degrid_smem(), ctx->stream>>>(
-                map, pl->items, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec, pl->gconj, pl->rot,
-                pl->wt, stage, pl->ntu, (const float2 *)grid, pitch, nv, pl->spec.vorigin,
-                (int)(pl->spec.uorigin == 1), ctx->d_status);
+            k_degrid<1><<<nb, DG_THREADS, degrid_smem(), ctx->stream>>>(
+                map, pl->items, pl->nitems, counter, pl->chunks, pl->gdd, pl->cft, pl->fobs, pl->rec,
+                pl->gconj, pl->rot, pl->wt, stage, pl->ntu, (const float2 *)grid, pitch, nv,
+                pl->spec.vorigin, (int)(pl->spec.uorigin == 1), ctx->d_status);
         SDE_CHECK_LAUNCH();
         if (mode == 1) {
             KTimer kg(ctx, "gather_user");

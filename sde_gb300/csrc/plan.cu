@@ -20,6 +20,7 @@ struct GParams {
     int uorigin, vorigin, nu, nv, supp, osamp;
     double s[9];
     int doshift, ntu;
+    int identity;  // SHIFT is exactly the identity matrix
     double twopi;
 };
 
@@ -30,15 +31,31 @@ struct DGeo {
 };
 
 // GRDDEH2D's per-visibility geometry (grd/grddeh2d.f:92-118): always rotated, FP32 cell.
+// With SHIFT exactly the identity the products and sums below are exact for finite
+// coordinates (1*x = x, 0*y = +-0, x + +-0 = x up to the sign of a zero, which no later step
+// can see), so ULOCAL = U, VLOCAL = V, WLOCAL = W and the phase is 0; the FP64 work is
+// skipped.  A zero phase gives COS = 1 and SIN = the phase itself, without the library calls.
 __device__ __forceinline__ DGeo degrid_geom(const GParams &p, float u, float v, float w) {
     DGeo g;
     double ug = (double)u, vg = (double)v, wg = (double)w;
-    double ul = __dadd_rn(__dadd_rn(__dmul_rn(p.s[0], ug), __dmul_rn(p.s[1], vg)), __dmul_rn(p.s[2], wg));
-    double vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
-    double wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
+    double ul, vl, wl;
+    if (p.identity) {
+        ul = ug;
+        vl = vg;
+        wl = wg;
+    } else {
+        ul = __dadd_rn(__dadd_rn(__dmul_rn(p.s[0], ug), __dmul_rn(p.s[1], vg)), __dmul_rn(p.s[2], wg));
+        vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
+        wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
+    }
     double ph = __dmul_rn(p.twopi, __dsub_rn(wl, wg));
-    g.rc = (float)cos(ph);
-    g.rs = (float)sin(ph);
+    if (ph == 0.0) {
+        g.rc = 1.0f;
+        g.rs = (float)ph;
+    } else {
+        g.rc = (float)cos(ph);
+        g.rs = (float)sin(ph);
+    }
     float ucell = __double2float_rn(__dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset));
     float vcell = __double2float_rn(__dadd_rn(__dmul_rn((double)p.vscale, vl), (double)p.voffset));
     if (ucell > 0.0f) {
@@ -83,7 +100,8 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
                 double vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
                 double wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
                 double ph = __dmul_rn(p.twopi, __dsub_rn(wl, wg));
-                float c = (float)cos(ph), s = (float)(-sin(ph));
+                float c = ph == 0.0 ? 1.0f : (float)cos(ph);
+                float s = ph == 0.0 ? (float)(-ph) : (float)(-sin(ph));
                 fr = __fsub_rn(__fmul_rn(vv.x, c), __fmul_rn(vv.y, s));
                 fi = __fadd_rn(__fmul_rn(vv.x, s), __fmul_rn(vv.y, c));
                 ucell = __dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset);
@@ -464,6 +482,9 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         gp.nu = spec->nu; gp.nv = spec->nv; gp.supp = spec->supp; gp.osamp = spec->osamp;
         memcpy(gp.s, spec->shift, sizeof gp.s);
         gp.doshift = pl->doshift;
+        gp.identity = 1;
+        for (int k = 0; k < 9; k++)
+            if (spec->shift[k] != ((k % 4) == 0 ? 1.0 : 0.0)) gp.identity = 0;
         gp.ntu = pl->ntu;
         gp.twopi = (double)(8.0f * atanf(1.0f));  // TWOPI = 8 * ATAN(1.0), REAL (grdh2d.f:91)
 

@@ -77,17 +77,70 @@ __global__ void k_wkey(WParams p, const float *__restrict__ wt, const float *__r
     }
 }
 
-// One thread per run head: GWT(cell) = ((0 + w1) + w2) + ... in visibility order.
+// GWT(cell) = ((0 + w1) + w2) + ... in visibility order: FP32 additions in the reference's
+// order, so every cell's sum is one sequential chain.  One thread per run head sums a run of
+// at most SEG_SHORT entries; a longer run (dense cells hold up to ~2e5 visibilities) is put
+// on a list for k_segsum_long, where a warp streams it through registers.
+constexpr int SEG_SHORT = 32;
 __global__ void k_segsum(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-                         const unsigned long long *counts, float *gwt) {
+                         unsigned long long *counts, float *gwt, uint32_t *longq) {
     int64_t nvalid = (int64_t)counts[0];
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nvalid) return;
     uint32_t k = keys[p];
     if (p > 0 && keys[p - 1] == k) return;
+    if (p + SEG_SHORT < nvalid && keys[p + SEG_SHORT] == k) {
+        const unsigned long long slot = atomicAdd(&counts[2], 1ull);
+        longq[slot] = (uint32_t)p;
+        return;
+    }
     float s = 0.0f;
     for (int64_t q = p; q < nvalid && keys[q] == k; q++) s = __fadd_rn(s, __uint_as_float(vals[q]));
     gwt[k] = s;
+}
+
+// One warp per long run: 32 entries at a time are loaded (coalesced, the next block in flight
+// while the current one is added) and added in order by every lane from shuffles, so the
+// chain costs one FADD latency per entry instead of one memory latency.
+__global__ void k_segsum_long(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+                              const unsigned long long *counts, const uint32_t *__restrict__ longq,
+                              float *gwt) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int64_t nvalid = (int64_t)counts[0];
+    const int64_t nlong = (int64_t)counts[2];
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < nlong; r += nwarps) {
+        const int64_t p = longq[r];
+        const uint32_t k = keys[p];
+        float s = 0.0f;
+        int64_t q = p;
+        uint32_t kk = q + lane < nvalid ? keys[q + lane] : KEY_INVALID;
+        float vv = q + lane < nvalid ? __uint_as_float(vals[q + lane]) : 0.0f;
+        while (true) {
+            // the run is a prefix of the block (keys are sorted)
+            const int cnt = __popc(__ballot_sync(FULL, kk == k));
+            const int64_t qn = q + 32;
+            uint32_t kn = KEY_INVALID;
+            float vn = 0.0f;
+            if (cnt == 32) {
+                if (qn + lane < nvalid) {
+                    kn = keys[qn + lane];
+                    vn = __uint_as_float(vals[qn + lane]);
+                }
+#pragma unroll
+                for (int j = 0; j < 32; j++) s = __fadd_rn(s, __shfl_sync(FULL, vv, j));
+            } else {
+                for (int j = 0; j < cnt; j++) s = __fadd_rn(s, __shfl_sync(FULL, vv, j));
+                break;
+            }
+            q = qn;
+            kk = kn;
+            vv = vn;
+        }
+        if (lane == 0) gwt[k] = s;
+    }
 }
 
 // Deterministic FP64 sums (block partials in a fixed order).
@@ -246,7 +299,12 @@ int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const 
         k_wkey<<<ceil_div(nvis, T), T, 0, st>>>(p, wt, u, v, w, nvis, keys, vals, counts);
         SDE_CHECK_LAUNCH();
         SDE_TRY(launch_radix_sort_u32(ctx, keys, vals, nvis, key_bits(ncell), ktmp, vtmp));
-        k_segsum<<<ceil_div(nvis, T), T, 0, st>>>(keys, vals, counts, gwt);
+        uint32_t *longq;
+        SDE_TRY(ctx_scratch(ctx, "w_longq", sizeof(uint32_t) * (size_t)(nvis / (SEG_SHORT + 1) + 1),
+                            (void **)&longq));
+        k_segsum<<<ceil_div(nvis, T), T, 0, st>>>(keys, vals, counts, gwt, longq);
+        SDE_CHECK_LAUNCH();
+        k_segsum_long<<<ctx->num_sms * 8, 256, 0, st>>>(keys, vals, counts, longq, gwt);
         SDE_CHECK_LAUNCH();
     }
     float f2 = 1.0f, d2 = 0.0f;
