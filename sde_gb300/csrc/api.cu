@@ -188,6 +188,10 @@ extern "C" int sde_ctx_create(sde_ctx **out, int device) {
         sde_ctx_destroy(c);
         return SDE_ENOMEM;
     }
+    if ((rc = clean_preload(c)) != SDE_OK) {
+        sde_ctx_destroy(c);
+        return rc;
+    }
     float cf[CFLEN];
     sf_cf_table(cf);
     cudaMemcpyAsync(c->d_cf, cf, sizeof cf, cudaMemcpyHostToDevice, c->stream);

@@ -177,14 +177,23 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
         }
         const int offx = A.pmpx + pmx, offy = A.pmpy + pmy;
         Cand lc{-1.0f, INT32_MAX, 0.0f};
-        for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
-            const int iy = (int)(k / A.nx) + 1, ix = (int)(k - (int64_t)(iy - 1) * A.nx) + 1;
-            const int64_t flat = (int64_t)(offx - ix - 1) + (int64_t)(offy - iy - 1) * A.pnx;
+        // the window has < 2^31 pixels: 32-bit positions, the pixel's (ix, iy) stepped along
+        // with it (one division per thread, not per pixel)
+        int kk = (int)lo + (int)threadIdx.x;
+        int iy0 = kk / A.nx, ix0 = kk - iy0 * A.nx;  // 0-based
+        for (; kk < (int)hi; kk += blockDim.x) {
+            // PSF(OFFX-IX, OFFY-IY) with 1-based IX = ix0 + 1, IY = iy0 + 1
+            const int64_t flat = (int64_t)(offx - ix0 - 2) + (int64_t)(offy - iy0 - 2) * A.pnx;
             const float p = (flat >= 0 && flat < pnpix) ? A.psf[flat] : 0.0f;
-            const float bx = A.box ? A.box[k] : 1.0f;
-            const float r = __fsub_rn(A.res[k], __fmul_rn(__fmul_rn(pntsub, p), bx));
-            A.res[k] = r;
-            lc = better(lc, Cand{fabsf(r), (int32_t)k, r});
+            const float bx = A.box ? A.box[kk] : 1.0f;
+            const float r = __fsub_rn(A.res[kk], __fmul_rn(__fmul_rn(pntsub, p), bx));
+            A.res[kk] = r;
+            lc = better(lc, Cand{fabsf(r), (int32_t)kk, r});
+            ix0 += blockDim.x;
+            while (ix0 >= A.nx) {
+                ix0 -= A.nx;
+                iy0++;
+            }
         }
         lc = block_best(lc);
         cur ^= 1;
@@ -307,6 +316,22 @@ int sde_image_scale_by_inverse(sde_ctx *ctx, float *image, int64_t n, const floa
     return SDE_OK;
 }
 
+// The CLEAN kernels are loaded when the context is created (with CUDA's lazy module
+// loading a kernel's first launch would otherwise load it, ~18 ms measured on the first
+// sde_hogbom of a process), and the cooperative launch's occupancy is queried once.
+int clean_preload(sde_ctx *ctx) {
+    cudaFuncAttributes a;
+    SDE_CUDA_TRY(cudaFuncGetAttributes(&a, k_isamax_part));
+    SDE_CUDA_TRY(cudaFuncGetAttributes(&a, k_isamax_final));
+    SDE_CUDA_TRY(cudaFuncGetAttributes(&a, k_max_part));
+    SDE_CUDA_TRY(cudaFuncGetAttributes(&a, k_max_final));
+    SDE_CUDA_TRY(cudaFuncGetAttributes(&a, k_scale_inv));
+    int per_sm = 0;
+    SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom, CL_THREADS, 0));
+    ctx->hogbom_per_sm = per_sm;
+    return SDE_OK;
+}
+
 int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *box, int nx, int ny,
                int pnx, int pny, float gain, int nsub, int bsub, float flux, float tflux_in,
                float *cln, float *res, float *cflux, int *cx, int *cy, volatile int *cancel_flag,
@@ -330,8 +355,8 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
     int pmpy = 1 + (ipeak - pmpx + 1) / pnx;
     if (pmpx >= pnx) pmpx = pnx / 2;
     if (pmpy >= pny) pmpy = pny / 2;
-    int per_sm = 0;
-    SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom, CL_THREADS, 0));
+    int per_sm = ctx->hogbom_per_sm;
+    if (per_sm < 1) SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom, CL_THREADS, 0));
     if (per_sm < 1) {
         sde_set_error("sde_hogbom: kernel cannot be resident");
         return SDE_ECUDA;

@@ -128,6 +128,7 @@ struct sde_ctx {
     int64_t nlaunch = 0;
     // gridding sums across work items with TwoSum compensation (sde_ctx_set_compensated)
     bool compensated = true;
+    int hogbom_per_sm = 0;            // resident k_hogbom CTAs per SM (queried at creation)
     const void *lo_clean = nullptr;  // compensation plane of the raw-grid scratch known to be zero
     struct EvPair {
         const char *name;
@@ -249,6 +250,7 @@ struct FftBatch {
     float *image[FFT_MAXB];
     const float *scale[FFT_MAXB];
 };
+int clean_preload(sde_ctx *ctx);  // loads the CLEAN kernels, caches their occupancy
 size_t grid_smem_bytes();
 int grid_ctas_per_sm();  // resident persistent gridding CTAs per SM
 // 2-D FP32 tensor map for cp.async.bulk.tensor (grid.cu): width floats x rows, row pitch in

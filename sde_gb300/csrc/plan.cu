@@ -21,8 +21,16 @@ struct GParams {
     double s[9];
     int doshift, ntu;
     int identity;  // SHIFT is exactly the identity matrix
+    int fast;      // identity SHIFT and UOFFSET = VOFFSET = 0 (see k_plan_geom)
     double twopi;
 };
+
+// NINT of a double, half away from zero (Fortran NINT): x + 0.5 is exact for |x| < 2^52, so
+// floor(x + 0.5) rounds halves up, and the negative side mirrors it.  Callers keep |x| far
+// below 2^31.
+__device__ __forceinline__ int nint_dd(double x) {
+    return x >= 0.0 ? __double2int_rd(__dadd_rn(x, 0.5)) : -__double2int_rd(__dadd_rn(-x, 0.5));
+}
 
 struct DGeo {
     int nud, nvd, dui, dvi;
@@ -31,31 +39,26 @@ struct DGeo {
 };
 
 // GRDDEH2D's per-visibility geometry (grd/grddeh2d.f:92-118): always rotated, FP32 cell.
-// With SHIFT exactly the identity the products and sums below are exact for finite
-// coordinates (1*x = x, 0*y = +-0, x + +-0 = x up to the sign of a zero, which no later step
-// can see), so ULOCAL = U, VLOCAL = V, WLOCAL = W and the phase is 0; the FP64 work is
-// skipped.  A zero phase gives COS = 1 and SIN = the phase itself, without the library calls.
-__device__ __forceinline__ DGeo degrid_geom(const GParams &p, float u, float v, float w) {
+// COS and SIN of GRDH2D/GRDDEH2D's phase in DOUBLE.  Below 2^-27 in magnitude the correctly
+// rounded values are exactly 1 and the phase itself (|sin x - x| <= |x|^3/6 and x^2/2 are
+// below half an ulp there), which is what a phase-centre rotation that differs from the
+// identity only by rounding (CRDSHIFT's sin^2 + cos^2 on the diagonal) produces for every
+// visibility: no library call is made for it.
+__device__ __forceinline__ void phase_cos_sin(double ph, double &c, double &s) {
+    if (fabs(ph) < 0x1p-27) {
+        c = 1.0;
+        s = ph;
+    } else {
+        sincos(ph, &s, &c);
+    }
+}
+
+// GRDDEH2D's per-visibility geometry (grd/grddeh2d.f:92-118) from the rotated coordinates:
+// FP32 cell, the REAL rotation (rc, rs).
+__device__ __forceinline__ DGeo degrid_cell(const GParams &p, double ul, double vl, float rc, float rs) {
     DGeo g;
-    double ug = (double)u, vg = (double)v, wg = (double)w;
-    double ul, vl, wl;
-    if (p.identity) {
-        ul = ug;
-        vl = vg;
-        wl = wg;
-    } else {
-        ul = __dadd_rn(__dadd_rn(__dmul_rn(p.s[0], ug), __dmul_rn(p.s[1], vg)), __dmul_rn(p.s[2], wg));
-        vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
-        wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
-    }
-    double ph = __dmul_rn(p.twopi, __dsub_rn(wl, wg));
-    if (ph == 0.0) {
-        g.rc = 1.0f;
-        g.rs = (float)ph;
-    } else {
-        g.rc = (float)cos(ph);
-        g.rs = (float)sin(ph);
-    }
+    g.rc = rc;
+    g.rs = rs;
     float ucell = __double2float_rn(__dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset));
     float vcell = __double2float_rn(__dadd_rn(__dmul_rn((double)p.vscale, vl), (double)p.voffset));
     if (ucell > 0.0f) {
@@ -74,44 +77,115 @@ __device__ __forceinline__ DGeo degrid_geom(const GParams &p, float u, float v, 
     return g;
 }
 
-// Per visibility (caller order): gridding key, packed offsets, observed value in the
-// gridding frame, rotation, conjugation flag.
+// The rotation ULOCAL, VLOCAL, WLOCAL = SHIFT applied to (U, V, W) in DOUBLE (GRDDEH2D
+// always applies it; GRDH2D when DOSHIFT).  With SHIFT exactly the identity the products
+// and sums are exact for finite coordinates (1*x = x, 0*y = +-0, x + +-0 = x up to the sign
+// of a zero, which no later step can see), so they are skipped.
+__device__ __forceinline__ void rotate_uvw(const GParams &p, double ug, double vg, double wg,
+                                           double &ul, double &vl, double &wl) {
+    if (p.identity) {
+        ul = ug;
+        vl = vg;
+        wl = wg;
+    } else {
+        ul = __dadd_rn(__dadd_rn(__dmul_rn(p.s[0], ug), __dmul_rn(p.s[1], vg)), __dmul_rn(p.s[2], wg));
+        vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
+        wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
+    }
+}
+
+// GRDDEH2D's per-visibility geometry (grd/grddeh2d.f:92-118): always rotated, FP32 cell.
+__device__ __forceinline__ DGeo degrid_geom(const GParams &p, float u, float v, float w) {
+    const double ug = (double)u, vg = (double)v, wg = (double)w;
+    double ul, vl, wl, c, s;
+    rotate_uvw(p, ug, vg, wg, ul, vl, wl);
+    phase_cos_sin(__dmul_rn(p.twopi, __dsub_rn(wl, wg)), c, s);
+    return degrid_cell(p, ul, vl, (float)c, (float)s);
+}
+
+// Bit 28 of a caller-order degridding word carries the gridding-frame conjugation (the
+// plan's own words leave it clear).
+constexpr uint32_t GDD_GCONJ_U = 1u << 28;
+
+// The fast path (identity SHIFT, zero offsets: every uvmap/mapper call without a phase-centre
+// shift) keeps the reference's results with fewer FP64 operations, which GB300 runs at a
+// small fraction of its FP32 rate:
+//   * GRDH2D's UCELL = USCALE*ULOCAL + UOFFSET with ULOCAL = DBLE(U): the product of two
+//     REALs is exact in DOUBLE and adding 0 changes nothing, so UCELL is that product; the
+//     origin, NINT and the oversampled offsets follow in DOUBLE as before;
+//   * GRDDEH2D's REAL cell SNGL(USCALE*ULOCAL + UOFFSET) is then the once-rounded REAL
+//     product, __fmul_rn(USCALE, U), and its phase is 0 (COS 1, SIN 0);
+//   * NINT by nint_dd (one add and one conversion) in place of the library's round().
+// Points so far off the grid that |UCELL| >= 2^30 are treated as outside it.
+__device__ __forceinline__ DGeo degrid_geom_fast(const GParams &p, float u, float v) {
+    DGeo g;
+    float ucell = __fmul_rn(p.uscale, u), vcell = __fmul_rn(p.vscale, v);
+    g.conj = __dmul_rn((double)p.uscale, (double)u) > 0.0;
+    g.rc = 1.0f;
+    g.rs = 0.0f;
+    if (ucell > 0.0f) {
+        ucell = __fadd_rn(ucell, (float)p.uorigin);
+        vcell = __fadd_rn(vcell, (float)p.vorigin);
+    } else {
+        ucell = __fadd_rn(-ucell, (float)p.uorigin);
+        vcell = __fadd_rn(-vcell, (float)p.vorigin);
+    }
+    g.nud = nint_f(ucell);
+    g.nvd = nint_f(vcell);
+    g.valid = !(g.nud + p.supp > p.nu) && !(g.nvd + p.supp > p.nv) && !(g.nvd - p.supp < 1);
+    g.dui = nint_f(__fmul_rn((float)p.osamp, __fsub_rn((float)g.nud, ucell)));
+    g.dvi = nint_f(__fmul_rn((float)p.osamp, __fsub_rn((float)g.nvd, vcell)));
+    return g;
+}
+
+// Per visibility (caller order): gridding key; the plan record {WT, packed GRDH2D offsets |
+// column-in-pair << 16, observed value in the gridding frame} (the gather moves it whole);
+// the degridding word with the conjugation in bit 28; the rotation.
 __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float *__restrict__ v,
                             const float *__restrict__ w, const float2 *__restrict__ vis,
                             const float *__restrict__ wt, int64_t n, uint32_t *keys,
-                            uint32_t *vals, uint16_t *gdg, uint32_t *gdd, float2 *fobs,
-                            float2 *rot, uint8_t *gconj, unsigned long long *counts) {
+                            uint32_t *vals, float4 *rec_u, uint32_t *gdd_u, float2 *rot,
+                            unsigned long long *counts) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t nvalid = 0, nexc = 0;
+    const float wi = i < n ? wt[i] : 0.0f;
     if (i < n) {
-        float wi = wt[i];
         uint32_t key = KEY_INVALID, pdd = 0;
         uint16_t pdg = 0;
         float2 f = make_float2(0.f, 0.f), r = make_float2(1.f, 0.f);
         uint8_t gc = 0;
         if (wi > 0.0f) {
             float2 vv = vis[i];
-            double ug = (double)u[i], vg = (double)v[i], wg = (double)w[i];
+            const float uf = u[i], vf = v[i], wf = w[i];
             double ucell, vcell;
             float fr, fi;
-            DGeo dg = degrid_geom(p, u[i], v[i], w[i]);
-            if (p.doshift) {
-                double ul = __dadd_rn(__dadd_rn(__dmul_rn(p.s[0], ug), __dmul_rn(p.s[1], vg)), __dmul_rn(p.s[2], wg));
-                double vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
-                double wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
-                double ph = __dmul_rn(p.twopi, __dsub_rn(wl, wg));
-                float c = ph == 0.0 ? 1.0f : (float)cos(ph);
-                float s = ph == 0.0 ? (float)(-ph) : (float)(-sin(ph));
-                fr = __fsub_rn(__fmul_rn(vv.x, c), __fmul_rn(vv.y, s));
-                fi = __fadd_rn(__fmul_rn(vv.x, s), __fmul_rn(vv.y, c));
-                ucell = __dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset);
-                vcell = __dadd_rn(__dmul_rn((double)p.vscale, vl), (double)p.voffset);
-                r = make_float2(dg.rc, dg.rs);
-            } else {
+            DGeo dg;
+            if (p.fast) {
+                dg = degrid_geom_fast(p, uf, vf);
                 fr = vv.x;
                 fi = vv.y;
-                ucell = __dadd_rn(__dmul_rn((double)p.uscale, ug), (double)p.uoffset);
-                vcell = __dadd_rn(__dmul_rn((double)p.vscale, vg), (double)p.voffset);
+                ucell = __dmul_rn((double)p.uscale, (double)uf);
+                vcell = __dmul_rn((double)p.vscale, (double)vf);
+            } else {
+                // one rotation and one phase serve GRDDEH2D (always) and GRDH2D (DOSHIFT)
+                const double ug = (double)uf, vg = (double)vf, wg = (double)wf;
+                double ul, vl, wl, cd, sd;
+                rotate_uvw(p, ug, vg, wg, ul, vl, wl);
+                phase_cos_sin(__dmul_rn(p.twopi, __dsub_rn(wl, wg)), cd, sd);
+                dg = degrid_cell(p, ul, vl, (float)cd, (float)sd);
+                if (p.doshift) {
+                    const float c = (float)cd, s = (float)(-sd);
+                    fr = __fsub_rn(__fmul_rn(vv.x, c), __fmul_rn(vv.y, s));
+                    fi = __fadd_rn(__fmul_rn(vv.x, s), __fmul_rn(vv.y, c));
+                    ucell = __dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset);
+                    vcell = __dadd_rn(__dmul_rn((double)p.vscale, vl), (double)p.voffset);
+                    r = make_float2(dg.rc, dg.rs);
+                } else {
+                    fr = vv.x;
+                    fi = vv.y;
+                    ucell = __dadd_rn(__dmul_rn((double)p.uscale, ug), (double)p.uoffset);
+                    vcell = __dadd_rn(__dmul_rn((double)p.vscale, vg), (double)p.voffset);
+                }
             }
             if (ucell > 0.0) {
                 fi = -fi;
@@ -122,11 +196,12 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
                 ucell = __dadd_rn(-ucell, (double)(float)p.uorigin);
                 vcell = __dadd_rn(-vcell, (double)(float)p.vorigin);
             }
-            int nuc = nint_d(ucell), nvc = nint_d(vcell);
-            bool gvalid = !(nuc + 2 * p.supp > p.nu) && !(nvc + p.supp > p.nv) && !(nvc - p.supp < 1);
+            const bool sane = fabs(ucell) < 1073741824.0 && fabs(vcell) < 1073741824.0;
+            int nuc = sane ? nint_dd(ucell) : 0, nvc = sane ? nint_dd(vcell) : 0;
+            bool gvalid = sane && !(nuc + 2 * p.supp > p.nu) && !(nvc + p.supp > p.nv) && !(nvc - p.supp < 1);
             if (gvalid) {
-                int dug = nint_d(__dmul_rn((double)p.osamp, __dsub_rn((double)(float)nuc, ucell)));
-                int dvg = nint_d(__dmul_rn((double)p.osamp, __dsub_rn((double)(float)nvc, vcell)));
+                int dug = nint_dd(__dmul_rn((double)p.osamp, __dsub_rn((double)(float)nuc, ucell)));
+                int dvg = nint_dd(__dmul_rn((double)p.osamp, __dsub_rn((double)(float)nvc, vcell)));
                 int ucen = nuc + p.supp, vcen = nvc;  // 1-based, gridding frame
                 int tu = (ucen - 1) >> TILE_LOG2, lu = (ucen - 1) & (TILE - 1);
                 int tv = (vcen - 1) >> TILE_LOG2, lv = (vcen - 1) & (TILE - 1);
@@ -151,14 +226,14 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
         }
         keys[i] = key;
         vals[i] = (uint32_t)i;
-        gdg[i] = pdg;
-        gdd[i] = pdd;
-        fobs[i] = f;
+        // bit 16: column of the visibility's cell within its chunk's cell pair
+        const uint32_t off = (pdd >> 16) & 1u;
+        rec_u[i] = make_float4(wi, __uint_as_float((uint32_t)pdg | (off << 16)), f.x, f.y);
+        gdd_u[i] = pdd | (gc ? GDD_GCONJ_U : 0u);
         if (rot) rot[i] = r;
-        gconj[i] = gc;
     }
     unsigned mv = __ballot_sync(0xffffffffu, nvalid), me = __ballot_sync(0xffffffffu, nexc);
-    const unsigned mt = __ballot_sync(0xffffffffu, i < n && wt[i] > 0.0f);
+    const unsigned mt = __ballot_sync(0xffffffffu, i < n && wi > 0.0f);
     if ((threadIdx.x & 31) == 0) {
         if (mv) atomicAdd(&counts[0], (unsigned long long)__popc(mv));
         if (me) atomicAdd(&counts[1], (unsigned long long)__popc(me));
@@ -166,29 +241,28 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
     }
 }
 
-// Gather the per-visibility arrays into sorted order.
+// Gather the per-visibility arrays into sorted order: one 16-byte record and one word (and
+// the rotation when shifted) per visibility.  An exception that also grids learns its
+// sorted position here.
 __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned long long *counts,
-                              const float2 *__restrict__ fobs_u, const float *__restrict__ wt_u,
-                              const uint16_t *__restrict__ gdg_u, const uint32_t *__restrict__ gdd_u,
-                              const float2 *__restrict__ rot_u,
-                              const uint8_t *__restrict__ gconj_u, float2 *fobs, float4 *rec,
-                              float *wt, uint32_t *gdd, uint32_t *orig,
-                              float2 *rot, uint8_t *gconj, uint32_t *pos_of) {
+                              const float4 *__restrict__ rec_u, const uint32_t *__restrict__ gdd_u,
+                              const float2 *__restrict__ rot_u, const uint32_t *__restrict__ exc_slot,
+                              float2 *fobs, float4 *rec, float *wt, uint32_t *gdd, uint32_t *orig,
+                              float2 *rot, uint8_t *gconj, DegridExc *exc) {
     int64_t nv = (int64_t)counts[0];
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
     uint32_t i = perm[p];
-    float2 f = fobs_u[i];
-    fobs[p] = f;
-    wt[p] = wt_u[i];
-    // bit 16: column of the visibility's cell within its chunk's cell pair
-    const uint32_t off = (gdd_u[i] >> 16) & 1u;
-    rec[p] = make_float4(wt_u[i], __uint_as_float((uint32_t)gdg_u[i] | (off << 16)), f.x, f.y);
-    gdd[p] = gdd_u[i];
+    const float4 r = rec_u[i];
+    const uint32_t d = gdd_u[i];
+    rec[p] = r;
+    fobs[p] = make_float2(r.z, r.w);
+    wt[p] = r.x;
+    gdd[p] = d & ~GDD_GCONJ_U;
     orig[p] = i;
-    gconj[p] = gconj_u[i];
+    gconj[p] = (d & GDD_GCONJ_U) ? 1 : 0;
     if (rot) rot[p] = rot_u[i];
-    pos_of[i] = (uint32_t)p;
+    if ((d & GDD_EXCEPTION) && exc) exc[exc_slot[i]].pos = (int32_t)p;
 }
 
 // flags for the exception compaction
@@ -201,25 +275,25 @@ __global__ void k_exc_flag(const float *__restrict__ wt, const uint32_t *__restr
     flag[i] = f;
 }
 
+// (pos is set by k_plan_gather for the exceptions that also grid)
 __global__ void k_exc_write(GParams p, const float *__restrict__ u, const float *__restrict__ v,
                             const float *__restrict__ w, const float *__restrict__ wt,
-                            const uint32_t *__restrict__ keys_u, const uint8_t *__restrict__ gconj_u,
+                            const uint32_t *__restrict__ gdd_u,
                             const uint32_t *__restrict__ flag, const uint32_t *__restrict__ slot,
-                            const uint32_t *__restrict__ pos_of, int64_t n, DegridExc *exc,
-                            float *exc_wt, float2 *exc_rot) {
+                            int64_t n, DegridExc *exc, float *exc_wt, float2 *exc_rot) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !flag[i]) return;
-    DGeo g = degrid_geom(p, u[i], v[i], w[i]);
+    DGeo g = p.fast ? degrid_geom_fast(p, u[i], v[i]) : degrid_geom(p, u[i], v[i], w[i]);
     DegridExc e;
     e.orig = (uint32_t)i;
-    e.pos = keys_u[i] == KEY_INVALID ? -1 : (int32_t)pos_of[i];
+    e.pos = -1;
     e.nuc = g.nud;
     e.nvc = g.nvd;
     e.delui = (int16_t)g.dui;
     e.delvi = (int16_t)g.dvi;
     e.conj = g.conj;
     e.valid = g.valid;
-    e.gconj = gconj_u[i];
+    e.gconj = (gdd_u[i] & GDD_GCONJ_U) ? 1 : 0;
     e.pad = 0;
     uint32_t s = slot[i];
     exc[s] = e;
@@ -485,30 +559,27 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         gp.identity = 1;
         for (int k = 0; k < 9; k++)
             if (spec->shift[k] != ((k % 4) == 0 ? 1.0 : 0.0)) gp.identity = 0;
+        gp.fast = gp.identity && spec->uoffset == 0.0f && spec->voffset == 0.0f;
         gp.ntu = pl->ntu;
         gp.twopi = (double)(8.0f * atanf(1.0f));  // TWOPI = 8 * ATAN(1.0), REAL (grdh2d.f:91)
 
-        uint32_t *keys, *vals, *ktmp, *vtmp, *gdd_u, *pos_of;
-        uint16_t *gdg_u;
-        float2 *fobs_u, *rot_u = nullptr;
-        uint8_t *gconj_u;
+        uint32_t *keys, *vals, *ktmp, *vtmp, *gdd_u;
+        float4 *rec_u;
+        float2 *rot_u = nullptr;
         unsigned long long *counts;
         PL_TRY(ctx_scratch(ctx, "pl_keys", 4 * n, (void **)&keys));
         PL_TRY(ctx_scratch(ctx, "pl_vals", 4 * n, (void **)&vals));
         PL_TRY(ctx_scratch(ctx, "pl_ktmp", 4 * n, (void **)&ktmp));
         PL_TRY(ctx_scratch(ctx, "pl_vtmp", 4 * n, (void **)&vtmp));
-        PL_TRY(ctx_scratch(ctx, "pl_gdg", 2 * n, (void **)&gdg_u));
         PL_TRY(ctx_scratch(ctx, "pl_gdd", 4 * n, (void **)&gdd_u));
-        PL_TRY(ctx_scratch(ctx, "pl_pos", 4 * n, (void **)&pos_of));
-        PL_TRY(ctx_scratch(ctx, "pl_fobs", 8 * n, (void **)&fobs_u));
+        PL_TRY(ctx_scratch(ctx, "pl_rec", 16 * n, (void **)&rec_u));
         if (pl->doshift) PL_TRY(ctx_scratch(ctx, "pl_rot", 8 * n, (void **)&rot_u));
-        PL_TRY(ctx_scratch(ctx, "pl_gconj", n, (void **)&gconj_u));
         PL_TRY(ctx_scratch(ctx, "pl_counts", 64, (void **)&counts));
         PL_CUDA(cudaMemsetAsync(counts, 0, 64, st));
         const int T = 256;
         if (nvis > 0) {
             k_plan_geom<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dvis, dwt, nvis, keys, vals,
-                                                       gdg_u, gdd_u, fobs_u, rot_u, gconj_u, counts);
+                                                       rec_u, gdd_u, rot_u, counts);
             PL_CUDA(cudaGetLastError());
         }
         // The user-order keys are needed again by the exception pass: keep a copy.
@@ -539,18 +610,13 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         PL_TRY(plan_alloc(pl, (void **)&pl->gconj, nv1));
         if (pl->doshift) PL_TRY(plan_alloc(pl, (void **)&pl->rot, 8 * nv1));
         PL_TRY(plan_alloc(pl, (void **)&pl->d_sums, 4 * sizeof(double)));
-        if (nvalid > 0) {
-            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, fobs_u, dwt, gdg_u, gdd_u,
-                                                           rot_u, gconj_u, pl->fobs, pl->rec,
-                                                           pl->wt, pl->gdd,
-                                                           pl->orig, pl->rot, pl->gconj, pos_of);
-            PL_CUDA(cudaGetLastError());
-        }
-        // exception list (also carries the GRDDEH2D geometry of non-gridding visibilities)
+        // exception list (also carries the GRDDEH2D geometry of non-gridding visibilities);
+        // the gather below fills in the sorted positions
         size_t ne1 = (size_t)(nexc > 0 ? nexc : 1);
         PL_TRY(plan_alloc(pl, (void **)&pl->exc, exc_bytes(ne1)));
+        uint32_t *slot = nullptr;
         if (nexc > 0) {
-            uint32_t *flag, *slot;
+            uint32_t *flag;
             PL_TRY(ctx_scratch(ctx, "pl_flag", 4 * n, (void **)&flag));
             PL_TRY(ctx_scratch(ctx, "pl_slot", 4 * n, (void **)&slot));
             k_exc_flag<<<ceil_div(nvis, T), T, 0, st>>>(dwt, keys_u, gdd_u, nvis, flag);
@@ -558,8 +624,15 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
             PL_TRY(launch_exclusive_scan_u32(ctx, flag, slot, nvis, nullptr));
             float *exc_wt = (float *)((char *)pl->exc + exc_wt_off(ne1));
             float2 *exc_rot = (float2 *)((char *)pl->exc + exc_rot_off(ne1));
-            k_exc_write<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dwt, keys_u, gconj_u, flag,
-                                                       slot, pos_of, nvis, pl->exc, exc_wt, exc_rot);
+            k_exc_write<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dwt, gdd_u, flag, slot, nvis,
+                                                       pl->exc, exc_wt, exc_rot);
+            PL_CUDA(cudaGetLastError());
+        }
+        if (nvalid > 0) {
+            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, rec_u, gdd_u, rot_u, slot,
+                                                           pl->fobs, pl->rec, pl->wt, pl->gdd,
+                                                           pl->orig, pl->rot, pl->gconj,
+                                                           nexc > 0 ? pl->exc : nullptr);
             PL_CUDA(cudaGetLastError());
         }
         // runs, chunks, work items

@@ -18,13 +18,18 @@ struct WParams {
     int uorigin, vorigin, nu, nv;
     double s[9];
     int doshift;
+    int near_identity;  // see wcell
 };
 
 // FP32 uv -> cell of the weighting routines (grd/grduwt2d.f:92-111, grd/grdruw2d.f:198-217).
 __device__ __forceinline__ bool wcell(const WParams &p, float u, float v, float w, int &uc,
                                       int &vc, float &ul, float &vl) {
     float ucell, vcell;
-    if (p.doshift) {
+    // With SHIFT(2,1) = SHIFT(3,1) = SHIFT(1,2) = SHIFT(3,2) = 0 and the diagonal within
+    // 2^-40 of 1 (CRDSHIFT without a shift: sin^2 + cos^2 can miss 1 by an ulp), the DOUBLE
+    // ULOCAL = SHIFT(1,1)*U + 0*V + 0*W and VLOCAL lie within |U|*2^-39 of U and V, far
+    // inside half a REAL ulp, so the REAL ULOCAL, VLOCAL are U and V themselves.
+    if (p.doshift && !p.near_identity) {
         double du = (double)u, dv = (double)v, dw = (double)w;
         ul = __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(p.s[0], du), __dmul_rn(p.s[1], dv)),
                                          __dmul_rn(p.s[2], dw)));
@@ -99,45 +104,79 @@ __global__ void k_segsum(const uint32_t *__restrict__ keys, const uint32_t *__re
     gwt[k] = s;
 }
 
-// One warp per long run: 32 entries at a time are loaded (coalesced, the next block in flight
-// while the current one is added) and added in order by every lane from shuffles, so the
-// chain costs one FADD latency per entry instead of one memory latency.
-__global__ void k_segsum_long(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-                              const unsigned long long *counts, const uint32_t *__restrict__ longq,
-                              float *gwt) {
+// One warp per long run.  Lane 0 finds the run's end (galloping then binary search over the
+// sorted keys), then the warp streams the run through shared memory in blocks of 256
+// entries -- the next block's coalesced loads in flight while lane 0 adds the current one
+// in order from 16-byte shared reads -- so the chain costs about one FADD latency per entry.
+constexpr int SEG_BLK = 256;
+constexpr int SEG_WARPS = 8;  // warps per block of k_segsum_long
+__global__ void __launch_bounds__(SEG_WARPS * 32) k_segsum_long(
+    const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+    const unsigned long long *counts, const uint32_t *__restrict__ longq, float *gwt) {
     constexpr unsigned FULL = 0xffffffffu;
+    __shared__ __align__(16) float buf[SEG_WARPS][2][SEG_BLK];
     const int64_t nvalid = (int64_t)counts[0];
     const int64_t nlong = (int64_t)counts[2];
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = warp; r < nlong; r += nwarps) {
         const int64_t p = longq[r];
         const uint32_t k = keys[p];
-        float s = 0.0f;
-        int64_t q = p;
-        uint32_t kk = q + lane < nvalid ? keys[q + lane] : KEY_INVALID;
-        float vv = q + lane < nvalid ? __uint_as_float(vals[q + lane]) : 0.0f;
-        while (true) {
-            // the run is a prefix of the block (keys are sorted)
-            const int cnt = __popc(__ballot_sync(FULL, kk == k));
-            const int64_t qn = q + 32;
-            uint32_t kn = KEY_INVALID;
-            float vn = 0.0f;
-            if (cnt == 32) {
-                if (qn + lane < nvalid) {
-                    kn = keys[qn + lane];
-                    vn = __uint_as_float(vals[qn + lane]);
-                }
-#pragma unroll
-                for (int j = 0; j < 32; j++) s = __fadd_rn(s, __shfl_sync(FULL, vv, j));
-            } else {
-                for (int j = 0; j < cnt; j++) s = __fadd_rn(s, __shfl_sync(FULL, vv, j));
-                break;
+        int64_t end = 0;
+        if (lane == 0) {
+            // keys[p + SEG_SHORT] == k (why the run is here); find the first index past the run
+            int64_t lo = p + SEG_SHORT, step = 64;
+            while (lo + step < nvalid && keys[lo + step] == k) {
+                lo += step;
+                step *= 2;
             }
-            q = qn;
-            kk = kn;
-            vv = vn;
+            int64_t hi = lo + step < nvalid ? lo + step : nvalid;  // keys[hi] != k or hi = nvalid
+            while (hi - lo > 1) {
+                const int64_t mid = lo + (hi - lo) / 2;
+                if (keys[mid] == k) lo = mid; else hi = mid;
+            }
+            end = hi;
+        }
+        end = __shfl_sync(FULL, end, 0);
+        const int64_t len = end - p;
+        const int nblk = (int)((len + SEG_BLK - 1) / SEG_BLK);
+        float reg[SEG_BLK / 32];
+#pragma unroll
+        for (int j = 0; j < SEG_BLK / 32; j++) {
+            const int64_t q = p + j * 32 + lane;
+            reg[j] = q < end ? __uint_as_float(vals[q]) : 0.0f;
+        }
+        float s = 0.0f;
+        for (int b = 0; b < nblk; b++) {
+            float *cur = buf[wib][b & 1];
+#pragma unroll
+            for (int j = 0; j < SEG_BLK / 32; j++) cur[j * 32 + lane] = reg[j];
+            __syncwarp();
+            if (b + 1 < nblk) {
+#pragma unroll
+                for (int j = 0; j < SEG_BLK / 32; j++) {
+                    const int64_t q = p + (int64_t)(b + 1) * SEG_BLK + j * 32 + lane;
+                    reg[j] = q < end ? __uint_as_float(vals[q]) : 0.0f;
+                }
+            }
+            if (lane == 0) {
+                const int cnt = (int)(len - (int64_t)b * SEG_BLK < SEG_BLK ? len - (int64_t)b * SEG_BLK : SEG_BLK);
+                const float4 *c4 = reinterpret_cast<const float4 *>(cur);
+                if (cnt == SEG_BLK) {
+#pragma unroll 8
+                    for (int j = 0; j < SEG_BLK / 4; j++) {
+                        const float4 x = c4[j];
+                        s = __fadd_rn(s, x.x);
+                        s = __fadd_rn(s, x.y);
+                        s = __fadd_rn(s, x.z);
+                        s = __fadd_rn(s, x.w);
+                    }
+                } else {
+                    for (int j = 0; j < cnt; j++) s = __fadd_rn(s, cur[j]);
+                }
+            }
+            __syncwarp();
         }
         if (lane == 0) gwt[k] = s;
     }
@@ -188,12 +227,19 @@ __global__ void __launch_bounds__(RED_THREADS) k_sumlocwt_part(const float *gwt,
     if (threadIdx.x == 0) partial[blockIdx.x] = r;
 }
 
-__global__ void k_sum_partials(const double *partial, int n, double *out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s = 0.0;
-        for (int k = 0; k < n; k++) s = __dadd_rn(s, partial[k]);
-        *out = s;
+// The partials in a fixed order: thread t adds partials t, t + RED_THREADS, ..., then a
+// fixed tree over the threads (deterministic for a given partial count).
+__global__ void __launch_bounds__(RED_THREADS) k_sum_partials(const double *partial, int n, double *out) {
+    __shared__ double sh[RED_THREADS];
+    double s = 0.0;
+    for (int k = threadIdx.x; k < n; k += RED_THREADS) s = __dadd_rn(s, partial[k]);
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = RED_THREADS / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) sh[threadIdx.x] = __dadd_rn(sh[threadIdx.x], sh[threadIdx.x + h]);
+        __syncthreads();
     }
+    if (threadIdx.x == 0) *out = sh[0];
 }
 
 struct AzParams {
@@ -282,6 +328,8 @@ int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const 
     p.uorigin = uorigin; p.vorigin = vorigin; p.nu = nu; p.nv = nv;
     memcpy(p.s, shift, sizeof p.s);
     p.doshift = (shift[0] != 1.0) || (shift[4] != 1.0) || (shift[8] != 1.0);
+    p.near_identity = shift[1] == 0.0 && shift[2] == 0.0 && shift[3] == 0.0 && shift[5] == 0.0 &&
+                      fabs(shift[0] - 1.0) <= 0x1p-40 && fabs(shift[4] - 1.0) <= 0x1p-40;
     const int64_t ncell = (int64_t)nu * nv;
     if (!gwt) SDE_TRY(ctx_scratch(ctx, "w_gwt", sizeof(float) * (size_t)ncell, (void **)&gwt));
     SDE_CUDA_TRY(cudaMemsetAsync(gwt, 0, sizeof(float) * (size_t)ncell, st));
@@ -304,7 +352,7 @@ int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const 
                             (void **)&longq));
         k_segsum<<<ceil_div(nvis, T), T, 0, st>>>(keys, vals, counts, gwt, longq);
         SDE_CHECK_LAUNCH();
-        k_segsum_long<<<ctx->num_sms * 8, 256, 0, st>>>(keys, vals, counts, longq, gwt);
+        k_segsum_long<<<ctx->num_sms * 4, SEG_WARPS * 32, 0, st>>>(keys, vals, counts, longq, gwt);
         SDE_CHECK_LAUNCH();
     }
     float f2 = 1.0f, d2 = 0.0f;
@@ -326,12 +374,12 @@ int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const 
                             (void **)&part));
         k_sumwt_part<<<nbw, RED_THREADS, 0, st>>>(vals, counts, per, part);
         SDE_CHECK_LAUNCH();
-        k_sum_partials<<<1, 32, 0, st>>>(part, nbw, sums);
+        k_sum_partials<<<1, RED_THREADS, 0, st>>>(part, nbw, sums);
         SDE_CHECK_LAUNCH();
         if (rmode == 1 || rmode == 3) {
             k_sumlocwt_part<<<nbc, RED_THREADS, 0, st>>>(gwt, ncell, per, part);
             SDE_CHECK_LAUNCH();
-            k_sum_partials<<<1, 32, 0, st>>>(part, nbc, sums + 1);
+            k_sum_partials<<<1, RED_THREADS, 0, st>>>(part, nbc, sums + 1);
             SDE_CHECK_LAUNCH();
         }
         SDE_CUDA_TRY(cudaMemcpyAsync(hs, sums, sizeof hs, cudaMemcpyDeviceToHost, st));
