@@ -539,6 +539,9 @@ def run_gpu(args):
     if args.e2e_steps > 0:  # every replica, timed by the slowest
         e2e = run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis,
                       tdist if dist else None, dev, world)
+        # the same through ordinary (pageable) host memory, beside it
+        e2e["pageable"] = run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis,
+                                  tdist if dist else None, dev, world, pinned_host=False)
 
     line = {
         "metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": world,
@@ -951,14 +954,16 @@ def run_clark(args):
             "ms_each": [round(x * 1e3, 3) for x in times], "cpu_baseline": cpu}
 
 
-def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis, tdist=None, dev=None, world=1):
-    """Same step through grdh2d_/fftr2d_/pixcor2d_/grddeh2d_ with pinned host buffers; with a
+def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis, tdist=None, dev=None, world=1,
+            pinned_host=True):
+    """Same step through grdh2d_/fftr2d_/pixcor2d_/grddeh2d_ with host buffers -- page-locked
+    (pinned_host) or ordinary pageable memory, as a Fortran program's MEMR arrays are; with a
     process group, every replica runs it and the slowest one's time counts."""
     from sde_gb300 import _abi
     P = C.c_void_p
 
     def pinned(t):
-        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=pinned_host)
         h.copy_(t)
         return h
 
@@ -966,11 +971,11 @@ def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis, tdist=
     hvis, hwt = pinned(vis), pinned(wt)
     hwt2 = pinned(wt)
     nu, nv, n = geom.nu, geom.nv, geom.nx
-    hgrid = torch.zeros((nv, nu), dtype=torch.complex64, pin_memory=True)
-    himg = torch.zeros((n, n), dtype=torch.float32, pin_memory=True)
+    hgrid = torch.zeros((nv, nu), dtype=torch.complex64, pin_memory=pinned_host)
+    himg = torch.zeros((n, n), dtype=torch.float32, pin_memory=pinned_host)
     hmodel = pinned(model)
-    hmc = torch.zeros((n, n), dtype=torch.float32, pin_memory=True)
-    hmgrid = torch.zeros((nv, nu), dtype=torch.complex64, pin_memory=True)
+    hmc = torch.zeros((n, n), dtype=torch.float32, pin_memory=pinned_host)
+    hmgrid = torch.zeros((nv, nu), dtype=torch.complex64, pin_memory=pinned_host)
     hout = pinned(vis)
     from sde_gb300.imaging import fftpwr2
     # the caller-side tables, built by the library's GRDCF/GRDCCF entry points
@@ -1026,10 +1031,10 @@ def run_e2e(args, torch, L, geom, plan, ud, vd, wd, vis, wt, model, nvis, tdist=
     d2h = gb + img + gb + img + img + gb + 8 * nvis + (4 * nvis if negated else 0)
     return {"value": whole_job_mvis(nvis, world, dt), "unit": "Mvis/s", "ms_per_step": dt * 1e3,
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "path": "grdh2d_ -> fftr2d_(-1) -> pixcor2d_ x2 -> fftr2d_(+1) -> grddeh2d_, pinned "
+            "path": "grdh2d_ -> fftr2d_(-1) -> pixcor2d_ x2 -> fftr2d_(+1) -> grddeh2d_, %s "
                     "host arrays; every call uploads its inputs and downloads its outputs; "
                     "GRDH2D/GRDDEH2D reuse their tile plan when U, V, W, WT are bitwise "
-                    "unchanged (compared on the device)",
+                    "unchanged (compared on the device)" % ("pinned" if pinned_host else "pageable"),
             "flagged_wt": flagged, "negated_wt": negated,
             "plan_cache": _shim_stats(L)}
 

@@ -351,6 +351,16 @@ int sde_model_image(sde_ctx *ctx, int ncomp, const char *types, const float *flu
                     const float *dec, const float *bmaj, const float *bmin, const float *bpa, int nx,
                     int ny, float refx, float deltx, float refy, float delty, float *image);
 
+/* IMGDOUBL (source/img/imgdoubl.f:7, with PIXRPAD, source/pix/pixrpad.f:7) for a 2-D image,
+ * called by IMGTOVIS (img/imgtovis.f:50) before it transforms and degrids a model: in
+ * (device, ny x nx, reference pixel rpix_x, rpix_y, 1-based) is placed in out (device,
+ * py x px, zero elsewhere), px = FFTPWR2(2 nx) and py = FFTPWR2(2 ny) (1 for a one-pixel
+ * axis; any other px, py is refused), with left margin NINT(px/2 - RPIX) per axis, so the
+ * reference pixel moves to about the centre; rpix_out (host, 2 floats, may be NULL)
+ * receives the new reference pixel.  Asynchronous on the context's stream. */
+int sde_image_double(sde_ctx *ctx, const float *in, int nx, int ny, float rpix_x, float rpix_y,
+                     float *out, int px, int py, float *rpix_out);
+
 /* Clark CLEAN, the default algorithm of SDE's clean task: the CLARK branch of
  * task/clean.f:147-205 and IMGCCLEA (img/imgcclea.f) on device arrays.
  *   dirty, psf  N x N images from uvmap (N a power of two, 64..8192; CRPIX = (N+1)/2, so

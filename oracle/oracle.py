@@ -129,6 +129,9 @@ def lib():
                                      C.POINTER(C.c_float), C.POINTER(C.c_double)]
         L.orc_grdh2d_end.restype = C.c_int
         L.orc_grdh2d_end.argtypes = [c64p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]
+        L.orc_imgdoubl.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_float, f32p, C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_imgtovis.argtypes = [C.POINTER(UvmapParams), C.c_int, f32p, f32p, f32p, c64p, f32p, f32p]
         L.orc64_uvmap_image_mt.argtypes = [C.POINTER(Geom), C.c_int, f32p, f32p, f32p, c64p,
                                            f32p, C.c_int, f64p, C.c_int]
         L.orc64_fftr2d_inv.argtypes = [c128p, f64p, C.c_int, C.c_int, C.c_int, C.c_int]
@@ -416,6 +419,30 @@ def vismodel(p, u, v, w, vis, wt, image):
     vis = _c64(vis).copy()
     wt = _f32(wt).copy()
     lib().orc_vismodel(C.byref(p), len(wt), _f32(u), _f32(v), _f32(w), vis, wt, _f32(image))
+    return vis, wt
+
+
+def imgdoubl(img, rpix_x, rpix_y):
+    """IMGDOUBL/PIXRPAD: (padded image [py][px], new rpix_x, new rpix_y)."""
+    img = _f32(img)
+    ny, nx = img.shape
+    pn = [max(1, fftpwr2_host(2 * nx)) if nx > 1 else 1, max(1, fftpwr2_host(2 * ny)) if ny > 1 else 1]
+    out = np.zeros((pn[1], pn[0]), np.float32)
+    px, py, rx, ry = C.c_int(), C.c_int(), C.c_float(), C.c_float()
+    lib().orc_imgdoubl(img, nx, ny, rpix_x, rpix_y, out, C.byref(px), C.byref(py), C.byref(rx), C.byref(ry))
+    assert (px.value, py.value) == (pn[0], pn[1])
+    return out, rx.value, ry.value
+
+
+def fftpwr2_host(i):
+    return lib().orc_fftpwr2(int(i))
+
+
+def imgtovis(p, u, v, w, vis, wt, image):
+    """IMGTOVIS: the model image padded (IMGDOUBL) and degridded from the padded grid."""
+    vis = _c64(vis).copy()
+    wt = _f32(wt).copy()
+    lib().orc_imgtovis(C.byref(p), len(wt), _f32(u), _f32(v), _f32(w), vis, wt, _f32(image))
     return vis, wt
 
 

@@ -2427,3 +2427,57 @@ void orc_point_vis_mt(int64_t n, const float *u, const float *v, int nsrc, const
     }
     for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
 }
+
+/* img/imgdoubl.f:56-86 with pix/pixrpad.f:38-62 (2-D): the image placed in a zeroed P x P'
+ * array, P = FFTPWR2(2N) on each axis longer than one pixel, with left margin
+ * LSHIFT = NINT(P/2 - RPIX) (P/2 an INTEGER division, RPIX REAL), so that the reference
+ * pixel moves to RPIX + LSHIFT.  out must hold px*py floats; returns the new RPIX. */
+void orc_imgdoubl(const float *in, int nx, int ny, float rpix_x, float rpix_y, float *out, int *px,
+                  int *py, float *rpix_x_out, float *rpix_y_out) {
+    int pn[2], ls[2];
+    const int n[2] = {nx, ny};
+    const float rp[2] = {rpix_x, rpix_y};
+    for (int a = 0; a < 2; a++) {
+        if (n[a] > 1) {
+            pn[a] = orc_fftpwr2(2 * n[a]);
+            if (pn[a] < 1) pn[a] = 1;
+            ls[a] = orc_nint_f((float)(pn[a] / 2) - rp[a]);
+        } else {
+            pn[a] = 1;
+            ls[a] = 0;
+        }
+    }
+    for (size_t k = 0; k < (size_t)pn[0] * pn[1]; k++) out[k] = 0.0f;  /* ARRSETCO */
+    for (int i2 = 1; i2 <= ny; i2++) {
+        const int j2 = i2 + ls[1];
+        for (int i1 = 1; i1 <= nx; i1++) {
+            const int j1 = i1 + ls[0];
+            out[(size_t)(j2 - 1) * pn[0] + (j1 - 1)] = in[(size_t)(i2 - 1) * nx + (i1 - 1)];
+        }
+    }
+    *px = pn[0];
+    *py = pn[1];
+    *rpix_x_out = rpix_x + (float)ls[0];
+    *rpix_y_out = rpix_y + (float)ls[1];
+}
+
+/* img/imgtovis.f:50-73: IMGDOUBL (the model padded to P = FFTPWR2(2N), its reference pixel
+ * moved to P/2), the grid of the padded image (FFTCONJA: NU = P/2+1, NV = P, uv cells half
+ * the size of the image's own grid), then IMGGRIDC CORRECT, IMGFFT and VISDEGRI on it.  The
+ * image's reference pixel is (N+1)/2, uvmap's; the padded one is then P/2 = (P+1)/2, the
+ * centre the padded geometry below assumes. */
+int orc_imgtovis(const orc_uvmap_params *p, int nvis, const float *u, const float *v,
+                 const float *w, float *vis, float *wt, const float *image) {
+    const int n = p->imsize;
+    const float rp = (float)((n + 1) / 2);
+    int px, py;
+    float rpx, rpy;
+    const int pn = orc_fftpwr2(2 * n);
+    float *pad = (float *)malloc(sizeof(float) * (size_t)pn * pn);
+    orc_imgdoubl(image, n, n, rp, rp, pad, &px, &py, &rpx, &rpy);
+    orc_uvmap_params q = *p;
+    q.imsize = px;
+    int rc = orc_vismodel(&q, nvis, u, v, w, vis, wt, pad);
+    free(pad);
+    return rc;
+}

@@ -186,6 +186,11 @@ void orc64_fftr2d_inv(const double *xarray, double *image, int nx, int ny, int f
 /* point-source visibilities in double -> complex64 on nthreads threads (benchmark data) */
 void orc_point_vis_mt(int64_t n, const float *u, const float *v, int nsrc, const double *flux,
                       const double *l, const double *m, float *out, int nthreads);
+/* img/imgdoubl.f + pix/pixrpad.f (2-D) and img/imgtovis.f (the padded degrid) */
+void orc_imgdoubl(const float *in, int nx, int ny, float rpix_x, float rpix_y, float *out, int *px,
+                  int *py, float *rpix_x_out, float *rpix_y_out);
+int  orc_imgtovis(const orc_uvmap_params *p, int nvis, const float *u, const float *v,
+                  const float *w, float *vis, float *wt, const float *image);
 void orc64_uvmap_image_mt(const orc_geom *g, int nvis, const float *u, const float *v,
                           const float *w, const float *vis, const float *wt, int psf,
                           double *image, int nthreads);

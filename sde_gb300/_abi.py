@@ -152,6 +152,7 @@ SIGNATURES = [
                                   C.POINTER(UruwtStats)]),
     ("sde_grid_box", I, [P, I64, P, P, P, P, P, F, F, F, F, I, I, I, I, I, P, P, I, C.POINTER(F)]),
     ("sde_model_image", I, [P, I, C.c_char_p, P, P, P, P, P, P, I, I, F, F, F, F, P]),
+    ("sde_image_double", I, [P, P, I, I, F, F, P, I, I, C.POINTER(F)]),
     ("sde_dft_image", I, [P, I64, P, P, P, P, I, I, C.c_double, C.c_double, C.c_double,
                           C.c_double, P, P]),
     ("sde_dft_vis", I, [P, P, I, I, C.c_double, C.c_double, C.c_double, C.c_double, I64, P, P,

@@ -209,3 +209,60 @@ extern "C" int sde_model_image(sde_ctx *ctx, int ncomp, const char *types, const
     SDE_CUDA_TRY(cudaStreamSynchronize(st));
     return SDE_OK;
 }
+
+// ---------------------------------------------------------------------------------------
+// IMGDOUBL (img/imgdoubl.f:56-86) with PIXRPAD (pix/pixrpad.f:38-62) for 2-D images: the
+// image placed in a zeroed px x py array, px = FFTPWR2(2 nx) (1 for a one-pixel axis), with
+// left margin LSHIFT = NINT(px/2 - RPIX) per axis, so the reference pixel moves to
+// RPIX + LSHIFT.  One thread per output pixel reads its source pixel or writes zero: every
+// output element written once, coalesced.
+namespace {
+__global__ void k_image_pad(const float *__restrict__ in, int nx, int ny, int lsx, int lsy,
+                            float *__restrict__ out, int px, int py) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (int64_t)px * py) return;
+    const int jy = (int)(k / px), jx = (int)(k - (int64_t)jy * px);  // 0-based output pixel
+    const int ix = jx - lsx, iy = jy - lsy;                          // 0-based source pixel
+    out[k] = (ix >= 0 && ix < nx && iy >= 0 && iy < ny) ? in[(int64_t)iy * nx + ix] : 0.0f;
+}
+}  // namespace
+
+extern "C" int sde_image_double(sde_ctx *ctx, const float *in, int nx, int ny, float rpix_x,
+                                float rpix_y, float *out, int px, int py, float *rpix_out) {
+    if (!ctx || !in || !out || nx < 1 || ny < 1) {
+        sde_set_error("sde_image_double: bad arguments");
+        return SDE_EINVAL;
+    }
+    const int n[2] = {nx, ny};
+    const float rp[2] = {rpix_x, rpix_y};
+    int pn[2], ls[2];
+    for (int a = 0; a < 2; a++) {
+        if (n[a] > 1) {
+            if (n[a] > (1 << 29)) {
+                sde_set_error("sde_image_double: axis of %d pixels too long", n[a]);
+                return SDE_EINVAL;
+            }
+            pn[a] = fftpwr2(2 * n[a]);
+            // NINT(REAL(P/2) - RPIX): REAL arithmetic, half away from zero
+            const float d = (float)(pn[a] / 2) - rp[a];
+            ls[a] = (int)(d >= 0.0f ? floorf(d + 0.5f) : -floorf(-d + 0.5f));
+        } else {
+            pn[a] = 1;
+            ls[a] = 0;
+        }
+    }
+    if (px != pn[0] || py != pn[1]) {
+        sde_set_error("sde_image_double: output must be %d x %d (FFTPWR2 of twice each axis)", pn[0], pn[1]);
+        return SDE_EINVAL;
+    }
+    SDE_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int64_t np = (int64_t)px * py;
+    KTimer kt(ctx, "image_pad");
+    k_image_pad<<<(unsigned)ceil_div(np, (int64_t)256), 256, 0, ctx->stream>>>(in, nx, ny, ls[0], ls[1], out, px, py);
+    SDE_CHECK_LAUNCH();
+    if (rpix_out) {
+        rpix_out[0] = rpix_x + (float)ls[0];
+        rpix_out[1] = rpix_y + (float)ls[1];
+    }
+    return SDE_OK;
+}

@@ -102,6 +102,7 @@ class Geom:
         ira = vra + float(f32(shift[0]) / f32(3600.0))
         idec = vdec + float(f32(shift[1]) / f32(3600.0))
         self.shift = crdshift(vra, vdec, ira, idec)
+        self.cellsize, self.vra, self.vdec, self.shift_arcsec, self.fov = cellsize, vra, vdec, tuple(shift), fov
         self.pitch = lib().sde_grid_pitch(self.nu)
 
     def spec(self):
@@ -344,6 +345,42 @@ def vismodel(ctx, geom, plan, image, vis_out, wt_out):
     grid = ctx.grid_buffer(geom)
     ctx.grid_from_image(geom, image, grid)
     return plan.degrid(grid, vis_out, wt_out)
+
+
+def image_double(ctx, image, rpix_x, rpix_y):
+    """IMGDOUBL (sde_image_double): the image padded to FFTPWR2 of twice each axis, its
+    reference pixel moved to about the centre.  Returns (padded image, new rpix_x, rpix_y)."""
+    ny, nx = int(image.shape[0]), int(image.shape[1])
+    px = fftpwr2(2 * nx) if nx > 1 else 1
+    py = fftpwr2(2 * ny) if ny > 1 else 1
+    out = ctx.empty((py, px), ctx.torch.float32)
+    rp = (C.c_float * 2)()
+    check(lib().sde_image_double(ctx.h, _ptr(image), nx, ny, float(rpix_x), float(rpix_y), _ptr(out),
+                                 px, py, rp), "sde_image_double")
+    return out, rp[0], rp[1]
+
+
+def padded_geom(geom):
+    """The grid geometry IMGTOVIS degrids from (img/imgtovis.f:52-56): FFTCONJA of the image
+    padded by IMGDOUBL -- FFTPWR2(2N) pixels at the same cell size, so the uv cells are half
+    as large; with uvmap's reference pixel (N+1)/2 the padded one is P/2, this geometry's
+    centre."""
+    return Geom(fftpwr2(2 * geom.nx), geom.cellsize, vra=geom.vra, vdec=geom.vdec,
+                shift=geom.shift_arcsec, fov=geom.fov)
+
+
+def imgtovis(ctx, geom, plan_padded, image, vis_out, wt_out):
+    """img/imgtovis.f:50-73 for a 2-D model image of geom (reference pixel (N+1)/2): IMGDOUBL,
+    then IMGGRIDC CORRECT, IMGFFT and VISDEGRI on the padded image's grid.  plan_padded is a
+    Plan built on padded_geom(geom) (once per job, like the degrid plan of a major cycle)."""
+    pg = plan_padded.geom
+    pad, rx, ry = image_double(ctx, image, geom.cenx, geom.ceny)
+    if (rx, ry) != (pg.cenx, pg.ceny):
+        raise ValueError("imgtovis: the padded reference pixel (%g, %g) is not the padded grid's "
+                         "centre (%g, %g)" % (rx, ry, pg.cenx, pg.ceny))
+    grid = ctx.grid_buffer(pg)
+    ctx.grid_from_image(pg, pad, grid)
+    return plan_padded.degrid(grid, vis_out, wt_out)
 
 
 def components_image(ctx, geom, cln_window):

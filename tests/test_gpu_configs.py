@@ -219,3 +219,40 @@ def test_weights_az_norm(gpu_ctx, orc, obs_small, obs_shift, case):
     assert np.array_equal(got[~touched], o["wt"][~touched])
     print("AZ-NORM %s: %.1f%% of NEWWT bit-identical, max relative difference %.2e (bound %.2e)"
           % (case, 100 * same, rel, tol))
+
+
+def test_imgtovis_padded_degrid_matches_oracle(gpu_ctx, orc, obs_small, obs_shift):
+    """IMGTOVIS (img/imgtovis.f:50-73), the degrid of mosclean's major cycle
+    (task/mosclean.f:361): IMGDOUBL pads the model to FFTPWR2(2N) with the reference pixel
+    moved to the centre (bit-exact against the oracle's PIXRPAD), then the padded image's
+    grid -- uv cells half as large -- is corrected, transformed and degridded; visibilities
+    within 1e-5 of the largest, WT flags identical.  Both observations: with and without a
+    phase-centre shift."""
+    from sde_gb300.imaging import Geom, Plan, image_double, imgtovis, padded_geom
+    ctx = gpu_ctx
+    for o in (obs_small, obs_shift):
+        g = Geom(o["imsize"], o["cell"], vra=o["vra"], vdec=o["vdec"], shift=o["shift"])
+        rng = np.random.default_rng(17)
+        model = np.zeros((g.ny, g.nx), np.float32)
+        lo, hi = g.window()
+        for _ in range(15):
+            iy, ix = rng.integers(lo, hi, 2)
+            model[iy, ix] += rng.uniform(0.05, 1.0)
+        # the padding alone, bit for bit
+        pad_ref, rx, ry = orc.imgdoubl(model, g.cenx, g.ceny)
+        pad, gx, gy = image_double(ctx, _t(ctx, model), g.cenx, g.ceny)
+        assert np.array_equal(pad.cpu().numpy(), pad_ref) and (gx, gy) == (rx, ry)
+        pg = padded_geom(g)
+        assert (pg.nx, pg.nu, pg.nv) == (2 * g.nx, g.nx + 1, 2 * g.nx) and (pg.cenx, pg.ceny) == (rx, ry)
+        p = orc.params(o["imsize"], o["cell"], fov=1.0, vdec=o["vdec"], shift=o["shift"])
+        ref_vis, ref_wt = orc.imgtovis(p, o["u"], o["v"], o["w"], o["vis"], o["wt"], model)
+        t = {k: _t(ctx, o[k]) for k in ("u", "v", "w", "wt", "vis")}
+        plan = Plan(ctx, pg, t["u"], t["v"], t["w"], t["vis"], t["wt"])
+        vis_out, wt_out = t["vis"].clone(), t["wt"].clone()
+        imgtovis(ctx, g, plan, _t(ctx, model), vis_out, wt_out)
+        got_w = wt_out.cpu().numpy()
+        assert np.array_equal(got_w, ref_wt)
+        ok = ref_wt > 0
+        scale = np.abs(ref_vis[ok]).max()
+        assert np.abs(vis_out.cpu().numpy()[ok] - ref_vis[ok]).max() / scale < 1e-5
+        plan.close()
