@@ -359,7 +359,7 @@ def run_gpu(args):
     import torch
     from sde_gb300 import _abi
     from sde_gb300._abi import lib
-    from sde_gb300.imaging import Context, Geom, MajorCycle, Plan, components_image, hogbom
+    from sde_gb300.imaging import Context, Geom, MajorCycle, Plan, components_image
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -431,13 +431,19 @@ def run_gpu(args):
     torch.cuda.synchronize()
     L = lib()
 
+    # CRDNHALF's window of the dirty image, cut out before the timing: the first strided copy
+    # of a process makes torch load that kernel (hundreds of ms), which is not CLEAN's time
+    wlo, whi = geom.window()
+    drt = mc.dirty[wlo:whi, wlo:whi].contiguous()
+    torch.cuda.synchronize()
+
     def timed_hogbom():
         """wall time of one Hogbom call through the library, and k_hogbom's device time"""
         L.sde_ctx_reset_stats(ctx.h)
         L.sde_ctx_profile(ctx.h, 1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = hogbom(ctx, geom, mc.dirty, psf, args.clean_iters, 0.1)
+        r = ctx.hogbom(drt, psf, args.clean_iters, 0.1)
         torch.cuda.synchronize()
         wall = (time.perf_counter() - t0) * 1e3
         tot, cnt = C.c_double(), C.c_int64()
