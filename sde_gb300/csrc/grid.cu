@@ -551,11 +551,12 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     fill_tap_tables(cft_g, vt, ut);
+    // reciprocal tap-row sums: GRDDEH2D's SUMWT is (sum of u taps)(sum of v taps)
     for (int d = threadIdx.x; d < 129; d += DG_THREADS) {
         float sacc = 0.f;
 #pragma unroll
         for (int a = 0; a < NTAP; a++) sacc += cft_g[d * 8 + a];
-        rsum[d] = sacc;
+        rsum[d] = 1.0f / sacc;
     }
     __syncthreads();
     const int q = tid & 3;
@@ -694,7 +695,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                 tr += __shfl_xor_sync(FULL, hi1 ? k0r : k1r, 1);
                 ti += __shfl_xor_sync(FULL, hi1 ? k0i : k1i, 1);
                 if (!mine || (gq & GDD_EXCEPTION)) continue;
-                const float inv = 1.0f / (rsum[gq & 0xFFu] * rsum[(gq >> 8) & 0xFFu]);
+                const float inv = rsum[gq & 0xFFu] * rsum[(gq >> 8) & 0xFFu];
                 float mr = tr * inv, mi = ti * inv;
                 if (MODE == 0) {
                     *rec_res(rec, pq) = make_float2(ob.x - mr, ob.y - mi);

@@ -74,11 +74,11 @@ __global__ void k_wkey(WParams p, const float *__restrict__ wt, const float *__r
         keys[i] = key;
         vals[i] = __float_as_uint(wi);
     }
-    // warp-aggregated counters: [0] on-grid, [1] dropped
-    unsigned mv = __ballot_sync(0xffffffffu, valid), md = __ballot_sync(0xffffffffu, drop);
-    if ((threadIdx.x & 31) == 0) {
-        if (mv) atomicAdd(&counts[0], (unsigned long long)__popc(mv));
-        if (md) atomicAdd(&counts[1], (unsigned long long)__popc(md));
+    // block-aggregated counters: [0] on-grid, [1] dropped (one atomic per block and counter)
+    const int cv = __syncthreads_count(valid), cd = __syncthreads_count(drop);
+    if (threadIdx.x == 0) {
+        if (cv) atomicAdd(&counts[0], (unsigned long long)cv);
+        if (cd) atomicAdd(&counts[1], (unsigned long long)cd);
     }
 }
 
