@@ -59,17 +59,27 @@ constexpr int CHUNK_LIMIT = 4096;       // largest accepted chunk size
 constexpr uint32_t KEY_INVALID = 0xFFFFFFFFu;
 
 // Per-visibility geometry words (sorted order):
-//   gdg (uint16): du_g+64 | (dv_g+64) << 8 -- gridding sub-cell offsets (FP64 cell);
-//   gdd (uint32): du_d+64 | (dv_d+64) << 8 | cell << 16 (12-bit tile-local cell of the
-//                 chunk) | GDD_EXCEPTION -- degridding offsets (FP32 cell); visibilities with
-//                 GDD_EXCEPTION set are handled by the degridder's exception path.
+//   gdg (uint16): du_g+64 | (dv_g+64) << 8 -- gridding sub-cell offsets (FP64 cell); the
+//                 plan record carries them as tap-table byte offsets instead (taps_word);
+//   gdd (uint32): taps_word(du_d, dv_d, column-in-pair) | GDD_EXCEPTION -- degridding
+//                 offsets (FP32 cell); visibilities with GDD_EXCEPTION set are handled by the
+//                 degridder's exception path.
 __host__ __device__ inline uint16_t pack_gdg(int dug, int dvg) {
     return (uint16_t)((uint32_t)(dug + 64) | ((uint32_t)(dvg + 64) << 8));
 }
-__host__ __device__ inline uint32_t pack_gdd(int dud, int dvd, uint32_t cell) {
-    return (uint32_t)(dud + 64) | ((uint32_t)(dvd + 64) << 8) | (cell << 16);
-}
 constexpr uint32_t GDD_EXCEPTION = 1u << 31;
+
+// Sub-cell offsets as byte offsets of the visibility's rows in the gridder's and degridder's
+// tap tables -- u table row (du+64)*2 + column of the cell within its chunk's cell pair, 128
+// bytes a row (low 16 bits); v table row dv+64, 128 bytes a row (bits 16..30) -- so that the
+// lanes only add them to their table copy's address.  The plan record's second word (du_g,
+// dv_g) and gdd (du_d, dv_d) hold them.
+constexpr uint32_t TAPROW_BYTES = 128;
+__host__ __device__ inline uint32_t taps_word(int du, int dv, uint32_t off) {
+    return (((uint32_t)(du + 64) * 2u + off) * TAPROW_BYTES) | (((uint32_t)(dv + 64) * TAPROW_BYTES) << 16);
+}
+__host__ __device__ inline int taps_du(uint32_t g) { return (int)((g & 0xFFFFu) / (2 * TAPROW_BYTES)); }
+__host__ __device__ inline int taps_dv(uint32_t g) { return (int)(((g >> 16) & 0x7FFFu) / TAPROW_BYTES); }
 
 // Exception entries for the degridder: visibilities whose FP32 degridding cell differs
 // from their FP64 gridding cell, whose conjugation flags differ, that only degrid, or that

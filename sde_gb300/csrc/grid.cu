@@ -50,8 +50,10 @@ constexpr int GRID_THREADS = TEAMS * TEAM_THREADS;
 constexpr int GLANES = 4;                          // lanes per chunk
 constexpr int GGROUPS = TEAM_THREADS / GLANES;     // chunks in flight per team
 constexpr int VT_ROW = 32;                         // floats per v-table row (4 copies x 8)
+static_assert(VT_ROW * 4 == TAPROW_BYTES, "the plan record's v-table offsets");
 constexpr int VT_FLOATS = 129 * VT_ROW;
 constexpr int UT_ROW = 32;                         // floats per u-table row (4 copies x 4 pairs)
+static_assert(UT_ROW * 4 == TAPROW_BYTES, "the plan record's u-table offsets");
 constexpr int UT_FLOATS = 2 * 129 * UT_ROW;
 constexpr int GTAB_FLOATS = VT_FLOATS + UT_FLOATS;
 constexpr int GTILE_FLOATS = 2 * STILE * STILE;    // a team's tile: re and im planes
@@ -139,8 +141,8 @@ __device__ __forceinline__ void grid_item(const WorkItem &it, const uint2 *__res
                 const float fr = __shfl_sync(FULL, frq, gbase + u);
                 const float fi = PSF ? 0.f : __shfl_sync(FULL, fiq, gbase + u);
                 const float2 gu = *reinterpret_cast<const float2 *>(
-                    ucopy + ((g & 0xFFu) * 2 + ((g >> 16) & 1u)) * UT_ROW);
-                const float4 *vr = reinterpret_cast<const float4 *>(vcopy + ((g >> 8) & 0xFFu) * VT_ROW);
+                    reinterpret_cast<const char *>(ucopy) + (g & 0xFFFFu));
+                const float4 *vr = reinterpret_cast<const float4 *>(reinterpret_cast<const char *>(vcopy) + (g >> 16));
                 const float4 v0 = vr[0], v1 = vr[1];
                 const float2 P[NPAIR] = {make_float2(v0.x, v0.y), make_float2(v0.z, v0.w),
                                          make_float2(v1.x, v1.y), make_float2(v1.z, v1.w)};
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(RED_T) k_plan_sums(const float4 *__restrict__ 
     for (int64_t p = (int64_t)blockIdx.x * RED_T + threadIdx.x; p < n; p += (int64_t)gridDim.x * RED_T) {
         const float2 wgp = reinterpret_cast<const float2 *>(rec + p)[0];
         const uint32_t g = __float_as_uint(wgp.y);
-        const float *gu = cft + (g & 0xFFu) * 8, *gv = cft + ((g >> 8) & 0xFFu) * 8;
+        const float *gu = cft + taps_du(g) * 8, *gv = cft + taps_dv(g) * 8;
         float su = 0.f, sv = 0.f;
 #pragma unroll
         for (int a = 0; a < NTAP; a++) {
@@ -566,7 +568,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     const float *vcopy = vt + (grp & 3) * 8;
     const float *ucopy = ut + (grp & 3) * 8 + 2 * q;
     constexpr uint32_t FULL = 0xffffffffu;
-    constexpr uint32_t GDD_PAD = 0x4040u;  // offsets 0, cell 0: a harmless table row
+    constexpr uint32_t GDD_PAD = 0u;  // table row 0: harmless reads for the padding lanes
     for (uint32_t iter = 0;; iter++) {
         if (tid == 0) s_next[team] = (long long)atomicAdd(counter, 1ull);
         team_sync(team);  // also: the team's reads of its previous tile are done
@@ -666,8 +668,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                 for (int u = 0; u < 4; u++) {
                     const uint32_t g = __shfl_sync(FULL, gq, gbase + u);
                     const float2 gu = *reinterpret_cast<const float2 *>(
-                        ucopy + ((g & 0xFFu) * 2 + ((g >> 16) & 1u)) * UT_ROW);
-                    const float4 *vr = reinterpret_cast<const float4 *>(vcopy + ((g >> 8) & 0xFFu) * VT_ROW);
+                        reinterpret_cast<const char *>(ucopy) + (g & 0xFFFFu));
+                    const float4 *vr = reinterpret_cast<const float4 *>(
+                        reinterpret_cast<const char *>(vcopy) + ((g >> 16) & 0x7FFFu));
                     const float4 v0 = vr[0], v1 = vr[1];
                     const float gv[NTAP] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z};
                     float c0r = 0.f, c0i = 0.f, c1r = 0.f, c1i = 0.f;
@@ -695,7 +698,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                 tr += __shfl_xor_sync(FULL, hi1 ? k0r : k1r, 1);
                 ti += __shfl_xor_sync(FULL, hi1 ? k0i : k1i, 1);
                 if (!mine || (gq & GDD_EXCEPTION)) continue;
-                const float inv = rsum[gq & 0xFFu] * rsum[(gq >> 8) & 0xFFu];
+                const float inv = rsum[taps_du(gq)] * rsum[taps_dv(gq)];
                 float mr = tr * inv, mi = ti * inv;
                 if (MODE == 0) {
                     *rec_res(rec, pq) = make_float2(ob.x - mr, ob.y - mi);

@@ -113,9 +113,10 @@ __device__ __forceinline__ DGeo degrid_geom(const GParams &p, float u, float v, 
     return degrid_cell(p, ul, vl, (float)c, (float)s);
 }
 
-// Bit 28 of a caller-order degridding word carries the gridding-frame conjugation (the
-// plan's own words leave it clear).
-constexpr uint32_t GDD_GCONJ_U = 1u << 28;
+// Bit 0 of a caller-order degridding word (a table byte offset, a multiple of 128, is even
+// there) carries the gridding-frame conjugation (the plan's own words leave it clear).
+constexpr uint32_t GDD_GCONJ_U = 1u;
+static_assert(TAPROW_BYTES % 2 == 0, "bit 0 of a degridding word is free");
 
 // The fast path (identity SHIFT, zero offsets: every uvmap/mapper call without a phase-centre
 // shift) keeps the reference's results with fewer FP64 operations, which GB300 runs at a
@@ -160,8 +161,7 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
     uint32_t nvalid = 0, nexc = 0;
     const float wi = i < n ? wt[i] : 0.0f;
     if (i < n) {
-        uint32_t key = KEY_INVALID, pdd = 0;
-        uint16_t pdg = 0;
+        uint32_t key = KEY_INVALID, pdd = 0, tw = 0;
         float2 f = make_float2(0.f, 0.f), r = make_float2(1.f, 0.f);
         uint8_t gc = 0;
         if (wi > 0.0f) {
@@ -224,9 +224,10 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
                                         2 * p.vorigin - (dg.nvd - p.supp) <= p.nv;
                 bool exc = !dg.valid || dg.nud != nuc || dg.nvd != nvc ||
                            (dg.nud <= p.supp && !refl_tiled) || dg.conj != (gc != 0);
-                const uint32_t cell = ((uint32_t)lv << 6) | (uint32_t)lu;
-                pdg = pack_gdg(dug, dvg);
-                pdd = exc ? (pack_gdd(0, 0, cell) | GDD_EXCEPTION) : pack_gdd(dg.dui, dg.dvi, cell);
+                // column of the cell within its chunk's cell pair (chunks start on even lu)
+                const uint32_t off = (uint32_t)lu & 1u;
+                tw = taps_word(dug, dvg, off);
+                pdd = exc ? (taps_word(0, 0, off) | GDD_EXCEPTION) : taps_word(dg.dui, dg.dvi, off);
                 nvalid = 1;
                 nexc = exc;
                 f = make_float2(fr, fi);
@@ -236,9 +237,7 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
         }
         keys[i] = key;
         vals[i] = (uint32_t)i;
-        // bit 16: column of the visibility's cell within its chunk's cell pair
-        const uint32_t off = (pdd >> 16) & 1u;
-        rec_u[i] = make_float4(wi, __uint_as_float((uint32_t)pdg | (off << 16)), f.x, f.y);
+        rec_u[i] = make_float4(wi, __uint_as_float(tw), f.x, f.y);
         gdd_u[i] = pdd | (gc ? GDD_GCONJ_U : 0u);
         if (rot) rot[i] = r;
     }
