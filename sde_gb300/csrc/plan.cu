@@ -12,150 +12,36 @@
 #include <string.h>
 
 #include "common.cuh"
+#include "geom.cuh"
 
 namespace {
 
-struct GParams {
-    float uscale, uoffset, vscale, voffset;
-    int uorigin, vorigin, nu, nv, supp, osamp;
-    double s[9];
-    int doshift, ntu;
-    int identity;  // SHIFT is exactly the identity matrix
-    int diagonal;  // SHIFT's off-diagonal entries are all zero
-    int fast;      // identity SHIFT and UOFFSET = VOFFSET = 0 (see k_plan_geom)
-    double twopi;
-};
-
-// NINT of a double, half away from zero (Fortran NINT): x + 0.5 is exact for |x| < 2^52, so
-// floor(x + 0.5) rounds halves up, and the negative side mirrors it.  Callers keep |x| far
-// below 2^31.
-__device__ __forceinline__ int nint_dd(double x) {
-    return x >= 0.0 ? __double2int_rd(__dadd_rn(x, 0.5)) : -__double2int_rd(__dadd_rn(-x, 0.5));
-}
+using namespace sde_geom;
 
 constexpr int LENBIN_BITS = 3;  // coarse length bins above the colour class in the chunk order
-
-struct DGeo {
-    int nud, nvd, dui, dvi;
-    bool valid, conj;
-    float rc, rs;
-};
-
-// GRDDEH2D's per-visibility geometry (grd/grddeh2d.f:92-118): always rotated, FP32 cell.
-// COS and SIN of GRDH2D/GRDDEH2D's phase in DOUBLE.  Below 2^-27 in magnitude the correctly
-// rounded values are exactly 1 and the phase itself (|sin x - x| <= |x|^3/6 and x^2/2 are
-// below half an ulp there), which is what a phase-centre rotation that differs from the
-// identity only by rounding (CRDSHIFT's sin^2 + cos^2 on the diagonal) produces for every
-// visibility: no library call is made for it.
-__device__ __forceinline__ void phase_cos_sin(double ph, double &c, double &s) {
-    if (fabs(ph) < 0x1p-27) {
-        c = 1.0;
-        s = ph;
-    } else {
-        sincos(ph, &s, &c);
-    }
-}
-
-// GRDDEH2D's per-visibility geometry (grd/grddeh2d.f:92-118) from the rotated coordinates:
-// FP32 cell, the REAL rotation (rc, rs).
-__device__ __forceinline__ DGeo degrid_cell(const GParams &p, double ul, double vl, float rc, float rs) {
-    DGeo g;
-    g.rc = rc;
-    g.rs = rs;
-    float ucell = __double2float_rn(__dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset));
-    float vcell = __double2float_rn(__dadd_rn(__dmul_rn((double)p.vscale, vl), (double)p.voffset));
-    if (ucell > 0.0f) {
-        ucell = __fadd_rn(ucell, (float)p.uorigin);
-        vcell = __fadd_rn(vcell, (float)p.vorigin);
-    } else {
-        ucell = __fadd_rn(-ucell, (float)p.uorigin);
-        vcell = __fadd_rn(-vcell, (float)p.vorigin);
-    }
-    g.nud = nint_f(ucell);
-    g.nvd = nint_f(vcell);
-    g.valid = !(g.nud + p.supp > p.nu) && !(g.nvd + p.supp > p.nv) && !(g.nvd - p.supp < 1);
-    g.dui = nint_f(__fmul_rn((float)p.osamp, __fsub_rn((float)g.nud, ucell)));
-    g.dvi = nint_f(__fmul_rn((float)p.osamp, __fsub_rn((float)g.nvd, vcell)));
-    g.conj = __dmul_rn((double)p.uscale, ul) > 0.0;
-    return g;
-}
-
-// The rotation ULOCAL, VLOCAL, WLOCAL = SHIFT applied to (U, V, W) in DOUBLE (GRDDEH2D
-// always applies it; GRDH2D when DOSHIFT).  With SHIFT exactly the identity the products
-// and sums are exact for finite coordinates (1*x = x, 0*y = +-0, x + +-0 = x up to the sign
-// of a zero, which no later step can see), so they are skipped.
-__device__ __forceinline__ void rotate_uvw(const GParams &p, double ug, double vg, double wg,
-                                           double &ul, double &vl, double &wl) {
-    if (p.identity) {
-        ul = ug;
-        vl = vg;
-        wl = wg;
-    } else if (p.diagonal) {
-        // zero off-diagonal terms add +-0: the sums are the diagonal products (up to the sign
-        // of a zero result, which no later step can see) -- CRDSHIFT without a shift, whose
-        // diagonal sin^2 + cos^2 can miss 1 by an ulp
-        ul = __dmul_rn(p.s[0], ug);
-        vl = __dmul_rn(p.s[4], vg);
-        wl = __dmul_rn(p.s[8], wg);
-    } else {
-        ul = __dadd_rn(__dadd_rn(__dmul_rn(p.s[0], ug), __dmul_rn(p.s[1], vg)), __dmul_rn(p.s[2], wg));
-        vl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[3], ug), __dmul_rn(p.s[4], vg)), __dmul_rn(p.s[5], wg));
-        wl = __dadd_rn(__dadd_rn(__dmul_rn(p.s[6], ug), __dmul_rn(p.s[7], vg)), __dmul_rn(p.s[8], wg));
-    }
-}
-
-// GRDDEH2D's per-visibility geometry (grd/grddeh2d.f:92-118): always rotated, FP32 cell.
-__device__ __forceinline__ DGeo degrid_geom(const GParams &p, float u, float v, float w) {
-    const double ug = (double)u, vg = (double)v, wg = (double)w;
-    double ul, vl, wl, c, s;
-    rotate_uvw(p, ug, vg, wg, ul, vl, wl);
-    phase_cos_sin(__dmul_rn(p.twopi, __dsub_rn(wl, wg)), c, s);
-    return degrid_cell(p, ul, vl, (float)c, (float)s);
-}
 
 // Bit 0 of a caller-order degridding word (a table byte offset, a multiple of 128, is even
 // there) carries the gridding-frame conjugation (the plan's own words leave it clear).
 constexpr uint32_t GDD_GCONJ_U = 1u;
 static_assert(TAPROW_BYTES % 2 == 0, "bit 0 of a degridding word is free");
 
-// The fast path (identity SHIFT, zero offsets: every uvmap/mapper call without a phase-centre
-// shift) keeps the reference's results with fewer FP64 operations, which GB300 runs at a
-// small fraction of its FP32 rate:
-//   * GRDH2D's UCELL = USCALE*ULOCAL + UOFFSET with ULOCAL = DBLE(U): the product of two
-//     REALs is exact in DOUBLE and adding 0 changes nothing, so UCELL is that product; the
-//     origin, NINT and the oversampled offsets follow in DOUBLE as before;
-//   * GRDDEH2D's REAL cell SNGL(USCALE*ULOCAL + UOFFSET) is then the once-rounded REAL
-//     product, __fmul_rn(USCALE, U), and its phase is 0 (COS 1, SIN 0);
-//   * NINT by nint_dd (one add and one conversion) in place of the library's round().
-// Points so far off the grid that |UCELL| >= 2^30 are treated as outside it.
-__device__ __forceinline__ DGeo degrid_geom_fast(const GParams &p, float u, float v) {
-    DGeo g;
-    float ucell = __fmul_rn(p.uscale, u), vcell = __fmul_rn(p.vscale, v);
-    g.conj = __dmul_rn((double)p.uscale, (double)u) > 0.0;
-    g.rc = 1.0f;
-    g.rs = 0.0f;
-    if (ucell > 0.0f) {
-        ucell = __fadd_rn(ucell, (float)p.uorigin);
-        vcell = __fadd_rn(vcell, (float)p.vorigin);
-    } else {
-        ucell = __fadd_rn(-ucell, (float)p.uorigin);
-        vcell = __fadd_rn(-vcell, (float)p.vorigin);
-    }
-    g.nud = nint_f(ucell);
-    g.nvd = nint_f(vcell);
-    g.valid = !(g.nud + p.supp > p.nu) && !(g.nvd + p.supp > p.nv) && !(g.nvd - p.supp < 1);
-    g.dui = nint_f(__fmul_rn((float)p.osamp, __fsub_rn((float)g.nud, ucell)));
-    g.dvi = nint_f(__fmul_rn((float)p.osamp, __fsub_rn((float)g.nvd, vcell)));
-    return g;
-}
+// A visibility's plan data in caller order, one 32-byte sector: the plan record {WT, the
+// gridder's tap-table offsets, observed value in the gridding frame}, the degridding word
+// (with the gridding-frame conjugation in bit 0) and the rotation.  The gather into sorted
+// order reads one sector per visibility.
+struct __align__(32) PlanRecU {
+    float4 rec;
+    uint32_t gdd;
+    float rc, rs;
+    uint32_t pad;
+};
 
-// Per visibility (caller order): gridding key; the plan record {WT, packed GRDH2D offsets |
-// column-in-pair << 16, observed value in the gridding frame} (the gather moves it whole);
-// the degridding word with the conjugation in bit 28; the rotation.
+// Per visibility (caller order): gridding key, the PlanRecU sector and the exception flag,
+// from both routines' geometry (geom_vis).
 __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float *__restrict__ v,
                             const float *__restrict__ w, const float2 *__restrict__ vis,
                             const float *__restrict__ wt, int64_t n, uint32_t *keys,
-                            uint32_t *vals, float4 *rec_u, uint32_t *gdd_u, float2 *rot,
+                            uint32_t *vals, PlanRecU *rec_u, uint32_t *exc_flag,
                             unsigned long long *counts) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t nvalid = 0, nexc = 0;
@@ -165,53 +51,15 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
         float2 f = make_float2(0.f, 0.f), r = make_float2(1.f, 0.f);
         uint8_t gc = 0;
         if (wi > 0.0f) {
-            float2 vv = vis[i];
-            const float uf = u[i], vf = v[i], wf = w[i];
-            double ucell, vcell;
-            float fr, fi;
-            DGeo dg;
-            if (p.fast) {
-                dg = degrid_geom_fast(p, uf, vf);
-                fr = vv.x;
-                fi = vv.y;
-                ucell = __dmul_rn((double)p.uscale, (double)uf);
-                vcell = __dmul_rn((double)p.vscale, (double)vf);
-            } else {
-                // one rotation and one phase serve GRDDEH2D (always) and GRDH2D (DOSHIFT)
-                const double ug = (double)uf, vg = (double)vf, wg = (double)wf;
-                double ul, vl, wl, cd, sd;
-                rotate_uvw(p, ug, vg, wg, ul, vl, wl);
-                phase_cos_sin(__dmul_rn(p.twopi, __dsub_rn(wl, wg)), cd, sd);
-                dg = degrid_cell(p, ul, vl, (float)cd, (float)sd);
-                if (p.doshift) {
-                    const float c = (float)cd, s = (float)(-sd);
-                    fr = __fsub_rn(__fmul_rn(vv.x, c), __fmul_rn(vv.y, s));
-                    fi = __fadd_rn(__fmul_rn(vv.x, s), __fmul_rn(vv.y, c));
-                    ucell = __dadd_rn(__dmul_rn((double)p.uscale, ul), (double)p.uoffset);
-                    vcell = __dadd_rn(__dmul_rn((double)p.vscale, vl), (double)p.voffset);
-                    r = make_float2(dg.rc, dg.rs);
-                } else {
-                    fr = vv.x;
-                    fi = vv.y;
-                    ucell = __dadd_rn(__dmul_rn((double)p.uscale, ug), (double)p.uoffset);
-                    vcell = __dadd_rn(__dmul_rn((double)p.vscale, vg), (double)p.voffset);
-                }
-            }
-            if (ucell > 0.0) {
-                fi = -fi;
-                gc = 1;
-                ucell = __dadd_rn(ucell, (double)(float)p.uorigin);
-                vcell = __dadd_rn(vcell, (double)(float)p.vorigin);
-            } else {
-                ucell = __dadd_rn(-ucell, (double)(float)p.uorigin);
-                vcell = __dadd_rn(-vcell, (double)(float)p.vorigin);
-            }
-            const bool sane = fabs(ucell) < 1073741824.0 && fabs(vcell) < 1073741824.0;
-            int nuc = sane ? nint_dd(ucell) : 0, nvc = sane ? nint_dd(vcell) : 0;
-            bool gvalid = sane && !(nuc + 2 * p.supp > p.nu) && !(nvc + p.supp > p.nv) && !(nvc - p.supp < 1);
+            const float2 vv = vis[i];
+            const GGeo g = geom_vis(p, u[i], v[i], w[i], vv.x, vv.y);
+            const DGeo &dg = g.dg;
+            gc = g.gc ? 1 : 0;
+            r = make_float2(g.rc, g.rs);
+            const int nuc = g.nuc, nvc = g.nvc;
+            const bool gvalid = g.sane && !(nuc + 2 * p.supp > p.nu) && !(nvc + p.supp > p.nv) && !(nvc - p.supp < 1);
             if (gvalid) {
-                int dug = nint_dd(__dmul_rn((double)p.osamp, __dsub_rn((double)(float)nuc, ucell)));
-                int dvg = nint_dd(__dmul_rn((double)p.osamp, __dsub_rn((double)(float)nvc, vcell)));
+                const int dug = g.dug, dvg = g.dvg;
                 int ucen = nuc + p.supp, vcen = nvc;  // 1-based, gridding frame
                 int tu = (ucen - 1) >> TILE_LOG2, lu = (ucen - 1) & (TILE - 1);
                 int tv = (vcen - 1) >> TILE_LOG2, lv = (vcen - 1) & (TILE - 1);
@@ -230,16 +78,23 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
                 pdd = exc ? (taps_word(0, 0, off) | GDD_EXCEPTION) : taps_word(dg.dui, dg.dvi, off);
                 nvalid = 1;
                 nexc = exc;
-                f = make_float2(fr, fi);
+                f = make_float2(g.fr, g.fi);
             } else {
                 nexc = 1;  // degrid-only or degrid-invalid: exception path
             }
         }
         keys[i] = key;
         vals[i] = (uint32_t)i;
-        rec_u[i] = make_float4(wi, __uint_as_float(tw), f.x, f.y);
-        gdd_u[i] = pdd | (gc ? GDD_GCONJ_U : 0u);
-        if (rot) rot[i] = r;
+        PlanRecU pr;
+        pr.rec = make_float4(wi, __uint_as_float(tw), f.x, f.y);
+        pr.gdd = pdd | (gc ? GDD_GCONJ_U : 0u);
+        pr.rc = r.x;
+        pr.rs = r.y;
+        pr.pad = 0;
+        rec_u[i] = pr;
+        // GRDDEH2D's exception path takes the visibilities with WT > 0 that do not grid or
+        // whose degridding cell is not the gridding cell
+        exc_flag[i] = wi > 0.0f && (key == KEY_INVALID || (pdd & GDD_EXCEPTION) != 0);
     }
     // block-aggregated counters (one atomic per block and counter: per-warp atomics on three
     // addresses serialise in L2 at this visibility count)
@@ -252,44 +107,33 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
     }
 }
 
-// Gather the per-visibility arrays into sorted order: one 16-byte record and one word (and
-// the rotation when shifted) per visibility.  An exception that also grids learns its
-// sorted position here.
+// Gather the per-visibility data into sorted order (one 32-byte sector read per
+// visibility).  An exception that also grids learns its sorted position here.
 __global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned long long *counts,
-                              const float4 *__restrict__ rec_u, const uint32_t *__restrict__ gdd_u,
-                              const float2 *__restrict__ rot_u, const uint32_t *__restrict__ exc_slot,
+                              const PlanRecU *__restrict__ rec_u, const uint32_t *__restrict__ exc_slot,
                               float2 *fobs, float4 *rec, float *wt, uint32_t *gdd, uint32_t *orig,
                               float2 *rot, uint8_t *gconj, DegridExc *exc) {
     int64_t nv = (int64_t)counts[0];
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
     uint32_t i = perm[p];
-    const float4 r = rec_u[i];
-    const uint32_t d = gdd_u[i];
+    const PlanRecU pr = rec_u[i];
+    const float4 r = pr.rec;
+    const uint32_t d = pr.gdd;
     rec[p] = r;
     fobs[p] = make_float2(r.z, r.w);
     wt[p] = r.x;
     gdd[p] = d & ~GDD_GCONJ_U;
     orig[p] = i;
     gconj[p] = (d & GDD_GCONJ_U) ? 1 : 0;
-    if (rot) rot[p] = rot_u[i];
+    if (rot) rot[p] = make_float2(pr.rc, pr.rs);
     if ((d & GDD_EXCEPTION) && exc) exc[exc_slot[i]].pos = (int32_t)p;
-}
-
-// flags for the exception compaction
-__global__ void k_exc_flag(const float *__restrict__ wt, const uint32_t *__restrict__ keys_u,
-                           const uint32_t *__restrict__ gdd_u, int64_t n, uint32_t *flag) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t f = 0;
-    if (wt[i] > 0.0f) f = (keys_u[i] == KEY_INVALID) || ((gdd_u[i] & GDD_EXCEPTION) != 0);
-    flag[i] = f;
 }
 
 // (pos is set by k_plan_gather for the exceptions that also grid)
 __global__ void k_exc_write(GParams p, const float *__restrict__ u, const float *__restrict__ v,
                             const float *__restrict__ w, const float *__restrict__ wt,
-                            const uint32_t *__restrict__ gdd_u,
+                            const PlanRecU *__restrict__ rec_u,
                             const uint32_t *__restrict__ flag, const uint32_t *__restrict__ slot,
                             int64_t n, DegridExc *exc, float *exc_wt, float2 *exc_rot) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -304,7 +148,7 @@ __global__ void k_exc_write(GParams p, const float *__restrict__ u, const float 
     e.delvi = (int16_t)g.dvi;
     e.conj = g.conj;
     e.valid = g.valid;
-    e.gconj = (gdd_u[i] & GDD_GCONJ_U) ? 1 : 0;
+    e.gconj = (rec_u[i].gdd & GDD_GCONJ_U) ? 1 : 0;
     e.pad = 0;
     uint32_t s = slot[i];
     exc[s] = e;
@@ -580,32 +424,28 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         for (int k = 0; k < 9; k++)
             if (k % 4 != 0 && spec->shift[k] != 0.0) gp.diagonal = 0;
         gp.fast = gp.identity && spec->uoffset == 0.0f && spec->voffset == 0.0f;
+        gp.near_id = gp.diagonal && fabs(spec->shift[0] - 1.0) <= 0x1p-50 && fabs(spec->shift[4] - 1.0) <= 0x1p-50 &&
+                     spec->uoffset == 0.0f && spec->voffset == 0.0f && spec->osamp >= 1 && spec->osamp <= 65536;
         gp.ntu = pl->ntu;
         gp.twopi = (double)(8.0f * atanf(1.0f));  // TWOPI = 8 * ATAN(1.0), REAL (grdh2d.f:91)
 
-        uint32_t *keys, *vals, *ktmp, *vtmp, *gdd_u;
-        float4 *rec_u;
-        float2 *rot_u = nullptr;
+        uint32_t *keys, *vals, *ktmp, *vtmp, *flag;
+        PlanRecU *rec_u;
         unsigned long long *counts;
         PL_TRY(ctx_scratch(ctx, "pl_keys", 4 * n, (void **)&keys));
         PL_TRY(ctx_scratch(ctx, "pl_vals", 4 * n, (void **)&vals));
         PL_TRY(ctx_scratch(ctx, "pl_ktmp", 4 * n, (void **)&ktmp));
         PL_TRY(ctx_scratch(ctx, "pl_vtmp", 4 * n, (void **)&vtmp));
-        PL_TRY(ctx_scratch(ctx, "pl_gdd", 4 * n, (void **)&gdd_u));
-        PL_TRY(ctx_scratch(ctx, "pl_rec", 16 * n, (void **)&rec_u));
-        if (pl->doshift) PL_TRY(ctx_scratch(ctx, "pl_rot", 8 * n, (void **)&rot_u));
+        PL_TRY(ctx_scratch(ctx, "pl_flag", 4 * n, (void **)&flag));
+        PL_TRY(ctx_scratch(ctx, "pl_rec", sizeof(PlanRecU) * n, (void **)&rec_u));
         PL_TRY(ctx_scratch(ctx, "pl_counts", 64, (void **)&counts));
         PL_CUDA(cudaMemsetAsync(counts, 0, 64, st));
         const int T = 256;
         if (nvis > 0) {
             k_plan_geom<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dvis, dwt, nvis, keys, vals,
-                                                       rec_u, gdd_u, rot_u, counts);
+                                                       rec_u, flag, counts);
             PL_CUDA(cudaGetLastError());
         }
-        // The user-order keys are needed again by the exception pass: keep a copy.
-        uint32_t *keys_u;
-        PL_TRY(ctx_scratch(ctx, "pl_keys_u", 4 * n, (void **)&keys_u));
-        if (nvis > 0) PL_CUDA(cudaMemcpyAsync(keys_u, keys, 4 * n, cudaMemcpyDeviceToDevice, st));
         int64_t ntiles = (int64_t)pl->ntu * pl->ntv;
         int kbits = bits_for((ntiles << 12) + 1);
         if (kbits > 32) {
@@ -636,20 +476,16 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         PL_TRY(plan_alloc(pl, (void **)&pl->exc, exc_bytes(ne1)));
         uint32_t *slot = nullptr;
         if (nexc > 0) {
-            uint32_t *flag;
-            PL_TRY(ctx_scratch(ctx, "pl_flag", 4 * n, (void **)&flag));
             PL_TRY(ctx_scratch(ctx, "pl_slot", 4 * n, (void **)&slot));
-            k_exc_flag<<<ceil_div(nvis, T), T, 0, st>>>(dwt, keys_u, gdd_u, nvis, flag);
-            PL_CUDA(cudaGetLastError());
             PL_TRY(launch_exclusive_scan_u32(ctx, flag, slot, nvis, nullptr));
             float *exc_wt = (float *)((char *)pl->exc + exc_wt_off(ne1));
             float2 *exc_rot = (float2 *)((char *)pl->exc + exc_rot_off(ne1));
-            k_exc_write<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dwt, gdd_u, flag, slot, nvis,
+            k_exc_write<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dwt, rec_u, flag, slot, nvis,
                                                        pl->exc, exc_wt, exc_rot);
             PL_CUDA(cudaGetLastError());
         }
         if (nvalid > 0) {
-            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, rec_u, gdd_u, rot_u, slot,
+            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, rec_u, slot,
                                                            pl->fobs, pl->rec, pl->wt, pl->gdd,
                                                            pl->orig, pl->rot, pl->gconj,
                                                            nexc > 0 ? pl->exc : nullptr);

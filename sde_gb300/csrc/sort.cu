@@ -118,27 +118,131 @@ __global__ void k_last_plus(const uint32_t *in, const uint32_t *scanned, int64_t
 }
 
 // ---------------------------------------------------------------------------------------
-// Radix sort.
+// Radix sort.  Each pass: per-block digit counts (k_rs_hist), one exclusive scan of the
+// digit-major count table (the global start of every (digit, block) run), and a scatter
+// that ranks the block's items stably in shared memory and writes each digit's run of the
+// block as consecutive addresses.
 constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ROUNDS = 16;
-constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;   // items per block
+constexpr int RS_WARP_ITEMS = RS_TILE / RS_WARPS;  // contiguous items per warp
 
 template <typename K>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const K *keys, int64_t n, int shift,
                                                          uint32_t *hist, int nb) {
-    __shared__ uint32_t h[256];
-    const int t = threadIdx.x;
-    h[t] = 0;
+    // one count table per warp: items of one digit arrive together in the later passes
+    __shared__ uint32_t h[RS_WARPS][256];
+    const int t = threadIdx.x, warp = t >> 5;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) h[w][t] = 0;
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    // all of the thread's loads before the first count
+    K k[RS_ROUNDS];
+#pragma unroll
     for (int r = 0; r < RS_ROUNDS; r++) {
-        int64_t i = base + r * RS_THREADS + t;
-        if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & 255u], 1u);
+        const int64_t i = base + r * RS_THREADS + t;
+        k[r] = i < n ? keys[i] : (K)0;
     }
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++)
+        if (base + r * RS_THREADS + t < n) atomicAdd(&h[warp][(uint32_t)(k[r] >> shift) & 255u], 1u);
     __syncthreads();
-    hist[(int64_t)t * nb + blockIdx.x] = h[t];
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) c += h[w][t];
+    hist[(int64_t)t * nb + blockIdx.x] = c;
 }
 
+// Scatter of one pass, for keys in any order: the block's RS_TILE items are ranked stably in
+// shared memory (warp w ranks its RS_WARP_ITEMS consecutive items round by round; item order
+// is (warp, round, lane)), and each digit's run of the block is written to consecutive
+// addresses.
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter_ranked(const uint32_t *kin, const uint32_t *vin,
+                                                                   uint32_t *kout, uint32_t *vout, int64_t n,
+                                                                   int shift, const uint32_t *offs, int nb) {
+    __shared__ uint32_t wcnt[RS_WARPS][256];  // per-warp digit counts, then the warp's offsets
+    __shared__ uint32_t dstart[256];          // the digit's first position in the block
+    __shared__ uint32_t gbase[256];           // the digit's first position in the output
+    __shared__ uint32_t wtot[RS_WARPS];
+    __shared__ uint32_t kbuf[RS_TILE], vbuf[RS_TILE];  // the block's items in (digit, item) order
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) wcnt[w][t] = 0;
+    gbase[t] = offs[(int64_t)t * nb + blockIdx.x];
+    const int64_t wbase = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * RS_WARP_ITEMS;
+    uint32_t key[RS_ROUNDS], val[RS_ROUNDS], pos[RS_ROUNDS];
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const int64_t i = wbase + r * 32 + lane;
+        key[r] = i < n ? kin[i] : 0u;
+        val[r] = i < n ? vin[i] : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const bool valid = wbase + r * 32 + lane < n;
+        const uint32_t digit = valid ? ((key[r] >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        const uint32_t before = valid ? wcnt[warp][digit] : 0u;
+        pos[r] = before + __popc(peers & lt);
+        __syncwarp();
+        if (valid && (peers & lt) == 0) wcnt[warp][digit] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // digit t: offsets of the warps' runs within the digit, and the digit's total
+    {
+        uint32_t acc = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) {
+            const uint32_t c = wcnt[w][t];
+            wcnt[w][t] = acc;
+            acc += c;
+        }
+        // block-wide exclusive scan of the digit totals
+        uint32_t x = acc;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        if (lane == 31) wtot[warp] = x;
+        __syncthreads();
+        uint32_t pre = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) pre += w < warp ? wtot[w] : 0u;
+        dstart[t] = pre + x - acc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        if (wbase + r * 32 + lane < n) {
+            const uint32_t digit = (key[r] >> shift) & 255u;
+            const uint32_t p = dstart[digit] + wcnt[warp][digit] + pos[r];
+            kbuf[p] = key[r];
+            vbuf[p] = val[r];
+        }
+    }
+    __syncthreads();
+    const int nblk = (int)min((int64_t)RS_TILE, n - (int64_t)blockIdx.x * RS_TILE);
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const int p = r * RS_THREADS + t;
+        if (p < nblk) {
+            const uint32_t k = kbuf[p];
+            const uint32_t digit = (k >> shift) & 255u;
+            const uint32_t d = gbase[digit] + (uint32_t)p - dstart[digit];
+            kout[d] = k;
+            vout[d] = vbuf[p];
+        }
+    }
+}
+
+// Scatter of one pass, round by round through the block (items of one digit in a round go
+// to consecutive addresses): the better choice once the keys are nearly in order.
 template <typename K>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const K *kin, const uint32_t *vin,
                                                             K *kout, uint32_t *vout, int64_t n,
@@ -202,8 +306,13 @@ int radix_sort(sde_ctx *ctx, K *keys, uint32_t *vals, int64_t n, int bits, K *kt
         k_rs_hist<K><<<nb, RS_THREADS, 0, ctx->stream>>>(src_k, n, shift, hist, nb);
         SDE_CHECK_LAUNCH();
         SDE_TRY((scan_impl<uint32_t, OpAdd>(ctx, hist, hist, (int64_t)256 * nb, 0u, 0, 0)));
-        k_rs_scatter<K><<<nb, RS_THREADS, 0, ctx->stream>>>(src_k, src_v, dst_k, dst_v, n, shift,
-                                                             hist, nb);
+        if (sizeof(K) == 4)
+            k_rs_scatter_ranked<<<nb, RS_THREADS, 0, ctx->stream>>>(
+                reinterpret_cast<const uint32_t *>(src_k), src_v, reinterpret_cast<uint32_t *>(dst_k),
+                dst_v, n, shift, hist, nb);
+        else
+            k_rs_scatter<K><<<nb, RS_THREADS, 0, ctx->stream>>>(src_k, src_v, dst_k, dst_v, n, shift,
+                                                                 hist, nb);
         SDE_CHECK_LAUNCH();
         K *tk = src_k; src_k = dst_k; dst_k = tk;
         uint32_t *tv = src_v; src_v = dst_v; dst_v = tv;
