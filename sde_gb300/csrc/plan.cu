@@ -5,7 +5,9 @@
 // GRDDEH2D uses (FP32 cell from FP64 coordinates, grd/grddeh2d.f:92-118).  Visibilities
 // are then sorted by (uv tile, cell), split into same-cell chunks of <= CHUNK_MAX, and the
 // chunks of each work item are ordered by (7x7 colour class, chunk index, cell) so that
-// the 32 chunks a warp flushes at once never overlap.  The observed visibilities are
+// the 32 chunks a warp flushes at once never overlap; the plan stores the visibilities in
+// that chunk order, so a team's concurrent chunks read one contiguous range.  The observed
+// visibilities are
 // stored already rotated/conjugated into the gridding frame (FVIS of grd/grdh2d.f:125-143),
 // so the per-cycle kernels carry no FP64 or trigonometric work.
 #include <math.h>
@@ -239,7 +241,7 @@ __global__ void k_chunk_len(const uint32_t *__restrict__ cstart, int64_t nchunks
 __global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t *__restrict__ cval,
                               const uint32_t *__restrict__ cstart, const uint32_t *__restrict__ keys,
                               int64_t nchunks, int64_t nvalid, int shift_item, uint2 *chunks,
-                              WorkItem *items) {
+                              uint32_t *clen, WorkItem *items) {
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nchunks) return;
     uint32_t orig = cval[c];
@@ -247,9 +249,32 @@ __global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t 
     uint32_t en = (int64_t)orig + 1 < nchunks ? cstart[orig + 1] : (uint32_t)nvalid;
     uint32_t cell = keys[st] & 4094u;
     chunks[c] = make_uint2(st, cell | ((en - st) << 16));
+    clen[c] = en - st;
     uint32_t it = (uint32_t)(ckey[c] >> shift_item);
     if (c == 0 || (uint32_t)(ckey[c - 1] >> shift_item) != it) items[it].cbeg = (int32_t)c;
     if (c == nchunks - 1 || (uint32_t)(ckey[c + 1] >> shift_item) != it) items[it].cend = (int32_t)(c + 1);
+}
+
+// The plan stores its visibilities in chunk order: chunk c's visibilities at
+// [cpos[c], cpos[c] + length), the chunks in the order the kernels take them, so that a team
+// reads the visibilities of the chunks it takes together from one contiguous range.  src[]
+// receives the caller index of every plan position (the sort's permutation through the
+// chunk order); chunk starts move to their new positions.
+__global__ void k_chunk_relocate(const uint32_t *__restrict__ perm, const uint32_t *__restrict__ cpos,
+                                 int64_t nchunks, uint2 *chunks, uint32_t *src) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const uint2 ch = chunks[c];
+    const uint32_t st = ch.x, len = ch.y >> 16, to = cpos[c];
+    for (uint32_t k = 0; k < len; k++) src[to + k] = perm[st + k];
+    chunks[c] = make_uint2(to, ch.y);
+}
+
+// a work item's first visibility: its first chunk's (new) start
+__global__ void k_item_vbeg(const uint2 *__restrict__ chunks, int64_t nitems, WorkItem *items) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nitems) return;
+    items[t].vbeg = (int32_t)chunks[items[t].cbeg].x;
 }
 
 // dense flag of each work item: its tile's items (contiguous, sorted by tile) together
@@ -484,13 +509,6 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
                                                        pl->exc, exc_wt, exc_rot);
             PL_CUDA(cudaGetLastError());
         }
-        if (nvalid > 0) {
-            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vals, counts, rec_u, slot,
-                                                           pl->fobs, pl->rec, pl->wt, pl->gdd,
-                                                           pl->orig, pl->rot, pl->gconj,
-                                                           nexc > 0 ? pl->exc : nullptr);
-            PL_CUDA(cudaGetLastError());
-        }
         // runs, chunks, work items
         if (nvalid > 0) {
             int32_t *runhead, *tilehead;
@@ -539,9 +557,24 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
             const int shift_item = LENBIN_BITS + 6 + lbits + jbits + 12;
             const int cbits = shift_item + bits_for(nitems);
             PL_TRY(launch_radix_sort_u64(ctx, ckey, cval, nchunks, cbits, cktmp, cvtmp));
+            uint32_t *clen, *cpos;
+            PL_TRY(ctx_scratch(ctx, "pl_clen", 4 * (size_t)nchunks, (void **)&clen));
+            PL_TRY(ctx_scratch(ctx, "pl_cpos", 4 * (size_t)nchunks, (void **)&cpos));
             k_chunk_final<<<ceil_div(nchunks, T), T, 0, st>>>(ckey, cval, cstart, keys, nchunks,
-                                                            nvalid, shift_item, pl->chunks,
+                                                            nvalid, shift_item, pl->chunks, clen,
                                                             pl->items);
+            PL_CUDA(cudaGetLastError());
+            // chunk order: the sort's permutation through the chunks (into the sort's
+            // value scratch, free now), then one gather of the caller-order sectors
+            PL_TRY(launch_exclusive_scan_u32(ctx, clen, cpos, nchunks, nullptr));
+            k_chunk_relocate<<<ceil_div(nchunks, T), T, 0, st>>>(vals, cpos, nchunks, pl->chunks, vtmp);
+            PL_CUDA(cudaGetLastError());
+            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vtmp, counts, rec_u, slot,
+                                                           pl->fobs, pl->rec, pl->wt, pl->gdd,
+                                                           pl->orig, pl->rot, pl->gconj,
+                                                           nexc > 0 ? pl->exc : nullptr);
+            PL_CUDA(cudaGetLastError());
+            k_item_vbeg<<<ceil_div(nitems, T), T, 0, st>>>(pl->chunks, nitems, pl->items);
             PL_CUDA(cudaGetLastError());
             k_item_vend<<<ceil_div(nitems, T), T, 0, st>>>(pl->items, nitems, nvalid);
             PL_CUDA(cudaGetLastError());
