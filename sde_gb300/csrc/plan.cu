@@ -1,15 +1,15 @@
-// plan.cu -- builds a resident, tile-sorted visibility set (sde_plan).
+// plan.cu -- builds a resident, tile- and chunk-sorted visibility set (sde_plan).
 //
-// For every visibility the plan evaluates, once and with the reference's exact FP64/FP32
-// operations, the cell placement that GRDH2D uses (FP64, grd/grdh2d.f:114-166) and the one
-// GRDDEH2D uses (FP32 cell from FP64 coordinates, grd/grddeh2d.f:92-118).  Visibilities
-// are then sorted by (uv tile, cell), split into same-cell chunks of <= CHUNK_MAX, and the
+// For every visibility the plan evaluates, once, the cell placement that GRDH2D uses (FP64,
+// grd/grdh2d.f:114-166) and the one GRDDEH2D uses (FP32 cell from FP64 coordinates,
+// grd/grddeh2d.f:92-118), with the reference's results: its exact operations, or FP32
+// arithmetic whose error bound decides the same roundings (geom.cuh).  Visibilities are
+// then sorted by (uv tile, cell), split into same-cell chunks of <= CHUNK_MAX, and the
 // chunks of each work item are ordered by (7x7 colour class, chunk index, cell) so that
 // the 32 chunks a warp flushes at once never overlap; the plan stores the visibilities in
 // that chunk order, so a team's concurrent chunks read one contiguous range.  The observed
-// visibilities are
-// stored already rotated/conjugated into the gridding frame (FVIS of grd/grdh2d.f:125-143),
-// so the per-cycle kernels carry no FP64 or trigonometric work.
+// visibilities are stored already rotated/conjugated into the gridding frame (FVIS of
+// grd/grdh2d.f:125-143), so the per-cycle kernels carry no FP64 or trigonometric work.
 #include <math.h>
 #include <string.h>
 
