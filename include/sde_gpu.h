@@ -352,7 +352,7 @@ int sde_model_image(sde_ctx *ctx, int ncomp, const char *types, const float *flu
                     int ny, float refx, float deltx, float refy, float delty, float *image);
 
 /* IMGDOUBL (source/img/imgdoubl.f:7, with PIXRPAD, source/pix/pixrpad.f:7) for a 2-D image,
- * called by IMGTOVIS (img/imgtovis.f:50) before it transforms and degrids a model: in
+ * called by IMGTOVIS (img/imgtovis.f:55) before it transforms and degrids a model: in
  * (device, ny x nx, reference pixel rpix_x, rpix_y, 1-based) is placed in out (device,
  * py x px, zero elsewhere), px = FFTPWR2(2 nx) and py = FFTPWR2(2 ny) (1 for a one-pixel
  * axis; any other px, py is refused), with left margin NINT(px/2 - RPIX) per axis, so the

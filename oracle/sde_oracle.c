@@ -2461,7 +2461,7 @@ void orc_imgdoubl(const float *in, int nx, int ny, float rpix_x, float rpix_y, f
     *rpix_y_out = rpix_y + (float)ls[1];
 }
 
-/* img/imgtovis.f:50-73: IMGDOUBL (the model padded to P = FFTPWR2(2N), its reference pixel
+/* img/imgtovis.f:55-84: IMGDOUBL (the model padded to P = FFTPWR2(2N), its reference pixel
  * moved to P/2), the grid of the padded image (FFTCONJA: NU = P/2+1, NV = P, uv cells half
  * the size of the image's own grid), then IMGGRIDC CORRECT, IMGFFT and VISDEGRI on it.  The
  * image's reference pixel is (N+1)/2, uvmap's; the padded one is then P/2 = (P+1)/2, the

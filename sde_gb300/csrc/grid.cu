@@ -1,17 +1,20 @@
 // grid.cu -- tiled gridding (GRDH2D) and degridding (GRDDEH2D) over a sde_plan.
 //
-// Gridding: one CTA per work item keeps the item's 64x64-cell tile plus a 3-cell halo in
-// shared memory.  A 4-lane group owns a chunk (<= CHUNK_MAX visibilities of one cell) and
-// accumulates the chunk's 7x7 complex footprint in registers (two columns per lane), then
-// adds it into the shared tile once; the chunk order (colour class, length class, chunk
-// index, cell) makes the 8 chunks of a warp write disjoint cells and have similar lengths.
-// The shared tile is then reduced into the raw grid in HBM with vector red.global.add (only
-// the cells the item touched).
+// Both kernels are persistent: one CTA per SM of TEAMS teams of 256 threads; a team takes
+// work items (<= ITEM_MAX visibilities of one 64x64-cell tile) from an atomic counter.
 //
-// Degridding: one CTA per work item stages the model grid's tile (+halo) into shared
-// memory with a single TMA 2-D bulk copy, then a 4-lane group per chunk interpolates the
-// chunk's visibilities from a register copy of the chunk cell's 7x7 neighbourhood (two
-// columns per lane) and reduces the lanes' partial sums with shuffles.
+// Gridding: a team keeps its item's tile plus a 3-cell halo in shared memory.  A 4-lane
+// group owns a chunk (<= CHUNK_MAX visibilities of one cell pair) and accumulates the
+// chunk's 7x8 complex footprint in registers (two columns per lane), then adds it into the
+// shared tile once; the chunk order (length bin, colour class, length class, chunk index,
+// cell) gives the 8 chunks of a warp mostly disjoint cells and similar lengths.  The shared
+// tile is then reduced into the raw grid in HBM with vector red.global.add (only the cells
+// the item touched).
+//
+// Degridding: a team stages the model grid's tile (+halo) into shared memory with a single
+// TMA 2-D bulk copy, then a 4-lane group per chunk interpolates the chunk's visibilities
+// from a register copy of the chunk cell's 7x8 neighbourhood (two columns per lane) and
+// reduces the lanes' partial sums with shuffles.
 #include <math.h>
 #include <string.h>
 

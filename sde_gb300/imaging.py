@@ -361,7 +361,7 @@ def image_double(ctx, image, rpix_x, rpix_y):
 
 
 def padded_geom(geom):
-    """The grid geometry IMGTOVIS degrids from (img/imgtovis.f:52-56): FFTCONJA of the image
+    """The grid geometry IMGTOVIS degrids from (img/imgtovis.f:60-63): FFTCONJA of the image
     padded by IMGDOUBL -- FFTPWR2(2N) pixels at the same cell size, so the uv cells are half
     as large; with uvmap's reference pixel (N+1)/2 the padded one is P/2, this geometry's
     centre."""
@@ -370,7 +370,7 @@ def padded_geom(geom):
 
 
 def imgtovis(ctx, geom, plan_padded, image, vis_out, wt_out):
-    """img/imgtovis.f:50-73 for a 2-D model image of geom (reference pixel (N+1)/2): IMGDOUBL,
+    """img/imgtovis.f:55-84 for a 2-D model image of geom (reference pixel (N+1)/2): IMGDOUBL,
     then IMGGRIDC CORRECT, IMGFFT and VISDEGRI on the padded image's grid.  plan_padded is a
     Plan built on padded_geom(geom) (once per job, like the degrid plan of a major cycle)."""
     pg = plan_padded.geom

@@ -222,7 +222,7 @@ def test_weights_az_norm(gpu_ctx, orc, obs_small, obs_shift, case):
 
 
 def test_imgtovis_padded_degrid_matches_oracle(gpu_ctx, orc, obs_small, obs_shift):
-    """IMGTOVIS (img/imgtovis.f:50-73), the degrid of mosclean's major cycle
+    """IMGTOVIS (img/imgtovis.f:55-84), the degrid of mosclean's major cycle
     (task/mosclean.f:361): IMGDOUBL pads the model to FFTPWR2(2N) with the reference pixel
     moved to the centre (bit-exact against the oracle's PIXRPAD), then the padded image's
     grid -- uv cells half as large -- is corrected, transformed and degridded; visibilities
