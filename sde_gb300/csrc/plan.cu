@@ -158,66 +158,89 @@ __global__ void k_exc_write(GParams p, const float *__restrict__ u, const float 
     exc_rot[s] = make_float2(g.rc, g.rs);
 }
 
-// Run / tile heads over the sorted keys (-1 where not a head) for the max-scans.
-__global__ void k_heads(const uint32_t *__restrict__ keys, const unsigned long long *counts,
-                        int32_t *runhead, int32_t *tilehead) {
-    int64_t nv = (int64_t)counts[0];
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Runs, work items and chunks from the sorted keys.  A run is one cell pair of one tile
+// (equal key >> 1); a tile's visibilities split into work items at every item_max from the
+// tile's first one; a run's part within one item (a piece) splits into chunks of chunk_max
+// from the piece's start.  Chunks and items are numbered in position order.
+__global__ void k_run_heads(const uint32_t *__restrict__ keys, const unsigned long long *counts,
+                            uint32_t *head) {
+    const int64_t nv = (int64_t)counts[0];
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nv) return;
-    uint32_t k = keys[q];
-    bool rh = q == 0 || (keys[q - 1] >> 1) != (k >> 1);  // runs of one cell pair
-    bool th = q == 0 || (keys[q - 1] >> 12) != (k >> 12);
-    runhead[q] = rh ? (int32_t)q : -1;
-    tilehead[q] = th ? (int32_t)q : -1;
+    head[q] = q == 0 || (keys[q - 1] >> 1) != (keys[q] >> 1);
 }
 
-__global__ void k_chunk_flags(const unsigned long long *counts, const int32_t *runstart,
-                              const int32_t *tilestart, int item_max, int chunk_max,
-                              uint32_t *ihead, uint32_t *chead) {
-    int64_t nv = (int64_t)counts[0];
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nv) return;
-    int32_t rs = runstart[q], ts = tilestart[q];
-    int32_t is = ts + ((int32_t)q - ts) / item_max * item_max;  // item start
-    int32_t cs = rs > is ? rs : is;                            // run start within item
-    bool ih = ((int32_t)q - ts) % item_max == 0;
-    bool ch = ((int32_t)q - cs) % chunk_max == 0;
-    ihead[q] = ih;
-    chead[q] = ch || ih;
+__global__ void k_run_compact(const uint32_t *__restrict__ head, const uint32_t *__restrict__ ridx,
+                              const unsigned long long *counts, uint32_t *rstart) {
+    const int64_t nv = (int64_t)counts[0];
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nv && head[q]) rstart[ridx[q]] = (uint32_t)q;
 }
 
-__global__ void k_chunk_write(const uint32_t *__restrict__ keys, const unsigned long long *counts,
-                              const int32_t *runstart, const int32_t *tilestart,
-                              const uint32_t *ihead, const uint32_t *chead,
-                              const uint32_t *item_id, const uint32_t *chunk_id, int item_max,
-                              int chunk_max, int lbits, int jbits,
-                              uint64_t *ckey, uint32_t *cval, uint32_t *cstart, WorkItem *items) {
-    int64_t nv = (int64_t)counts[0];
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nv) return;
-    uint32_t k = keys[q];
-    uint32_t it = item_id[q] + ihead[q] - 1;  // inclusive item index
-    if (ihead[q]) {
-        WorkItem wi;
-        wi.tile = (int32_t)(k >> 12);
-        wi.cbeg = wi.cend = 0;
-        wi.vbeg = (int32_t)q;
-        wi.vend = 0;
-        wi.dense = 0;
-        items[it] = wi;
+// a run that starts a tile: its start (the tile's first visibility), else -1, for a max-scan
+__global__ void k_run_tilehead(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ rstart,
+                               int64_t nruns, int32_t *tstart) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nruns) return;
+    const uint32_t rs = rstart[r];
+    const bool th = r == 0 || (keys[rstart[r - 1]] >> 12) != (keys[rs] >> 12);
+    tstart[r] = th ? (int32_t)rs : -1;
+}
+
+// the run's chunks and item heads (an item head is a position ts + k*item_max of the run)
+__global__ void k_run_counts(const uint32_t *__restrict__ rstart, const int32_t *__restrict__ tstart,
+                             int64_t nruns, int64_t nvalid, int item_max, int chunk_max, uint32_t *nch,
+                             uint32_t *nih) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nruns) return;
+    const int64_t rs = rstart[r], re = r + 1 < nruns ? (int64_t)rstart[r + 1] : nvalid, ts = tstart[r];
+    uint32_t c = 0, h = 0;
+    for (int64_t a = rs; a < re;) {
+        const int64_t is = ts + (a - ts) / item_max * item_max;
+        h += is == a;
+        const int64_t b = min(re, is + item_max);
+        c += (uint32_t)((b - a + chunk_max - 1) / chunk_max);
+        a = b;
     }
-    if (!chead[q]) return;
-    uint32_t c = chunk_id[q];
-    int32_t rs = runstart[q], ts = tilestart[q];
-    int32_t is = ts + ((int32_t)q - ts) / item_max * item_max;
-    int32_t cs = rs > is ? rs : is;
-    uint32_t j = ((uint32_t)q - (uint32_t)cs) / (uint32_t)chunk_max;
-    uint32_t cell = k & 4094u, lu = cell & 63u, lv = cell >> 6;  // pair's even cell
-    uint32_t color = ((lu >> 1) & 3u) * 7u + (lv % 7u);
-    ckey[c] = ((uint64_t)it << (LENBIN_BITS + 6 + lbits + jbits + 12)) |
-              ((uint64_t)color << (lbits + jbits + 12)) | ((uint64_t)j << 12) | cell;
-    cval[c] = c;
-    cstart[c] = (uint32_t)q;
+    nch[r] = c;
+    nih[r] = h;
+}
+
+// the run's chunk records (sort key, index, start) and the items that start in it
+__global__ void k_run_emit(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ rstart,
+                           const int32_t *__restrict__ tstart, int64_t nruns, int64_t nvalid,
+                           const uint32_t *__restrict__ cbase, const uint32_t *__restrict__ ibase,
+                           int item_max, int chunk_max, int lbits, int jbits, uint64_t *ckey,
+                           uint32_t *cval, uint32_t *cstart, WorkItem *items) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nruns) return;
+    const int64_t rs = rstart[r], re = r + 1 < nruns ? (int64_t)rstart[r + 1] : nvalid, ts = tstart[r];
+    const uint32_t k = keys[rs];
+    const uint32_t cell = k & 4094u, lu = cell & 63u, lv = cell >> 6;  // pair's even cell
+    const uint32_t color = ((lu >> 1) & 3u) * 7u + (lv % 7u);
+    uint32_t c = cbase[r], nit = ibase[r];  // items started before the run's current piece
+    for (int64_t a = rs; a < re;) {
+        const int64_t is = ts + (a - ts) / item_max * item_max;
+        if (is == a) {
+            WorkItem wi;
+            wi.tile = (int32_t)(k >> 12);
+            wi.cbeg = wi.cend = 0;
+            wi.vbeg = (int32_t)a;
+            wi.vend = 0;
+            wi.dense = 0;
+            items[nit++] = wi;
+        }
+        const uint64_t it = nit - 1;
+        const int64_t b = min(re, is + item_max);
+        uint32_t j = 0;
+        for (int64_t q = a; q < b; q += chunk_max, j++, c++) {
+            ckey[c] = (it << (LENBIN_BITS + 6 + lbits + jbits + 12)) |
+                      ((uint64_t)color << (lbits + jbits + 12)) | ((uint64_t)j << 12) | cell;
+            cval[c] = c;
+            cstart[c] = (uint32_t)q;
+        }
+        a = b;
+    }
 }
 
 // Length class (CHUNK_MAX - length) of each chunk, above the chunk index in its sort key,
@@ -511,26 +534,37 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         }
         // runs, chunks, work items
         if (nvalid > 0) {
-            int32_t *runhead, *tilehead;
-            uint32_t *ihead, *chead, *item_id, *chunk_id, *tot;
-            PL_TRY(ctx_scratch(ctx, "pl_runhead", 4 * nv1, (void **)&runhead));
-            PL_TRY(ctx_scratch(ctx, "pl_tilehead", 4 * nv1, (void **)&tilehead));
-            PL_TRY(ctx_scratch(ctx, "pl_ihead", 4 * nv1, (void **)&ihead));
-            PL_TRY(ctx_scratch(ctx, "pl_chead", 4 * nv1, (void **)&chead));
-            PL_TRY(ctx_scratch(ctx, "pl_itemid", 4 * nv1, (void **)&item_id));
-            PL_TRY(ctx_scratch(ctx, "pl_chunkid", 4 * nv1, (void **)&chunk_id));
+            uint32_t *head, *ridx, *tot;
+            PL_TRY(ctx_scratch(ctx, "pl_runhead", 4 * nv1, (void **)&head));
+            PL_TRY(ctx_scratch(ctx, "pl_runidx", 4 * nv1, (void **)&ridx));
             PL_TRY(ctx_scratch(ctx, "pl_tot", 16, (void **)&tot));
-            k_heads<<<ceil_div(nvalid, T), T, 0, st>>>(keys, counts, runhead, tilehead);
+            k_run_heads<<<ceil_div(nvalid, T), T, 0, st>>>(keys, counts, head);
             PL_CUDA(cudaGetLastError());
-            PL_TRY(launch_inclusive_max_scan_i32(ctx, runhead, runhead, nvalid));
-            PL_TRY(launch_inclusive_max_scan_i32(ctx, tilehead, tilehead, nvalid));
-            k_chunk_flags<<<ceil_div(nvalid, T), T, 0, st>>>(counts, runhead, tilehead, pl->item_max,
-                                                           pl->chunk_max, ihead, chead);
+            PL_TRY(launch_exclusive_scan_u32(ctx, head, ridx, nvalid, tot));
+            uint32_t hruns = 0;
+            PL_CUDA(cudaMemcpyAsync(&hruns, tot, sizeof hruns, cudaMemcpyDeviceToHost, st));
+            PL_CUDA(cudaStreamSynchronize(st));
+            const int64_t nruns = hruns;
+            uint32_t *rstart, *nch, *nih, *cbase, *ibase;
+            int32_t *tstart;
+            PL_TRY(ctx_scratch(ctx, "pl_rstart", 4 * (size_t)nruns, (void **)&rstart));
+            PL_TRY(ctx_scratch(ctx, "pl_tstart", 4 * (size_t)nruns, (void **)&tstart));
+            PL_TRY(ctx_scratch(ctx, "pl_nch", 4 * (size_t)nruns, (void **)&nch));
+            PL_TRY(ctx_scratch(ctx, "pl_nih", 4 * (size_t)nruns, (void **)&nih));
+            PL_TRY(ctx_scratch(ctx, "pl_cbase", 4 * (size_t)nruns, (void **)&cbase));
+            PL_TRY(ctx_scratch(ctx, "pl_ibase", 4 * (size_t)nruns, (void **)&ibase));
+            k_run_compact<<<ceil_div(nvalid, T), T, 0, st>>>(head, ridx, counts, rstart);
             PL_CUDA(cudaGetLastError());
-            PL_TRY(launch_exclusive_scan_u32(ctx, ihead, item_id, nvalid, tot));
-            PL_TRY(launch_exclusive_scan_u32(ctx, chead, chunk_id, nvalid, tot + 1));
+            k_run_tilehead<<<ceil_div(nruns, T), T, 0, st>>>(keys, rstart, nruns, tstart);
+            PL_CUDA(cudaGetLastError());
+            PL_TRY(launch_inclusive_max_scan_i32(ctx, tstart, tstart, nruns));
+            k_run_counts<<<ceil_div(nruns, T), T, 0, st>>>(rstart, tstart, nruns, nvalid, pl->item_max,
+                                                         pl->chunk_max, nch, nih);
+            PL_CUDA(cudaGetLastError());
+            PL_TRY(launch_exclusive_scan_u32(ctx, nih, ibase, nruns, tot + 1));
+            PL_TRY(launch_exclusive_scan_u32(ctx, nch, cbase, nruns, tot + 2));
             uint32_t htot[2];
-            PL_CUDA(cudaMemcpyAsync(htot, tot, sizeof htot, cudaMemcpyDeviceToHost, st));
+            PL_CUDA(cudaMemcpyAsync(htot, tot + 1, sizeof htot, cudaMemcpyDeviceToHost, st));
             PL_CUDA(cudaStreamSynchronize(st));
             const int64_t nitems = htot[0], nchunks = htot[1];
             pl->nitems = nitems;
@@ -546,10 +580,9 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
             PL_TRY(ctx_scratch(ctx, "pl_cstart", 4 * (size_t)nchunks, (void **)&cstart));
             const int jbits = bits_for(pl->item_max / pl->chunk_max);
             const int lbits = bits_for(pl->chunk_max - 1);
-            k_chunk_write<<<ceil_div(nvalid, T), T, 0, st>>>(keys, counts, runhead, tilehead, ihead,
-                                                           chead, item_id, chunk_id, pl->item_max,
-                                                           pl->chunk_max, lbits, jbits, ckey,
-                                                           cval, cstart, pl->items);
+            k_run_emit<<<ceil_div(nruns, T), T, 0, st>>>(keys, rstart, tstart, nruns, nvalid, cbase, ibase,
+                                                       pl->item_max, pl->chunk_max, lbits, jbits, ckey,
+                                                       cval, cstart, pl->items);
             PL_CUDA(cudaGetLastError());
             k_chunk_len<<<ceil_div(nchunks, T), T, 0, st>>>(cstart, nchunks, nvalid, pl->chunk_max,
                                                           jbits + 12, 6 + lbits + jbits + 12, ckey);
