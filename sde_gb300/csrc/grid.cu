@@ -309,26 +309,43 @@ __global__ void __launch_bounds__(GRID_THREADS, 1)
 }
 
 // Plan-invariant sums: LSUMWT = sum of UVWT (grd/grdh2d.f:185) and SUMWT (grd/grdh2d.f:157).
+// A visibility's UVWT sum over its 7x7 taps is W * SU * SV, SU and SV the sums of its u and v
+// tap rows (REAL, in tap order, once per row).  Each thread sums its visibilities as
+// float-float pairs (exact products by FMA, TwoSum additions: ~2^-44 relative), and the
+// partial sums meet in DOUBLE: FP64 arithmetic per visibility is the slow path on this GPU.
 constexpr int RED_T = 256;
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
 __global__ void __launch_bounds__(RED_T) k_plan_sums(const float4 *__restrict__ rec,
                                                       const float *__restrict__ cft, int64_t n,
                                                       double *partial) {
     __shared__ double sh[2][RED_T / 32];
-    double s0 = 0.0, s1 = 0.0;
+    __shared__ float rowsum[129];
+    for (int d = threadIdx.x; d < 129; d += RED_T) {
+        float t = 0.f;
+        for (int a = 0; a < NTAP; a++) t = __fadd_rn(t, cft[d * 8 + a]);
+        rowsum[d] = t;
+    }
+    __syncthreads();
+    float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
     for (int64_t p = (int64_t)blockIdx.x * RED_T + threadIdx.x; p < n; p += (int64_t)gridDim.x * RED_T) {
         const float2 wgp = reinterpret_cast<const float2 *>(rec + p)[0];
         const uint32_t g = __float_as_uint(wgp.y);
-        const float *gu = cft + taps_du(g) * 8, *gv = cft + taps_dv(g) * 8;
-        float su = 0.f, sv = 0.f;
-#pragma unroll
-        for (int a = 0; a < NTAP; a++) {
-            su += gu[a];
-            sv += gv[a];
-        }
-        const float w = wgp.x;
-        s0 += (double)w * (double)su * (double)sv;
-        s1 += (double)w;
+        const float su = rowsum[taps_du(g)], sv = rowsum[taps_dv(g)], w = wgp.x;
+        // W*SU exactly as ph + pl, then (ph + pl)*SV as th + tl
+        const float ph = __fmul_rn(w, su), pl = __fmaf_rn(w, su, -ph);
+        const float th = __fmul_rn(ph, sv);
+        const float tl = __fmaf_rn(pl, sv, __fmaf_rn(ph, sv, -th));
+        two_sum_acc(h0, l0, th);
+        l0 = __fadd_rn(l0, tl);
+        two_sum_acc(h1, l1, w);
     }
+    double s0 = (double)h0 + (double)l0, s1 = (double)h1 + (double)l1;
     for (int d = 16; d > 0; d >>= 1) {
         s0 += __shfl_down_sync(0xffffffffu, s0, d);
         s1 += __shfl_down_sync(0xffffffffu, s1, d);
