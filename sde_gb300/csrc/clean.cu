@@ -20,6 +20,7 @@
 namespace {
 
 constexpr int CL_THREADS = 512;
+constexpr size_t CL_SMEM_SLICE_MAX = 100 * 1024;  // largest RES slice kept in shared memory
 constexpr unsigned SPIN_LIMIT = 1u << 26;
 
 struct Cand {
@@ -68,7 +69,23 @@ struct Barrier {
     unsigned count;
     unsigned gen;
     int stopreq[2];  // cancel requests published by CTA 0 before each barrier
+    unsigned long long best[3];  // each iteration's maximum, as a packed key (cand_key)
 };
+
+// A candidate as a 64-bit key whose unsigned order is better()'s: |value| bits (|value| >= 0
+// and not NaN here, so the bits order as the values do), then INT32_MAX - index (the first
+// index wins a tie), then the value's sign bit.  One atomicMax per CTA finds the maximum.
+__device__ __forceinline__ unsigned long long cand_key(Cand c) {
+    return ((unsigned long long)__float_as_uint(c.a) << 32) |
+           ((unsigned long long)(uint32_t)(INT32_MAX - c.idx) << 1) | (__float_as_uint(c.v) >> 31);
+}
+__device__ __forceinline__ Cand key_cand(unsigned long long k) {
+    Cand c;
+    c.a = __uint_as_float((uint32_t)(k >> 32));
+    c.idx = INT32_MAX - (int32_t)((uint32_t)k >> 1);
+    c.v = (k & 1ull) ? -c.a : c.a;
+    return c;
+}
 
 // Grid-wide barrier; gives up after SPIN_LIMIT polls and reports through *timeout.
 __device__ bool grid_sync(Barrier *b, unsigned nblocks, int *timeout) {
@@ -118,24 +135,34 @@ struct CleanArgs {
     float *out;      // [0] maxres [1] tflux [2] ansub (as int bits)
 };
 
+// SMEM: the CTA's slice of RES lives in shared memory for all iterations (dynamic shared
+// memory of one slice) and goes to A.res once at the end; otherwise RES is read and written
+// in global memory every iteration.  The arithmetic is the same either way.
+template <bool SMEM>
 __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
+    extern __shared__ float sres[];
     const int64_t npix = (int64_t)A.nx * A.ny;
     const int64_t per = (npix + gridDim.x - 1) / gridDim.x;
     const int64_t lo = per * blockIdx.x;
     const int64_t hi = lo + per < npix ? lo + per : npix;
     const int64_t pnpix = (int64_t)A.pnx * A.pny;
+    auto R = [&](int64_t k) -> float & { return SMEM ? sres[k - lo] : A.res[k]; };
     __shared__ int stop_sh;
     // RES = DRT * BOX, and the first maximum of the slice
     Cand c{-1.0f, INT32_MAX, 0.0f};
     for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
         float r = A.box ? __fmul_rn(A.drt[k], A.box[k]) : __fmul_rn(A.drt[k], 1.0f);
-        A.res[k] = r;
+        R(k) = r;
         c = better(c, Cand{fabsf(r), (int32_t)k, r});
     }
     c = block_best(c);
-    if (threadIdx.x == 0) A.partial[blockIdx.x] = c;
+    if (threadIdx.x == 0 && c.a >= 0.0f) atomicMax(&A.bar->best[0], cand_key(c));
     if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->stopreq[0] = (A.cancel && *A.cancel) ? 1 : 0;
     if (!grid_sync(A.bar, gridDim.x, &A.status[STATUS_TIMEOUT])) return;
+    // the maxima of successive passes take best[0], best[1], best[2] in turn: a word is read
+    // after the barrier that follows its pass, and cleared by CTA 0 one pass before it is
+    // used again (after every CTA has read it, before any CTA adds to it)
+    int ph = 0;
     int cur = 0;
     float tflux = A.tflux_in;
     const int nabs = A.nsub < 0 ? -A.nsub : A.nsub;
@@ -143,11 +170,9 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
     int stopped = 0;
     float maxres = 0.0f;
     for (isub = A.bsub; isub <= nabs; isub++) {
-        // global first maximum from the partials of every CTA
-        Cand g{-1.0f, INT32_MAX, 0.0f};
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-            g = better(g, A.partial[cur * gridDim.x + b]);
-        g = block_best(g);
+        // global first maximum of the last pass
+        const Cand g = key_cand(__ldcg(&A.bar->best[ph % 3]));
+        if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->best[(ph + 2) % 3] = 0ull;
         // PIXISAMA returns 1 (index 0) when no |value| exceeds 0
         // every |value| >= 0 beats the -1 sentinel, so when nothing exceeds 0 the winner
         // is index 0 -- PIXISAMA's default of 1 (pix/pixisama.f:45)
@@ -177,30 +202,55 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
         }
         const int offx = A.pmpx + pmx, offy = A.pmpy + pmy;
         Cand lc{-1.0f, INT32_MAX, 0.0f};
-        // the window has < 2^31 pixels: 32-bit positions, the pixel's (ix, iy) stepped along
-        // with it (one division per thread, not per pixel)
-        int kk = (int)lo + (int)threadIdx.x;
-        int iy0 = kk / A.nx, ix0 = kk - iy0 * A.nx;  // 0-based
-        for (; kk < (int)hi; kk += blockDim.x) {
-            // PSF(OFFX-IX, OFFY-IY) with 1-based IX = ix0 + 1, IY = iy0 + 1
-            const int64_t flat = (int64_t)(offx - ix0 - 2) + (int64_t)(offy - iy0 - 2) * A.pnx;
-            const float p = (flat >= 0 && flat < pnpix) ? A.psf[flat] : 0.0f;
-            const float bx = A.box ? A.box[kk] : 1.0f;
-            const float r = __fsub_rn(A.res[kk], __fmul_rn(__fmul_rn(pntsub, p), bx));
-            A.res[kk] = r;
-            lc = better(lc, Cand{fabsf(r), (int32_t)kk, r});
-            ix0 += blockDim.x;
-            while (ix0 >= A.nx) {
-                ix0 -= A.nx;
-                iy0++;
+        // RES -= (PNTSUB*PSF(OFFX-IX, OFFY-IY))*BOX over the slice.  PSF is addressed as the
+        // reference's array is, by its flat index (OFFX-IX-1) + (OFFY-IY-1)*PNX (0-based IX,
+        // IY here: -2), which steps by -1 per pixel and by NX-PNX per row; when the whole
+        // window's indices lie in the PSF no per-pixel check is made.  A thread visits its
+        // pixels in increasing order, so a strictly larger |RES| is its first maximum.
+        {
+            const int nslice = (int)(hi - lo);
+            int sidx = threadIdx.x;
+            const int64_t k0 = lo + sidx;
+            int ix0 = (int)(k0 % A.nx);
+            const int iy0 = (int)(k0 / A.nx);
+            int64_t flat = (int64_t)(offx - ix0 - 2) + (int64_t)(offy - iy0 - 2) * A.pnx;
+            const int64_t fmin = (int64_t)(offx - (A.nx - 1) - 2) + (int64_t)(offy - (A.ny - 1) - 2) * A.pnx;
+            const int64_t fmax = (int64_t)(offx - 2) + (int64_t)(offy - 2) * A.pnx;
+            const bool inside = fmin >= 0 && fmax < pnpix;
+            const int step = blockDim.x;
+            const int64_t wrap = (int64_t)A.nx - A.pnx;
+            float la = -1.0f, lv = 0.0f;
+            int li = INT32_MAX;
+            for (; sidx < nslice; sidx += step) {
+                const float p = inside ? A.psf[flat] : ((flat >= 0 && flat < pnpix) ? A.psf[flat] : 0.0f);
+                float sub = __fmul_rn(pntsub, p);
+                if (A.box) sub = __fmul_rn(sub, A.box[lo + sidx]);
+                float &rs = R(lo + sidx);
+                const float r = __fsub_rn(rs, sub);
+                rs = r;
+                if (fabsf(r) > la) {
+                    la = fabsf(r);
+                    li = (int)(lo + sidx);
+                    lv = r;
+                }
+                ix0 += step;
+                flat -= step;
+                while (ix0 >= A.nx) {
+                    ix0 -= A.nx;
+                    flat += wrap;
+                }
             }
+            lc = Cand{la, li, lv};
         }
         lc = block_best(lc);
         cur ^= 1;
-        if (threadIdx.x == 0) A.partial[cur * gridDim.x + blockIdx.x] = lc;
+        if (threadIdx.x == 0 && lc.a >= 0.0f) atomicMax(&A.bar->best[(ph + 1) % 3], cand_key(lc));
         if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->stopreq[cur] = (A.cancel && *A.cancel) ? 1 : 0;
         if (!grid_sync(A.bar, gridDim.x, &A.status[STATUS_TIMEOUT])) return;
+        ph++;
     }
+    if (SMEM)
+        for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) A.res[k] = R(k);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         int ansub;
         if (!stopped) {
@@ -214,12 +264,8 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
         if (stopped) A.out[0] = maxres;
     }
     if (!stopped) {
-        // final PIXISAMA over the residual (pix/pix2drcl.f:134-138)
-        Cand g{-1.0f, INT32_MAX, 0.0f};
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-            g = better(g, A.partial[cur * gridDim.x + b]);
-        g = block_best(g);
-        if (blockIdx.x == 0 && threadIdx.x == 0) A.out[0] = g.v;
+        // final PIXISAMA over the residual (pix/pix2drcl.f:134-138): the last pass's maximum
+        if (blockIdx.x == 0 && threadIdx.x == 0) A.out[0] = key_cand(__ldcg(&A.bar->best[ph % 3])).v;
     }
 }
 
@@ -327,8 +373,10 @@ int clean_preload(sde_ctx *ctx) {
     SDE_CUDA_TRY(cudaFuncGetAttributes(&a, k_max_final));
     SDE_CUDA_TRY(cudaFuncGetAttributes(&a, k_scale_inv));
     int per_sm = 0;
-    SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom, CL_THREADS, 0));
+    SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom<false>, CL_THREADS, 0));
     ctx->hogbom_per_sm = per_sm;
+    SDE_CUDA_TRY(cudaFuncSetAttribute(k_hogbom<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)CL_SMEM_SLICE_MAX));
     return SDE_OK;
 }
 
@@ -356,7 +404,7 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
     if (pmpx >= pnx) pmpx = pnx / 2;
     if (pmpy >= pny) pmpy = pny / 2;
     int per_sm = ctx->hogbom_per_sm;
-    if (per_sm < 1) SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom, CL_THREADS, 0));
+    if (per_sm < 1) SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom<false>, CL_THREADS, 0));
     if (per_sm < 1) {
         sde_set_error("sde_hogbom: kernel cannot be resident");
         return SDE_ECUDA;
@@ -365,6 +413,15 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
     int nblocks = ctx->num_sms * (per_sm > 2 ? 2 : per_sm);
     int64_t want = (npix + 4 * CL_THREADS - 1) / (4 * CL_THREADS);  // small windows: fewer CTAs
     if (want < nblocks) nblocks = (int)(want < 1 ? 1 : want);
+    // the residual in shared memory when every CTA's slice fits there and the launch stays
+    // co-resident with it (windows up to ~2800^2 on GB300, two CTAs per SM)
+    const size_t slice = sizeof(float) * (size_t)((npix + nblocks - 1) / nblocks);
+    bool smem_res = false;
+    if (slice <= CL_SMEM_SLICE_MAX) {
+        int fit = 0;
+        SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_hogbom<true>, CL_THREADS, slice));
+        smem_res = (int64_t)fit * ctx->num_sms >= nblocks;
+    }
     Cand *partial;
     Barrier *bar;
     float *dout;
@@ -381,8 +438,12 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
     A.status = ctx->d_status; A.out = dout;
     void *args[] = {&A};
     KTimer kt(ctx, "hogbom");
-    SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom, dim3(nblocks), dim3(CL_THREADS),
-                                             args, 0, ctx->stream));
+    if (smem_res)
+        SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom<true>, dim3(nblocks), dim3(CL_THREADS),
+                                                 args, slice, ctx->stream));
+    else
+        SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom<false>, dim3(nblocks), dim3(CL_THREADS),
+                                                 args, 0, ctx->stream));
     float h[4];
     SDE_CUDA_TRY(cudaMemcpyAsync(h, dout, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     SDE_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(int) * STATUS_COUNT,
@@ -530,7 +591,7 @@ extern "C" int sde_hogbom_noalloc(void *stream, const float *drt, const float *p
     if (pmpx >= pnx) pmpx = pnx / 2;
     if (pmpy >= pny) pmpy = pny / 2;
     int per_sm = 0;
-    SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom, CL_THREADS, 0));
+    SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hogbom<false>, CL_THREADS, 0));
     if (per_sm < 1) {
         sde_set_error("sde_hogbom_noalloc: kernel cannot be resident");
         return SDE_ECUDA;
@@ -551,7 +612,7 @@ extern "C" int sde_hogbom_noalloc(void *stream, const float *drt, const float *p
     A.nsub = nsub; A.bsub = bsub; A.cancel = cancel_flag; A.partial = S->partial; A.bar = &S->bar;
     A.status = S->status; A.out = S->out;
     void *args[] = {&A};
-    SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom, dim3(nblocks), dim3(CL_THREADS),
+    SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom<false>, dim3(nblocks), dim3(CL_THREADS),
                                              args, 0, st));
     float h[4];
     int hs[STATUS_COUNT];
