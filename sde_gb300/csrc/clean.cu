@@ -66,8 +66,7 @@ __device__ Cand block_best(Cand c) {
 }
 
 struct Barrier {
-    unsigned count;
-    unsigned gen;
+    unsigned count;  // arrivals since the launch (grid_sync)
     int stopreq[2];  // cancel requests published by CTA 0 before each barrier
     unsigned long long best[3];  // each iteration's maximum, as a packed key (cand_key)
 };
@@ -87,23 +86,22 @@ __device__ __forceinline__ Cand key_cand(unsigned long long k) {
     return c;
 }
 
-// Grid-wide barrier; gives up after SPIN_LIMIT polls and reports through *timeout.
-__device__ bool grid_sync(Barrier *b, unsigned nblocks, int *timeout) {
+// Grid-wide barrier on a monotonic arrival count: barrier number `epoch` (0, 1, ...) is passed
+// when the count reaches (epoch + 1) * nblocks, so the last CTA's arrival releases the others
+// (no reset, no second word) and that CTA does not wait.  Gives up after SPIN_LIMIT polls and
+// reports through *timeout.  The count is cleared before each launch.
+__device__ bool grid_sync(Barrier *b, unsigned nblocks, unsigned epoch, int *timeout) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         ok = 1;
-        volatile unsigned *vgen = &b->gen;
-        const unsigned g = *vgen;
+        const unsigned target = (epoch + 1u) * nblocks;
         __threadfence();
-        const unsigned arrived = atomicAdd(&b->count, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(&b->count, 0u);
-            __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
+        const unsigned arrived = atomicAdd(&b->count, 1u) + 1u;
+        if ((int)(arrived - target) < 0) {
+            volatile unsigned *vc = &b->count;
             unsigned spins = 0;
-            while (*vgen == g) {
+            while ((int)(*vc - target) < 0) {
                 if (++spins > SPIN_LIMIT) {
                     atomicExch(timeout, 1);
                     ok = 0;
@@ -158,7 +156,8 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
     c = block_best(c);
     if (threadIdx.x == 0 && c.a >= 0.0f) atomicMax(&A.bar->best[0], cand_key(c));
     if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->stopreq[0] = (A.cancel && *A.cancel) ? 1 : 0;
-    if (!grid_sync(A.bar, gridDim.x, &A.status[STATUS_TIMEOUT])) return;
+    unsigned epoch = 0;
+    if (!grid_sync(A.bar, gridDim.x, epoch++, &A.status[STATUS_TIMEOUT])) return;
     // the maxima of successive passes take best[0], best[1], best[2] in turn: a word is read
     // after the barrier that follows its pass, and cleared by CTA 0 one pass before it is
     // used again (after every CTA has read it, before any CTA adds to it)
@@ -246,7 +245,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
         cur ^= 1;
         if (threadIdx.x == 0 && lc.a >= 0.0f) atomicMax(&A.bar->best[(ph + 1) % 3], cand_key(lc));
         if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->stopreq[cur] = (A.cancel && *A.cancel) ? 1 : 0;
-        if (!grid_sync(A.bar, gridDim.x, &A.status[STATUS_TIMEOUT])) return;
+        if (!grid_sync(A.bar, gridDim.x, epoch++, &A.status[STATUS_TIMEOUT])) return;
         ph++;
     }
     if (SMEM)
