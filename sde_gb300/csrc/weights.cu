@@ -83,25 +83,44 @@ __global__ void k_wkey(WParams p, const float *__restrict__ wt, const float *__r
 }
 
 // GWT(cell) = ((0 + w1) + w2) + ... in visibility order: FP32 additions in the reference's
-// order, so every cell's sum is one sequential chain.  One thread per run head sums a run of
-// at most SEG_SHORT entries; a longer run (dense cells hold up to ~2e5 visibilities) is put
-// on a list for k_segsum_long, where a warp streams it through registers.
+// order, so every cell's sum is one sequential chain.  A block stages SEG_TILE sorted entries
+// (plus the one before and SEG_SHORT after) in shared memory; one thread per run head sums a
+// run of at most SEG_SHORT entries from there; a longer run (dense cells hold up to ~2e5
+// visibilities) is put on a list for k_segsum_long, where a warp streams it.
 constexpr int SEG_SHORT = 32;
-__global__ void k_segsum(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-                         unsigned long long *counts, float *gwt, uint32_t *longq) {
-    int64_t nvalid = (int64_t)counts[0];
-    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nvalid) return;
-    uint32_t k = keys[p];
-    if (p > 0 && keys[p - 1] == k) return;
-    if (p + SEG_SHORT < nvalid && keys[p + SEG_SHORT] == k) {
-        const unsigned long long slot = atomicAdd(&counts[2], 1ull);
-        longq[slot] = (uint32_t)p;
-        return;
+constexpr int SEG_TILE = 2048;
+constexpr int SEG_T = 256;
+__global__ void __launch_bounds__(SEG_T) k_segsum(const uint32_t *__restrict__ keys,
+                                                  const uint32_t *__restrict__ vals,
+                                                  unsigned long long *counts, float *gwt, uint32_t *longq) {
+    __shared__ uint32_t sk[SEG_TILE + SEG_SHORT + 1];  // keys[base - 1 ...]
+    __shared__ float sv[SEG_TILE + SEG_SHORT];          // vals[base ...]
+    const int64_t nvalid = (int64_t)counts[0];
+    const int64_t base = (int64_t)blockIdx.x * SEG_TILE;
+    if (base >= nvalid) return;
+    for (int i = threadIdx.x; i < SEG_TILE + SEG_SHORT + 1; i += SEG_T) {
+        const int64_t q = base - 1 + i;
+        sk[i] = q >= 0 && q < nvalid ? keys[q] : KEY_INVALID;  // valid keys are below KEY_INVALID
     }
-    float s = 0.0f;
-    for (int64_t q = p; q < nvalid && keys[q] == k; q++) s = __fadd_rn(s, __uint_as_float(vals[q]));
-    gwt[k] = s;
+    for (int i = threadIdx.x; i < SEG_TILE + SEG_SHORT; i += SEG_T) {
+        const int64_t q = base + i;
+        sv[i] = q < nvalid ? __uint_as_float(vals[q]) : 0.0f;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < SEG_TILE; j += SEG_T) {
+        const int64_t p = base + j;
+        if (p >= nvalid) break;
+        const uint32_t k = sk[j + 1];
+        if (sk[j] == k) continue;  // not the first entry of its run
+        if (sk[j + 1 + SEG_SHORT] == k) {
+            const unsigned long long slot = atomicAdd(&counts[2], 1ull);
+            longq[slot] = (uint32_t)p;
+            continue;
+        }
+        float s = 0.0f;
+        for (int q = j; sk[q + 1] == k; q++) s = __fadd_rn(s, sv[q]);
+        gwt[k] = s;
+    }
 }
 
 // One warp per long run.  Lane 0 finds the run's end (galloping then binary search over the
@@ -112,15 +131,19 @@ constexpr int SEG_BLK = 256;
 constexpr int SEG_WARPS = 8;  // warps per block of k_segsum_long
 __global__ void __launch_bounds__(SEG_WARPS * 32) k_segsum_long(
     const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-    const unsigned long long *counts, const uint32_t *__restrict__ longq, float *gwt) {
+    unsigned long long *counts, const uint32_t *__restrict__ longq, float *gwt) {
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ __align__(16) float buf[SEG_WARPS][2][SEG_BLK];
     const int64_t nvalid = (int64_t)counts[0];
     const int64_t nlong = (int64_t)counts[2];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t r = warp; r < nlong; r += nwarps) {
+    // runs are taken from a counter, so the warp that holds the longest run (the bound of
+    // this kernel: one sequential FP32 chain) takes no other
+    for (;;) {
+        int64_t r = 0;
+        if (lane == 0) r = (int64_t)atomicAdd(&counts[3], 1ull);
+        r = __shfl_sync(FULL, r, 0);
+        if (r >= nlong) break;
         const int64_t p = longq[r];
         const uint32_t k = keys[p];
         int64_t end = 0;
@@ -350,7 +373,7 @@ int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const 
         uint32_t *longq;
         SDE_TRY(ctx_scratch(ctx, "w_longq", sizeof(uint32_t) * (size_t)(nvis / (SEG_SHORT + 1) + 1),
                             (void **)&longq));
-        k_segsum<<<ceil_div(nvis, T), T, 0, st>>>(keys, vals, counts, gwt, longq);
+        k_segsum<<<ceil_div(nvis, SEG_TILE), SEG_T, 0, st>>>(keys, vals, counts, gwt, longq);
         SDE_CHECK_LAUNCH();
         k_segsum_long<<<ctx->num_sms * 4, SEG_WARPS * 32, 0, st>>>(keys, vals, counts, longq, gwt);
         SDE_CHECK_LAUNCH();
