@@ -21,6 +21,7 @@ namespace {
 
 constexpr int CL_THREADS = 512;
 constexpr size_t CL_SMEM_SLICE_MAX = 100 * 1024;  // largest RES slice kept in shared memory
+constexpr int CL_BATCH = 4;                        // pixels per thread with PSF loads in flight
 constexpr unsigned SPIN_LIMIT = 1u << 26;
 
 struct Cand {
@@ -220,23 +221,37 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
             const int64_t wrap = (int64_t)A.nx - A.pnx;
             float la = -1.0f, lv = 0.0f;
             int li = INT32_MAX;
-            for (; sidx < nslice; sidx += step) {
-                const float p = inside ? A.psf[flat] : ((flat >= 0 && flat < pnpix) ? A.psf[flat] : 0.0f);
-                float sub = __fmul_rn(pntsub, p);
-                if (A.box) sub = __fmul_rn(sub, A.box[lo + sidx]);
-                float &rs = R(lo + sidx);
-                const float r = __fsub_rn(rs, sub);
-                rs = r;
-                if (fabsf(r) > la) {
-                    la = fabsf(r);
-                    li = (int)(lo + sidx);
-                    lv = r;
+            // CL_BATCH pixels at a time: their PSF and RES loads are issued before any is used
+            for (; sidx < nslice; sidx += CL_BATCH * step) {
+                float p[CL_BATCH], r0[CL_BATCH];
+#pragma unroll
+                for (int j = 0; j < CL_BATCH; j++) {
+                    const bool in = sidx + j * step < nslice;
+                    p[j] = !in ? 0.0f
+                               : inside ? A.psf[flat]
+                                        : ((flat >= 0 && flat < pnpix) ? A.psf[flat] : 0.0f);
+                    r0[j] = in ? R(lo + sidx + j * step) : 0.0f;
+                    ix0 += step;
+                    flat -= step;
+                    while (ix0 >= A.nx) {
+                        ix0 -= A.nx;
+                        flat += wrap;
+                    }
                 }
-                ix0 += step;
-                flat -= step;
-                while (ix0 >= A.nx) {
-                    ix0 -= A.nx;
-                    flat += wrap;
+#pragma unroll
+                for (int j = 0; j < CL_BATCH; j++) {
+                    const int sj = sidx + j * step;
+                    if (sj < nslice) {
+                        float sub = __fmul_rn(pntsub, p[j]);
+                        if (A.box) sub = __fmul_rn(sub, A.box[lo + sj]);
+                        const float r = __fsub_rn(r0[j], sub);
+                        R(lo + sj) = r;
+                        if (fabsf(r) > la) {
+                            la = fabsf(r);
+                            li = (int)(lo + sj);
+                            lv = r;
+                        }
+                    }
                 }
             }
             lc = Cand{la, li, lv};
