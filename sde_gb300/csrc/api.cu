@@ -102,6 +102,17 @@ void ctx_free(sde_ctx *ctx, void *p, size_t bytes) {
     if (p) cudaFreeAsync(p, ctx->stream);
 }
 
+int ctx_read_small(sde_ctx *ctx, cudaStream_t st, void *dst, const void *src, size_t bytes) {
+    if (bytes > H_SMALL_BYTES) {
+        sde_set_error("ctx_read_small: %zu bytes", bytes);
+        return SDE_EINVAL;
+    }
+    SDE_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, src, bytes, cudaMemcpyDeviceToHost, st));
+    SDE_CUDA_TRY(cudaStreamSynchronize(st));
+    memcpy(dst, ctx->h_small, bytes);
+    return SDE_OK;
+}
+
 int ctx_scratch(sde_ctx *ctx, const char *name, size_t bytes, void **out) {
     DevBuf &b = ctx->scratch[name];
     if (b.bytes < bytes) {
@@ -184,7 +195,8 @@ extern "C" int sde_ctx_create(sde_ctx **out, int device) {
         sde_ctx_destroy(c);
         return rc;
     }
-    if (cudaMallocHost((void **)&c->h_status, sizeof(int) * STATUS_COUNT) != cudaSuccess) {
+    if (cudaMallocHost((void **)&c->h_status, sizeof(int) * STATUS_COUNT) != cudaSuccess ||
+        cudaMallocHost((void **)&c->h_small, H_SMALL_BYTES) != cudaSuccess) {
         sde_ctx_destroy(c);
         return SDE_ENOMEM;
     }
@@ -216,6 +228,7 @@ extern "C" int sde_ctx_destroy(sde_ctx *c) {
     ctx_free(c, c->d_cft, 0);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->h_small) cudaFreeHost(c->h_small);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return SDE_OK;

@@ -130,6 +130,9 @@ struct sde_ctx {
     float *d_cft = nullptr;                // transposed table [129][8]
     int *d_status = nullptr;               // device status words (see STATUS_*)
     int *h_status = nullptr;               // pinned mirror
+    // pinned bytes for the small device-to-host reads (counts, sums): a copy into pageable
+    // memory goes through the driver's staging shared by every stream of the process
+    unsigned char *h_small = nullptr;
     std::unordered_map<std::string, DevBuf> scratch;
     std::unordered_map<int, float2 *> twiddles;  // N -> exp(+-2 pi i k/N) table
     CUtensorMap *h_tmap = nullptr;
@@ -173,6 +176,10 @@ enum { STATUS_ERR = 0, STATUS_NOWEIGHT = 1, STATUS_TIMEOUT = 2, STATUS_COUNT = 8
 
 // scratch buffer by name, grown on demand (contents undefined)
 int ctx_scratch(sde_ctx *ctx, const char *name, size_t bytes, void **out);
+constexpr size_t H_SMALL_BYTES = 256;
+// Reads `bytes` (<= H_SMALL_BYTES) from device memory after the work queued on st, through the
+// context's pinned buffer; waits for st.
+int ctx_read_small(sde_ctx *ctx, cudaStream_t st, void *dst, const void *src, size_t bytes);
 int ctx_alloc(sde_ctx *ctx, void **p, size_t bytes);
 void ctx_free(sde_ctx *ctx, void *p, size_t bytes);
 int ctx_twiddles(sde_ctx *ctx, int n, const float2 **out);

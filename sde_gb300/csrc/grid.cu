@@ -957,8 +957,7 @@ int plan_sums(sde_plan *pl, double *lsumwt, double *sumwt) {
     k_sum_pairs<<<1, RED_T, 0, ctx->stream>>>(part, nb, pl->d_sums);
     SDE_CHECK_LAUNCH();
     double h[2];
-    SDE_CUDA_TRY(cudaMemcpyAsync(h, pl->d_sums, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
-    SDE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    SDE_TRY(ctx_read_small(ctx, ctx->stream, h, pl->d_sums, sizeof h));
     *lsumwt = h[0];
     *sumwt = h[1];
     return SDE_OK;

@@ -70,8 +70,11 @@ extern "C" int sde_uvmap(sde_ctx *ctx, const sde_uvmap_args *a, int64_t nvis, co
         if (e == cudaSuccess && psf)
             e = cudaMemcpyAsync(psf, dpsf, sizeof(float) * (size_t)npix,
                                 a->out_where == SDE_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&r.psf_peak, peak, sizeof(float), cudaMemcpyDeviceToHost, st);
+        // the peak through the context's pinned bytes (a pageable read would go through the
+        // driver's staging, shared with the other slots' streams)
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small, peak, sizeof(float), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) memcpy(&r.psf_peak, ctx->h_small, sizeof(float));
         if (e != cudaSuccess) {
             sde_set_error("sde_uvmap: %s", cudaGetErrorString(e));
             rc = SDE_ECUDA;

@@ -163,11 +163,11 @@ __global__ void k_exc_write(GParams p, const float *__restrict__ u, const float 
 // tile's first one; a run's part within one item (a piece) splits into chunks of chunk_max
 // from the piece's start.  Chunks and items are numbered in position order.
 __global__ void k_run_heads(const uint32_t *__restrict__ keys, const unsigned long long *counts,
-                            uint32_t *head) {
+                            int64_t n, uint32_t *head) {
     const int64_t nv = (int64_t)counts[0];
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nv) return;
-    head[q] = q == 0 || (keys[q - 1] >> 1) != (keys[q] >> 1);
+    if (q >= n) return;
+    head[q] = q < nv && (q == 0 || (keys[q - 1] >> 1) != (keys[q] >> 1));
 }
 
 __global__ void k_run_compact(const uint32_t *__restrict__ head, const uint32_t *__restrict__ ridx,
@@ -502,9 +502,26 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
             goto fail;
         }
         if (nvis > 0) PL_TRY(launch_radix_sort_u32(ctx, keys, vals, nvis, kbits, ktmp, vtmp));
+        // run heads of the sorted keys (0 past the gridded visibilities) and their count, read
+        // back with the visibility counts: one wait for both
+        uint32_t *head, *ridx, *tot;
+        PL_TRY(ctx_scratch(ctx, "pl_runhead", 4 * n, (void **)&head));
+        PL_TRY(ctx_scratch(ctx, "pl_runidx", 4 * n, (void **)&ridx));
+        PL_TRY(ctx_scratch(ctx, "pl_tot", 16, (void **)&tot));
+        if (nvis > 0) {
+            k_run_heads<<<ceil_div(nvis, T), T, 0, st>>>(keys, counts, nvis, head);
+            PL_CUDA(cudaGetLastError());
+            PL_TRY(launch_exclusive_scan_u32(ctx, head, ridx, nvis, tot));
+        } else {
+            PL_CUDA(cudaMemsetAsync(tot, 0, 16, st));
+        }
         unsigned long long hc[3] = {0, 0, 0};
-        PL_CUDA(cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, st));
+        uint32_t hruns = 0;
+        PL_CUDA(cudaMemcpyAsync(ctx->h_small, counts, sizeof hc, cudaMemcpyDeviceToHost, st));
+        PL_CUDA(cudaMemcpyAsync(ctx->h_small + sizeof hc, tot, sizeof hruns, cudaMemcpyDeviceToHost, st));
         PL_CUDA(cudaStreamSynchronize(st));
+        memcpy(hc, ctx->h_small, sizeof hc);
+        memcpy(&hruns, ctx->h_small + sizeof hc, sizeof hruns);
         const int64_t nvalid = (int64_t)hc[0], nexc = (int64_t)hc[1];
         pl->nuntouched = nvis - (int64_t)hc[2];
         pl->nvis = nvalid;
@@ -534,16 +551,6 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         }
         // runs, chunks, work items
         if (nvalid > 0) {
-            uint32_t *head, *ridx, *tot;
-            PL_TRY(ctx_scratch(ctx, "pl_runhead", 4 * nv1, (void **)&head));
-            PL_TRY(ctx_scratch(ctx, "pl_runidx", 4 * nv1, (void **)&ridx));
-            PL_TRY(ctx_scratch(ctx, "pl_tot", 16, (void **)&tot));
-            k_run_heads<<<ceil_div(nvalid, T), T, 0, st>>>(keys, counts, head);
-            PL_CUDA(cudaGetLastError());
-            PL_TRY(launch_exclusive_scan_u32(ctx, head, ridx, nvalid, tot));
-            uint32_t hruns = 0;
-            PL_CUDA(cudaMemcpyAsync(&hruns, tot, sizeof hruns, cudaMemcpyDeviceToHost, st));
-            PL_CUDA(cudaStreamSynchronize(st));
             const int64_t nruns = hruns;
             uint32_t *rstart, *nch, *nih, *cbase, *ibase;
             int32_t *tstart;
@@ -564,8 +571,7 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
             PL_TRY(launch_exclusive_scan_u32(ctx, nih, ibase, nruns, tot + 1));
             PL_TRY(launch_exclusive_scan_u32(ctx, nch, cbase, nruns, tot + 2));
             uint32_t htot[2];
-            PL_CUDA(cudaMemcpyAsync(htot, tot + 1, sizeof htot, cudaMemcpyDeviceToHost, st));
-            PL_CUDA(cudaStreamSynchronize(st));
+            PL_TRY(ctx_read_small(ctx, st, htot, tot + 1, sizeof htot));
             const int64_t nitems = htot[0], nchunks = htot[1];
             pl->nitems = nitems;
             pl->nchunks = nchunks;

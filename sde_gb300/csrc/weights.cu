@@ -405,9 +405,12 @@ int sde_weights(sde_ctx *ctx, int rmode, const float robust[3], float ds, const 
             k_sum_partials<<<1, RED_THREADS, 0, st>>>(part, nbc, sums + 1);
             SDE_CHECK_LAUNCH();
         }
-        SDE_CUDA_TRY(cudaMemcpyAsync(hs, sums, sizeof hs, cudaMemcpyDeviceToHost, st));
-        SDE_CUDA_TRY(cudaMemcpyAsync(hcounts, counts, sizeof hcounts, cudaMemcpyDeviceToHost, st));
+        // both through the context's pinned bytes (one wait)
+        SDE_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, sums, sizeof hs, cudaMemcpyDeviceToHost, st));
+        SDE_CUDA_TRY(cudaMemcpyAsync(ctx->h_small + sizeof hs, counts, sizeof hcounts, cudaMemcpyDeviceToHost, st));
         SDE_CUDA_TRY(cudaStreamSynchronize(st));
+        memcpy(hs, ctx->h_small, sizeof hs);
+        memcpy(hcounts, ctx->h_small + sizeof hs, sizeof hcounts);
     }
     // robust parameters on the host, with the reference's REAL/DOUBLE mix (grd/grdruw2d.f:106-193)
     float rob = robust ? robust[0] : 0.0f;
