@@ -16,16 +16,10 @@ NGROUPS = 300
 
 
 def reference_root():
-    """The reference tree: $SDE_REFERENCE, else the benchmark's reference_path (None if
-    neither names an existing directory)."""
-    import json
-    root = os.environ.get("SDE_REFERENCE")
-    if not root:
-        try:
-            root = json.load(open(os.path.join(HERE, "..", "..", "BASELINE.json")))["reference_path"]
-        except (OSError, ValueError, KeyError):
-            root = None
-    return root if root and os.path.isdir(root) else None
+    """The reference tree: $SDE_REFERENCE, else /root/reference (None if that is not an
+    existing directory)."""
+    root = os.environ.get("SDE_REFERENCE") or "/root/reference"
+    return root if os.path.isdir(root) else None
 
 def main(reqdata):
     raw = open(os.path.join(reqdata, "3C10UV.FTS"), "rb").read()

@@ -23,15 +23,9 @@ HEAD = os.path.join(HERE, "golden", "3c10uv_head.fts")
 
 
 def _reference_uv():
-    """reqdata/3C10UV.FTS of the reference tree named by $SDE_REFERENCE or the benchmark's
-    reference_path ("" when absent: the test that reads it is skipped)."""
-    import json
-    root = os.environ.get("SDE_REFERENCE")
-    if not root:
-        try:
-            root = json.load(open(os.path.join(HERE, "..", "BASELINE.json")))["reference_path"]
-        except (OSError, ValueError, KeyError):
-            return ""
+    """reqdata/3C10UV.FTS of the reference tree named by $SDE_REFERENCE, else /root/reference
+    (a path that does not exist skips the test that reads it)."""
+    root = os.environ.get("SDE_REFERENCE") or "/root/reference"
     return os.path.join(root, "reqdata", "3C10UV.FTS")
 
 
