@@ -409,7 +409,7 @@ int sde_clark(sde_ctx *ctx, const float *dirty, const float *psf, int n, const f
  * module loading, at the first call on that GPU) and keeps it until the process exits, so
  * make the first call at start-up, before an arena has taken all device memory.  The first
  * call on a device, and the first after the caller resets it, also takes that array's
- * address (cudaGetSymbolAddress), so make it before any stream capture.  Every call shares
+ * address (cudaGetSymbolAddress).  Every call shares
  * the array and the call clears what must start at zero; calls that overlap on the GPU (two
  * streams, two host threads) race on it and must be serialised by the caller.  Windows or
  * PSFs over 2^31-1 pixels are rejected with SDE_EINVAL. */
