@@ -109,27 +109,39 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
     }
 }
 
-// Gather the per-visibility data into sorted order (one 32-byte sector read per
-// visibility).  An exception that also grids learns its sorted position here.
-__global__ void k_plan_gather(const uint32_t *__restrict__ perm, const unsigned long long *counts,
-                              const PlanRecU *__restrict__ rec_u, const uint32_t *__restrict__ exc_slot,
-                              float2 *fobs, float4 *rec, float *wt, uint32_t *gdd, uint32_t *orig,
-                              float2 *rot, uint8_t *gconj, DegridExc *exc) {
-    int64_t nv = (int64_t)counts[0];
-    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nv) return;
-    uint32_t i = perm[p];
-    const PlanRecU pr = rec_u[i];
-    const float4 r = pr.rec;
-    const uint32_t d = pr.gdd;
-    rec[p] = r;
-    fobs[p] = make_float2(r.z, r.w);
-    wt[p] = r.x;
-    gdd[p] = d & ~GDD_GCONJ_U;
-    orig[p] = i;
-    gconj[p] = (d & GDD_GCONJ_U) ? 1 : 0;
-    if (rot) rot[p] = make_float2(pr.rc, pr.rs);
-    if ((d & GDD_EXCEPTION) && exc) exc[exc_slot[i]].pos = (int32_t)p;
+// Gather the per-visibility data into the plan's order (one 32-byte sector read per
+// visibility), one warp per chunk: chunk c's visibilities, at [st, st + length) in the sort's
+// order, go to [cpos[c], cpos[c] + length) -- the chunk order, the order the kernels take
+// them -- and the chunk's start moves there.  An exception that also grids learns its
+// position here.
+__global__ void __launch_bounds__(256) k_plan_gather(const uint32_t *__restrict__ perm,
+                                                     const uint32_t *__restrict__ cpos, int64_t nchunks,
+                                                     uint2 *chunks, const PlanRecU *__restrict__ rec_u,
+                                                     const uint32_t *__restrict__ exc_slot, float2 *fobs,
+                                                     float4 *rec, float *wt, uint32_t *gdd, uint32_t *orig,
+                                                     float2 *rot, uint8_t *gconj, DegridExc *exc) {
+    const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (c >= nchunks) return;
+    const uint2 ch = chunks[c];
+    const uint32_t st = ch.x, len = ch.y >> 16, to = cpos[c];
+    for (uint32_t k = lane; k < len; k += 32) {
+        const uint32_t i = perm[st + k];
+        const int64_t p = (int64_t)to + k;
+        const PlanRecU pr = rec_u[i];
+        const float4 r = pr.rec;
+        const uint32_t d = pr.gdd;
+        rec[p] = r;
+        fobs[p] = make_float2(r.z, r.w);
+        wt[p] = r.x;
+        gdd[p] = d & ~GDD_GCONJ_U;
+        orig[p] = i;
+        gconj[p] = (d & GDD_GCONJ_U) ? 1 : 0;
+        if (rot) rot[p] = make_float2(pr.rc, pr.rs);
+        if ((d & GDD_EXCEPTION) && exc) exc[exc_slot[i]].pos = (int32_t)p;
+    }
+    __syncwarp();  // every lane has read the chunk record
+    if (lane == 0) chunks[c] = make_uint2(to, ch.y);
 }
 
 // (pos is set by k_plan_gather for the exceptions that also grid)
@@ -276,21 +288,6 @@ __global__ void k_chunk_final(const uint64_t *__restrict__ ckey, const uint32_t 
     uint32_t it = (uint32_t)(ckey[c] >> shift_item);
     if (c == 0 || (uint32_t)(ckey[c - 1] >> shift_item) != it) items[it].cbeg = (int32_t)c;
     if (c == nchunks - 1 || (uint32_t)(ckey[c + 1] >> shift_item) != it) items[it].cend = (int32_t)(c + 1);
-}
-
-// The plan stores its visibilities in chunk order: chunk c's visibilities at
-// [cpos[c], cpos[c] + length), the chunks in the order the kernels take them, so that a team
-// reads the visibilities of the chunks it takes together from one contiguous range.  src[]
-// receives the caller index of every plan position (the sort's permutation through the
-// chunk order); chunk starts move to their new positions.
-__global__ void k_chunk_relocate(const uint32_t *__restrict__ perm, const uint32_t *__restrict__ cpos,
-                                 int64_t nchunks, uint2 *chunks, uint32_t *src) {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nchunks) return;
-    const uint2 ch = chunks[c];
-    const uint32_t st = ch.x, len = ch.y >> 16, to = cpos[c];
-    for (uint32_t k = 0; k < len; k++) src[to + k] = perm[st + k];
-    chunks[c] = make_uint2(to, ch.y);
 }
 
 // a work item's first visibility: its first chunk's (new) start
@@ -603,15 +600,12 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
                                                             nvalid, shift_item, pl->chunks, clen,
                                                             pl->items);
             PL_CUDA(cudaGetLastError());
-            // chunk order: the sort's permutation through the chunks (into the sort's
-            // value scratch, free now), then one gather of the caller-order sectors
+            // chunk order: each chunk's new start, then one gather of the caller-order sectors
             PL_TRY(launch_exclusive_scan_u32(ctx, clen, cpos, nchunks, nullptr));
-            k_chunk_relocate<<<ceil_div(nchunks, T), T, 0, st>>>(vals, cpos, nchunks, pl->chunks, vtmp);
-            PL_CUDA(cudaGetLastError());
-            k_plan_gather<<<ceil_div(nvalid, T), T, 0, st>>>(vtmp, counts, rec_u, slot,
-                                                           pl->fobs, pl->rec, pl->wt, pl->gdd,
-                                                           pl->orig, pl->rot, pl->gconj,
-                                                           nexc > 0 ? pl->exc : nullptr);
+            k_plan_gather<<<ceil_div(nchunks, T / 32), T, 0, st>>>(vals, cpos, nchunks, pl->chunks, rec_u, slot,
+                                                                 pl->fobs, pl->rec, pl->wt, pl->gdd,
+                                                                 pl->orig, pl->rot, pl->gconj,
+                                                                 nexc > 0 ? pl->exc : nullptr);
             PL_CUDA(cudaGetLastError());
             k_item_vbeg<<<ceil_div(nitems, T), T, 0, st>>>(pl->chunks, nitems, pl->items);
             PL_CUDA(cudaGetLastError());
