@@ -513,6 +513,86 @@ __attribute__((weak)) void msgput_(const char *msg, const char *type, size_t lms
 static std::mutex g_shim_mu;
 static sde_ctx *g_shim_ctx = nullptr;
 
+// Copies between the drop-ins' caller arrays and the device.  SDE's arrays are ordinary
+// pageable memory, which cudaMemcpyAsync stages through the driver's buffers (14 GB/s on
+// first touch, ~190 GB/s at best, measured on GB300).  Where the device reads and writes
+// pageable host memory directly (cudaDevAttrPageableMemoryAccess), a copy kernel moves large
+// pageable arrays at the link's rate (~200 GB/s) on a few SMs; pinned and device memory, small
+// copies and unaligned ones go to the CUDA copy as before.  Either way the copy is ordered on
+// the given stream, and every drop-in waits for its stream before it returns, so the caller's
+// array is only touched during the call.
+static constexpr size_t SHIM_KCOPY_MIN = 256 * 1024;
+static constexpr int SHIM_KCOPY_CTAS = 32;
+
+__global__ void __launch_bounds__(512) k_copy16(uint4 *__restrict__ dst, const uint4 *__restrict__ src, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n; i += stride) dst[i] = src[i];
+}
+
+__global__ void __launch_bounds__(512) k_copy4_2d(char *__restrict__ dst, size_t dpitch,
+                                                  const char *__restrict__ src, size_t spitch,
+                                                  int64_t words, int64_t rows) {
+    for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        uint32_t *d = reinterpret_cast<uint32_t *>(dst + r * dpitch);
+        const uint32_t *sr = reinterpret_cast<const uint32_t *>(src + r * spitch);
+        for (int64_t w = threadIdx.x; w < words; w += blockDim.x) d[w] = sr[w];
+    }
+}
+
+static bool shim_pageable_direct(const void *host) {
+    static int access[64];
+    static bool known[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (!known[dev]) {
+        int a = 0;
+        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) a = 0;
+        access[dev] = a;
+        known[dev] = true;
+    }
+    if (!access[dev]) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeUnregistered;
+}
+
+static cudaError_t shim_memcpy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+    const bool h2d = kind == cudaMemcpyHostToDevice, d2h = kind == cudaMemcpyDeviceToHost;
+    if (bytes >= SHIM_KCOPY_MIN && (h2d || d2h) && bytes % 16 == 0 &&
+        (reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) % 16 == 0 &&
+        shim_pageable_direct(h2d ? src : dst)) {
+        k_copy16<<<SHIM_KCOPY_CTAS, 512, 0, st>>>(static_cast<uint4 *>(dst), static_cast<const uint4 *>(src),
+                                                  (int64_t)(bytes / 16));
+        return cudaGetLastError();
+    }
+    return cudaMemcpyAsync(dst, src, bytes, kind, st);
+}
+
+static cudaError_t shim_memcpy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                                 size_t rows, cudaMemcpyKind kind, cudaStream_t st) {
+    const bool h2d = kind == cudaMemcpyHostToDevice, d2h = kind == cudaMemcpyDeviceToHost;
+    if (width * rows >= SHIM_KCOPY_MIN && (h2d || d2h) && width % 4 == 0 && dpitch % 4 == 0 &&
+        spitch % 4 == 0 && (reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) % 4 == 0 &&
+        shim_pageable_direct(h2d ? src : dst)) {
+        k_copy4_2d<<<SHIM_KCOPY_CTAS * 4, 512, 0, st>>>(static_cast<char *>(dst), dpitch,
+                                                        static_cast<const char *>(src), spitch,
+                                                        (int64_t)(width / 4), (int64_t)rows);
+        return cudaGetLastError();
+    }
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, kind, st);
+}
+
 // The drop-ins' context: on device SDE_DEVICE if set, else on the calling thread's current
 // device (0 unless the caller chose another), created by the first drop-in call.
 static sde_ctx *shim_ctx() {
@@ -547,7 +627,7 @@ static int fstr_eq(const char *s, size_t len, const char *lit) {
 
 // upload the caller's 'SF'-style table into the plan (1+2*(SUPP+1)*OSAMP values)
 static int plan_use_table(sde_plan *pl, const float *cf) {
-    SDE_CUDA_TRY(cudaMemcpyAsync(pl->cf, cf, sizeof(float) * (2 * (SUPP + 1) * OSAMP + 1),
+    SDE_CUDA_TRY(shim_memcpy(pl->cf, cf, sizeof(float) * (2 * (SUPP + 1) * OSAMP + 1),
                                  cudaMemcpyHostToDevice, pl->ctx->stream));
     return plan_build_cft(pl);
 }
@@ -734,7 +814,7 @@ static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const floa
     const bool cached = g_pc.pl && g_pc.nvis == n && g_pc.cf_hash == h &&
                         memcmp(&g_pc.spec, &sp, sizeof sp) == 0;
     SDE_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
-    if (n > 0 && vis) SDE_CUDA_TRY(cudaMemcpyAsync(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
+    if (n > 0 && vis) SDE_CUDA_TRY(shim_memcpy(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
     // the copy stream follows everything queued so far (scratch allocations, earlier users
     // of the buffers, the visibilities' copy)
     SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[0], st));
@@ -742,11 +822,11 @@ static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const floa
     if (n > 0 && vis && cached) SDE_TRY(sde_plan_set_vis(g_pc.pl, dvis, SDE_DEVICE));  // speculative
     const float *src[4] = {u, v, w, wt};
     for (int k = 0; k < 4 && n > 0; k++) {
-        SDE_CUDA_TRY(cudaMemcpyAsync(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
+        SDE_CUDA_TRY(shim_memcpy(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
         SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[1 + k], cs));
     }
     if (extra)
-        SDE_CUDA_TRY(cudaMemcpy2DAsync(extra->dst, extra->dpitch, extra->src, extra->spitch,
+        SDE_CUDA_TRY(shim_memcpy2d(extra->dst, extra->dpitch, extra->src, extra->spitch,
                                        extra->width, extra->rows, cudaMemcpyHostToDevice, cs));
     SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[5], cs));
     if (cached) {
@@ -761,7 +841,7 @@ static int shim_plan(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, const floa
     SDE_CUDA_TRY(cudaStreamWaitEvent(st, g_ss.ev[5], 0));
     if (cached) {
         int hf = 1;
-        SDE_CUDA_TRY(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SDE_CUDA_TRY(shim_memcpy(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
         SDE_CUDA_TRY(cudaStreamSynchronize(st));
         if (!hf) {
             g_pc.hits++;
@@ -791,7 +871,7 @@ static int shim_plan_build(sde_ctx *ctx, const sde_gridspec &sp, int64_t n, cons
         if (rc == SDE_OK) g_pc.cap = 4 * nb;
     }
     if (rc == SDE_OK && n > 0) {
-        cudaError_t e = cudaMemcpyAsync(g_pc.inputs, in, 4 * nb, cudaMemcpyDeviceToDevice, st);
+        cudaError_t e = shim_memcpy(g_pc.inputs, in, 4 * nb, cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) {
             sde_set_error("%s", cudaGetErrorString(e));
             rc = SDE_ECUDA;
@@ -849,7 +929,7 @@ static int shim_grid_speculative(sde_ctx *ctx, const sde_gridspec &sp, int64_t n
     SDE_TRY(ctx_scratch(ctx, "shim_flag", sizeof(int), (void **)&flag));
     SDE_TRY(ctx_scratch(ctx, "shim_grid", sizeof(float2) * (size_t)pitch * nv, (void **)&dg));
     SDE_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
-    SDE_CUDA_TRY(cudaMemcpyAsync(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
+    SDE_CUDA_TRY(shim_memcpy(dvis, vis, 2 * nb, cudaMemcpyHostToDevice, st));
     SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[0], st));
     SDE_CUDA_TRY(cudaStreamWaitEvent(cs, g_ss.ev[0], 0));
     // the grid of the cached plan and its way back on the main stream ...
@@ -858,19 +938,19 @@ static int shim_grid_speculative(sde_ctx *ctx, const sde_gridspec &sp, int64_t n
     float sw = 0.0f;
     int rc = sde_plan_grid(pl, psf ? SDE_GRID_PSF : SDE_GRID_VIS, (float *)dg, pitch, &sw);
     if (rc != SDE_OK && rc != SDE_ENOWEIGHT) return rc;
-    SDE_CUDA_TRY(cudaMemcpy2DAsync(gvis, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, (size_t)nv,
+    SDE_CUDA_TRY(shim_memcpy2d(gvis, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, (size_t)nv,
                                    cudaMemcpyDeviceToHost, st));
     // ... while U, V, W, WT go up and are compared on the copy stream
     const float *src[4] = {u, v, w, wt};
     for (int k = 0; k < 4; k++) {
-        SDE_CUDA_TRY(cudaMemcpyAsync(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
+        SDE_CUDA_TRY(shim_memcpy(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
         k_words_differ<<<ctx->num_sms * 4, 256, 0, cs>>>(reinterpret_cast<const uint32_t *>(in + k * n),
                                                         reinterpret_cast<const uint32_t *>(g_pc.inputs + k * n), n,
                                                         flag);
         SDE_CHECK_LAUNCH();
     }
     int hf = 1;
-    SDE_CUDA_TRY(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, cs));
+    SDE_CUDA_TRY(shim_memcpy(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, cs));
     SDE_CUDA_TRY(cudaStreamSynchronize(cs));
     SDE_CUDA_TRY(cudaStreamSynchronize(st));
     *done = 1;
@@ -883,7 +963,7 @@ static int shim_grid_speculative(sde_ctx *ctx, const sde_gridspec &sp, int64_t n
     SDE_TRY(shim_plan_build(ctx, sp, n, in, dvis, cf, h, &pl));
     rc = sde_plan_grid(pl, psf ? SDE_GRID_PSF : SDE_GRID_VIS, (float *)dg, pitch, &sw);
     if (rc != SDE_OK && rc != SDE_ENOWEIGHT) return rc;
-    SDE_CUDA_TRY(cudaMemcpy2DAsync(gvis, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, (size_t)nv,
+    SDE_CUDA_TRY(shim_memcpy2d(gvis, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, (size_t)nv,
                                    cudaMemcpyDeviceToHost, st));
     SDE_CUDA_TRY(cudaStreamSynchronize(st));
     *sumwt = sw;
@@ -925,7 +1005,7 @@ extern "C" void grdh2d_(float *vis, float *wt, float *u, float *v, float *w, int
     float sw = 0.0f;
     if (rc == SDE_OK) rc = sde_plan_grid(pl, *psf ? SDE_GRID_PSF : SDE_GRID_VIS, (float *)dg, pitch, &sw);
     if (rc == SDE_OK || rc == SDE_ENOWEIGHT) {
-        cudaError_t e = cudaMemcpy2DAsync(gvis, (size_t)*nu * 8, dg, (size_t)pitch * 8, (size_t)*nu * 8,
+        cudaError_t e = shim_memcpy2d(gvis, (size_t)*nu * 8, dg, (size_t)pitch * 8, (size_t)*nu * 8,
                                           *nv, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess && rc == SDE_OK) {
@@ -951,7 +1031,7 @@ static int h23_upload(sde_ctx *ctx, int64_t n, const float *vis, const float *wt
     const size_t len[7] = {2 * (size_t)n, (size_t)n, (size_t)n, (size_t)n, (size_t)n, (size_t)lu, (size_t)lv};
     const size_t off[7] = {0, 2 * nb, 3 * nb, 4 * nb, 5 * nb, 6 * nb, 6 * nb + (size_t)lu};
     for (int i = 0; i < 7; i++)
-        if (len[i]) SDE_CUDA_TRY(cudaMemcpyAsync(p + off[i], src[i], sizeof(float) * len[i], cudaMemcpyHostToDevice,
+        if (len[i]) SDE_CUDA_TRY(shim_memcpy(p + off[i], src[i], sizeof(float) * len[i], cudaMemcpyHostToDevice,
                                                  ctx->stream));
     return SDE_OK;
 }
@@ -985,7 +1065,7 @@ extern "C" void grdh23d_(float *vis, float *wt, float *u, float *v, float *w, in
                        *uorigin, *vorigin, *psf, *nu, *nv, d + 6 * nb, *suppu, *osampu, d + 6 * nb + lu, *suppv,
                        *osampv, *nz, *cellz, *refz, shift, dg, &sw);
     if (rc == SDE_OK || rc == SDE_ENOWEIGHT) {
-        cudaError_t e = cudaMemcpyAsync(gvis, dg, sizeof(float2) * cells, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = shim_memcpy(gvis, dg, sizeof(float2) * cells, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess && rc == SDE_OK) {
             sde_set_error("%s", cudaGetErrorString(e));
@@ -1023,7 +1103,7 @@ extern "C" void grddeh23_(float *vis, float *wt, float *u, float *v, float *w, i
     if (rc == SDE_OK) rc = h23_upload(ctx, n, vis, wt, u, v, w, intfnu, lu, intfnv, lv, &d);
     if (rc == SDE_OK) rc = ctx_scratch(ctx, "h23_mgrid", sizeof(float2) * cells, (void **)&dg);
     if (rc == SDE_OK) {
-        cudaError_t e = cudaMemcpyAsync(dg, gvis, sizeof(float2) * cells, cudaMemcpyHostToDevice, ctx->stream);
+        cudaError_t e = shim_memcpy(dg, gvis, sizeof(float2) * cells, cudaMemcpyHostToDevice, ctx->stream);
         if (e != cudaSuccess) {
             sde_set_error("%s", cudaGetErrorString(e));
             rc = SDE_ECUDA;
@@ -1035,8 +1115,8 @@ extern "C" void grddeh23_(float *vis, float *wt, float *u, float *v, float *w, i
                         *uorigin, *vorigin, dg, *nu, *nv, d + 6 * nb, *suppu, *osampu, d + 6 * nb + lu, *suppv,
                         *osampv, *nz, *cellz, *refz, shift, &nbad);
     if (rc == SDE_OK && n > 0) {
-        cudaError_t e = cudaMemcpyAsync(vis, d, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(wt, d + 2 * nb, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = shim_memcpy(vis, d, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = shim_memcpy(wt, d + 2 * nb, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) {
             sde_set_error("%s", cudaGetErrorString(e));
@@ -1075,11 +1155,11 @@ extern "C" void grdqh2d_(float *vis, float *wt, float *u, float *v, float *w, in
     cudaStream_t st = ctx->stream;
     cudaError_t e = cudaSuccess;
     if (rc == SDE_OK && n > 0) {
-        e = cudaMemcpyAsync(dvis, vis, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dwt, wt, sizeof(float) * n, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(du, u, sizeof(float) * n, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v, sizeof(float) * n, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dw, w, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        e = shim_memcpy(dvis, vis, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = shim_memcpy(dwt, wt, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = shim_memcpy(du, u, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = shim_memcpy(dv, v, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = shim_memcpy(dw, w, sizeof(float) * n, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) {
             sde_set_error("%s", cudaGetErrorString(e));
             rc = SDE_ECUDA;
@@ -1090,7 +1170,7 @@ extern "C" void grdqh2d_(float *vis, float *wt, float *u, float *v, float *w, in
         rc = grid_box(ctx, n, dvis, dwt, du, dv, dw, *uscale, *uoffset, *vscale, *voffset, *uorigin, *vorigin, *psf,
                       *nu, *nv, shift, dg, *nu, &sw, nullptr);
     if (rc == SDE_OK || rc == SDE_ENOWEIGHT) {
-        e = cudaMemcpyAsync(gvis, dg, sizeof(float2) * (size_t)*nu * *nv, cudaMemcpyDeviceToHost, st);
+        e = shim_memcpy(gvis, dg, sizeof(float2) * (size_t)*nu * *nv, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess && rc == SDE_OK) {
             sde_set_error("%s", cudaGetErrorString(e));
@@ -1139,33 +1219,33 @@ static int shim_degrid_speculative(sde_ctx *ctx, const sde_gridspec &sp, int64_t
     SDE_CUDA_TRY(cudaEventRecord(g_ss.ev[0], st));
     SDE_CUDA_TRY(cudaStreamWaitEvent(cs, g_ss.ev[0], 0));
     // WT first, compared on the copy stream
-    SDE_CUDA_TRY(cudaMemcpyAsync(in + 3 * n, wt, nb, cudaMemcpyHostToDevice, cs));
+    SDE_CUDA_TRY(shim_memcpy(in + 3 * n, wt, nb, cudaMemcpyHostToDevice, cs));
     k_words_differ<<<ctx->num_sms * 4, 256, 0, cs>>>(reinterpret_cast<const uint32_t *>(in + 3 * n),
                                                     reinterpret_cast<const uint32_t *>(g_pc.inputs + 3 * n), n,
                                                     flag);
     SDE_CHECK_LAUNCH();
     int fw = 1;
-    SDE_CUDA_TRY(cudaMemcpyAsync(&fw, flag, sizeof(int), cudaMemcpyDeviceToHost, cs));
+    SDE_CUDA_TRY(shim_memcpy(&fw, flag, sizeof(int), cudaMemcpyDeviceToHost, cs));
     SDE_CUDA_TRY(cudaStreamSynchronize(cs));
     if (fw) return SDE_OK;  // WT changed: the ordinary path
     // the model grid, the degrid with the cached plan and VIS down on the main stream ...
-    SDE_CUDA_TRY(cudaMemcpy2DAsync(dg, (size_t)pitch * 8, gvis, (size_t)nu * 8, (size_t)nu * 8, (size_t)nv,
+    SDE_CUDA_TRY(shim_memcpy2d(dg, (size_t)pitch * 8, gvis, (size_t)nu * 8, (size_t)nu * 8, (size_t)nv,
                                    cudaMemcpyHostToDevice, st));
     SDE_TRY(plan_degrid(g_pc.pl, (const float *)dg, pitch, 1, dv, dw, cnt));
-    SDE_CUDA_TRY(cudaMemcpyAsync(vis, dv, 2 * nb, cudaMemcpyDeviceToHost, st));
+    SDE_CUDA_TRY(shim_memcpy(vis, dv, 2 * nb, cudaMemcpyDeviceToHost, st));
     // ... while U, V, W go up and are compared on the copy stream
     const float *src[3] = {u, v, w};
     for (int k = 0; k < 3; k++) {
-        SDE_CUDA_TRY(cudaMemcpyAsync(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
+        SDE_CUDA_TRY(shim_memcpy(in + k * n, src[k], nb, cudaMemcpyHostToDevice, cs));
         k_words_differ<<<ctx->num_sms * 4, 256, 0, cs>>>(reinterpret_cast<const uint32_t *>(in + k * n),
                                                         reinterpret_cast<const uint32_t *>(g_pc.inputs + k * n), n,
                                                         flag + 1);
         SDE_CHECK_LAUNCH();
     }
     int fuvw = 1;
-    SDE_CUDA_TRY(cudaMemcpyAsync(&fuvw, flag + 1, sizeof(int), cudaMemcpyDeviceToHost, cs));
+    SDE_CUDA_TRY(shim_memcpy(&fuvw, flag + 1, sizeof(int), cudaMemcpyDeviceToHost, cs));
     unsigned long long hc[2] = {0, 0};
-    SDE_CUDA_TRY(cudaMemcpyAsync(hc, cnt, 16, cudaMemcpyDeviceToHost, st));
+    SDE_CUDA_TRY(shim_memcpy(hc, cnt, 16, cudaMemcpyDeviceToHost, st));
     SDE_CUDA_TRY(cudaStreamSynchronize(cs));
     SDE_CUDA_TRY(cudaStreamSynchronize(st));
     *done = 1;
@@ -1173,7 +1253,7 @@ static int shim_degrid_speculative(sde_ctx *ctx, const sde_gridspec &sp, int64_t
         g_pc.hits++;
         *nbad = (int64_t)hc[0];
         if (hc[1] > 0) {  // points not degridded: WT negated
-            SDE_CUDA_TRY(cudaMemcpyAsync(wt, dw, nb, cudaMemcpyDeviceToHost, st));
+            SDE_CUDA_TRY(shim_memcpy(wt, dw, nb, cudaMemcpyDeviceToHost, st));
             SDE_CUDA_TRY(cudaStreamSynchronize(st));
         }
         return SDE_OK;
@@ -1250,17 +1330,17 @@ static void weights_shim(float *wt, float *u, float *v, float *w, int *nvis, flo
     const bool alias = newwt == wt;
     cudaStream_t st = ctx->stream;
     size_t nb = 4 * (size_t)*nvis;
-    cudaMemcpyAsync(du, u, nb, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dv, v, nb, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dw, w, nb, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dwt, wt, nb, cudaMemcpyHostToDevice, st);
-    if (!alias) cudaMemcpyAsync(dnew, newwt, nb, cudaMemcpyHostToDevice, st);
+    shim_memcpy(du, u, nb, cudaMemcpyHostToDevice, st);
+    shim_memcpy(dv, v, nb, cudaMemcpyHostToDevice, st);
+    shim_memcpy(dw, w, nb, cudaMemcpyHostToDevice, st);
+    shim_memcpy(dwt, wt, nb, cudaMemcpyHostToDevice, st);
+    if (!alias) shim_memcpy(dnew, newwt, nb, cudaMemcpyHostToDevice, st);
     sde_wstats stats;
     rc = sde_weights(ctx, rmode, robust, ds, dwt, du, dv, dw, *nvis, *uscale, *uoffset, *vscale,
                      *voffset, *uorigin, *vorigin, *nu, *nv, shift, alias ? dwt : dnew, dg, &stats);
     if (rc == SDE_OK) {
-        cudaMemcpyAsync(newwt, alias ? dwt : dnew, nb, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(gwt, dg, 4 * ncell, cudaMemcpyDeviceToHost, st);
+        shim_memcpy(newwt, alias ? dwt : dnew, nb, cudaMemcpyDeviceToHost, st);
+        shim_memcpy(gwt, dg, 4 * ncell, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) rc = SDE_ECUDA;
     }
     if (rc == SDE_EBADMODE) {
@@ -1336,20 +1416,20 @@ extern "C" void fftr2d_(float *rarray, float *xarray, float *work, float *work2,
     }
     cudaStream_t st = ctx->stream;
     if (*dir < 0) {
-        cudaMemcpy2DAsync(dg, (size_t)pitch * 8, xarray, (size_t)nu * 8, (size_t)nu * 8, *nv,
+        shim_memcpy2d(dg, (size_t)pitch * 8, xarray, (size_t)nu * 8, (size_t)nu * 8, *nv,
                           cudaMemcpyHostToDevice, st);
         rc = sde_image_from_grid(ctx, (float *)dg, pitch, *nx, *ny, *fnu, *nv, 0, nullptr, di);
         if (rc == SDE_OK) {
-            cudaMemcpyAsync(rarray, di, sizeof(float) * (size_t)*nx * *ny, cudaMemcpyDeviceToHost, st);
+            shim_memcpy(rarray, di, sizeof(float) * (size_t)*nx * *ny, cudaMemcpyDeviceToHost, st);
             // FFTR2D leaves the column-transformed grid in XARRAY (fft/fftr2d.f:82-90)
-            cudaMemcpy2DAsync(xarray, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, *nv,
+            shim_memcpy2d(xarray, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, *nv,
                               cudaMemcpyDeviceToHost, st);
         }
     } else {
-        cudaMemcpyAsync(di, rarray, sizeof(float) * (size_t)*nx * *ny, cudaMemcpyHostToDevice, st);
+        shim_memcpy(di, rarray, sizeof(float) * (size_t)*nx * *ny, cudaMemcpyHostToDevice, st);
         rc = sde_grid_from_image(ctx, di, *nx, *ny, *fnu, *nv, 0, (float *)dg, pitch);
         if (rc == SDE_OK)
-            cudaMemcpy2DAsync(xarray, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, *nv,
+            shim_memcpy2d(xarray, (size_t)nu * 8, dg, (size_t)pitch * 8, (size_t)nu * 8, *nv,
                               cudaMemcpyDeviceToHost, st);
     }
     if (rc == SDE_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = SDE_ECUDA;
@@ -1397,11 +1477,11 @@ extern "C" void pixcor2d_(float *in, int *nx, int *ny, float *cf, int *cflen, ch
         return;
     }
     cudaStream_t st = ctx->stream;
-    cudaMemcpyAsync(di, in, 4 * npix, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dc, cf, 4 * (size_t)*cflen, cudaMemcpyHostToDevice, st);
+    shim_memcpy(di, in, 4 * npix, cudaMemcpyHostToDevice, st);
+    shim_memcpy(dc, cf, 4 * (size_t)*cflen, cudaMemcpyHostToDevice, st);
     KTimer kt(ctx, "pixcor2d");
     k_pixcor2d<<<ceil_div((int64_t)npix, 256), 256, 0, st>>>(di, *nx, *ny, dc, correct, di, sx, sy, *cenx, *ceny);
-    cudaMemcpyAsync(out, di, 4 * npix, cudaMemcpyDeviceToHost, st);
+    shim_memcpy(out, di, 4 * npix, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) {
         sde_set_error("%s", cudaGetErrorString(cudaGetLastError()));
         report_rc(SDE_ECUDA, R);
@@ -1432,14 +1512,14 @@ extern "C" void pix2drcl_(float *drt, float *psf, float *box, int *nx, int *ny, 
         return;
     }
     cudaStream_t st = ctx->stream;
-    cudaMemcpyAsync(dd, drt, 4 * npix, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dp, psf, 4 * pnpix, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(db, box, 4 * npix, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dcl, cln, 4 * npix, cudaMemcpyHostToDevice, st);
+    shim_memcpy(dd, drt, 4 * npix, cudaMemcpyHostToDevice, st);
+    shim_memcpy(dp, psf, 4 * pnpix, cudaMemcpyHostToDevice, st);
+    shim_memcpy(db, box, 4 * npix, cudaMemcpyHostToDevice, st);
+    shim_memcpy(dcl, cln, 4 * npix, cudaMemcpyHostToDevice, st);
     if (nabs > 0) {
-        cudaMemcpyAsync(dcf, cflux, 4 * (size_t)nabs, cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(dcx, cx, 4 * (size_t)nabs, cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(dcy, cy, 4 * (size_t)nabs, cudaMemcpyHostToDevice, st);
+        shim_memcpy(dcf, cflux, 4 * (size_t)nabs, cudaMemcpyHostToDevice, st);
+        shim_memcpy(dcx, cx, 4 * (size_t)nabs, cudaMemcpyHostToDevice, st);
+        shim_memcpy(dcy, cy, 4 * (size_t)nabs, cudaMemcpyHostToDevice, st);
     }
     sde_clean_result out;
     int rc = sde_hogbom(ctx, dd, dp, db, *nx, *ny, *pnx, *pny, *gain, *nsub, *bsub, *flux, *tflux, dcl,
@@ -1448,12 +1528,12 @@ extern "C" void pix2drcl_(float *drt, float *psf, float *box, int *nx, int *ny, 
         report_rc(rc, R);
         return;
     }
-    cudaMemcpyAsync(cln, dcl, 4 * npix, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(res, dr, 4 * npix, cudaMemcpyDeviceToHost, st);
+    shim_memcpy(cln, dcl, 4 * npix, cudaMemcpyDeviceToHost, st);
+    shim_memcpy(res, dr, 4 * npix, cudaMemcpyDeviceToHost, st);
     if (nabs > 0) {
-        cudaMemcpyAsync(cflux, dcf, 4 * (size_t)nabs, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(cx, dcx, 4 * (size_t)nabs, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(cy, dcy, 4 * (size_t)nabs, cudaMemcpyDeviceToHost, st);
+        shim_memcpy(cflux, dcf, 4 * (size_t)nabs, cudaMemcpyDeviceToHost, st);
+        shim_memcpy(cx, dcx, 4 * (size_t)nabs, cudaMemcpyDeviceToHost, st);
+        shim_memcpy(cy, dcy, 4 * (size_t)nabs, cudaMemcpyDeviceToHost, st);
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) {
         report_rc(SDE_ECUDA, R);
@@ -1478,7 +1558,7 @@ extern "C" int pixisama_(int *n, float *a, int *i) {
         report_rc(SDE_ENOMEM, "PIXISAMA");
         return *i;
     }
-    cudaMemcpyAsync(d, a, 4 * (size_t)*n, cudaMemcpyHostToDevice, ctx->stream);
+    shim_memcpy(d, a, 4 * (size_t)*n, cudaMemcpyHostToDevice, ctx->stream);
     int64_t idx = 0;
     if (sde_isamax0(ctx, d, *n, &idx) != SDE_OK) {
         report_rc(SDE_ECUDA, "PIXISAMA");
