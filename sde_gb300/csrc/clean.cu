@@ -79,6 +79,14 @@ __device__ __forceinline__ unsigned long long cand_key(Cand c) {
     return ((unsigned long long)__float_as_uint(c.a) << 32) |
            ((unsigned long long)(uint32_t)(INT32_MAX - c.idx) << 1) | (__float_as_uint(c.v) >> 31);
 }
+// the largest key of a warp's lanes: the largest high word, then the largest low word among
+// the lanes that hold it
+__device__ __forceinline__ unsigned long long warp_key_max(unsigned long long k) {
+    const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+    return ((unsigned long long)mhi << 32) | mlo;
+}
 __device__ __forceinline__ Cand key_cand(unsigned long long k) {
     Cand c;
     c.a = __uint_as_float((uint32_t)(k >> 32));
@@ -91,12 +99,15 @@ __device__ __forceinline__ Cand key_cand(unsigned long long k) {
 // when the count reaches (epoch + 1) * nblocks, so the last CTA's arrival releases the others
 // (no reset, no second word) and that CTA does not wait.  Gives up after SPIN_LIMIT polls and
 // reports through *timeout.  The count is cleared before each launch.
-__device__ bool grid_sync(Barrier *b, unsigned nblocks, unsigned epoch, int *timeout) {
+__device__ bool grid_sync(Barrier *b, unsigned nblocks, unsigned epoch, int *timeout,
+                          unsigned long long *pub = nullptr, const unsigned long long *key = nullptr) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         ok = 1;
         const unsigned target = (epoch + 1u) * nblocks;
+        // the CTA's maximum (a key, 0 for none) joins the global one before the CTA arrives
+        if (pub && *key) atomicMax(pub, *key);
         __threadfence();
         const unsigned arrived = atomicAdd(&b->count, 1u) + 1u;
         if ((int)(arrived - target) < 0) {
@@ -147,6 +158,11 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
     const int64_t pnpix = (int64_t)A.pnx * A.pny;
     auto R = [&](int64_t k) -> float & { return SMEM ? sres[k - lo] : A.res[k]; };
     __shared__ int stop_sh;
+    // the CTA's maximum of a pass as a key (cand_key; 0 for none): warps add theirs with
+    // atomicMax, thread 0 adds it to the global word inside the next grid barrier
+    __shared__ unsigned long long s_key;
+    if (threadIdx.x == 0) s_key = 0ull;
+    __syncthreads();
     // RES = DRT * BOX, and the first maximum of the slice
     Cand c{-1.0f, INT32_MAX, 0.0f};
     for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
@@ -154,11 +170,13 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
         R(k) = r;
         c = better(c, Cand{fabsf(r), (int32_t)k, r});
     }
-    c = block_best(c);
-    if (threadIdx.x == 0 && c.a >= 0.0f) atomicMax(&A.bar->best[0], cand_key(c));
+    {
+        const unsigned long long wk = warp_key_max(c.a >= 0.0f ? cand_key(c) : 0ull);
+        if ((threadIdx.x & 31) == 0 && wk) atomicMax(&s_key, wk);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->stopreq[0] = (A.cancel && *A.cancel) ? 1 : 0;
     unsigned epoch = 0;
-    if (!grid_sync(A.bar, gridDim.x, epoch++, &A.status[STATUS_TIMEOUT])) return;
+    if (!grid_sync(A.bar, gridDim.x, epoch++, &A.status[STATUS_TIMEOUT], &A.bar->best[0], &s_key)) return;
     // the maxima of successive passes take best[0], best[1], best[2] in turn: a word is read
     // after the barrier that follows its pass, and cleared by CTA 0 one pass before it is
     // used again (after every CTA has read it, before any CTA adds to it)
@@ -173,6 +191,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
         // global first maximum of the last pass
         const Cand g = key_cand(__ldcg(&A.bar->best[ph % 3]));
         if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->best[(ph + 2) % 3] = 0ull;
+        if (threadIdx.x == 0) s_key = 0ull;  // (ordered before the warps' additions by the barrier below)
         // PIXISAMA returns 1 (index 0) when no |value| exceeds 0
         // every |value| >= 0 beats the -1 sentinel, so when nothing exceeds 0 the winner
         // is index 0 -- PIXISAMA's default of 1 (pix/pixisama.f:45)
@@ -256,11 +275,14 @@ __global__ void __launch_bounds__(CL_THREADS) k_hogbom(CleanArgs A) {
             }
             lc = Cand{la, li, lv};
         }
-        lc = block_best(lc);
+        {
+            const unsigned long long wk = warp_key_max(lc.a >= 0.0f ? cand_key(lc) : 0ull);
+            if ((threadIdx.x & 31) == 0 && wk) atomicMax(&s_key, wk);
+        }
         cur ^= 1;
-        if (threadIdx.x == 0 && lc.a >= 0.0f) atomicMax(&A.bar->best[(ph + 1) % 3], cand_key(lc));
         if (blockIdx.x == 0 && threadIdx.x == 0) A.bar->stopreq[cur] = (A.cancel && *A.cancel) ? 1 : 0;
-        if (!grid_sync(A.bar, gridDim.x, epoch++, &A.status[STATUS_TIMEOUT])) return;
+        if (!grid_sync(A.bar, gridDim.x, epoch++, &A.status[STATUS_TIMEOUT], &A.bar->best[(ph + 1) % 3], &s_key))
+            return;
         ph++;
     }
     if (SMEM)
