@@ -404,7 +404,7 @@ int sde_clark(sde_ctx *ctx, const float *dirty, const float *psf, int n, const f
  * takes the same device arrays and returns the same results as sde_hogbom, on the caller's
  * stream (a cudaStream_t, 0 for the legacy stream, on the current device).  Its scratch --
  * partial maxima of at most 1024 CTAs per search, the grid barrier, status words and result
- * scalars, about 36 KB -- lives in one static device array that comes with the library's
+ * scalars, about 12 KB -- lives in one static device array that comes with the library's
  * device code: a GPU gets it when the library's module is loaded there (with CUDA's lazy
  * module loading, at the first call on that GPU) and keeps it until the process exits, so
  * make the first call at start-up, before an arena has taken all device memory.  The first

@@ -6,9 +6,10 @@
 // then RES -= (PNTSUB*PSF(OFFX-IX,OFFY-IY))*BOX over the whole window in FP32.  Here one
 // cooperative persistent launch runs every iteration: each CTA owns a contiguous slice of
 // the window, applies the previous component's subtraction to it with the same FP32
-// operations (no FMA), finds its slice's first maximum, and a grid barrier (bounded spin)
-// publishes the partial maxima; every CTA then reduces the same partials to the same
-// global (max, first index), so component positions are identical to the reference's.
+// operations (no FMA), finds its slice's first maximum, and that maximum joins a global one
+// (a packed key, one atomicMax per CTA) inside a grid barrier (bounded spin); every CTA then
+// reads the same global (max, first index), so component positions are identical to the
+// reference's.
 #include <cooperative_groups.h>
 #include <math.h>
 #include <string.h>
@@ -139,7 +140,6 @@ struct CleanArgs {
     float gain, flux, tflux_in;
     int nsub, bsub;
     volatile int *cancel;
-    Cand *partial;   // [2][gridDim]
     Barrier *bar;
     int *status;     // [STATUS_TIMEOUT]
     float *out;      // [0] maxres [1] tflux [2] ansub (as int bits)
@@ -458,10 +458,8 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
         SDE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_hogbom<true>, CL_THREADS, slice));
         smem_res = (int64_t)fit * ctx->num_sms >= nblocks;
     }
-    Cand *partial;
     Barrier *bar;
     float *dout;
-    SDE_TRY(ctx_scratch(ctx, "cl_partial", sizeof(Cand) * 2 * (size_t)nblocks, (void **)&partial));
     SDE_TRY(ctx_scratch(ctx, "cl_bar", sizeof(Barrier), (void **)&bar));
     SDE_TRY(ctx_scratch(ctx, "cl_out", 4 * sizeof(float), (void **)&dout));
     SDE_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(Barrier), ctx->stream));
@@ -470,7 +468,7 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
     A.drt = drt; A.psf = psf; A.box = box; A.cln = cln; A.res = res; A.cflux = cflux;
     A.cx = cx; A.cy = cy; A.nx = nx; A.ny = ny; A.pnx = pnx; A.pny = pny;
     A.pmpx = pmpx; A.pmpy = pmpy; A.gain = gain; A.flux = flux; A.tflux_in = tflux_in;
-    A.nsub = nsub; A.bsub = bsub; A.cancel = cancel_flag; A.partial = partial; A.bar = bar;
+    A.nsub = nsub; A.bsub = bsub; A.cancel = cancel_flag; A.bar = bar;
     A.status = ctx->d_status; A.out = dout;
     void *args[] = {&A};
     KTimer kt(ctx, "hogbom");
@@ -506,15 +504,14 @@ int sde_hogbom(sde_ctx *ctx, const float *drt, const float *psf, const float *bo
 // allocator or a fixed arena, embedded/real-time hosts that forbid allocation after start-up,
 // and serving loops that must not block on the allocator.  For them this entry point runs the
 // same minor cycle as sde_hogbom on arrays the caller already holds, keeping its scratch --
-// the per-CTA partial maxima of the PSF-peak search and of every CLEAN iteration, the grid
-// barrier, the status words and the result scalars -- in one file-scope device array of fixed
+// the per-CTA partial maxima of the PSF-peak search, the grid barrier with the iterations'
+// maxima, the status words and the result scalars -- in one file-scope device array of fixed
 // size.  That array exists on every GPU that loads the library, for the life of the process.
 namespace {
-constexpr int NOALLOC_MAX_CTAS = 1024;  // partial maxima kept per search (~36 KB in all)
+constexpr int NOALLOC_MAX_CTAS = 1024;  // CTAs of the PSF-peak search and of CLEAN (~12 KB in all)
 struct NoAllocScratch {
     Cand isa_part[NOALLOC_MAX_CTAS];
     int64_t isa_out;
-    Cand partial[2 * NOALLOC_MAX_CTAS];
     Barrier bar;
     int status[STATUS_COUNT];
     float out[4];
@@ -645,7 +642,7 @@ extern "C" int sde_hogbom_noalloc(void *stream, const float *drt, const float *p
     A.drt = drt; A.psf = psf; A.box = box; A.cln = cln; A.res = res; A.cflux = cflux;
     A.cx = cx; A.cy = cy; A.nx = nx; A.ny = ny; A.pnx = pnx; A.pny = pny;
     A.pmpx = pmpx; A.pmpy = pmpy; A.gain = gain; A.flux = flux; A.tflux_in = tflux_in;
-    A.nsub = nsub; A.bsub = bsub; A.cancel = cancel_flag; A.partial = S->partial; A.bar = &S->bar;
+    A.nsub = nsub; A.bsub = bsub; A.cancel = cancel_flag; A.bar = &S->bar;
     A.status = S->status; A.out = S->out;
     void *args[] = {&A};
     SDE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_hogbom<false>, dim3(nblocks), dim3(CL_THREADS),
