@@ -242,7 +242,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter_ranked(const uint32_t
 }
 
 // Scatter of one pass, round by round through the block (items of one digit in a round go
-// to consecutive addresses): the better choice once the keys are nearly in order.
+// to consecutive addresses): the 64-bit keys' pass (the chunk sort, a few million items),
+// whose keys and values would not fit k_rs_scatter_ranked's shared memory.
 template <typename K>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const K *kin, const uint32_t *vin,
                                                             K *kout, uint32_t *vout, int64_t n,
