@@ -271,6 +271,16 @@ struct CorrParams {
     const float *corry;  // CCF(ICFY) for each image row (pix/pixcor2d.f:60)
 };
 
+// PIXCOR2D's correction VAL / (CCF(ICFX)*CCF(ICFY)) (pix/pixcor2d.f:58-64) of an image
+// pixel going into a forward transform.  For a zero pixel and a positive divisor the
+// quotient is the pixel itself (sign included), so the division is skipped there: the model
+// images a CLEAN major cycle transforms are mostly zero.
+__device__ __forceinline__ float pixcor_in(float val, float cx, float cy) {
+    const float d = __fmul_rn(cx, cy);
+    return (val == 0.0f && d > 0.0f) ? val : __fdiv_rn(val, d);
+}
+
+
 // Row pass grid -> image (c2r), one CTA per image row, with grid correction and an
 // optional final scale OUT = s*IN (ARRSCALE by 1/max, pix/pixrscal.f).
 __global__ void __launch_bounds__(FFT_THREADS) k_row_c2r(const float2 *__restrict__ grid,
@@ -356,7 +366,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_row_r2c(const float *__restrict
             float val = 0.f;
             if (ix >= 0 && ix < nx) {
                 val = row[ix];
-                if (cp.ccf) val = __fdiv_rn(val, __fmul_rn(cp.corrx[ix], cfy));
+                if (cp.ccf) val = pixcor_in(val, cp.corrx[ix], cfy);
             }
             xv[e] = val;
         }
@@ -724,7 +734,7 @@ __global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB)
                 float val = 0.f;
                 if (ix >= 0 && ix < nx) {
                     val = stg[rr * FNU + ix];
-                    if (cp.ccf) val = __fdiv_rn(val, __fmul_rn(cp.corrx[ix], cfy));
+                    if (cp.ccf) val = pixcor_in(val, cp.corrx[ix], cfy);
                 }
                 xv[e] = val;
             }
@@ -764,7 +774,7 @@ __global__ void __launch_bounds__(RowShape<LOGH>::T, RowShape<LOGH>::MINB)
             float val = 0.f;
             if (ix >= 0 && ix < nx) {
                 val = row[ix];
-                if (cp.ccf) val = __fdiv_rn(val, __fmul_rn(cp.corrx[ix], cfy));
+                if (cp.ccf) val = pixcor_in(val, cp.corrx[ix], cfy);
             }
             xv[e] = val;
         }
