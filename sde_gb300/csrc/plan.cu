@@ -29,21 +29,23 @@ static_assert(TAPROW_BYTES % 2 == 0, "bit 0 of a degridding word is free");
 
 // A visibility's plan data in caller order, one 32-byte sector: the plan record {WT, the
 // gridder's tap-table offsets, observed value in the gridding frame}, the degridding word
-// (with the gridding-frame conjugation in bit 0) and the rotation.  The gather into sorted
+// (with the gridding-frame conjugation in bit 0), the rotation and, for an exception, its
+// place in the exception list.  The gather into sorted
 // order reads one sector per visibility.
 struct __align__(32) PlanRecU {
     float4 rec;
     uint32_t gdd;
     float rc, rs;
-    uint32_t pad;
+    uint32_t exc_slot;  // the visibility's place in the exception list (exceptions only)
 };
 
-// Per visibility (caller order): gridding key, the PlanRecU sector and the exception flag,
+// Per visibility (caller order): gridding key, the PlanRecU sector and, for an exception, its
+// entry in the exception list,
 // from both routines' geometry (geom_vis).
 __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float *__restrict__ v,
                             const float *__restrict__ w, const float2 *__restrict__ vis,
                             const float *__restrict__ wt, int64_t n, uint32_t *keys,
-                            uint32_t *vals, PlanRecU *rec_u, uint32_t *exc_flag,
+                            uint32_t *vals, PlanRecU *rec_u, uint32_t *exc_list,
                             unsigned long long *counts) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t nvalid = 0, nexc = 0;
@@ -92,11 +94,15 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
         pr.gdd = pdd | (gc ? GDD_GCONJ_U : 0u);
         pr.rc = r.x;
         pr.rs = r.y;
-        pr.pad = 0;
-        rec_u[i] = pr;
+        pr.exc_slot = 0;
         // GRDDEH2D's exception path takes the visibilities with WT > 0 that do not grid or
-        // whose degridding cell is not the gridding cell
-        exc_flag[i] = wi > 0.0f && (key == KEY_INVALID || (pdd & GDD_EXCEPTION) != 0);
+        // whose degridding cell is not the gridding cell: appended to the list (a few in 10^4;
+        // the list's order does not matter, each is degridded on its own)
+        if (wi > 0.0f && (key == KEY_INVALID || (pdd & GDD_EXCEPTION) != 0)) {
+            pr.exc_slot = (uint32_t)atomicAdd(&counts[3], 1ull);
+            exc_list[pr.exc_slot] = (uint32_t)i;
+        }
+        rec_u[i] = pr;
     }
     // block-aggregated counters (one atomic per block and counter: per-warp atomics on three
     // addresses serialise in L2 at this visibility count)
@@ -117,7 +123,7 @@ __global__ void k_plan_geom(GParams p, const float *__restrict__ u, const float 
 __global__ void __launch_bounds__(256) k_plan_gather(const uint32_t *__restrict__ perm,
                                                      const uint32_t *__restrict__ cpos, int64_t nchunks,
                                                      uint2 *chunks, const PlanRecU *__restrict__ rec_u,
-                                                     const uint32_t *__restrict__ exc_slot, float2 *fobs,
+                                                     float2 *fobs,
                                                      float4 *rec, float *wt, uint32_t *gdd, uint32_t *orig,
                                                      float2 *rot, uint8_t *gconj, DegridExc *exc) {
     const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -138,23 +144,24 @@ __global__ void __launch_bounds__(256) k_plan_gather(const uint32_t *__restrict_
         orig[p] = i;
         gconj[p] = (d & GDD_GCONJ_U) ? 1 : 0;
         if (rot) rot[p] = make_float2(pr.rc, pr.rs);
-        if ((d & GDD_EXCEPTION) && exc) exc[exc_slot[i]].pos = (int32_t)p;
+        if ((d & GDD_EXCEPTION) && exc) exc[pr.exc_slot].pos = (int32_t)p;
     }
     __syncwarp();  // every lane has read the chunk record
     if (lane == 0) chunks[c] = make_uint2(to, ch.y);
 }
 
-// (pos is set by k_plan_gather for the exceptions that also grid)
+// The exception list's entries, one thread per exception (pos is set by k_plan_gather for the
+// exceptions that also grid).
 __global__ void k_exc_write(GParams p, const float *__restrict__ u, const float *__restrict__ v,
                             const float *__restrict__ w, const float *__restrict__ wt,
-                            const PlanRecU *__restrict__ rec_u,
-                            const uint32_t *__restrict__ flag, const uint32_t *__restrict__ slot,
-                            int64_t n, DegridExc *exc, float *exc_wt, float2 *exc_rot) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !flag[i]) return;
+                            const PlanRecU *__restrict__ rec_u, const uint32_t *__restrict__ exc_list,
+                            int64_t nexc, DegridExc *exc, float *exc_wt, float2 *exc_rot) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nexc) return;
+    const uint32_t i = exc_list[s];
     DGeo g = p.fast ? degrid_geom_fast(p, u[i], v[i]) : degrid_geom(p, u[i], v[i], w[i]);
     DegridExc e;
-    e.orig = (uint32_t)i;
+    e.orig = i;
     e.pos = -1;
     e.nuc = g.nud;
     e.nvc = g.nvd;
@@ -164,7 +171,6 @@ __global__ void k_exc_write(GParams p, const float *__restrict__ u, const float 
     e.valid = g.valid;
     e.gconj = (rec_u[i].gdd & GDD_GCONJ_U) ? 1 : 0;
     e.pad = 0;
-    uint32_t s = slot[i];
     exc[s] = e;
     exc_wt[s] = wt[i];
     exc_rot[s] = make_float2(g.rc, g.rs);
@@ -474,21 +480,21 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         gp.ntu = pl->ntu;
         gp.twopi = (double)(8.0f * atanf(1.0f));  // TWOPI = 8 * ATAN(1.0), REAL (grdh2d.f:91)
 
-        uint32_t *keys, *vals, *ktmp, *vtmp, *flag;
+        uint32_t *keys, *vals, *ktmp, *vtmp, *exc_list;
         PlanRecU *rec_u;
         unsigned long long *counts;
         PL_TRY(ctx_scratch(ctx, "pl_keys", 4 * n, (void **)&keys));
         PL_TRY(ctx_scratch(ctx, "pl_vals", 4 * n, (void **)&vals));
         PL_TRY(ctx_scratch(ctx, "pl_ktmp", 4 * n, (void **)&ktmp));
         PL_TRY(ctx_scratch(ctx, "pl_vtmp", 4 * n, (void **)&vtmp));
-        PL_TRY(ctx_scratch(ctx, "pl_flag", 4 * n, (void **)&flag));
+        PL_TRY(ctx_scratch(ctx, "pl_exclist", 4 * n, (void **)&exc_list));
         PL_TRY(ctx_scratch(ctx, "pl_rec", sizeof(PlanRecU) * n, (void **)&rec_u));
         PL_TRY(ctx_scratch(ctx, "pl_counts", 64, (void **)&counts));
         PL_CUDA(cudaMemsetAsync(counts, 0, 64, st));
         const int T = 256;
         if (nvis > 0) {
             k_plan_geom<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dvis, dwt, nvis, keys, vals,
-                                                       rec_u, flag, counts);
+                                                       rec_u, exc_list, counts);
             PL_CUDA(cudaGetLastError());
         }
         int64_t ntiles = (int64_t)pl->ntu * pl->ntv;
@@ -536,14 +542,11 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
         // the gather below fills in the sorted positions
         size_t ne1 = (size_t)(nexc > 0 ? nexc : 1);
         PL_TRY(plan_alloc(pl, (void **)&pl->exc, exc_bytes(ne1)));
-        uint32_t *slot = nullptr;
         if (nexc > 0) {
-            PL_TRY(ctx_scratch(ctx, "pl_slot", 4 * n, (void **)&slot));
-            PL_TRY(launch_exclusive_scan_u32(ctx, flag, slot, nvis, nullptr));
             float *exc_wt = (float *)((char *)pl->exc + exc_wt_off(ne1));
             float2 *exc_rot = (float2 *)((char *)pl->exc + exc_rot_off(ne1));
-            k_exc_write<<<ceil_div(nvis, T), T, 0, st>>>(gp, du, dv, dw, dwt, rec_u, flag, slot, nvis,
-                                                       pl->exc, exc_wt, exc_rot);
+            k_exc_write<<<ceil_div(nexc, T), T, 0, st>>>(gp, du, dv, dw, dwt, rec_u, exc_list, nexc, pl->exc,
+                                                       exc_wt, exc_rot);
             PL_CUDA(cudaGetLastError());
         }
         // runs, chunks, work items
@@ -602,7 +605,7 @@ int sde_plan_create_opts(sde_ctx *ctx, const sde_gridspec *spec, int64_t nvis, c
             PL_CUDA(cudaGetLastError());
             // chunk order: each chunk's new start, then one gather of the caller-order sectors
             PL_TRY(launch_exclusive_scan_u32(ctx, clen, cpos, nchunks, nullptr));
-            k_plan_gather<<<ceil_div(nchunks, T / 32), T, 0, st>>>(vals, cpos, nchunks, pl->chunks, rec_u, slot,
+            k_plan_gather<<<ceil_div(nchunks, T / 32), T, 0, st>>>(vals, cpos, nchunks, pl->chunks, rec_u,
                                                                  pl->fobs, pl->rec, pl->wt, pl->gdd,
                                                                  pl->orig, pl->rot, pl->gconj,
                                                                  nexc > 0 ? pl->exc : nullptr);
